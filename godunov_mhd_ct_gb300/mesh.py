@@ -1,0 +1,193 @@
+"""Block mesh: leaf blocks of a p4est-style brick forest at one refinement level, with the
+neighbour table the kernels use in place of kalypsso-core's hashmap + StencilHelper lookups.
+
+Block order follows p4est: bricks (trees) in x-fastest order, then leaves along the Morton
+(Z-order) curve inside each brick (SolverGodunovMHD.cpp:323-371 partitions along that curve).
+
+Neighbour table: ``neighbor[b, (oz+1)*9 + (oy+1)*3 + (ox+1)]`` is the block sharing the face,
+edge or corner of block ``b`` in direction (ox, oy, oz) in {-1,0,1}^3, or -1 across a domain
+boundary that has no outside block.
+
+Outside blocks (non-periodic directions) are appended after the owned blocks, as the reference
+stores its "outside" quadrants after owned + ghost ones; ``border_conditions/FillOutside.cpp``
+fills them before each step. ``outside_src[b - n_owned]`` is the inside block an outside block
+copies from and ``outside_dir`` the direction (0..2) and side (-1/+1) it lies across.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+def _morton_key(ix: np.ndarray, iy: np.ndarray, iz: np.ndarray, bits: int) -> np.ndarray:
+    key = np.zeros(ix.shape, dtype=np.int64)
+    for b in range(bits):
+        key |= ((ix >> b) & 1).astype(np.int64) << (3 * b)
+        key |= ((iy >> b) & 1).astype(np.int64) << (3 * b + 1)
+        key |= ((iz >> b) & 1).astype(np.int64) << (3 * b + 2)
+    return key
+
+
+def nb_slot(ox: int, oy: int, oz: int) -> int:
+    return (oz + 1) * 9 + (oy + 1) * 3 + (ox + 1)
+
+
+@dataclass
+class BlockMesh:
+    dim: int
+    block: tuple            # (bx, by, bz); bz == 1 in 2D
+    level: np.ndarray       # [n_blocks] int32
+    neighbor: np.ndarray    # [n_blocks, 27] int32
+    coords: np.ndarray      # [n_blocks, 3] int64 block coordinates (outside blocks: outside the grid)
+    n_owned: int
+    grid: tuple             # blocks per direction over the whole domain
+    periodic: tuple
+    scaling_factor: float = 1.0
+    outside_src: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    outside_dir: np.ndarray = field(default_factory=lambda: np.zeros((0, 2), np.int32))
+
+    @property
+    def n_blocks(self) -> int:
+        return int(self.level.shape[0])
+
+    @property
+    def ncell(self) -> int:
+        bx, by, bz = self.block
+        return bx * by * bz
+
+    @property
+    def face_counts(self):
+        bx, by, bz = self.block
+        nfx = (bx + 1) * by * bz
+        nfy = bx * (by + 1) * bz
+        nfz = bx * by * (bz + 1) if self.dim == 3 else bx * by
+        return nfx, nfy, nfz
+
+    @property
+    def nface(self) -> int:
+        return sum(self.face_counts)
+
+    def cell_length(self, level: int | None = None) -> float:
+        """dx = (1 / (bx * 2^level)) * scaling_factor (core compute_cell_length, unit brick)."""
+        lv = int(self.level[0]) if level is None else level
+        return (1.0 / float(self.block[0] << lv)) * self.scaling_factor
+
+    @staticmethod
+    def uniform(dim: int, bricks=(1, 1, 1), level: int = 0, block=(16, 16, 16), periodic=(True, True, True),
+                scaling_factor: float = 1.0) -> "BlockMesh":
+        """All leaves of a brick forest refined uniformly to ``level``."""
+        if dim not in (2, 3):
+            raise ValueError("dim must be 2 or 3")
+        bx, by, bz = block
+        if dim == 2:
+            bz = 1
+            bricks = (bricks[0], bricks[1], 1)
+        if min(bx, by) < 4 or (dim == 3 and bz < 4):
+            raise ValueError("block sizes must be >= 2*ghost_width = 4 (SolverGodunovMHD.cpp:118-140)")
+        n_side = 1 << level
+        gx, gy = bricks[0] * n_side, bricks[1] * n_side
+        gz = bricks[2] * n_side if dim == 3 else 1
+        per = tuple(bool(p) for p in periodic[:dim]) + (True,) * (3 - dim)
+        # enumerate blocks in p4est order
+        tz, ty, tx = np.meshgrid(np.arange(bricks[2]), np.arange(bricks[1]), np.arange(bricks[0]), indexing="ij")
+        trees = np.stack([tx.ravel(), ty.ravel(), tz.ravel()], axis=1)
+        lz, ly, lx = np.meshgrid(np.arange(n_side if dim == 3 else 1), np.arange(n_side), np.arange(n_side),
+                                 indexing="ij")
+        lx, ly, lz = lx.ravel(), ly.ravel(), lz.ravel()
+        order = np.argsort(_morton_key(lx, ly, lz, max(level, 1)), kind="stable")
+        lx, ly, lz = lx[order], ly[order], lz[order]
+        coords = []
+        for t in trees:
+            coords.append(np.stack([t[0] * n_side + lx, t[1] * n_side + ly,
+                                    (t[2] * n_side if dim == 3 else 0) + lz], axis=1))
+        coords = np.concatenate(coords).astype(np.int64)
+        n_owned = coords.shape[0]
+        lookup = -np.ones((gx, gy, gz), dtype=np.int64)
+        lookup[coords[:, 0], coords[:, 1], coords[:, 2]] = np.arange(n_owned)
+
+        # outside blocks across non-periodic boundaries: one layer, including edge/corner ones
+        ext_lookup = {}
+        out_coords, out_src, out_dir = [], [], []
+        if not all(per[:dim]):
+            rng = [range(-1, g + 1) if not per[d] else range(g) for d, g in enumerate((gx, gy, gz))]
+            if dim == 2:
+                rng[2] = range(1)
+            for cz in rng[2]:
+                for cy in rng[1]:
+                    for cx in rng[0]:
+                        c = (cx, cy, cz)
+                        inside = 0 <= cx < gx and 0 <= cy < gy and 0 <= cz < gz
+                        if inside:
+                            continue
+                        # source: clamp to the grid; direction: first axis that is outside
+                        src = (min(max(cx, 0), gx - 1), min(max(cy, 0), gy - 1), min(max(cz, 0), gz - 1))
+                        d_out = next(d for d in range(3) if c[d] != src[d])
+                        side = -1 if c[d_out] < 0 else 1
+                        ext_lookup[c] = n_owned + len(out_coords)
+                        out_coords.append(c)
+                        out_src.append(lookup[src])
+                        out_dir.append((d_out, side))
+        n_blocks = n_owned + len(out_coords)
+        all_coords = np.concatenate([coords, np.array(out_coords, dtype=np.int64).reshape(-1, 3)])
+        gsz = (gx, gy, gz)
+
+        def find(c):
+            c = list(c)
+            for d in range(3):
+                if per[d]:
+                    c[d] %= gsz[d]
+            if all(0 <= c[d] < gsz[d] for d in range(3)):
+                return int(lookup[c[0], c[1], c[2]])
+            return ext_lookup.get(tuple(c), -1)
+
+        neighbor = -np.ones((n_blocks, 27), dtype=np.int32)
+        offs = [(ox, oy, oz) for oz in (-1, 0, 1) for oy in (-1, 0, 1) for ox in (-1, 0, 1)]
+        if all(per[:dim]):
+            # vectorised periodic case
+            for ox, oy, oz in offs:
+                if dim == 2 and oz != 0:
+                    continue
+                nc = (coords + np.array([ox, oy, oz])) % np.array(gsz)
+                neighbor[:n_owned, nb_slot(ox, oy, oz)] = lookup[nc[:, 0], nc[:, 1], nc[:, 2]]
+        else:
+            for b in range(n_blocks):
+                for ox, oy, oz in offs:
+                    if dim == 2 and oz != 0:
+                        continue
+                    c = all_coords[b] + np.array([ox, oy, oz])
+                    neighbor[b, nb_slot(ox, oy, oz)] = find(tuple(int(v) for v in c))
+        return BlockMesh(dim=dim, block=(bx, by, bz), level=np.full(n_blocks, level, dtype=np.int32),
+                         neighbor=neighbor, coords=all_coords, n_owned=n_owned, grid=gsz, periodic=per,
+                         scaling_factor=scaling_factor,
+                         outside_src=np.array(out_src, dtype=np.int32),
+                         outside_dir=np.array(out_dir, dtype=np.int32).reshape(-1, 2))
+
+    # ---- layout helpers -------------------------------------------------------------------------
+    def alloc_state(self):
+        """Zeroed U [n_blocks, 5, bz, by, bx] and B [n_blocks, nface] (C-ABI layout, FP64)."""
+        bx, by, bz = self.block
+        return (np.zeros((self.n_blocks, 5, bz, by, bx), dtype=np.float64),
+                np.zeros((self.n_blocks, self.nface), dtype=np.float64))
+
+    def split_faces(self, B: np.ndarray):
+        """Views (Bx, By, Bz) of a face array [n_blocks, nface] with shapes (z, y, x)."""
+        bx, by, bz = self.block
+        nfx, nfy, nfz = self.face_counts
+        Bx = B[:, :nfx].reshape(-1, bz, by, bx + 1)
+        By = B[:, nfx:nfx + nfy].reshape(-1, bz, by + 1, bx)
+        if self.dim == 3:
+            Bz = B[:, nfx + nfy:].reshape(-1, bz + 1, by, bx)
+        else:
+            Bz = B[:, nfx + nfy:].reshape(-1, bz, by, bx)
+        return Bx, By, Bz
+
+    def global_cell_index(self):
+        """Global integer (x, y, z) cell coordinates per owned cell, arrays shaped like U[:, 0]."""
+        bx, by, bz = self.block
+        c = self.coords[: self.n_blocks]
+        k, j, i = np.meshgrid(np.arange(bz), np.arange(by), np.arange(bx), indexing="ij")
+        gi = c[:, 0, None, None, None] * bx + i[None]
+        gj = c[:, 1, None, None, None] * by + j[None]
+        gk = c[:, 2, None, None, None] * bz + k[None]
+        return gi, gj, gk

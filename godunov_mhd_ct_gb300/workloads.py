@@ -1,0 +1,182 @@
+"""Seeded synthetic initial states for the benchmark configurations (host side, numpy).
+
+The reference has no shipped datasets; these generators stand in for its init/ problems with
+the shapes, sizes and distributions of the benchmark configurations:
+
+* Orszag-Tang 2D/3D (init/InitOrszagTang.cpp): rho = 25/(36 pi), p = 5/(12 pi),
+  v = (-sin 2 pi y, sin 2 pi x, 0); face B is the discrete curl of
+  A_z = B0 (cos 4 pi x / (4 pi) + cos 2 pi y / (2 pi)) sampled at edges, B0 = 1/sqrt(4 pi), so the
+  discrete divergence is zero to round-off. Optional seeded density perturbation
+  rho *= 1 + amp (2U - 1), U from splitmix64(seed, global cell id).
+* field loop advection (init/InitFieldLoopAdvection.cpp), magnetic blast (init/InitBlast.cpp).
+
+Every value is computed from global integer cell/face/edge indices, so the copies of a face that
+two blocks share are bit-identical.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .mesh import BlockMesh
+
+def splitmix64(x: np.ndarray) -> np.ndarray:
+    """splitmix64 finaliser (Steele, Lea & Flood 2014) on uint64 arrays, wrapping arithmetic."""
+    with np.errstate(over="ignore"):
+        z = (x.astype(np.uint64) + np.uint64(0x9E3779B97F4A7C15))
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def uniform01(seed: int, ids: np.ndarray) -> np.ndarray:
+    """Counter-based U[0,1) from (seed, id)."""
+    with np.errstate(over="ignore"):
+        x = (np.uint64(seed) << np.uint64(40)) ^ ids.astype(np.uint64)
+    return (splitmix64(x) >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def _faces_from_az(mesh: BlockMesh, B: np.ndarray, az, x0=0.0, y0=0.0):
+    """Face B = curl(A_z e_z) on the faces of every block; az(x, y) evaluated at edges."""
+    bx, by, bz = mesh.block
+    dx = mesh.cell_length()
+    Bx, By, Bz = mesh.split_faces(B)
+    c = mesh.coords
+    # x faces: Bx(i, j) = (Az(x_i, y_{j+1}) - Az(x_i, y_j)) / dy
+    k, j, i = np.meshgrid(np.arange(bz), np.arange(by), np.arange(bx + 1), indexing="ij")
+    gi = (c[:, 0, None, None, None] * bx + i[None]).astype(np.float64)
+    gj = (c[:, 1, None, None, None] * by + j[None]).astype(np.float64)
+    Bx[...] = (az(x0 + gi * dx, y0 + (gj + 1) * dx) - az(x0 + gi * dx, y0 + gj * dx)) / dx
+    # y faces: By(i, j) = -(Az(x_{i+1}, y_j) - Az(x_i, y_j)) / dx
+    k, j, i = np.meshgrid(np.arange(bz), np.arange(by + 1), np.arange(bx), indexing="ij")
+    gi = (c[:, 0, None, None, None] * bx + i[None]).astype(np.float64)
+    gj = (c[:, 1, None, None, None] * by + j[None]).astype(np.float64)
+    By[...] = -(az(x0 + (gi + 1) * dx, y0 + gj * dx) - az(x0 + gi * dx, y0 + gj * dx)) / dx
+    Bz[...] = 0.0
+
+
+def _cell_centred_b(mesh: BlockMesh, B: np.ndarray):
+    Bx, By, Bz = mesh.split_faces(B)
+    bcx = 0.5 * (Bx[..., :-1] + Bx[..., 1:])
+    bcy = 0.5 * (By[..., :-1, :] + By[..., 1:, :])
+    if mesh.dim == 3:
+        bcz = 0.5 * (Bz[:, :-1] + Bz[:, 1:])
+    else:
+        bcz = Bz
+    return bcx, bcy, bcz
+
+
+def _fill_energy(mesh, U, B, rho, p, vx, vy, vz, gamma):
+    bcx, bcy, bcz = _cell_centred_b(mesh, B)
+    n = mesh.n_owned
+    U[:n, 0] = rho
+    U[:n, 2] = rho * vx
+    U[:n, 3] = rho * vy
+    U[:n, 4] = rho * vz
+    U[:n, 1] = p / (gamma - 1.0) + 0.5 * rho * (vx * vx + vy * vy + vz * vz) + 0.5 * (
+        bcx[:n] ** 2 + bcy[:n] ** 2 + bcz[:n] ** 2)
+
+
+def orszag_tang(mesh: BlockMesh, gamma: float = 5.0 / 3.0, rho_perturbation: float = 0.0, seed: int = 0):
+    """Orszag-Tang vortex on [0,1]^d (uniform in z in 3D). Returns (U, B)."""
+    U, B = mesh.alloc_state()
+    B0 = 1.0 / math.sqrt(4.0 * math.pi)
+    twopi = 2.0 * math.pi
+
+    def az(x, y):
+        return B0 * (np.cos(2.0 * twopi * x) / (2.0 * twopi) + np.cos(twopi * y) / twopi)
+
+    _faces_from_az(mesh, B, az)
+    n = mesh.n_owned
+    gi, gj, gk = mesh.global_cell_index()
+    gi, gj, gk = gi[:n], gj[:n], gk[:n]
+    dx = mesh.cell_length()
+    x = (gi + 0.5) * dx
+    y = (gj + 0.5) * dx
+    rho = np.full(x.shape, 25.0 / (36.0 * math.pi))
+    if rho_perturbation:
+        gx = mesh.grid[0] * mesh.block[0]
+        gy = mesh.grid[1] * mesh.block[1]
+        ids = gi + gx * (gj + gy * gk)
+        rho = rho * (1.0 + rho_perturbation * (2.0 * uniform01(seed, ids) - 1.0))
+    p = np.full(x.shape, 5.0 / (12.0 * math.pi))
+    vx = -np.sin(twopi * y)
+    vy = np.sin(twopi * x)
+    vz = np.zeros_like(x)
+    _fill_energy(mesh, U, B, rho, p, vx, vy, vz, gamma)
+    return U, B
+
+
+def field_loop(mesh: BlockMesh, gamma=5.0 / 3.0, radius=0.3, speed=1.0, angle=0.0, A0=1e-3,
+               x0=-1.0, y0=-0.5):
+    """Field-loop advection: rho = 1, p = 1, v = speed (cos a, sin a), A_z = A0 (R - r) for r < R,
+    on [x0, x0 + Lx] x [y0, y0 + Ly] (init/InitFieldLoopAdvection.cpp)."""
+    U, B = mesh.alloc_state()
+
+    def az(x, y):
+        r = np.sqrt(x * x + y * y)
+        return np.where(r < radius, A0 * (radius - r), 0.0)
+
+    _faces_from_az(mesh, B, az, x0=x0, y0=y0)
+    n = mesh.n_owned
+    shape = U[:n, 0].shape
+    vx = np.full(shape, speed * math.cos(angle))
+    vy = np.full(shape, speed * math.sin(angle))
+    _fill_energy(mesh, U, B, np.ones(shape), np.ones(shape), vx, vy, np.zeros(shape), gamma)
+    return U, B
+
+
+def uniform_state(mesh: BlockMesh, gamma=1.4, rho=1.3, p=0.7, v=(0.3, -0.2, 0.1), b=(0.4, -0.25, 0.15)):
+    """Exactly uniform state (must be preserved exactly by the scheme)."""
+    U, B = mesh.alloc_state()
+    Bx, By, Bz = mesh.split_faces(B)
+    Bx[...] = b[0]
+    By[...] = b[1]
+    Bz[...] = b[2]
+    n = mesh.n_owned
+    shape = U[:n, 0].shape
+    vz = v[2]
+    _fill_energy(mesh, U, B, np.full(shape, rho), np.full(shape, p), np.full(shape, v[0]),
+                 np.full(shape, v[1]), np.full(shape, vz), gamma)
+    return U, B
+
+
+def random_smooth(mesh: BlockMesh, gamma=1.4, seed=0, amp=0.2):
+    """Smooth random periodic state (few Fourier modes) with a divergence-free face B."""
+    rng = np.random.default_rng(seed)
+    U, B = mesh.alloc_state()
+    kx, ky = rng.integers(1, 3, 2)
+    ph = rng.uniform(0, 2 * math.pi, 6)
+    Lx = mesh.grid[0] * mesh.block[0] * mesh.cell_length()
+    Ly = mesh.grid[1] * mesh.block[1] * mesh.cell_length()
+
+    def az(x, y):
+        return 0.1 * (np.sin(2 * math.pi * kx * x / Lx + ph[0]) * np.cos(2 * math.pi * ky * y / Ly + ph[1]))
+
+    _faces_from_az(mesh, B, az)
+    Bx, By, Bz = mesh.split_faces(B)
+    Bx += 0.3
+    By -= 0.2
+    n = mesh.n_owned
+    gi, gj, gk = mesh.global_cell_index()
+    dx = mesh.cell_length()
+    x = (gi[:n] + 0.5) * dx
+    y = (gj[:n] + 0.5) * dx
+    z = (gk[:n] + 0.5) * dx
+    Lz = mesh.grid[2] * mesh.block[2] * dx
+    if mesh.dim == 3:
+        # Bz face values: a constant keeps the field divergence-free
+        Bz[...] = 0.15
+    else:
+        Bz[...] = 0.1
+    s = np.sin(2 * math.pi * x / Lx + ph[2]) * np.cos(2 * math.pi * y / Ly + ph[3])
+    if mesh.dim == 3:
+        s = s * np.cos(2 * math.pi * z / Lz + ph[4])
+    rho = 1.0 + amp * s
+    p = 1.0 + amp * np.cos(2 * math.pi * x / Lx + ph[4])
+    vx = 0.5 * amp * np.sin(2 * math.pi * y / Ly + ph[1])
+    vy = 0.5 * amp * np.cos(2 * math.pi * x / Lx + ph[0])
+    vz = 0.3 * amp * s if mesh.dim == 3 else 0.2 * amp * s
+    _fill_energy(mesh, U, B, rho, p, vx, vy, vz, gamma)
+    return U, B

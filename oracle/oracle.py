@@ -1,0 +1,157 @@
+"""ctypes front-end of the FP64 CPU oracle (test infrastructure only; see ``oracle/__init__.py``).
+
+Parity is pinned per call against golden vectors recorded from the reference's own model headers
+(``tests/golden/``); the stage orchestration follows scheme/GodunovImplemV0.cpp:101-207.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_REF_PATH = os.path.join(_HERE, "_ref", "libref_models.so")
+_lib = None
+
+
+class OracleMesh(ctypes.Structure):
+    _fields_ = [
+        ("dim", ctypes.c_int32), ("bx", ctypes.c_int32), ("by", ctypes.c_int32),
+        ("bz", ctypes.c_int32), ("n_blocks", ctypes.c_int32), ("n_owned", ctypes.c_int32),
+        ("level", ctypes.POINTER(ctypes.c_int32)), ("neighbor", ctypes.POINTER(ctypes.c_int32)),
+        ("scaling_factor", ctypes.c_double),
+    ]
+
+
+class OracleSettings(ctypes.Structure):
+    _fields_ = [
+        ("gamma0", ctypes.c_double), ("cfl", ctypes.c_double), ("slope_type", ctypes.c_double),
+        ("smallr", ctypes.c_double), ("smallc", ctypes.c_double), ("riemann", ctypes.c_int32),
+    ]
+
+
+def build() -> None:
+    """Compile liboracle.so with the committed Makefile (no-op when up to date)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+def build_refkat() -> bool:
+    """Compile the reference-header bridge when the reference tree is mounted. Returns success."""
+    ref = os.environ.get("GMHD_REFERENCE_TREE", "/root/reference")
+    if not os.path.isdir(os.path.join(ref, "models")):
+        return False
+    subprocess.run(["make", "-s", "-C", os.path.join(_HERE, "refkat"), f"REF={ref}"], check=True)
+    return os.path.exists(_REF_PATH)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.oracle_step.restype = ctypes.c_int
+        L.oracle_step.argtypes = [ctypes.POINTER(OracleMesh), ctypes.POINTER(OracleSettings), dp, dp, dp, dp,
+                                  ctypes.c_double]
+        L.oracle_inv_dt.restype = ctypes.c_double
+        L.oracle_inv_dt.argtypes = [ctypes.POINTER(OracleMesh), ctypes.POINTER(OracleSettings), dp, dp]
+        L.oracle_run.restype = ctypes.c_int
+        L.oracle_run.argtypes = [ctypes.POINTER(OracleMesh), ctypes.POINTER(OracleSettings), dp, dp, ctypes.c_int,
+                                 dp]
+        L.oracle_riemann.argtypes = [ctypes.POINTER(OracleSettings), dp, dp, dp]
+        L.oracle_compute_emf.restype = ctypes.c_double
+        L.oracle_compute_emf.argtypes = [ctypes.POINTER(OracleSettings), dp, ctypes.c_int]
+        L.oracle_compute_primitives.argtypes = [ctypes.POINTER(OracleSettings), dp, dp, dp]
+        L.oracle_find_speed_info.argtypes = [ctypes.POINTER(OracleSettings), dp, ctypes.c_int, dp]
+        L.oracle_find_speed_fast.restype = ctypes.c_double
+        L.oracle_find_speed_fast.argtypes = [ctypes.POINTER(OracleSettings), dp, ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def _dp(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def settings(gamma0=1.4, cfl=0.5, slope_type=1.0, smallr=1e-10, smallc=1e-10, riemann=5) -> OracleSettings:
+    return OracleSettings(gamma0, cfl, slope_type, smallr, smallc, riemann)
+
+
+class Mesh:
+    """Holds the ctypes mesh plus the numpy arrays it points into."""
+
+    def __init__(self, dim, bx, by, bz, level, neighbor, n_owned, scaling_factor=1.0):
+        self.level = np.ascontiguousarray(level, dtype=np.int32)
+        self.neighbor = np.ascontiguousarray(neighbor, dtype=np.int32)
+        self.c = OracleMesh(dim, bx, by, bz if dim == 3 else 1, len(self.level), n_owned,
+                            self.level.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                            self.neighbor.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), scaling_factor)
+
+
+def step(mesh: Mesh, st: OracleSettings, U, B, dt):
+    """One do_time_step from (U, B); returns (U2, B2)."""
+    U2 = np.array(U, dtype=np.float64, copy=True, order="C")
+    B2 = np.array(B, dtype=np.float64, copy=True, order="C")
+    rc = lib().oracle_step(ctypes.byref(mesh.c), ctypes.byref(st), _dp(U), _dp(U2), _dp(B), _dp(B2), dt)
+    if rc != 0:
+        raise RuntimeError(f"oracle_step failed: {rc}")
+    return U2, B2
+
+
+def inv_dt(mesh: Mesh, st: OracleSettings, U, B) -> float:
+    return lib().oracle_inv_dt(ctypes.byref(mesh.c), ctypes.byref(st), _dp(U), _dp(B))
+
+
+def run(mesh: Mesh, st: OracleSettings, U, B, nsteps):
+    """nsteps of CFL + step, in place on copies; returns (U, B, dts)."""
+    U = np.array(U, dtype=np.float64, copy=True, order="C")
+    B = np.array(B, dtype=np.float64, copy=True, order="C")
+    dts = np.zeros(max(nsteps, 1), dtype=np.float64)
+    rc = lib().oracle_run(ctypes.byref(mesh.c), ctypes.byref(st), _dp(U), _dp(B), nsteps, _dp(dts))
+    if rc != 0:
+        raise RuntimeError(f"oracle_run failed: {rc}")
+    return U, B, dts[:nsteps]
+
+
+# ---- per-call math (known-answer tests) -------------------------------------------------------
+def riemann(st, qL, qR):
+    qL = np.ascontiguousarray(qL, dtype=np.float64)
+    qR = np.ascontiguousarray(qR, dtype=np.float64)
+    out = np.zeros_like(qL)
+    for i in range(qL.shape[0]):
+        lib().oracle_riemann(ctypes.byref(st), _dp(qL[i]), _dp(qR[i]), _dp(out[i]))
+    return out
+
+
+def compute_emf(st, q, emf_dir):
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    return np.array([lib().oracle_compute_emf(ctypes.byref(st), _dp(q[i]), emf_dir) for i in range(q.shape[0])])
+
+
+def compute_primitives(st, u):
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    q = np.zeros_like(u)
+    c = np.zeros(u.shape[0])
+    cc = ctypes.c_double()
+    for i in range(u.shape[0]):
+        lib().oracle_compute_primitives(ctypes.byref(st), _dp(u[i]), _dp(q[i]), ctypes.byref(cc))
+        c[i] = cc.value
+    return q, c
+
+
+def find_speed_info(st, q, dim):
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    out = np.zeros((q.shape[0], 3))
+    for i in range(q.shape[0]):
+        lib().oracle_find_speed_info(ctypes.byref(st), _dp(q[i]), dim, _dp(out[i]))
+    return out
+
+
+def find_speed_fast(st, q, d):
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    return np.array([lib().oracle_find_speed_fast(ctypes.byref(st), _dp(q[i]), d) for i in range(q.shape[0])])

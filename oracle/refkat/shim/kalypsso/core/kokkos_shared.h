@@ -1,0 +1,59 @@
+// Stub of the Kokkos pieces the reference's models/*.h use (Kokkos::Array, the inline-function
+// macro, abort) plus kalypsso-core's small index enums. Host-only, for the known-answer bridge.
+#pragma once
+#include <cstddef>
+#include <cstdio>
+#include <cstdlib>
+#include <kalypsso/core/real_type.h>
+
+#define KOKKOS_INLINE_FUNCTION inline
+#define KOKKOS_ASSERT(x) ((void)0)
+
+namespace Kokkos
+{
+template <typename T, std::size_t N>
+struct Array
+{
+  T m_data[N > 0 ? N : 1];
+  T &       operator[](std::size_t i) { return m_data[i]; }
+  const T & operator[](std::size_t i) const { return m_data[i]; }
+  static constexpr std::size_t size() { return N; }
+};
+[[noreturn]] inline void
+abort(const char * msg)
+{
+  std::fprintf(stderr, "Kokkos::abort: %s\n", msg);
+  std::abort();
+}
+} // namespace Kokkos
+
+namespace kalypsso
+{
+enum ComponentIndex3D : int
+{
+  IX = 0,
+  IY = 1,
+  IZ = 2
+};
+enum EmfDir : int
+{
+  EMFX = 0,
+  EMFY = 1,
+  EMFZ = 2
+};
+// positions of the four states of the 2D magnetic Riemann problem / of the edge states
+enum RiemannProblemPos : int
+{
+  ILL = 0,
+  IRL = 1,
+  ILR = 2,
+  IRR = 3
+};
+enum EdgeStatePos : int
+{
+  IRT = 0,
+  IRB = 1,
+  ILT = 2,
+  ILB = 3
+};
+} // namespace kalypsso
