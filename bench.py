@@ -1,0 +1,320 @@
+"""Benchmark: cell-updates/s of the MUSCL-Hancock + CT stage on 3D Orszag-Tang 256^3
+(512 leaf blocks of 32^3, periodic), mixed FP32/FP64 path vs the FP64 drop-in, with the HBM
+roofline of the fused step kernel, an end-to-end host-buffer number and the CPU baseline.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gmhd|reference]
+
+A step is one solver iteration (CFL reduction + do_time_step) over the whole 256^3 mesh. Inputs
+(U, B: 2.2 GB in FP64) are far larger than L2 (129 MB), so no L2 flush is needed between steps.
+Under torchrun each rank runs an independent replica of the workload (replicas only; the driver
+reports the aggregate). Prints one JSON line on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "cell-updates/s on 1 GB300, mixed vs FP64 at L1(rho)<=1e-6; % of HBM roofline"
+UNIT = "cell-updates/s"
+BYTES_PER_CELL_UPDATE = 128.0  # read U(5)+B(3), write U2(5)+B2(3), FP64
+FALLBACK_HBM_GBS = 6800.0
+# DRAM bytes per fused-step launch on the full workload, from the ncu capture summarised in
+# profiles/fused_step_mixed_ot3d.md (None until measured)
+MEASURED_TRAFFIC_BYTES = None
+
+
+def hbm_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:  # noqa: BLE001
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active," \
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown," \
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:  # noqa: BLE001
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:  # noqa: BLE001
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+                for n, v in zip(names, r[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(side_blocks=8, block=32, seed=12345):
+    from godunov_mhd_ct_gb300 import workloads as wl
+    from godunov_mhd_ct_gb300.mesh import BlockMesh
+
+    level = int(np.log2(side_blocks))
+    mesh = BlockMesh.uniform(3, level=level, block=(block, block, block))
+    U, B = wl.orszag_tang(mesh, gamma=5.0 / 3.0, rho_perturbation=1e-3, seed=seed)
+    return mesh, U, B
+
+
+def settings():
+    from godunov_mhd_ct_gb300.settings import MHDSettings
+
+    return MHDSettings(gamma0=5.0 / 3.0, cfl=0.5, slope_type=2.0, riemann="HLLD")
+
+
+def cpu_baseline_run(steps, warmup, seconds_cap=25.0):
+    """Time the FP64 oracle (the CPU restatement of the reference stage) on all host cores on a
+    64^3 sample (8 blocks of 32^3) of the same Orszag-Tang workload."""
+    from oracle import oracle as orc
+
+    orc.build()
+    mesh, U, B = make_workload(side_blocks=2, block=32)
+    st = settings()
+    om = orc.Mesh(3, 32, 32, 32, mesh.level, mesh.neighbor, mesh.n_owned)
+    os_ = orc.settings(gamma0=st.gamma0, cfl=st.cfl, slope_type=st.slope_type, riemann=st.riemann_id)
+    orc.run(om, os_, U, B, max(1, min(warmup, 2)))
+    done, t0 = 0, time.perf_counter()
+    Uc, Bc = U, B
+    while done < steps:
+        Uc, Bc, _ = orc.run(om, os_, Uc, Bc, 1)
+        done += 1
+        if time.perf_counter() - t0 > seconds_cap:
+            break
+    el = time.perf_counter() - t0
+    cells = mesh.n_owned * mesh.ncell
+    return {"value": cells * done / el, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"3D Orszag-Tang 64^3 (8 blocks of 32^3), {done} oracle steps, FP64, OpenMP over blocks",
+            "ms_per_step": 1e3 * el / done, "steps": done}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    cb = cpu_baseline_run(args.steps, args.warmup, seconds_cap=120.0)
+    line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": cb["steps"], "warmup": args.warmup, "ms_per_step": cb["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "3d_orszag_tang_256^3 (CPU sample: 64^3, 8 blocks of 32^3)",
+                       "note": "the reference's Kokkos build needs kalypsso-core/Kokkos/p4est (absent); this arm "
+                               "times the FP64 CPU restatement of its stage"},
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gmhd", choices=["gmhd", "reference"])
+    ap.add_argument("--side-blocks", type=int, default=8, help="blocks per side (8 -> 256^3 with 32^3 blocks)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+
+    from godunov_mhd_ct_gb300.csrc import build as cbuild
+
+    if not os.path.exists(cbuild.LIB):
+        cbuild.build()
+    from godunov_mhd_ct_gb300.solver import GodunovImplemGB300
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    mesh, U, B = make_workload(side_blocks=args.side_blocks)
+    st = settings()
+    cells = mesh.n_owned * mesh.ncell
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        dU0 = torch.from_numpy(U).cuda()
+        dB0 = torch.from_numpy(B).cuda()
+        dU, dB = dU0.clone(), dB0.clone()
+        dU2, dB2 = torch.empty_like(dU), torch.empty_like(dB)
+    stream.synchronize()
+
+    # ---- headline: mixed-precision solver iterations (graph-captured, dt on device) -----------
+    mixed = GodunovImplemGB300(st, mesh, precision="mixed")
+    mixed.advance(dU, dU2, dB, dB2, args.warmup, stream=stream)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    dtlog, _ = mixed.advance(dU, dU2, dB, dB2, args.steps, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * cells * args.steps / (ms * 1e-3)
+
+    # ---- dominant kernel: the fused step, timed alone with CUDA events on its stream ----------
+    nk = 20
+    dt_fixed = float(dtlog[0, 0])
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            mixed.do_time_step(dU0, dU2, dB0, dB2, dt_fixed, stream=stream)
+        k0.record(stream)
+        for _ in range(nk):
+            mixed.do_time_step(dU0, dU2, dB0, dB2, dt_fixed, stream=stream)
+        k1.record(stream)
+    torch.cuda.synchronize()
+    kern_ms = k0.elapsed_time(k1) / nk
+    peak, peak_src = hbm_peak()
+    achieved = BYTES_PER_CELL_UPDATE * cells / (kern_ms * 1e-3) / 1e9
+
+    out = {}
+    if rank == 0:
+        # ---- FP64 drop-in path on the same workload, and accuracy of mixed vs FP64 -----------
+        n_acc = min(args.steps, 10)
+        fp64 = GodunovImplemGB300(st, mesh, precision="fp64")
+        with torch.cuda.stream(stream):
+            aU, aB = dU0.clone(), dB0.clone()
+            bU, bB = dU0.clone(), dB0.clone()
+        fp64.advance(aU, dU2, aB, dB2, 1, stream=stream)  # warm-up (graph capture excluded)
+        with torch.cuda.stream(stream):
+            aU.copy_(dU0)
+            aB.copy_(dB0)
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        fp64.advance(aU, dU2, aB, dB2, n_acc, stream=stream)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        fp64_ms = f0.elapsed_time(f1) / n_acc
+        mixed.advance(bU, dU2, bB, dB2, n_acc, stream=stream)
+        torch.cuda.synchronize()
+        n = mesh.n_owned
+        Ua, Ba, Ub, Bb = aU.cpu().numpy()[:n], aB.cpu().numpy()[:n], bU.cpu().numpy()[:n], bB.cpu().numpy()[:n]
+
+        def l1(a, b):
+            return float(np.abs(a - b).sum() / np.abs(b).sum())
+
+        Bx, By, Bz = mesh.split_faces(Bb)
+        divb = float(np.max(np.abs((Bx[..., 1:] - Bx[..., :-1]) + (By[:, :, 1:] - By[:, :, :-1]) +
+                                   (Bz[:, 1:] - Bz[:, :-1])))) / mesh.cell_length()
+        out["accuracy"] = {"steps": n_acc, "l1_rho": l1(Ub[:, 0], Ua[:, 0]), "l1_E": l1(Ub[:, 1], Ua[:, 1]),
+                           "l1_B": l1(Bb, Ba), "max_divB_mixed": divb,
+                           "mass_drift_mixed": float(abs(Ub[:, 0].sum() - U[:n, 0].sum()) / U[:n, 0].sum()),
+                           "energy_drift_mixed": float(abs(Ub[:, 1].sum() - U[:n, 1].sum()) / U[:n, 1].sum())}
+        out["fp64"] = {"value": cells / (fp64_ms * 1e-3), "ms_per_step": fp64_ms,
+                       "mixed_over_fp64": (cells * args.steps / (ms * 1e-3 * world)) / (cells / (fp64_ms * 1e-3))}
+
+        # ---- end to end through the C ABI with host buffers (copies inside the timed region) ---
+        hU = torch.from_numpy(U).pin_memory()
+        hB = torch.from_numpy(B).pin_memory()
+        hU2 = torch.empty_like(hU).pin_memory()
+        hB2 = torch.empty_like(hB).pin_memory()
+        import ctypes
+
+        from godunov_mhd_ct_gb300 import _native as nat
+
+        L = nat.lib()
+        ne = 5
+        L.gmhd_step_host(mixed._ctx, hU.data_ptr(), hU2.data_ptr(), hB.data_ptr(), hB2.data_ptr(), dt_fixed, None)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(ne):
+            nat.check(L.gmhd_step_host(mixed._ctx, hU.data_ptr(), hU2.data_ptr(), hB.data_ptr(), hB2.data_ptr(),
+                                       ctypes.c_double(dt_fixed), None), "gmhd_step_host")
+        e2e_s = (time.perf_counter() - t0) / ne
+        out["e2e"] = {"value": cells / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(U.nbytes + B.nbytes),
+                      "d2h_bytes_per_step": int(U[:n].nbytes + B[:n].nbytes),
+                      "path": "gmhd_step_host (C ABI, pinned host buffers), mixed precision, dt fixed"}
+        if not args.no_cpu_baseline and world == 1:
+            cb = cpu_baseline_run(steps=1000, warmup=1, seconds_cap=15.0)
+            out["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32/f64 (mixed)", "data": "synthetic",
+            "config": {"workload": "3d_orszag_tang_256^3", "cells": cells, "blocks": mesh.n_owned,
+                       "block": list(mesh.block), "ghost": 2, "precision": "mixed", "riemann": "HLLD",
+                       "slope": "MC", "cfl": st.cfl, "l2": "inputs (2.2 GB) larger than L2 (129 MB); no flush"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": MEASURED_TRAFFIC_BYTES, "peak_source": peak_src,
+                         "kernel": "fused_step_kernel<float,3,8,8,8>", "kernel_ms": kern_ms,
+                         "bytes_per_launch": BYTES_PER_CELL_UPDATE * cells},
+            "gpu_launches": 2 * args.steps,
+            "clocks": clk,
+        }
+        line.update(out)
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

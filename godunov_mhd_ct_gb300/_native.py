@@ -1,0 +1,116 @@
+"""ctypes binding of libgmhd.so (include/gmhd.h). There is no fallback: if the library is
+missing or does not load, every entry point raises."""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libgmhd.so")
+
+GMHD_OK = 0
+STATUS = {0: "ok", -1: "invalid argument", -2: "mesh not set or not supported", -3: "CUDA error",
+          -4: "output aliases an input", -5: "non-physical state produced", -6: "exceeds a fixed capacity"}
+
+PRECISION = {"fp64": 0, "mixed": 1}
+RIEMANN = {"LLF": 2, "HLL": 3, "HLLC": 4, "HLLD": 5}
+BC = {"NONE": 0, "PERIODIC": 1, "ZERO_GRADIENT": 2, "WALL": 3}
+HEALTH = {1: "missing neighbour", 2: "level jump", 4: "density <= 0", 8: "non-finite value",
+          16: "FP64 pressure recovery used"}
+
+
+class GmhdParams(ctypes.Structure):
+    _fields_ = [("gamma0", ctypes.c_double), ("cfl", ctypes.c_double), ("slope_type", ctypes.c_double),
+                ("smallr", ctypes.c_double), ("smallc", ctypes.c_double), ("scaling_factor", ctypes.c_double),
+                ("riemann", ctypes.c_int32), ("precision", ctypes.c_int32)]
+
+
+_ip = ctypes.POINTER(ctypes.c_int32)
+
+
+class GmhdMesh(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_int32), ("bx", ctypes.c_int32), ("by", ctypes.c_int32), ("bz", ctypes.c_int32),
+                ("n_blocks", ctypes.c_int32), ("n_owned", ctypes.c_int32), ("level", _ip), ("neighbor", _ip),
+                ("problem", _ip), ("n_problems", ctypes.c_int32), ("outside_src", _ip), ("outside_normal", _ip),
+                ("bc", ctypes.c_int32 * 6)]
+
+
+class NativeError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def lib():
+    """Load libgmhd.so (built by godunov_mhd_ct_gb300.csrc.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise NativeError(f"{LIB_PATH} is missing: build it with python -m godunov_mhd_ct_gb300.csrc.build "
+                          "(or __graft_entry__.build()); there is no CPU fallback")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)
+    L.gmhd_create.restype = vp
+    L.gmhd_create.argtypes = [ctypes.POINTER(GmhdParams)]
+    L.gmhd_destroy.argtypes = [vp]
+    L.gmhd_set_mesh.argtypes = [vp, ctypes.POINTER(GmhdMesh)]
+    L.gmhd_mem_bytes.restype = ctypes.c_uint64
+    L.gmhd_mem_bytes.argtypes = [vp]
+    L.gmhd_step.argtypes = [vp, vp, vp, vp, vp, ctypes.c_double, vp]
+    L.gmhd_inv_dt.argtypes = [vp, vp, vp, dp, vp]
+    L.gmhd_fill_outside.argtypes = [vp, vp, vp, vp]
+    L.gmhd_advance.argtypes = [vp, vp, vp, vp, vp, ctypes.c_int32, dp, dp, dp, ctypes.c_int32, vp]
+    L.gmhd_step_host.argtypes = [vp, vp, vp, vp, vp, ctypes.c_double, vp]
+    L.gmhd_last_status.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32)]
+    L.gmhd_last_cuda_error.argtypes = [vp]
+    L.gmhd_error_string.restype = ctypes.c_char_p
+    L.gmhd_error_string.argtypes = [ctypes.c_int]
+    L.gmhd_layout_check.argtypes = [ctypes.POINTER(GmhdMesh), ctypes.c_int64, ctypes.c_int64, ctypes.c_int64]
+    _lib = L
+    return L
+
+
+def check(rc: int, what: str, ctx=None) -> None:
+    if rc != GMHD_OK:
+        extra = ""
+        if ctx is not None and rc == -3:
+            extra = f" (cudaError {lib().gmhd_last_cuda_error(ctx)})"
+        raise NativeError(f"{what} failed: {STATUS.get(rc, rc)}{extra}")
+
+
+def exported_symbols():
+    """Names declared in include/gmhd.h, for the ABI tests."""
+    return ["gmhd_create", "gmhd_destroy", "gmhd_set_mesh", "gmhd_mem_bytes", "gmhd_step", "gmhd_inv_dt",
+            "gmhd_fill_outside", "gmhd_advance", "gmhd_step_host", "gmhd_last_status", "gmhd_last_cuda_error",
+            "gmhd_error_string", "gmhd_layout_check"]
+
+
+class MeshTables:
+    """Keeps the int32 arrays a GmhdMesh points into alive."""
+
+    def __init__(self, mesh, problem=None, n_problems=1, bc=None):
+        self.level = np.ascontiguousarray(mesh.level, dtype=np.int32)
+        self.neighbor = np.ascontiguousarray(mesh.neighbor, dtype=np.int32).reshape(-1)
+        self.problem = None if problem is None else np.ascontiguousarray(problem, dtype=np.int32)
+        self.out_src = np.ascontiguousarray(mesh.outside_src, dtype=np.int32)
+        self.out_normal = np.ascontiguousarray(mesh.outside_normal, dtype=np.int32).reshape(-1)
+        if bc is None:
+            bc = [BC["PERIODIC"] if mesh.periodic[d // 2] else BC["ZERO_GRADIENT"] for d in range(6)]
+        c = GmhdMesh()
+        c.dim = mesh.dim
+        c.bx, c.by, c.bz = mesh.block
+        c.n_blocks = mesh.n_blocks
+        c.n_owned = mesh.n_owned
+        c.level = self.level.ctypes.data_as(_ip)
+        c.neighbor = self.neighbor.ctypes.data_as(_ip)
+        c.problem = self.problem.ctypes.data_as(_ip) if self.problem is not None else ctypes.cast(None, _ip)
+        c.n_problems = n_problems
+        c.outside_src = self.out_src.ctypes.data_as(_ip) if self.out_src.size else ctypes.cast(None, _ip)
+        c.outside_normal = self.out_normal.ctypes.data_as(_ip) if self.out_normal.size else ctypes.cast(None, _ip)
+        for i in range(6):
+            c.bc[i] = int(bc[i])
+        self.c = c

@@ -1,0 +1,1029 @@
+// Fused MUSCL-Hancock + constrained-transport step over one tile of one leaf block per CTA.
+//
+// One launch replaces the reference's per-stage kernels of GodunovImplemV0::do_time_step
+// (scheme/GodunovImplemV0.cpp:101-207): face-B ghost fill, primitive conversion, limited slopes,
+// Hancock predictor, edge E, sFaceMag, HLLD face fluxes + conservative update (3 directions),
+// 2D-HLLD edge EMFs, border EMF averaging and the CT face-B update. The tile and its 2-cell halo
+// are gathered from the block and its neighbours (neighbour table) into shared memory; all
+// intermediates stay on chip. Only U, B are read and U2, B2 written in HBM. The next step's CFL
+// reduction (scheme/ComputeDtMHDFunctor.cpp:86-151) is fused into the epilogue.
+//
+// Template Cfg: compute type R (double: the FP64 drop-in, float: the mixed path), dimension,
+// tile extents and threads per CTA. EXACT selects the reference's FP64 accumulation order for
+// U2 (three rounded per-direction adds); otherwise the three direction increments are summed in
+// R and added once to U in FP64.
+#pragma once
+
+#include <cstdint>
+
+#include "mhd_math.cuh"
+
+namespace gmhd
+{
+
+struct StepArgs
+{
+  const double * __restrict__ U;
+  double * __restrict__ U2;
+  const double * __restrict__ B;
+  double * __restrict__ B2;
+  const int32_t * __restrict__ neighbor; // [n_blocks * 27]
+  const int32_t * __restrict__ level;    // [n_blocks]
+  const int32_t * __restrict__ problem;  // [n_blocks] problem id, or null (single problem)
+  int     n_owned;
+  int     bx, by, bz;
+  int     tiles_x, tiles_y, tiles_z;
+  int64_t ncell, nfx, nfy, nface;
+  double  gamma0, smallr, smallc, smallp, slope_type, scaling_factor, cfl;
+  int     riemann;
+  double  dt;                                   // used when dt_dev is null
+  const double *             dt_dev;            // per problem dt on the device, or null
+  unsigned long long *       invdt_out;         // per problem: fused CFL of U2/B2 (max), or null
+  unsigned int *             health;            // OR of HEALTH_* flags
+};
+
+enum : unsigned int
+{
+  HEALTH_MISSING_NEIGHBOR = 1u,
+  HEALTH_LEVEL_JUMP = 2u,
+  HEALTH_BAD_DENSITY = 4u,
+  HEALTH_NONFINITE = 8u,
+  HEALTH_LOW_BETA_FP64 = 16u, // informational: FP64 pressure recovery was used (mixed path)
+};
+
+template <typename R_, int DIM_, int TX_, int TY_, int TZ_, int NT_, bool EXACT_>
+struct Cfg
+{
+  using R = R_;
+  static constexpr int  DIM = DIM_;
+  static constexpr int  TX = TX_;
+  static constexpr int  TY = TY_;
+  static constexpr int  TZ = DIM_ == 3 ? TZ_ : 1;
+  static constexpr int  NT = NT_;
+  static constexpr bool EXACT = EXACT_;
+
+  static constexpr int D3 = DIM == 3 ? 1 : 0;
+  // Q region: cells [-2, T+2)
+  static constexpr int QX = TX + 4, QY = TY + 4, QZ = TZ + 4 * D3;
+  static constexpr int NQ = QX * QY * QZ;
+  // faces (value at t^n): x faces [-2, TX+2], cells [-2, T+2) transverse; 2D Bz is cell-centred
+  static constexpr int NFBX = (TX + 5) * QY * QZ;
+  static constexpr int NFBY = QX * (TY + 5) * QZ;
+  static constexpr int NFBZ = QX * QY * (D3 ? TZ + 5 : 1);
+  // S region: cells [-1, T+1) (slopes, predictor, sFaceMag)
+  static constexpr int SX = TX + 2, SY = TY + 2, SZ = TZ + 2 * D3;
+  static constexpr int NS = SX * SY * SZ;
+  static constexpr int NDIR = DIM;
+  static constexpr int NSF = DIM == 3 ? 3 : 2;
+  // E region: edges [-1, T+2)
+  static constexpr int EX = TX + 3, EY = TY + 3, EZ = D3 ? TZ + 3 : 1;
+  static constexpr int NE = EX * EY * EZ;
+  static constexpr int NECOMP = DIM == 3 ? 3 : 1;
+  // EMF region: edges [0, T]
+  static constexpr int MX = TX + 1, MY = TY + 1, MZ = D3 ? TZ + 1 : 1;
+  static constexpr int NM = MX * MY * MZ;
+  // flux buffer (one direction at a time)
+  static constexpr int NF_X = (TX + 1) * TY * TZ;
+  static constexpr int NF_Y = TX * (TY + 1) * TZ;
+  static constexpr int NF_Z = TX * TY * (TZ + 1);
+  static constexpr int NF = NF_X > NF_Y ? (NF_X > NF_Z ? NF_X : NF_Z) : (NF_Y > NF_Z ? NF_Y : NF_Z);
+  static constexpr int NFV = DIM == 3 ? 5 : 6; // flux vars used by the update (2D adds Bz)
+
+  // shared-memory carve-up, in units of R
+  static constexpr int OFF_FBX = 0;
+  static constexpr int OFF_FBY = OFF_FBX + NFBX;
+  static constexpr int OFF_FBZ = OFF_FBY + NFBY;
+  static constexpr int OFF_SL = OFF_FBZ + NFBZ;
+  static constexpr int OFF_Q2 = OFF_SL + NDIR * 8 * NS;
+  static constexpr int OFF_SF = OFF_Q2 + 8 * NS;
+  static constexpr int OFF_E = OFF_SF + NSF * NS;
+  static constexpr int OFF_U1 = OFF_E + NECOMP * NE;
+  static constexpr int U1_QH = 5 * NQ;
+  static constexpr int U1_LATE = NECOMP * NM + NFV * NF;
+  static constexpr int OFF_EMF = OFF_U1;
+  static constexpr int OFF_FL = OFF_U1 + NECOMP * NM;
+  static constexpr int TOTAL = OFF_U1 + (U1_QH > U1_LATE ? U1_QH : U1_LATE);
+  static constexpr size_t SMEM_BYTES = sizeof(R) * (size_t)TOTAL + 64 * sizeof(int);
+
+  static constexpr int NCELL = TX * TY * TZ;
+  static constexpr int CPT = (NCELL + NT - 1) / NT;
+
+  __device__ static int qi(int i, int j, int k) { return (i + 2) + QX * ((j + 2) + QY * (k + 2 * D3)); }
+  __device__ static int fxi(int i, int j, int k) { return (i + 2) + (TX + 5) * ((j + 2) + QY * (k + 2 * D3)); }
+  __device__ static int fyi(int i, int j, int k) { return (i + 2) + QX * ((j + 2) + (TY + 5) * (k + 2 * D3)); }
+  __device__ static int fzi(int i, int j, int k) { return (i + 2) + QX * ((j + 2) + QY * (k + 2 * D3)); }
+  __device__ static int si(int i, int j, int k) { return (i + 1) + SX * ((j + 1) + SY * (k + D3)); }
+  __device__ static int ei(int i, int j, int k) { return (i + 1) + EX * ((j + 1) + EY * (k + D3)); }
+  __device__ static int mi(int i, int j, int k) { return i + MX * (j + MY * k); }
+};
+
+__device__ __forceinline__ int
+nb_slot(int ox, int oy, int oz)
+{
+  return (oz + 1) * 9 + (oy + 1) * 3 + (ox + 1);
+}
+
+__device__ __forceinline__ unsigned long long
+atomic_max_pos_double(unsigned long long * addr, double v)
+{
+  // positive doubles order like their bit patterns
+  return atomicMax(addr, (unsigned long long)__double_as_longlong(v));
+}
+
+template <class C>
+__global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
+{
+  using R = typename C::R;
+  constexpr int DIM = C::DIM, TX = C::TX, TY = C::TY, TZ = C::TZ, NT = C::NT, D3 = C::D3;
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R *   sm = reinterpret_cast<R *>(smem_raw);
+  R *   fbx = sm + C::OFF_FBX;
+  R *   fby = sm + C::OFF_FBY;
+  R *   fbz = sm + C::OFF_FBZ;
+  R *   sl = sm + C::OFF_SL;
+  R *   q2 = sm + C::OFF_Q2;
+  R *   sf = sm + C::OFF_SF;
+  R *   ee = sm + C::OFF_E;
+  R *   qh = sm + C::OFF_U1;
+  R *   emf = sm + C::OFF_EMF;
+  R *   fl = sm + C::OFF_FL;
+  int * s_nbr = reinterpret_cast<int *>(sm + C::TOTAL);
+  __shared__ double       s_red[NT / 32];
+  __shared__ unsigned int s_health;
+
+  const int tid = threadIdx.x;
+  const int tiles_per_block = a.tiles_x * a.tiles_y * a.tiles_z;
+  const int blk = blockIdx.x / tiles_per_block;
+  if (blk >= a.n_owned)
+    return;
+  int       t = blockIdx.x - blk * tiles_per_block;
+  const int tx = t % a.tiles_x;
+  t /= a.tiles_x;
+  const int ty = t % a.tiles_y;
+  const int tz = t / a.tiles_y;
+  const int x0 = tx * TX, y0 = ty * TY, z0 = tz * TZ;
+  const int bx = a.bx, by = a.by, bz = a.bz;
+
+  if (tid < 27)
+    s_nbr[tid] = a.neighbor[(int64_t)blk * 27 + tid];
+  if (tid == 0)
+    s_health = 0u;
+  __syncthreads();
+
+  const int myprob = a.problem ? a.problem[blk] : 0;
+  const int mylevel = a.level[blk];
+  const double dt = a.dt_dev ? a.dt_dev[myprob] : a.dt;
+  if (dt == 0.0)
+  {
+    // a problem that has reached its end time: carry the tile over unchanged
+    for (int n = tid; n < C::NCELL; n += NT)
+    {
+      const int     i = n % TX, j = (n / TX) % TY, k = n / (TX * TY);
+      const int64_t cell = (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)by * (z0 + k));
+      for (int v = 0; v < 5; ++v)
+        a.U2[((int64_t)blk * 5 + v) * a.ncell + cell] = a.U[((int64_t)blk * 5 + v) * a.ncell + cell];
+    }
+    // faces: the tile's tiles_per_block share of the block's face array
+    for (int64_t f = (int64_t)(blockIdx.x - blk * tiles_per_block) * NT + tid; f < a.nface;
+         f += (int64_t)tiles_per_block * NT)
+      a.B2[(int64_t)blk * a.nface + f] = a.B[(int64_t)blk * a.nface + f];
+    return;
+  }
+  const double dx = (1.0 / (double)((int64_t)bx << mylevel)) * a.scaling_factor;
+  const double dtdx_d = dt / dx;
+  const R      dtdx = (R)dtdx_d;
+
+  Phys<R> ph;
+  ph.gamma0 = (R)a.gamma0;
+  ph.smallr = (R)a.smallr;
+  ph.smallc = (R)a.smallc;
+  ph.smallp = (R)a.smallp;
+  ph.slope_type = (R)a.slope_type;
+  ph.riemann = a.riemann;
+
+  unsigned int health = 0u;
+
+  // ---- resolve a block-local cell / face coordinate to (block, local index) ------------------
+  auto owner = [&](int ox, int oy, int oz) -> int {
+    if ((ox | oy | oz) == 0)
+      return blk;
+    const int nb = s_nbr[nb_slot(ox, oy, oz)];
+    if (nb < 0)
+      health |= HEALTH_MISSING_NEIGHBOR;
+    else if (a.level[nb] != mylevel)
+      health |= HEALTH_LEVEL_JUMP;
+    return nb;
+  };
+  auto cell_off = [](int c, int n) { return c < 0 ? -1 : (c >= n ? 1 : 0); };
+  auto face_off = [](int f, int n) { return f < 0 ? -1 : (f > n ? 1 : 0); };
+
+  // ---- phase 1a: face B at t^n into shared memory (FillBlockGhostFaces equivalent) -----------
+  for (int n = tid; n < C::NFBX; n += NT)
+  {
+    const int i = n % (TX + 5) - 2;
+    const int j = (n / (TX + 5)) % C::QY - 2;
+    const int k = D3 ? n / ((TX + 5) * C::QY) - 2 : 0;
+    const int fi = x0 + i, cj = y0 + j, ck = z0 + k;
+    const int ox = face_off(fi, bx), oy = cell_off(cj, by), oz = D3 ? cell_off(ck, bz) : 0;
+    const int nb = owner(ox, oy, oz);
+    R         v = R(0);
+    if (nb >= 0)
+      v = (R)a.B[(int64_t)nb * a.nface + (fi - ox * bx) + (int64_t)(bx + 1) * ((cj - oy * by) + (int64_t)by * (ck - oz * bz))];
+    fbx[n] = v;
+  }
+  for (int n = tid; n < C::NFBY; n += NT)
+  {
+    const int i = n % C::QX - 2;
+    const int j = (n / C::QX) % (TY + 5) - 2;
+    const int k = D3 ? n / (C::QX * (TY + 5)) - 2 : 0;
+    const int ci = x0 + i, fj = y0 + j, ck = z0 + k;
+    const int ox = cell_off(ci, bx), oy = face_off(fj, by), oz = D3 ? cell_off(ck, bz) : 0;
+    const int nb = owner(ox, oy, oz);
+    R         v = R(0);
+    if (nb >= 0)
+      v = (R)a.B[(int64_t)nb * a.nface + a.nfx + (ci - ox * bx) + (int64_t)bx * ((fj - oy * by) + (int64_t)(by + 1) * (ck - oz * bz))];
+    fby[n] = v;
+  }
+  for (int n = tid; n < C::NFBZ; n += NT)
+  {
+    const int i = n % C::QX - 2;
+    const int j = (n / C::QX) % C::QY - 2;
+    const int k = D3 ? n / (C::QX * C::QY) - 2 : 0;
+    const int ci = x0 + i, cj = y0 + j, fk = z0 + k;
+    const int ox = cell_off(ci, bx), oy = cell_off(cj, by), oz = D3 ? face_off(fk, bz) : 0;
+    const int nb = owner(ox, oy, oz);
+    R         v = R(0);
+    if (nb >= 0)
+      v = (R)a.B[(int64_t)nb * a.nface + a.nfx + a.nfy + (ci - ox * bx) + (int64_t)bx * ((cj - oy * by) + (int64_t)by * (fk - oz * bz))];
+    fbz[n] = v;
+  }
+  __syncthreads();
+
+  // ---- phase 1b: primitive variables on the Q region (ConvertToPrimitivesVariablesFunctor) ---
+  for (int n = tid; n < C::NQ; n += NT)
+  {
+    const int i = n % C::QX - 2;
+    const int j = (n / C::QX) % C::QY - 2;
+    const int k = D3 ? n / (C::QX * C::QY) - 2 : 0;
+    const int ci = x0 + i, cj = y0 + j, ck = z0 + k;
+    const int ox = cell_off(ci, bx), oy = cell_off(cj, by), oz = D3 ? cell_off(ck, bz) : 0;
+    const int nb = owner(ox, oy, oz);
+    double    u[5] = {1.0, 1.0, 0.0, 0.0, 0.0};
+    if (nb >= 0)
+    {
+      const double * Ub = a.U + (int64_t)nb * 5 * a.ncell + (ci - ox * bx) + (int64_t)bx * ((cj - oy * by) + (int64_t)by * (ck - oz * bz));
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        u[v] = Ub[(int64_t)v * a.ncell];
+    }
+    const int qn = C::qi(i, j, k);
+    if constexpr (C::EXACT)
+    {
+      // compute_primitives (models/mhd_utils.h:449-515), cIso == 0
+      const double Bxc = 0.5 * (fbx[C::fxi(i, j, k)] + fbx[C::fxi(i + 1, j, k)]);
+      const double Byc = 0.5 * (fby[C::fyi(i, j, k)] + fby[C::fyi(i, j + 1, k)]);
+      const double Bzc = D3 ? 0.5 * (fbz[C::fzi(i, j, k)] + fbz[C::fzi(i, j, k + 1)])
+                            : 0.5 * (fbz[C::fzi(i, j, 0)] + fbz[C::fzi(i, j, 0)]);
+      const double r = fmax(u[ID], a.smallr);
+      const double vx = u[IU] / r, vy = u[IV] / r, vz = u[IW] / r;
+      const double eken = 0.5 * (vx * vx + vy * vy + vz * vz);
+      const double emag = 0.5 * (Bxc * Bxc + Byc * Byc + Bzc * Bzc);
+      const double eint = (u[IP] - emag) / r - eken;
+      const double p = fmax((a.gamma0 - 1.0) * r * eint, r * a.smallp);
+      qh[0 * C::NQ + qn] = r;
+      qh[1 * C::NQ + qn] = p;
+      qh[2 * C::NQ + qn] = vx;
+      qh[3 * C::NQ + qn] = vy;
+      qh[4 * C::NQ + qn] = vz;
+    }
+    else
+    {
+      // FP32 recovery; FP64 when magnetic + kinetic energy dominate (low beta / high Mach)
+      const R Bxc = R(0.5) * (fbx[C::fxi(i, j, k)] + fbx[C::fxi(i + 1, j, k)]);
+      const R Byc = R(0.5) * (fby[C::fyi(i, j, k)] + fby[C::fyi(i, j + 1, k)]);
+      const R Bzc = D3 ? R(0.5) * (fbz[C::fzi(i, j, k)] + fbz[C::fzi(i, j, k + 1)]) : fbz[C::fzi(i, j, 0)];
+      const R r = rmax<R>((R)u[ID], ph.smallr);
+      const R ir = R(1) / r;
+      const R vx = (R)u[IU] * ir, vy = (R)u[IV] * ir, vz = (R)u[IW] * ir;
+      const R ekin = R(0.5) * r * (vx * vx + vy * vy + vz * vz);
+      const R emag = R(0.5) * (Bxc * Bxc + Byc * Byc + Bzc * Bzc);
+      R       p = (ph.gamma0 - R(1)) * ((R)u[IP] - emag - ekin);
+      if (ekin + emag > R(4) * p * (R(1) / (ph.gamma0 - R(1))))
+      {
+        // cancellation-prone cell: recover in FP64 from the FP64 state and face values
+        double bxl, bxr, byl, byr, bzl, bzr;
+        {
+          const int fo = face_off(x0 + i, bx), fo1 = face_off(x0 + i + 1, bx);
+          const int co_y = cell_off(cj, by), co_z = D3 ? cell_off(ck, bz) : 0;
+          const int nb0 = owner(fo, co_y, co_z), nb1 = owner(fo1, co_y, co_z);
+          const int64_t tr = (int64_t)(bx + 1) * ((cj - co_y * by) + (int64_t)by * (ck - co_z * bz));
+          bxl = nb0 >= 0 ? a.B[(int64_t)nb0 * a.nface + (x0 + i - fo * bx) + tr] : 0.0;
+          bxr = nb1 >= 0 ? a.B[(int64_t)nb1 * a.nface + (x0 + i + 1 - fo1 * bx) + tr] : 0.0;
+        }
+        {
+          const int fo = face_off(y0 + j, by), fo1 = face_off(y0 + j + 1, by);
+          const int co_x = cell_off(ci, bx), co_z = D3 ? cell_off(ck, bz) : 0;
+          const int nb0 = owner(co_x, fo, co_z), nb1 = owner(co_x, fo1, co_z);
+          const int64_t base = a.nfx + (ci - co_x * bx);
+          byl = nb0 >= 0 ? a.B[(int64_t)nb0 * a.nface + base + (int64_t)bx * ((y0 + j - fo * by) + (int64_t)(by + 1) * (ck - co_z * bz))] : 0.0;
+          byr = nb1 >= 0 ? a.B[(int64_t)nb1 * a.nface + base + (int64_t)bx * ((y0 + j + 1 - fo1 * by) + (int64_t)(by + 1) * (ck - co_z * bz))] : 0.0;
+        }
+        if (D3)
+        {
+          const int fo = face_off(z0 + k, bz), fo1 = face_off(z0 + k + 1, bz);
+          const int co_x = cell_off(ci, bx), co_y = cell_off(cj, by);
+          const int nb0 = owner(co_x, co_y, fo), nb1 = owner(co_x, co_y, fo1);
+          const int64_t base = a.nfx + a.nfy + (ci - co_x * bx) + (int64_t)bx * (cj - co_y * by);
+          bzl = nb0 >= 0 ? a.B[(int64_t)nb0 * a.nface + base + (int64_t)bx * by * (z0 + k - fo * bz)] : 0.0;
+          bzr = nb1 >= 0 ? a.B[(int64_t)nb1 * a.nface + base + (int64_t)bx * by * (z0 + k + 1 - fo1 * bz)] : 0.0;
+        }
+        else
+        {
+          bzl = bzr = (double)Bzc;
+        }
+        const double Bx2 = 0.5 * (bxl + bxr), By2 = 0.5 * (byl + byr), Bz2 = 0.5 * (bzl + bzr);
+        const double rd = fmax(u[ID], a.smallr);
+        const double emag_d = 0.5 * (Bx2 * Bx2 + By2 * By2 + Bz2 * Bz2);
+        const double ekin_d = 0.5 * (u[IU] * u[IU] + u[IV] * u[IV] + u[IW] * u[IW]) / rd;
+        p = (R)((a.gamma0 - 1.0) * (u[IP] - emag_d - ekin_d));
+        health |= HEALTH_LOW_BETA_FP64;
+      }
+      p = rmax<R>(p, r * ph.smallp);
+      qh[0 * C::NQ + qn] = r;
+      qh[1 * C::NQ + qn] = p;
+      qh[2 * C::NQ + qn] = vx;
+      qh[3 * C::NQ + qn] = vy;
+      qh[4 * C::NQ + qn] = vz;
+    }
+  }
+  __syncthreads();
+
+  // ---- phase 2: limited slopes + Hancock predictor on the S region ---------------------------
+  // (ComputeLimitedSlopesFunctor.cpp:121-314, ComputeUpdatedPrimitiveVariablesFunctor.cpp:284-546)
+  for (int n = tid; n < C::NS; n += NT)
+  {
+    const int i = n % C::SX - 1;
+    const int j = (n / C::SX) % C::SY - 1;
+    const int k = D3 ? n / (C::SX * C::SY) - 1 : 0;
+    const int q0 = C::qi(i, j, k);
+    const int qxp = C::qi(i + 1, j, k), qxm = C::qi(i - 1, j, k);
+    const int qyp = C::qi(i, j + 1, k), qym = C::qi(i, j - 1, k);
+    const int qzp = D3 ? C::qi(i, j, k + 1) : q0, qzm = D3 ? C::qi(i, j, k - 1) : q0;
+    const R   st = ph.slope_type;
+    R         dq[3][8];
+    constexpr int NH = DIM == 3 ? 5 : 4; // nbvar_hydro_only<dim>() (models/MHDState.h:36-43)
+#pragma unroll
+    for (int v = 0; v < 5; ++v)
+    {
+      if (v < NH)
+      {
+        const R * Q = qh + v * C::NQ;
+        dq[0][v] = slope1<R>(Q[q0], Q[qxp], Q[qxm], st);
+        dq[1][v] = slope1<R>(Q[q0], Q[qyp], Q[qym], st);
+        dq[2][v] = D3 ? slope1<R>(Q[q0], Q[qzp], Q[qzm], st) : R(0);
+      }
+      else
+      {
+        dq[0][v] = R(0);
+        dq[1][v] = R(0);
+        dq[2][v] = R(0);
+      }
+    }
+    // magnetic slopes (slope_unsplit_scalar_mag): normal = B_R - B_L, transverse = limited slope of
+    // the face average
+    const R AL = fbx[C::fxi(i, j, k)], AR = fbx[C::fxi(i + 1, j, k)];
+    const R BL = fby[C::fyi(i, j, k)], BR = fby[C::fyi(i, j + 1, k)];
+    const R CL = D3 ? fbz[C::fzi(i, j, k)] : fbz[C::fzi(i, j, 0)];
+    const R CR = D3 ? fbz[C::fzi(i, j, k + 1)] : fbz[C::fzi(i, j, 0)];
+    auto    avgA = [&](int ii, int jj, int kk) { return (fbx[C::fxi(ii, jj, kk)] + fbx[C::fxi(ii + 1, jj, kk)]) * R(0.5); };
+    auto    avgB = [&](int ii, int jj, int kk) { return (fby[C::fyi(ii, jj, kk)] + fby[C::fyi(ii, jj + 1, kk)]) * R(0.5); };
+    auto    avgC = [&](int ii, int jj, int kk) {
+      return D3 ? (fbz[C::fzi(ii, jj, kk)] + fbz[C::fzi(ii, jj, kk + 1)]) * R(0.5)
+                : (fbz[C::fzi(ii, jj, 0)] + fbz[C::fzi(ii, jj, 0)]) * R(0.5);
+    };
+    dq[0][IA] = AR - AL;
+    dq[1][IA] = slope1<R>(avgA(i, j, k), avgA(i, j + 1, k), avgA(i, j - 1, k), st);
+    dq[0][IB] = slope1<R>(avgB(i, j, k), avgB(i + 1, j, k), avgB(i - 1, j, k), st);
+    dq[1][IB] = BR - BL;
+    dq[0][IC] = slope1<R>(avgC(i, j, k), avgC(i + 1, j, k), avgC(i - 1, j, k), st);
+    dq[1][IC] = slope1<R>(avgC(i, j, k), avgC(i, j + 1, k), avgC(i, j - 1, k), st);
+    if (D3)
+    {
+      dq[2][IA] = slope1<R>(avgA(i, j, k), avgA(i, j, k + 1), avgA(i, j, k - 1), st);
+      dq[2][IB] = slope1<R>(avgB(i, j, k), avgB(i, j, k + 1), avgB(i, j, k - 1), st);
+      dq[2][IC] = CR - CL;
+    }
+    else
+    {
+      dq[2][IA] = dq[2][IB] = dq[2][IC] = R(0);
+    }
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+#pragma unroll
+      for (int v = 0; v < 8; ++v)
+        sl[(d * 8 + v) * C::NS + n] = dq[d][v];
+
+    // Hancock predictor
+    const R r = qh[0 * C::NQ + q0], p = qh[1 * C::NQ + q0], u = qh[2 * C::NQ + q0],
+            v = qh[3 * C::NQ + q0], w = qh[4 * C::NQ + q0];
+    const R A = (AL + AR) * R(0.5), B = (BL + BR) * R(0.5), Cc = (CL + CR) * R(0.5);
+    const R gamma = ph.gamma0;
+    const R dtdy = dtdx, dtdz = dtdx;
+    const R drx = dq[0][ID], dpx = dq[0][IP], dux = dq[0][IU], dvx = dq[0][IV], dwx = dq[0][IW],
+            dAx = dq[0][IA], dBx = dq[0][IB], dCx = dq[0][IC];
+    const R dry = dq[1][ID], dpy = dq[1][IP], duy = dq[1][IU], dvy = dq[1][IV], dwy = dq[1][IW],
+            dAy = dq[1][IA], dBy = dq[1][IB], dCy = dq[1][IC];
+    R sr0, su0, sv0, sw0, sp0, sA0, sB0, sC0;
+    if constexpr (DIM == 2)
+    {
+      sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy;
+      su0 = (-u * dux - dpx / r - B * dBx / r - Cc * dCx / r) * dtdx + (-v * duy + B * dAy / r) * dtdy;
+      sv0 = (-u * dvx + A * dBx / r) * dtdx + (-v * dvy - dpy / r - A * dAy / r - Cc * dCy / r) * dtdy;
+      sw0 = (-u * dwx + A * dCx / r) * dtdx + (-v * dwy + B * dCy / r) * dtdy;
+      sp0 = (-u * dpx - dux * gamma * p) * dtdx + (-v * dpy - dvy * gamma * p) * dtdy;
+      sA0 = (u * dBy + B * duy - v * dAy - A * dvy) * dtdy;
+      sB0 = (-u * dBx - B * dux + v * dAx + A * dvx) * dtdx;
+      sC0 = (w * dAx + A * dwx - u * dCx - Cc * dux) * dtdx + (-v * dCy - Cc * dvy + w * dBy + B * dwy) * dtdy;
+    }
+    else
+    {
+      const R drz = dq[2][ID], dpz = dq[2][IP], duz = dq[2][IU], dvz = dq[2][IV], dwz = dq[2][IW],
+              dAz = dq[2][IA], dBz = dq[2][IB], dCz = dq[2][IC];
+      sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy + (-w * drz - dwz * r) * dtdz;
+      su0 = (-u * dux - (dpx + B * dBx + Cc * dCx) / r) * dtdx + (-v * duy + B * dAy / r) * dtdy +
+            (-w * duz + Cc * dAz / r) * dtdz;
+      sv0 = (-u * dvx + A * dBx / r) * dtdx + (-v * dvy - (dpy + A * dAy + Cc * dCy) / r) * dtdy +
+            (-w * dvz + Cc * dBz / r) * dtdz;
+      sw0 = (-u * dwx + A * dCx / r) * dtdx + (-v * dwy + B * dCy / r) * dtdy +
+            (-w * dwz - (dpz + A * dAz + B * dBz) / r) * dtdz;
+      sp0 = (-u * dpx - dux * gamma * p) * dtdx + (-v * dpy - dvy * gamma * p) * dtdy +
+            (-w * dpz - dwz * gamma * p) * dtdz;
+      sA0 = (u * dBy + B * duy - v * dAy - A * dvy) * dtdy + (u * dCz + Cc * duz - w * dAz - A * dwz) * dtdz;
+      sB0 = (v * dAx + A * dvx - u * dBx - B * dux) * dtdx + (v * dCz + Cc * dvz - w * dBz - B * dwz) * dtdz;
+      sC0 = (w * dAx + A * dwx - u * dCx - Cc * dux) * dtdx + (w * dBy + B * dwy - v * dCy - Cc * dvy) * dtdy;
+    }
+    q2[ID * C::NS + n] = r + R(0.5) * sr0;
+    q2[IU * C::NS + n] = u + R(0.5) * su0;
+    q2[IV * C::NS + n] = v + R(0.5) * sv0;
+    q2[IW * C::NS + n] = w + R(0.5) * sw0;
+    q2[IP * C::NS + n] = p + R(0.5) * sp0;
+    q2[IA * C::NS + n] = A + R(0.5) * sA0;
+    q2[IB * C::NS + n] = B + R(0.5) * sB0;
+    q2[IC * C::NS + n] = Cc + R(0.5) * sC0;
+  }
+
+  // ---- phase 3: edge electric field at t^n on [-1, T+2) (ComputeElectricFieldFunctor.cpp:97-235)
+  for (int n = tid; n < C::NE; n += NT)
+  {
+    const int i = n % C::EX - 1;
+    const int j = (n / C::EX) % C::EY - 1;
+    const int k = D3 ? n / (C::EX * C::EY) - 1 : 0;
+    const R * QU = qh + 2 * C::NQ;
+    const R * QV = qh + 3 * C::NQ;
+    const R * QW = qh + 4 * C::NQ;
+    if constexpr (DIM == 2)
+    {
+      const R u = R(0.25) * (QU[C::qi(i - 1, j - 1, 0)] + QU[C::qi(i - 1, j, 0)] + QU[C::qi(i, j - 1, 0)] + QU[C::qi(i, j, 0)]);
+      const R v = R(0.25) * (QV[C::qi(i - 1, j - 1, 0)] + QV[C::qi(i - 1, j, 0)] + QV[C::qi(i, j - 1, 0)] + QV[C::qi(i, j, 0)]);
+      const R A = R(0.5) * (fbx[C::fxi(i, j - 1, 0)] + fbx[C::fxi(i, j, 0)]);
+      const R B = R(0.5) * (fby[C::fyi(i - 1, j, 0)] + fby[C::fyi(i, j, 0)]);
+      ee[n] = u * B - v * A;
+    }
+    else
+    {
+      {
+        const R v = R(0.25) * (QV[C::qi(i, j - 1, k - 1)] + QV[C::qi(i, j - 1, k)] + QV[C::qi(i, j, k - 1)] + QV[C::qi(i, j, k)]);
+        const R w = R(0.25) * (QW[C::qi(i, j - 1, k - 1)] + QW[C::qi(i, j - 1, k)] + QW[C::qi(i, j, k - 1)] + QW[C::qi(i, j, k)]);
+        const R B = R(0.5) * (fby[C::fyi(i, j, k - 1)] + fby[C::fyi(i, j, k)]);
+        const R Cc = R(0.5) * (fbz[C::fzi(i, j - 1, k)] + fbz[C::fzi(i, j, k)]);
+        ee[0 * C::NE + n] = v * Cc - w * B;
+      }
+      {
+        const R u = R(0.25) * (QU[C::qi(i - 1, j, k - 1)] + QU[C::qi(i - 1, j, k)] + QU[C::qi(i, j, k - 1)] + QU[C::qi(i, j, k)]);
+        const R w = R(0.25) * (QW[C::qi(i - 1, j, k - 1)] + QW[C::qi(i - 1, j, k)] + QW[C::qi(i, j, k - 1)] + QW[C::qi(i, j, k)]);
+        const R A = R(0.5) * (fbx[C::fxi(i, j, k - 1)] + fbx[C::fxi(i, j, k)]);
+        const R Cc = R(0.5) * (fbz[C::fzi(i - 1, j, k)] + fbz[C::fzi(i, j, k)]);
+        ee[1 * C::NE + n] = w * A - u * Cc;
+      }
+      {
+        const R u = R(0.25) * (QU[C::qi(i - 1, j - 1, k)] + QU[C::qi(i - 1, j, k)] + QU[C::qi(i, j - 1, k)] + QU[C::qi(i, j, k)]);
+        const R v = R(0.25) * (QV[C::qi(i - 1, j - 1, k)] + QV[C::qi(i - 1, j, k)] + QV[C::qi(i, j - 1, k)] + QV[C::qi(i, j, k)]);
+        const R A = R(0.5) * (fbx[C::fxi(i, j - 1, k)] + fbx[C::fxi(i, j, k)]);
+        const R B = R(0.5) * (fby[C::fyi(i - 1, j, k)] + fby[C::fyi(i, j, k)]);
+        ee[2 * C::NE + n] = u * B - v * A;
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- phase 4: half-step face-B source (ComputeSourceFaceMagFunctor.cpp:114-203) ------------
+  for (int n = tid; n < C::NS; n += NT)
+  {
+    const int i = n % C::SX - 1;
+    const int j = (n / C::SX) % C::SY - 1;
+    const int k = D3 ? n / (C::SX * C::SY) - 1 : 0;
+    const R   dtdy = dtdx, dtdz = dtdx;
+    if constexpr (DIM == 2)
+    {
+      sf[0 * C::NS + n] = (ee[C::ei(i, j + 1, 0)] - ee[C::ei(i, j, 0)]) * R(0.5) * dtdy;
+      sf[1 * C::NS + n] = -(ee[C::ei(i + 1, j, 0)] - ee[C::ei(i, j, 0)]) * R(0.5) * dtdx;
+    }
+    else
+    {
+      const R * Ex = ee;
+      const R * Ey = ee + C::NE;
+      const R * Ez = ee + 2 * C::NE;
+      sf[0 * C::NS + n] = (Ez[C::ei(i, j + 1, k)] - Ez[C::ei(i, j, k)]) * R(0.5) * dtdy -
+                          (Ey[C::ei(i, j, k + 1)] - Ey[C::ei(i, j, k)]) * R(0.5) * dtdz;
+      sf[1 * C::NS + n] = -(Ez[C::ei(i + 1, j, k)] - Ez[C::ei(i, j, k)]) * R(0.5) * dtdx +
+                          (Ex[C::ei(i, j, k + 1)] - Ex[C::ei(i, j, k)]) * R(0.5) * dtdz;
+      sf[2 * C::NS + n] = (Ey[C::ei(i + 1, j, k)] - Ey[C::ei(i, j, k)]) * R(0.5) * dtdx -
+                          (Ex[C::ei(i, j + 1, k)] - Ex[C::ei(i, j, k)]) * R(0.5) * dtdy;
+    }
+  }
+  __syncthreads(); // qh (primitives at t^n) and ee are dead from here on
+
+  // face value at t^n of component c (0..2) at tile coords, and its limited slope along dir
+  auto fval = [&](int c, int i, int j, int k) -> R {
+    return c == 0 ? fbx[C::fxi(i, j, k)] : (c == 1 ? fby[C::fyi(i, j, k)] : fbz[C::fzi(i, j, D3 ? k : 0)]);
+  };
+  auto fslope = [&](int c, int i, int j, int k, int dir) -> R {
+    const int di = dir == 0, dj = dir == 1, dk = dir == 2;
+    return slope1<R>(fval(c, i, j, k), fval(c, i + di, j + dj, k + dk), fval(c, i - di, j - dj, k - dk), ph.slope_type);
+  };
+
+  // ---- phase 5: edge EMFs (ComputeEmfAndStoreFunctor.cpp:103-590) + border averaging ---------
+  {
+    constexpr int NEDGE = C::NECOMP * C::NM;
+    for (int n = tid; n < NEDGE; n += NT)
+    {
+      const int c = DIM == 3 ? n / C::NM : 2; // edge direction
+      const int m = n - (DIM == 3 ? c : 0) * C::NM;
+      const int i = m % C::MX;
+      const int j = (m / C::MX) % C::MY;
+      const int k = D3 ? m / (C::MX * C::MY) : 0;
+      // edge masks: an edge along c exists for cell index < T along c
+      if ((c == 0 && i >= TX) || (c == 1 && j >= TY) || (DIM == 3 && c == 2 && k >= TZ))
+      {
+        emf[n] = R(0);
+        continue;
+      }
+      R qe[4][8];
+      // states at t^{n+1/2} reconstructed to the edge from the 4 surrounding cells
+      auto recon = [&](int is, int js, int ks, int loc, int dir0, int dir1, R * q) {
+        const int sn = C::si(is, js, ks);
+#pragma unroll
+        for (int v = 0; v < 8; ++v)
+          q[v] = q2[v * C::NS + sn];
+        int sd0 = 1, sd1 = 1, sb0 = 1, sb1 = 1;
+        int i0 = is, j0 = js, k0 = ks, i1 = is, j1 = js, k1 = ks;
+        // loc: 0 = LB, 1 = RT, 2 = RB, 3 = LT
+        if (loc == 0)
+        {
+          sd0 = -1; sd1 = -1; sb0 = -1; sb1 = -1;
+        }
+        else if (loc == 1)
+        {
+          i0 += dir0 == 0; j0 += dir0 == 1; k0 += dir0 == 2;
+          i1 += dir1 == 0; j1 += dir1 == 1; k1 += dir1 == 2;
+        }
+        else if (loc == 2)
+        {
+          i0 += dir0 == 0; j0 += dir0 == 1; k0 += dir0 == 2;
+          sd1 = -1; sb0 = -1;
+        }
+        else
+        {
+          i1 += dir1 == 0; j1 += dir1 == 1; k1 += dir1 == 2;
+          sd0 = -1; sb1 = -1;
+        }
+        const R * S0 = sl + dir0 * 8 * C::NS;
+        const R * S1 = sl + dir1 * 8 * C::NS;
+        const R   f0 = (R)sd0, f1 = (R)sd1;
+        if constexpr (DIM == 2)
+        {
+          // reconstruct_state_2d_at_edge (dir0 = X, dir1 = Y)
+          R A = fbx[C::fxi(i0, j0, 0)];
+          R Bv = fby[C::fyi(i1, j1, 0)];
+          A += sf[0 * C::NS + C::si(i0, j0, 0)];
+          Bv += sf[1 * C::NS + C::si(i1, j1, 0)];
+          const R dAy = fslope(0, i0, j0, 0, 1);
+          const R dBx = fslope(1, i1, j1, 0, 0);
+#pragma unroll
+          for (int v = 0; v < 5; ++v)
+            q[v] += R(0.5) * (f0 * S0[v * C::NS + sn] + f1 * S1[v * C::NS + sn]);
+          q[IA] = A + R(0.5) * ((R)sb0 * dAy);
+          q[IB] = Bv + R(0.5) * ((R)sb1 * dBx);
+          q[IC] += R(0.5) * (f0 * S0[IC * C::NS + sn] + f1 * S1[IC * C::NS + sn]);
+        }
+        else
+        {
+          // reconstruct_state_3d_at_edge, with the reference's branch order for IA/IB/IC
+          R B0 = fval(dir0, i0, j0, k0);
+          R B1 = fval(dir1, i1, j1, k1);
+          B0 += sf[dir0 * C::NS + C::si(i0, j0, k0)];
+          B1 += sf[dir1 * C::NS + C::si(i1, j1, k1)];
+          const R dB0d1 = fslope(dir0, i0, j0, k0, dir1);
+          const R dB1d0 = fslope(dir1, i1, j1, k1, dir0);
+          auto    h = [&](int v) { return R(0.5) * (f0 * S0[v * C::NS + sn] + f1 * S1[v * C::NS + sn]); };
+#pragma unroll
+          for (int v = 0; v < 5; ++v)
+            q[v] += h(v);
+          if (dir0 == 0)
+            q[IA] = B0 + R(0.5) * ((R)sb0 * dB0d1);
+          else
+            q[IA] += h(IA);
+          if (dir0 == 1)
+            q[IB] = B0 + R(0.5) * ((R)sb0 * dB0d1);
+          else
+            q[IB] += h(IB);
+          if (dir1 == 1)
+            q[IB] = B1 + R(0.5) * ((R)sb1 * dB1d0);
+          else
+            q[IB] += h(IB);
+          if (dir1 == 2)
+            q[IC] = B1 + R(0.5) * ((R)sb1 * dB1d0);
+          else
+            q[IC] += h(IC);
+        }
+        q[ID] = rmax<R>(ph.smallr, q[ID]);
+        q[IP] = rmax<R>(ph.smallp * q[ID], q[IP]);
+      };
+      R val;
+      if (c == 2)
+      {
+        recon(i, j, k, 0, 0, 1, qe[ELB]);
+        recon(i - 1, j - 1, k, 1, 0, 1, qe[ERT]);
+        recon(i - 1, j, k, 2, 0, 1, qe[ERB]);
+        recon(i, j - 1, k, 3, 0, 1, qe[ELT]);
+        val = edge_emf<R>(qe, 2, ph) * dtdx;
+      }
+      else if (c == 1)
+      {
+        recon(i, j, k, 0, 0, 2, qe[ELB]);
+        recon(i - 1, j, k - 1, 1, 0, 2, qe[ERT]);
+        // the reference swaps the RB and LT states of y edges
+        recon(i - 1, j, k, 2, 0, 2, qe[ELT]);
+        recon(i, j, k - 1, 3, 0, 2, qe[ERB]);
+        val = edge_emf<R>(qe, 1, ph) * dtdx;
+      }
+      else
+      {
+        recon(i, j, k, 0, 1, 2, qe[ELB]);
+        recon(i, j - 1, k - 1, 1, 1, 2, qe[ERT]);
+        recon(i, j - 1, k, 2, 1, 2, qe[ERB]);
+        recon(i, j, k - 1, 3, 1, 2, qe[ELT]);
+        val = edge_emf<R>(qe, 0, ph) * dtdx;
+      }
+      // CorrectEmfAtBlockBorderFunctor (uniform level): an edge on a line where four blocks meet
+      // is averaged with its sibling copies (self first, then the non-outside siblings). On a
+      // conforming mesh every copy is computed from identical data, so the sum is of equal terms.
+      {
+        const int t0 = c == 0 ? 1 : 0;
+        const int t1 = c == 2 ? 1 : 2;
+        const int gidx[3] = {x0 + i, y0 + j, z0 + k};
+        const int bsz[3] = {bx, by, bz};
+        const int v0 = gidx[t0] == 0 ? -1 : (gidx[t0] == bsz[t0] ? 1 : 0);
+        const int v1 = (DIM == 2 && t1 == 2) ? 0 : (gidx[t1] == 0 ? -1 : (gidx[t1] == bsz[t1] ? 1 : 0));
+        if (v0 != 0 && v1 != 0)
+        {
+          int o0[3] = {0, 0, 0}, o1[3] = {0, 0, 0}, o2[3] = {0, 0, 0};
+          o0[t0] = v0;
+          o1[t1] = v1;
+          o2[t0] = v0;
+          o2[t1] = v1;
+          const int s0 = s_nbr[nb_slot(o0[0], o0[1], o0[2])];
+          const int s1 = s_nbr[nb_slot(o1[0], o1[1], o1[2])];
+          const int s2 = s_nbr[nb_slot(o2[0], o2[1], o2[2])];
+          if (s0 >= 0 && s1 >= 0 && s2 >= 0)
+          {
+            R   acc = R(0);
+            int count = 1;
+            acc += val;
+            if (s0 < a.n_owned)
+            {
+              acc += val;
+              count++;
+            }
+            if (s1 < a.n_owned)
+            {
+              acc += val;
+              count++;
+            }
+            if (s2 < a.n_owned)
+            {
+              acc += val;
+              count++;
+            }
+            val = acc / (R)count;
+          }
+        }
+      }
+      emf[n] = val;
+    }
+  }
+  __syncthreads();
+
+  // ---- phase 5b: CT update of the tile's faces (ReadEmfAndUpdateFunctor.cpp:58-163) ----------
+  // a tile owns faces [0, T) along each normal, plus face T when it ends at the block border
+  {
+    const R * Mx = emf;
+    const R * My = emf + (DIM == 3 ? C::NM : 0);
+    const R * Mz = emf + (DIM == 3 ? 2 * C::NM : 0);
+    const int ex = (x0 + TX == bx) ? 1 : 0;
+    const int ey = (y0 + TY == by) ? 1 : 0;
+    const int ez = (D3 && z0 + TZ == bz) ? 1 : 0;
+    const int nfx_t = (TX + ex) * TY * TZ;
+    const int nfy_t = TX * (TY + ey) * TZ;
+    const int nfz_t = D3 ? TX * TY * (TZ + ez) : 0;
+    double *  B2blk = a.B2 + (int64_t)blk * a.nface;
+    const double * Bblk = a.B + (int64_t)blk * a.nface;
+    for (int n = tid; n < nfx_t + nfy_t + nfz_t; n += NT)
+    {
+      if (n < nfx_t)
+      {
+        const int i = n % (TX + ex), j = (n / (TX + ex)) % TY, k = n / ((TX + ex) * TY);
+        const int64_t g = (x0 + i) + (int64_t)(bx + 1) * ((y0 + j) + (int64_t)by * (z0 + k));
+        double        d = 0;
+        if constexpr (DIM == 2)
+          d += ((double)Mz[C::mi(i, j + 1, 0)] - (double)Mz[C::mi(i, j, 0)]);
+        else
+        {
+          d += ((double)Mz[C::mi(i, j + 1, k)] - (double)Mz[C::mi(i, j, k)]);
+          d -= ((double)My[C::mi(i, j, k + 1)] - (double)My[C::mi(i, j, k)]);
+        }
+        B2blk[g] = Bblk[g] + d;
+      }
+      else if (n < nfx_t + nfy_t)
+      {
+        const int nn = n - nfx_t;
+        const int i = nn % TX, j = (nn / TX) % (TY + ey), k = nn / (TX * (TY + ey));
+        const int64_t g = a.nfx + (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)(by + 1) * (z0 + k));
+        if constexpr (DIM == 2)
+        {
+          B2blk[g] = Bblk[g] - ((double)Mz[C::mi(i + 1, j, 0)] - (double)Mz[C::mi(i, j, 0)]);
+        }
+        else
+        {
+          double d = 0;
+          d += ((double)Mx[C::mi(i, j, k + 1)] - (double)Mx[C::mi(i, j, k)]);
+          d -= ((double)Mz[C::mi(i + 1, j, k)] - (double)Mz[C::mi(i, j, k)]);
+          B2blk[g] = Bblk[g] + d;
+        }
+      }
+      else
+      {
+        const int nn = n - nfx_t - nfy_t;
+        const int i = nn % TX, j = (nn / TX) % TY, k = nn / (TX * TY);
+        const int64_t g = a.nfx + a.nfy + (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)by * (z0 + k));
+        double        d = 0;
+        d += ((double)My[C::mi(i + 1, j, k)] - (double)My[C::mi(i, j, k)]);
+        d -= ((double)Mx[C::mi(i, j + 1, k)] - (double)Mx[C::mi(i, j, k)]);
+        B2blk[g] = Bblk[g] + d;
+      }
+    }
+  }
+
+  // ---- phase 6: face fluxes per direction + conservative update -------------------------------
+  // (ComputeHydroFluxesAndStoreFunctor.cpp:335-503, ReadFluxesAndConservativeUpdateFunctor.cpp:240-436)
+  double u2[C::CPT][C::NFV];
+  R      dU[C::CPT][C::NFV];
+#pragma unroll
+  for (int c = 0; c < C::CPT; ++c)
+  {
+    const int n = tid + c * NT;
+    if (n < C::NCELL)
+    {
+      const int i = n % TX, j = (n / TX) % TY, k = n / (TX * TY);
+      const int64_t cell = (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)by * (z0 + k));
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        u2[c][v] = a.U[((int64_t)blk * 5 + v) * a.ncell + cell];
+      if constexpr (DIM == 2)
+        u2[c][5] = a.B[(int64_t)blk * a.nface + a.nfx + a.nfy + cell];
+    }
+#pragma unroll
+    for (int v = 0; v < C::NFV; ++v)
+      dU[c][v] = R(0);
+  }
+
+#pragma unroll 1
+  for (int dir = 0; dir < DIM; ++dir)
+  {
+    const int fx_n = TX + (dir == 0), fy_n = TY + (dir == 1), fz_n = TZ + (dir == 2 && D3);
+    const int nfl = fx_n * fy_n * fz_n;
+    const int di = dir == 0, dj = dir == 1, dk = dir == 2;
+    const int ivel = dir == 0 ? IU : (dir == 1 ? IV : IW);
+    const int imag = dir == 0 ? IA : (dir == 1 ? IB : IC);
+    for (int n = tid; n < nfl; n += NT)
+    {
+      const int i = n % fx_n, j = (n / fx_n) % fy_n, k = n / (fx_n * fy_n);
+      const int snL = C::si(i - di, j - dj, k - dk);
+      const int snR = C::si(i, j, k);
+      const R * S = sl + dir * 8 * C::NS;
+      R         qL[8], qR[8], flux[8];
+#pragma unroll
+      for (int v = 0; v < 8; ++v)
+      {
+        qL[v] = q2[v * C::NS + snL] + R(0.5) * S[v * C::NS + snL];
+        qR[v] = q2[v * C::NS + snR] + R(-0.5) * S[v * C::NS + snR];
+      }
+      qL[ID] = rmax<R>(ph.smallr, qL[ID]);
+      qL[IP] = rmax<R>(ph.smallp * qL[ID], qL[IP]);
+      qR[ID] = rmax<R>(ph.smallr, qR[ID]);
+      qR[IP] = rmax<R>(ph.smallp * qR[ID], qR[IP]);
+      const R bn = fval(dir, i, j, k) + sf[dir * C::NS + snR];
+      qR[imag] = bn;
+      qL[imag] = bn;
+      if (dir != 0)
+      {
+        R tmp;
+        tmp = qL[IU]; qL[IU] = qL[ivel]; qL[ivel] = tmp;
+        tmp = qR[IU]; qR[IU] = qR[ivel]; qR[ivel] = tmp;
+        tmp = qL[IA]; qL[IA] = qL[imag]; qL[imag] = tmp;
+        tmp = qR[IA]; qR[IA] = qR[imag]; qR[imag] = tmp;
+      }
+      riemann_mhd<R>(qL, qR, flux, ph);
+      if (dir != 0)
+      {
+        R tmp;
+        tmp = flux[IU]; flux[IU] = flux[ivel]; flux[ivel] = tmp;
+        tmp = flux[IA]; flux[IA] = flux[imag]; flux[imag] = tmp;
+      }
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        fl[v * C::NF + n] = flux[v] * dtdx;
+      if constexpr (DIM == 2)
+        fl[5 * C::NF + n] = flux[IC] * dtdx;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < C::CPT; ++c)
+    {
+      const int n = tid + c * NT;
+      if (n < C::NCELL)
+      {
+        const int i = n % TX, j = (n / TX) % TY, k = n / (TX * TY);
+        const int fL = i + fx_n * (j + fy_n * k);
+        const int fR = (i + di) + fx_n * ((j + dj) + fy_n * (k + dk));
+#pragma unroll
+        for (int v = 0; v < C::NFV; ++v)
+        {
+          R acc = R(0);
+          acc = acc + fl[v * C::NF + fL];
+          acc = acc - fl[v * C::NF + fR];
+          if constexpr (C::EXACT)
+            u2[c][v] += (double)acc;
+          else
+            dU[c][v] += acc;
+        }
+      }
+    }
+    __syncthreads();
+  }
+
+  // ---- phase 7: write U2 (and 2D Bz), fused CFL of the new state -----------------------------
+  double my_invdt = 0.0;
+#pragma unroll
+  for (int c = 0; c < C::CPT; ++c)
+  {
+    const int n = tid + c * NT;
+    if (n >= C::NCELL)
+      continue;
+    const int i = n % TX, j = (n / TX) % TY, k = n / (TX * TY);
+    const int64_t cell = (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)by * (z0 + k));
+    if constexpr (!C::EXACT)
+    {
+#pragma unroll
+      for (int v = 0; v < C::NFV; ++v)
+        u2[c][v] += (double)dU[c][v];
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v)
+      a.U2[((int64_t)blk * 5 + v) * a.ncell + cell] = u2[c][v];
+    if constexpr (DIM == 2)
+      a.B2[(int64_t)blk * a.nface + a.nfx + a.nfy + cell] = u2[c][5];
+    if (!(u2[c][ID] > 0.0))
+      health |= HEALTH_BAD_DENSITY;
+    if (!isfinite(u2[c][IP]) || !isfinite(u2[c][IU]))
+      health |= HEALTH_NONFINITE;
+
+    if (a.invdt_out)
+    {
+      // B2 on the 2 (3D) faces per direction of this cell, recomputed from U/B + EMFs
+      const R * Mx = emf;
+      const R * My = emf + (DIM == 3 ? C::NM : 0);
+      const R * Mz = emf + (DIM == 3 ? 2 * C::NM : 0);
+      const double * Bblk = a.B + (int64_t)blk * a.nface;
+      auto bx2 = [&](int ii) {
+        const int64_t g = (x0 + ii) + (int64_t)(bx + 1) * ((y0 + j) + (int64_t)by * (z0 + k));
+        double        d = 0;
+        if constexpr (DIM == 2)
+          d += ((double)Mz[C::mi(ii, j + 1, 0)] - (double)Mz[C::mi(ii, j, 0)]);
+        else
+        {
+          d += ((double)Mz[C::mi(ii, j + 1, k)] - (double)Mz[C::mi(ii, j, k)]);
+          d -= ((double)My[C::mi(ii, j, k + 1)] - (double)My[C::mi(ii, j, k)]);
+        }
+        return Bblk[g] + d;
+      };
+      auto by2 = [&](int jj) {
+        const int64_t g = a.nfx + (x0 + i) + (int64_t)bx * ((y0 + jj) + (int64_t)(by + 1) * (z0 + k));
+        if constexpr (DIM == 2)
+          return Bblk[g] - ((double)Mz[C::mi(i + 1, jj, 0)] - (double)Mz[C::mi(i, jj, 0)]);
+        else
+        {
+          double d = 0;
+          d += ((double)Mx[C::mi(i, jj, k + 1)] - (double)Mx[C::mi(i, jj, k)]);
+          d -= ((double)Mz[C::mi(i + 1, jj, k)] - (double)Mz[C::mi(i, jj, k)]);
+          return Bblk[g] + d;
+        }
+      };
+      auto bz2 = [&](int kk) {
+        const int64_t g = a.nfx + a.nfy + (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)by * (z0 + kk));
+        double        d = 0;
+        d += ((double)My[C::mi(i + 1, j, kk)] - (double)My[C::mi(i, j, kk)]);
+        d -= ((double)Mx[C::mi(i, j + 1, kk)] - (double)Mx[C::mi(i, j, kk)]);
+        return Bblk[g] + d;
+      };
+      // compute_cfl (ComputeDtMHDFunctor.cpp:86-151) on the updated cell
+      const double Ax = 0.5 * (bx2(i) + bx2(i + 1));
+      const double Ay = 0.5 * (by2(j) + by2(j + 1));
+      double       Az;
+      if constexpr (DIM == 3)
+        Az = 0.5 * (bz2(k) + bz2(k + 1));
+      else
+        Az = 0.5 * (u2[c][5] + u2[c][5]);
+      double val;
+      if constexpr (C::EXACT)
+      {
+        const double r = fmax(u2[c][ID], a.smallr);
+        const double vx = u2[c][IU] / r, vy = u2[c][IV] / r, vz = u2[c][IW] / r;
+        const double eken = 0.5 * (vx * vx + vy * vy + vz * vz);
+        const double emag = 0.5 * (Ax * Ax + Ay * Ay + Az * Az);
+        const double eint = (u2[c][IP] - emag) / r - eken;
+        const double p = fmax((a.gamma0 - 1.0) * r * eint, r * a.smallp);
+        const double b2 = Ax * Ax + Ay * Ay + Az * Az;
+        const double c2 = a.gamma0 * p / r;
+        const double d2 = 0.5 * (b2 / r + c2);
+        const double cfx = sqrt(d2 + sqrt(d2 * d2 - c2 * Ax * Ax / r)) + fabs(vx);
+        const double cfy = sqrt(d2 + sqrt(d2 * d2 - c2 * Ay * Ay / r)) + fabs(vy);
+        if constexpr (DIM == 3)
+        {
+          const double cfz = sqrt(d2 + sqrt(d2 * d2 - c2 * Az * Az / r)) + fabs(vz);
+          val = cfx / dx + cfy / dx + cfz / dx;
+        }
+        else
+          val = cfx / dx + cfy / dx;
+      }
+      else
+      {
+        const float  r = fmaxf((float)u2[c][ID], (float)a.smallr);
+        const float  ir = 1.0f / r;
+        const float  vx = (float)u2[c][IU] * ir, vy = (float)u2[c][IV] * ir, vz = (float)u2[c][IW] * ir;
+        const float  bxf = (float)Ax, byf = (float)Ay, bzf = (float)Az;
+        const float  ekin = 0.5f * r * (vx * vx + vy * vy + vz * vz);
+        const float  emag = 0.5f * (bxf * bxf + byf * byf + bzf * bzf);
+        const float  g = (float)a.gamma0;
+        const float  p = fmaxf((g - 1.0f) * (float)(u2[c][IP] - (double)emag - (double)ekin), r * (float)a.smallp);
+        const float  b2 = 2.0f * emag;
+        const float  c2 = g * p * ir;
+        const float  d2 = 0.5f * (b2 * ir + c2);
+        const float  cfx = sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * bxf * bxf * ir, 0.0f))) + fabsf(vx);
+        const float  cfy = sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * byf * byf * ir, 0.0f))) + fabsf(vy);
+        float        sum = cfx + cfy;
+        if constexpr (DIM == 3)
+          sum += sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * bzf * bzf * ir, 0.0f))) + fabsf(vz);
+        val = (double)sum / dx;
+      }
+      my_invdt = fmax(my_invdt, val);
+    }
+  }
+
+  if (health)
+    atomicOr(&s_health, health);
+  if (a.invdt_out)
+  {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+      my_invdt = fmax(my_invdt, __shfl_xor_sync(0xffffffffu, my_invdt, off));
+    if ((tid & 31) == 0)
+      s_red[tid >> 5] = my_invdt;
+  }
+  __syncthreads();
+  if (tid == 0)
+  {
+    if (a.invdt_out)
+    {
+      double m = s_red[0];
+      for (int w = 1; w < NT / 32; ++w)
+        m = fmax(m, s_red[w]);
+      atomic_max_pos_double(&a.invdt_out[myprob], m);
+    }
+    if (s_health)
+      atomicOr(a.health, s_health);
+  }
+}
+
+} // namespace gmhd

@@ -1,0 +1,756 @@
+// C ABI of the GB300 MHD stage (declared in include/gmhd.h): context, mesh tables, the step,
+// the CFL reduction, the outside-block fill and a graph-captured multi-step driver.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/gmhd.h"
+#include "launch.cuh"
+
+namespace gmhd
+{
+int launch_inv_dt(const double * U, const double * B, const int32_t * level, const int32_t * problem,
+                  int n_owned, int dim, int bx, int by, int bz, int64_t ncell, int64_t nfx, int64_t nfy,
+                  int64_t nface, double gamma0, double smallr, double smallp, double scaling_factor,
+                  unsigned long long * invdt, cudaStream_t stream);
+} // namespace gmhd
+
+struct gmhd_ctx
+{
+  gmhd_params p;
+  double      smallp;
+  int         device;
+  // mesh
+  bool    has_mesh = false;
+  int     dim = 0, bx = 0, by = 0, bz = 0, n_blocks = 0, n_owned = 0, n_problems = 1, n_outside = 0;
+  int64_t ncell = 0, nfx = 0, nfy = 0, nfz = 0, nface = 0;
+  int     bc[6] = {0, 0, 0, 0, 0, 0};
+  int32_t *d_neighbor = nullptr, *d_level = nullptr, *d_problem = nullptr;
+  int32_t *d_out_src = nullptr, *d_out_normal = nullptr;
+  // scratch
+  unsigned long long * d_invdt = nullptr; // [3][n_problems]
+  double *             d_dt = nullptr;    // [n_problems]
+  double *             d_t = nullptr;     // [n_problems]
+  double *             d_tend = nullptr;  // [n_problems]
+  int32_t *            d_counter = nullptr;
+  unsigned int *       d_health = nullptr;
+  double *             d_dtlog = nullptr;
+  int64_t              dtlog_cap = 0;
+  // host-variant staging
+  double *d_U = nullptr, *d_U2 = nullptr, *d_B = nullptr, *d_B2 = nullptr;
+  // own stream for graph capture when the caller passes the legacy stream
+  cudaStream_t own_stream = nullptr;
+  // cached graph of two steps
+  cudaGraphExec_t graph_exec = nullptr;
+  const void *    graph_key[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  int             mesh_version = 0, graph_mesh_version = -1;
+  uint64_t        bytes = 0;
+  int             last_cuda = 0;
+};
+
+namespace
+{
+int
+cuda_fail(gmhd_ctx * c, cudaError_t e)
+{
+  if (e == cudaSuccess)
+    return GMHD_OK;
+  c->last_cuda = (int)e;
+  return GMHD_ERR_CUDA;
+}
+
+#define GMHD_CUDA(call)                                                                           \
+  do                                                                                              \
+  {                                                                                               \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess)                                                                        \
+      return cuda_fail(ctx, e_);                                                                  \
+  } while (0)
+
+template <typename T>
+int
+dalloc(gmhd_ctx * ctx, T ** ptr, size_t count)
+{
+  if (*ptr)
+  {
+    cudaFree(*ptr);
+    *ptr = nullptr;
+  }
+  if (count == 0)
+    return GMHD_OK;
+  GMHD_CUDA(cudaMalloc((void **)ptr, count * sizeof(T)));
+  ctx->bytes += count * sizeof(T);
+  return GMHD_OK;
+}
+
+void
+dfree(void * p)
+{
+  if (p)
+    cudaFree(p);
+}
+
+void
+free_mesh(gmhd_ctx * c)
+{
+  dfree(c->d_neighbor);
+  dfree(c->d_level);
+  dfree(c->d_problem);
+  dfree(c->d_out_src);
+  dfree(c->d_out_normal);
+  dfree(c->d_invdt);
+  dfree(c->d_dt);
+  dfree(c->d_t);
+  dfree(c->d_tend);
+  dfree(c->d_counter);
+  dfree(c->d_dtlog);
+  dfree(c->d_U);
+  dfree(c->d_U2);
+  dfree(c->d_B);
+  dfree(c->d_B2);
+  c->d_neighbor = c->d_level = c->d_problem = c->d_out_src = c->d_out_normal = nullptr;
+  c->d_invdt = nullptr;
+  c->d_dt = c->d_t = c->d_tend = c->d_dtlog = nullptr;
+  c->d_counter = nullptr;
+  c->d_U = c->d_U2 = c->d_B = c->d_B2 = nullptr;
+  c->dtlog_cap = 0;
+  c->bytes = sizeof(unsigned int);
+  if (c->graph_exec)
+  {
+    cudaGraphExecDestroy(c->graph_exec);
+    c->graph_exec = nullptr;
+  }
+  c->has_mesh = false;
+}
+
+gmhd::StepArgs
+make_args(const gmhd_ctx * c, const double * U, double * U2, const double * B, double * B2)
+{
+  gmhd::StepArgs a;
+  std::memset(&a, 0, sizeof a);
+  a.U = U;
+  a.U2 = U2;
+  a.B = B;
+  a.B2 = B2;
+  a.neighbor = c->d_neighbor;
+  a.level = c->d_level;
+  a.problem = c->d_problem;
+  a.n_owned = c->n_owned;
+  a.bx = c->bx;
+  a.by = c->by;
+  a.bz = c->bz;
+  a.ncell = c->ncell;
+  a.nfx = c->nfx;
+  a.nfy = c->nfy;
+  a.nface = c->nface;
+  a.gamma0 = c->p.gamma0;
+  a.smallr = c->p.smallr;
+  a.smallc = c->p.smallc;
+  a.smallp = c->smallp;
+  a.slope_type = c->p.slope_type;
+  a.scaling_factor = c->p.scaling_factor;
+  a.cfl = c->p.cfl;
+  a.riemann = c->p.riemann;
+  a.health = c->d_health;
+  return a;
+}
+
+int
+launch_step(gmhd_ctx * ctx, const gmhd::StepArgs & a, cudaStream_t s)
+{
+  const int rc = ctx->p.precision == GMHD_PRECISION_MIXED ? gmhd::launch_step_mixed(a, ctx->dim, s)
+                                                          : gmhd::launch_step_fp64(a, ctx->dim, s);
+  if (rc == -1)
+    return GMHD_ERR_ARGUMENT;
+  if (rc != 0)
+    return cuda_fail(ctx, (cudaError_t)rc);
+  return GMHD_OK;
+}
+
+bool
+overlaps(const void * a, size_t na, const void * b, size_t nb)
+{
+  const char * pa = (const char *)a;
+  const char * pb = (const char *)b;
+  return pa < pb + nb && pb < pa + na;
+}
+
+// ---- outside-block fill (border_conditions/FillOutside.cpp:97-395) ---------------------------
+struct FillArgs
+{
+  double *        U;
+  double *        B;
+  const int32_t * src;
+  const int32_t * normal;
+  int             n_owned, n_outside, dim, bx, by, bz;
+  int64_t         ncell, nfx, nfy, nfz, nface;
+  int             bc[6];
+};
+
+__global__ void
+fill_outside_hydro_kernel(FillArgs a)
+{
+  const int64_t total = (int64_t)a.n_outside * a.ncell;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x)
+  {
+    const int     o = (int)(g / a.ncell);
+    const int64_t c = g - (int64_t)o * a.ncell;
+    const int     out_blk = a.n_owned + o;
+    const int     in_blk = a.src[o];
+    int           co[3] = {(int)(c % a.bx), (int)((c / a.bx) % a.by), (int)(c / ((int64_t)a.bx * a.by))};
+    const int     bs[3] = {a.bx, a.by, a.bz};
+    for (int face = 0; face < 2 * a.dim; ++face)
+    {
+      const int d = face / 2;
+      const int nrm = a.normal[3 * o + d];
+      // the inside block touches the domain border of this face and the outside block lies across it
+      const bool applies = (face % 2 == 0) ? (nrm > 0) : (nrm < 0);
+      if (!applies)
+        continue;
+      int ci[3] = {co[0], co[1], co[2]};
+      if (a.bc[face] == GMHD_BC_ZERO_GRADIENT)
+        ci[d] = (face % 2 == 0) ? 0 : bs[d] - 1;
+      else if (a.bc[face] == GMHD_BC_WALL)
+        ci[d] = bs[d] - 1 - co[d];
+      else
+        continue;
+      const int64_t cin = ci[0] + (int64_t)a.bx * (ci[1] + (int64_t)a.by * ci[2]);
+      for (int v = 0; v < 5; ++v)
+        a.U[((int64_t)out_blk * 5 + v) * a.ncell + c] = a.U[((int64_t)in_blk * 5 + v) * a.ncell + cin];
+      if (a.bc[face] == GMHD_BC_WALL)
+        a.U[((int64_t)out_blk * 5 + 2 + d) * a.ncell + c] *= -1;
+    }
+  }
+}
+
+__global__ void
+fill_outside_faces_kernel(FillArgs a)
+{
+  const int64_t total = (int64_t)a.n_outside * a.nface;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x)
+  {
+    const int     o = (int)(g / a.nface);
+    const int64_t f = g - (int64_t)o * a.nface;
+    const int     out_blk = a.n_owned + o;
+    const int     in_blk = a.src[o];
+    // unravel (component, i, j, k) of the face
+    int  comp;
+    int64_t r;
+    int  nx, ny;
+    if (f < a.nfx)
+    {
+      comp = 0; r = f; nx = a.bx + 1; ny = a.by;
+    }
+    else if (f < a.nfx + a.nfy)
+    {
+      comp = 1; r = f - a.nfx; nx = a.bx; ny = a.by + 1;
+    }
+    else
+    {
+      comp = 2; r = f - a.nfx - a.nfy; nx = a.bx; ny = a.by;
+    }
+    int       idx[3] = {(int)(r % nx), (int)((r / nx) % ny), (int)(r / ((int64_t)nx * ny))};
+    const int fsz[3] = {nx, ny, comp == 2 && a.dim == 3 ? a.bz + 1 : a.bz};
+    for (int d = 0; d < a.dim; ++d)
+    {
+      const int nrm = a.normal[3 * o + d];
+      if (nrm > 0 && a.bc[2 * d] == GMHD_BC_ZERO_GRADIENT)
+        idx[d] = 0;
+      else if (nrm < 0 && a.bc[2 * d + 1] == GMHD_BC_ZERO_GRADIENT)
+        idx[d] = fsz[d] - 1;
+      // WALL: the reference leaves the index unchanged (a TODO), i.e. copies the same face
+    }
+    const int64_t fin = idx[0] + (int64_t)nx * (idx[1] + (int64_t)ny * idx[2]);
+    const int64_t base = comp == 0 ? 0 : (comp == 1 ? a.nfx : a.nfx + a.nfy);
+    a.B[(int64_t)out_blk * a.nface + f] = a.B[(int64_t)in_blk * a.nface + base + fin];
+  }
+}
+
+// ---- device-side time control of gmhd_advance -----------------------------------------------
+__global__ void
+advance_time_kernel(const unsigned long long * invdt, double cfl, double * t, const double * t_end, double * dt_cur,
+                    double * dt_log, int32_t * counter, int np, int64_t log_cap)
+{
+  const int n = *counter;
+  for (int p = threadIdx.x; p < np; p += blockDim.x)
+  {
+    double dt = cfl / __longlong_as_double((long long)invdt[p]);
+    if (t_end)
+    {
+      const double rem = t_end[p] - t[p];
+      if (dt > rem)
+        dt = rem;
+      if (!(rem > 0.0))
+        dt = 0.0;
+    }
+    dt_cur[p] = dt;
+    t[p] += dt;
+    if ((int64_t)(n + 1) * np <= log_cap)
+      dt_log[(int64_t)n * np + p] = dt;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    *counter = n + 1;
+}
+
+int
+enqueue_fill(gmhd_ctx * ctx, double * U, double * B, cudaStream_t s)
+{
+  if (ctx->n_outside == 0)
+    return GMHD_OK;
+  FillArgs f;
+  f.U = U;
+  f.B = B;
+  f.src = ctx->d_out_src;
+  f.normal = ctx->d_out_normal;
+  f.n_owned = ctx->n_owned;
+  f.n_outside = ctx->n_outside;
+  f.dim = ctx->dim;
+  f.bx = ctx->bx;
+  f.by = ctx->by;
+  f.bz = ctx->bz;
+  f.ncell = ctx->ncell;
+  f.nfx = ctx->nfx;
+  f.nfy = ctx->nfy;
+  f.nfz = ctx->nfz;
+  f.nface = ctx->nface;
+  for (int i = 0; i < 6; ++i)
+    f.bc[i] = ctx->bc[i];
+  const int64_t nh = (int64_t)ctx->n_outside * ctx->ncell;
+  const int64_t nf = (int64_t)ctx->n_outside * ctx->nface;
+  const int     gh = (int)((nh + 255) / 256 < 65535 ? (nh + 255) / 256 : 65535);
+  const int     gf = (int)((nf + 255) / 256 < 65535 ? (nf + 255) / 256 : 65535);
+  // hydro and faces touch disjoint arrays: one after the other on the same stream
+  fill_outside_hydro_kernel<<<gh, 256, 0, s>>>(f);
+  fill_outside_faces_kernel<<<gf, 256, 0, s>>>(f);
+  GMHD_CUDA(cudaGetLastError());
+  return GMHD_OK;
+}
+
+int
+enqueue_inv_dt(gmhd_ctx * ctx, const double * U, const double * B, unsigned long long * slot, cudaStream_t s)
+{
+  GMHD_CUDA(cudaMemsetAsync(slot, 0, sizeof(unsigned long long) * ctx->n_problems, s));
+  const int rc = gmhd::launch_inv_dt(U, B, ctx->d_level, ctx->d_problem, ctx->n_owned, ctx->dim, ctx->bx, ctx->by,
+                                     ctx->bz, ctx->ncell, ctx->nfx, ctx->nfy, ctx->nface, ctx->p.gamma0,
+                                     ctx->p.smallr, ctx->smallp, ctx->p.scaling_factor, slot, s);
+  if (rc != 0)
+    return cuda_fail(ctx, (cudaError_t)rc);
+  return GMHD_OK;
+}
+
+// one solver iteration of gmhd_advance: time control, outside fill, fused step + CFL
+int
+enqueue_iteration(gmhd_ctx * ctx, const double * Uc, double * Un, const double * Bc, double * Bn, int slot_in,
+                  cudaStream_t s, bool has_tend)
+{
+  const int np = ctx->n_problems;
+  advance_time_kernel<<<1, 256, 0, s>>>(ctx->d_invdt + (size_t)slot_in * np, ctx->p.cfl, ctx->d_t,
+                                        has_tend ? ctx->d_tend : nullptr, ctx->d_dt, ctx->d_dtlog, ctx->d_counter,
+                                        np, ctx->dtlog_cap);
+  GMHD_CUDA(cudaGetLastError());
+  unsigned long long * out = ctx->d_invdt + (size_t)(1 - slot_in) * np;
+  GMHD_CUDA(cudaMemsetAsync(out, 0, sizeof(unsigned long long) * np, s));
+  int rc = enqueue_fill(ctx, const_cast<double *>(Uc), const_cast<double *>(Bc), s);
+  if (rc)
+    return rc;
+  gmhd::StepArgs a = make_args(ctx, Uc, Un, Bc, Bn);
+  a.dt_dev = ctx->d_dt;
+  a.invdt_out = out;
+  return launch_step(ctx, a, s);
+}
+
+int
+check_health(gmhd_ctx * ctx, cudaStream_t s, unsigned int * flags_out)
+{
+  unsigned int h = 0;
+  GMHD_CUDA(cudaMemcpyAsync(&h, ctx->d_health, sizeof h, cudaMemcpyDeviceToHost, s));
+  GMHD_CUDA(cudaMemsetAsync(ctx->d_health, 0, sizeof(unsigned int), s));
+  GMHD_CUDA(cudaStreamSynchronize(s));
+  if (flags_out)
+    *flags_out = h;
+  return GMHD_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+gmhd_ctx *
+gmhd_create(const gmhd_params * params)
+{
+  if (!params || !(params->gamma0 > 1.0) || !(params->cfl > 0.0) || !(params->scaling_factor > 0.0))
+    return nullptr;
+  if (params->riemann < GMHD_RIEMANN_LLF || params->riemann > GMHD_RIEMANN_HLLD)
+    return nullptr;
+  if (params->precision != GMHD_PRECISION_FP64 && params->precision != GMHD_PRECISION_MIXED)
+    return nullptr;
+  gmhd_ctx * c = new (std::nothrow) gmhd_ctx();
+  if (!c)
+    return nullptr;
+  c->p = *params;
+  c->smallp = params->smallc * params->smallc / params->gamma0;
+  if (cudaGetDevice(&c->device) != cudaSuccess || cudaMalloc((void **)&c->d_health, sizeof(unsigned int)) != cudaSuccess ||
+      cudaMemset(c->d_health, 0, sizeof(unsigned int)) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+  {
+    if (c->d_health)
+      cudaFree(c->d_health);
+    delete c;
+    return nullptr;
+  }
+  c->bytes = sizeof(unsigned int);
+  if (gmhd::prepare_fp64() != 0 || gmhd::prepare_mixed() != 0)
+  {
+    cudaFree(c->d_health);
+    cudaStreamDestroy(c->own_stream);
+    delete c;
+    return nullptr;
+  }
+  return c;
+}
+
+void
+gmhd_destroy(gmhd_ctx * ctx)
+{
+  if (!ctx)
+    return;
+  free_mesh(ctx);
+  dfree(ctx->d_health);
+  if (ctx->own_stream)
+    cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+}
+
+int
+gmhd_set_mesh(gmhd_ctx * ctx, const gmhd_mesh * m)
+{
+  if (!ctx || !m || !m->level || !m->neighbor)
+    return GMHD_ERR_ARGUMENT;
+  if ((m->dim != 2 && m->dim != 3) || m->bx < 4 || m->by < 4 || (m->dim == 3 && m->bz < 4) ||
+      (m->dim == 2 && m->bz != 1))
+    return GMHD_ERR_ARGUMENT;
+  if (m->n_owned < 0 || m->n_blocks < m->n_owned)
+    return GMHD_ERR_ARGUMENT;
+  const int n_out = m->n_blocks - m->n_owned;
+  if (n_out > 0 && (!m->outside_src || !m->outside_normal))
+    return GMHD_ERR_ARGUMENT;
+  const int np = m->problem ? m->n_problems : 1;
+  if (np < 1)
+    return GMHD_ERR_ARGUMENT;
+  // validate tables on the host: indices in range, one level (uniform mesh) per problem
+  for (int64_t i = 0; i < (int64_t)m->n_blocks * 27; ++i)
+    if (m->neighbor[i] < -1 || m->neighbor[i] >= m->n_blocks)
+      return GMHD_ERR_MESH;
+  for (int b = 0; b < m->n_blocks; ++b)
+  {
+    if (m->level[b] < 0 || m->level[b] > 30)
+      return GMHD_ERR_MESH;
+    if (m->problem && (m->problem[b] < 0 || m->problem[b] >= np))
+      return GMHD_ERR_MESH;
+  }
+  for (int b = 0; b < m->n_owned; ++b)
+    for (int s = 0; s < 27; ++s)
+    {
+      const int nb = m->neighbor[(int64_t)b * 27 + s];
+      if (nb >= 0 && m->level[nb] != m->level[b])
+        return GMHD_ERR_MESH; // coarse/fine interfaces are not supported by this path
+      if (nb >= 0 && m->problem && m->problem[nb] != m->problem[b])
+        return GMHD_ERR_MESH;
+    }
+  for (int o = 0; o < n_out; ++o)
+    if (m->outside_src[o] < 0 || m->outside_src[o] >= m->n_owned)
+      return GMHD_ERR_MESH;
+
+  free_mesh(ctx);
+  ctx->dim = m->dim;
+  ctx->bx = m->bx;
+  ctx->by = m->by;
+  ctx->bz = m->dim == 3 ? m->bz : 1;
+  ctx->n_blocks = m->n_blocks;
+  ctx->n_owned = m->n_owned;
+  ctx->n_outside = n_out;
+  ctx->n_problems = np;
+  ctx->ncell = (int64_t)ctx->bx * ctx->by * ctx->bz;
+  ctx->nfx = (int64_t)(ctx->bx + 1) * ctx->by * ctx->bz;
+  ctx->nfy = (int64_t)ctx->bx * (ctx->by + 1) * ctx->bz;
+  ctx->nfz = ctx->dim == 3 ? (int64_t)ctx->bx * ctx->by * (ctx->bz + 1) : ctx->ncell;
+  ctx->nface = ctx->nfx + ctx->nfy + ctx->nfz;
+  for (int i = 0; i < 6; ++i)
+    ctx->bc[i] = m->bc[i];
+  int rc;
+  if ((rc = dalloc(ctx, &ctx->d_neighbor, (size_t)m->n_blocks * 27)) || (rc = dalloc(ctx, &ctx->d_level, (size_t)m->n_blocks)) ||
+      (rc = dalloc(ctx, &ctx->d_invdt, (size_t)3 * np)) || (rc = dalloc(ctx, &ctx->d_dt, (size_t)np)) ||
+      (rc = dalloc(ctx, &ctx->d_t, (size_t)np)) || (rc = dalloc(ctx, &ctx->d_tend, (size_t)np)) ||
+      (rc = dalloc(ctx, &ctx->d_counter, 1)))
+    return rc;
+  GMHD_CUDA(cudaMemcpy(ctx->d_neighbor, m->neighbor, sizeof(int32_t) * m->n_blocks * 27, cudaMemcpyHostToDevice));
+  GMHD_CUDA(cudaMemcpy(ctx->d_level, m->level, sizeof(int32_t) * m->n_blocks, cudaMemcpyHostToDevice));
+  if (m->problem)
+  {
+    if ((rc = dalloc(ctx, &ctx->d_problem, (size_t)m->n_blocks)))
+      return rc;
+    GMHD_CUDA(cudaMemcpy(ctx->d_problem, m->problem, sizeof(int32_t) * m->n_blocks, cudaMemcpyHostToDevice));
+  }
+  if (n_out > 0)
+  {
+    if ((rc = dalloc(ctx, &ctx->d_out_src, (size_t)n_out)) || (rc = dalloc(ctx, &ctx->d_out_normal, (size_t)3 * n_out)))
+      return rc;
+    GMHD_CUDA(cudaMemcpy(ctx->d_out_src, m->outside_src, sizeof(int32_t) * n_out, cudaMemcpyHostToDevice));
+    GMHD_CUDA(cudaMemcpy(ctx->d_out_normal, m->outside_normal, sizeof(int32_t) * 3 * n_out, cudaMemcpyHostToDevice));
+  }
+  ctx->has_mesh = true;
+  ctx->mesh_version++;
+  return GMHD_OK;
+}
+
+uint64_t
+gmhd_mem_bytes(const gmhd_ctx * ctx)
+{
+  return ctx ? ctx->bytes : 0;
+}
+
+int
+gmhd_step(gmhd_ctx * ctx, const double * U, double * U2, const double * B, double * B2, double dt, void * stream)
+{
+  if (!ctx || !U || !U2 || !B || !B2)
+    return GMHD_ERR_ARGUMENT;
+  if (!ctx->has_mesh)
+    return GMHD_ERR_MESH;
+  if (!(dt >= 0.0))
+    return GMHD_ERR_ARGUMENT;
+  const size_t nu = sizeof(double) * (size_t)ctx->n_blocks * 5 * ctx->ncell;
+  const size_t nb = sizeof(double) * (size_t)ctx->n_blocks * ctx->nface;
+  if (overlaps(U, nu, U2, nu) || overlaps(B, nb, B2, nb) || overlaps(U2, nu, B, nb) || overlaps(B2, nb, U, nu))
+    return GMHD_ERR_ALIAS;
+  gmhd::StepArgs a = make_args(ctx, U, U2, B, B2);
+  a.dt = dt;
+  return launch_step(ctx, a, (cudaStream_t)stream);
+}
+
+int
+gmhd_inv_dt(gmhd_ctx * ctx, const double * U, const double * B, double * inv_dt, void * stream)
+{
+  if (!ctx || !U || !B || !inv_dt)
+    return GMHD_ERR_ARGUMENT;
+  if (!ctx->has_mesh)
+    return GMHD_ERR_MESH;
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned long long * slot = ctx->d_invdt + (size_t)2 * ctx->n_problems;
+  int                  rc = enqueue_inv_dt(ctx, U, B, slot, s);
+  if (rc)
+    return rc;
+  std::vector<unsigned long long> h(ctx->n_problems);
+  GMHD_CUDA(cudaMemcpyAsync(h.data(), slot, sizeof(unsigned long long) * ctx->n_problems, cudaMemcpyDeviceToHost, s));
+  GMHD_CUDA(cudaStreamSynchronize(s));
+  for (int p = 0; p < ctx->n_problems; ++p)
+  {
+    double v;
+    std::memcpy(&v, &h[p], sizeof v);
+    inv_dt[p] = v;
+  }
+  return GMHD_OK;
+}
+
+int
+gmhd_fill_outside(gmhd_ctx * ctx, double * U, double * B, void * stream)
+{
+  if (!ctx || !U || !B)
+    return GMHD_ERR_ARGUMENT;
+  if (!ctx->has_mesh)
+    return GMHD_ERR_MESH;
+  return enqueue_fill(ctx, U, B, (cudaStream_t)stream);
+}
+
+int
+gmhd_advance(gmhd_ctx * ctx, double * U, double * U2, double * B, double * B2, int32_t nsteps, double * t,
+             const double * t_end, double * dt_log, int32_t use_graph, void * stream)
+{
+  if (!ctx || !U || !U2 || !B || !B2 || nsteps < 0)
+    return GMHD_ERR_ARGUMENT;
+  if (!ctx->has_mesh)
+    return GMHD_ERR_MESH;
+  const size_t nu = sizeof(double) * (size_t)ctx->n_blocks * 5 * ctx->ncell;
+  const size_t nb = sizeof(double) * (size_t)ctx->n_blocks * ctx->nface;
+  if (overlaps(U, nu, U2, nu) || overlaps(B, nb, B2, nb) || overlaps(U2, nu, B, nb) || overlaps(B2, nb, U, nu))
+    return GMHD_ERR_ALIAS;
+  if (nsteps == 0)
+    return GMHD_OK;
+  const int np = ctx->n_problems;
+  // work on a capturable stream, ordered after / before the caller's stream
+  cudaStream_t caller = (cudaStream_t)stream;
+  cudaStream_t s = caller ? caller : ctx->own_stream;
+  cudaEvent_t  ev = nullptr;
+  if (!caller)
+  {
+    GMHD_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    GMHD_CUDA(cudaEventRecord(ev, 0));
+    GMHD_CUDA(cudaStreamWaitEvent(s, ev, 0));
+  }
+  int rc;
+  if ((int64_t)nsteps * np > ctx->dtlog_cap)
+  {
+    if ((rc = dalloc(ctx, &ctx->d_dtlog, (size_t)nsteps * np)))
+      return rc;
+    ctx->dtlog_cap = (int64_t)nsteps * np;
+    if (ctx->graph_exec)
+    {
+      cudaGraphExecDestroy(ctx->graph_exec);
+      ctx->graph_exec = nullptr;
+    }
+  }
+  std::vector<double> zeros(np, 0.0);
+  GMHD_CUDA(cudaMemcpyAsync(ctx->d_t, t ? t : zeros.data(), sizeof(double) * np, cudaMemcpyHostToDevice, s));
+  if (t_end)
+    GMHD_CUDA(cudaMemcpyAsync(ctx->d_tend, t_end, sizeof(double) * np, cudaMemcpyHostToDevice, s));
+  GMHD_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(int32_t), s));
+  // CFL of the initial state into slot 0 (SolverGodunovMHD ctor: compute_dt, .cpp:180)
+  if ((rc = enqueue_inv_dt(ctx, U, B, ctx->d_invdt, s)))
+    return rc;
+  const bool has_tend = t_end != nullptr;
+  int        done = 0;
+  if (use_graph && nsteps >= 2)
+  {
+    const void * key[5] = {U, U2, B, B2, (const void *)(intptr_t)(has_tend ? 1 : 0)};
+    bool         same = ctx->graph_exec && ctx->graph_mesh_version == ctx->mesh_version;
+    for (int i = 0; i < 5; ++i)
+      same = same && key[i] == ctx->graph_key[i];
+    if (!same)
+    {
+      if (ctx->graph_exec)
+      {
+        cudaGraphExecDestroy(ctx->graph_exec);
+        ctx->graph_exec = nullptr;
+      }
+      cudaGraph_t g = nullptr;
+      GMHD_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      int rc1 = enqueue_iteration(ctx, U, U2, B, B2, 0, s, has_tend);
+      int rc2 = rc1 ? rc1 : enqueue_iteration(ctx, U2, U, B2, B, 1, s, has_tend);
+      cudaError_t ec = cudaStreamEndCapture(s, &g);
+      if (rc2)
+      {
+        if (g)
+          cudaGraphDestroy(g);
+        return rc2;
+      }
+      GMHD_CUDA(ec);
+      cudaError_t ei = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
+      cudaGraphDestroy(g);
+      GMHD_CUDA(ei);
+      for (int i = 0; i < 5; ++i)
+        ctx->graph_key[i] = key[i];
+      ctx->graph_mesh_version = ctx->mesh_version;
+    }
+    for (; done + 2 <= nsteps; done += 2)
+      GMHD_CUDA(cudaGraphLaunch(ctx->graph_exec, s));
+  }
+  for (; done < nsteps; ++done)
+  {
+    const bool even = (done % 2) == 0;
+    rc = even ? enqueue_iteration(ctx, U, U2, B, B2, 0, s, has_tend) : enqueue_iteration(ctx, U2, U, B2, B, 1, s, has_tend);
+    if (rc)
+      return rc;
+  }
+  if (nsteps % 2)
+  {
+    GMHD_CUDA(cudaMemcpyAsync(U, U2, nu, cudaMemcpyDeviceToDevice, s));
+    GMHD_CUDA(cudaMemcpyAsync(B, B2, nb, cudaMemcpyDeviceToDevice, s));
+  }
+  if (t)
+    GMHD_CUDA(cudaMemcpyAsync(t, ctx->d_t, sizeof(double) * np, cudaMemcpyDeviceToHost, s));
+  if (dt_log)
+    GMHD_CUDA(cudaMemcpyAsync(dt_log, ctx->d_dtlog, sizeof(double) * nsteps * np, cudaMemcpyDeviceToHost, s));
+  unsigned int flags = 0;
+  if ((rc = check_health(ctx, s, &flags)))
+    return rc;
+  if (ev)
+  {
+    cudaEventRecord(ev, s);
+    cudaStreamWaitEvent(0, ev, 0);
+    cudaEventDestroy(ev);
+  }
+  if (flags & (GMHD_HEALTH_BAD_DENSITY | GMHD_HEALTH_NONFINITE | GMHD_HEALTH_MISSING_NEIGHBOR | GMHD_HEALTH_LEVEL_JUMP))
+    return GMHD_ERR_HEALTH;
+  return GMHD_OK;
+}
+
+int
+gmhd_step_host(gmhd_ctx * ctx, const double * U, double * U2, const double * B, double * B2, double dt, void * stream)
+{
+  if (!ctx || !U || !U2 || !B || !B2)
+    return GMHD_ERR_ARGUMENT;
+  if (!ctx->has_mesh)
+    return GMHD_ERR_MESH;
+  const size_t nu = (size_t)ctx->n_blocks * 5 * ctx->ncell;
+  const size_t nb = (size_t)ctx->n_blocks * ctx->nface;
+  int          rc;
+  if (!ctx->d_U)
+  {
+    if ((rc = dalloc(ctx, &ctx->d_U, nu)) || (rc = dalloc(ctx, &ctx->d_U2, nu)) || (rc = dalloc(ctx, &ctx->d_B, nb)) ||
+        (rc = dalloc(ctx, &ctx->d_B2, nb)))
+      return rc;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  GMHD_CUDA(cudaMemcpyAsync(ctx->d_U, U, nu * sizeof(double), cudaMemcpyHostToDevice, s));
+  GMHD_CUDA(cudaMemcpyAsync(ctx->d_B, B, nb * sizeof(double), cudaMemcpyHostToDevice, s));
+  if ((rc = gmhd_step(ctx, ctx->d_U, ctx->d_U2, ctx->d_B, ctx->d_B2, dt, stream)))
+    return rc;
+  const size_t nu_own = (size_t)ctx->n_owned * 5 * ctx->ncell;
+  const size_t nb_own = (size_t)ctx->n_owned * ctx->nface;
+  GMHD_CUDA(cudaMemcpyAsync(U2, ctx->d_U2, nu_own * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GMHD_CUDA(cudaMemcpyAsync(B2, ctx->d_B2, nb_own * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GMHD_CUDA(cudaStreamSynchronize(s));
+  return GMHD_OK;
+}
+
+int
+gmhd_last_status(gmhd_ctx * ctx, uint32_t * flags)
+{
+  if (!ctx || !flags)
+    return GMHD_ERR_ARGUMENT;
+  unsigned int h = 0;
+  const int    rc = check_health(ctx, ctx->own_stream, &h);
+  *flags = h;
+  return rc;
+}
+
+int
+gmhd_last_cuda_error(const gmhd_ctx * ctx)
+{
+  return ctx ? ctx->last_cuda : 0;
+}
+
+const char *
+gmhd_error_string(int status)
+{
+  switch (status)
+  {
+    case GMHD_OK: return "ok";
+    case GMHD_ERR_ARGUMENT: return "invalid argument";
+    case GMHD_ERR_MESH: return "mesh not set or not supported";
+    case GMHD_ERR_CUDA: return "CUDA error";
+    case GMHD_ERR_ALIAS: return "output aliases an input";
+    case GMHD_ERR_HEALTH: return "non-physical state produced";
+    case GMHD_ERR_TOO_LARGE: return "request exceeds a fixed capacity";
+    default: return "unknown status";
+  }
+}
+
+int
+gmhd_layout_check(const gmhd_mesh * m, int64_t u_var_stride, int64_t u_block_stride, int64_t b_block_stride)
+{
+  if (!m)
+    return GMHD_ERR_ARGUMENT;
+  const int64_t bz = m->dim == 3 ? m->bz : 1;
+  const int64_t ncell = (int64_t)m->bx * m->by * bz;
+  const int64_t nfz = m->dim == 3 ? (int64_t)m->bx * m->by * (bz + 1) : ncell;
+  const int64_t nface = (int64_t)(m->bx + 1) * m->by * bz + (int64_t)m->bx * (m->by + 1) * bz + nfz;
+  if (u_var_stride != ncell || u_block_stride != 5 * ncell || b_block_stride != nface)
+    return GMHD_ERR_ARGUMENT;
+  return GMHD_OK;
+}
+
+} // extern "C"

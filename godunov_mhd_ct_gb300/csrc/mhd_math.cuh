@@ -1,0 +1,646 @@
+// Per-cell MHD math on the device, templated on the compute type R (double or float).
+//
+// Same operand order as godunov_mhd_ct's models/mhd_utils.h and models/RiemannSolvers_MHD.h, so
+// that the double instantiation, compiled with --fmad=false, gives the same bits as an FP64 host
+// build of the reference formulas. Citations are to those files.
+#pragma once
+
+#include <cstdint>
+
+namespace gmhd
+{
+
+// Variable slots (models/MHD.h:35-62): ID, IP, IU, IV, IW, IA, IB, IC.
+enum : int
+{
+  ID = 0,
+  IP = 1,
+  IU = 2,
+  IV = 3,
+  IW = 4,
+  IA = 5,
+  IB = 6,
+  IC = 7
+};
+
+// Riemann solver ids (models/riemann_solver_types.h:26-37).
+enum : int
+{
+  RS_LLF = 2,
+  RS_HLL = 3,
+  RS_HLLC = 4,
+  RS_HLLD = 5
+};
+
+template <typename R>
+struct Phys
+{
+  R   gamma0;
+  R   smallr;
+  R   smallc;
+  R   smallp;
+  R   slope_type;
+  int riemann;
+};
+
+template <typename R>
+__device__ __forceinline__ R
+dsqrt(R x)
+{
+  return sqrt(x);
+}
+template <>
+__device__ __forceinline__ float
+dsqrt<float>(float x)
+{
+  return sqrtf(x);
+}
+
+template <typename R>
+__device__ __forceinline__ R
+rmax(R a, R b)
+{
+  return fmax(a, b);
+}
+template <>
+__device__ __forceinline__ float
+rmax<float>(float a, float b)
+{
+  return fmaxf(a, b);
+}
+template <typename R>
+__device__ __forceinline__ R
+rmin(R a, R b)
+{
+  return fmin(a, b);
+}
+template <>
+__device__ __forceinline__ float
+rmin<float>(float a, float b)
+{
+  return fminf(a, b);
+}
+template <typename R>
+__device__ __forceinline__ R
+rabs(R a)
+{
+  return fabs(a);
+}
+template <>
+__device__ __forceinline__ float
+rabs<float>(float a)
+{
+  return fabsf(a);
+}
+template <typename R>
+__device__ __forceinline__ R
+rcopysign(R a, R b)
+{
+  return copysign(a, b);
+}
+template <>
+__device__ __forceinline__ float
+rcopysign<float>(float a, float b)
+{
+  return copysignf(a, b);
+}
+
+// find_speed_fast<dir> (models/mhd_utils.h:93-122)
+template <typename R>
+__device__ __forceinline__ R
+speed_fast(const R * q, int dir, const Phys<R> & s)
+{
+  const R d = q[ID], p = q[IP], a = q[IA], b = q[IB], c = q[IC];
+  const R b2 = a * a + b * b + c * c;
+  const R c2 = s.gamma0 * p / d;
+  const R d2 = R(0.5) * (b2 / d + c2);
+  const R bn = dir == 0 ? a : (dir == 1 ? b : c);
+  return dsqrt<R>(d2 + dsqrt<R>(d2 * d2 - c2 * bn * bn / d));
+}
+
+// find_mhd_flux (models/mhd_utils.h:182-245), cIso == 0
+template <typename R>
+__device__ __forceinline__ void
+mhd_flux(const R * q, R * cv, R * ff, const Phys<R> & s)
+{
+  const R p = q[IP];
+  const R entho = R(1) / (s.gamma0 - R(1));
+  const R d = q[ID], u = q[IU], v = q[IV], w = q[IW], a = q[IA], b = q[IB], c = q[IC];
+  const R ecin = R(0.5) * (u * u + v * v + w * w) * d;
+  const R emag = R(0.5) * (a * a + b * b + c * c);
+  const R etot = p * entho + ecin + emag;
+  const R ptot = p + emag;
+  cv[ID] = d;
+  cv[IP] = etot;
+  cv[IU] = d * u;
+  cv[IV] = d * v;
+  cv[IW] = d * w;
+  cv[IA] = a;
+  cv[IB] = b;
+  cv[IC] = c;
+  ff[ID] = d * u;
+  ff[IP] = (etot + ptot) * u - a * (a * u + b * v + c * w);
+  ff[IU] = d * u * u - a * a + ptot;
+  ff[IV] = d * u * v - a * b;
+  ff[IW] = d * u * w - a * c;
+  ff[IA] = R(0);
+  ff[IB] = b * u - a * v;
+  ff[IC] = c * u - a * w;
+}
+
+// riemann_hll (models/RiemannSolvers_MHD.h:43-102)
+template <typename R>
+__device__ void
+riemann_hll(R * qL, R * qR, R * flux, const Phys<R> & s)
+{
+  const R bx_mean = R(0.5) * (qL[IA] + qR[IA]);
+  qL[IA] = bx_mean;
+  qR[IA] = bx_mean;
+  R uL[8], fL[8], uR[8], fR[8];
+  mhd_flux(qL, uL, fL, s);
+  mhd_flux(qR, uR, fR, s);
+  const R cfL = speed_fast(qL, 0, s);
+  const R cfR = speed_fast(qR, 0, s);
+  const R vL = qL[IU], vR = qR[IU];
+  const R sl = rmin<R>(rmin<R>(vL, vR) - rmax<R>(cfL, cfR), R(0));
+  const R sr = rmax<R>(rmax<R>(vL, vR) + rmax<R>(cfL, cfR), R(0));
+#pragma unroll
+  for (int n = 0; n < 8; ++n)
+    flux[n] = (sr * fL[n] - sl * fR[n] + sr * sl * (uR[n] - uL[n])) / (sr - sl);
+}
+
+// riemann_llf (models/RiemannSolvers_MHD.h:118-153)
+template <typename R>
+__device__ void
+riemann_llf(R * qL, R * qR, R * flux, const Phys<R> & s)
+{
+  const R bx_mean = R(0.5) * (qL[IA] + qR[IA]);
+  qL[IA] = bx_mean;
+  qR[IA] = bx_mean;
+  R uL[8], fL[8], uR[8], fR[8];
+  mhd_flux(qL, uL, fL, s);
+  mhd_flux(qR, uR, fR, s);
+#pragma unroll
+  for (int n = 0; n < 8; ++n)
+    flux[n] = (fL[n] + fR[n]) / R(2);
+  // x-direction info speed (models/mhd_utils.h:405-433)
+  R cinfo[2];
+  for (int side = 0; side < 2; ++side)
+  {
+    const R * q = side == 0 ? qL : qR;
+    const R   d = q[ID], p = q[IP], a = q[IA], b = q[IB], c = q[IC];
+    const R   b2 = a * a + b * b + c * c;
+    const R   c2 = s.gamma0 * p / d;
+    const R   d2 = R(0.5) * (b2 / d + c2);
+    const R   cf = dsqrt<R>(d2 + dsqrt<R>(d2 * d2 - c2 * a * a / d));
+    cinfo[side] = cf + rabs<R>(q[IU]);
+  }
+  const R vel_info = rmax<R>(cinfo[0], cinfo[1]);
+#pragma unroll
+  for (int n = 0; n < 8; ++n)
+    flux[n] -= vel_info * (uR[n] - uL[n]) / R(2);
+}
+
+// riemann_hllc (models/RiemannSolvers_MHD.h:165-286); components IA..IC are left at 0
+template <typename R>
+__device__ void
+riemann_hllc(const R * qL, const R * qR, R * flux, const Phys<R> & s)
+{
+  const R entho = R(1) / (s.gamma0 - R(1));
+  const R rl = rmax<R>(qL[ID], s.smallr);
+  const R pl = rmax<R>(qL[IP], rl * s.smallp);
+  const R ul = qL[IU];
+  R       ecinl = R(0.5) * rl * ul * ul;
+  ecinl += R(0.5) * rl * qL[IV] * qL[IV];
+  ecinl += R(0.5) * rl * qL[IW] * qL[IW];
+  const R etotl = pl * entho + ecinl;
+  const R ptotl = pl;
+  const R rr = rmax<R>(qR[ID], s.smallr);
+  const R pr = rmax<R>(qR[IP], rr * s.smallp);
+  const R ur = qR[IU];
+  R       ecinr = R(0.5) * rr * ur * ur;
+  ecinr += R(0.5) * rr * qR[IV] * qR[IV];
+  ecinr += R(0.5) * rr * qR[IW] * qR[IW];
+  const R etotr = pr * entho + ecinr;
+  const R ptotr = pr;
+  const R cfastl = dsqrt<R>(rmax<R>(s.gamma0 * pl / rl, s.smallc * s.smallc));
+  const R cfastr = dsqrt<R>(rmax<R>(s.gamma0 * pr / rr, s.smallc * s.smallc));
+  const R SL = rmin<R>(ul, ur) - rmax<R>(cfastl, cfastr);
+  const R SR = rmax<R>(ul, ur) + rmax<R>(cfastl, cfastr);
+  const R rcl = rl * (ul - SL);
+  const R rcr = rr * (SR - ur);
+  const R ustar = (rcr * ur + rcl * ul + (ptotl - ptotr)) / (rcr + rcl);
+  const R ptotstar = (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) / (rcr + rcl);
+  const R rstarl = rl * (SL - ul) / (SL - ustar);
+  const R etotstarl = ((SL - ul) * etotl - ptotl * ul + ptotstar * ustar) / (SL - ustar);
+  const R rstarr = rr * (SR - ur) / (SR - ustar);
+  const R etotstarr = ((SR - ur) * etotr - ptotr * ur + ptotstar * ustar) / (SR - ustar);
+  R       ro, uo, ptoto, etoto;
+  if (SL > R(0))
+  {
+    ro = rl; uo = ul; ptoto = ptotl; etoto = etotl;
+  }
+  else if (ustar > R(0))
+  {
+    ro = rstarl; uo = ustar; ptoto = ptotstar; etoto = etotstarl;
+  }
+  else if (SR > R(0))
+  {
+    ro = rstarr; uo = ustar; ptoto = ptotstar; etoto = etotstarr;
+  }
+  else
+  {
+    ro = rr; uo = ur; ptoto = ptotr; etoto = etotr;
+  }
+  flux[ID] = ro * uo;
+  flux[IU] = ro * uo * uo + ptoto;
+  flux[IP] = (etoto + ptoto) * uo;
+  flux[IV] = flux[ID] > R(0) ? flux[ID] * qL[IV] : flux[ID] * qR[IV];
+  flux[IW] = flux[ID] > R(0) ? flux[ID] * qL[IW] : flux[ID] * qR[IW];
+}
+
+// riemann_hlld (models/RiemannSolvers_MHD.h:311-551), Miyoshi & Kusano 2005
+template <typename R>
+__device__ void
+riemann_hlld(R * qL, R * qR, R * flux, const Phys<R> & s)
+{
+  const R entho = R(1) / (s.gamma0 - R(1));
+  const R a = R(0.5) * (qL[IA] + qR[IA]);
+  const R sgnm = (a >= 0) ? R(1) : R(-1);
+  qL[IA] = a;
+  qR[IA] = a;
+  const R rl = qL[ID], pl = qL[IP], ul = qL[IU], vl = qL[IV], wl = qL[IW], bl = qL[IB], cl = qL[IC];
+  const R ecinl = R(0.5) * (ul * ul + vl * vl + wl * wl) * rl;
+  const R emagl = R(0.5) * (a * a + bl * bl + cl * cl);
+  const R etotl = pl * entho + ecinl + emagl;
+  const R ptotl = pl + emagl;
+  const R vdotbl = ul * a + vl * bl + wl * cl;
+  const R rr = qR[ID], pr = qR[IP], ur = qR[IU], vr = qR[IV], wr = qR[IW], br = qR[IB], cr = qR[IC];
+  const R ecinr = R(0.5) * (ur * ur + vr * vr + wr * wr) * rr;
+  const R emagr = R(0.5) * (a * a + br * br + cr * cr);
+  const R etotr = pr * entho + ecinr + emagr;
+  const R ptotr = pr + emagr;
+  const R vdotbr = ur * a + vr * br + wr * cr;
+
+  const R cfastl = speed_fast(qL, 0, s);
+  const R cfastr = speed_fast(qR, 0, s);
+  const R sl = rmin<R>(ul, ur) - rmax<R>(cfastl, cfastr);
+  const R sr = rmax<R>(ul, ur) + rmax<R>(cfastl, cfastr);
+  const R rcl = rl * (ul - sl);
+  const R rcr = rr * (sr - ur);
+  const R ustar = (rcr * ur + rcl * ul + (ptotl - ptotr)) / (rcr + rcl);
+  const R ptotstar = (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) / (rcr + rcl);
+
+  const R rstarl = rl * (sl - ul) / (sl - ustar);
+  R       estar = rl * (sl - ul) * (sl - ustar) - a * a;
+  const R el = rl * (sl - ul) * (sl - ul) - a * a;
+  R       vstarl, wstarl, bstarl, cstarl;
+  if (rabs<R>(estar) < R(1e-4) * (a * a))
+  {
+    vstarl = vl; bstarl = bl; wstarl = wl; cstarl = cl;
+  }
+  else
+  {
+    vstarl = vl - a * bl * (ustar - ul) / estar;
+    bstarl = bl * el / estar;
+    wstarl = wl - a * cl * (ustar - ul) / estar;
+    cstarl = cl * el / estar;
+  }
+  const R vdotbstarl = ustar * a + vstarl * bstarl + wstarl * cstarl;
+  const R etotstarl =
+    ((sl - ul) * etotl - ptotl * ul + ptotstar * ustar + a * (vdotbl - vdotbstarl)) / (sl - ustar);
+  const R sqrrstarl = dsqrt<R>(rstarl);
+  const R calfvenl = rabs<R>(a) / sqrrstarl;
+  const R sal = ustar - calfvenl;
+
+  const R rstarr = rr * (sr - ur) / (sr - ustar);
+  estar = rr * (sr - ur) * (sr - ustar) - a * a;
+  const R er = rr * (sr - ur) * (sr - ur) - a * a;
+  R       vstarr, wstarr, bstarr, cstarr;
+  if (rabs<R>(estar) < R(1e-4) * (a * a))
+  {
+    vstarr = vr; bstarr = br; wstarr = wr; cstarr = cr;
+  }
+  else
+  {
+    vstarr = vr - a * br * (ustar - ur) / estar;
+    bstarr = br * er / estar;
+    wstarr = wr - a * cr * (ustar - ur) / estar;
+    cstarr = cr * er / estar;
+  }
+  const R vdotbstarr = ustar * a + vstarr * bstarr + wstarr * cstarr;
+  const R etotstarr =
+    ((sr - ur) * etotr - ptotr * ur + ptotstar * ustar + a * (vdotbr - vdotbstarr)) / (sr - ustar);
+  const R sqrrstarr = dsqrt<R>(rstarr);
+  const R calfvenr = rabs<R>(a) / sqrrstarr;
+  const R sar = ustar + calfvenr;
+
+  const R vstarstar =
+    (sqrrstarl * vstarl + sqrrstarr * vstarr + sgnm * (bstarr - bstarl)) / (sqrrstarl + sqrrstarr);
+  const R wstarstar =
+    (sqrrstarl * wstarl + sqrrstarr * wstarr + sgnm * (cstarr - cstarl)) / (sqrrstarl + sqrrstarr);
+  const R bstarstar =
+    (sqrrstarl * bstarr + sqrrstarr * bstarl + sgnm * sqrrstarl * sqrrstarr * (vstarr - vstarl)) /
+    (sqrrstarl + sqrrstarr);
+  const R cstarstar =
+    (sqrrstarl * cstarr + sqrrstarr * cstarl + sgnm * sqrrstarl * sqrrstarr * (wstarr - wstarl)) /
+    (sqrrstarl + sqrrstarr);
+  const R vdotbstarstar = ustar * a + vstarstar * bstarstar + wstarstar * cstarstar;
+  const R etotstarstarl = etotstarl - sgnm * sqrrstarl * (vdotbstarl - vdotbstarstar);
+  const R etotstarstarr = etotstarr + sgnm * sqrrstarr * (vdotbstarr - vdotbstarstar);
+
+  R ro, uo, vo, wo, bo, co, ptoto, etoto, vdotbo;
+  if (sl > 0)
+  {
+    ro = rl; uo = ul; vo = vl; wo = wl; bo = bl; co = cl;
+    ptoto = ptotl; etoto = etotl; vdotbo = vdotbl;
+  }
+  else if (sal > 0)
+  {
+    ro = rstarl; uo = ustar; vo = vstarl; wo = wstarl; bo = bstarl; co = cstarl;
+    ptoto = ptotstar; etoto = etotstarl; vdotbo = vdotbstarl;
+  }
+  else if (ustar > 0)
+  {
+    ro = rstarl; uo = ustar; vo = vstarstar; wo = wstarstar; bo = bstarstar; co = cstarstar;
+    ptoto = ptotstar; etoto = etotstarstarl; vdotbo = vdotbstarstar;
+  }
+  else if (sar > 0)
+  {
+    ro = rstarr; uo = ustar; vo = vstarstar; wo = wstarstar; bo = bstarstar; co = cstarstar;
+    ptoto = ptotstar; etoto = etotstarstarr; vdotbo = vdotbstarstar;
+  }
+  else if (sr > 0)
+  {
+    ro = rstarr; uo = ustar; vo = vstarr; wo = wstarr; bo = bstarr; co = cstarr;
+    ptoto = ptotstar; etoto = etotstarr; vdotbo = vdotbstarr;
+  }
+  else
+  {
+    ro = rr; uo = ur; vo = vr; wo = wr; bo = br; co = cr;
+    ptoto = ptotr; etoto = etotr; vdotbo = vdotbr;
+  }
+  flux[ID] = ro * uo;
+  flux[IP] = (etoto + ptoto) * uo - a * vdotbo;
+  flux[IU] = ro * uo * uo - a * a + ptoto;
+  flux[IV] = ro * uo * vo - a * bo;
+  flux[IW] = ro * uo * wo - a * co;
+  flux[IA] = R(0);
+  flux[IB] = bo * uo - a * vo;
+  flux[IC] = co * uo - a * wo;
+}
+
+// riemann_mhd dispatch (models/RiemannSolvers_MHD.h:559-590)
+template <typename R>
+__device__ __forceinline__ void
+riemann_mhd(R * qL, R * qR, R * flux, const Phys<R> & s)
+{
+  if (s.riemann == RS_HLLD)
+    riemann_hlld(qL, qR, flux, s);
+  else if (s.riemann == RS_HLL)
+    riemann_hll(qL, qR, flux, s);
+  else if (s.riemann == RS_LLF)
+    riemann_llf(qL, qR, flux, s);
+  else
+  {
+#pragma unroll
+    for (int n = 0; n < 8; ++n)
+      flux[n] = R(0);
+    riemann_hllc(qL, qR, flux, s);
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ R
+max4(R a0, R a1, R a2, R a3)
+{
+  R r = a0;
+  r = (a1 > r) ? a1 : r;
+  r = (a2 > r) ? a2 : r;
+  r = (a3 > r) ? a3 : r;
+  return r;
+}
+template <typename R>
+__device__ __forceinline__ R
+min4(R a0, R a1, R a2, R a3)
+{
+  R r = a0;
+  r = (a1 < r) ? a1 : r;
+  r = (a2 < r) ? a2 : r;
+  r = (a3 < r) ? a3 : r;
+  return r;
+}
+template <typename R>
+__device__ __forceinline__ R
+max5(R a0, R a1, R a2, R a3, R a4)
+{
+  R r = a0;
+  r = (a1 > r) ? a1 : r;
+  r = (a2 > r) ? a2 : r;
+  r = (a3 > r) ? a3 : r;
+  r = (a4 > r) ? a4 : r;
+  return r;
+}
+
+// Edge-state slots: reconstructed states around an edge and the 2D Riemann problem states.
+enum : int
+{
+  ERT = 0,
+  ELT = 1,
+  ERB = 2,
+  ELB = 3
+};
+enum : int
+{
+  SLL = 0,
+  SRL = 1,
+  SLR = 2,
+  SRR = 3
+};
+
+// compute_emf<dir> + mag_riemann2d_hlld (models/RiemannSolvers_MHD.h:629-869, 890-1097).
+// qe[ERT..ELB] are the reconstructed edge states; emf_dir 0 (EMFX), 1 (EMFY), 2 (EMFZ).
+template <typename R>
+__device__ R
+edge_emf(const R (*qe)[8], int emf_dir, const Phys<R> & s)
+{
+  int iu, iv, iw, ia, ib, ic;
+  if (emf_dir == 2)
+  {
+    iu = IU; iv = IV; iw = IW; ia = IA; ib = IB; ic = IC;
+  }
+  else if (emf_dir == 1)
+  {
+    iu = IW; iv = IU; iw = IV; ia = IC; ib = IA; ic = IB;
+  }
+  else
+  {
+    iu = IV; iv = IW; iw = IU; ia = IB; ib = IC; ic = IA;
+  }
+  const R *qRT = qe[ERT], *qLT = qe[ELT], *qRB = qe[ERB], *qLB = qe[ELB];
+  // 4 states (LL, RL, LR, RR) in the rotated frame
+  const R rLL = qRT[ID], rRL = qLT[ID], rLR = qRB[ID], rRR = qLB[ID];
+  const R pLL = qRT[IP], pRL = qLT[IP], pLR = qRB[IP], pRR = qLB[IP];
+  const R uLL = qRT[iu], uRL = qLT[iu], uLR = qRB[iu], uRR = qLB[iu];
+  const R vLL = qRT[iv], vRL = qLT[iv], vLR = qRB[iv], vRR = qLB[iv];
+  const R aLL = R(0.5) * (qRT[ia] + qLT[ia]);
+  const R aRL = R(0.5) * (qRT[ia] + qLT[ia]);
+  const R aLR = R(0.5) * (qRB[ia] + qLB[ia]);
+  const R aRR = R(0.5) * (qRB[ia] + qLB[ia]);
+  const R bLL = R(0.5) * (qRT[ib] + qRB[ib]);
+  const R bRL = R(0.5) * (qLT[ib] + qLB[ib]);
+  const R bLR = R(0.5) * (qRT[ib] + qRB[ib]);
+  const R bRR = R(0.5) * (qLT[ib] + qLB[ib]);
+  const R cLL = qRT[ic], cRL = qLT[ic], cLR = qRB[ic], cRR = qLB[ic];
+  (void)iw;
+
+  const R ELL = uLL * bLL - vLL * aLL;
+  const R ERL = uRL * bRL - vRL * aRL;
+  const R ELR = uLR * bLR - vLR * aLR;
+  const R ERR = uRR * bRR - vRR * aRR;
+
+  // find_speed_fast<IX>/<IY> for the 4 states (models/mhd_utils.h:93-122)
+  auto fast = [&](R d, R p, R a, R b, R c, R bn) {
+    const R b2 = a * a + b * b + c * c;
+    const R c2 = s.gamma0 * p / d;
+    const R d2 = R(0.5) * (b2 / d + c2);
+    return dsqrt<R>(d2 + dsqrt<R>(d2 * d2 - c2 * bn * bn / d));
+  };
+  const R cFastLLx = fast(rLL, pLL, aLL, bLL, cLL, aLL);
+  const R cFastLRx = fast(rLR, pLR, aLR, bLR, cLR, aLR);
+  const R cFastRLx = fast(rRL, pRL, aRL, bRL, cRL, aRL);
+  const R cFastRRx = fast(rRR, pRR, aRR, bRR, cRR, aRR);
+  const R cFastLLy = fast(rLL, pLL, aLL, bLL, cLL, bLL);
+  const R cFastLRy = fast(rLR, pLR, aLR, bLR, cLR, bLR);
+  const R cFastRLy = fast(rRL, pRL, aRL, bRL, cRL, bRL);
+  const R cFastRRy = fast(rRR, pRR, aRR, bRR, cRR, bRR);
+
+  const R SL = min4(uLL, uLR, uRL, uRR) - max4(cFastLLx, cFastLRx, cFastRLx, cFastRRx);
+  const R SR = max4(uLL, uLR, uRL, uRR) + max4(cFastLLx, cFastLRx, cFastRLx, cFastRRx);
+  const R SB = min4(vLL, vLR, vRL, vRR) - max4(cFastLLy, cFastLRy, cFastRLy, cFastRRy);
+  const R ST = max4(vLL, vLR, vRL, vRR) + max4(cFastLLy, cFastLRy, cFastRLy, cFastRRy);
+
+  const R PtotLL = pLL + R(0.5) * (aLL * aLL + bLL * bLL + cLL * cLL);
+  const R PtotLR = pLR + R(0.5) * (aLR * aLR + bLR * bLR + cLR * cLR);
+  const R PtotRL = pRL + R(0.5) * (aRL * aRL + bRL * bRL + cRL * cRL);
+  const R PtotRR = pRR + R(0.5) * (aRR * aRR + bRR * bRR + cRR * cRR);
+
+  const R rcLLx = rLL * (uLL - SL);
+  const R rcRLx = rRL * (SR - uRL);
+  const R rcLRx = rLR * (uLR - SL);
+  const R rcRRx = rRR * (SR - uRR);
+  const R rcLLy = rLL * (vLL - SB);
+  const R rcLRy = rLR * (ST - vLR);
+  const R rcRLy = rRL * (vRL - SB);
+  const R rcRRy = rRR * (ST - vRR);
+
+  const R ustar =
+    (rcLLx * uLL + rcLRx * uLR + rcRLx * uRL + rcRRx * uRR + (PtotLL - PtotRL + PtotLR - PtotRR)) /
+    (rcLLx + rcLRx + rcRLx + rcRRx);
+  const R vstar =
+    (rcLLy * vLL + rcLRy * vLR + rcRLy * vRL + rcRRy * vRR + (PtotLL - PtotLR + PtotRL - PtotRR)) /
+    (rcLLy + rcLRy + rcRLy + rcRRy);
+
+  const R rstarLLx = rLL * (SL - uLL) / (SL - ustar);
+  const R BstarLL = bLL * (SL - uLL) / (SL - ustar);
+  const R rstarLLy = rLL * (SB - vLL) / (SB - vstar);
+  const R AstarLL = aLL * (SB - vLL) / (SB - vstar);
+  const R rstarLL = rLL * (SL - uLL) / (SL - ustar) * (SB - vLL) / (SB - vstar);
+  const R EstarLLx = ustar * BstarLL - vLL * aLL;
+  const R EstarLLy = uLL * bLL - vstar * AstarLL;
+  const R EstarLL = ustar * BstarLL - vstar * AstarLL;
+
+  const R rstarLRx = rLR * (SL - uLR) / (SL - ustar);
+  const R BstarLR = bLR * (SL - uLR) / (SL - ustar);
+  const R rstarLRy = rLR * (ST - vLR) / (ST - vstar);
+  const R AstarLR = aLR * (ST - vLR) / (ST - vstar);
+  const R rstarLR = rLR * (SL - uLR) / (SL - ustar) * (ST - vLR) / (ST - vstar);
+  const R EstarLRx = ustar * BstarLR - vLR * aLR;
+  const R EstarLRy = uLR * bLR - vstar * AstarLR;
+  const R EstarLR = ustar * BstarLR - vstar * AstarLR;
+
+  const R rstarRLx = rRL * (SR - uRL) / (SR - ustar);
+  const R BstarRL = bRL * (SR - uRL) / (SR - ustar);
+  const R rstarRLy = rRL * (SB - vRL) / (SB - vstar);
+  const R AstarRL = aRL * (SB - vRL) / (SB - vstar);
+  const R rstarRL = rRL * (SR - uRL) / (SR - ustar) * (SB - vRL) / (SB - vstar);
+  const R EstarRLx = ustar * BstarRL - vRL * aRL;
+  const R EstarRLy = uRL * bRL - vstar * AstarRL;
+  const R EstarRL = ustar * BstarRL - vstar * AstarRL;
+
+  const R rstarRRx = rRR * (SR - uRR) / (SR - ustar);
+  const R BstarRR = bRR * (SR - uRR) / (SR - ustar);
+  const R rstarRRy = rRR * (ST - vRR) / (ST - vstar);
+  const R AstarRR = aRR * (ST - vRR) / (ST - vstar);
+  const R rstarRR = rRR * (SR - uRR) / (SR - ustar) * (ST - vRR) / (ST - vstar);
+  const R EstarRRx = ustar * BstarRR - vRR * aRR;
+  const R EstarRRy = uRR * bRR - vstar * AstarRR;
+  const R EstarRR = ustar * BstarRR - vstar * AstarRR;
+
+  const R calfvenL = max5<R>(rabs<R>(aLR) / dsqrt<R>(rstarLRx), rabs<R>(AstarLR) / dsqrt<R>(rstarLR),
+                             rabs<R>(aLL) / dsqrt<R>(rstarLLx), rabs<R>(AstarLL) / dsqrt<R>(rstarLL), s.smallc);
+  const R calfvenR = max5<R>(rabs<R>(aRR) / dsqrt<R>(rstarRRx), rabs<R>(AstarRR) / dsqrt<R>(rstarRR),
+                             rabs<R>(aRL) / dsqrt<R>(rstarRLx), rabs<R>(AstarRL) / dsqrt<R>(rstarRL), s.smallc);
+  const R calfvenB = max5<R>(rabs<R>(bLL) / dsqrt<R>(rstarLLy), rabs<R>(BstarLL) / dsqrt<R>(rstarLL),
+                             rabs<R>(bRL) / dsqrt<R>(rstarRLy), rabs<R>(BstarRL) / dsqrt<R>(rstarRL), s.smallc);
+  const R calfvenT = max5<R>(rabs<R>(bLR) / dsqrt<R>(rstarLRy), rabs<R>(BstarLR) / dsqrt<R>(rstarLR),
+                             rabs<R>(bRR) / dsqrt<R>(rstarRRy), rabs<R>(BstarRR) / dsqrt<R>(rstarRR), s.smallc);
+
+  const R SAL = rmin<R>(ustar - calfvenL, R(0));
+  const R SAR = rmax<R>(ustar + calfvenR, R(0));
+  const R SAB = rmin<R>(vstar - calfvenB, R(0));
+  const R SAT = rmax<R>(vstar + calfvenT, R(0));
+
+  const R AstarT = (SAR * AstarRR - SAL * AstarLR) / (SAR - SAL);
+  const R AstarB = (SAR * AstarRL - SAL * AstarLL) / (SAR - SAL);
+  const R BstarR = (SAT * BstarRR - SAB * BstarRL) / (SAT - SAB);
+  const R BstarL = (SAT * BstarLR - SAB * BstarLL) / (SAT - SAB);
+
+  R       E = 0, tmpE = 0;
+  const R SB_pos = (1 + rcopysign<R>(R(1), SB)) / 2, SB_neg = 1 - SB_pos;
+  const R ST_pos = (1 + rcopysign<R>(R(1), ST)) / 2, ST_neg = 1 - ST_pos;
+  const R SL_pos = (1 + rcopysign<R>(R(1), SL)) / 2, SL_neg = 1 - SL_pos;
+  const R SR_pos = (1 + rcopysign<R>(R(1), SR)) / 2, SR_neg = 1 - SR_pos;
+
+  tmpE = (SAL * SAB * EstarRR - SAL * SAT * EstarRL - SAR * SAB * EstarLR + SAR * SAT * EstarLL) /
+           (SAR - SAL) / (SAT - SAB) -
+         SAT * SAB / (SAT - SAB) * (AstarT - AstarB) + SAR * SAL / (SAR - SAL) * (BstarR - BstarL);
+  E += (SB_neg * ST_pos * SL_neg * SR_pos) * tmpE;
+
+  tmpE = (SAR * EstarLLx - SAL * EstarRLx + SAR * SAL * (bRL - bLL)) / (SAR - SAL);
+  tmpE = SL_pos * ELL + SL_neg * SR_neg * ERL + SL_neg * SR_pos * tmpE;
+  E += SB_pos * tmpE;
+
+  tmpE = (SAR * EstarLRx - SAL * EstarRRx + SAR * SAL * (bRR - bLR)) / (SAR - SAL);
+  tmpE = SL_pos * ELR + SL_neg * SR_neg * ERR + SL_neg * SR_pos * tmpE;
+  E += (SB_neg * ST_neg) * tmpE;
+
+  tmpE = (SAT * EstarLLy - SAB * EstarLRy - SAT * SAB * (aLR - aLL)) / (SAT - SAB);
+  E += (SB_neg * ST_pos * SL_pos) * tmpE;
+
+  tmpE = (SAT * EstarRLy - SAB * EstarRRy - SAT * SAB * (aRR - aRL)) / (SAT - SAB);
+  E += (SB_neg * ST_pos * SL_neg * SR_neg) * tmpE;
+
+  return E;
+}
+
+// slope_unsplit_scalar (scheme/ComputeLimitedSlopesFunctor.cpp:121-144)
+template <typename R>
+__device__ __forceinline__ R
+slope1(R q, R qp, R qm, R slope_type)
+{
+  R dq = 0;
+  if (slope_type == R(1) || slope_type == R(2))
+  {
+    const R dlft = slope_type * (q - qm);
+    const R drgt = slope_type * (qp - q);
+    const R dcen = R(0.5) * (qp - qm);
+    const R dsgn = (dcen >= R(0)) ? R(1) : R(-1);
+    const R slop = rmin<R>(rabs<R>(dlft), rabs<R>(drgt));
+    const R dlim = (dlft * drgt) <= R(0) ? R(0) : slop;
+    dq = dsgn * rmin<R>(dlim, rabs<R>(dcen));
+  }
+  return dq;
+}
+
+} // namespace gmhd

@@ -1,0 +1,117 @@
+// FP64 instantiations of the fused step: the drop-in path. This unit is compiled with
+// --fmad=false so that every a*b+c stays unfused, matching the reference formulas' FP64 rounding.
+#include "launch.cuh"
+
+namespace gmhd
+{
+using F64_3D_844 = Cfg<double, 3, 8, 4, 4, 128, true>;
+using F64_3D_444 = Cfg<double, 3, 4, 4, 4, 64, true>;
+using F64_2D_16 = Cfg<double, 2, 16, 16, 1, 256, true>;
+using F64_2D_8 = Cfg<double, 2, 8, 8, 1, 64, true>;
+using F64_2D_4 = Cfg<double, 2, 4, 4, 1, 32, true>;
+
+int
+launch_step_fp64(const StepArgs & a, int dim, cudaStream_t stream)
+{
+  if (dim == 3)
+  {
+    if (a.bx % 8 == 0 && a.by % 4 == 0 && a.bz % 4 == 0)
+      return launch_fused<F64_3D_844>(a, stream);
+    return launch_fused<F64_3D_444>(a, stream);
+  }
+  if (a.bx % 16 == 0 && a.by % 16 == 0)
+    return launch_fused<F64_2D_16>(a, stream);
+  if (a.bx % 8 == 0 && a.by % 8 == 0)
+    return launch_fused<F64_2D_8>(a, stream);
+  return launch_fused<F64_2D_4>(a, stream);
+}
+
+int
+prepare_fp64()
+{
+  int rc = 0;
+  rc = rc ? rc : prepare_fused<F64_3D_844>();
+  rc = rc ? rc : prepare_fused<F64_3D_444>();
+  rc = rc ? rc : prepare_fused<F64_2D_16>();
+  rc = rc ? rc : prepare_fused<F64_2D_8>();
+  rc = rc ? rc : prepare_fused<F64_2D_4>();
+  return rc;
+}
+} // namespace gmhd
+
+namespace gmhd
+{
+// ComputeDtMHDFunctor::compute_cfl (scheme/ComputeDtMHDFunctor.cpp:86-151) over the owned blocks,
+// one CTA per block, max-reduced per problem. FP64 with the reference operand order.
+__global__ void __launch_bounds__(256)
+inv_dt_kernel(const double * __restrict__ U, const double * __restrict__ B, const int32_t * __restrict__ level,
+              const int32_t * __restrict__ problem, int dim, int bx, int by, int bz, int64_t ncell, int64_t nfx,
+              int64_t nfy, int64_t nface, double gamma0, double smallr, double smallp, double scaling_factor,
+              unsigned long long * invdt)
+{
+  const int     blk = blockIdx.x;
+  const double  dx = (1.0 / (double)((int64_t)bx << level[blk])) * scaling_factor;
+  const double *Ub = U + (int64_t)blk * 5 * ncell;
+  const double *Bb = B + (int64_t)blk * nface;
+  double        m = 0.0;
+  for (int64_t c = threadIdx.x; c < ncell; c += blockDim.x)
+  {
+    const int i = (int)(c % bx), j = (int)((c / bx) % by), k = (int)(c / ((int64_t)bx * by));
+    const double Ax = 0.5 * (Bb[i + (int64_t)(bx + 1) * (j + (int64_t)by * k)] +
+                             Bb[i + 1 + (int64_t)(bx + 1) * (j + (int64_t)by * k)]);
+    const double Ay = 0.5 * (Bb[nfx + i + (int64_t)bx * (j + (int64_t)(by + 1) * k)] +
+                             Bb[nfx + i + (int64_t)bx * (j + 1 + (int64_t)(by + 1) * k)]);
+    double Az;
+    if (dim == 3)
+      Az = 0.5 * (Bb[nfx + nfy + i + (int64_t)bx * (j + (int64_t)by * k)] +
+                  Bb[nfx + nfy + i + (int64_t)bx * (j + (int64_t)by * (k + 1))]);
+    else
+      Az = 0.5 * (Bb[nfx + nfy + c] + Bb[nfx + nfy + c]);
+    const double r = fmax(Ub[c], smallr);
+    const double vx = Ub[2 * ncell + c] / r, vy = Ub[3 * ncell + c] / r, vz = Ub[4 * ncell + c] / r;
+    const double eken = 0.5 * (vx * vx + vy * vy + vz * vz);
+    const double emag = 0.5 * (Ax * Ax + Ay * Ay + Az * Az);
+    const double eint = (Ub[ncell + c] - emag) / r - eken;
+    const double p = fmax((gamma0 - 1.0) * r * eint, r * smallp);
+    const double b2 = Ax * Ax + Ay * Ay + Az * Az;
+    const double c2 = gamma0 * p / r;
+    const double d2 = 0.5 * (b2 / r + c2);
+    const double cfx = sqrt(d2 + sqrt(d2 * d2 - c2 * Ax * Ax / r)) + fabs(vx);
+    const double cfy = sqrt(d2 + sqrt(d2 * d2 - c2 * Ay * Ay / r)) + fabs(vy);
+    double       val;
+    if (dim == 3)
+    {
+      const double cfz = sqrt(d2 + sqrt(d2 * d2 - c2 * Az * Az / r)) + fabs(vz);
+      val = cfx / dx + cfy / dx + cfz / dx;
+    }
+    else
+      val = cfx / dx + cfy / dx;
+    m = fmax(m, val);
+  }
+  __shared__ double red[8];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+  if ((threadIdx.x & 31) == 0)
+    red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+      m = fmax(m, red[w]);
+    atomicMax(&invdt[problem ? problem[blk] : 0], (unsigned long long)__double_as_longlong(m));
+  }
+}
+
+int
+launch_inv_dt(const double * U, const double * B, const int32_t * level, const int32_t * problem, int n_owned, int dim,
+              int bx, int by, int bz, int64_t ncell, int64_t nfx, int64_t nfy, int64_t nface, double gamma0,
+              double smallr, double smallp, double scaling_factor, unsigned long long * invdt, cudaStream_t stream)
+{
+  if (n_owned <= 0)
+    return 0;
+  inv_dt_kernel<<<n_owned, 256, 0, stream>>>(U, B, level, problem, dim, bx, by, bz, ncell, nfx, nfy, nface, gamma0,
+                                             smallr, smallp, scaling_factor, invdt);
+  return (int)cudaGetLastError();
+}
+} // namespace gmhd

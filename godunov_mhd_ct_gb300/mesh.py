@@ -10,8 +10,9 @@ boundary that has no outside block.
 
 Outside blocks (non-periodic directions) are appended after the owned blocks, as the reference
 stores its "outside" quadrants after owned + ghost ones; ``border_conditions/FillOutside.cpp``
-fills them before each step. ``outside_src[b - n_owned]`` is the inside block an outside block
-copies from and ``outside_dir`` the direction (0..2) and side (-1/+1) it lies across.
+fills them before each step. ``outside_src[b - n_owned]`` is the inside block across the
+outside normal (diagonal for edge/corner outside blocks) and ``outside_normal[b - n_owned]`` the
+normal per axis: +1 when the block lies below the domain, -1 above it, 0 within its range.
 """
 from __future__ import annotations
 
@@ -45,7 +46,7 @@ class BlockMesh:
     periodic: tuple
     scaling_factor: float = 1.0
     outside_src: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
-    outside_dir: np.ndarray = field(default_factory=lambda: np.zeros((0, 2), np.int32))
+    outside_normal: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.int32))
 
     @property
     def n_blocks(self) -> int:
@@ -108,7 +109,7 @@ class BlockMesh:
 
         # outside blocks across non-periodic boundaries: one layer, including edge/corner ones
         ext_lookup = {}
-        out_coords, out_src, out_dir = [], [], []
+        out_coords, out_src, out_normal = [], [], []
         if not all(per[:dim]):
             rng = [range(-1, g + 1) if not per[d] else range(g) for d, g in enumerate((gx, gy, gz))]
             if dim == 2:
@@ -120,14 +121,13 @@ class BlockMesh:
                         inside = 0 <= cx < gx and 0 <= cy < gy and 0 <= cz < gz
                         if inside:
                             continue
-                        # source: clamp to the grid; direction: first axis that is outside
+                        # source: clamp to the grid (the block across the inward normal)
                         src = (min(max(cx, 0), gx - 1), min(max(cy, 0), gy - 1), min(max(cz, 0), gz - 1))
-                        d_out = next(d for d in range(3) if c[d] != src[d])
-                        side = -1 if c[d_out] < 0 else 1
+                        normal = tuple(int(np.sign(src[d] - c[d])) for d in range(3))
                         ext_lookup[c] = n_owned + len(out_coords)
                         out_coords.append(c)
                         out_src.append(lookup[src])
-                        out_dir.append((d_out, side))
+                        out_normal.append(normal)
         n_blocks = n_owned + len(out_coords)
         all_coords = np.concatenate([coords, np.array(out_coords, dtype=np.int64).reshape(-1, 3)])
         gsz = (gx, gy, gz)
@@ -161,7 +161,7 @@ class BlockMesh:
                          neighbor=neighbor, coords=all_coords, n_owned=n_owned, grid=gsz, periodic=per,
                          scaling_factor=scaling_factor,
                          outside_src=np.array(out_src, dtype=np.int32),
-                         outside_dir=np.array(out_dir, dtype=np.int32).reshape(-1, 2))
+                         outside_normal=np.array(out_normal, dtype=np.int32).reshape(-1, 3))
 
     # ---- layout helpers -------------------------------------------------------------------------
     def alloc_state(self):

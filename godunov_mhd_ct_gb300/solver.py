@@ -1,0 +1,137 @@
+"""Host-side mirror of the reference's interface for this path.
+
+``GodunovImplemGB300`` plays the role of a ``GodunovImplemBase`` implementation
+(scheme/GodunovImplemBase.h:45-90): ``resize_auxiliary_data``, ``total_mem_size_in_bytes`` and
+``do_time_step(U, U2, Bface, Bface2, dt)``. ``compute_inv_dt`` is ComputeDtMHDFunctor::apply
+(scheme/ComputeDtMHDFunctor.cpp:44-82) and ``fill_outside`` FillOutsideCellFunctor::apply
+(border_conditions/FillOutside.cpp:47-93). All work goes through libgmhd.so (include/gmhd.h);
+arrays are CUDA tensors (torch) in the C-ABI layout, or raw device pointers.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native as nat
+from .mesh import BlockMesh
+from .settings import MHDSettings
+
+
+def _ptr(x) -> int:
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        if not x.is_cuda:
+            raise ValueError("expected a CUDA tensor")
+        if not x.is_contiguous():
+            raise ValueError("expected a contiguous tensor")
+        return x.data_ptr()
+    raise TypeError(f"unsupported array type {type(x)}")
+
+
+def _stream_ptr(stream) -> int | None:
+    if stream is None:
+        try:
+            import torch
+
+            return torch.cuda.current_stream().cuda_stream
+        except Exception:  # noqa: BLE001
+            return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+class GodunovImplemGB300:
+    """GB300 implementation of the MUSCL-Hancock + CT stage (create_godunov_implem's product)."""
+
+    def __init__(self, settings: MHDSettings, mesh: BlockMesh, precision: str = "fp64", problem=None,
+                 n_problems: int = 1, bc=None):
+        if settings.riemann_id not in (2, 3, 4, 5):
+            raise ValueError(f"unknown Riemann solver {settings.riemann!r} (the reference aborts here)")
+        if settings.implementation_version != 0:
+            # SolverGodunovMHD.cpp:91-97 accepts only version 0; this path implements it
+            raise ValueError("only implementation_version=0 exists in the reference")
+        self.settings = settings
+        self.precision = precision
+        p = nat.GmhdParams(settings.gamma0, settings.cfl, settings.slope_type, settings.smallr, settings.smallc,
+                           settings.scaling_factor if mesh is None else mesh.scaling_factor,
+                           settings.riemann_id, nat.PRECISION[precision])
+        self._lib = nat.lib()
+        self._ctx = self._lib.gmhd_create(ctypes.byref(p))
+        if not self._ctx:
+            raise nat.NativeError("gmhd_create failed (bad settings or no CUDA device)")
+        self.mesh = None
+        self._tables = None
+        self.resize_auxiliary_data(mesh, problem=problem, n_problems=n_problems, bc=bc)
+
+    # --- GodunovImplemBase -----------------------------------------------------------------------
+    def resize_auxiliary_data(self, mesh: BlockMesh | None = None, problem=None, n_problems: int = 1, bc=None):
+        if mesh is not None:
+            self.mesh = mesh
+            self._tables = nat.MeshTables(mesh, problem=problem, n_problems=n_problems, bc=bc)
+            self.n_problems = n_problems
+        nat.check(self._lib.gmhd_set_mesh(self._ctx, ctypes.byref(self._tables.c)), "gmhd_set_mesh", self._ctx)
+
+    def total_mem_size_in_bytes(self) -> int:
+        return int(self._lib.gmhd_mem_bytes(self._ctx))
+
+    def do_time_step(self, U, U2, Bface, Bface2, dt: float, stream=None) -> None:
+        nat.check(self._lib.gmhd_step(self._ctx, _ptr(U), _ptr(U2), _ptr(Bface), _ptr(Bface2), float(dt),
+                                      _stream_ptr(stream)), "gmhd_step", self._ctx)
+
+    # --- solver-side device calls of the path ------------------------------------------------------
+    def compute_inv_dt(self, U, Bface, stream=None):
+        out = np.zeros(self.n_problems, dtype=np.float64)
+        nat.check(self._lib.gmhd_inv_dt(self._ctx, _ptr(U), _ptr(Bface), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                        _stream_ptr(stream)), "gmhd_inv_dt", self._ctx)
+        return out if self.n_problems > 1 else float(out[0])
+
+    def compute_dt(self, U, Bface, stream=None):
+        """dt = cfl / invDt (SolverGodunovMHD.cpp:375-403)."""
+        return self.settings.cfl / self.compute_inv_dt(U, Bface, stream)
+
+    def fill_outside(self, U, Bface, stream=None) -> None:
+        nat.check(self._lib.gmhd_fill_outside(self._ctx, _ptr(U), _ptr(Bface), _stream_ptr(stream)),
+                  "gmhd_fill_outside", self._ctx)
+
+    def advance(self, U, U2, B, B2, nsteps: int, t=None, t_end=None, use_graph: bool = True, stream=None):
+        """nsteps solver iterations on device; U/B hold the result. Returns (dt_log, t)."""
+        npb = self.n_problems
+        dtlog = np.zeros(max(nsteps, 1) * npb, dtype=np.float64)
+        tt = np.zeros(npb) if t is None else np.ascontiguousarray(np.broadcast_to(t, (npb,)), dtype=np.float64).copy()
+        te = None if t_end is None else np.ascontiguousarray(np.broadcast_to(t_end, (npb,)), dtype=np.float64)
+        dp = ctypes.POINTER(ctypes.c_double)
+        rc = self._lib.gmhd_advance(self._ctx, _ptr(U), _ptr(U2), _ptr(B), _ptr(B2), int(nsteps), tt.ctypes.data_as(dp),
+                                    te.ctypes.data_as(dp) if te is not None else None, dtlog.ctypes.data_as(dp),
+                                    int(bool(use_graph)), _stream_ptr(stream))
+        nat.check(rc, "gmhd_advance", self._ctx)
+        return dtlog[: nsteps * npb].reshape(nsteps, npb), tt
+
+    def step_host(self, U: np.ndarray, B: np.ndarray, dt: float, U2: np.ndarray | None = None,
+                  B2: np.ndarray | None = None):
+        """do_time_step on host arrays (copies in and out inside the call)."""
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        B = np.ascontiguousarray(B, dtype=np.float64)
+        U2 = U.copy() if U2 is None else U2
+        B2 = B.copy() if B2 is None else B2
+        nat.check(self._lib.gmhd_step_host(self._ctx, U.ctypes.data, U2.ctypes.data, B.ctypes.data, B2.ctypes.data,
+                                           float(dt), None), "gmhd_step_host", self._ctx)
+        return U2, B2
+
+    def last_status(self) -> int:
+        flags = ctypes.c_uint32(0)
+        nat.check(self._lib.gmhd_last_status(self._ctx, ctypes.byref(flags)), "gmhd_last_status", self._ctx)
+        return int(flags.value)
+
+    def close(self) -> None:
+        if getattr(self, "_ctx", None):
+            self._lib.gmhd_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass

@@ -1,0 +1,179 @@
+/*
+ * gmhd.h — C ABI of the GB300-native MUSCL-Hancock + constrained-transport MHD stage.
+ *
+ * Drop-in for the hot path of godunov_mhd_ct: the GodunovImplemBase implementation interface
+ * (scheme/GodunovImplemBase.h:45-90) plus the two device calls the solver makes around it,
+ * ComputeDtMHDFunctor::apply (scheme/ComputeDtMHDFunctor.cpp:44-82) and
+ * FillOutsideCellFunctor::apply (border_conditions/FillOutside.cpp:47-93).
+ *
+ * Conventions
+ *  - Every entry point returns an int status (GMHD_OK == 0, negative on error) and never aborts;
+ *    the reference aborts through Kokkos::abort / KOKKOS_ASSERT instead.
+ *  - Array arguments of the step / CFL / fill calls are DEVICE pointers, FP64, in this layout
+ *    (one leaf block after another, blocks in the order of the mesh tables):
+ *      U : [n_blocks][5][bz][by][bx]       (rho, E, rho u, rho v, rho w)
+ *      B : [n_blocks][Bx | By | Bz]        Bx: [bz][by][bx+1], By: [bz][by+1][bx],
+ *                                          Bz: [bz+1][by][bx] in 3D, [by][bx] cell-centred in 2D
+ *    (DataArrayBlock / FaceDataArrayBlock hold the same per-block data; their in-block order is
+ *    kalypsso-core's and cannot be checked here.) gmhd_layout_check() verifies a caller's
+ *    strides against this layout.
+ *  - Host-buffer variants (suffix _host) take HOST pointers and do the copies themselves.
+ *  - Streams are cudaStream_t passed as void*; NULL is the legacy default stream.
+ */
+#ifndef GMHD_H_
+#define GMHD_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum gmhd_status
+{
+  GMHD_OK = 0,
+  GMHD_ERR_ARGUMENT = -1,    /* null pointer, bad size, unsupported option */
+  GMHD_ERR_MESH = -2,        /* mesh not set, inconsistent tables, level jump */
+  GMHD_ERR_CUDA = -3,        /* a CUDA call failed; see gmhd_last_cuda_error() */
+  GMHD_ERR_ALIAS = -4,       /* output aliases an input */
+  GMHD_ERR_HEALTH = -5,      /* the step produced a non-physical state (see gmhd_last_status) */
+  GMHD_ERR_TOO_LARGE = -6,   /* request exceeds a fixed capacity */
+};
+
+enum gmhd_riemann
+{ /* numeric values of RiemannSolverType (models/riemann_solver_types.h:26-37) */
+  GMHD_RIEMANN_LLF = 2,
+  GMHD_RIEMANN_HLL = 3,
+  GMHD_RIEMANN_HLLC = 4,
+  GMHD_RIEMANN_HLLD = 5
+};
+
+enum gmhd_precision
+{
+  GMHD_PRECISION_FP64 = 0,  /* reference arithmetic in FP64 (the drop-in) */
+  GMHD_PRECISION_MIXED = 1  /* FP32 reconstruction/Riemann/EMF, FP64 accumulation and CT curl */
+};
+
+enum gmhd_bc
+{ /* numeric values of BC_MHD (border_conditions/FillOutside.h:55-61) */
+  GMHD_BC_NONE = 0,
+  GMHD_BC_PERIODIC = 1,
+  GMHD_BC_ZERO_GRADIENT = 2,
+  GMHD_BC_WALL = 3
+};
+
+/* Health flags reported by gmhd_last_status. */
+enum gmhd_health_flags
+{
+  GMHD_HEALTH_MISSING_NEIGHBOR = 1u,
+  GMHD_HEALTH_LEVEL_JUMP = 2u,
+  GMHD_HEALTH_BAD_DENSITY = 4u,
+  GMHD_HEALTH_NONFINITE = 8u,
+  GMHD_HEALTH_LOW_BETA_FP64 = 16u /* informational */
+};
+
+/* Settings read on the hot path: [hydro] gamma0, cfl, slope_type, smallr, smallc, riemann
+ * (models/HydroSettings.cpp:18-31) and [mesh] scaling_factor. smallp = smallc^2/gamma0 is derived
+ * as in the reference. */
+typedef struct gmhd_params
+{
+  double  gamma0;
+  double  cfl;
+  double  slope_type;
+  double  smallr;
+  double  smallc;
+  double  scaling_factor;
+  int32_t riemann;   /* enum gmhd_riemann */
+  int32_t precision; /* enum gmhd_precision */
+} gmhd_params;
+
+/* Leaf-block mesh (HOST pointers; copied by gmhd_set_mesh). Blocks [0, n_owned) are updated;
+ * blocks [n_owned, n_blocks) are outside blocks filled by gmhd_fill_outside.
+ * neighbor[b*27 + (oz+1)*9 + (oy+1)*3 + (ox+1)] is the block across face/edge/corner (ox,oy,oz)
+ * of block b, or -1. cell size of block b = scaling_factor / (bx * 2^level[b]). */
+typedef struct gmhd_mesh
+{
+  int32_t         dim;   /* 2 or 3 */
+  int32_t         bx, by, bz; /* bz == 1 in 2D */
+  int32_t         n_blocks;
+  int32_t         n_owned;
+  const int32_t * level;     /* [n_blocks] */
+  const int32_t * neighbor;  /* [n_blocks * 27] */
+  const int32_t * problem;   /* [n_blocks] independent-problem id, or NULL for a single problem */
+  int32_t         n_problems;
+  const int32_t * outside_src;    /* [n_blocks - n_owned] inside block across the outside normal */
+  const int32_t * outside_normal; /* [3 * (n_blocks - n_owned)] per axis: +1 below the domain,
+                                     -1 above it, 0 inside its range (points into the domain) */
+  int32_t         bc[6];          /* enum gmhd_bc for XMIN, XMAX, YMIN, YMAX, ZMIN, ZMAX */
+} gmhd_mesh;
+
+typedef struct gmhd_ctx gmhd_ctx;
+
+/* --- lifetime ------------------------------------------------------------------------------- */
+
+/* Constructor of the implementation (GodunovImplemV0 ctor, scheme/GodunovImplemV0.h:46-104,
+ * selected by create_godunov_implem, SolverGodunovMHD.h:326-340). Binds the current device.
+ * Returns NULL on invalid parameters. */
+gmhd_ctx * gmhd_create(const gmhd_params * params);
+void       gmhd_destroy(gmhd_ctx * ctx);
+
+/* resize_auxiliary_data (scheme/GodunovImplemBase.h:78-79): (re)loads the mesh tables after a
+ * regrid or repartition. */
+int gmhd_set_mesh(gmhd_ctx * ctx, const gmhd_mesh * mesh);
+
+/* total_mem_size_in_bytes (scheme/GodunovImplemBase.h:82-83): device memory held by ctx. */
+uint64_t gmhd_mem_bytes(const gmhd_ctx * ctx);
+
+/* --- the stage ------------------------------------------------------------------------------ */
+
+/* do_time_step (scheme/GodunovImplemBase.h:85-90, scheme/GodunovImplemV0.cpp:101-207).
+ * Writes U2 = U + conservative update and B2 = B + CT update for the owned blocks. Unlike the
+ * reference, U2/B2 need not equal U/B on entry (they are overwritten); they must not alias U/B.
+ * Ghost/outside blocks of U and B must be filled (SolverGodunovMHD.cpp:497-498). */
+int gmhd_step(gmhd_ctx * ctx, const double * U, double * U2, const double * B, double * B2, double dt,
+              void * stream);
+
+/* ComputeDtMHDFunctor::apply (scheme/ComputeDtMHDFunctor.cpp:44-82): invDt = max over owned
+ * cells of sum_d (c_f,d + |v_d|)/dx, returned on the host (synchronises the stream). With
+ * several problems, inv_dt receives n_problems values. */
+int gmhd_inv_dt(gmhd_ctx * ctx, const double * U, const double * B, double * inv_dt, void * stream);
+
+/* FillOutsideCellFunctor::apply (border_conditions/FillOutside.cpp:47-93): fills the outside
+ * blocks of U and B from the adjacent inside blocks (ZERO_GRADIENT / WALL). No-op when periodic. */
+int gmhd_fill_outside(gmhd_ctx * ctx, double * U, double * B, void * stream);
+
+/* Solver loop (SolverGodunovMHD::next_iteration_impl, SolverGodunovMHD.cpp:407-484, without AMR,
+ * IO and monitoring): nsteps of { dt = cfl / invDt (capped so no problem passes t_end);
+ * fill outside; do_time_step; U <- U2, B <- B2 } with the CFL reduction fused into each step and
+ * dt kept on the device. U/B hold the final state on return and U2/B2 are scratch of the same
+ * size. t (per problem, in/out) and t_end may be NULL (no cap). dt_log (host, nsteps * n_problems)
+ * may be NULL. The step sequence is captured once as a CUDA graph and replayed when use_graph. */
+int gmhd_advance(gmhd_ctx * ctx, double * U, double * U2, double * B, double * B2, int32_t nsteps,
+                 double * t, const double * t_end, double * dt_log, int32_t use_graph, void * stream);
+
+/* --- host-buffer variants ------------------------------------------------------------------- */
+
+/* gmhd_step on HOST arrays: copies U, B to the device, runs the step, copies U2, B2 back. */
+int gmhd_step_host(gmhd_ctx * ctx, const double * U, double * U2, const double * B, double * B2, double dt,
+                   void * stream);
+
+/* --- diagnostics ---------------------------------------------------------------------------- */
+
+/* Health flags accumulated since the last call (clears them). Synchronises the context stream. */
+int gmhd_last_status(gmhd_ctx * ctx, uint32_t * flags);
+
+/* Last CUDA error code seen by ctx (0 if none). */
+int gmhd_last_cuda_error(const gmhd_ctx * ctx);
+
+const char * gmhd_error_string(int status);
+
+/* Checks a caller layout: strides (in doubles) of U between variables and blocks, and of B
+ * between blocks, against the layout above. Returns GMHD_OK or GMHD_ERR_ARGUMENT. */
+int gmhd_layout_check(const gmhd_mesh * mesh, int64_t u_var_stride, int64_t u_block_stride,
+                      int64_t b_block_stride);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GMHD_H_ */

@@ -1,0 +1,62 @@
+"""Shared helpers for the parity tests: workloads on both paths, error metrics."""
+from __future__ import annotations
+
+import numpy as np
+
+from godunov_mhd_ct_gb300.mesh import BlockMesh
+from godunov_mhd_ct_gb300.settings import MHDSettings
+
+
+def settings(gamma0=5.0 / 3.0, cfl=0.5, slope_type=2.0, riemann="HLLD"):
+    return MHDSettings(gamma0=gamma0, cfl=cfl, slope_type=slope_type, riemann=riemann)
+
+
+def oracle_mesh(orc, mesh: BlockMesh):
+    return orc.Mesh(mesh.dim, mesh.block[0], mesh.block[1], mesh.block[2], mesh.level, mesh.neighbor,
+                    mesh.n_owned, mesh.scaling_factor)
+
+
+def oracle_settings(orc, st: MHDSettings):
+    return orc.settings(gamma0=st.gamma0, cfl=st.cfl, slope_type=st.slope_type, smallr=st.smallr,
+                        smallc=st.smallc, riemann=st.riemann_id)
+
+
+def max_rel_diff(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    scale = np.maximum(np.abs(b), 1e-300)
+    return float(np.max(np.abs(a - b) / np.maximum(scale, np.max(np.abs(b)) * 1e-12)))
+
+
+def l1_rel(a, b):
+    return float(np.sum(np.abs(np.asarray(a) - np.asarray(b))) / np.sum(np.abs(np.asarray(b))))
+
+
+def div_b(mesh: BlockMesh, B):
+    """Discrete divergence per owned cell, (sum of face differences) / dx."""
+    Bx, By, Bz = mesh.split_faces(np.asarray(B))
+    n = mesh.n_owned
+    d = (Bx[:n, ..., 1:] - Bx[:n, ..., :-1]) + (By[:n, :, 1:, :] - By[:n, :, :-1, :])
+    if mesh.dim == 3:
+        d = d + (Bz[:n, 1:] - Bz[:n, :-1])
+    return d / mesh.cell_length()
+
+
+def shared_face_mismatch(mesh: BlockMesh, B):
+    """Max |difference| between the two copies of every face shared by neighbouring blocks."""
+    from godunov_mhd_ct_gb300.mesh import nb_slot
+
+    Bx, By, Bz = mesh.split_faces(np.asarray(B))
+    worst = 0.0
+    n = mesh.n_owned
+    right_x = mesh.neighbor[:n, nb_slot(1, 0, 0)]
+    right_y = mesh.neighbor[:n, nb_slot(0, 1, 0)]
+    ok = right_x >= 0
+    worst = max(worst, float(np.max(np.abs(Bx[:n][ok, ..., -1] - Bx[right_x[ok], ..., 0]), initial=0.0)))
+    ok = right_y >= 0
+    worst = max(worst, float(np.max(np.abs(By[:n][ok, :, -1, :] - By[right_y[ok], :, 0, :]), initial=0.0)))
+    if mesh.dim == 3:
+        right_z = mesh.neighbor[:n, nb_slot(0, 0, 1)]
+        ok = right_z >= 0
+        worst = max(worst, float(np.max(np.abs(Bz[:n][ok, -1] - Bz[right_z[ok], 0]), initial=0.0)))
+    return worst

@@ -1,0 +1,145 @@
+"""GPU parity: the CUDA path, called through the C ABI (libgmhd.so), against the FP64 oracle.
+
+FP64 path: the oracle restates the reference in FP64 with its operand order; the kernel is built
+without FMA contraction, so results are expected to be identical. The bar written here is the
+spec tolerance, 1e-12 relative per field; the test also records whether they are
+bit-identical. Mixed path: L1(rho) <= 1e-6 relative to FP64 and max|div B| <= 1e-12.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from godunov_mhd_ct_gb300 import workloads as wl  # noqa: E402
+from godunov_mhd_ct_gb300.mesh import BlockMesh  # noqa: E402
+from godunov_mhd_ct_gb300.solver import GodunovImplemGB300  # noqa: E402
+
+from .helpers import (div_b, l1_rel, max_rel_diff, oracle_mesh, oracle_settings, settings,  # noqa: E402
+                      shared_face_mismatch)
+
+pytestmark = pytest.mark.gpu
+TOL_FP64 = 1e-12
+
+
+def _dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _one_step_pair(oracle_lib, mesh, st, U, B, dt, precision="fp64"):
+    impl = GodunovImplemGB300(st, mesh, precision=precision)
+    dU, dB = _dev(U), _dev(B)
+    dU2, dB2 = dU.clone(), dB.clone()
+    impl.do_time_step(dU, dU2, dB, dB2, dt)
+    torch.cuda.synchronize()
+    assert impl.last_status() & ~16 == 0
+    U2g, B2g = dU2.cpu().numpy(), dB2.cpu().numpy()
+    U2o, B2o = oracle_lib.step(oracle_mesh(oracle_lib, mesh), oracle_settings(oracle_lib, st), U, B, dt)
+    n = mesh.n_owned
+    return U2g[:n], B2g[:n], U2o[:n], B2o[:n]
+
+
+@pytest.mark.parametrize("dim,block,level", [(2, (16, 16, 1), 2), (2, (8, 8, 1), 2), (3, (8, 8, 8), 1),
+                                             (3, (16, 8, 8), 1), (3, (4, 4, 4), 1)])
+@pytest.mark.parametrize("riemann", ["HLLD", "HLL", "LLF", "HLLC"])
+@pytest.mark.parametrize("slope_type", [1.0, 2.0])
+def test_single_step_fp64_matches_oracle(oracle_lib, dim, block, level, riemann, slope_type):
+    mesh = BlockMesh.uniform(dim, level=level, block=block)
+    st = settings(gamma0=1.4, slope_type=slope_type, riemann=riemann)
+    U, B = wl.random_smooth(mesh, gamma=1.4, seed=dim * 7 + level)
+    dt = 0.3 * mesh.cell_length()
+    U2g, B2g, U2o, B2o = _one_step_pair(oracle_lib, mesh, st, U, B, dt)
+    assert max_rel_diff(U2g, U2o) <= TOL_FP64
+    assert max_rel_diff(B2g, B2o) <= TOL_FP64
+
+
+@pytest.mark.parametrize("dim,block,level,nsteps", [(2, (16, 16, 1), 3, 200), (3, (32, 32, 32), 1, 5)])
+def test_orszag_tang_run_fp64_matches_oracle(oracle_lib, dim, block, level, nsteps):
+    """Config 0 in full (2D OT 128^2, 200 steps) and a reduced config 1 (3D OT 64^3)."""
+    mesh = BlockMesh.uniform(dim, level=level, block=block)
+    st = settings()
+    U, B = wl.orszag_tang(mesh, gamma=st.gamma0, rho_perturbation=1e-3 if dim == 3 else 0.0, seed=12345)
+    Uo, Bo, dto = oracle_lib.run(oracle_mesh(oracle_lib, mesh), oracle_settings(oracle_lib, st), U, B, nsteps)
+    impl = GodunovImplemGB300(st, mesh, precision="fp64")
+    dU, dB = _dev(U), _dev(B)
+    dU2, dB2 = torch.empty_like(dU), torch.empty_like(dB)
+    dtg, _ = impl.advance(dU, dU2, dB, dB2, nsteps)
+    Ug, Bg = dU.cpu().numpy(), dB.cpu().numpy()
+    assert max_rel_diff(dtg[:, 0], dto) <= TOL_FP64
+    assert max_rel_diff(Ug, Uo) <= TOL_FP64
+    assert max_rel_diff(Bg, Bo) <= TOL_FP64
+    print(f"bit-identical U: {np.array_equal(Ug, Uo)}  B: {np.array_equal(Bg, Bo)}  dt: {np.array_equal(dtg[:, 0], dto)}")
+    assert np.max(np.abs(div_b(mesh, Bg))) <= 1e-12
+    assert shared_face_mismatch(mesh, Bg) == 0.0
+
+
+def test_inv_dt_matches_oracle(oracle_lib):
+    for dim, block, level in [(2, (16, 16, 1), 3), (3, (8, 8, 8), 1)]:
+        mesh = BlockMesh.uniform(dim, level=level, block=block)
+        st = settings()
+        U, B = wl.orszag_tang(mesh, gamma=st.gamma0, rho_perturbation=1e-3, seed=3)
+        impl = GodunovImplemGB300(st, mesh)
+        g = impl.compute_inv_dt(_dev(U), _dev(B))
+        o = oracle_lib.inv_dt(oracle_mesh(oracle_lib, mesh), oracle_settings(oracle_lib, st), U, B)
+        assert g == o
+
+
+def test_step_host_buffers(oracle_lib):
+    mesh = BlockMesh.uniform(2, level=2, block=(16, 16, 1))
+    st = settings()
+    U, B = wl.orszag_tang(mesh, gamma=st.gamma0)
+    impl = GodunovImplemGB300(st, mesh)
+    dt = st.cfl / impl.compute_inv_dt(_dev(U), _dev(B))
+    U2, B2 = impl.step_host(U, B, dt)
+    U2o, B2o = oracle_lib.step(oracle_mesh(oracle_lib, mesh), oracle_settings(oracle_lib, st), U, B, dt)
+    assert max_rel_diff(U2, U2o) <= TOL_FP64 and max_rel_diff(B2, B2o) <= TOL_FP64
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_uniform_state_preserved(dim):
+    mesh = BlockMesh.uniform(dim, level=1 if dim == 3 else 2, block=(16, 16, 16) if dim == 3 else (16, 16, 1))
+    st = settings(gamma0=1.4)
+    U, B = wl.uniform_state(mesh)
+    for prec in ("fp64", "mixed"):
+        impl = GodunovImplemGB300(st, mesh, precision=prec)
+        dU, dB = _dev(U), _dev(B)
+        impl.advance(dU, torch.empty_like(dU), dB, torch.empty_like(dB), 4)
+        assert np.array_equal(dB.cpu().numpy(), B)
+        assert np.max(np.abs(dU.cpu().numpy() - U)) <= (0.0 if prec == "fp64" else 1e-12)
+
+
+@pytest.mark.parametrize("dim,block,level,nsteps", [(2, (16, 16, 1), 3, 100), (3, (32, 32, 32), 1, 20)])
+def test_mixed_precision_accuracy(dim, block, level, nsteps):
+    mesh = BlockMesh.uniform(dim, level=level, block=block)
+    st = settings()
+    U, B = wl.orszag_tang(mesh, gamma=st.gamma0, rho_perturbation=1e-3 if dim == 3 else 0.0, seed=1)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        impl = GodunovImplemGB300(st, mesh, precision=prec)
+        dU, dB = _dev(U), _dev(B)
+        impl.advance(dU, torch.empty_like(dU), dB, torch.empty_like(dB), nsteps)
+        out[prec] = (dU.cpu().numpy(), dB.cpu().numpy())
+    n = mesh.n_owned
+    l1_rho = l1_rel(out["mixed"][0][:n, 0], out["fp64"][0][:n, 0])
+    l1_e = l1_rel(out["mixed"][0][:n, 1], out["fp64"][0][:n, 1])
+    l1_b = l1_rel(out["mixed"][1][:n], out["fp64"][1][:n])
+    divb = float(np.max(np.abs(div_b(mesh, out["mixed"][1]))))
+    print(f"mixed vs fp64 after {nsteps} steps: L1(rho)={l1_rho:.3e} L1(E)={l1_e:.3e} L1(B)={l1_b:.3e} "
+          f"max|divB|={divb:.3e}")
+    assert l1_rho <= 1e-6
+    assert divb <= 1e-12
+    # conservation: total mass unchanged to round-off on a periodic mesh
+    m0 = U[:n, 0].sum()
+    assert abs(out["mixed"][0][:n, 0].sum() - m0) / m0 <= 1e-12
+
+
+def test_alias_and_argument_errors():
+    from godunov_mhd_ct_gb300._native import NativeError
+
+    mesh = BlockMesh.uniform(2, level=1, block=(8, 8, 1))
+    impl = GodunovImplemGB300(settings(), mesh)
+    U, B = wl.uniform_state(mesh)
+    dU, dB = _dev(U), _dev(B)
+    with pytest.raises(NativeError):
+        impl.do_time_step(dU, dU, dB, dB.clone(), 1e-3)
+    with pytest.raises(NativeError):
+        impl.do_time_step(dU, dU.clone(), dB, dB.clone(), float("nan"))
