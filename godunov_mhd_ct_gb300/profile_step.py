@@ -1,0 +1,54 @@
+"""Run W warm-up steps and one measured do_time_step of the fused kernel on a 3D Orszag-Tang
+mesh, for profiling a single launch (e.g. under ncu -k regex:fused_step -s W -c 1).
+
+    python -m godunov_mhd_ct_gb300.profile_step --precision mixed --side-blocks 4 --block 32
+"""
+from __future__ import annotations
+
+import argparse
+import time
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--side-blocks", type=int, default=4)
+    ap.add_argument("--block", type=int, default=32)
+    ap.add_argument("--dim", type=int, default=3, choices=[2, 3])
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--repeat", type=int, default=1)
+    args = ap.parse_args()
+
+    import numpy as np
+    import torch
+
+    from . import workloads as wl
+    from .mesh import BlockMesh
+    from .settings import MHDSettings
+    from .solver import GodunovImplemGB300
+
+    level = int(np.log2(args.side_blocks))
+    blk = (args.block, args.block, args.block if args.dim == 3 else 1)
+    mesh = BlockMesh.uniform(args.dim, level=level, block=blk)
+    st = MHDSettings(gamma0=5.0 / 3.0, cfl=0.5, slope_type=2.0, riemann="HLLD")
+    U, B = wl.orszag_tang(mesh, gamma=st.gamma0, rho_perturbation=1e-3, seed=12345)
+    impl = GodunovImplemGB300(st, mesh, precision=args.precision)
+    dU, dB = torch.from_numpy(U).cuda(), torch.from_numpy(B).cuda()
+    dU2, dB2 = torch.empty_like(dU), torch.empty_like(dB)
+    dt = impl.compute_dt(dU, dB)
+    for _ in range(args.warmup):
+        impl.do_time_step(dU, dU2, dB, dB2, dt)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.repeat):
+        impl.do_time_step(dU, dU2, dB, dB2, dt)
+    torch.cuda.synchronize()
+    el = (time.perf_counter() - t0) / args.repeat
+    cells = mesh.n_owned * mesh.ncell
+    flags = impl.last_status()
+    print(f"{args.precision} {args.dim}D {cells} cells: {el * 1e3:.3f} ms/step, {cells / el / 1e9:.3f} Gcell/s, "
+          f"health flags {flags}")
+
+
+if __name__ == "__main__":
+    main()
