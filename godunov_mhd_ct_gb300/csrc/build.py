@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 UNITS = {
     "step_fp64.cu": ["--fmad=false"],
-    "step_mixed.cu": ["--fmad=true"],
+    "step_mixed.cu": ["--use_fast_math"],
     "gmhd_abi.cu": ["--fmad=false"],
 }
 HEADERS = ["mhd_math.cuh", "fused_step.cuh", "launch.cuh", os.path.join("..", "..", "include", "gmhd.h")]

@@ -15,6 +15,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 
 #include "mhd_math.cuh"
 
@@ -99,9 +100,12 @@ struct Cfg
   static constexpr int OFF_E = OFF_SF + NSF * NS;
   static constexpr int OFF_U1 = OFF_E + NECOMP * NE;
   static constexpr int U1_QH = 5 * NQ;
-  static constexpr int U1_LATE = NECOMP * NM + NFV * NF;
+  // mixed path: the CT curl reads an FP64 copy of the EMFs (EMFD doubles, in units of R)
+  static constexpr int NEMFD = std::is_same<R, double>::value ? 0 : 2 * NECOMP * NM;
+  static constexpr int U1_LATE = NECOMP * NM + NEMFD + NFV * NF;
   static constexpr int OFF_EMF = OFF_U1;
-  static constexpr int OFF_FL = OFF_U1 + NECOMP * NM;
+  static constexpr int OFF_EMFD = OFF_U1 + NECOMP * NM;
+  static constexpr int OFF_FL = OFF_EMFD + NEMFD;
   static constexpr int TOTAL = OFF_U1 + (U1_QH > U1_LATE ? U1_QH : U1_LATE);
   static constexpr size_t SMEM_BYTES = sizeof(R) * (size_t)TOTAL + 64 * sizeof(int);
 
@@ -148,6 +152,9 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
   R *   qh = sm + C::OFF_U1;
   R *   emf = sm + C::OFF_EMF;
   R *   fl = sm + C::OFF_FL;
+  // FP64 EMFs for the CT curl: the R array itself when R is double
+  double * emfd = std::is_same<R, double>::value ? reinterpret_cast<double *>(emf)
+                                                  : reinterpret_cast<double *>(sm + C::OFF_EMFD);
   int * s_nbr = reinterpret_cast<int *>(sm + C::TOTAL);
   __shared__ double       s_red[NT / 32];
   __shared__ unsigned int s_health;
@@ -567,6 +574,8 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       if ((c == 0 && i >= TX) || (c == 1 && j >= TY) || (DIM == 3 && c == 2 && k >= TZ))
       {
         emf[n] = R(0);
+        if constexpr (!std::is_same<R, double>::value)
+          emfd[n] = 0.0;
         continue;
       }
       R qe[4][8];
@@ -721,6 +730,8 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
         }
       }
       emf[n] = val;
+      if constexpr (!std::is_same<R, double>::value)
+        emfd[n] = (double)val;
     }
   }
   __syncthreads();
@@ -728,9 +739,9 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
   // ---- phase 5b: CT update of the tile's faces (ReadEmfAndUpdateFunctor.cpp:58-163) ----------
   // a tile owns faces [0, T) along each normal, plus face T when it ends at the block border
   {
-    const R * Mx = emf;
-    const R * My = emf + (DIM == 3 ? C::NM : 0);
-    const R * Mz = emf + (DIM == 3 ? 2 * C::NM : 0);
+    const double * Mx = emfd;
+    const double * My = emfd + (DIM == 3 ? C::NM : 0);
+    const double * Mz = emfd + (DIM == 3 ? 2 * C::NM : 0);
     const int ex = (x0 + TX == bx) ? 1 : 0;
     const int ey = (y0 + TY == by) ? 1 : 0;
     const int ez = (D3 && z0 + TZ == bz) ? 1 : 0;
@@ -747,11 +758,11 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
         const int64_t g = (x0 + i) + (int64_t)(bx + 1) * ((y0 + j) + (int64_t)by * (z0 + k));
         double        d = 0;
         if constexpr (DIM == 2)
-          d += ((double)Mz[C::mi(i, j + 1, 0)] - (double)Mz[C::mi(i, j, 0)]);
+          d += (Mz[C::mi(i, j + 1, 0)] - Mz[C::mi(i, j, 0)]);
         else
         {
-          d += ((double)Mz[C::mi(i, j + 1, k)] - (double)Mz[C::mi(i, j, k)]);
-          d -= ((double)My[C::mi(i, j, k + 1)] - (double)My[C::mi(i, j, k)]);
+          d += (Mz[C::mi(i, j + 1, k)] - Mz[C::mi(i, j, k)]);
+          d -= (My[C::mi(i, j, k + 1)] - My[C::mi(i, j, k)]);
         }
         B2blk[g] = Bblk[g] + d;
       }
@@ -762,13 +773,13 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
         const int64_t g = a.nfx + (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)(by + 1) * (z0 + k));
         if constexpr (DIM == 2)
         {
-          B2blk[g] = Bblk[g] - ((double)Mz[C::mi(i + 1, j, 0)] - (double)Mz[C::mi(i, j, 0)]);
+          B2blk[g] = Bblk[g] - (Mz[C::mi(i + 1, j, 0)] - Mz[C::mi(i, j, 0)]);
         }
         else
         {
           double d = 0;
-          d += ((double)Mx[C::mi(i, j, k + 1)] - (double)Mx[C::mi(i, j, k)]);
-          d -= ((double)Mz[C::mi(i + 1, j, k)] - (double)Mz[C::mi(i, j, k)]);
+          d += (Mx[C::mi(i, j, k + 1)] - Mx[C::mi(i, j, k)]);
+          d -= (Mz[C::mi(i + 1, j, k)] - Mz[C::mi(i, j, k)]);
           B2blk[g] = Bblk[g] + d;
         }
       }
@@ -778,8 +789,8 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
         const int i = nn % TX, j = (nn / TX) % TY, k = nn / (TX * TY);
         const int64_t g = a.nfx + a.nfy + (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)by * (z0 + k));
         double        d = 0;
-        d += ((double)My[C::mi(i + 1, j, k)] - (double)My[C::mi(i, j, k)]);
-        d -= ((double)Mx[C::mi(i, j + 1, k)] - (double)Mx[C::mi(i, j, k)]);
+        d += (My[C::mi(i + 1, j, k)] - My[C::mi(i, j, k)]);
+        d -= (Mx[C::mi(i, j + 1, k)] - Mx[C::mi(i, j, k)]);
         B2blk[g] = Bblk[g] + d;
       }
     }
@@ -911,53 +922,53 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
 
     if (a.invdt_out)
     {
-      // B2 on the 2 (3D) faces per direction of this cell, recomputed from U/B + EMFs
+      // compute_cfl (ComputeDtMHDFunctor.cpp:86-151) on the updated cell; B2 on the 2 faces per
+      // direction of this cell is recomputed from B and the tile's EMFs
       const R * Mx = emf;
       const R * My = emf + (DIM == 3 ? C::NM : 0);
       const R * Mz = emf + (DIM == 3 ? 2 * C::NM : 0);
-      const double * Bblk = a.B + (int64_t)blk * a.nface;
-      auto bx2 = [&](int ii) {
-        const int64_t g = (x0 + ii) + (int64_t)(bx + 1) * ((y0 + j) + (int64_t)by * (z0 + k));
-        double        d = 0;
-        if constexpr (DIM == 2)
-          d += ((double)Mz[C::mi(ii, j + 1, 0)] - (double)Mz[C::mi(ii, j, 0)]);
-        else
-        {
-          d += ((double)Mz[C::mi(ii, j + 1, k)] - (double)Mz[C::mi(ii, j, k)]);
-          d -= ((double)My[C::mi(ii, j, k + 1)] - (double)My[C::mi(ii, j, k)]);
-        }
-        return Bblk[g] + d;
-      };
-      auto by2 = [&](int jj) {
-        const int64_t g = a.nfx + (x0 + i) + (int64_t)bx * ((y0 + jj) + (int64_t)(by + 1) * (z0 + k));
-        if constexpr (DIM == 2)
-          return Bblk[g] - ((double)Mz[C::mi(i + 1, jj, 0)] - (double)Mz[C::mi(i, jj, 0)]);
-        else
-        {
-          double d = 0;
-          d += ((double)Mx[C::mi(i, jj, k + 1)] - (double)Mx[C::mi(i, jj, k)]);
-          d -= ((double)Mz[C::mi(i + 1, jj, k)] - (double)Mz[C::mi(i, jj, k)]);
-          return Bblk[g] + d;
-        }
-      };
-      auto bz2 = [&](int kk) {
-        const int64_t g = a.nfx + a.nfy + (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)by * (z0 + kk));
-        double        d = 0;
-        d += ((double)My[C::mi(i + 1, j, kk)] - (double)My[C::mi(i, j, kk)]);
-        d -= ((double)Mx[C::mi(i, j + 1, kk)] - (double)Mx[C::mi(i, j, kk)]);
-        return Bblk[g] + d;
-      };
-      // compute_cfl (ComputeDtMHDFunctor.cpp:86-151) on the updated cell
-      const double Ax = 0.5 * (bx2(i) + bx2(i + 1));
-      const double Ay = 0.5 * (by2(j) + by2(j + 1));
-      double       Az;
-      if constexpr (DIM == 3)
-        Az = 0.5 * (bz2(k) + bz2(k + 1));
-      else
-        Az = 0.5 * (u2[c][5] + u2[c][5]);
-      double val;
+      double    val;
       if constexpr (C::EXACT)
       {
+        const double * Bblk = a.B + (int64_t)blk * a.nface;
+        auto bx2 = [&](int ii) {
+          const int64_t g = (x0 + ii) + (int64_t)(bx + 1) * ((y0 + j) + (int64_t)by * (z0 + k));
+          double        d = 0;
+          if constexpr (DIM == 2)
+            d += ((double)Mz[C::mi(ii, j + 1, 0)] - (double)Mz[C::mi(ii, j, 0)]);
+          else
+          {
+            d += ((double)Mz[C::mi(ii, j + 1, k)] - (double)Mz[C::mi(ii, j, k)]);
+            d -= ((double)My[C::mi(ii, j, k + 1)] - (double)My[C::mi(ii, j, k)]);
+          }
+          return Bblk[g] + d;
+        };
+        auto by2 = [&](int jj) {
+          const int64_t g = a.nfx + (x0 + i) + (int64_t)bx * ((y0 + jj) + (int64_t)(by + 1) * (z0 + k));
+          if constexpr (DIM == 2)
+            return Bblk[g] - ((double)Mz[C::mi(i + 1, jj, 0)] - (double)Mz[C::mi(i, jj, 0)]);
+          else
+          {
+            double d = 0;
+            d += ((double)Mx[C::mi(i, jj, k + 1)] - (double)Mx[C::mi(i, jj, k)]);
+            d -= ((double)Mz[C::mi(i + 1, jj, k)] - (double)Mz[C::mi(i, jj, k)]);
+            return Bblk[g] + d;
+          }
+        };
+        auto bz2 = [&](int kk) {
+          const int64_t g = a.nfx + a.nfy + (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)by * (z0 + kk));
+          double        d = 0;
+          d += ((double)My[C::mi(i + 1, j, kk)] - (double)My[C::mi(i, j, kk)]);
+          d -= ((double)Mx[C::mi(i, j + 1, kk)] - (double)Mx[C::mi(i, j, kk)]);
+          return Bblk[g] + d;
+        };
+        const double Ax = 0.5 * (bx2(i) + bx2(i + 1));
+        const double Ay = 0.5 * (by2(j) + by2(j + 1));
+        double       Az;
+        if constexpr (DIM == 3)
+          Az = 0.5 * (bz2(k) + bz2(k + 1));
+        else
+          Az = 0.5 * (u2[c][5] + u2[c][5]);
         const double r = fmax(u2[c][ID], a.smallr);
         const double vx = u2[c][IU] / r, vy = u2[c][IV] / r, vz = u2[c][IW] / r;
         const double eken = 0.5 * (vx * vx + vy * vy + vz * vz);
@@ -979,23 +990,48 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       }
       else
       {
-        const float  r = fmaxf((float)u2[c][ID], (float)a.smallr);
-        const float  ir = 1.0f / r;
-        const float  vx = (float)u2[c][IU] * ir, vy = (float)u2[c][IV] * ir, vz = (float)u2[c][IW] * ir;
-        const float  bxf = (float)Ax, byf = (float)Ay, bzf = (float)Az;
-        const float  ekin = 0.5f * r * (vx * vx + vy * vy + vz * vz);
-        const float  emag = 0.5f * (bxf * bxf + byf * byf + bzf * bzf);
-        const float  g = (float)a.gamma0;
-        const float  p = fmaxf((g - 1.0f) * (float)(u2[c][IP] - (double)emag - (double)ekin), r * (float)a.smallp);
-        const float  b2 = 2.0f * emag;
-        const float  c2 = g * p * ir;
-        const float  d2 = 0.5f * (b2 * ir + c2);
-        const float  cfx = sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * bxf * bxf * ir, 0.0f))) + fabsf(vx);
-        const float  cfy = sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * byf * byf * ir, 0.0f))) + fabsf(vy);
-        float        sum = cfx + cfy;
+        // FP32 estimate: B^n faces from shared memory plus the FP32 EMF curl
+        auto bx2 = [&](int ii) {
+          R d = Mz[C::mi(ii, j + 1, D3 ? k : 0)] - Mz[C::mi(ii, j, D3 ? k : 0)];
+          if constexpr (DIM == 3)
+            d -= My[C::mi(ii, j, k + 1)] - My[C::mi(ii, j, k)];
+          return fbx[C::fxi(ii, j, k)] + d;
+        };
+        auto by2 = [&](int jj) {
+          R d;
+          if constexpr (DIM == 2)
+            d = -(Mz[C::mi(i + 1, jj, 0)] - Mz[C::mi(i, jj, 0)]);
+          else
+            d = (Mx[C::mi(i, jj, k + 1)] - Mx[C::mi(i, jj, k)]) - (Mz[C::mi(i + 1, jj, k)] - Mz[C::mi(i, jj, k)]);
+          return fby[C::fyi(i, jj, k)] + d;
+        };
+        auto bz2 = [&](int kk) {
+          const R d = (My[C::mi(i + 1, j, kk)] - My[C::mi(i, j, kk)]) - (Mx[C::mi(i, j + 1, kk)] - Mx[C::mi(i, j, kk)]);
+          return fbz[C::fzi(i, j, kk)] + d;
+        };
+        const float bxf = 0.5f * (bx2(i) + bx2(i + 1));
+        const float byf = 0.5f * (by2(j) + by2(j + 1));
+        float       bzf;
+        if constexpr (DIM == 3)
+          bzf = 0.5f * (bz2(k) + bz2(k + 1));
+        else
+          bzf = (float)u2[c][5];
+        const float r = fmaxf((float)u2[c][ID], (float)a.smallr);
+        const float ir = 1.0f / r;
+        const float vx = (float)u2[c][IU] * ir, vy = (float)u2[c][IV] * ir, vz = (float)u2[c][IW] * ir;
+        const float ekin = 0.5f * r * (vx * vx + vy * vy + vz * vz);
+        const float emag = 0.5f * (bxf * bxf + byf * byf + bzf * bzf);
+        const float g = ph.gamma0;
+        const float p = fmaxf((g - 1.0f) * ((float)u2[c][IP] - emag - ekin), r * ph.smallp);
+        const float b2 = 2.0f * emag;
+        const float c2 = g * p * ir;
+        const float d2 = 0.5f * (b2 * ir + c2);
+        const float cfx = sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * bxf * bxf * ir, 0.0f))) + fabsf(vx);
+        const float cfy = sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * byf * byf * ir, 0.0f))) + fabsf(vy);
+        float       sum = cfx + cfy;
         if constexpr (DIM == 3)
           sum += sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * bzf * bzf * ir, 0.0f))) + fabsf(vz);
-        val = (double)sum / dx;
+        val = (double)(sum * (float)(1.0 / dx));
       }
       my_invdt = fmax(my_invdt, val);
     }

@@ -4,7 +4,7 @@
 
 namespace gmhd
 {
-using MX_3D_888 = Cfg<float, 3, 8, 8, 8, 256, false>;
+using MX_3D_888 = Cfg<float, 3, 8, 8, 8, 512, false>;
 using MX_3D_444 = Cfg<float, 3, 4, 4, 4, 64, false>;
 using MX_2D_16 = Cfg<float, 2, 16, 16, 1, 256, false>;
 using MX_2D_8 = Cfg<float, 2, 8, 8, 1, 64, false>;
