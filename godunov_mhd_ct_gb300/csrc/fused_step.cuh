@@ -90,23 +90,36 @@ struct Cfg
   static constexpr int NF = NF_X > NF_Y ? (NF_X > NF_Z ? NF_X : NF_Z) : (NF_Y > NF_Z ? NF_Y : NF_Z);
   static constexpr int NFV = DIM == 3 ? 5 : 6; // flux vars used by the update (2D adds Bz)
 
-  // shared-memory carve-up, in units of R
+  // fluxes of all directions (one list: x faces, then y, then z)
+  static constexpr int NFT = NF_X + NF_Y + (DIM == 3 ? NF_Z : 0);
+  // updated face B on [0, T] along each normal (for the fused CFL)
+  static constexpr int NB2X = (TX + 1) * TY * TZ;
+  static constexpr int NB2Y = TX * (TY + 1) * TZ;
+  static constexpr int NB2Z = DIM == 3 ? TX * TY * (TZ + 1) : 0;
+  static constexpr int NB2 = NB2X + NB2Y + NB2Z;
+  // edges of the tile per direction (z edges are the only ones in 2D)
+  static constexpr int NEZ = (TX + 1) * (TY + 1) * TZ;
+  static constexpr int NEY = DIM == 3 ? (TX + 1) * TY * (TZ + 1) : 0;
+  static constexpr int NEX = DIM == 3 ? TX * (TY + 1) * (TZ + 1) : 0;
+  static constexpr int NEDGE = NEZ + NEY + NEX;
+  static constexpr int RPD = (int)(sizeof(double) / sizeof(R)); // R slots per double
+
+  // shared-memory carve-up, in units of R. The union U1 holds the primitives at t^n and the edge
+  // electric field (phases 1-4), then the FP64 EMFs, the face fluxes and the updated faces.
   static constexpr int OFF_FBX = 0;
   static constexpr int OFF_FBY = OFF_FBX + NFBX;
   static constexpr int OFF_FBZ = OFF_FBY + NFBY;
   static constexpr int OFF_SL = OFF_FBZ + NFBZ;
   static constexpr int OFF_Q2 = OFF_SL + NDIR * 8 * NS;
   static constexpr int OFF_SF = OFF_Q2 + 8 * NS;
-  static constexpr int OFF_E = OFF_SF + NSF * NS;
-  static constexpr int OFF_U1 = OFF_E + NECOMP * NE;
-  static constexpr int U1_QH = 5 * NQ;
-  // mixed path: the CT curl reads an FP64 copy of the EMFs (EMFD doubles, in units of R)
-  static constexpr int NEMFD = std::is_same<R, double>::value ? 0 : 2 * NECOMP * NM;
-  static constexpr int U1_LATE = NECOMP * NM + NEMFD + NFV * NF;
-  static constexpr int OFF_EMF = OFF_U1;
-  static constexpr int OFF_EMFD = OFF_U1 + NECOMP * NM;
-  static constexpr int OFF_FL = OFF_EMFD + NEMFD;
-  static constexpr int TOTAL = OFF_U1 + (U1_QH > U1_LATE ? U1_QH : U1_LATE);
+  static constexpr int OFF_U1 = ((OFF_SF + NSF * NS + 1) / 2) * 2; // 8-byte aligned
+  static constexpr int U1_EARLY = 5 * NQ + NECOMP * NE;
+  static constexpr int OFF_E = OFF_U1 + 5 * NQ;
+  static constexpr int OFF_EMFD = OFF_U1;
+  static constexpr int OFF_FL = OFF_EMFD + RPD * NECOMP * NM;
+  static constexpr int OFF_B2 = OFF_FL + NFV * NFT;
+  static constexpr int U1_LATE = RPD * NECOMP * NM + NFV * NFT + NB2;
+  static constexpr int TOTAL = OFF_U1 + (U1_EARLY > U1_LATE ? U1_EARLY : U1_LATE);
   static constexpr size_t SMEM_BYTES = sizeof(R) * (size_t)TOTAL + 64 * sizeof(int);
 
   static constexpr int NCELL = TX * TY * TZ;
@@ -148,13 +161,11 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
   R *   sl = sm + C::OFF_SL;
   R *   q2 = sm + C::OFF_Q2;
   R *   sf = sm + C::OFF_SF;
-  R *   ee = sm + C::OFF_E;
-  R *   qh = sm + C::OFF_U1;
-  R *   emf = sm + C::OFF_EMF;
-  R *   fl = sm + C::OFF_FL;
-  // FP64 EMFs for the CT curl: the R array itself when R is double
-  double * emfd = std::is_same<R, double>::value ? reinterpret_cast<double *>(emf)
-                                                  : reinterpret_cast<double *>(sm + C::OFF_EMFD);
+  R *      ee = sm + C::OFF_E;
+  R *      qh = sm + C::OFF_U1;
+  double * emfd = reinterpret_cast<double *>(sm + C::OFF_EMFD); // FP64 EMFs for the CT curl
+  R *      fl = sm + C::OFF_FL;
+  R *      b2s = sm + C::OFF_B2;
   int * s_nbr = reinterpret_cast<int *>(sm + C::TOTAL);
   __shared__ double       s_red[NT / 32];
   __shared__ unsigned int s_health;
@@ -236,7 +247,7 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
     const int nb = owner(ox, oy, oz);
     R         v = R(0);
     if (nb >= 0)
-      v = (R)a.B[(int64_t)nb * a.nface + (fi - ox * bx) + (int64_t)(bx + 1) * ((cj - oy * by) + (int64_t)by * (ck - oz * bz))];
+      v = to_r<R>(a.B[(int64_t)nb * a.nface + (fi - ox * bx) + (int64_t)(bx + 1) * ((cj - oy * by) + (int64_t)by * (ck - oz * bz))]);
     fbx[n] = v;
   }
   for (int n = tid; n < C::NFBY; n += NT)
@@ -249,7 +260,7 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
     const int nb = owner(ox, oy, oz);
     R         v = R(0);
     if (nb >= 0)
-      v = (R)a.B[(int64_t)nb * a.nface + a.nfx + (ci - ox * bx) + (int64_t)bx * ((fj - oy * by) + (int64_t)(by + 1) * (ck - oz * bz))];
+      v = to_r<R>(a.B[(int64_t)nb * a.nface + a.nfx + (ci - ox * bx) + (int64_t)bx * ((fj - oy * by) + (int64_t)(by + 1) * (ck - oz * bz))]);
     fby[n] = v;
   }
   for (int n = tid; n < C::NFBZ; n += NT)
@@ -262,7 +273,7 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
     const int nb = owner(ox, oy, oz);
     R         v = R(0);
     if (nb >= 0)
-      v = (R)a.B[(int64_t)nb * a.nface + a.nfx + a.nfy + (ci - ox * bx) + (int64_t)bx * ((cj - oy * by) + (int64_t)by * (fk - oz * bz))];
+      v = to_r<R>(a.B[(int64_t)nb * a.nface + a.nfx + a.nfy + (ci - ox * bx) + (int64_t)bx * ((cj - oy * by) + (int64_t)by * (fk - oz * bz))]);
     fbz[n] = v;
   }
   __syncthreads();
@@ -310,12 +321,12 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       const R Bxc = R(0.5) * (fbx[C::fxi(i, j, k)] + fbx[C::fxi(i + 1, j, k)]);
       const R Byc = R(0.5) * (fby[C::fyi(i, j, k)] + fby[C::fyi(i, j + 1, k)]);
       const R Bzc = D3 ? R(0.5) * (fbz[C::fzi(i, j, k)] + fbz[C::fzi(i, j, k + 1)]) : fbz[C::fzi(i, j, 0)];
-      const R r = rmax<R>((R)u[ID], ph.smallr);
+      const R r = rmax<R>(to_r<R>(u[ID]), ph.smallr);
       const R ir = R(1) / r;
-      const R vx = (R)u[IU] * ir, vy = (R)u[IV] * ir, vz = (R)u[IW] * ir;
+      const R vx = to_r<R>(u[IU]) * ir, vy = to_r<R>(u[IV]) * ir, vz = to_r<R>(u[IW]) * ir;
       const R ekin = R(0.5) * r * (vx * vx + vy * vy + vz * vz);
       const R emag = R(0.5) * (Bxc * Bxc + Byc * Byc + Bzc * Bzc);
-      R       p = (ph.gamma0 - R(1)) * ((R)u[IP] - emag - ekin);
+      R       p = (ph.gamma0 - R(1)) * (to_r<R>(u[IP]) - emag - ekin);
       if (ekin + emag > R(4) * p * (R(1) / (ph.gamma0 - R(1))))
       {
         // cancellation-prone cell: recover in FP64 from the FP64 state and face values
@@ -560,276 +571,211 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
     return slope1<R>(fval(c, i, j, k), fval(c, i + di, j + dj, k + dk), fval(c, i - di, j - dj, k - dk), ph.slope_type);
   };
 
-  // ---- phase 5: edge EMFs (ComputeEmfAndStoreFunctor.cpp:103-590) + border averaging ---------
+  // ---- phase 5: one work list of edge EMFs (ComputeEmfAndStoreFunctor.cpp:103-590, with the
+  // border averaging of CorrectEmfAtBlockBorderFunctor) and face fluxes of all directions
+  // (ComputeHydroFluxesAndStoreFunctor.cpp:335-503), balanced over the CTA's threads
+  for (int n = tid; n < C::NEDGE + C::NFT; n += NT)
   {
-    constexpr int NEDGE = C::NECOMP * C::NM;
-    for (int n = tid; n < NEDGE; n += NT)
+    if (n < C::NEDGE)
     {
-      const int c = DIM == 3 ? n / C::NM : 2; // edge direction
-      const int m = n - (DIM == 3 ? c : 0) * C::NM;
-      const int i = m % C::MX;
-      const int j = (m / C::MX) % C::MY;
-      const int k = D3 ? m / (C::MX * C::MY) : 0;
-      // edge masks: an edge along c exists for cell index < T along c
-      if ((c == 0 && i >= TX) || (c == 1 && j >= TY) || (DIM == 3 && c == 2 && k >= TZ))
+      int c, i, j, k;
+      if (n < C::NEZ)
       {
-        emf[n] = R(0);
-        if constexpr (!std::is_same<R, double>::value)
-          emfd[n] = 0.0;
-        continue;
+        c = 2;
+        i = n % (TX + 1);
+        j = (n / (TX + 1)) % (TY + 1);
+        k = n / ((TX + 1) * (TY + 1));
       }
-      R qe[4][8];
-      // states at t^{n+1/2} reconstructed to the edge from the 4 surrounding cells
-      auto recon = [&](int is, int js, int ks, int loc, int dir0, int dir1, R * q) {
-        const int sn = C::si(is, js, ks);
-#pragma unroll
-        for (int v = 0; v < 8; ++v)
-          q[v] = q2[v * C::NS + sn];
-        int sd0 = 1, sd1 = 1, sb0 = 1, sb1 = 1;
-        int i0 = is, j0 = js, k0 = ks, i1 = is, j1 = js, k1 = ks;
-        // loc: 0 = LB, 1 = RT, 2 = RB, 3 = LT
-        if (loc == 0)
-        {
-          sd0 = -1; sd1 = -1; sb0 = -1; sb1 = -1;
-        }
-        else if (loc == 1)
-        {
-          i0 += dir0 == 0; j0 += dir0 == 1; k0 += dir0 == 2;
-          i1 += dir1 == 0; j1 += dir1 == 1; k1 += dir1 == 2;
-        }
-        else if (loc == 2)
-        {
-          i0 += dir0 == 0; j0 += dir0 == 1; k0 += dir0 == 2;
-          sd1 = -1; sb0 = -1;
-        }
-        else
-        {
-          i1 += dir1 == 0; j1 += dir1 == 1; k1 += dir1 == 2;
-          sd0 = -1; sb1 = -1;
-        }
-        const R * S0 = sl + dir0 * 8 * C::NS;
-        const R * S1 = sl + dir1 * 8 * C::NS;
-        const R   f0 = (R)sd0, f1 = (R)sd1;
-        if constexpr (DIM == 2)
-        {
-          // reconstruct_state_2d_at_edge (dir0 = X, dir1 = Y)
-          R A = fbx[C::fxi(i0, j0, 0)];
-          R Bv = fby[C::fyi(i1, j1, 0)];
-          A += sf[0 * C::NS + C::si(i0, j0, 0)];
-          Bv += sf[1 * C::NS + C::si(i1, j1, 0)];
-          const R dAy = fslope(0, i0, j0, 0, 1);
-          const R dBx = fslope(1, i1, j1, 0, 0);
-#pragma unroll
-          for (int v = 0; v < 5; ++v)
-            q[v] += R(0.5) * (f0 * S0[v * C::NS + sn] + f1 * S1[v * C::NS + sn]);
-          q[IA] = A + R(0.5) * ((R)sb0 * dAy);
-          q[IB] = Bv + R(0.5) * ((R)sb1 * dBx);
-          q[IC] += R(0.5) * (f0 * S0[IC * C::NS + sn] + f1 * S1[IC * C::NS + sn]);
-        }
-        else
-        {
-          // reconstruct_state_3d_at_edge, with the reference's branch order for IA/IB/IC
-          R B0 = fval(dir0, i0, j0, k0);
-          R B1 = fval(dir1, i1, j1, k1);
-          B0 += sf[dir0 * C::NS + C::si(i0, j0, k0)];
-          B1 += sf[dir1 * C::NS + C::si(i1, j1, k1)];
-          const R dB0d1 = fslope(dir0, i0, j0, k0, dir1);
-          const R dB1d0 = fslope(dir1, i1, j1, k1, dir0);
-          auto    h = [&](int v) { return R(0.5) * (f0 * S0[v * C::NS + sn] + f1 * S1[v * C::NS + sn]); };
-#pragma unroll
-          for (int v = 0; v < 5; ++v)
-            q[v] += h(v);
-          if (dir0 == 0)
-            q[IA] = B0 + R(0.5) * ((R)sb0 * dB0d1);
-          else
-            q[IA] += h(IA);
-          if (dir0 == 1)
-            q[IB] = B0 + R(0.5) * ((R)sb0 * dB0d1);
-          else
-            q[IB] += h(IB);
-          if (dir1 == 1)
-            q[IB] = B1 + R(0.5) * ((R)sb1 * dB1d0);
-          else
-            q[IB] += h(IB);
-          if (dir1 == 2)
-            q[IC] = B1 + R(0.5) * ((R)sb1 * dB1d0);
-          else
-            q[IC] += h(IC);
-        }
-        q[ID] = rmax<R>(ph.smallr, q[ID]);
-        q[IP] = rmax<R>(ph.smallp * q[ID], q[IP]);
-      };
-      R val;
-      if (c == 2)
+      else if (n < C::NEZ + C::NEY)
       {
-        recon(i, j, k, 0, 0, 1, qe[ELB]);
-        recon(i - 1, j - 1, k, 1, 0, 1, qe[ERT]);
-        recon(i - 1, j, k, 2, 0, 1, qe[ERB]);
-        recon(i, j - 1, k, 3, 0, 1, qe[ELT]);
-        val = edge_emf<R>(qe, 2, ph) * dtdx;
-      }
-      else if (c == 1)
-      {
-        recon(i, j, k, 0, 0, 2, qe[ELB]);
-        recon(i - 1, j, k - 1, 1, 0, 2, qe[ERT]);
-        // the reference swaps the RB and LT states of y edges
-        recon(i - 1, j, k, 2, 0, 2, qe[ELT]);
-        recon(i, j, k - 1, 3, 0, 2, qe[ERB]);
-        val = edge_emf<R>(qe, 1, ph) * dtdx;
+        const int m = n - C::NEZ;
+        c = 1;
+        i = m % (TX + 1);
+        j = (m / (TX + 1)) % TY;
+        k = m / ((TX + 1) * TY);
       }
       else
       {
-        recon(i, j, k, 0, 1, 2, qe[ELB]);
-        recon(i, j - 1, k - 1, 1, 1, 2, qe[ERT]);
-        recon(i, j - 1, k, 2, 1, 2, qe[ERB]);
-        recon(i, j, k - 1, 3, 1, 2, qe[ELT]);
-        val = edge_emf<R>(qe, 0, ph) * dtdx;
+        const int m = n - C::NEZ - C::NEY;
+        c = 0;
+        i = m % TX;
+        j = (m / TX) % (TY + 1);
+        k = m / (TX * (TY + 1));
       }
-      // CorrectEmfAtBlockBorderFunctor (uniform level): an edge on a line where four blocks meet
-      // is averaged with its sibling copies (self first, then the non-outside siblings). On a
-      // conforming mesh every copy is computed from identical data, so the sum is of equal terms.
-      {
-        const int t0 = c == 0 ? 1 : 0;
-        const int t1 = c == 2 ? 1 : 2;
-        const int gidx[3] = {x0 + i, y0 + j, z0 + k};
-        const int bsz[3] = {bx, by, bz};
-        const int v0 = gidx[t0] == 0 ? -1 : (gidx[t0] == bsz[t0] ? 1 : 0);
-        const int v1 = (DIM == 2 && t1 == 2) ? 0 : (gidx[t1] == 0 ? -1 : (gidx[t1] == bsz[t1] ? 1 : 0));
-        if (v0 != 0 && v1 != 0)
-        {
-          int o0[3] = {0, 0, 0}, o1[3] = {0, 0, 0}, o2[3] = {0, 0, 0};
-          o0[t0] = v0;
-          o1[t1] = v1;
-          o2[t0] = v0;
-          o2[t1] = v1;
-          const int s0 = s_nbr[nb_slot(o0[0], o0[1], o0[2])];
-          const int s1 = s_nbr[nb_slot(o1[0], o1[1], o1[2])];
-          const int s2 = s_nbr[nb_slot(o2[0], o2[1], o2[2])];
-          if (s0 >= 0 && s1 >= 0 && s2 >= 0)
+        R qe[4][8];
+        // states at t^{n+1/2} reconstructed to the edge from the 4 surrounding cells
+        auto recon = [&](int is, int js, int ks, int loc, int dir0, int dir1, R * q) {
+          const int sn = C::si(is, js, ks);
+  #pragma unroll
+          for (int v = 0; v < 8; ++v)
+            q[v] = q2[v * C::NS + sn];
+          int sd0 = 1, sd1 = 1, sb0 = 1, sb1 = 1;
+          int i0 = is, j0 = js, k0 = ks, i1 = is, j1 = js, k1 = ks;
+          // loc: 0 = LB, 1 = RT, 2 = RB, 3 = LT
+          if (loc == 0)
           {
-            R   acc = R(0);
-            int count = 1;
-            acc += val;
-            if (s0 < a.n_owned)
+            sd0 = -1; sd1 = -1; sb0 = -1; sb1 = -1;
+          }
+          else if (loc == 1)
+          {
+            i0 += dir0 == 0; j0 += dir0 == 1; k0 += dir0 == 2;
+            i1 += dir1 == 0; j1 += dir1 == 1; k1 += dir1 == 2;
+          }
+          else if (loc == 2)
+          {
+            i0 += dir0 == 0; j0 += dir0 == 1; k0 += dir0 == 2;
+            sd1 = -1; sb0 = -1;
+          }
+          else
+          {
+            i1 += dir1 == 0; j1 += dir1 == 1; k1 += dir1 == 2;
+            sd0 = -1; sb1 = -1;
+          }
+          const R * S0 = sl + dir0 * 8 * C::NS;
+          const R * S1 = sl + dir1 * 8 * C::NS;
+          const R   f0 = (R)sd0, f1 = (R)sd1;
+          if constexpr (DIM == 2)
+          {
+            // reconstruct_state_2d_at_edge (dir0 = X, dir1 = Y)
+            R A = fbx[C::fxi(i0, j0, 0)];
+            R Bv = fby[C::fyi(i1, j1, 0)];
+            A += sf[0 * C::NS + C::si(i0, j0, 0)];
+            Bv += sf[1 * C::NS + C::si(i1, j1, 0)];
+            const R dAy = fslope(0, i0, j0, 0, 1);
+            const R dBx = fslope(1, i1, j1, 0, 0);
+  #pragma unroll
+            for (int v = 0; v < 5; ++v)
+              q[v] += R(0.5) * (f0 * S0[v * C::NS + sn] + f1 * S1[v * C::NS + sn]);
+            q[IA] = A + R(0.5) * ((R)sb0 * dAy);
+            q[IB] = Bv + R(0.5) * ((R)sb1 * dBx);
+            q[IC] += R(0.5) * (f0 * S0[IC * C::NS + sn] + f1 * S1[IC * C::NS + sn]);
+          }
+          else
+          {
+            // reconstruct_state_3d_at_edge, with the reference's branch order for IA/IB/IC
+            R B0 = fval(dir0, i0, j0, k0);
+            R B1 = fval(dir1, i1, j1, k1);
+            B0 += sf[dir0 * C::NS + C::si(i0, j0, k0)];
+            B1 += sf[dir1 * C::NS + C::si(i1, j1, k1)];
+            const R dB0d1 = fslope(dir0, i0, j0, k0, dir1);
+            const R dB1d0 = fslope(dir1, i1, j1, k1, dir0);
+            auto    h = [&](int v) { return R(0.5) * (f0 * S0[v * C::NS + sn] + f1 * S1[v * C::NS + sn]); };
+  #pragma unroll
+            for (int v = 0; v < 5; ++v)
+              q[v] += h(v);
+            if (dir0 == 0)
+              q[IA] = B0 + R(0.5) * ((R)sb0 * dB0d1);
+            else
+              q[IA] += h(IA);
+            if (dir0 == 1)
+              q[IB] = B0 + R(0.5) * ((R)sb0 * dB0d1);
+            else
+              q[IB] += h(IB);
+            if (dir1 == 1)
+              q[IB] = B1 + R(0.5) * ((R)sb1 * dB1d0);
+            else
+              q[IB] += h(IB);
+            if (dir1 == 2)
+              q[IC] = B1 + R(0.5) * ((R)sb1 * dB1d0);
+            else
+              q[IC] += h(IC);
+          }
+          q[ID] = rmax<R>(ph.smallr, q[ID]);
+          q[IP] = rmax<R>(ph.smallp * q[ID], q[IP]);
+        };
+        R val;
+        if (c == 2)
+        {
+          recon(i, j, k, 0, 0, 1, qe[ELB]);
+          recon(i - 1, j - 1, k, 1, 0, 1, qe[ERT]);
+          recon(i - 1, j, k, 2, 0, 1, qe[ERB]);
+          recon(i, j - 1, k, 3, 0, 1, qe[ELT]);
+          val = edge_emf<R>(qe, 2, ph) * dtdx;
+        }
+        else if (c == 1)
+        {
+          recon(i, j, k, 0, 0, 2, qe[ELB]);
+          recon(i - 1, j, k - 1, 1, 0, 2, qe[ERT]);
+          // the reference swaps the RB and LT states of y edges
+          recon(i - 1, j, k, 2, 0, 2, qe[ELT]);
+          recon(i, j, k - 1, 3, 0, 2, qe[ERB]);
+          val = edge_emf<R>(qe, 1, ph) * dtdx;
+        }
+        else
+        {
+          recon(i, j, k, 0, 1, 2, qe[ELB]);
+          recon(i, j - 1, k - 1, 1, 1, 2, qe[ERT]);
+          recon(i, j - 1, k, 2, 1, 2, qe[ERB]);
+          recon(i, j, k - 1, 3, 1, 2, qe[ELT]);
+          val = edge_emf<R>(qe, 0, ph) * dtdx;
+        }
+        // CorrectEmfAtBlockBorderFunctor (uniform level): an edge on a line where four blocks meet
+        // is averaged with its sibling copies (self first, then the non-outside siblings). On a
+        // conforming mesh every copy is computed from identical data, so the sum is of equal terms.
+        {
+          const int t0 = c == 0 ? 1 : 0;
+          const int t1 = c == 2 ? 1 : 2;
+          const int gidx[3] = {x0 + i, y0 + j, z0 + k};
+          const int bsz[3] = {bx, by, bz};
+          const int v0 = gidx[t0] == 0 ? -1 : (gidx[t0] == bsz[t0] ? 1 : 0);
+          const int v1 = (DIM == 2 && t1 == 2) ? 0 : (gidx[t1] == 0 ? -1 : (gidx[t1] == bsz[t1] ? 1 : 0));
+          if (v0 != 0 && v1 != 0)
+          {
+            int o0[3] = {0, 0, 0}, o1[3] = {0, 0, 0}, o2[3] = {0, 0, 0};
+            o0[t0] = v0;
+            o1[t1] = v1;
+            o2[t0] = v0;
+            o2[t1] = v1;
+            const int s0 = s_nbr[nb_slot(o0[0], o0[1], o0[2])];
+            const int s1 = s_nbr[nb_slot(o1[0], o1[1], o1[2])];
+            const int s2 = s_nbr[nb_slot(o2[0], o2[1], o2[2])];
+            if (s0 >= 0 && s1 >= 0 && s2 >= 0)
             {
+              R   acc = R(0);
+              int count = 1;
               acc += val;
-              count++;
+              if (s0 < a.n_owned)
+              {
+                acc += val;
+                count++;
+              }
+              if (s1 < a.n_owned)
+              {
+                acc += val;
+                count++;
+              }
+              if (s2 < a.n_owned)
+              {
+                acc += val;
+                count++;
+              }
+              val = acc / (R)count;
             }
-            if (s1 < a.n_owned)
-            {
-              acc += val;
-              count++;
-            }
-            if (s2 < a.n_owned)
-            {
-              acc += val;
-              count++;
-            }
-            val = acc / (R)count;
           }
         }
-      }
-      emf[n] = val;
-      if constexpr (!std::is_same<R, double>::value)
-        emfd[n] = (double)val;
+        emfd[(DIM == 3 ? c : 0) * C::NM + C::mi(i, j, k)] = to_d<R>(val);
     }
-  }
-  __syncthreads();
-
-  // ---- phase 5b: CT update of the tile's faces (ReadEmfAndUpdateFunctor.cpp:58-163) ----------
-  // a tile owns faces [0, T) along each normal, plus face T when it ends at the block border
-  {
-    const double * Mx = emfd;
-    const double * My = emfd + (DIM == 3 ? C::NM : 0);
-    const double * Mz = emfd + (DIM == 3 ? 2 * C::NM : 0);
-    const int ex = (x0 + TX == bx) ? 1 : 0;
-    const int ey = (y0 + TY == by) ? 1 : 0;
-    const int ez = (D3 && z0 + TZ == bz) ? 1 : 0;
-    const int nfx_t = (TX + ex) * TY * TZ;
-    const int nfy_t = TX * (TY + ey) * TZ;
-    const int nfz_t = D3 ? TX * TY * (TZ + ez) : 0;
-    double *  B2blk = a.B2 + (int64_t)blk * a.nface;
-    const double * Bblk = a.B + (int64_t)blk * a.nface;
-    for (int n = tid; n < nfx_t + nfy_t + nfz_t; n += NT)
+    else
     {
-      if (n < nfx_t)
+      // face flux: left state from cell i-1, right state from cell i along dir
+      const int m = n - C::NEDGE;
+      int       dir, l, fx_n, fy_n;
+      if (m < C::NF_X)
       {
-        const int i = n % (TX + ex), j = (n / (TX + ex)) % TY, k = n / ((TX + ex) * TY);
-        const int64_t g = (x0 + i) + (int64_t)(bx + 1) * ((y0 + j) + (int64_t)by * (z0 + k));
-        double        d = 0;
-        if constexpr (DIM == 2)
-          d += (Mz[C::mi(i, j + 1, 0)] - Mz[C::mi(i, j, 0)]);
-        else
-        {
-          d += (Mz[C::mi(i, j + 1, k)] - Mz[C::mi(i, j, k)]);
-          d -= (My[C::mi(i, j, k + 1)] - My[C::mi(i, j, k)]);
-        }
-        B2blk[g] = Bblk[g] + d;
+        dir = 0; l = m; fx_n = TX + 1; fy_n = TY;
       }
-      else if (n < nfx_t + nfy_t)
+      else if (m < C::NF_X + C::NF_Y)
       {
-        const int nn = n - nfx_t;
-        const int i = nn % TX, j = (nn / TX) % (TY + ey), k = nn / (TX * (TY + ey));
-        const int64_t g = a.nfx + (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)(by + 1) * (z0 + k));
-        if constexpr (DIM == 2)
-        {
-          B2blk[g] = Bblk[g] - (Mz[C::mi(i + 1, j, 0)] - Mz[C::mi(i, j, 0)]);
-        }
-        else
-        {
-          double d = 0;
-          d += (Mx[C::mi(i, j, k + 1)] - Mx[C::mi(i, j, k)]);
-          d -= (Mz[C::mi(i + 1, j, k)] - Mz[C::mi(i, j, k)]);
-          B2blk[g] = Bblk[g] + d;
-        }
+        dir = 1; l = m - C::NF_X; fx_n = TX; fy_n = TY + 1;
       }
       else
       {
-        const int nn = n - nfx_t - nfy_t;
-        const int i = nn % TX, j = (nn / TX) % TY, k = nn / (TX * TY);
-        const int64_t g = a.nfx + a.nfy + (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)by * (z0 + k));
-        double        d = 0;
-        d += (My[C::mi(i + 1, j, k)] - My[C::mi(i, j, k)]);
-        d -= (Mx[C::mi(i, j + 1, k)] - Mx[C::mi(i, j, k)]);
-        B2blk[g] = Bblk[g] + d;
+        dir = 2; l = m - C::NF_X - C::NF_Y; fx_n = TX; fy_n = TY;
       }
-    }
-  }
-
-  // ---- phase 6: face fluxes per direction + conservative update -------------------------------
-  // (ComputeHydroFluxesAndStoreFunctor.cpp:335-503, ReadFluxesAndConservativeUpdateFunctor.cpp:240-436)
-  double u2[C::CPT][C::NFV];
-  R      dU[C::CPT][C::NFV];
-#pragma unroll
-  for (int c = 0; c < C::CPT; ++c)
-  {
-    const int n = tid + c * NT;
-    if (n < C::NCELL)
-    {
-      const int i = n % TX, j = (n / TX) % TY, k = n / (TX * TY);
-      const int64_t cell = (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)by * (z0 + k));
-#pragma unroll
-      for (int v = 0; v < 5; ++v)
-        u2[c][v] = a.U[((int64_t)blk * 5 + v) * a.ncell + cell];
-      if constexpr (DIM == 2)
-        u2[c][5] = a.B[(int64_t)blk * a.nface + a.nfx + a.nfy + cell];
-    }
-#pragma unroll
-    for (int v = 0; v < C::NFV; ++v)
-      dU[c][v] = R(0);
-  }
-
-#pragma unroll 1
-  for (int dir = 0; dir < DIM; ++dir)
-  {
-    const int fx_n = TX + (dir == 0), fy_n = TY + (dir == 1), fz_n = TZ + (dir == 2 && D3);
-    const int nfl = fx_n * fy_n * fz_n;
-    const int di = dir == 0, dj = dir == 1, dk = dir == 2;
-    const int ivel = dir == 0 ? IU : (dir == 1 ? IV : IW);
-    const int imag = dir == 0 ? IA : (dir == 1 ? IB : IC);
-    for (int n = tid; n < nfl; n += NT)
-    {
-      const int i = n % fx_n, j = (n / fx_n) % fy_n, k = n / (fx_n * fy_n);
+      const int i = l % fx_n, j = (l / fx_n) % fy_n, k = l / (fx_n * fy_n);
+      const int di = dir == 0, dj = dir == 1, dk = dir == 2;
+      const int ivel = dir == 0 ? IU : (dir == 1 ? IV : IW);
+      const int imag = dir == 0 ? IA : (dir == 1 ? IB : IC);
       const int snL = C::si(i - di, j - dj, k - dk);
       const int snR = C::si(i, j, k);
       const R * S = sl + dir * 8 * C::NS;
@@ -864,116 +810,164 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       }
 #pragma unroll
       for (int v = 0; v < 5; ++v)
-        fl[v * C::NF + n] = flux[v] * dtdx;
+        fl[v * C::NFT + m] = flux[v] * dtdx;
       if constexpr (DIM == 2)
-        fl[5 * C::NF + n] = flux[IC] * dtdx;
+        fl[5 * C::NFT + m] = flux[IC] * dtdx;
     }
-    __syncthreads();
-#pragma unroll
-    for (int c = 0; c < C::CPT; ++c)
-    {
-      const int n = tid + c * NT;
-      if (n < C::NCELL)
-      {
-        const int i = n % TX, j = (n / TX) % TY, k = n / (TX * TY);
-        const int fL = i + fx_n * (j + fy_n * k);
-        const int fR = (i + di) + fx_n * ((j + dj) + fy_n * (k + dk));
-#pragma unroll
-        for (int v = 0; v < C::NFV; ++v)
-        {
-          R acc = R(0);
-          acc = acc + fl[v * C::NF + fL];
-          acc = acc - fl[v * C::NF + fR];
-          if constexpr (C::EXACT)
-            u2[c][v] += (double)acc;
-          else
-            dU[c][v] += acc;
-        }
-      }
-    }
-    __syncthreads();
   }
+  __syncthreads();
 
-  // ---- phase 7: write U2 (and 2D Bz), fused CFL of the new state -----------------------------
+  // ---- phase 6: CT update (ReadEmfAndUpdateFunctor.cpp:58-163) on faces [0, T] along each
+  // normal; a tile writes faces [0, T) and face T when it ends at the block border, and keeps all
+  // of them in shared memory for the CFL of the updated cells
+  {
+    const double * Mx = emfd;
+    const double * My = emfd + (DIM == 3 ? C::NM : 0);
+    const double * Mz = emfd + (DIM == 3 ? 2 * C::NM : 0);
+    const bool     ex = (x0 + TX == bx), ey = (y0 + TY == by), ez = (z0 + TZ == bz);
+    double *       B2blk = a.B2 + (int64_t)blk * a.nface;
+    const double * Bblk = a.B + (int64_t)blk * a.nface;
+    for (int n = tid; n < C::NB2; n += NT)
+    {
+      int64_t g;
+      double  bnew;
+      bool    owned;
+      if (n < C::NB2X)
+      {
+        const int i = n % (TX + 1), j = (n / (TX + 1)) % TY, k = n / ((TX + 1) * TY);
+        g = (x0 + i) + (int64_t)(bx + 1) * ((y0 + j) + (int64_t)by * (z0 + k));
+        double d = 0;
+        if constexpr (DIM == 2)
+          d += (Mz[C::mi(i, j + 1, 0)] - Mz[C::mi(i, j, 0)]);
+        else
+        {
+          d += (Mz[C::mi(i, j + 1, k)] - Mz[C::mi(i, j, k)]);
+          d -= (My[C::mi(i, j, k + 1)] - My[C::mi(i, j, k)]);
+        }
+        bnew = Bblk[g] + d;
+        owned = i < TX || ex;
+      }
+      else if (n < C::NB2X + C::NB2Y)
+      {
+        const int nn = n - C::NB2X;
+        const int i = nn % TX, j = (nn / TX) % (TY + 1), k = nn / (TX * (TY + 1));
+        g = a.nfx + (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)(by + 1) * (z0 + k));
+        if constexpr (DIM == 2)
+          bnew = Bblk[g] - (Mz[C::mi(i + 1, j, 0)] - Mz[C::mi(i, j, 0)]);
+        else
+        {
+          double d = 0;
+          d += (Mx[C::mi(i, j, k + 1)] - Mx[C::mi(i, j, k)]);
+          d -= (Mz[C::mi(i + 1, j, k)] - Mz[C::mi(i, j, k)]);
+          bnew = Bblk[g] + d;
+        }
+        owned = j < TY || ey;
+      }
+      else
+      {
+        const int nn = n - C::NB2X - C::NB2Y;
+        const int i = nn % TX, j = (nn / TX) % TY, k = nn / (TX * TY);
+        g = a.nfx + a.nfy + (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)by * (z0 + k));
+        double d = 0;
+        d += (My[C::mi(i + 1, j, k)] - My[C::mi(i, j, k)]);
+        d -= (Mx[C::mi(i, j + 1, k)] - Mx[C::mi(i, j, k)]);
+        bnew = Bblk[g] + d;
+        owned = k < TZ || ez;
+      }
+      if (owned)
+        B2blk[g] = bnew;
+      b2s[n] = to_r<R>(bnew);
+    }
+  }
+  __syncthreads();
+
+  // ---- phase 7: conservative update (ReadFluxesAndConservativeUpdateFunctor.cpp:240-436),
+  // write U2 (and 2D Bz), fused CFL of the new state (ComputeDtMHDFunctor.cpp:86-151) ----------
   double my_invdt = 0.0;
-#pragma unroll
+#pragma unroll 1
   for (int c = 0; c < C::CPT; ++c)
   {
     const int n = tid + c * NT;
     if (n >= C::NCELL)
       continue;
-    const int i = n % TX, j = (n / TX) % TY, k = n / (TX * TY);
+    const int     i = n % TX, j = (n / TX) % TY, k = n / (TX * TY);
     const int64_t cell = (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)by * (z0 + k));
+    double        u2[C::NFV];
+#pragma unroll
+    for (int v = 0; v < 5; ++v)
+      u2[v] = a.U[((int64_t)blk * 5 + v) * a.ncell + cell];
+    if constexpr (DIM == 2)
+      u2[5] = a.B[(int64_t)blk * a.nface + a.nfx + a.nfy + cell];
+    R dU[C::NFV];
+#pragma unroll
+    for (int v = 0; v < C::NFV; ++v)
+      dU[v] = R(0);
+#pragma unroll
+    for (int dir = 0; dir < DIM; ++dir)
+    {
+      int fL, fR;
+      if (dir == 0)
+      {
+        fL = i + (TX + 1) * (j + TY * k);
+        fR = fL + 1;
+      }
+      else if (dir == 1)
+      {
+        fL = C::NF_X + i + TX * (j + (TY + 1) * k);
+        fR = fL + TX;
+      }
+      else
+      {
+        fL = C::NF_X + C::NF_Y + i + TX * (j + TY * k);
+        fR = fL + TX * TY;
+      }
+#pragma unroll
+      for (int v = 0; v < C::NFV; ++v)
+      {
+        R acc = R(0);
+        acc = acc + fl[v * C::NFT + fL];
+        acc = acc - fl[v * C::NFT + fR];
+        if constexpr (C::EXACT)
+          u2[v] += (double)acc;
+        else
+          dU[v] += acc;
+      }
+    }
     if constexpr (!C::EXACT)
     {
 #pragma unroll
       for (int v = 0; v < C::NFV; ++v)
-        u2[c][v] += (double)dU[c][v];
+        u2[v] += to_d<R>(dU[v]);
     }
 #pragma unroll
     for (int v = 0; v < 5; ++v)
-      a.U2[((int64_t)blk * 5 + v) * a.ncell + cell] = u2[c][v];
+      a.U2[((int64_t)blk * 5 + v) * a.ncell + cell] = u2[v];
     if constexpr (DIM == 2)
-      a.B2[(int64_t)blk * a.nface + a.nfx + a.nfy + cell] = u2[c][5];
-    if (!(u2[c][ID] > 0.0))
+      a.B2[(int64_t)blk * a.nface + a.nfx + a.nfy + cell] = u2[5];
+    if (!(u2[ID] > 0.0))
       health |= HEALTH_BAD_DENSITY;
-    if (!isfinite(u2[c][IP]) || !isfinite(u2[c][IU]))
+    if (!isfinite(u2[IP]) || !isfinite(u2[IU]))
       health |= HEALTH_NONFINITE;
 
     if (a.invdt_out)
     {
-      // compute_cfl (ComputeDtMHDFunctor.cpp:86-151) on the updated cell; B2 on the 2 faces per
-      // direction of this cell is recomputed from B and the tile's EMFs
-      const R * Mx = emf;
-      const R * My = emf + (DIM == 3 ? C::NM : 0);
-      const R * Mz = emf + (DIM == 3 ? 2 * C::NM : 0);
-      double    val;
+      const R Axl = b2s[i + (TX + 1) * (j + TY * k)], Axr = b2s[i + 1 + (TX + 1) * (j + TY * k)];
+      const R Ayl = b2s[C::NB2X + i + TX * (j + (TY + 1) * k)], Ayr = b2s[C::NB2X + i + TX * (j + 1 + (TY + 1) * k)];
+      double  val;
       if constexpr (C::EXACT)
       {
-        const double * Bblk = a.B + (int64_t)blk * a.nface;
-        auto bx2 = [&](int ii) {
-          const int64_t g = (x0 + ii) + (int64_t)(bx + 1) * ((y0 + j) + (int64_t)by * (z0 + k));
-          double        d = 0;
-          if constexpr (DIM == 2)
-            d += ((double)Mz[C::mi(ii, j + 1, 0)] - (double)Mz[C::mi(ii, j, 0)]);
-          else
-          {
-            d += ((double)Mz[C::mi(ii, j + 1, k)] - (double)Mz[C::mi(ii, j, k)]);
-            d -= ((double)My[C::mi(ii, j, k + 1)] - (double)My[C::mi(ii, j, k)]);
-          }
-          return Bblk[g] + d;
-        };
-        auto by2 = [&](int jj) {
-          const int64_t g = a.nfx + (x0 + i) + (int64_t)bx * ((y0 + jj) + (int64_t)(by + 1) * (z0 + k));
-          if constexpr (DIM == 2)
-            return Bblk[g] - ((double)Mz[C::mi(i + 1, jj, 0)] - (double)Mz[C::mi(i, jj, 0)]);
-          else
-          {
-            double d = 0;
-            d += ((double)Mx[C::mi(i, jj, k + 1)] - (double)Mx[C::mi(i, jj, k)]);
-            d -= ((double)Mz[C::mi(i + 1, jj, k)] - (double)Mz[C::mi(i, jj, k)]);
-            return Bblk[g] + d;
-          }
-        };
-        auto bz2 = [&](int kk) {
-          const int64_t g = a.nfx + a.nfy + (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)by * (z0 + kk));
-          double        d = 0;
-          d += ((double)My[C::mi(i + 1, j, kk)] - (double)My[C::mi(i, j, kk)]);
-          d -= ((double)Mx[C::mi(i, j + 1, kk)] - (double)Mx[C::mi(i, j, kk)]);
-          return Bblk[g] + d;
-        };
-        const double Ax = 0.5 * (bx2(i) + bx2(i + 1));
-        const double Ay = 0.5 * (by2(j) + by2(j + 1));
+        const double Ax = 0.5 * (Axl + Axr);
+        const double Ay = 0.5 * (Ayl + Ayr);
         double       Az;
         if constexpr (DIM == 3)
-          Az = 0.5 * (bz2(k) + bz2(k + 1));
+          Az = 0.5 * (b2s[C::NB2X + C::NB2Y + i + TX * (j + TY * k)] + b2s[C::NB2X + C::NB2Y + i + TX * (j + TY * (k + 1))]);
         else
-          Az = 0.5 * (u2[c][5] + u2[c][5]);
-        const double r = fmax(u2[c][ID], a.smallr);
-        const double vx = u2[c][IU] / r, vy = u2[c][IV] / r, vz = u2[c][IW] / r;
+          Az = 0.5 * (u2[5] + u2[5]);
+        const double r = fmax(u2[ID], a.smallr);
+        const double vx = u2[IU] / r, vy = u2[IV] / r, vz = u2[IW] / r;
         const double eken = 0.5 * (vx * vx + vy * vy + vz * vz);
         const double emag = 0.5 * (Ax * Ax + Ay * Ay + Az * Az);
-        const double eint = (u2[c][IP] - emag) / r - eken;
+        const double eint = (u2[IP] - emag) / r - eken;
         const double p = fmax((a.gamma0 - 1.0) * r * eint, r * a.smallp);
         const double b2 = Ax * Ax + Ay * Ay + Az * Az;
         const double c2 = a.gamma0 * p / r;
@@ -990,39 +984,21 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       }
       else
       {
-        // FP32 estimate: B^n faces from shared memory plus the FP32 EMF curl
-        auto bx2 = [&](int ii) {
-          R d = Mz[C::mi(ii, j + 1, D3 ? k : 0)] - Mz[C::mi(ii, j, D3 ? k : 0)];
-          if constexpr (DIM == 3)
-            d -= My[C::mi(ii, j, k + 1)] - My[C::mi(ii, j, k)];
-          return fbx[C::fxi(ii, j, k)] + d;
-        };
-        auto by2 = [&](int jj) {
-          R d;
-          if constexpr (DIM == 2)
-            d = -(Mz[C::mi(i + 1, jj, 0)] - Mz[C::mi(i, jj, 0)]);
-          else
-            d = (Mx[C::mi(i, jj, k + 1)] - Mx[C::mi(i, jj, k)]) - (Mz[C::mi(i + 1, jj, k)] - Mz[C::mi(i, jj, k)]);
-          return fby[C::fyi(i, jj, k)] + d;
-        };
-        auto bz2 = [&](int kk) {
-          const R d = (My[C::mi(i + 1, j, kk)] - My[C::mi(i, j, kk)]) - (Mx[C::mi(i, j + 1, kk)] - Mx[C::mi(i, j, kk)]);
-          return fbz[C::fzi(i, j, kk)] + d;
-        };
-        const float bxf = 0.5f * (bx2(i) + bx2(i + 1));
-        const float byf = 0.5f * (by2(j) + by2(j + 1));
+        // FP32 estimate of the fastest signal speed
+        const float bxf = 0.5f * (Axl + Axr);
+        const float byf = 0.5f * (Ayl + Ayr);
         float       bzf;
         if constexpr (DIM == 3)
-          bzf = 0.5f * (bz2(k) + bz2(k + 1));
+          bzf = 0.5f * (b2s[C::NB2X + C::NB2Y + i + TX * (j + TY * k)] + b2s[C::NB2X + C::NB2Y + i + TX * (j + TY * (k + 1))]);
         else
-          bzf = (float)u2[c][5];
-        const float r = fmaxf((float)u2[c][ID], (float)a.smallr);
+          bzf = to_r<R>(u2[5]);
+        const float r = fmaxf(to_r<R>(u2[ID]), ph.smallr);
         const float ir = 1.0f / r;
-        const float vx = (float)u2[c][IU] * ir, vy = (float)u2[c][IV] * ir, vz = (float)u2[c][IW] * ir;
+        const float vx = to_r<R>(u2[IU]) * ir, vy = to_r<R>(u2[IV]) * ir, vz = to_r<R>(u2[IW]) * ir;
         const float ekin = 0.5f * r * (vx * vx + vy * vy + vz * vz);
         const float emag = 0.5f * (bxf * bxf + byf * byf + bzf * bzf);
         const float g = ph.gamma0;
-        const float p = fmaxf((g - 1.0f) * ((float)u2[c][IP] - emag - ekin), r * ph.smallp);
+        const float p = fmaxf((g - 1.0f) * (to_r<R>(u2[IP]) - emag - ekin), r * ph.smallp);
         const float b2 = 2.0f * emag;
         const float c2 = g * p * ir;
         const float d2 = 0.5f * (b2 * ir + c2);
@@ -1031,7 +1007,7 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
         float       sum = cfx + cfy;
         if constexpr (DIM == 3)
           sum += sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * bzf * bzf * ir, 0.0f))) + fabsf(vz);
-        val = (double)(sum * (float)(1.0 / dx));
+        val = to_d<R>(sum * (float)(1.0 / dx));
       }
       my_invdt = fmax(my_invdt, val);
     }

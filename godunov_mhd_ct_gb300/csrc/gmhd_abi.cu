@@ -16,6 +16,10 @@ int launch_inv_dt(const double * U, const double * B, const int32_t * level, con
                   int n_owned, int dim, int bx, int by, int bz, int64_t ncell, int64_t nfx, int64_t nfy,
                   int64_t nface, double gamma0, double smallr, double smallp, double scaling_factor,
                   unsigned long long * invdt, cudaStream_t stream);
+int launch_inv_dt_mixed(const double * U, const double * B, const int32_t * level, const int32_t * problem,
+                        int n_owned, int dim, int bx, int by, int bz, int64_t ncell, int64_t nfx, int64_t nfy,
+                        int64_t nface, double gamma0, double smallr, double smallp, double scaling_factor,
+                        unsigned long long * invdt, cudaStream_t stream);
 } // namespace gmhd
 
 struct gmhd_ctx
@@ -330,11 +334,15 @@ enqueue_fill(gmhd_ctx * ctx, double * U, double * B, cudaStream_t s)
   return GMHD_OK;
 }
 
+// exact: FP64 with the reference operand order (gmhd_inv_dt); otherwise the precision of the
+// context's step (the mixed solver loop seeds dt with an FP32 estimate)
 int
-enqueue_inv_dt(gmhd_ctx * ctx, const double * U, const double * B, unsigned long long * slot, cudaStream_t s)
+enqueue_inv_dt(gmhd_ctx * ctx, const double * U, const double * B, unsigned long long * slot, cudaStream_t s,
+               bool exact = true)
 {
   GMHD_CUDA(cudaMemsetAsync(slot, 0, sizeof(unsigned long long) * ctx->n_problems, s));
-  const int rc = gmhd::launch_inv_dt(U, B, ctx->d_level, ctx->d_problem, ctx->n_owned, ctx->dim, ctx->bx, ctx->by,
+  auto launch = (exact || ctx->p.precision != GMHD_PRECISION_MIXED) ? gmhd::launch_inv_dt : gmhd::launch_inv_dt_mixed;
+  const int rc = launch(U, B, ctx->d_level, ctx->d_problem, ctx->n_owned, ctx->dim, ctx->bx, ctx->by,
                                      ctx->bz, ctx->ncell, ctx->nfx, ctx->nfy, ctx->nface, ctx->p.gamma0,
                                      ctx->p.smallr, ctx->smallp, ctx->p.scaling_factor, slot, s);
   if (rc != 0)
@@ -608,7 +616,7 @@ gmhd_advance(gmhd_ctx * ctx, double * U, double * U2, double * B, double * B2, i
     GMHD_CUDA(cudaMemcpyAsync(ctx->d_tend, t_end, sizeof(double) * np, cudaMemcpyHostToDevice, s));
   GMHD_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(int32_t), s));
   // CFL of the initial state into slot 0 (SolverGodunovMHD ctor: compute_dt, .cpp:180)
-  if ((rc = enqueue_inv_dt(ctx, U, B, ctx->d_invdt, s)))
+  if ((rc = enqueue_inv_dt(ctx, U, B, ctx->d_invdt, s, false)))
     return rc;
   const bool has_tend = t_end != nullptr;
   int        done = 0;

@@ -644,3 +644,70 @@ slope1(R q, R qp, R qm, R slope_type)
 }
 
 } // namespace gmhd
+
+namespace gmhd
+{
+// FP64 <-> FP32 conversions on the integer pipe. On GB300 the FP64 pipe (which also executes
+// F2F conversions) has a small fraction of the FP32 rate, so the mixed path converts by
+// rebuilding the IEEE-754 bit patterns instead.
+
+// double -> float, rounding the 29 dropped mantissa bits half away from zero; results below the
+// float normal range flush to signed zero, above it saturate to infinity; NaN stays NaN.
+__device__ __forceinline__ float
+d2f_bits(double x)
+{
+  const unsigned hi = (unsigned)__double2hiint(x);
+  const unsigned lo = (unsigned)__double2loint(x);
+  const unsigned sign = hi & 0x80000000u;
+  const unsigned e = (hi >> 20) & 0x7ffu;
+  const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const int      ef = (int)e - 896; // rebias 1023 -> 127
+  unsigned       bits = sign | (((unsigned)ef << 23) + m + ((lo >> 28) & 1u));
+  bits = ef <= 0 ? sign : bits;
+  const bool nan = e == 0x7ffu && ((hi & 0xfffffu) | lo) != 0u;
+  bits = ef >= 255 ? (sign | 0x7f800000u | (nan ? 0x400000u : 0u)) : bits;
+  return __uint_as_float(bits);
+}
+
+// float -> double, exact for normal numbers, zero, infinity and NaN (subnormals flush to zero).
+__device__ __forceinline__ double
+f2d_bits(float x)
+{
+  const unsigned b = __float_as_uint(x);
+  const unsigned sign = b & 0x80000000u;
+  const unsigned e = (b >> 23) & 0xffu;
+  const unsigned m = b & 0x7fffffu;
+  const unsigned eb = e == 0xffu ? 0x7ffu : e + 896u;
+  unsigned       hi = sign | (eb << 20) | (m >> 3);
+  unsigned       lo = m << 29;
+  hi = e == 0u ? sign : hi;
+  lo = e == 0u ? 0u : lo;
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+template <typename R>
+__device__ __forceinline__ R
+to_r(double x)
+{
+  return x;
+}
+template <>
+__device__ __forceinline__ float
+to_r<float>(double x)
+{
+  return d2f_bits(x);
+}
+
+template <typename R>
+__device__ __forceinline__ double
+to_d(R x)
+{
+  return x;
+}
+template <>
+__device__ __forceinline__ double
+to_d<float>(float x)
+{
+  return f2d_bits(x);
+}
+} // namespace gmhd

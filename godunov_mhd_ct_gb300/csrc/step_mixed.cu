@@ -38,3 +38,73 @@ prepare_mixed()
   return rc;
 }
 } // namespace gmhd
+
+namespace gmhd
+{
+// FP32 estimate of ComputeDtMHDFunctor::compute_cfl (scheme/ComputeDtMHDFunctor.cpp:86-151) for
+// the mixed path's solver loop: one CTA per owned block, max-reduced per problem.
+__global__ void __launch_bounds__(256)
+inv_dt_mixed_kernel(const double * __restrict__ U, const double * __restrict__ B, const int32_t * __restrict__ level,
+                    const int32_t * __restrict__ problem, int dim, int bx, int by, int bz, int64_t ncell,
+                    int64_t nfx, int64_t nfy, int64_t nface, float gamma0, float smallr, float smallp,
+                    double scaling_factor, unsigned long long * invdt)
+{
+  const int     blk = blockIdx.x;
+  const double  dx = (1.0 / (double)((int64_t)bx << level[blk])) * scaling_factor;
+  const float   idx = d2f_bits(1.0 / dx);
+  const double *Ub = U + (int64_t)blk * 5 * ncell;
+  const double *Bb = B + (int64_t)blk * nface;
+  float         m = 0.0f;
+  for (int64_t c = threadIdx.x; c < ncell; c += blockDim.x)
+  {
+    const int   i = (int)(c % bx), j = (int)((c / bx) % by), k = (int)(c / ((int64_t)bx * by));
+    const float Ax = 0.5f * (d2f_bits(Bb[i + (int64_t)(bx + 1) * (j + (int64_t)by * k)]) +
+                             d2f_bits(Bb[i + 1 + (int64_t)(bx + 1) * (j + (int64_t)by * k)]));
+    const float Ay = 0.5f * (d2f_bits(Bb[nfx + i + (int64_t)bx * (j + (int64_t)(by + 1) * k)]) +
+                             d2f_bits(Bb[nfx + i + (int64_t)bx * (j + 1 + (int64_t)(by + 1) * k)]));
+    const float Az = dim == 3 ? 0.5f * (d2f_bits(Bb[nfx + nfy + i + (int64_t)bx * (j + (int64_t)by * k)]) +
+                                        d2f_bits(Bb[nfx + nfy + i + (int64_t)bx * (j + (int64_t)by * (k + 1))]))
+                              : d2f_bits(Bb[nfx + nfy + c]);
+    const float r = fmaxf(d2f_bits(Ub[c]), smallr);
+    const float ir = 1.0f / r;
+    const float vx = d2f_bits(Ub[2 * ncell + c]) * ir, vy = d2f_bits(Ub[3 * ncell + c]) * ir,
+                vz = d2f_bits(Ub[4 * ncell + c]) * ir;
+    const float ekin = 0.5f * r * (vx * vx + vy * vy + vz * vz);
+    const float emag = 0.5f * (Ax * Ax + Ay * Ay + Az * Az);
+    const float p = fmaxf((gamma0 - 1.0f) * (d2f_bits(Ub[ncell + c]) - emag - ekin), r * smallp);
+    const float c2 = gamma0 * p * ir;
+    const float d2 = 0.5f * (2.0f * emag * ir + c2);
+    float       sum = sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * Ax * Ax * ir, 0.0f))) + fabsf(vx) +
+                sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * Ay * Ay * ir, 0.0f))) + fabsf(vy);
+    if (dim == 3)
+      sum += sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * Az * Az * ir, 0.0f))) + fabsf(vz);
+    m = fmaxf(m, sum * idx);
+  }
+  __shared__ float red[8];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+    m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+  if ((threadIdx.x & 31) == 0)
+    red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+      m = fmaxf(m, red[w]);
+    atomicMax(&invdt[problem ? problem[blk] : 0], (unsigned long long)__double_as_longlong(f2d_bits(m)));
+  }
+}
+
+int
+launch_inv_dt_mixed(const double * U, const double * B, const int32_t * level, const int32_t * problem, int n_owned,
+                    int dim, int bx, int by, int bz, int64_t ncell, int64_t nfx, int64_t nfy, int64_t nface,
+                    double gamma0, double smallr, double smallp, double scaling_factor, unsigned long long * invdt,
+                    cudaStream_t stream)
+{
+  if (n_owned <= 0)
+    return 0;
+  inv_dt_mixed_kernel<<<n_owned, 256, 0, stream>>>(U, B, level, problem, dim, bx, by, bz, ncell, nfx, nfy, nface,
+                                                   (float)gamma0, (float)smallr, (float)smallp, scaling_factor, invdt);
+  return (int)cudaGetLastError();
+}
+} // namespace gmhd

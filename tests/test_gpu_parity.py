@@ -127,9 +127,16 @@ def test_mixed_precision_accuracy(dim, block, level, nsteps):
           f"max|divB|={divb:.3e}")
     assert l1_rho <= 1e-6
     assert divb <= 1e-12
-    # conservation: total mass unchanged to round-off on a periodic mesh
-    m0 = U[:n, 0].sum()
-    assert abs(out["mixed"][0][:n, 0].sum() - m0) / m0 <= 1e-12
+    # conservation on a periodic mesh: exact to FP64 round-off on the FP64 path; the mixed path
+    # adds each cell's FP32 sum of flux differences to U once in FP64, so its drift is the
+    # accumulated FP32 rounding of those increments
+    for v in (0, 1):
+        m0 = U[:n, v].sum()
+        drift64 = abs(out["fp64"][0][:n, v].sum() - m0) / abs(m0)
+        drift32 = abs(out["mixed"][0][:n, v].sum() - m0) / abs(m0)
+        print(f"var {v}: relative drift fp64 {drift64:.2e} mixed {drift32:.2e}")
+        assert drift64 <= 1e-13
+        assert drift32 <= 1e-10
 
 
 def test_alias_and_argument_errors():
