@@ -70,6 +70,8 @@ def lib():
     L.gmhd_error_string.restype = ctypes.c_char_p
     L.gmhd_error_string.argtypes = [ctypes.c_int]
     L.gmhd_layout_check.argtypes = [ctypes.POINTER(GmhdMesh), ctypes.c_int64, ctypes.c_int64, ctypes.c_int64]
+    L.gmhd_inv_dt_noalloc.argtypes = [ctypes.POINTER(GmhdParams)] + [ctypes.c_int32] * 6 + [vp, ctypes.c_int32, vp, vp,
+                                                                                          vp, vp]
     _lib = L
     return L
 
@@ -86,7 +88,7 @@ def exported_symbols():
     """Names declared in include/gmhd.h, for the ABI tests."""
     return ["gmhd_create", "gmhd_destroy", "gmhd_set_mesh", "gmhd_mem_bytes", "gmhd_step", "gmhd_inv_dt",
             "gmhd_fill_outside", "gmhd_advance", "gmhd_step_host", "gmhd_last_status", "gmhd_last_cuda_error",
-            "gmhd_error_string", "gmhd_layout_check"]
+            "gmhd_error_string", "gmhd_layout_check", "gmhd_inv_dt_noalloc"]
 
 
 class MeshTables:

@@ -23,6 +23,7 @@ UNITS = {
     "step_fp64.cu": ["--fmad=false"],
     "step_mixed.cu": ["--use_fast_math"],
     "gmhd_abi.cu": ["--fmad=false"],
+    "noalloc.cu": ["--fmad=false"],
 }
 HEADERS = ["mhd_math.cuh", "fused_step.cuh", "launch.cuh", os.path.join("..", "..", "include", "gmhd.h")]
 

@@ -151,6 +151,23 @@ int gmhd_fill_outside(gmhd_ctx * ctx, double * U, double * B, void * stream);
 int gmhd_advance(gmhd_ctx * ctx, double * U, double * U2, double * B, double * B2, int32_t nsteps,
                  double * t, const double * t_end, double * dt_log, int32_t use_graph, void * stream);
 
+/* Capacity of gmhd_inv_dt_noalloc: independent problems per call. */
+#define GMHD_NOALLOC_MAX_PROBLEMS 1024
+
+/* No counterpart in the reference. gmhd_inv_dt without any device allocation, for callers that
+ * cannot call cudaMalloc (code running under CUDA-graph stream capture, frameworks that own all
+ * device memory). No context is needed: the caller passes the state U, B (device, the layout
+ * above, n_blocks blocks all at refinement level `level`), optional per-block problem ids
+ * (device, NULL for one problem) and a device output inv_dt[n_problems]; the call is asynchronous
+ * on `stream`. The reduction uses a fixed array of GMHD_NOALLOC_MAX_PROBLEMS slots in the library
+ * (8 KB per GPU, held until the process exits); larger n_problems returns GMHD_ERR_TOO_LARGE.
+ * The first call on each device looks that array up (cudaGetSymbolAddress); make that first call
+ * before any stream capture. Calls share the array and clear their slots first; calls that
+ * overlap on the GPU race on it. Results equal gmhd_inv_dt's. */
+int gmhd_inv_dt_noalloc(const gmhd_params * params, int32_t dim, int32_t bx, int32_t by, int32_t bz,
+                        int32_t n_blocks, int32_t level, const int32_t * problem, int32_t n_problems,
+                        const double * U, const double * B, double * inv_dt, void * stream);
+
 /* --- host-buffer variants ------------------------------------------------------------------- */
 
 /* gmhd_step on HOST arrays: copies U, B to the device, runs the step, copies U2, B2 back. */
