@@ -30,9 +30,10 @@ METRIC = "cell-updates/s on 1 GB300, mixed vs FP64 at L1(rho)<=1e-6; % of HBM ro
 UNIT = "cell-updates/s"
 BYTES_PER_CELL_UPDATE = 128.0  # read U(5)+B(3), write U2(5)+B2(3), FP64
 FALLBACK_HBM_GBS = 6800.0
-# DRAM bytes per fused-step launch on the full workload, from the ncu capture summarised in
-# profiles/fused_step_mixed_ot3d.md (None until measured)
-MEASURED_TRAFFIC_BYTES = None
+# DRAM bytes (read + write) of one mixed fused-step launch on the full 256^3 workload: the 128^3
+# capture summarised in profiles/fused_step_mixed_ot3d.md (266.3 MB for 2,097,152 cells) scaled by
+# the cell count (x8); traffic grows in proportion to the cells processed
+MEASURED_TRAFFIC_BYTES = 266.3e6 * 8
 
 
 def hbm_peak():
