@@ -163,6 +163,53 @@ class BlockMesh:
                          outside_src=np.array(out_src, dtype=np.int32),
                          outside_normal=np.array(out_normal, dtype=np.int32).reshape(-1, 3))
 
+    @staticmethod
+    def batch(meshes) -> tuple["BlockMesh", np.ndarray]:
+        """Concatenate independent single-problem meshes (same dim and block size) into one block
+        list for a batched launch. Returns (mesh, problem id per block). Owned blocks of all problems
+        come first, in problem order; outside blocks follow."""
+        dims = {m.dim for m in meshes}
+        blocks = {tuple(m.block) for m in meshes}
+        if len(dims) != 1 or len(blocks) != 1:
+            raise ValueError("batched problems must share dim and block size")
+        n_owned = sum(m.n_owned for m in meshes)
+        own_off, out_off = [], []
+        o, q = 0, n_owned
+        for m in meshes:
+            own_off.append(o)
+            out_off.append(q)
+            o += m.n_owned
+            q += m.n_blocks - m.n_owned
+        n_blocks = q
+
+        def remap(m, idx, p):
+            idx = np.asarray(idx)
+            return np.where(idx < 0, -1, np.where(idx < m.n_owned, idx + own_off[p], idx - m.n_owned + out_off[p]))
+
+        level = np.zeros(n_blocks, np.int32)
+        neighbor = -np.ones((n_blocks, 27), np.int32)
+        coords = np.zeros((n_blocks, 3), np.int64)
+        problem = np.zeros(n_blocks, np.int32)
+        out_src, out_normal = [], []
+        for p, m in enumerate(meshes):
+            own = slice(own_off[p], own_off[p] + m.n_owned)
+            out = slice(out_off[p], out_off[p] + m.n_blocks - m.n_owned)
+            level[own], level[out] = m.level[: m.n_owned], m.level[m.n_owned:]
+            neighbor[own] = remap(m, m.neighbor[: m.n_owned], p)
+            neighbor[out] = remap(m, m.neighbor[m.n_owned:], p)
+            coords[own], coords[out] = m.coords[: m.n_owned], m.coords[m.n_owned:]
+            problem[own] = p
+            problem[out] = p
+            out_src.append(remap(m, m.outside_src, p))
+            out_normal.append(m.outside_normal)
+        first = meshes[0]
+        bm = BlockMesh(dim=first.dim, block=first.block, level=level, neighbor=neighbor, coords=coords,
+                       n_owned=n_owned, grid=first.grid, periodic=first.periodic,
+                       scaling_factor=first.scaling_factor,
+                       outside_src=np.concatenate(out_src).astype(np.int32) if out_src else np.zeros(0, np.int32),
+                       outside_normal=np.concatenate(out_normal).astype(np.int32).reshape(-1, 3))
+        return bm, problem
+
     # ---- layout helpers -------------------------------------------------------------------------
     def alloc_state(self):
         """Zeroed U [n_blocks, 5, bz, by, bx] and B [n_blocks, nface] (C-ABI layout, FP64)."""

@@ -180,3 +180,62 @@ def random_smooth(mesh: BlockMesh, gamma=1.4, seed=0, amp=0.2):
     vz = 0.3 * amp * s if mesh.dim == 3 else 0.2 * amp * s
     _fill_energy(mesh, U, B, rho, p, vx, vy, vz, gamma)
     return U, B
+
+
+def gaussian01(seed: int, ids: np.ndarray) -> np.ndarray:
+    """Counter-based standard normal from (seed, id) (Box-Muller on two splitmix64 uniforms)."""
+    u1 = uniform01(seed, 2 * ids)
+    u2 = uniform01(seed, 2 * ids + 1)
+    return np.sqrt(-2.0 * np.log1p(-u1)) * np.cos(2.0 * math.pi * u2)
+
+
+def kelvin_helmholtz(mesh: BlockMesh, gamma=1.4, p0=2.5, bx0=0.1, width=0.01, noise=1e-3, seed=0):
+    """Magnetised shear layer on [0,1]^d (init/InitKelvinHelmholtz.cpp): rho = 2, vx = +0.5 for
+    |y - 0.5| < 0.25 and rho = 1, vx = -0.5 outside, tanh-smoothed with `width`; vy = 0.01 sin(4 pi x)
+    plus seeded Gaussian noise of amplitude `noise`; p = p0; uniform Bx = bx0."""
+    U, B = mesh.alloc_state()
+    Bx, By, Bz = mesh.split_faces(B)
+    Bx[...] = bx0
+    By[...] = 0.0
+    Bz[...] = 0.0
+    n = mesh.n_owned
+    gi, gj, gk = mesh.global_cell_index()
+    gi, gj, gk = gi[:n], gj[:n], gk[:n]
+    dx = mesh.cell_length()
+    x = (gi + 0.5) * dx
+    y = (gj + 0.5) * dx
+    s = 0.5 * (1.0 + np.tanh((0.25 - np.abs(y - 0.5)) / width))
+    rho = 1.0 + s
+    vx = -0.5 + s
+    gx = mesh.grid[0] * mesh.block[0]
+    gy = mesh.grid[1] * mesh.block[1]
+    ids = gi + gx * (gj + gy * gk)
+    vy = 0.01 * np.sin(4.0 * math.pi * x) + noise * gaussian01(seed, ids)
+    vz = np.zeros_like(x)
+    _fill_energy(mesh, U, B, rho, np.full(x.shape, p0), vx, vy, vz, gamma)
+    return U, B
+
+
+def field_loop_batch(n_problems: int, seed: int = 0, sizes=(32, 64, 128, 256), block: int = 16, gamma=5.0 / 3.0):
+    """Independent 2D field-loop problems on [-1,1] x [-0.5,0.5] (periodic), each (2N) x N cells in
+    block x block leaf blocks (2 x 1 bricks, level log2(N / block)). Per problem, from the seed:
+    loop radius R ~ U[0.2, 0.35], speed |v| ~ U[1, 3], direction ~ U[0, 2 pi), and N drawn so that the
+    cell count 2N^2 is log-uniform between the smallest and the largest allowed size.
+    Returns (meshes, [(U, B)], params) per problem."""
+    rng = np.random.default_rng(seed)
+    sizes = sorted(sizes)
+    lo, hi = np.log(2.0 * sizes[0] ** 2), np.log(2.0 * sizes[-1] ** 2)
+    meshes, states, params = [], [], []
+    for _ in range(n_problems):
+        target = np.exp(rng.uniform(lo, hi))
+        n = min(sizes, key=lambda s_: abs(np.log(2.0 * s_ * s_) - np.log(target)))
+        level = int(round(np.log2(n // block)))
+        radius = float(rng.uniform(0.2, 0.35))
+        speed = float(rng.uniform(1.0, 3.0))
+        angle = float(rng.uniform(0.0, 2.0 * math.pi))
+        mesh = BlockMesh.uniform(2, bricks=(2, 1, 1), level=level, block=(block, block, 1))
+        U, B = field_loop(mesh, gamma=gamma, radius=radius, speed=speed, angle=angle)
+        meshes.append(mesh)
+        states.append((U, B))
+        params.append({"N": n, "radius": radius, "speed": speed, "angle": angle})
+    return meshes, states, params

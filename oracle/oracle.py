@@ -22,7 +22,8 @@ class OracleMesh(ctypes.Structure):
         ("dim", ctypes.c_int32), ("bx", ctypes.c_int32), ("by", ctypes.c_int32),
         ("bz", ctypes.c_int32), ("n_blocks", ctypes.c_int32), ("n_owned", ctypes.c_int32),
         ("level", ctypes.POINTER(ctypes.c_int32)), ("neighbor", ctypes.POINTER(ctypes.c_int32)),
-        ("scaling_factor", ctypes.c_double),
+        ("scaling_factor", ctypes.c_double), ("outside_src", ctypes.POINTER(ctypes.c_int32)),
+        ("outside_normal", ctypes.POINTER(ctypes.c_int32)), ("bc", ctypes.c_int32 * 6),
     ]
 
 
@@ -62,6 +63,9 @@ def lib():
         L.oracle_run.restype = ctypes.c_int
         L.oracle_run.argtypes = [ctypes.POINTER(OracleMesh), ctypes.POINTER(OracleSettings), dp, dp, ctypes.c_int,
                                  dp]
+        L.oracle_run_to.restype = ctypes.c_int
+        L.oracle_run_to.argtypes = [ctypes.POINTER(OracleMesh), ctypes.POINTER(OracleSettings), dp, dp, ctypes.c_int,
+                                    dp, dp, ctypes.c_double]
         L.oracle_riemann.argtypes = [ctypes.POINTER(OracleSettings), dp, dp, dp]
         L.oracle_compute_emf.restype = ctypes.c_double
         L.oracle_compute_emf.argtypes = [ctypes.POINTER(OracleSettings), dp, ctypes.c_int]
@@ -69,6 +73,7 @@ def lib():
         L.oracle_find_speed_info.argtypes = [ctypes.POINTER(OracleSettings), dp, ctypes.c_int, dp]
         L.oracle_find_speed_fast.restype = ctypes.c_double
         L.oracle_find_speed_fast.argtypes = [ctypes.POINTER(OracleSettings), dp, ctypes.c_int]
+        L.oracle_fill_outside.argtypes = [ctypes.POINTER(OracleMesh), dp, dp]
         _lib = L
     return _lib
 
@@ -85,12 +90,18 @@ def settings(gamma0=1.4, cfl=0.5, slope_type=1.0, smallr=1e-10, smallc=1e-10, ri
 class Mesh:
     """Holds the ctypes mesh plus the numpy arrays it points into."""
 
-    def __init__(self, dim, bx, by, bz, level, neighbor, n_owned, scaling_factor=1.0):
+    def __init__(self, dim, bx, by, bz, level, neighbor, n_owned, scaling_factor=1.0, outside_src=None,
+                 outside_normal=None, bc=(1, 1, 1, 1, 1, 1)):
+        ip = ctypes.POINTER(ctypes.c_int32)
         self.level = np.ascontiguousarray(level, dtype=np.int32)
         self.neighbor = np.ascontiguousarray(neighbor, dtype=np.int32)
+        self.out_src = np.ascontiguousarray(outside_src if outside_src is not None else np.zeros(1), dtype=np.int32)
+        self.out_normal = np.ascontiguousarray(outside_normal if outside_normal is not None else np.zeros(3),
+                                               dtype=np.int32).reshape(-1)
         self.c = OracleMesh(dim, bx, by, bz if dim == 3 else 1, len(self.level), n_owned,
-                            self.level.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
-                            self.neighbor.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), scaling_factor)
+                            self.level.ctypes.data_as(ip), self.neighbor.ctypes.data_as(ip), scaling_factor,
+                            self.out_src.ctypes.data_as(ip), self.out_normal.ctypes.data_as(ip),
+                            (ctypes.c_int32 * 6)(*[int(b) for b in bc]))
 
 
 def step(mesh: Mesh, st: OracleSettings, U, B, dt):
@@ -101,6 +112,14 @@ def step(mesh: Mesh, st: OracleSettings, U, B, dt):
     if rc != 0:
         raise RuntimeError(f"oracle_step failed: {rc}")
     return U2, B2
+
+
+def fill_outside(mesh: Mesh, U, B):
+    """FillOutsideCellFunctor on copies of U, B; returns (U, B)."""
+    U = np.array(U, dtype=np.float64, copy=True, order="C")
+    B = np.array(B, dtype=np.float64, copy=True, order="C")
+    lib().oracle_fill_outside(ctypes.byref(mesh.c), _dp(U), _dp(B))
+    return U, B
 
 
 def inv_dt(mesh: Mesh, st: OracleSettings, U, B) -> float:
@@ -116,6 +135,19 @@ def run(mesh: Mesh, st: OracleSettings, U, B, nsteps):
     if rc != 0:
         raise RuntimeError(f"oracle_run failed: {rc}")
     return U, B, dts[:nsteps]
+
+
+def run_to(mesh: Mesh, st: OracleSettings, U, B, nsteps, t0, t_end):
+    """nsteps with dt capped so that t does not pass t_end; returns (U, B, dts, t)."""
+    U = np.array(U, dtype=np.float64, copy=True, order="C")
+    B = np.array(B, dtype=np.float64, copy=True, order="C")
+    dts = np.zeros(max(nsteps, 1), dtype=np.float64)
+    t = ctypes.c_double(t0)
+    rc = lib().oracle_run_to(ctypes.byref(mesh.c), ctypes.byref(st), _dp(U), _dp(B), nsteps, _dp(dts),
+                             ctypes.byref(t), t_end)
+    if rc != 0:
+        raise RuntimeError(f"oracle_run_to failed: {rc}")
+    return U, B, dts[:nsteps], t.value
 
 
 # ---- per-call math (known-answer tests) -------------------------------------------------------

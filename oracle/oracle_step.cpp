@@ -883,6 +883,9 @@ struct oracle_mesh
   const int32_t * level;
   const int32_t * neighbor;
   double          scaling_factor;
+  const int32_t * outside_src;    // [n_blocks - n_owned]
+  const int32_t * outside_normal; // [3 * (n_blocks - n_owned)], +1 below / -1 above the domain
+  int32_t         bc[6];          // BC_MHD values for XMIN..ZMAX (FillOutside.h:55-61)
 };
 
 struct oracle_settings
@@ -1007,11 +1010,106 @@ oracle_inv_dt(const oracle_mesh * om, const oracle_settings * os, const double *
   return inv_dt;
 }
 
-// nsteps of (dt = cfl / invDt; do_time_step; U <- U2, B <- B2) on U/B in place. dt_out[n] receives
+// FillOutsideCellFunctor (border_conditions/FillOutside.cpp:97-395) over the outside blocks
+// [n_owned, n_blocks). Hydro: for every domain face the inside block touches on the outside block's
+// side, ZERO_GRADIENT copies the first/last inside cell along the normal, WALL mirrors it and negates
+// the normal velocity (later faces overwrite earlier ones, as in the reference loop). Face B:
+// ZERO_GRADIENT clamps the face index to the first/last face along each outside direction; WALL leaves
+// the index unchanged (a TODO in the reference) so the same face of the inside block is copied.
+void
+oracle_fill_outside(const oracle_mesh * om, double * U, double * B)
+{
+  const Mesh        m = to_mesh(om);
+  const BlockLayout L = block_layout(m);
+  const int         n_out = m.n_blocks - m.n_owned;
+  const int         bs[3] = {m.bx, m.by, m.bz};
+  enum
+  {
+    ZERO_GRADIENT = 2,
+    WALL = 3
+  };
+  for (int o = 0; o < n_out; ++o)
+  {
+    const int      ob = m.n_owned + o, ib = om->outside_src[o];
+    const int32_t *nrm = om->outside_normal + 3 * o;
+    for (int k = 0; k < m.bz; ++k)
+      for (int j = 0; j < m.by; ++j)
+        for (int i = 0; i < m.bx; ++i)
+        {
+          const int     co[3] = {i, j, k};
+          const int64_t c = i + (int64_t)m.bx * (j + (int64_t)m.by * k);
+          for (int face = 0; face < 2 * m.dim; ++face)
+          {
+            const int  d = face / 2;
+            const bool applies = (face % 2 == 0) ? nrm[d] > 0 : nrm[d] < 0;
+            if (!applies)
+              continue;
+            int ci[3] = {co[0], co[1], co[2]};
+            if (om->bc[face] == ZERO_GRADIENT)
+              ci[d] = (face % 2 == 0) ? 0 : bs[d] - 1;
+            else if (om->bc[face] == WALL)
+              ci[d] = bs[d] - 1 - co[d];
+            else
+              continue;
+            const int64_t cin = ci[0] + (int64_t)m.bx * (ci[1] + (int64_t)m.by * ci[2]);
+            for (int v = 0; v < 5; ++v)
+              U[((int64_t)ob * 5 + v) * L.ncell + c] = U[((int64_t)ib * 5 + v) * L.ncell + cin];
+            if (om->bc[face] == WALL)
+              U[((int64_t)ob * 5 + 2 + d) * L.ncell + c] *= -1;
+          }
+        }
+    for (int64_t f = 0; f < L.nface; ++f)
+    {
+      int     comp, nx, ny, nz;
+      int64_t r, base;
+      if (f < L.nfx)
+      {
+        comp = 0; r = f; nx = m.bx + 1; ny = m.by; nz = m.bz; base = 0;
+      }
+      else if (f < L.nfx + L.nfy)
+      {
+        comp = 1; r = f - L.nfx; nx = m.bx; ny = m.by + 1; nz = m.bz; base = L.nfx;
+      }
+      else
+      {
+        comp = 2; r = f - L.nfx - L.nfy; nx = m.bx; ny = m.by; nz = m.dim == 3 ? m.bz + 1 : m.bz;
+        base = L.nfx + L.nfy;
+      }
+      int       idx[3] = {(int)(r % nx), (int)((r / nx) % ny), (int)(r / ((int64_t)nx * ny))};
+      const int fsz[3] = {nx, ny, nz};
+      for (int d = 0; d < m.dim; ++d)
+      {
+        if (nrm[d] > 0 && om->bc[2 * d] == ZERO_GRADIENT)
+          idx[d] = 0;
+        else if (nrm[d] < 0 && om->bc[2 * d + 1] == ZERO_GRADIENT)
+          idx[d] = fsz[d] - 1;
+      }
+      (void)comp;
+      const int64_t fin = idx[0] + (int64_t)nx * (idx[1] + (int64_t)ny * idx[2]);
+      B[(int64_t)ob * L.nface + f] = B[(int64_t)ib * L.nface + base + fin];
+    }
+  }
+}
+
+// nsteps of (dt = cfl / invDt; fill outside blocks; do_time_step; U <- U2, B <- B2) on U/B in place
+// (SolverGodunovMHD::next_iteration_impl + godunov_unsplit, SolverGodunovMHD.cpp:407-549). dt_out[n] receives
 // the dt of step n. Returns 0 or the first step error.
+int
+oracle_run_to(const oracle_mesh * om, const oracle_settings * os, double * U, double * B, int nsteps,
+              double * dt_out, double * t, double t_end);
+
 int
 oracle_run(const oracle_mesh * om, const oracle_settings * os, double * U, double * B, int nsteps,
            double * dt_out)
+{
+  return oracle_run_to(om, os, U, B, nsteps, dt_out, nullptr, 0.0);
+}
+
+// As oracle_run, with the solver's end-time control when t != nullptr: dt = min(cfl/invDt, t_end - t),
+// and dt = 0 once t has reached t_end (the state is then carried over unchanged).
+int
+oracle_run_to(const oracle_mesh * om, const oracle_settings * os, double * U, double * B, int nsteps,
+              double * dt_out, double * t, double t_end)
 {
   const Mesh        m = to_mesh(om);
   const BlockLayout L = block_layout(m);
@@ -1021,7 +1119,22 @@ oracle_run(const oracle_mesh * om, const oracle_settings * os, double * U, doubl
   for (int n = 0; n < nsteps; ++n)
   {
     const double inv_dt = oracle_inv_dt(om, os, U, B);
-    const double dt = os->cfl / inv_dt;
+    double       dt = os->cfl / inv_dt;
+    if (t)
+    {
+      const double rem = t_end - *t;
+      if (dt > rem)
+        dt = rem;
+      if (!(rem > 0.0))
+        dt = 0.0;
+      *t += dt;
+    }
+    if (m.n_blocks > m.n_owned)
+    {
+      oracle_fill_outside(om, U, B);
+      std::memcpy(U2.data(), U, nu * sizeof(double));
+      std::memcpy(B2.data(), B, nb * sizeof(double));
+    }
     if (dt_out)
       dt_out[n] = dt;
     const int st = oracle_step(om, os, U, U2.data(), B, B2.data(), dt);

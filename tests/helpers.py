@@ -11,9 +11,11 @@ def settings(gamma0=5.0 / 3.0, cfl=0.5, slope_type=2.0, riemann="HLLD"):
     return MHDSettings(gamma0=gamma0, cfl=cfl, slope_type=slope_type, riemann=riemann)
 
 
-def oracle_mesh(orc, mesh: BlockMesh):
+def oracle_mesh(orc, mesh: BlockMesh, bc=None):
+    if bc is None:
+        bc = [1 if mesh.periodic[f // 2] else 2 for f in range(6)]
     return orc.Mesh(mesh.dim, mesh.block[0], mesh.block[1], mesh.block[2], mesh.level, mesh.neighbor,
-                    mesh.n_owned, mesh.scaling_factor)
+                    mesh.n_owned, mesh.scaling_factor, mesh.outside_src, mesh.outside_normal, bc)
 
 
 def oracle_settings(orc, st: MHDSettings):

@@ -1,0 +1,61 @@
+"""Batched independent problems (configuration 3: field loops of uneven sizes) in one launch per
+step, each with its own CFL dt and end time, against the oracle run problem by problem."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from godunov_mhd_ct_gb300 import workloads as wl  # noqa: E402
+from godunov_mhd_ct_gb300.mesh import BlockMesh  # noqa: E402
+from godunov_mhd_ct_gb300.solver import GodunovImplemGB300  # noqa: E402
+
+from .helpers import max_rel_diff, oracle_mesh, oracle_settings, settings  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+TOL_FP64 = 1e-12
+
+
+def _batch(n, seed, sizes):
+    meshes, states, params = wl.field_loop_batch(n, seed=seed, sizes=sizes)
+    mesh, problem = BlockMesh.batch(meshes)
+    U = np.concatenate([s[0] for s in states])
+    B = np.concatenate([s[1] for s in states])
+    return meshes, states, mesh, problem, U, B
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_field_loop_batch_matches_per_problem_oracle(oracle_lib, precision):
+    st = settings(gamma0=5.0 / 3.0, slope_type=2.0)
+    meshes, states, mesh, problem, U, B = _batch(7, seed=3, sizes=(32, 64))
+    assert len({m.n_owned for m in meshes}) > 1  # uneven sizes
+    t_end, nsteps = 0.01, 12
+    impl = GodunovImplemGB300(st, mesh, precision=precision, problem=problem, n_problems=len(meshes))
+    dU, dB = torch.from_numpy(U).cuda(), torch.from_numpy(B).cuda()
+    dtlog, t = impl.advance(dU, torch.empty_like(dU), dB, torch.empty_like(dB), nsteps, t=0.0, t_end=t_end)
+    Ug, Bg = dU.cpu().numpy(), dB.cpu().numpy()
+    assert np.allclose(t, t_end, rtol=0, atol=1e-15)
+    off = 0
+    for p, (m, (Up, Bp)) in enumerate(zip(meshes, states)):
+        Uo, Bo, dto, to = oracle_lib.run_to(oracle_mesh(oracle_lib, m), oracle_settings(oracle_lib, st), Up, Bp,
+                                            nsteps, 0.0, t_end)
+        sl = slice(off, off + m.n_owned)
+        off += m.n_owned
+        assert dto[-1] == 0.0 and to == t_end  # every problem finished inside the step budget
+        if precision == "fp64":
+            assert max_rel_diff(dtlog[:, p], dto) <= TOL_FP64
+            assert max_rel_diff(Ug[sl], Uo) <= TOL_FP64
+            assert max_rel_diff(Bg[sl], Bo) <= TOL_FP64
+        else:
+            l1 = float(np.abs(Ug[sl, 0] - Uo[:, 0]).sum() / np.abs(Uo[:, 0]).sum())
+            assert l1 <= 1e-6
+            assert np.all(np.abs(dtlog[:, p] - dto) <= 1e-6 * np.max(dto))
+
+
+def test_batch_rejects_cross_problem_neighbours():
+    from godunov_mhd_ct_gb300._native import NativeError
+
+    meshes, _, mesh, problem, _, _ = _batch(3, seed=1, sizes=(32,))
+    bad = problem.copy()
+    bad[0] = 1  # block 0 now claims problem 1 while its neighbours belong to problem 0
+    with pytest.raises(NativeError):
+        GodunovImplemGB300(settings(), mesh, problem=bad, n_problems=3)
