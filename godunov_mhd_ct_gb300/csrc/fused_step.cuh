@@ -147,6 +147,246 @@ atomic_max_pos_double(unsigned long long * addr, double v)
   return atomicMax(addr, (unsigned long long)__double_as_longlong(v));
 }
 
+// ---- phase-5 work: per-direction passes with compile-time strides ------------------------------
+// Shared-memory views of one tile, passed to the passes below.
+template <class C>
+struct TileView
+{
+  using R = typename C::R;
+  const R *   fb[3]; // face B at t^n, components x, y, z (2D z: cell-centred Bz)
+  const R *   sl;    // slopes [dir][var][S cell]
+  const R *   q2;    // predictor [var][S cell]
+  const R *   sf;    // half-step face-B source [comp][S cell]
+  double *    emfd;  // EMFs [comp][edge], FP64
+  R *         fl;    // fluxes [var][face item]
+  const int * s_nbr;
+  Phys<R>     ph;
+  R           dtdx;
+  int         x0, y0, z0, bx, by, bz, n_owned;
+};
+
+// stride of the S region along direction d
+template <class C>
+__device__ constexpr int
+s_stride(int d)
+{
+  return d == 0 ? 1 : (d == 1 ? C::SX : C::SX * C::SY);
+}
+// stride of face array c along direction d
+template <class C>
+__device__ constexpr int
+f_stride(int c, int d)
+{
+  return d == 0 ? 1
+                : (c == 0 ? (d == 1 ? C::TX + 5 : (C::TX + 5) * C::QY)
+                          : (c == 1 ? (d == 1 ? C::QX : C::QX * (C::TY + 5)) : (d == 1 ? C::QX : C::QX * C::QY)));
+}
+template <class C, int CMP>
+__device__ __forceinline__ int
+f_index(int i, int j, int k)
+{
+  return CMP == 0 ? C::fxi(i, j, k) : (CMP == 1 ? C::fyi(i, j, k) : C::fzi(i, j, C::D3 ? k : 0));
+}
+
+// Corner positions of the 4 cells around an edge (the cell itself is LB).
+enum : int
+{
+  LOC_LB = 0,
+  LOC_RT = 1,
+  LOC_RB = 2,
+  LOC_LT = 3
+};
+
+// reconstruct_state_{2d,3d}_at_edge (scheme/ComputeEmfAndStoreFunctor.cpp:103-367) of the cell at
+// S index sc, whose own faces are fb0 (array D0) and fb1 (array D1); LOC selects which edge of the
+// cell. Signs and shifts follow the reference's table of LB/RT/RB/LT.
+template <class C, int D0, int D1, int LOC>
+__device__ __forceinline__ void
+recon_edge(const TileView<C> & t, int sc, int fb0, int fb1, typename C::R * q)
+{
+  using R = typename C::R;
+  constexpr bool sh0 = LOC == LOC_RT || LOC == LOC_RB;
+  constexpr bool sh1 = LOC == LOC_RT || LOC == LOC_LT;
+  constexpr int  sd0 = (LOC == LOC_RT || LOC == LOC_RB) ? 1 : -1;
+  constexpr int  sd1 = (LOC == LOC_RT || LOC == LOC_LT) ? 1 : -1;
+  constexpr int  sb0 = (LOC == LOC_RT || LOC == LOC_LT) ? 1 : -1;
+  constexpr int  sb1 = (LOC == LOC_RT || LOC == LOC_RB) ? 1 : -1;
+  constexpr int  NS = C::NS;
+#pragma unroll
+  for (int v = 0; v < 8; ++v)
+    q[v] = t.q2[v * NS + sc];
+  const int f0 = fb0 + (sh0 ? f_stride<C>(D0, D0) : 0);
+  const int f1 = fb1 + (sh1 ? f_stride<C>(D1, D1) : 0);
+  const R * F0 = t.fb[D0];
+  const R * F1 = t.fb[D1];
+  R         B0 = F0[f0];
+  R         B1 = F1[f1];
+  B0 += t.sf[D0 * NS + sc + (sh0 ? s_stride<C>(D0) : 0)];
+  B1 += t.sf[D1 * NS + sc + (sh1 ? s_stride<C>(D1) : 0)];
+  const R   dB0d1 = slope1<R>(F0[f0], F0[f0 + f_stride<C>(D0, D1)], F0[f0 - f_stride<C>(D0, D1)], t.ph.slope_type);
+  const R   dB1d0 = slope1<R>(F1[f1], F1[f1 + f_stride<C>(D1, D0)], F1[f1 - f_stride<C>(D1, D0)], t.ph.slope_type);
+  const R * S0 = t.sl + D0 * 8 * NS + sc;
+  const R * S1 = t.sl + D1 * 8 * NS + sc;
+  const R   g0 = (R)sd0, g1 = (R)sd1;
+  auto      h = [&](int v) { return R(0.5) * (g0 * S0[v * NS] + g1 * S1[v * NS]); };
+#pragma unroll
+  for (int v = 0; v < 5; ++v)
+    q[v] += h(v);
+  if constexpr (C::DIM == 2)
+  {
+    q[IA] = B0 + R(0.5) * ((R)sb0 * dB0d1);
+    q[IB] = B1 + R(0.5) * ((R)sb1 * dB1d0);
+    q[IC] += h(IC);
+  }
+  else
+  {
+    // the reference's branch order for IA / IB / IC (ComputeEmfAndStoreFunctor.cpp:324-363)
+    if constexpr (D0 == 0)
+      q[IA] = B0 + R(0.5) * ((R)sb0 * dB0d1);
+    else
+      q[IA] += h(IA);
+    if constexpr (D0 == 1)
+      q[IB] = B0 + R(0.5) * ((R)sb0 * dB0d1);
+    else
+      q[IB] += h(IB);
+    if constexpr (D1 == 1)
+      q[IB] = B1 + R(0.5) * ((R)sb1 * dB1d0);
+    else
+      q[IB] += h(IB);
+    if constexpr (D1 == 2)
+      q[IC] = B1 + R(0.5) * ((R)sb1 * dB1d0);
+    else
+      q[IC] += h(IC);
+  }
+  q[ID] = rmax<R>(t.ph.smallr, q[ID]);
+  q[IP] = rmax<R>(t.ph.smallp * q[ID], q[IP]);
+}
+
+// EMFs along direction CD on the tile's edges [0, T] (ComputeEmfAndStoreFunctor.cpp:371-590), with
+// the border averaging of CorrectEmfAtBlockBorderFunctor (uniform level, .cpp:298-356)
+template <class C, int CD>
+__device__ __forceinline__ void
+edge_pass(const TileView<C> & t, int tid)
+{
+  using R = typename C::R;
+  constexpr int D0 = CD == 0 ? 1 : 0;
+  constexpr int D1 = CD == 2 ? 1 : 2;
+  constexpr int NX = CD == 0 ? C::TX : C::TX + 1;
+  constexpr int NY = CD == 1 ? C::TY : C::TY + 1;
+  constexpr int NZ = C::DIM == 3 ? (CD == 2 ? C::TZ : C::TZ + 1) : 1;
+  constexpr int s0 = s_stride<C>(D0), s1 = s_stride<C>(D1);
+  constexpr int f00 = f_stride<C>(D0, D0), f01 = f_stride<C>(D0, D1);
+  constexpr int f10 = f_stride<C>(D1, D0), f11 = f_stride<C>(D1, D1);
+  for (int m = tid; m < NX * NY * NZ; m += C::NT)
+  {
+    const int i = m % NX, j = (m / NX) % NY, k = m / (NX * NY);
+    const int sc = C::si(i, j, k);
+    const int g0 = f_index<C, D0>(i, j, k);
+    const int g1 = f_index<C, D1>(i, j, k);
+    R         qe[4][8];
+    recon_edge<C, D0, D1, LOC_LB>(t, sc, g0, g1, qe[ELB]);
+    recon_edge<C, D0, D1, LOC_RT>(t, sc - s0 - s1, g0 - f00 - f01, g1 - f10 - f11, qe[ERT]);
+    // y edges: the reference swaps the RB and LT states (ComputeEmfAndStoreFunctor.cpp:551-560)
+    recon_edge<C, D0, D1, LOC_RB>(t, sc - s0, g0 - f00, g1 - f10, qe[CD == 1 ? ELT : ERB]);
+    recon_edge<C, D0, D1, LOC_LT>(t, sc - s1, g0 - f01, g1 - f11, qe[CD == 1 ? ERB : ELT]);
+    R val = edge_emf<R, CD>(qe, t.ph) * t.dtdx;
+    // an edge on a line where four blocks meet is averaged with its sibling copies (self first,
+    // then the non-outside siblings); on a conforming mesh the copies are computed from identical
+    // data, so the sum is of equal terms
+    {
+      const int gi[3] = {t.x0 + i, t.y0 + j, t.z0 + k};
+      const int bs[3] = {t.bx, t.by, t.bz};
+      const int v0 = gi[D0] == 0 ? -1 : (gi[D0] == bs[D0] ? 1 : 0);
+      const int v1 = (C::DIM == 2 && D1 == 2) ? 0 : (gi[D1] == 0 ? -1 : (gi[D1] == bs[D1] ? 1 : 0));
+      if (v0 != 0 && v1 != 0)
+      {
+        const int sl0 = nb_slot(D0 == 0 ? v0 : 0, D0 == 1 ? v0 : 0, 0);
+        const int sl1 = nb_slot(D1 == 0 ? v1 : 0, D1 == 1 ? v1 : 0, D1 == 2 ? v1 : 0);
+        const int sl2 = nb_slot(D0 == 0 ? v0 : (D1 == 0 ? v1 : 0), D0 == 1 ? v0 : (D1 == 1 ? v1 : 0), D1 == 2 ? v1 : 0);
+        const int n0 = t.s_nbr[sl0], n1 = t.s_nbr[sl1], n2 = t.s_nbr[sl2];
+        if (n0 >= 0 && n1 >= 0 && n2 >= 0)
+        {
+          R   acc = R(0);
+          int count = 1;
+          acc += val;
+          if (n0 < t.n_owned)
+          {
+            acc += val;
+            count++;
+          }
+          if (n1 < t.n_owned)
+          {
+            acc += val;
+            count++;
+          }
+          if (n2 < t.n_owned)
+          {
+            acc += val;
+            count++;
+          }
+          val = acc / (R)count;
+        }
+      }
+    }
+    t.emfd[(C::DIM == 3 ? CD : 0) * C::NM + C::mi(i, j, k)] = to_d<R>(val);
+  }
+}
+
+// Fluxes through the tile's faces normal to D (ComputeHydroFluxesAndStoreFunctor.cpp:335-503):
+// left state from cell i-1, right state from cell i, normal B = face value + sFaceMag.
+template <class C, int D>
+__device__ __forceinline__ void
+flux_pass(const TileView<C> & t, int tid)
+{
+  using R = typename C::R;
+  constexpr int NX = C::TX + (D == 0), NY = C::TY + (D == 1), NZ = C::TZ + (D == 2 && C::D3);
+  constexpr int OFF = D == 0 ? 0 : (D == 1 ? C::NF_X : C::NF_X + C::NF_Y);
+  constexpr int ivel = D == 0 ? IU : (D == 1 ? IV : IW);
+  constexpr int imag = D == 0 ? IA : (D == 1 ? IB : IC);
+  constexpr int NS = C::NS;
+  const R *     S = t.sl + D * 8 * NS;
+  for (int m = tid; m < NX * NY * NZ; m += C::NT)
+  {
+    const int i = m % NX, j = (m / NX) % NY, k = m / (NX * NY);
+    const int snR = C::si(i, j, k);
+    const int snL = snR - s_stride<C>(D);
+    R         qL[8], qR[8], flux[8];
+#pragma unroll
+    for (int v = 0; v < 8; ++v)
+    {
+      qL[v] = t.q2[v * NS + snL] + R(0.5) * S[v * NS + snL];
+      qR[v] = t.q2[v * NS + snR] + R(-0.5) * S[v * NS + snR];
+    }
+    qL[ID] = rmax<R>(t.ph.smallr, qL[ID]);
+    qL[IP] = rmax<R>(t.ph.smallp * qL[ID], qL[IP]);
+    qR[ID] = rmax<R>(t.ph.smallr, qR[ID]);
+    qR[IP] = rmax<R>(t.ph.smallp * qR[ID], qR[IP]);
+    const R bn = t.fb[D][f_index<C, D>(i, j, k)] + t.sf[D * NS + snR];
+    qR[imag] = bn;
+    qL[imag] = bn;
+    if constexpr (D != 0)
+    {
+      R tmp;
+      tmp = qL[IU]; qL[IU] = qL[ivel]; qL[ivel] = tmp;
+      tmp = qR[IU]; qR[IU] = qR[ivel]; qR[ivel] = tmp;
+      tmp = qL[IA]; qL[IA] = qL[imag]; qL[imag] = tmp;
+      tmp = qR[IA]; qR[IA] = qR[imag]; qR[imag] = tmp;
+    }
+    riemann_mhd<R>(qL, qR, flux, t.ph);
+    if constexpr (D != 0)
+    {
+      R tmp;
+      tmp = flux[IU]; flux[IU] = flux[ivel]; flux[ivel] = tmp;
+      tmp = flux[IA]; flux[IA] = flux[imag]; flux[imag] = tmp;
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v)
+      t.fl[v * C::NFT + OFF + m] = flux[v] * t.dtdx;
+    if constexpr (C::DIM == 2)
+      t.fl[5 * C::NFT + OFF + m] = flux[IC] * t.dtdx;
+  }
+}
+
 template <class C>
 __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
 {
@@ -236,65 +476,116 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
   auto cell_off = [](int c, int n) { return c < 0 ? -1 : (c >= n ? 1 : 0); };
   auto face_off = [](int f, int n) { return f < 0 ? -1 : (f > n ? 1 : 0); };
 
-  // ---- phase 1a: face B at t^n into shared memory (FillBlockGhostFaces equivalent) -----------
-  for (int n = tid; n < C::NFBX; n += NT)
+  // ---- phase 1: gather face B at t^n (FillBlockGhostFaces equivalent) and the conservative state
+  // of the Q region. Every global load of the phase is issued before any is consumed, so HBM latency
+  // is paid once for the phase rather than once per loop trip.
+  constexpr int ITX = (C::NFBX + NT - 1) / NT;
+  constexpr int ITY = (C::NFBY + NT - 1) / NT;
+  constexpr int ITZ = (C::NFBZ + NT - 1) / NT;
+  constexpr int ITQ = (C::NQ + NT - 1) / NT;
+  double        fvx[ITX], fvy[ITY], fvz[ITZ];
+  double        uq[ITQ][5];
+#pragma unroll
+  for (int it = 0; it < ITX; ++it)
   {
-    const int i = n % (TX + 5) - 2;
-    const int j = (n / (TX + 5)) % C::QY - 2;
-    const int k = D3 ? n / ((TX + 5) * C::QY) - 2 : 0;
-    const int fi = x0 + i, cj = y0 + j, ck = z0 + k;
-    const int ox = face_off(fi, bx), oy = cell_off(cj, by), oz = D3 ? cell_off(ck, bz) : 0;
-    const int nb = owner(ox, oy, oz);
-    R         v = R(0);
-    if (nb >= 0)
-      v = to_r<R>(a.B[(int64_t)nb * a.nface + (fi - ox * bx) + (int64_t)(bx + 1) * ((cj - oy * by) + (int64_t)by * (ck - oz * bz))]);
-    fbx[n] = v;
+    const int n = tid + it * NT;
+    fvx[it] = 0.0;
+    if (n < C::NFBX)
+    {
+      const int i = n % (TX + 5) - 2;
+      const int j = (n / (TX + 5)) % C::QY - 2;
+      const int k = D3 ? n / ((TX + 5) * C::QY) - 2 : 0;
+      const int fi = x0 + i, cj = y0 + j, ck = z0 + k;
+      const int ox = face_off(fi, bx), oy = cell_off(cj, by), oz = D3 ? cell_off(ck, bz) : 0;
+      const int nb = owner(ox, oy, oz);
+      if (nb >= 0)
+        fvx[it] = a.B[(int64_t)nb * a.nface + (fi - ox * bx) + (int64_t)(bx + 1) * ((cj - oy * by) + (int64_t)by * (ck - oz * bz))];
+    }
   }
-  for (int n = tid; n < C::NFBY; n += NT)
+#pragma unroll
+  for (int it = 0; it < ITY; ++it)
   {
-    const int i = n % C::QX - 2;
-    const int j = (n / C::QX) % (TY + 5) - 2;
-    const int k = D3 ? n / (C::QX * (TY + 5)) - 2 : 0;
-    const int ci = x0 + i, fj = y0 + j, ck = z0 + k;
-    const int ox = cell_off(ci, bx), oy = face_off(fj, by), oz = D3 ? cell_off(ck, bz) : 0;
-    const int nb = owner(ox, oy, oz);
-    R         v = R(0);
-    if (nb >= 0)
-      v = to_r<R>(a.B[(int64_t)nb * a.nface + a.nfx + (ci - ox * bx) + (int64_t)bx * ((fj - oy * by) + (int64_t)(by + 1) * (ck - oz * bz))]);
-    fby[n] = v;
+    const int n = tid + it * NT;
+    fvy[it] = 0.0;
+    if (n < C::NFBY)
+    {
+      const int i = n % C::QX - 2;
+      const int j = (n / C::QX) % (TY + 5) - 2;
+      const int k = D3 ? n / (C::QX * (TY + 5)) - 2 : 0;
+      const int ci = x0 + i, fj = y0 + j, ck = z0 + k;
+      const int ox = cell_off(ci, bx), oy = face_off(fj, by), oz = D3 ? cell_off(ck, bz) : 0;
+      const int nb = owner(ox, oy, oz);
+      if (nb >= 0)
+        fvy[it] = a.B[(int64_t)nb * a.nface + a.nfx + (ci - ox * bx) + (int64_t)bx * ((fj - oy * by) + (int64_t)(by + 1) * (ck - oz * bz))];
+    }
   }
-  for (int n = tid; n < C::NFBZ; n += NT)
+#pragma unroll
+  for (int it = 0; it < ITZ; ++it)
   {
-    const int i = n % C::QX - 2;
-    const int j = (n / C::QX) % C::QY - 2;
-    const int k = D3 ? n / (C::QX * C::QY) - 2 : 0;
-    const int ci = x0 + i, cj = y0 + j, fk = z0 + k;
-    const int ox = cell_off(ci, bx), oy = cell_off(cj, by), oz = D3 ? face_off(fk, bz) : 0;
-    const int nb = owner(ox, oy, oz);
-    R         v = R(0);
-    if (nb >= 0)
-      v = to_r<R>(a.B[(int64_t)nb * a.nface + a.nfx + a.nfy + (ci - ox * bx) + (int64_t)bx * ((cj - oy * by) + (int64_t)by * (fk - oz * bz))]);
-    fbz[n] = v;
+    const int n = tid + it * NT;
+    fvz[it] = 0.0;
+    if (n < C::NFBZ)
+    {
+      const int i = n % C::QX - 2;
+      const int j = (n / C::QX) % C::QY - 2;
+      const int k = D3 ? n / (C::QX * C::QY) - 2 : 0;
+      const int ci = x0 + i, cj = y0 + j, fk = z0 + k;
+      const int ox = cell_off(ci, bx), oy = cell_off(cj, by), oz = D3 ? face_off(fk, bz) : 0;
+      const int nb = owner(ox, oy, oz);
+      if (nb >= 0)
+        fvz[it] = a.B[(int64_t)nb * a.nface + a.nfx + a.nfy + (ci - ox * bx) + (int64_t)bx * ((cj - oy * by) + (int64_t)by * (fk - oz * bz))];
+    }
   }
+#pragma unroll
+  for (int it = 0; it < ITQ; ++it)
+  {
+    const int n = tid + it * NT;
+    uq[it][0] = 1.0;
+    uq[it][1] = 1.0;
+    uq[it][2] = uq[it][3] = uq[it][4] = 0.0;
+    if (n < C::NQ)
+    {
+      const int i = n % C::QX - 2;
+      const int j = (n / C::QX) % C::QY - 2;
+      const int k = D3 ? n / (C::QX * C::QY) - 2 : 0;
+      const int ci = x0 + i, cj = y0 + j, ck = z0 + k;
+      const int ox = cell_off(ci, bx), oy = cell_off(cj, by), oz = D3 ? cell_off(ck, bz) : 0;
+      const int nb = owner(ox, oy, oz);
+      if (nb >= 0)
+      {
+        const double * Ub = a.U + (int64_t)nb * 5 * a.ncell + (ci - ox * bx) + (int64_t)bx * ((cj - oy * by) + (int64_t)by * (ck - oz * bz));
+#pragma unroll
+        for (int v = 0; v < 5; ++v)
+          uq[it][v] = Ub[(int64_t)v * a.ncell];
+      }
+    }
+  }
+#pragma unroll
+  for (int it = 0; it < ITX; ++it)
+    if (tid + it * NT < C::NFBX)
+      fbx[tid + it * NT] = to_r<R>(fvx[it]);
+#pragma unroll
+  for (int it = 0; it < ITY; ++it)
+    if (tid + it * NT < C::NFBY)
+      fby[tid + it * NT] = to_r<R>(fvy[it]);
+#pragma unroll
+  for (int it = 0; it < ITZ; ++it)
+    if (tid + it * NT < C::NFBZ)
+      fbz[tid + it * NT] = to_r<R>(fvz[it]);
   __syncthreads();
 
-  // ---- phase 1b: primitive variables on the Q region (ConvertToPrimitivesVariablesFunctor) ---
-  for (int n = tid; n < C::NQ; n += NT)
+  // primitive variables on the Q region (ConvertToPrimitivesVariablesFunctor)
+#pragma unroll
+  for (int it = 0; it < ITQ; ++it)
   {
+    const int n = tid + it * NT;
+    if (n >= C::NQ)
+      continue;
     const int i = n % C::QX - 2;
     const int j = (n / C::QX) % C::QY - 2;
     const int k = D3 ? n / (C::QX * C::QY) - 2 : 0;
     const int ci = x0 + i, cj = y0 + j, ck = z0 + k;
-    const int ox = cell_off(ci, bx), oy = cell_off(cj, by), oz = D3 ? cell_off(ck, bz) : 0;
-    const int nb = owner(ox, oy, oz);
-    double    u[5] = {1.0, 1.0, 0.0, 0.0, 0.0};
-    if (nb >= 0)
-    {
-      const double * Ub = a.U + (int64_t)nb * 5 * a.ncell + (ci - ox * bx) + (int64_t)bx * ((cj - oy * by) + (int64_t)by * (ck - oz * bz));
-#pragma unroll
-      for (int v = 0; v < 5; ++v)
-        u[v] = Ub[(int64_t)v * a.ncell];
-    }
+    const double * u = uq[it];
     const int qn = C::qi(i, j, k);
     if constexpr (C::EXACT)
     {
@@ -562,264 +853,45 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
   }
   __syncthreads(); // qh (primitives at t^n) and ee are dead from here on
 
-  // face value at t^n of component c (0..2) at tile coords, and its limited slope along dir
-  auto fval = [&](int c, int i, int j, int k) -> R {
-    return c == 0 ? fbx[C::fxi(i, j, k)] : (c == 1 ? fby[C::fyi(i, j, k)] : fbz[C::fzi(i, j, D3 ? k : 0)]);
-  };
-  auto fslope = [&](int c, int i, int j, int k, int dir) -> R {
-    const int di = dir == 0, dj = dir == 1, dk = dir == 2;
-    return slope1<R>(fval(c, i, j, k), fval(c, i + di, j + dj, k + dk), fval(c, i - di, j - dj, k - dk), ph.slope_type);
-  };
-
-  // ---- phase 5: one work list of edge EMFs (ComputeEmfAndStoreFunctor.cpp:103-590, with the
-  // border averaging of CorrectEmfAtBlockBorderFunctor) and face fluxes of all directions
-  // (ComputeHydroFluxesAndStoreFunctor.cpp:335-503), balanced over the CTA's threads
-  for (int n = tid; n < C::NEDGE + C::NFT; n += NT)
+  // ---- phase 5: edge EMFs and face fluxes, one pass per direction; no barrier between passes
   {
-    if (n < C::NEDGE)
+    TileView<C> tv;
+    tv.fb[0] = fbx;
+    tv.fb[1] = fby;
+    tv.fb[2] = fbz;
+    tv.sl = sl;
+    tv.q2 = q2;
+    tv.sf = sf;
+    tv.emfd = emfd;
+    tv.fl = fl;
+    tv.s_nbr = s_nbr;
+    tv.ph = ph;
+    tv.dtdx = dtdx;
+    tv.x0 = x0;
+    tv.y0 = y0;
+    tv.z0 = z0;
+    tv.bx = bx;
+    tv.by = by;
+    tv.bz = bz;
+    tv.n_owned = a.n_owned;
+    edge_pass<C, 2>(tv, tid);
+    if constexpr (DIM == 3)
     {
-      int c, i, j, k;
-      if (n < C::NEZ)
-      {
-        c = 2;
-        i = n % (TX + 1);
-        j = (n / (TX + 1)) % (TY + 1);
-        k = n / ((TX + 1) * (TY + 1));
-      }
-      else if (n < C::NEZ + C::NEY)
-      {
-        const int m = n - C::NEZ;
-        c = 1;
-        i = m % (TX + 1);
-        j = (m / (TX + 1)) % TY;
-        k = m / ((TX + 1) * TY);
-      }
-      else
-      {
-        const int m = n - C::NEZ - C::NEY;
-        c = 0;
-        i = m % TX;
-        j = (m / TX) % (TY + 1);
-        k = m / (TX * (TY + 1));
-      }
-        R qe[4][8];
-        // states at t^{n+1/2} reconstructed to the edge from the 4 surrounding cells
-        auto recon = [&](int is, int js, int ks, int loc, int dir0, int dir1, R * q) {
-          const int sn = C::si(is, js, ks);
-  #pragma unroll
-          for (int v = 0; v < 8; ++v)
-            q[v] = q2[v * C::NS + sn];
-          int sd0 = 1, sd1 = 1, sb0 = 1, sb1 = 1;
-          int i0 = is, j0 = js, k0 = ks, i1 = is, j1 = js, k1 = ks;
-          // loc: 0 = LB, 1 = RT, 2 = RB, 3 = LT
-          if (loc == 0)
-          {
-            sd0 = -1; sd1 = -1; sb0 = -1; sb1 = -1;
-          }
-          else if (loc == 1)
-          {
-            i0 += dir0 == 0; j0 += dir0 == 1; k0 += dir0 == 2;
-            i1 += dir1 == 0; j1 += dir1 == 1; k1 += dir1 == 2;
-          }
-          else if (loc == 2)
-          {
-            i0 += dir0 == 0; j0 += dir0 == 1; k0 += dir0 == 2;
-            sd1 = -1; sb0 = -1;
-          }
-          else
-          {
-            i1 += dir1 == 0; j1 += dir1 == 1; k1 += dir1 == 2;
-            sd0 = -1; sb1 = -1;
-          }
-          const R * S0 = sl + dir0 * 8 * C::NS;
-          const R * S1 = sl + dir1 * 8 * C::NS;
-          const R   f0 = (R)sd0, f1 = (R)sd1;
-          if constexpr (DIM == 2)
-          {
-            // reconstruct_state_2d_at_edge (dir0 = X, dir1 = Y)
-            R A = fbx[C::fxi(i0, j0, 0)];
-            R Bv = fby[C::fyi(i1, j1, 0)];
-            A += sf[0 * C::NS + C::si(i0, j0, 0)];
-            Bv += sf[1 * C::NS + C::si(i1, j1, 0)];
-            const R dAy = fslope(0, i0, j0, 0, 1);
-            const R dBx = fslope(1, i1, j1, 0, 0);
-  #pragma unroll
-            for (int v = 0; v < 5; ++v)
-              q[v] += R(0.5) * (f0 * S0[v * C::NS + sn] + f1 * S1[v * C::NS + sn]);
-            q[IA] = A + R(0.5) * ((R)sb0 * dAy);
-            q[IB] = Bv + R(0.5) * ((R)sb1 * dBx);
-            q[IC] += R(0.5) * (f0 * S0[IC * C::NS + sn] + f1 * S1[IC * C::NS + sn]);
-          }
-          else
-          {
-            // reconstruct_state_3d_at_edge, with the reference's branch order for IA/IB/IC
-            R B0 = fval(dir0, i0, j0, k0);
-            R B1 = fval(dir1, i1, j1, k1);
-            B0 += sf[dir0 * C::NS + C::si(i0, j0, k0)];
-            B1 += sf[dir1 * C::NS + C::si(i1, j1, k1)];
-            const R dB0d1 = fslope(dir0, i0, j0, k0, dir1);
-            const R dB1d0 = fslope(dir1, i1, j1, k1, dir0);
-            auto    h = [&](int v) { return R(0.5) * (f0 * S0[v * C::NS + sn] + f1 * S1[v * C::NS + sn]); };
-  #pragma unroll
-            for (int v = 0; v < 5; ++v)
-              q[v] += h(v);
-            if (dir0 == 0)
-              q[IA] = B0 + R(0.5) * ((R)sb0 * dB0d1);
-            else
-              q[IA] += h(IA);
-            if (dir0 == 1)
-              q[IB] = B0 + R(0.5) * ((R)sb0 * dB0d1);
-            else
-              q[IB] += h(IB);
-            if (dir1 == 1)
-              q[IB] = B1 + R(0.5) * ((R)sb1 * dB1d0);
-            else
-              q[IB] += h(IB);
-            if (dir1 == 2)
-              q[IC] = B1 + R(0.5) * ((R)sb1 * dB1d0);
-            else
-              q[IC] += h(IC);
-          }
-          q[ID] = rmax<R>(ph.smallr, q[ID]);
-          q[IP] = rmax<R>(ph.smallp * q[ID], q[IP]);
-        };
-        R val;
-        if (c == 2)
-        {
-          recon(i, j, k, 0, 0, 1, qe[ELB]);
-          recon(i - 1, j - 1, k, 1, 0, 1, qe[ERT]);
-          recon(i - 1, j, k, 2, 0, 1, qe[ERB]);
-          recon(i, j - 1, k, 3, 0, 1, qe[ELT]);
-          val = edge_emf<R>(qe, 2, ph) * dtdx;
-        }
-        else if (c == 1)
-        {
-          recon(i, j, k, 0, 0, 2, qe[ELB]);
-          recon(i - 1, j, k - 1, 1, 0, 2, qe[ERT]);
-          // the reference swaps the RB and LT states of y edges
-          recon(i - 1, j, k, 2, 0, 2, qe[ELT]);
-          recon(i, j, k - 1, 3, 0, 2, qe[ERB]);
-          val = edge_emf<R>(qe, 1, ph) * dtdx;
-        }
-        else
-        {
-          recon(i, j, k, 0, 1, 2, qe[ELB]);
-          recon(i, j - 1, k - 1, 1, 1, 2, qe[ERT]);
-          recon(i, j - 1, k, 2, 1, 2, qe[ERB]);
-          recon(i, j, k - 1, 3, 1, 2, qe[ELT]);
-          val = edge_emf<R>(qe, 0, ph) * dtdx;
-        }
-        // CorrectEmfAtBlockBorderFunctor (uniform level): an edge on a line where four blocks meet
-        // is averaged with its sibling copies (self first, then the non-outside siblings). On a
-        // conforming mesh every copy is computed from identical data, so the sum is of equal terms.
-        {
-          const int t0 = c == 0 ? 1 : 0;
-          const int t1 = c == 2 ? 1 : 2;
-          const int gidx[3] = {x0 + i, y0 + j, z0 + k};
-          const int bsz[3] = {bx, by, bz};
-          const int v0 = gidx[t0] == 0 ? -1 : (gidx[t0] == bsz[t0] ? 1 : 0);
-          const int v1 = (DIM == 2 && t1 == 2) ? 0 : (gidx[t1] == 0 ? -1 : (gidx[t1] == bsz[t1] ? 1 : 0));
-          if (v0 != 0 && v1 != 0)
-          {
-            int o0[3] = {0, 0, 0}, o1[3] = {0, 0, 0}, o2[3] = {0, 0, 0};
-            o0[t0] = v0;
-            o1[t1] = v1;
-            o2[t0] = v0;
-            o2[t1] = v1;
-            const int s0 = s_nbr[nb_slot(o0[0], o0[1], o0[2])];
-            const int s1 = s_nbr[nb_slot(o1[0], o1[1], o1[2])];
-            const int s2 = s_nbr[nb_slot(o2[0], o2[1], o2[2])];
-            if (s0 >= 0 && s1 >= 0 && s2 >= 0)
-            {
-              R   acc = R(0);
-              int count = 1;
-              acc += val;
-              if (s0 < a.n_owned)
-              {
-                acc += val;
-                count++;
-              }
-              if (s1 < a.n_owned)
-              {
-                acc += val;
-                count++;
-              }
-              if (s2 < a.n_owned)
-              {
-                acc += val;
-                count++;
-              }
-              val = acc / (R)count;
-            }
-          }
-        }
-        emfd[(DIM == 3 ? c : 0) * C::NM + C::mi(i, j, k)] = to_d<R>(val);
+      edge_pass<C, 1>(tv, tid);
+      edge_pass<C, 0>(tv, tid);
     }
-    else
-    {
-      // face flux: left state from cell i-1, right state from cell i along dir
-      const int m = n - C::NEDGE;
-      int       dir, l, fx_n, fy_n;
-      if (m < C::NF_X)
-      {
-        dir = 0; l = m; fx_n = TX + 1; fy_n = TY;
-      }
-      else if (m < C::NF_X + C::NF_Y)
-      {
-        dir = 1; l = m - C::NF_X; fx_n = TX; fy_n = TY + 1;
-      }
-      else
-      {
-        dir = 2; l = m - C::NF_X - C::NF_Y; fx_n = TX; fy_n = TY;
-      }
-      const int i = l % fx_n, j = (l / fx_n) % fy_n, k = l / (fx_n * fy_n);
-      const int di = dir == 0, dj = dir == 1, dk = dir == 2;
-      const int ivel = dir == 0 ? IU : (dir == 1 ? IV : IW);
-      const int imag = dir == 0 ? IA : (dir == 1 ? IB : IC);
-      const int snL = C::si(i - di, j - dj, k - dk);
-      const int snR = C::si(i, j, k);
-      const R * S = sl + dir * 8 * C::NS;
-      R         qL[8], qR[8], flux[8];
-#pragma unroll
-      for (int v = 0; v < 8; ++v)
-      {
-        qL[v] = q2[v * C::NS + snL] + R(0.5) * S[v * C::NS + snL];
-        qR[v] = q2[v * C::NS + snR] + R(-0.5) * S[v * C::NS + snR];
-      }
-      qL[ID] = rmax<R>(ph.smallr, qL[ID]);
-      qL[IP] = rmax<R>(ph.smallp * qL[ID], qL[IP]);
-      qR[ID] = rmax<R>(ph.smallr, qR[ID]);
-      qR[IP] = rmax<R>(ph.smallp * qR[ID], qR[IP]);
-      const R bn = fval(dir, i, j, k) + sf[dir * C::NS + snR];
-      qR[imag] = bn;
-      qL[imag] = bn;
-      if (dir != 0)
-      {
-        R tmp;
-        tmp = qL[IU]; qL[IU] = qL[ivel]; qL[ivel] = tmp;
-        tmp = qR[IU]; qR[IU] = qR[ivel]; qR[ivel] = tmp;
-        tmp = qL[IA]; qL[IA] = qL[imag]; qL[imag] = tmp;
-        tmp = qR[IA]; qR[IA] = qR[imag]; qR[imag] = tmp;
-      }
-      riemann_mhd<R>(qL, qR, flux, ph);
-      if (dir != 0)
-      {
-        R tmp;
-        tmp = flux[IU]; flux[IU] = flux[ivel]; flux[ivel] = tmp;
-        tmp = flux[IA]; flux[IA] = flux[imag]; flux[imag] = tmp;
-      }
-#pragma unroll
-      for (int v = 0; v < 5; ++v)
-        fl[v * C::NFT + m] = flux[v] * dtdx;
-      if constexpr (DIM == 2)
-        fl[5 * C::NFT + m] = flux[IC] * dtdx;
-    }
+    flux_pass<C, 0>(tv, tid);
+    flux_pass<C, 1>(tv, tid);
+    if constexpr (DIM == 3)
+      flux_pass<C, 2>(tv, tid);
   }
   __syncthreads();
 
   // ---- phase 6: CT update (ReadEmfAndUpdateFunctor.cpp:58-163) on faces [0, T] along each
   // normal; a tile writes faces [0, T) and face T when it ends at the block border, and keeps all
-  // of them in shared memory for the CFL of the updated cells
+  // of them in shared memory for the CFL of the updated cells. The face loads of this phase and the
+  // conservative state of phase 7 are issued together, before either is used.
+  double upre[C::CPT][C::NFV];
   {
     const double * Mx = emfd;
     const double * My = emfd + (DIM == 3 ? C::NM : 0);
@@ -827,16 +899,61 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
     const bool     ex = (x0 + TX == bx), ey = (y0 + TY == by), ez = (z0 + TZ == bz);
     double *       B2blk = a.B2 + (int64_t)blk * a.nface;
     const double * Bblk = a.B + (int64_t)blk * a.nface;
-    for (int n = tid; n < C::NB2; n += NT)
-    {
-      int64_t g;
-      double  bnew;
-      bool    owned;
+    // block-local face index of shared-memory face item n
+    auto face_g = [&](int n) -> int64_t {
       if (n < C::NB2X)
       {
         const int i = n % (TX + 1), j = (n / (TX + 1)) % TY, k = n / ((TX + 1) * TY);
-        g = (x0 + i) + (int64_t)(bx + 1) * ((y0 + j) + (int64_t)by * (z0 + k));
-        double d = 0;
+        return (x0 + i) + (int64_t)(bx + 1) * ((y0 + j) + (int64_t)by * (z0 + k));
+      }
+      if (n < C::NB2X + C::NB2Y)
+      {
+        const int nn = n - C::NB2X;
+        const int i = nn % TX, j = (nn / TX) % (TY + 1), k = nn / (TX * (TY + 1));
+        return a.nfx + (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)(by + 1) * (z0 + k));
+      }
+      const int nn = n - C::NB2X - C::NB2Y;
+      const int i = nn % TX, j = (nn / TX) % TY, k = nn / (TX * TY);
+      return a.nfx + a.nfy + (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)by * (z0 + k));
+    };
+    constexpr int ITB = (C::NB2 + NT - 1) / NT;
+    double        bold[ITB];
+#pragma unroll
+    for (int it = 0; it < ITB; ++it)
+    {
+      const int n = tid + it * NT;
+      bold[it] = n < C::NB2 ? Bblk[face_g(n)] : 0.0;
+    }
+#pragma unroll
+    for (int c = 0; c < C::CPT; ++c)
+    {
+      const int n = tid + c * NT;
+#pragma unroll
+      for (int v = 0; v < C::NFV; ++v)
+        upre[c][v] = 0.0;
+      if (n < C::NCELL)
+      {
+        const int     i = n % TX, j = (n / TX) % TY, k = n / (TX * TY);
+        const int64_t cell = (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)by * (z0 + k));
+#pragma unroll
+        for (int v = 0; v < 5; ++v)
+          upre[c][v] = a.U[((int64_t)blk * 5 + v) * a.ncell + cell];
+        if constexpr (DIM == 2)
+          upre[c][5] = a.B[(int64_t)blk * a.nface + a.nfx + a.nfy + cell];
+      }
+    }
+#pragma unroll
+    for (int it = 0; it < ITB; ++it)
+    {
+      const int n = tid + it * NT;
+      if (n >= C::NB2)
+        continue;
+      double bnew;
+      bool   owned;
+      if (n < C::NB2X)
+      {
+        const int i = n % (TX + 1), j = (n / (TX + 1)) % TY, k = n / ((TX + 1) * TY);
+        double    d = 0;
         if constexpr (DIM == 2)
           d += (Mz[C::mi(i, j + 1, 0)] - Mz[C::mi(i, j, 0)]);
         else
@@ -844,22 +961,21 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
           d += (Mz[C::mi(i, j + 1, k)] - Mz[C::mi(i, j, k)]);
           d -= (My[C::mi(i, j, k + 1)] - My[C::mi(i, j, k)]);
         }
-        bnew = Bblk[g] + d;
+        bnew = bold[it] + d;
         owned = i < TX || ex;
       }
       else if (n < C::NB2X + C::NB2Y)
       {
         const int nn = n - C::NB2X;
         const int i = nn % TX, j = (nn / TX) % (TY + 1), k = nn / (TX * (TY + 1));
-        g = a.nfx + (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)(by + 1) * (z0 + k));
         if constexpr (DIM == 2)
-          bnew = Bblk[g] - (Mz[C::mi(i + 1, j, 0)] - Mz[C::mi(i, j, 0)]);
+          bnew = bold[it] - (Mz[C::mi(i + 1, j, 0)] - Mz[C::mi(i, j, 0)]);
         else
         {
           double d = 0;
           d += (Mx[C::mi(i, j, k + 1)] - Mx[C::mi(i, j, k)]);
           d -= (Mz[C::mi(i + 1, j, k)] - Mz[C::mi(i, j, k)]);
-          bnew = Bblk[g] + d;
+          bnew = bold[it] + d;
         }
         owned = j < TY || ey;
       }
@@ -867,15 +983,14 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       {
         const int nn = n - C::NB2X - C::NB2Y;
         const int i = nn % TX, j = (nn / TX) % TY, k = nn / (TX * TY);
-        g = a.nfx + a.nfy + (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)by * (z0 + k));
-        double d = 0;
+        double    d = 0;
         d += (My[C::mi(i + 1, j, k)] - My[C::mi(i, j, k)]);
         d -= (Mx[C::mi(i, j + 1, k)] - Mx[C::mi(i, j, k)]);
-        bnew = Bblk[g] + d;
+        bnew = bold[it] + d;
         owned = k < TZ || ez;
       }
       if (owned)
-        B2blk[g] = bnew;
+        B2blk[face_g(n)] = bnew;
       b2s[n] = to_r<R>(bnew);
     }
   }
@@ -884,7 +999,7 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
   // ---- phase 7: conservative update (ReadFluxesAndConservativeUpdateFunctor.cpp:240-436),
   // write U2 (and 2D Bz), fused CFL of the new state (ComputeDtMHDFunctor.cpp:86-151) ----------
   double my_invdt = 0.0;
-#pragma unroll 1
+#pragma unroll
   for (int c = 0; c < C::CPT; ++c)
   {
     const int n = tid + c * NT;
@@ -894,10 +1009,8 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
     const int64_t cell = (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)by * (z0 + k));
     double        u2[C::NFV];
 #pragma unroll
-    for (int v = 0; v < 5; ++v)
-      u2[v] = a.U[((int64_t)blk * 5 + v) * a.ncell + cell];
-    if constexpr (DIM == 2)
-      u2[5] = a.B[(int64_t)blk * a.nface + a.nfx + a.nfy + cell];
+    for (int v = 0; v < C::NFV; ++v)
+      u2[v] = upre[c][v];
     R dU[C::NFV];
 #pragma unroll
     for (int v = 0; v < C::NFV; ++v)

@@ -460,23 +460,17 @@ enum : int
 
 // compute_emf<dir> + mag_riemann2d_hlld (models/RiemannSolvers_MHD.h:629-869, 890-1097).
 // qe[ERT..ELB] are the reconstructed edge states; emf_dir 0 (EMFX), 1 (EMFY), 2 (EMFZ).
-template <typename R>
+template <typename R, int EMF_DIR>
 __device__ R
-edge_emf(const R (*qe)[8], int emf_dir, const Phys<R> & s)
+edge_emf(const R (*qe)[8], const Phys<R> & s)
 {
-  int iu, iv, iw, ia, ib, ic;
-  if (emf_dir == 2)
-  {
-    iu = IU; iv = IV; iw = IW; ia = IA; ib = IB; ic = IC;
-  }
-  else if (emf_dir == 1)
-  {
-    iu = IW; iv = IU; iw = IV; ia = IC; ib = IA; ic = IB;
-  }
-  else
-  {
-    iu = IV; iv = IW; iw = IU; ia = IB; ib = IC; ic = IA;
-  }
+  // (first, second parallel velocity; orthogonal velocity) and the same for B
+  constexpr int iu = EMF_DIR == 2 ? IU : (EMF_DIR == 1 ? IW : IV);
+  constexpr int iv = EMF_DIR == 2 ? IV : (EMF_DIR == 1 ? IU : IW);
+  constexpr int iw = EMF_DIR == 2 ? IW : (EMF_DIR == 1 ? IV : IU);
+  constexpr int ia = EMF_DIR == 2 ? IA : (EMF_DIR == 1 ? IC : IB);
+  constexpr int ib = EMF_DIR == 2 ? IB : (EMF_DIR == 1 ? IA : IC);
+  constexpr int ic = EMF_DIR == 2 ? IC : (EMF_DIR == 1 ? IB : IA);
   const R *qRT = qe[ERT], *qLT = qe[ELT], *qRB = qe[ERB], *qLB = qe[ELB];
   // 4 states (LL, RL, LR, RR) in the rotated frame
   const R rLL = qRT[ID], rRL = qLT[ID], rLR = qRB[ID], rRR = qLB[ID];
