@@ -47,6 +47,9 @@ class BlockMesh:
     scaling_factor: float = 1.0
     outside_src: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     outside_normal: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.int32))
+    # [n_blocks, 27, 8] leaves covering a neighbour region one level finer (children x fastest,
+    # -1 where absent); None on meshes without level jumps
+    fine_neighbor: np.ndarray | None = None
 
     @property
     def n_blocks(self) -> int:
@@ -68,6 +71,18 @@ class BlockMesh:
     @property
     def nface(self) -> int:
         return sum(self.face_counts)
+
+    @property
+    def is_amr(self) -> bool:
+        return self.fine_neighbor is not None or bool(np.any(self.level[: self.n_owned] != self.level[0]))
+
+    def domain_length(self, d: int) -> float:
+        """Extent of the domain along axis d (``grid`` counts blocks at the finest level)."""
+        return self.grid[d] * self.block[d] * self.cell_length(int(self.level[: self.n_owned].max()))
+
+    def block_dx(self) -> np.ndarray:
+        """Cell length per block: (1 / (bx * 2^level)) * scaling_factor."""
+        return (1.0 / (float(self.block[0]) * np.exp2(self.level.astype(np.float64)))) * self.scaling_factor
 
     def cell_length(self, level: int | None = None) -> float:
         """dx = (1 / (bx * 2^level)) * scaling_factor (core compute_cell_length, unit brick)."""
@@ -162,6 +177,162 @@ class BlockMesh:
                          scaling_factor=scaling_factor,
                          outside_src=np.array(out_src, dtype=np.int32),
                          outside_normal=np.array(out_normal, dtype=np.int32).reshape(-1, 3))
+
+    @staticmethod
+    def amr(dim: int, refine, bricks=(1, 1, 1), base_level: int = 1, max_level: int = 2, block=(16, 16, 16),
+            periodic=(True, True, True), scaling_factor: float = 1.0) -> "BlockMesh":
+        """Leaves of a brick forest refined from ``base_level`` up to ``max_level`` where
+        ``refine(level, lo, hi)`` is true for the leaf's box [lo, hi) (unit-brick coordinates, 3
+        components), then 2:1-balanced across faces, edges and corners (p4est's full balance).
+
+        Neighbour region o of a leaf at level L is: a leaf at L (``neighbor``), part of a leaf at
+        L-1 (``neighbor`` = that leaf), split into leaves at L+1 (``neighbor`` = -1 and
+        ``fine_neighbor[b, slot]`` = the 2^d children, x fastest), or an outside block at L. Outside
+        blocks need a same-level inside leaf across the border (FillOutside.cpp:134-145 looks the
+        inside quadrant up at the outside quadrant's level)."""
+        if dim not in (2, 3):
+            raise ValueError("dim must be 2 or 3")
+        bx, by, bz = block
+        if dim == 2:
+            bz = 1
+            bricks = (bricks[0], bricks[1], 1)
+        if min(bx, by) < 4 or (dim == 3 and bz < 4) or bx % 2 or by % 2 or (dim == 3 and bz % 2):
+            raise ValueError("block sizes must be even and >= 4 on AMR meshes")
+        if not (0 <= base_level <= max_level):
+            raise ValueError("need 0 <= base_level <= max_level")
+        per = tuple(bool(p) for p in periodic[:dim]) + (True,) * (3 - dim)
+
+        def ext(L):
+            return (bricks[0] << L, bricks[1] << L, (bricks[2] << L) if dim == 3 else 1)
+
+        def kids(key):
+            L, cx, cy, cz = key
+            return [(L + 1, 2 * cx + ex, 2 * cy + ey, 2 * cz + ez) for ez in ((0, 1) if dim == 3 else (0,))
+                    for ey in (0, 1) for ex in (0, 1)]
+
+        e0 = ext(base_level)
+        leaves = {(base_level, cx, cy, cz) for cz in range(e0[2]) for cy in range(e0[1]) for cx in range(e0[0])}
+        for L in range(base_level, max_level):
+            h = 1.0 / (1 << L)
+            for key in sorted(k for k in leaves if k[0] == L):
+                lo = np.array([key[1] * h, key[2] * h, key[3] * h if dim == 3 else 0.0])
+                hi = lo + np.array([h, h, h if dim == 3 else 1.0])
+                if refine(L, lo, hi):
+                    leaves.remove(key)
+                    leaves.update(kids(key))
+        offs = [(ox, oy, oz) for oz in ((-1, 0, 1) if dim == 3 else (0,)) for oy in (-1, 0, 1) for ox in (-1, 0, 1)
+                if (ox, oy, oz) != (0, 0, 0)]
+
+        def wrap(L, c):
+            e = ext(L)
+            out = []
+            for d in range(3):
+                v = c[d]
+                if per[d]:
+                    v %= e[d]
+                elif not 0 <= v < e[d]:
+                    return None
+                out.append(v)
+            return tuple(out)
+
+        changed = True
+        while changed:
+            changed = False
+            for key in sorted(leaves):
+                if key not in leaves or key[0] - 2 < base_level:
+                    continue
+                L = key[0]
+                for o in offs:
+                    r = wrap(L, (key[1] + o[0], key[2] + o[1], key[3] + o[2]))
+                    if r is None:
+                        continue
+                    for lv in range(L - 2, base_level - 1, -1):
+                        sh = L - lv
+                        anc = (lv, r[0] >> sh, r[1] >> sh, r[2] >> sh)
+                        if anc in leaves:
+                            leaves.remove(anc)
+                            leaves.update(kids(anc))
+                            changed = True
+                            break
+
+        # p4est order: trees x fastest, then Morton order of the anchor at max_level
+        def order_key(key):
+            L, cx, cy, cz = key
+            t = (cx >> L, cy >> L, cz >> L)
+            tid = t[0] + bricks[0] * (t[1] + bricks[1] * t[2])
+            sh = max_level - L
+            a = [((cx - (t[0] << L)) << sh), ((cy - (t[1] << L)) << sh), ((cz - (t[2] << L)) << sh)]
+            m = 0
+            for bit in range(max(max_level, 1)):
+                m |= ((a[0] >> bit) & 1) << (3 * bit) | ((a[1] >> bit) & 1) << (3 * bit + 1) | \
+                    ((a[2] >> bit) & 1) << (3 * bit + 2)
+            return (tid, m, L)
+
+        owned = sorted(leaves, key=order_key)
+        ids = {k: n for n, k in enumerate(owned)}
+        n_owned = len(owned)
+        out_keys, out_ids, out_src, out_normal = [], {}, [], []
+        for key in owned:
+            L = key[0]
+            e = ext(L)
+            for o in offs:
+                c = [key[1] + o[0], key[2] + o[1], key[3] + o[2]]
+                r = wrap(L, c)
+                if r is not None:
+                    continue
+                cw = [c[d] % e[d] if per[d] else c[d] for d in range(3)]
+                ok = (L, cw[0], cw[1], cw[2])
+                if ok in out_ids:
+                    continue
+                src = tuple(min(max(cw[d], 0), e[d] - 1) for d in range(3))
+                skey = (L,) + src
+                if skey not in ids:
+                    raise ValueError(f"outside block {ok} has no same-level inside leaf {skey}; keep the level "
+                                     "uniform along non-periodic borders")
+                out_ids[ok] = n_owned + len(out_keys)
+                out_keys.append(ok)
+                out_src.append(ids[skey])
+                out_normal.append(tuple(int(np.sign(src[d] - cw[d])) for d in range(3)))
+        all_keys = owned + out_keys
+        n_blocks = len(all_keys)
+        level = np.array([k[0] for k in all_keys], dtype=np.int32)
+        coords = np.array([k[1:] for k in all_keys], dtype=np.int64).reshape(-1, 3)
+        neighbor = -np.ones((n_blocks, 27), dtype=np.int32)
+        fine = -np.ones((n_blocks, 27, 8), dtype=np.int32)
+        any_jump = False
+        for b, key in enumerate(owned):
+            L = key[0]
+            e = ext(L)
+            for o in offs:
+                s_ = nb_slot(*o)
+                c = [key[1] + o[0], key[2] + o[1], key[3] + o[2]]
+                r = wrap(L, c)
+                if r is None:
+                    cw = tuple(c[d] % e[d] if per[d] else c[d] for d in range(3))
+                    neighbor[b, s_] = out_ids[(L,) + cw]
+                    continue
+                if (L,) + r in ids:
+                    neighbor[b, s_] = ids[(L,) + r]
+                    continue
+                if L - 1 >= base_level and (L - 1, r[0] >> 1, r[1] >> 1, r[2] >> 1) in ids:
+                    neighbor[b, s_] = ids[(L - 1, r[0] >> 1, r[1] >> 1, r[2] >> 1)]
+                    any_jump = True
+                    continue
+                ch = kids((L,) + r)
+                found = False
+                for n, kk in enumerate(ch):
+                    if kk in ids:
+                        fine[b, s_, n] = ids[kk]
+                        found = True
+                if not found:
+                    raise ValueError(f"neighbour region {r} of leaf {key} is not covered within one level")
+                any_jump = True
+        gsz = ext(max(k[0] for k in owned))
+        return BlockMesh(dim=dim, block=(bx, by, bz), level=level, neighbor=neighbor, coords=coords,
+                         n_owned=n_owned, grid=gsz, periodic=per, scaling_factor=scaling_factor,
+                         outside_src=np.array(out_src, dtype=np.int32),
+                         outside_normal=np.array(out_normal, dtype=np.int32).reshape(-1, 3),
+                         fine_neighbor=fine if any_jump else None)
 
     @staticmethod
     def batch(meshes) -> tuple["BlockMesh", np.ndarray]:

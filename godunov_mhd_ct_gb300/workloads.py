@@ -40,7 +40,7 @@ def uniform01(seed: int, ids: np.ndarray) -> np.ndarray:
 def _faces_from_az(mesh: BlockMesh, B: np.ndarray, az, x0=0.0, y0=0.0):
     """Face B = curl(A_z e_z) on the faces of every block; az(x, y) evaluated at edges."""
     bx, by, bz = mesh.block
-    dx = mesh.cell_length()
+    dx = mesh.block_dx()[:, None, None, None]  # per block (AMR meshes mix levels)
     Bx, By, Bz = mesh.split_faces(B)
     c = mesh.coords
     # x faces: Bx(i, j) = (Az(x_i, y_{j+1}) - Az(x_i, y_j)) / dy
@@ -91,11 +91,13 @@ def orszag_tang(mesh: BlockMesh, gamma: float = 5.0 / 3.0, rho_perturbation: flo
     n = mesh.n_owned
     gi, gj, gk = mesh.global_cell_index()
     gi, gj, gk = gi[:n], gj[:n], gk[:n]
-    dx = mesh.cell_length()
+    dx = mesh.block_dx()[:n, None, None, None]
     x = (gi + 0.5) * dx
     y = (gj + 0.5) * dx
     rho = np.full(x.shape, 25.0 / (36.0 * math.pi))
     if rho_perturbation:
+        if mesh.is_amr:
+            raise ValueError("the density perturbation is defined on uniform meshes")
         gx = mesh.grid[0] * mesh.block[0]
         gy = mesh.grid[1] * mesh.block[1]
         ids = gi + gx * (gj + gy * gk)
@@ -148,8 +150,8 @@ def random_smooth(mesh: BlockMesh, gamma=1.4, seed=0, amp=0.2):
     U, B = mesh.alloc_state()
     kx, ky = rng.integers(1, 3, 2)
     ph = rng.uniform(0, 2 * math.pi, 6)
-    Lx = mesh.grid[0] * mesh.block[0] * mesh.cell_length()
-    Ly = mesh.grid[1] * mesh.block[1] * mesh.cell_length()
+    Lx = mesh.domain_length(0)
+    Ly = mesh.domain_length(1)
 
     def az(x, y):
         return 0.1 * (np.sin(2 * math.pi * kx * x / Lx + ph[0]) * np.cos(2 * math.pi * ky * y / Ly + ph[1]))
@@ -160,11 +162,11 @@ def random_smooth(mesh: BlockMesh, gamma=1.4, seed=0, amp=0.2):
     By -= 0.2
     n = mesh.n_owned
     gi, gj, gk = mesh.global_cell_index()
-    dx = mesh.cell_length()
+    dx = mesh.block_dx()[:n, None, None, None]
     x = (gi[:n] + 0.5) * dx
     y = (gj[:n] + 0.5) * dx
     z = (gk[:n] + 0.5) * dx
-    Lz = mesh.grid[2] * mesh.block[2] * dx
+    Lz = mesh.domain_length(2)
     if mesh.dim == 3:
         # Bz face values: a constant keeps the field divergence-free
         Bz[...] = 0.15

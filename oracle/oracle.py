@@ -24,6 +24,8 @@ class OracleMesh(ctypes.Structure):
         ("level", ctypes.POINTER(ctypes.c_int32)), ("neighbor", ctypes.POINTER(ctypes.c_int32)),
         ("scaling_factor", ctypes.c_double), ("outside_src", ctypes.POINTER(ctypes.c_int32)),
         ("outside_normal", ctypes.POINTER(ctypes.c_int32)), ("bc", ctypes.c_int32 * 6),
+        ("coord", ctypes.POINTER(ctypes.c_int32)), ("fine_neighbor", ctypes.POINTER(ctypes.c_int32)),
+        ("prolongation", ctypes.c_int32),
     ]
 
 
@@ -91,17 +93,34 @@ class Mesh:
     """Holds the ctypes mesh plus the numpy arrays it points into."""
 
     def __init__(self, dim, bx, by, bz, level, neighbor, n_owned, scaling_factor=1.0, outside_src=None,
-                 outside_normal=None, bc=(1, 1, 1, 1, 1, 1)):
+                 outside_normal=None, bc=(1, 1, 1, 1, 1, 1), coord=None, fine_neighbor=None, prolongation=0):
         ip = ctypes.POINTER(ctypes.c_int32)
         self.level = np.ascontiguousarray(level, dtype=np.int32)
         self.neighbor = np.ascontiguousarray(neighbor, dtype=np.int32)
         self.out_src = np.ascontiguousarray(outside_src if outside_src is not None else np.zeros(1), dtype=np.int32)
         self.out_normal = np.ascontiguousarray(outside_normal if outside_normal is not None else np.zeros(3),
                                                dtype=np.int32).reshape(-1)
+        self.coord = None if coord is None else np.ascontiguousarray(coord, dtype=np.int32).reshape(-1)
+        self.fine = None if fine_neighbor is None else np.ascontiguousarray(fine_neighbor, dtype=np.int32).reshape(-1)
         self.c = OracleMesh(dim, bx, by, bz if dim == 3 else 1, len(self.level), n_owned,
                             self.level.ctypes.data_as(ip), self.neighbor.ctypes.data_as(ip), scaling_factor,
                             self.out_src.ctypes.data_as(ip), self.out_normal.ctypes.data_as(ip),
-                            (ctypes.c_int32 * 6)(*[int(b) for b in bc]))
+                            (ctypes.c_int32 * 6)(*[int(b) for b in bc]),
+                            self.coord.ctypes.data_as(ip) if self.coord is not None else ctypes.cast(None, ip),
+                            self.fine.ctypes.data_as(ip) if self.fine is not None else ctypes.cast(None, ip),
+                            int(prolongation))
+
+    @staticmethod
+    def from_block_mesh(mesh, bc=None, prolongation=0):
+        """Oracle view of a godunov_mhd_ct_gb300 BlockMesh (uniform or AMR)."""
+        if bc is None:
+            bc = [1 if mesh.periodic[d // 2] else 2 for d in range(6)]
+        bx, by, bz = mesh.block
+        return Mesh(mesh.dim, bx, by, bz, mesh.level, mesh.neighbor.reshape(-1), mesh.n_owned,
+                    scaling_factor=mesh.scaling_factor,
+                    outside_src=mesh.outside_src if mesh.outside_src.size else None,
+                    outside_normal=mesh.outside_normal if mesh.outside_normal.size else None, bc=bc,
+                    coord=mesh.coords, fine_neighbor=mesh.fine_neighbor, prolongation=prolongation)
 
 
 def step(mesh: Mesh, st: OracleSettings, U, B, dt):

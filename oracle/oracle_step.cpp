@@ -18,14 +18,35 @@
 //   CFL                      scheme/ComputeDtMHDFunctor.cpp:86-151
 //   outside-block fill       border_conditions/FillOutside.cpp:97-395
 //
-// Assumptions where the reference relies on kalypsso-core (absent, so these are unpinned):
-//   * all neighbours are at the same AMR level (uniform meshes); a level jump is rejected;
-//   * the face-B ghost layer is a copy of the neighbour's faces; faces on the block border are
-//     taken from the block itself (they equal the neighbour's copy whenever shared faces agree);
-//   * dx = (1 / (bx * 2^level)) * scaling_factor;
-//   * an edge on a block border has as siblings the blocks sharing it: one across a block face,
-//     three around a block edge (2D: block corner). Outside blocks count as valid siblings but
-//     are not averaged in, as in the reference.
+// Definitions where the reference relies on kalypsso-core (absent, so these are unpinned). The mesh
+// is a 2:1-balanced (face, edge and corner) forest of equal-size blocks; the neighbour region of block
+// b in direction o in {-1,0,1}^3 is the level-L(b) block-sized region next to b, and it is either a
+// leaf at L (same), part of a leaf at L-1 (coarser), split into 2^d leaves at L+1 (finer), or an
+// outside block at L (non-periodic borders).
+//   * face-B ghost layer (core FillBlockGhostFacesFunctor): faces with normal index 0..b and
+//     transverse cells inside the block are the block's own; a same-level or outside region copies
+//     the neighbour's face; a finer region takes the mean of the 2^(d-1) fine faces covering the face
+//     (sum with the first transverse axis fastest, then divide); a coarser region takes the coarse
+//     face containing the face when the face lies on a coarse face, else the mean of the two coarse
+//     faces bounding the coarse cell along the normal. 2D Bz is cell-centred: mean of the 4 fine
+//     cells (x fastest) / the coarse cell value;
+//   * cell-centred hydro ghosts follow ConvertToPrimitivesVariablesFunctor.cpp:217-283, 471-719:
+//     same level copies U and takes B_cc from the ghost faces (equal to the neighbour's faces when
+//     shared faces agree); finer takes the mean of the 2^d fine cells (core compute_siblings_average:
+//     x fastest, sum then divide) with B_cc from the ghost faces; coarser SIMPLE_COPY copies the
+//     coarse cell's U and its B_cc from the coarse block's faces; EXTRAPOLATE_LINEAR_MINMOD adds
+//     0.25 * (+-1) * minmod slope per axis (core compute_minmod_slopes: minmod(u - u_left,
+//     u_right - u); neighbours at the coarse level, a refined one read as the mean of its fine cells,
+//     a coarser one as its containing cell) with B_cc from the ghost faces;
+//   * a coarse cell next to a finer face takes the sum of the 2^(d-1) fine face fluxes (core
+//     compute_face_siblings_sum: first transverse axis fastest, from 0) / 2^d
+//     (ReadFluxesAndConservativeUpdateFunctor.cpp:141-172);
+//   * an edge on a block border has as siblings (core getEdgeSiblingLoc) the regions across its two
+//     transverse block borders and across both: one across a block face, three around a block edge
+//     (2D: block corner). Outside blocks count as valid siblings but are not averaged in, as in the
+//     reference. A finer sibling's edge is the fine edge at the same place in the child touching it
+//     (3D: the two fine sub-edges along the edge);
+//   * dx = (1 / (bx * 2^level)) * scaling_factor.
 //
 // Compile with -ffp-contract=off.
 #include "oracle_models.h"
@@ -44,7 +65,10 @@ struct Mesh
   int             n_blocks;   // owned + outside
   int             n_owned;    // blocks [0, n_owned) are updated
   const int32_t * level;      // [n_blocks]
-  const int32_t * neighbor;   // [n_blocks * 27], -1 when absent
+  const int32_t * neighbor;   // [n_blocks * 27]: same-level, coarser or outside block; -1 otherwise
+  const int32_t * coord;      // [n_blocks * 3] block coordinates at the block's level, or null
+  const int32_t * fine;       // [n_blocks * 27 * 8] children of a refined neighbour region, or null
+  int             prolongation; // 0 SIMPLE_COPY, 1 EXTRAPOLATE_LINEAR_MINMOD
   double          scaling_factor;
 };
 
@@ -102,6 +126,11 @@ struct Fields
   {
     return B[(int64_t)blk * L.nface + L.nfx + L.nfy + i + (int64_t)m->bx * (j + (int64_t)m->by * k)];
   }
+  double
+  face(int blk, int comp, int i, int j, int k) const
+  {
+    return comp == 0 ? bx(blk, i, j, k) : (comp == 1 ? by(blk, i, j, k) : bz(blk, i, j, k));
+  }
 };
 
 // A ghosted 3D index space [lo, lo + n) per axis, var-slowest.
@@ -128,21 +157,70 @@ struct Box
   }
 };
 
-// Locate the block and local coordinates holding cell (i,j,k) of block blk. Returns -1 if the
-// neighbour does not exist.
-static int
-locate_cell(const Mesh & m, int blk, int & i, int & j, int & k)
+// Neighbour-region classification (see the definitions at the top of this file).
+enum RegionKind
 {
-  const int ox = i < 0 ? -1 : (i >= m.bx ? 1 : 0);
-  const int oy = j < 0 ? -1 : (j >= m.by ? 1 : 0);
-  const int oz = m.dim == 3 ? (k < 0 ? -1 : (k >= m.bz ? 1 : 0)) : 0;
+  RK_MISSING = 0,
+  RK_SAME = 1,
+  RK_COARSER = 2,
+  RK_FINER = 3,
+  RK_OUTSIDE = 4
+};
+
+struct Region
+{
+  int             kind;
+  int             id;     // same, outside, coarser: the block holding the region
+  int             sub[3]; // coarser: position of the region inside the coarse block (0 or 1 per axis)
+  const int32_t * child;  // finer: 8 children, x fastest (-1 where not a leaf)
+};
+
+static Region
+region_of(const Mesh & m, int blk, int ox, int oy, int oz)
+{
+  Region r{RK_MISSING, -1, {0, 0, 0}, nullptr};
   if (ox == 0 && oy == 0 && oz == 0)
-    return blk;
-  const int nb = m.neighbor[(int64_t)blk * 27 + nb_slot(ox, oy, oz)];
-  i -= ox * m.bx;
-  j -= oy * m.by;
-  k -= oz * m.bz;
-  return nb;
+  {
+    r.kind = RK_SAME;
+    r.id = blk;
+    return r;
+  }
+  const int64_t s = (int64_t)blk * 27 + nb_slot(ox, oy, oz);
+  const int     id = m.neighbor[s];
+  if (id >= 0)
+  {
+    r.id = id;
+    if (id >= m.n_owned)
+      r.kind = RK_OUTSIDE;
+    else if (m.level[id] == m.level[blk])
+      r.kind = RK_SAME;
+    else if (m.level[id] == m.level[blk] - 1 && m.coord)
+    {
+      r.kind = RK_COARSER;
+      const int o[3] = {ox, oy, oz};
+      for (int d = 0; d < m.dim; ++d)
+        r.sub[d] = (m.coord[(int64_t)blk * 3 + d] + o[d]) & 1;
+    }
+    return r;
+  }
+  if (m.fine)
+  {
+    const int32_t * ch = m.fine + s * 8;
+    for (int c = 0; c < (1 << m.dim); ++c)
+      if (ch[c] >= 0)
+      {
+        r.kind = RK_FINER;
+        r.child = ch;
+        break;
+      }
+  }
+  return r;
+}
+
+static inline int
+region_axis(int idx, int n)
+{
+  return idx < 0 ? -1 : (idx >= n ? 1 : 0);
 }
 
 struct StepWork
@@ -154,7 +232,6 @@ struct StepWork
   Box Q2;            // 8 vars on [-1, b+1)
   Box E;             // 3 (2D: 1) comps on [-2, b+2)
   Box SF;            // 3 (2D: 2) comps on [-1, b+1)
-  Box F;             // flux, 8 vars
 };
 
 static double
@@ -176,7 +253,129 @@ slope_scalar(double q, double qp, double qm, const Settings & s)
   return dq;
 }
 
-// Fill ghosted face-B for block blk. Returns 0 or -1 when a needed neighbour is missing.
+// Level of a neighbour region relative to the block (missing regions rank below everything).
+static int
+region_level(const Region & r)
+{
+  return r.kind == RK_COARSER ? -1 : (r.kind == RK_FINER ? 1 : (r.kind == RK_MISSING ? -100 : 0));
+}
+
+// Face value of component comp at q (region-local indices) of neighbour region r.
+static bool
+region_face(const Mesh & m, const Fields & f, const Region & r, int comp, const int * q, double & out)
+{
+  const int  b[3] = {m.bx, m.by, m.bz};
+  const bool cellc = m.dim == 2 && comp == 2;
+  switch (r.kind)
+  {
+    case RK_SAME:
+    case RK_OUTSIDE:
+      out = f.face(r.id, comp, q[0], q[1], q[2]);
+      return true;
+    case RK_FINER:
+    {
+      double acc = 0.0;
+      if (cellc)
+      {
+        for (int ey = 0; ey < 2; ++ey)
+          for (int ex = 0; ex < 2; ++ex)
+          {
+            const int F0 = 2 * q[0] + ex, F1 = 2 * q[1] + ey;
+            const int c0 = F0 >= b[0], c1 = F1 >= b[1];
+            const int id = r.child[c0 + 2 * c1];
+            if (id < 0)
+              return false;
+            acc += f.bz(id, F0 - c0 * b[0], F1 - c1 * b[1], 0);
+          }
+        out = acc / 4.0;
+        return true;
+      }
+      const int t1 = comp == 0 ? 1 : 0;
+      const int t2 = comp == 2 ? 1 : 2;
+      const int n2 = m.dim == 3 ? 2 : 1;
+      for (int e2 = 0; e2 < n2; ++e2)
+        for (int e1 = 0; e1 < 2; ++e1)
+        {
+          int F[3] = {0, 0, 0}, c[3] = {0, 0, 0};
+          F[comp] = 2 * q[comp];
+          c[comp] = F[comp] >= b[comp];
+          F[t1] = 2 * q[t1] + e1;
+          c[t1] = F[t1] >= b[t1];
+          if (m.dim == 3)
+          {
+            F[t2] = 2 * q[t2] + e2;
+            c[t2] = F[t2] >= b[t2];
+          }
+          const int id = r.child[c[0] + 2 * c[1] + 4 * c[2]];
+          if (id < 0)
+            return false;
+          acc += f.face(id, comp, F[0] - c[0] * b[0], F[1] - c[1] * b[1], F[2] - c[2] * b[2]);
+        }
+      out = acc / (m.dim == 3 ? 4.0 : 2.0);
+      return true;
+    }
+    case RK_COARSER:
+    {
+      int F[3] = {0, 0, 0};
+      for (int d = 0; d < m.dim; ++d)
+        F[d] = r.sub[d] * b[d] + q[d];
+      if (cellc)
+      {
+        out = f.bz(r.id, F[0] >> 1, F[1] >> 1, 0);
+        return true;
+      }
+      int T[3] = {F[0] >> 1, F[1] >> 1, F[2] >> 1};
+      if ((F[comp] & 1) == 0)
+      {
+        T[comp] = F[comp] / 2;
+        out = f.face(r.id, comp, T[0], T[1], T[2]);
+      }
+      else
+      {
+        int T1[3] = {T[0], T[1], T[2]};
+        T[comp] = (F[comp] - 1) / 2;
+        T1[comp] = (F[comp] + 1) / 2;
+        out = 0.5 * (f.face(r.id, comp, T[0], T[1], T[2]) + f.face(r.id, comp, T1[0], T1[1], T1[2]));
+      }
+      return true;
+    }
+    default:
+      return false;
+  }
+}
+
+// Value of face component comp at (i, j, k) of block blk's ghosted face space (2D comp 2: the
+// cell-centred Bz), following the face-B ghost definition at the top of this file. A face lying on
+// the border between two neighbour regions along its normal is taken from the finer of the two (the
+// first when they are at the same level), so every block sees the same value for it. Returns false
+// when the neighbour region is missing.
+static bool
+ghost_face(const Mesh & m, const Fields & f, int blk, int comp, int i, int j, int k, double & out)
+{
+  const int  b[3] = {m.bx, m.by, m.bz};
+  const bool cellc = m.dim == 2 && comp == 2;
+  const int  idx[3] = {i, j, k};
+  int        o[3] = {0, 0, 0};
+  for (int d = 0; d < m.dim; ++d)
+    o[d] = (d == comp && !cellc) ? (idx[d] < 0 ? -1 : (idx[d] > b[d] ? 1 : 0)) : region_axis(idx[d], b[d]);
+  Region r = region_of(m, blk, o[0], o[1], o[2]);
+  int    q[3] = {idx[0] - o[0] * b[0], idx[1] - o[1] * b[1], idx[2] - o[2] * b[2]};
+  if (!cellc && (o[0] != 0 || o[1] != 0 || o[2] != 0) && (idx[comp] == 0 || idx[comp] == b[comp]))
+  {
+    int o1[3] = {o[0], o[1], o[2]};
+    o1[comp] = idx[comp] == 0 ? -1 : 1;
+    const Region r1 = region_of(m, blk, o1[0], o1[1], o1[2]);
+    if (region_level(r1) > region_level(r))
+    {
+      r = r1;
+      q[comp] = idx[comp] == 0 ? b[comp] : 0;
+    }
+  }
+  return region_face(m, f, r, comp, q, out);
+}
+
+// Fill ghosted face-B for block blk (GodunovImplemV0.cpp:211-237). Returns 0 or -1 when a needed
+// neighbour is missing.
 static int
 fill_bface_ghosted(const Mesh & m, const Fields & f, int blk, StepWork & w)
 {
@@ -188,68 +387,76 @@ fill_bface_ghosted(const Mesh & m, const Fields & f, int blk, StepWork & w)
     w.Bgz.init(-g, m.bx + 2 * g, -g, m.by + 2 * g, -gz, m.bz + 2 * gz + 1, 1);
   else
     w.Bgz.init(-g, m.bx + 2 * g, -g, m.by + 2 * g, 0, 1, 1);
-
-  // x faces: i in [-2, bx+2]
-  for (int k = -gz; k < m.bz + gz; ++k)
-    for (int j = -g; j < m.by + g; ++j)
-      for (int i = -g; i <= m.bx + g; ++i)
-      {
-        const int ox = i < 0 ? -1 : (i > m.bx ? 1 : 0);
-        const int oy = j < 0 ? -1 : (j >= m.by ? 1 : 0);
-        const int oz = m.dim == 3 ? (k < 0 ? -1 : (k >= m.bz ? 1 : 0)) : 0;
-        int       nb = blk;
-        if (ox || oy || oz)
-          nb = m.neighbor[(int64_t)blk * 27 + nb_slot(ox, oy, oz)];
-        if (nb < 0)
-          return -1;
-        w.Bgx(i, j, k, 0) = f.bx(nb, i - ox * m.bx, j - oy * m.by, k - oz * m.bz);
-      }
-  // y faces: j in [-2, by+2]
-  for (int k = -gz; k < m.bz + gz; ++k)
-    for (int j = -g; j <= m.by + g; ++j)
-      for (int i = -g; i < m.bx + g; ++i)
-      {
-        const int ox = i < 0 ? -1 : (i >= m.bx ? 1 : 0);
-        const int oy = j < 0 ? -1 : (j > m.by ? 1 : 0);
-        const int oz = m.dim == 3 ? (k < 0 ? -1 : (k >= m.bz ? 1 : 0)) : 0;
-        int       nb = blk;
-        if (ox || oy || oz)
-          nb = m.neighbor[(int64_t)blk * 27 + nb_slot(ox, oy, oz)];
-        if (nb < 0)
-          return -1;
-        w.Bgy(i, j, k, 0) = f.by(nb, i - ox * m.bx, j - oy * m.by, k - oz * m.bz);
-      }
-  // z faces (3D: k in [-2, bz+2]) or cell-centred Bz (2D)
-  if (m.dim == 3)
+  Box * box[3] = {&w.Bgx, &w.Bgy, &w.Bgz};
+  for (int c = 0; c < 3; ++c)
   {
-    for (int k = -gz; k <= m.bz + gz; ++k)
-      for (int j = -g; j < m.by + g; ++j)
-        for (int i = -g; i < m.bx + g; ++i)
-        {
-          const int ox = i < 0 ? -1 : (i >= m.bx ? 1 : 0);
-          const int oy = j < 0 ? -1 : (j >= m.by ? 1 : 0);
-          const int oz = k < 0 ? -1 : (k > m.bz ? 1 : 0);
-          int       nb = blk;
-          if (ox || oy || oz)
-            nb = m.neighbor[(int64_t)blk * 27 + nb_slot(ox, oy, oz)];
-          if (nb < 0)
+    Box & bb = *box[c];
+    for (int k = bb.lo[2]; k < bb.lo[2] + bb.n[2]; ++k)
+      for (int j = bb.lo[1]; j < bb.lo[1] + bb.n[1]; ++j)
+        for (int i = bb.lo[0]; i < bb.lo[0] + bb.n[0]; ++i)
+          if (!ghost_face(m, f, blk, c, i, j, k, bb(i, j, k, 0)))
             return -1;
-          w.Bgz(i, j, k, 0) = f.bz(nb, i - ox * m.bx, j - oy * m.by, k - oz * m.bz);
-        }
-  }
-  else
-  {
-    for (int j = -g; j < m.by + g; ++j)
-      for (int i = -g; i < m.bx + g; ++i)
-      {
-        int ii = i, jj = j, kk = 0;
-        const int nb = locate_cell(m, blk, ii, jj, kk);
-        if (nb < 0)
-          return -1;
-        w.Bgz(i, j, 0, 0) = f.bz(nb, ii, jj, 0);
-      }
   }
   return 0;
+}
+
+// Mean of the 2^d fine cells of variable v covering cell q of a finer region (core
+// compute_siblings_average: x fastest, sum then divide).
+static bool
+restrict_cell(const Mesh & m, const Fields & f, const Region & r, const int * q, int v, double & out)
+{
+  const int b[3] = {m.bx, m.by, m.bz};
+  double    acc = 0.0;
+  for (int ez = 0; ez < (m.dim == 3 ? 2 : 1); ++ez)
+    for (int ey = 0; ey < 2; ++ey)
+      for (int ex = 0; ex < 2; ++ex)
+      {
+        const int F[3] = {2 * q[0] + ex, 2 * q[1] + ey, m.dim == 3 ? 2 * q[2] + ez : 0};
+        const int c[3] = {F[0] >= b[0], F[1] >= b[1], F[2] >= b[2]};
+        const int id = r.child[c[0] + 2 * c[1] + 4 * c[2]];
+        if (id < 0)
+          return false;
+        acc += f.u(id, v, F[0] - c[0] * b[0], F[1] - c[1] * b[1], F[2] - c[2] * b[2]);
+      }
+  out = acc / (double)(1 << m.dim);
+  return true;
+}
+
+// Conservative variable v of cell (i, j, k) at block blk's level, at most one block away: same
+// level or outside reads the cell, a refined region its fine-cell mean, a coarser one its containing
+// cell.
+static bool
+level_cell_value(const Mesh & m, const Fields & f, int blk, int v, int i, int j, int k, double & out)
+{
+  const int    b[3] = {m.bx, m.by, m.bz};
+  const int    o[3] = {region_axis(i, m.bx), region_axis(j, m.by), m.dim == 3 ? region_axis(k, m.bz) : 0};
+  const Region r = region_of(m, blk, o[0], o[1], o[2]);
+  const int    q[3] = {i - o[0] * b[0], j - o[1] * b[1], k - o[2] * b[2]};
+  switch (r.kind)
+  {
+    case RK_SAME:
+    case RK_OUTSIDE:
+      out = f.u(r.id, v, q[0], q[1], q[2]);
+      return true;
+    case RK_FINER:
+      return restrict_cell(m, f, r, q, v, out);
+    case RK_COARSER:
+      out = f.u(r.id, v, (r.sub[0] * b[0] + q[0]) >> 1, (r.sub[1] * b[1] + q[1]) >> 1,
+                (r.sub[2] * b[2] + q[2]) >> 1);
+      return true;
+    default:
+      return false;
+  }
+}
+
+// core compute_minmod_slopes with slope_type 1
+static double
+minmod_slope(double u, double ur, double ul)
+{
+  const double dl = u - ul, dr = ur - u;
+  if (dl * dr <= 0.0)
+    return 0.0;
+  return dl > 0.0 ? std::fmin(dl, dr) : std::fmax(dl, dr);
 }
 
 // Primitive variables on the (b+4)^d ghosted block (ConvertToPrimitivesVariablesFunctor).
@@ -263,32 +470,91 @@ convert_to_primitives(const Mesh & m, const Fields & f, const Settings & s, int 
     for (int j = -g; j < m.by + g; ++j)
       for (int i = -g; i < m.bx + g; ++i)
       {
-        int ii = i, jj = j, kk = k;
-        const int nb = locate_cell(m, blk, ii, jj, kk);
-        if (nb < 0)
-          return -1;
-        if (m.level[nb] != m.level[blk])
-          return -2;
-        double u[8];
-        u[ID] = f.u(nb, ID, ii, jj, kk);
-        u[IP] = f.u(nb, IP, ii, jj, kk);
-        u[IU] = f.u(nb, IU, ii, jj, kk);
-        u[IV] = f.u(nb, IV, ii, jj, kk);
-        u[IW] = f.u(nb, IW, ii, jj, kk);
-        // cell-centred B from face values (get_conservative_vars, .cpp:175-210)
-        u[IA] = 0.5 * (w.Bgx(i, j, k, 0) + w.Bgx(i + 1, j, k, 0));
-        u[IB] = 0.5 * (w.Bgy(i, j, k, 0) + w.Bgy(i, j + 1, k, 0));
-        if (m.dim == 3)
-          u[IC] = 0.5 * (w.Bgz(i, j, k, 0) + w.Bgz(i, j, k + 1, 0));
-        else
-          u[IC] = 0.5 * (w.Bgz(i, j, 0, 0) + w.Bgz(i, j, 0, 0));
-        double q[8];
-        compute_primitives(u, q, nullptr, s);
-        w.Q(i, j, k, ID) = q[ID];
-        w.Q(i, j, k, IP) = q[IP];
-        w.Q(i, j, k, IU) = q[IU];
-        w.Q(i, j, k, IV) = q[IV];
-        w.Q(i, j, k, IW) = q[IW];
+        const int    o[3] = {region_axis(i, m.bx), region_axis(j, m.by), m.dim == 3 ? region_axis(k, m.bz) : 0};
+        const Region r = region_of(m, blk, o[0], o[1], o[2]);
+        const int    qc[3] = {i - o[0] * m.bx, j - o[1] * m.by, k - o[2] * m.bz};
+        const int *  q = qc;
+        double       u[8];
+        bool         bcc_from_ghost_faces = true;
+        switch (r.kind)
+        {
+          case RK_SAME:
+          case RK_OUTSIDE:
+            // fill_inner / fill_ghost_copy at the same level (.cpp:373-468)
+            for (int v = 0; v < 5; ++v)
+              u[v] = f.u(r.id, v, q[0], q[1], q[2]);
+            break;
+          case RK_FINER:
+            // get_conservative_vars_restriction (.cpp:217-283)
+            for (int v = 0; v < 5; ++v)
+              if (!restrict_cell(m, f, r, q, v, u[v]))
+                return -1;
+            break;
+          case RK_COARSER:
+          {
+            const int I[3] = {(r.sub[0] * m.bx + q[0]) >> 1, (r.sub[1] * m.by + q[1]) >> 1,
+                              (r.sub[2] * m.bz + q[2]) >> 1};
+            if (m.prolongation == 0)
+            {
+              // SIMPLE_COPY: fill_ghost_copy of the coarse cell with its own B_cc (.cpp:439-446)
+              for (int v = 0; v < 5; ++v)
+                u[v] = f.u(r.id, v, I[0], I[1], I[2]);
+              u[IA] = 0.5 * (f.bx(r.id, I[0], I[1], I[2]) + f.bx(r.id, I[0] + 1, I[1], I[2]));
+              u[IB] = 0.5 * (f.by(r.id, I[0], I[1], I[2]) + f.by(r.id, I[0], I[1] + 1, I[2]));
+              if (m.dim == 3)
+                u[IC] = 0.5 * (f.bz(r.id, I[0], I[1], I[2]) + f.bz(r.id, I[0], I[1], I[2] + 1));
+              else
+                u[IC] = 0.5 * (f.bz(r.id, I[0], I[1], 0) + f.bz(r.id, I[0], I[1], 0));
+              bcc_from_ghost_faces = false;
+            }
+            else
+            {
+              // EXTRAPOLATE_LINEAR_MINMOD (.cpp:471-635): position of this cell inside the coarse
+              // cell in {-1, +1} per axis, slopes at the coarse level
+              const int sgn[3] = {2 * (q[0] & 1) - 1, 2 * (q[1] & 1) - 1, 2 * (q[2] & 1) - 1};
+              for (int v = 0; v < 5; ++v)
+              {
+                const double uc = f.u(r.id, v, I[0], I[1], I[2]);
+                double       sl[3] = {0, 0, 0};
+                for (int d = 0; d < m.dim; ++d)
+                {
+                  int    ip[3] = {I[0], I[1], I[2]}, im[3] = {I[0], I[1], I[2]};
+                  double ur, ul;
+                  ip[d] += 1;
+                  im[d] -= 1;
+                  if (!level_cell_value(m, f, r.id, v, ip[0], ip[1], ip[2], ur) ||
+                      !level_cell_value(m, f, r.id, v, im[0], im[1], im[2], ul))
+                    return -1;
+                  sl[d] = minmod_slope(uc, ur, ul);
+                }
+                double val = uc + 0.25 * (double)sgn[0] * sl[0] + 0.25 * (double)sgn[1] * sl[1];
+                if (m.dim == 3)
+                  val = val + 0.25 * (double)sgn[2] * sl[2];
+                u[v] = val;
+              }
+            }
+            break;
+          }
+          default:
+            return -1;
+        }
+        if (bcc_from_ghost_faces)
+        {
+          // cell-centred B from face values (get_conservative_vars, .cpp:175-210)
+          u[IA] = 0.5 * (w.Bgx(i, j, k, 0) + w.Bgx(i + 1, j, k, 0));
+          u[IB] = 0.5 * (w.Bgy(i, j, k, 0) + w.Bgy(i, j + 1, k, 0));
+          if (m.dim == 3)
+            u[IC] = 0.5 * (w.Bgz(i, j, k, 0) + w.Bgz(i, j, k + 1, 0));
+          else
+            u[IC] = 0.5 * (w.Bgz(i, j, 0, 0) + w.Bgz(i, j, 0, 0));
+        }
+        double qp[8];
+        compute_primitives(u, qp, nullptr, s);
+        w.Q(i, j, k, ID) = qp[ID];
+        w.Q(i, j, k, IP) = qp[IP];
+        w.Q(i, j, k, IU) = qp[IU];
+        w.Q(i, j, k, IV) = qp[IV];
+        w.Q(i, j, k, IW) = qp[IW];
         // face values (get_face_mag, .cpp:287-369)
         w.Q(i, j, k, IA) = w.Bgx(i, j, k, 0);
         w.Q(i, j, k, IAR) = w.Bgx(i + 1, j, k, 0);
@@ -523,19 +789,41 @@ reconstruct_face(StepWork & w, const Settings & s, int i, int j, int k, int dir,
   qr[IP] = std::fmax(s.smallp * qr[ID], qr[IP]);
 }
 
-// compute_fluxes_and_store_{2d,3d} (scheme/ComputeHydroFluxesAndStoreFunctor.cpp:216-503) followed by
-// read_fluxes_and_update_{2d,3d} (scheme/ReadFluxesAndConservativeUpdateFunctor.cpp:103-436) for one
-// direction; U2 and (2D) Bz of block blk are updated in place.
-static int
-fluxes_and_update(const Mesh & m, const Settings & s, double dtdx, int dir, StepWork & w, double * U2blk,
-                  double * Bz2blk)
+// Per-block face fluxes of all directions: [dir][var 0..7][face], faces of direction d indexed
+// i + nx * (j + ny * k) with nx = bx + (d == 0) etc.
+struct FluxLayout
 {
+  int64_t n[3];   // faces per direction (0 for z in 2D)
+  int64_t off[3]; // offset of direction d (times 8 vars)
+  int64_t total;
+};
+
+static FluxLayout
+flux_layout(const Mesh & m)
+{
+  FluxLayout F;
+  F.n[0] = (int64_t)(m.bx + 1) * m.by * m.bz;
+  F.n[1] = (int64_t)m.bx * (m.by + 1) * m.bz;
+  F.n[2] = m.dim == 3 ? (int64_t)m.bx * m.by * (m.bz + 1) : 0;
+  F.off[0] = 0;
+  F.off[1] = 8 * F.n[0];
+  F.off[2] = F.off[1] + 8 * F.n[1];
+  F.total = F.off[2] + 8 * F.n[2];
+  return F;
+}
+
+// compute_fluxes_and_store_{2d,3d} (scheme/ComputeHydroFluxesAndStoreFunctor.cpp:216-503) for one
+// direction: flux * dt/dx into Fblk (FluxLayout).
+static int
+compute_fluxes(const Mesh & m, const Settings & s, double dtdx, int dir, StepWork & w, double * Fblk)
+{
+  const FluxLayout FL = flux_layout(m);
   const int nx = m.bx + (dir == 0), ny = m.by + (dir == 1), nz = m.bz + (dir == 2 && m.dim == 3);
-  w.F.init(0, nx, 0, ny, 0, nz, 8);
   const int di = dir == 0, dj = dir == 1, dk = dir == 2;
   // normal-B slot and the velocity / B component swapped with x for this direction
   const int ivel = dir == 0 ? IU : (dir == 1 ? IV : IW);
   const int imag = dir == 0 ? IA : (dir == 1 ? IB : IC);
+  double *  Fd = Fblk + FL.off[dir];
   for (int k = 0; k < nz; ++k)
     for (int j = 0; j < ny; ++j)
       for (int i = 0; i < nx; ++i)
@@ -560,30 +848,108 @@ fluxes_and_update(const Mesh & m, const Settings & s, double dtdx, int dir, Step
           std::swap(flux[IU], flux[ivel]);
           std::swap(flux[IA], flux[imag]);
         }
+        const int64_t fi = i + (int64_t)nx * (j + (int64_t)ny * k);
         for (int v = 0; v < 8; ++v)
-          w.F(i, j, k, v) = flux[v] * dtdx;
+          Fd[v * FL.n[dir] + fi] = flux[v] * dtdx;
       }
-  const int64_t ncell = (int64_t)m.bx * m.by * m.bz;
-  for (int k = 0; k < m.bz; ++k)
-    for (int j = 0; j < m.by; ++j)
-      for (int i = 0; i < m.bx; ++i)
+  return 0;
+}
+
+// get_flux_from_fine_neighbor (scheme/ReadFluxesAndConservativeUpdateFunctor.h:233-270): sum of the
+// 2^(d-1) fine fluxes through the face of cell q on side `side` (-1 left, +1 right) along dir.
+static bool
+fine_flux_sum(const Mesh & m, const std::vector<std::vector<double>> & flux_all, const Region & r, int dir,
+              int side, const int * q, int v, double & out)
+{
+  const FluxLayout FL = flux_layout(m);
+  const int        b[3] = {m.bx, m.by, m.bz};
+  const int        t1 = dir == 0 ? 1 : 0;
+  const int        t2 = dir == 2 ? 1 : 2;
+  double           acc = 0.0;
+  for (int e2 = 0; e2 < (m.dim == 3 ? 2 : 1); ++e2)
+    for (int e1 = 0; e1 < 2; ++e1)
+    {
+      int F[3] = {0, 0, 0}, c[3] = {0, 0, 0};
+      c[dir] = side < 0 ? 1 : 0;
+      F[dir] = side < 0 ? b[dir] : 0; // right flux of the last fine cell / left flux of the first
+      F[t1] = 2 * q[t1] + e1;
+      c[t1] = F[t1] >= b[t1];
+      F[t1] -= c[t1] * b[t1];
+      if (m.dim == 3)
       {
-        const int64_t c = i + (int64_t)m.bx * (j + (int64_t)m.by * k);
-        for (int v = 0; v < 5; ++v)
-        {
-          double acc = 0.0;
-          acc = acc + w.F(i, j, k, v);
-          acc = acc - w.F(i + di, j + dj, k + dk, v);
-          U2blk[v * ncell + c] += acc;
-        }
-        if (m.dim == 2)
-        {
-          double acc = 0.0;
-          acc = acc + w.F(i, j, k, IC);
-          acc = acc - w.F(i + di, j + dj, k + dk, IC);
-          Bz2blk[c] += acc;
-        }
+        F[t2] = 2 * q[t2] + e2;
+        c[t2] = F[t2] >= b[t2];
+        F[t2] -= c[t2] * b[t2];
       }
+      const int id = r.child[c[0] + 2 * c[1] + 4 * c[2]];
+      if (id < 0 || id >= m.n_owned)
+        return false;
+      const int nx = m.bx + (dir == 0), ny = m.by + (dir == 1);
+      acc += flux_all[id][FL.off[dir] + v * FL.n[dir] + F[0] + (int64_t)nx * (F[1] + (int64_t)ny * F[2])];
+    }
+  out = acc;
+  return true;
+}
+
+// read_fluxes_and_update_{2d,3d} (scheme/ReadFluxesAndConservativeUpdateFunctor.cpp:103-436): per
+// direction accum = 0 + F(i) - F(i+1), a face with finer neighbours taking their flux sum / 2^d, then
+// U2 += accum (2D: Bz too).
+static int
+update_u(const Mesh & m, int blk, const std::vector<std::vector<double>> & flux_all, double * U2blk,
+         double * Bz2blk)
+{
+  const FluxLayout FL = flux_layout(m);
+  const int        b[3] = {m.bx, m.by, m.bz};
+  const int64_t    ncell = (int64_t)m.bx * m.by * m.bz;
+  const double     vr = (double)(1 << m.dim);
+  const std::vector<double> & Fb = flux_all[blk];
+  const int nvar = m.dim == 2 ? 6 : 5;
+  for (int dir = 0; dir < m.dim; ++dir)
+  {
+    int olo[3] = {0, 0, 0}, ohi[3] = {0, 0, 0};
+    olo[dir] = -1;
+    ohi[dir] = 1;
+    const Region rlo = region_of(m, blk, olo[0], olo[1], olo[2]);
+    const Region rhi = region_of(m, blk, ohi[0], ohi[1], ohi[2]);
+    const int    nx = m.bx + (dir == 0), ny = m.by + (dir == 1);
+    const int    di = dir == 0, dj = dir == 1, dk = dir == 2;
+    for (int k = 0; k < m.bz; ++k)
+      for (int j = 0; j < m.by; ++j)
+        for (int i = 0; i < m.bx; ++i)
+        {
+          const int     q[3] = {i, j, k};
+          const int64_t c = i + (int64_t)m.bx * (j + (int64_t)m.by * k);
+          const int64_t fl = i + (int64_t)nx * (j + (int64_t)ny * k);
+          const int64_t fr = (i + di) + (int64_t)nx * ((j + dj) + (int64_t)ny * (k + dk));
+          for (int n = 0; n < nvar; ++n)
+          {
+            const int v = n < 5 ? n : IC;
+            double    acc = 0.0;
+            if (q[dir] == 0 && rlo.kind == RK_FINER)
+            {
+              double sum;
+              if (!fine_flux_sum(m, flux_all, rlo, dir, -1, q, v, sum))
+                return -1;
+              acc = acc + sum / vr;
+            }
+            else
+              acc = acc + Fb[FL.off[dir] + v * FL.n[dir] + fl];
+            if (q[dir] == b[dir] - 1 && rhi.kind == RK_FINER)
+            {
+              double sum;
+              if (!fine_flux_sum(m, flux_all, rhi, dir, 1, q, v, sum))
+                return -1;
+              acc = acc - sum / vr;
+            }
+            else
+              acc = acc - Fb[FL.off[dir] + v * FL.n[dir] + fr];
+            if (n < 5)
+              U2blk[v * ncell + c] += acc;
+            else
+              Bz2blk[c] += acc;
+          }
+        }
+  }
   return 0;
 }
 
@@ -746,7 +1112,7 @@ emf_count(const Mesh & m)
 
 // correct_emf, uniform-level branch (scheme/CorrectEmfAtBlockBorderFunctor.cpp:94-360) followed by
 // read_emf_and_update_{2d,3d} (scheme/ReadEmfAndUpdateFunctor.cpp:58-163) for block blk.
-static void
+static int
 correct_emf_and_update_b(const Mesh & m, int blk, const std::vector<double> & emf_all, double * B2blk)
 {
   const int     ex = m.bx + 1, ey = m.by + 1, ez = m.dim == 3 ? m.bz + 1 : 1;
@@ -774,9 +1140,13 @@ correct_emf_and_update_b(const Mesh & m, int blk, const std::vector<double> & em
           const int v1 = (m.dim == 2 && t1 == 2) ? 0 : (a1 == 0 ? -1 : (a1 == bsz[t1] ? 1 : 0));
           if (v0 == 0 && v1 == 0)
             continue;
-          // sibling edges: across t0, across t1, across both
-          int sib[3];
-          int sidx[3][3];
+          // sibling edges (core getEdgeSiblingLoc): across t0, across t1, across both
+          // (CorrectEmfAtBlockBorderFunctor.cpp:94-360)
+          Region rs[3];
+          bool   valid[3];
+          int    lev[3]; // sibling level - own level
+          int    sidx[3][3];
+          int    so[3][3];
           for (int n = 0; n < 3; ++n)
           {
             int o[3] = {0, 0, 0};
@@ -785,30 +1155,87 @@ correct_emf_and_update_b(const Mesh & m, int blk, const std::vector<double> & em
             if (n == 1 || n == 2)
               o[t1] = v1;
             const bool exists = (n == 0 && v0 != 0) || (n == 1 && v1 != 0) || (n == 2 && v0 != 0 && v1 != 0);
-            sib[n] = exists ? m.neighbor[(int64_t)blk * 27 + nb_slot(o[0], o[1], o[2])] : -1;
+            rs[n] = exists ? region_of(m, blk, o[0], o[1], o[2]) : Region{RK_MISSING, -1, {0, 0, 0}, nullptr};
+            valid[n] = rs[n].kind != RK_MISSING;
+            lev[n] = rs[n].kind == RK_COARSER ? -1 : (rs[n].kind == RK_FINER ? 1 : 0);
             for (int d = 0; d < 3; ++d)
-              sidx[n][d] = idx[d] - o[d] * bsz[d];
-          }
-          for (int n = 0; n < 3; ++n)
-            if (sib[n] >= 0 && m.level[sib[n]] != m.level[blk])
-              sib[n] = -2; // level jump: not supported by this restatement (checked by caller)
-          const bool all_same = sib[0] >= 0 && sib[1] >= 0 && sib[2] >= 0;
-          if (!all_same)
-            continue; // neither coarser nor finer neighbours on uniform meshes: emf2 keeps emf
-          const int64_t e = i + (int64_t)ex * (j + (int64_t)ey * k);
-          double        acc = 0.0;
-          int           count = 1;
-          acc += emf_self[c * ne + e];
-          for (int n = 0; n < 3; ++n)
-          {
-            if (sib[n] < m.n_owned)
             {
-              const int64_t es = sidx[n][0] + (int64_t)ex * (sidx[n][1] + (int64_t)ey * sidx[n][2]);
-              acc += emf_all[(size_t)sib[n] * ncomp * ne + c * ne + es];
-              count++;
+              so[n][d] = o[d];
+              sidx[n][d] = idx[d] - o[d] * bsz[d];
             }
           }
-          emf2[c * ne + e] = acc / (double)count;
+          const bool coarser = (valid[0] && lev[0] < 0) || (valid[1] && lev[1] < 0) || (valid[2] && lev[2] < 0);
+          const bool finer = (valid[0] && lev[0] > 0) || (valid[1] && lev[1] > 0) || (valid[2] && lev[2] > 0);
+          const bool all_same = valid[0] && lev[0] == 0 && valid[1] && lev[1] == 0 && valid[2] && lev[2] == 0;
+          const int64_t e = i + (int64_t)ex * (j + (int64_t)ey * k);
+          auto          sib_emf = [&](int id, const int * ix) {
+            const int64_t es = ix[0] + (int64_t)ex * (ix[1] + (int64_t)ey * ix[2]);
+            return emf_all[(size_t)id * ncomp * ne + c * ne + es];
+          };
+          if (coarser)
+          {
+            // average with the same-level siblings
+            double acc = emf_self[c * ne + e];
+            int    count = 1;
+            for (int n = 0; n < 3; ++n)
+              if (valid[n] && lev[n] == 0 && rs[n].kind != RK_OUTSIDE)
+              {
+                acc += sib_emf(rs[n].id, sidx[n]);
+                count++;
+              }
+            emf2[c * ne + e] = acc / (double)count;
+          }
+          else if (finer)
+          {
+            // average over the finer siblings' edges (3D: both sub-edges along the edge)
+            double acc = 0.0;
+            int    count = 0;
+            for (int n = 0; n < 3; ++n)
+            {
+              if (!(valid[n] && lev[n] > 0))
+                continue;
+              int F[3] = {0, 0, 0}, ch[3] = {0, 0, 0};
+              for (int d = 0; d < m.dim; ++d)
+              {
+                if (so[n][d] != 0)
+                {
+                  ch[d] = so[n][d] < 0 ? 1 : 0;
+                  F[d] = so[n][d] < 0 ? bsz[d] : 0;
+                }
+                else
+                {
+                  const int x = 2 * idx[d];
+                  ch[d] = x >= bsz[d];
+                  F[d] = x - ch[d] * bsz[d];
+                }
+              }
+              const int id = rs[n].child[ch[0] + 2 * ch[1] + 4 * ch[2]];
+              if (id < 0 || id >= m.n_owned)
+                return -1;
+              acc += sib_emf(id, F);
+              if (m.dim == 3)
+              {
+                int F1[3] = {F[0], F[1], F[2]};
+                F1[edir] += 1;
+                acc += sib_emf(id, F1);
+              }
+              count++;
+            }
+            emf2[c * ne + e] = acc / (double)count / (double)(1 << (m.dim - 1));
+          }
+          if (all_same)
+          {
+            double acc = 0.0;
+            int    count = 1;
+            acc += emf_self[c * ne + e];
+            for (int n = 0; n < 3; ++n)
+              if (rs[n].kind != RK_OUTSIDE)
+              {
+                acc += sib_emf(rs[n].id, sidx[n]);
+                count++;
+              }
+            emf2[c * ne + e] = acc / (double)count;
+          }
         }
   }
   // CT update
@@ -825,7 +1252,7 @@ correct_emf_and_update_b(const Mesh & m, int blk, const std::vector<double> & em
     for (int j = 0; j <= m.by; ++j)
       for (int i = 0; i < m.bx; ++i)
         By[i + (int64_t)m.bx * j] -= (E(0, i + 1, j, 0) - E(0, i, j, 0));
-    return;
+    return 0;
   }
   for (int k = 0; k < m.bz; ++k)
     for (int j = 0; j < m.by; ++j)
@@ -854,15 +1281,7 @@ correct_emf_and_update_b(const Mesh & m, int blk, const std::vector<double> & em
         d -= (E(0, i, j + 1, k) - E(0, i, j, k));
         Bz[i + (int64_t)m.bx * (j + (int64_t)m.by * k)] += d;
       }
-}
-
-static bool
-mesh_is_uniform(const Mesh & m)
-{
-  for (int b = 0; b < m.n_blocks; ++b)
-    if (m.level[b] != m.level[0])
-      return false;
-  return true;
+  return 0;
 }
 
 static double
@@ -886,6 +1305,9 @@ struct oracle_mesh
   const int32_t * outside_src;    // [n_blocks - n_owned]
   const int32_t * outside_normal; // [3 * (n_blocks - n_owned)], +1 below / -1 above the domain
   int32_t         bc[6];          // BC_MHD values for XMIN..ZMAX (FillOutside.h:55-61)
+  const int32_t * coord;          // [3 * n_blocks] block coordinates at the block's level, or null
+  const int32_t * fine_neighbor;  // [27 * 8 * n_blocks] children of refined neighbour regions, or null
+  int32_t         prolongation;   // [amr] cell_centered_prolongation_type: 0 SIMPLE_COPY, 1 LINEAR_MINMOD
 };
 
 struct oracle_settings
@@ -906,6 +1328,9 @@ to_mesh(const oracle_mesh * om)
   m.n_owned = om->n_owned;
   m.level = om->level;
   m.neighbor = om->neighbor;
+  m.coord = om->coord;
+  m.fine = om->fine_neighbor;
+  m.prolongation = om->prolongation;
   m.scaling_factor = om->scaling_factor;
   return m;
 }
@@ -918,29 +1343,40 @@ to_settings(const oracle_settings * os)
 
 // One do_time_step: U2 and B2 must equal U and B on entry (SolverGodunovMHD.cpp:166-167, 545-548).
 // Returns 0, -1 (missing neighbour), -2 (level jump), -3 (unknown Riemann solver).
+static double * g_flux_sink = nullptr; // oracle_step_fluxes: copy of the per-block face fluxes
+
 int
 oracle_step(const oracle_mesh * om, const oracle_settings * os, const double * U, double * U2,
             const double * B, double * B2, double dt)
 {
   const Mesh     m = to_mesh(om);
   const Settings s = to_settings(os);
-  if (!mesh_is_uniform(m))
-    return -2;
+  for (int b = 0; b < m.n_owned; ++b)
+    for (int sl = 0; sl < 27; ++sl)
+    {
+      const int id = m.neighbor[(int64_t)b * 27 + sl];
+      if (id >= 0 && id < m.n_owned && m.level[id] != m.level[b] && (m.level[id] != m.level[b] - 1 || !m.coord))
+        return -2;
+    }
   Fields f;
   f.m = &m;
   f.L = block_layout(m);
   f.U = U;
   f.B = B;
-  const int64_t       ne = emf_count(m) * (m.dim == 3 ? 3 : 1);
-  std::vector<double> emf_all((size_t)m.n_owned * ne, 0.0);
-  const double        dtdx = dt / cell_length(m, m.level[0]);
-  int                 status = 0;
+  const int64_t                    ne = emf_count(m) * (m.dim == 3 ? 3 : 1);
+  const FluxLayout                 FL = flux_layout(m);
+  std::vector<double>              emf_all((size_t)m.n_owned * ne, 0.0);
+  std::vector<std::vector<double>> flux_all((size_t)m.n_owned);
+  int                              status = 0;
+  // stages K2-K11 per block: everything up to the face fluxes and the raw edge EMFs
 #pragma omp parallel
   {
     StepWork w;
 #pragma omp for schedule(dynamic, 1)
     for (int blk = 0; blk < m.n_owned; ++blk)
     {
+      const double dtdx = dt / cell_length(m, m.level[blk]);
+      flux_all[blk].assign((size_t)FL.total, 0.0);
       int st = fill_bface_ghosted(m, f, blk, w);
       if (st == 0)
         st = convert_to_primitives(m, f, s, blk, w);
@@ -950,10 +1386,8 @@ oracle_step(const oracle_mesh * om, const oracle_settings * os, const double * U
         compute_predictor(m, s, dtdx, w);
         compute_elec_field(m, w);
         compute_sfacemag(m, dtdx, w);
-        double * U2blk = U2 + (int64_t)blk * 5 * f.L.ncell;
-        double * Bz2blk = B2 + (int64_t)blk * f.L.nface + f.L.nfx + f.L.nfy;
         for (int dir = 0; dir < m.dim && st == 0; ++dir)
-          st = fluxes_and_update(m, s, dtdx, dir, w, U2blk, Bz2blk);
+          st = compute_fluxes(m, s, dtdx, dir, w, flux_all[blk].data());
         if (st == 0)
           compute_emfs(m, s, dtdx, w, &emf_all[(size_t)blk * ne]);
       }
@@ -966,10 +1400,37 @@ oracle_step(const oracle_mesh * om, const oracle_settings * os, const double * U
   }
   if (status != 0)
     return status;
+  if (g_flux_sink)
+    for (int blk = 0; blk < m.n_owned; ++blk)
+      std::memcpy(g_flux_sink + (size_t)blk * FL.total, flux_all[blk].data(), sizeof(double) * FL.total);
+  // conservative update with the coarse/fine flux correction, then EMF correction + CT
 #pragma omp parallel for schedule(dynamic, 1)
   for (int blk = 0; blk < m.n_owned; ++blk)
-    correct_emf_and_update_b(m, blk, emf_all, B2 + (int64_t)blk * f.L.nface);
-  return 0;
+  {
+    double * U2blk = U2 + (int64_t)blk * 5 * f.L.ncell;
+    double * B2blk = B2 + (int64_t)blk * f.L.nface;
+    int      st = update_u(m, blk, flux_all, U2blk, B2blk + f.L.nfx + f.L.nfy);
+    if (st == 0)
+      st = correct_emf_and_update_b(m, blk, emf_all, B2blk);
+    if (st != 0)
+    {
+#pragma omp critical
+      status = st;
+    }
+  }
+  return status;
+}
+
+// oracle_step that also copies the per-block face fluxes (flux * dt/dx, [block][dir][var][face]) to
+// fluxes_out, for checks of the coarse/fine flux correction.
+int
+oracle_step_fluxes(const oracle_mesh * om, const oracle_settings * os, const double * U, double * U2,
+                   const double * B, double * B2, double dt, double * fluxes_out)
+{
+  g_flux_sink = fluxes_out;
+  const int st = oracle_step(om, os, U, U2, B, B2, dt);
+  g_flux_sink = nullptr;
+  return st;
 }
 
 // ComputeDtMHDFunctor::apply over owned blocks; returns invDt (max over cells).
