@@ -15,6 +15,7 @@ STATUS = {0: "ok", -1: "invalid argument", -2: "mesh not set or not supported", 
           -4: "output aliases an input", -5: "non-physical state produced", -6: "exceeds a fixed capacity"}
 
 PRECISION = {"fp64": 0, "mixed": 1}
+PROLONGATION = {"SIMPLE_COPY": 0, "EXTRAPOLATE_LINEAR_MINMOD": 1}
 RIEMANN = {"LLF": 2, "HLL": 3, "HLLC": 4, "HLLD": 5}
 BC = {"NONE": 0, "PERIODIC": 1, "ZERO_GRADIENT": 2, "WALL": 3}
 HEALTH = {1: "missing neighbour", 2: "level jump", 4: "density <= 0", 8: "non-finite value",
@@ -24,7 +25,7 @@ HEALTH = {1: "missing neighbour", 2: "level jump", 4: "density <= 0", 8: "non-fi
 class GmhdParams(ctypes.Structure):
     _fields_ = [("gamma0", ctypes.c_double), ("cfl", ctypes.c_double), ("slope_type", ctypes.c_double),
                 ("smallr", ctypes.c_double), ("smallc", ctypes.c_double), ("scaling_factor", ctypes.c_double),
-                ("riemann", ctypes.c_int32), ("precision", ctypes.c_int32)]
+                ("riemann", ctypes.c_int32), ("precision", ctypes.c_int32), ("prolongation", ctypes.c_int32)]
 
 
 _ip = ctypes.POINTER(ctypes.c_int32)
@@ -34,7 +35,7 @@ class GmhdMesh(ctypes.Structure):
     _fields_ = [("dim", ctypes.c_int32), ("bx", ctypes.c_int32), ("by", ctypes.c_int32), ("bz", ctypes.c_int32),
                 ("n_blocks", ctypes.c_int32), ("n_owned", ctypes.c_int32), ("level", _ip), ("neighbor", _ip),
                 ("problem", _ip), ("n_problems", ctypes.c_int32), ("outside_src", _ip), ("outside_normal", _ip),
-                ("bc", ctypes.c_int32 * 6)]
+                ("bc", ctypes.c_int32 * 6), ("coord", _ip), ("fine_neighbor", _ip)]
 
 
 class NativeError(RuntimeError):
@@ -115,4 +116,10 @@ class MeshTables:
         c.outside_normal = self.out_normal.ctypes.data_as(_ip) if self.out_normal.size else ctypes.cast(None, _ip)
         for i in range(6):
             c.bc[i] = int(bc[i])
+        # coarse/fine meshes: block coordinates and the children of refined neighbour regions
+        self.coord = np.ascontiguousarray(mesh.coords, dtype=np.int32).reshape(-1)
+        c.coord = self.coord.ctypes.data_as(_ip)
+        fine = getattr(mesh, "fine_neighbor", None)
+        self.fine = None if fine is None else np.ascontiguousarray(fine, dtype=np.int32).reshape(-1)
+        c.fine_neighbor = self.fine.ctypes.data_as(_ip) if self.fine is not None else ctypes.cast(None, _ip)
         self.c = c

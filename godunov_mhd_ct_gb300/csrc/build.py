@@ -24,6 +24,7 @@ UNITS = {
     "step_mixed.cu": ["--use_fast_math"],
     "gmhd_abi.cu": ["--fmad=false"],
     "noalloc.cu": ["--fmad=false"],
+    "amr.cu": ["--fmad=false"],
 }
 HEADERS = ["mhd_math.cuh", "fused_step.cuh", "launch.cuh", os.path.join("..", "..", "include", "gmhd.h")]
 

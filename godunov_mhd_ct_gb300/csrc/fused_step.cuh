@@ -41,6 +41,40 @@ struct StepArgs
   const double *             dt_dev;            // per problem dt on the device, or null
   unsigned long long *       invdt_out;         // per problem: fused CFL of U2/B2 (max), or null
   unsigned int *             health;            // OR of HEALTH_* flags
+  int                        n_blocks;          // ids >= n_blocks in `neighbor` are virtual blocks
+
+  // ---- coarse/fine meshes (all null / zero when no block has a neighbour at another level) ----
+  // Neighbour regions at another level are presented to the gather as virtual same-level blocks
+  // (Uv, Bv), built each step by the ghost prepass; Bccv holds the cell-centred B of SIMPLE_COPY
+  // ghosts (the coarse cell's own, ConvertToPrimitivesVariablesFunctor.cpp:439-446).
+  const int8_t *  kind;       // [n_owned * 27] RegionKind of each neighbour slot
+  const int32_t * fine;       // [n_blocks * 27 * 8] children of refined neighbour regions
+  const double *  Uv;         // [virtual][5][ncell]
+  const double *  Bv;         // [virtual][nface]
+  const double *  Bccv;       // [virtual][3][ncell]
+  int             prolongation; // 0 SIMPLE_COPY, 1 EXTRAPOLATE_LINEAR_MINMOD
+  // Two passes: pass 1 runs every tile that has no finer neighbour (and, side data only, the
+  // tiles that have both) and stores the fine-side face fluxes and raw border EMFs that coarse
+  // neighbours need; pass 2 runs the tiles next to finer blocks and reads them
+  // (ReadFluxesAndConservativeUpdateFunctor.cpp:141-172, CorrectEmfAtBlockBorderFunctor.cpp:94-360).
+  const int32_t * tile_list;  // tiles of this launch, ~tile for side-data-only tiles; null: all tiles
+  int             n_list;     // entries of tile_list
+  int             pass;       // 0 (single pass), 1 or 2
+  double *        flux_side;  // [slot][2*dim faces][NFV][flux_face_stride] fluxes * dt/dx
+  const int32_t * flux_slot;  // [n_owned] slot of blocks with a coarser face neighbour, else -1
+  int             flux_face_stride;
+  double *        emf_side;   // [slot][ncomp][(bx+1)(by+1)(bz+1 | 1)] raw EMFs * dt/dx
+  const int32_t * emf_slot;   // [n_owned] slot of blocks with any coarser neighbour, else -1
+};
+
+// Neighbour-region kinds of a coarse/fine mesh (RK_SAME also for the block itself).
+enum : int
+{
+  RK_MISSING = 0,
+  RK_SAME = 1,
+  RK_COARSER = 2,
+  RK_FINER = 3,
+  RK_OUTSIDE = 4
 };
 
 enum : unsigned int
@@ -52,10 +86,11 @@ enum : unsigned int
   HEALTH_LOW_BETA_FP64 = 16u, // informational: FP64 pressure recovery was used (mixed path)
 };
 
-template <typename R_, int DIM_, int TX_, int TY_, int TZ_, int NT_, bool EXACT_>
+template <typename R_, int DIM_, int TX_, int TY_, int TZ_, int NT_, bool EXACT_, bool AMR_ = false>
 struct Cfg
 {
   using R = R_;
+  static constexpr bool AMR = AMR_; // coarse/fine mesh support compiled in
   static constexpr int  DIM = DIM_;
   static constexpr int  TX = TX_;
   static constexpr int  TY = TY_;
@@ -163,6 +198,13 @@ struct TileView
   Phys<R>     ph;
   R           dtdx;
   int         x0, y0, z0, bx, by, bz, n_owned;
+  // coarse/fine meshes (s_kind null otherwise)
+  const int *     s_kind;
+  int             blk, pass;
+  const int32_t * fine;
+  const double *  emf_side;
+  const int32_t * emf_slot;
+  double *        emf_self; // this block's raw-EMF side slot in pass 1, or null
 };
 
 // stride of the S region along direction d
@@ -186,6 +228,191 @@ __device__ __forceinline__ int
 f_index(int i, int j, int k)
 {
   return CMP == 0 ? C::fxi(i, j, k) : (CMP == 1 ? C::fyi(i, j, k) : C::fzi(i, j, C::D3 ? k : 0));
+}
+
+// CorrectEmfAtBlockBorderFunctor::correct_emf (CorrectEmfAtBlockBorderFunctor.cpp:94-360) of a
+// block-border edge on a coarse/fine mesh. Siblings are the regions across the two transverse block
+// borders (v0 along D0, v1 along D1) and across both. Same-level copies are this tile's own value
+// (every block computes a shared edge from identical ghost data); a finer sibling's edge is the
+// fine block's raw EMF from pass 1 (3D: its two sub-edges along the edge). In pass 1 the raw value
+// is also stored for coarse neighbours.
+template <class C, int CD, int D0, int D1>
+__device__ __forceinline__ double
+amr_border_emf(const TileView<C> & t, const int * gi, int v0, int v1, typename C::R val)
+{
+  using R = typename C::R;
+  constexpr int COMP = C::DIM == 3 ? CD : 0;
+  if (v0 == 0 && v1 == 0)
+    return to_d<R>(val);
+  const int     sx = t.bx + 1, sy = t.by + 1;
+  const int64_t ne = (int64_t)sx * sy * (C::DIM == 3 ? t.bz + 1 : 1);
+  if (t.emf_self)
+    t.emf_self[COMP * ne + gi[0] + (int64_t)sx * (gi[1] + (int64_t)sy * gi[2])] = to_d<R>(val);
+  int kd[3], sl[3], so[3][3];
+#pragma unroll
+  for (int n = 0; n < 3; ++n)
+  {
+    so[n][0] = so[n][1] = so[n][2] = 0;
+    if (n == 0 || n == 2)
+      so[n][D0] = v0;
+    if (n == 1 || n == 2)
+      so[n][D1] = v1;
+    const bool exists = (n == 0 && v0 != 0) || (n == 1 && v1 != 0) || (n == 2 && v0 != 0 && v1 != 0);
+    sl[n] = nb_slot(so[n][0], so[n][1], so[n][2]);
+    kd[n] = exists ? t.s_kind[sl[n]] : (int)RK_MISSING;
+  }
+  bool coarser = false, finer = false, all_same = true;
+#pragma unroll
+  for (int n = 0; n < 3; ++n)
+  {
+    const bool valid = kd[n] != RK_MISSING;
+    coarser = coarser || (valid && kd[n] == RK_COARSER);
+    finer = finer || (valid && kd[n] == RK_FINER);
+    all_same = all_same && valid && kd[n] != RK_COARSER && kd[n] != RK_FINER;
+  }
+  double out = to_d<R>(val);
+  if (coarser)
+  {
+    R   acc = val;
+    int count = 1;
+#pragma unroll
+    for (int n = 0; n < 3; ++n)
+      if (kd[n] == RK_SAME)
+      {
+        acc += val;
+        ++count;
+      }
+    out = to_d<R>(acc / (R)count);
+  }
+  else if (finer)
+  {
+    const int bs[3] = {t.bx, t.by, t.bz};
+    double    acc = 0.0;
+    int       count = 0;
+#pragma unroll
+    for (int n = 0; n < 3; ++n)
+    {
+      if (kd[n] != RK_FINER)
+        continue;
+      int F[3] = {0, 0, 0}, ch[3] = {0, 0, 0};
+#pragma unroll
+      for (int d = 0; d < C::DIM; ++d)
+      {
+        if (so[n][d] != 0)
+        {
+          ch[d] = so[n][d] < 0 ? 1 : 0;
+          F[d] = so[n][d] < 0 ? bs[d] : 0;
+        }
+        else
+        {
+          const int x = 2 * gi[d];
+          ch[d] = x >= bs[d] ? 1 : 0;
+          F[d] = x - ch[d] * bs[d];
+        }
+      }
+      const int id = t.fine[((int64_t)t.blk * 27 + sl[n]) * 8 + ch[0] + 2 * ch[1] + 4 * ch[2]];
+      const int cs = id >= 0 ? t.emf_slot[id] : -1;
+      if (cs < 0)
+        continue;
+      const double * E = t.emf_side + ((int64_t)cs * C::NECOMP + COMP) * ne;
+      const int64_t  e = F[0] + (int64_t)sx * (F[1] + (int64_t)sy * F[2]);
+      acc += E[e];
+      if constexpr (C::DIM == 3)
+        acc += E[e + (CD == 0 ? 1 : (CD == 1 ? (int64_t)sx : (int64_t)sx * sy))];
+      ++count;
+    }
+    out = acc / (double)count / (double)(1 << (C::DIM - 1));
+  }
+  if (all_same)
+  {
+    R   acc = R(0);
+    int count = 1;
+    acc += val;
+#pragma unroll
+    for (int n = 0; n < 3; ++n)
+      if (kd[n] != RK_OUTSIDE)
+      {
+        acc += val;
+        ++count;
+      }
+    out = to_d<R>(acc / (R)count);
+  }
+  return out;
+}
+
+// Face fluxes on the tile's block-border faces of a coarse/fine mesh
+// (ReadFluxesAndConservativeUpdateFunctor.cpp:141-172, .h:233-270): pass 1 stores the fluxes of
+// faces whose neighbour is coarser; pass 2 replaces the flux of faces whose neighbour is finer by
+// the sum of the 2^(d-1) fine fluxes (first transverse axis fastest) / 2^d.
+template <class C>
+__device__ __forceinline__ void
+amr_border_fluxes(const StepArgs & a, typename C::R * fl, const int * s_kind, int blk, int x0, int y0, int z0, int tid)
+{
+  using R = typename C::R;
+  const int bs[3] = {a.bx, a.by, a.bz};
+  const int org[3] = {x0, y0, z0};
+  const int T[3] = {C::TX, C::TY, C::TZ};
+  const int my_slot = a.pass == 1 ? a.flux_slot[blk] : -1;
+  for (int f = 0; f < 2 * C::DIM; ++f)
+  {
+    const int d = f >> 1, side = (f & 1) ? 1 : -1;
+    if (side < 0 ? org[d] != 0 : org[d] + T[d] != bs[d])
+      continue;
+    int o[3] = {0, 0, 0};
+    o[d] = side;
+    const int  slot = nb_slot(o[0], o[1], o[2]);
+    const int  kd = s_kind[slot];
+    const bool write = a.pass == 1 && kd == RK_COARSER && my_slot >= 0;
+    const bool read = a.pass == 2 && kd == RK_FINER;
+    if (!write && !read)
+      continue;
+    const int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;
+    const int n1 = T[t1], n2 = C::DIM == 3 ? T[t2] : 1;
+    const int off = d == 0 ? 0 : (d == 1 ? C::NF_X : C::NF_X + C::NF_Y);
+    const int nxd = C::TX + (d == 0), nyd = C::TY + (d == 1);
+    for (int m = tid; m < n1 * n2 * C::NFV; m += C::NT)
+    {
+      const int v = m / (n1 * n2), r = m - v * (n1 * n2);
+      const int u1 = r % n1, u2 = r / n1;
+      int       li[3] = {0, 0, 0};
+      li[d] = side < 0 ? 0 : T[d];
+      li[t1] = u1;
+      if (C::DIM == 3)
+        li[t2] = u2;
+      const int idx = off + li[0] + nxd * (li[1] + nyd * li[2]);
+      const int g1 = org[t1] + u1, g2 = C::DIM == 3 ? org[t2] + u2 : 0;
+      if (write)
+      {
+        a.flux_side[(((int64_t)my_slot * 2 * C::DIM + f) * C::NFV + v) * a.flux_face_stride + g1 + (int64_t)bs[t1] * g2] =
+          to_d<R>(fl[v * C::NFT + idx]);
+        continue;
+      }
+      const int ff = 2 * d + (side < 0 ? 1 : 0); // the fine block's face toward this block
+      double    acc = 0.0;
+      for (int e2 = 0; e2 < (C::DIM == 3 ? 2 : 1); ++e2)
+        for (int e1 = 0; e1 < 2; ++e1)
+        {
+          int ch[3] = {0, 0, 0};
+          ch[d] = side < 0 ? 1 : 0;
+          int F1 = 2 * g1 + e1;
+          ch[t1] = F1 >= bs[t1] ? 1 : 0;
+          F1 -= ch[t1] * bs[t1];
+          int F2 = 0;
+          if (C::DIM == 3)
+          {
+            F2 = 2 * g2 + e2;
+            ch[t2] = F2 >= bs[t2] ? 1 : 0;
+            F2 -= ch[t2] * bs[t2];
+          }
+          const int id = a.fine[((int64_t)blk * 27 + slot) * 8 + ch[0] + 2 * ch[1] + 4 * ch[2]];
+          const int cs = id >= 0 ? a.flux_slot[id] : -1;
+          if (cs >= 0)
+            acc += a.flux_side[(((int64_t)cs * 2 * C::DIM + ff) * C::NFV + v) * a.flux_face_stride + F1 +
+                               (int64_t)bs[t1] * F2];
+        }
+      fl[v * C::NFT + idx] = to_r<R>(acc / (double)(1 << C::DIM));
+    }
+  }
 }
 
 // Corner positions of the 4 cells around an edge (the cell itself is LB).
@@ -289,7 +516,8 @@ edge_pass(const TileView<C> & t, int tid)
     // y edges: the reference swaps the RB and LT states (ComputeEmfAndStoreFunctor.cpp:551-560)
     recon_edge<C, D0, D1, LOC_RB>(t, sc - s0, g0 - f00, g1 - f10, qe[CD == 1 ? ELT : ERB]);
     recon_edge<C, D0, D1, LOC_LT>(t, sc - s1, g0 - f01, g1 - f11, qe[CD == 1 ? ERB : ELT]);
-    R val = edge_emf<R, CD>(qe, t.ph) * t.dtdx;
+    R      val = edge_emf<R, CD>(qe, t.ph) * t.dtdx;
+    double out;
     // an edge on a line where four blocks meet is averaged with its sibling copies (self first,
     // then the non-outside siblings); on a conforming mesh the copies are computed from identical
     // data, so the sum is of equal terms
@@ -298,7 +526,9 @@ edge_pass(const TileView<C> & t, int tid)
       const int bs[3] = {t.bx, t.by, t.bz};
       const int v0 = gi[D0] == 0 ? -1 : (gi[D0] == bs[D0] ? 1 : 0);
       const int v1 = (C::DIM == 2 && D1 == 2) ? 0 : (gi[D1] == 0 ? -1 : (gi[D1] == bs[D1] ? 1 : 0));
-      if (v0 != 0 && v1 != 0)
+      if constexpr (C::AMR)
+        out = amr_border_emf<C, CD, D0, D1>(t, gi, v0, v1, val);
+      else if (v0 != 0 && v1 != 0)
       {
         const int sl0 = nb_slot(D0 == 0 ? v0 : 0, D0 == 1 ? v0 : 0, 0);
         const int sl1 = nb_slot(D1 == 0 ? v1 : 0, D1 == 1 ? v1 : 0, D1 == 2 ? v1 : 0);
@@ -327,8 +557,10 @@ edge_pass(const TileView<C> & t, int tid)
           val = acc / (R)count;
         }
       }
+      if constexpr (!C::AMR)
+        out = to_d<R>(val);
     }
-    t.emfd[(C::DIM == 3 ? CD : 0) * C::NM + C::mi(i, j, k)] = to_d<R>(val);
+    t.emfd[(C::DIM == 3 ? CD : 0) * C::NM + C::mi(i, j, k)] = out;
   }
 }
 
@@ -412,10 +644,21 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
 
   const int tid = threadIdx.x;
   const int tiles_per_block = a.tiles_x * a.tiles_y * a.tiles_z;
-  const int blk = blockIdx.x / tiles_per_block;
+  int       tile = blockIdx.x;
+  bool      side_only = false; // pass 1 of a tile that also runs in pass 2: side data only
+  if (a.tile_list)
+  {
+    tile = a.tile_list[blockIdx.x];
+    if (tile < 0)
+    {
+      tile = ~tile;
+      side_only = true;
+    }
+  }
+  const int blk = tile / tiles_per_block;
   if (blk >= a.n_owned)
     return;
-  int       t = blockIdx.x - blk * tiles_per_block;
+  int       t = tile - blk * tiles_per_block;
   const int tx = t % a.tiles_x;
   t /= a.tiles_x;
   const int ty = t % a.tiles_y;
@@ -423,8 +666,13 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
   const int x0 = tx * TX, y0 = ty * TY, z0 = tz * TZ;
   const int bx = a.bx, by = a.by, bz = a.bz;
 
+  int * s_kind = s_nbr + 32;
   if (tid < 27)
+  {
     s_nbr[tid] = a.neighbor[(int64_t)blk * 27 + tid];
+    if constexpr (C::AMR)
+      s_kind[tid] = (int)a.kind[(int64_t)blk * 27 + tid];
+  }
   if (tid == 0)
     s_health = 0u;
   __syncthreads();
@@ -443,7 +691,7 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
         a.U2[((int64_t)blk * 5 + v) * a.ncell + cell] = a.U[((int64_t)blk * 5 + v) * a.ncell + cell];
     }
     // faces: the tile's tiles_per_block share of the block's face array
-    for (int64_t f = (int64_t)(blockIdx.x - blk * tiles_per_block) * NT + tid; f < a.nface;
+    for (int64_t f = (int64_t)(tile - blk * tiles_per_block) * NT + tid; f < a.nface;
          f += (int64_t)tiles_per_block * NT)
       a.B2[(int64_t)blk * a.nface + f] = a.B[(int64_t)blk * a.nface + f];
     return;
@@ -469,9 +717,38 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
     const int nb = s_nbr[nb_slot(ox, oy, oz)];
     if (nb < 0)
       health |= HEALTH_MISSING_NEIGHBOR;
-    else if (a.level[nb] != mylevel)
+    else if (nb < a.n_blocks && a.level[nb] != mylevel)
       health |= HEALTH_LEVEL_JUMP;
     return nb;
+  };
+  // face / conservative arrays of a real or virtual (coarse/fine ghost) neighbour block
+  auto bsrc = [&](int nb) -> const double * {
+    if constexpr (C::AMR)
+      return nb < a.n_blocks ? a.B + (int64_t)nb * a.nface : a.Bv + (int64_t)(nb - a.n_blocks) * a.nface;
+    else
+      return a.B + (int64_t)nb * a.nface;
+  };
+  auto usrc = [&](int nb) -> const double * {
+    if constexpr (C::AMR)
+      return nb < a.n_blocks ? a.U + (int64_t)nb * 5 * a.ncell : a.Uv + (int64_t)(nb - a.n_blocks) * 5 * a.ncell;
+    else
+      return a.U + (int64_t)nb * 5 * a.ncell;
+  };
+  // coarse/fine meshes: the block's own border face shared with a finer face neighbour is that
+  // neighbour's value (restriction), read from its virtual block
+  auto shared_face = [&](int d, int f, int n, int & nb, int & fq) {
+    if constexpr (C::AMR)
+    {
+      if (nb == blk && (f == 0 || f == n))
+      {
+        const int sl = nb_slot(d == 0 ? (f == 0 ? -1 : 1) : 0, d == 1 ? (f == 0 ? -1 : 1) : 0, d == 2 ? (f == 0 ? -1 : 1) : 0);
+        if (s_kind[sl] == RK_FINER)
+        {
+          nb = s_nbr[sl];
+          fq = f == 0 ? n : 0;
+        }
+      }
+    }
   };
   auto cell_off = [](int c, int n) { return c < 0 ? -1 : (c >= n ? 1 : 0); };
   auto face_off = [](int f, int n) { return f < 0 ? -1 : (f > n ? 1 : 0); };
@@ -497,9 +774,11 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       const int k = D3 ? n / ((TX + 5) * C::QY) - 2 : 0;
       const int fi = x0 + i, cj = y0 + j, ck = z0 + k;
       const int ox = face_off(fi, bx), oy = cell_off(cj, by), oz = D3 ? cell_off(ck, bz) : 0;
-      const int nb = owner(ox, oy, oz);
+      int       nb = owner(ox, oy, oz);
+      int       fq = fi - ox * bx;
+      shared_face(0, fi, bx, nb, fq);
       if (nb >= 0)
-        fvx[it] = a.B[(int64_t)nb * a.nface + (fi - ox * bx) + (int64_t)(bx + 1) * ((cj - oy * by) + (int64_t)by * (ck - oz * bz))];
+        fvx[it] = bsrc(nb)[fq + (int64_t)(bx + 1) * ((cj - oy * by) + (int64_t)by * (ck - oz * bz))];
     }
   }
 #pragma unroll
@@ -514,9 +793,11 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       const int k = D3 ? n / (C::QX * (TY + 5)) - 2 : 0;
       const int ci = x0 + i, fj = y0 + j, ck = z0 + k;
       const int ox = cell_off(ci, bx), oy = face_off(fj, by), oz = D3 ? cell_off(ck, bz) : 0;
-      const int nb = owner(ox, oy, oz);
+      int       nb = owner(ox, oy, oz);
+      int       fq = fj - oy * by;
+      shared_face(1, fj, by, nb, fq);
       if (nb >= 0)
-        fvy[it] = a.B[(int64_t)nb * a.nface + a.nfx + (ci - ox * bx) + (int64_t)bx * ((fj - oy * by) + (int64_t)(by + 1) * (ck - oz * bz))];
+        fvy[it] = bsrc(nb)[a.nfx + (ci - ox * bx) + (int64_t)bx * (fq + (int64_t)(by + 1) * (ck - oz * bz))];
     }
   }
 #pragma unroll
@@ -531,9 +812,12 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       const int k = D3 ? n / (C::QX * C::QY) - 2 : 0;
       const int ci = x0 + i, cj = y0 + j, fk = z0 + k;
       const int ox = cell_off(ci, bx), oy = cell_off(cj, by), oz = D3 ? face_off(fk, bz) : 0;
-      const int nb = owner(ox, oy, oz);
+      int       nb = owner(ox, oy, oz);
+      int       fq = fk - oz * bz;
+      if (D3)
+        shared_face(2, fk, bz, nb, fq);
       if (nb >= 0)
-        fvz[it] = a.B[(int64_t)nb * a.nface + a.nfx + a.nfy + (ci - ox * bx) + (int64_t)bx * ((cj - oy * by) + (int64_t)by * (fk - oz * bz))];
+        fvz[it] = bsrc(nb)[a.nfx + a.nfy + (ci - ox * bx) + (int64_t)bx * ((cj - oy * by) + (int64_t)by * fq)];
     }
   }
 #pragma unroll
@@ -553,7 +837,7 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       const int nb = owner(ox, oy, oz);
       if (nb >= 0)
       {
-        const double * Ub = a.U + (int64_t)nb * 5 * a.ncell + (ci - ox * bx) + (int64_t)bx * ((cj - oy * by) + (int64_t)by * (ck - oz * bz));
+        const double * Ub = usrc(nb) + (ci - ox * bx) + (int64_t)bx * ((cj - oy * by) + (int64_t)by * (ck - oz * bz));
 #pragma unroll
         for (int v = 0; v < 5; ++v)
           uq[it][v] = Ub[(int64_t)v * a.ncell];
@@ -574,6 +858,24 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       fbz[tid + it * NT] = to_r<R>(fvz[it]);
   __syncthreads();
 
+  // SIMPLE_COPY ghosts of a coarser neighbour take the coarse cell's own cell-centred B
+  // (ConvertToPrimitivesVariablesFunctor.cpp:439-446), kept by the ghost prepass in Bccv
+  const bool coarse_copy = C::AMR && a.prolongation == 0;
+  auto       coarse_bcc = [&](int ci, int cj, int ck, double * bc) -> bool {
+    const int ox = cell_off(ci, bx), oy = cell_off(cj, by), oz = D3 ? cell_off(ck, bz) : 0;
+    if ((ox | oy | oz) == 0)
+      return false;
+    const int sl = nb_slot(ox, oy, oz);
+    if (s_kind[sl] != RK_COARSER || s_nbr[sl] < a.n_blocks)
+      return false;
+    const int64_t  loc = (ci - ox * bx) + (int64_t)bx * ((cj - oy * by) + (int64_t)by * (ck - oz * bz));
+    const double * Bc = a.Bccv + (int64_t)(s_nbr[sl] - a.n_blocks) * 3 * a.ncell + loc;
+    bc[0] = Bc[0];
+    bc[1] = Bc[a.ncell];
+    bc[2] = Bc[2 * a.ncell];
+    return true;
+  };
+
   // primitive variables on the Q region (ConvertToPrimitivesVariablesFunctor)
 #pragma unroll
   for (int it = 0; it < ITQ; ++it)
@@ -590,10 +892,20 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
     if constexpr (C::EXACT)
     {
       // compute_primitives (models/mhd_utils.h:449-515), cIso == 0
-      const double Bxc = 0.5 * (fbx[C::fxi(i, j, k)] + fbx[C::fxi(i + 1, j, k)]);
-      const double Byc = 0.5 * (fby[C::fyi(i, j, k)] + fby[C::fyi(i, j + 1, k)]);
-      const double Bzc = D3 ? 0.5 * (fbz[C::fzi(i, j, k)] + fbz[C::fzi(i, j, k + 1)])
-                            : 0.5 * (fbz[C::fzi(i, j, 0)] + fbz[C::fzi(i, j, 0)]);
+      double Bxc = 0.5 * (fbx[C::fxi(i, j, k)] + fbx[C::fxi(i + 1, j, k)]);
+      double Byc = 0.5 * (fby[C::fyi(i, j, k)] + fby[C::fyi(i, j + 1, k)]);
+      double Bzc = D3 ? 0.5 * (fbz[C::fzi(i, j, k)] + fbz[C::fzi(i, j, k + 1)])
+                      : 0.5 * (fbz[C::fzi(i, j, 0)] + fbz[C::fzi(i, j, 0)]);
+      if (coarse_copy)
+      {
+        double bc[3];
+        if (coarse_bcc(ci, cj, ck, bc))
+        {
+          Bxc = bc[0];
+          Byc = bc[1];
+          Bzc = bc[2];
+        }
+      }
       const double r = fmax(u[ID], a.smallr);
       const double vx = u[IU] / r, vy = u[IV] / r, vz = u[IW] / r;
       const double eken = 0.5 * (vx * vx + vy * vy + vz * vz);
@@ -609,9 +921,17 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
     else
     {
       // FP32 recovery; FP64 when magnetic + kinetic energy dominate (low beta / high Mach)
-      const R Bxc = R(0.5) * (fbx[C::fxi(i, j, k)] + fbx[C::fxi(i + 1, j, k)]);
-      const R Byc = R(0.5) * (fby[C::fyi(i, j, k)] + fby[C::fyi(i, j + 1, k)]);
-      const R Bzc = D3 ? R(0.5) * (fbz[C::fzi(i, j, k)] + fbz[C::fzi(i, j, k + 1)]) : fbz[C::fzi(i, j, 0)];
+      R      Bxc = R(0.5) * (fbx[C::fxi(i, j, k)] + fbx[C::fxi(i + 1, j, k)]);
+      R      Byc = R(0.5) * (fby[C::fyi(i, j, k)] + fby[C::fyi(i, j + 1, k)]);
+      R      Bzc = D3 ? R(0.5) * (fbz[C::fzi(i, j, k)] + fbz[C::fzi(i, j, k + 1)]) : fbz[C::fzi(i, j, 0)];
+      double bcc[3];
+      const bool cc = coarse_copy && coarse_bcc(ci, cj, ck, bcc);
+      if (cc)
+      {
+        Bxc = to_r<R>(bcc[0]);
+        Byc = to_r<R>(bcc[1]);
+        Bzc = to_r<R>(bcc[2]);
+      }
       const R r = rmax<R>(to_r<R>(u[ID]), ph.smallr);
       const R ir = R(1) / r;
       const R vx = to_r<R>(u[IU]) * ir, vy = to_r<R>(u[IV]) * ir, vz = to_r<R>(u[IW]) * ir;
@@ -627,16 +947,16 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
           const int co_y = cell_off(cj, by), co_z = D3 ? cell_off(ck, bz) : 0;
           const int nb0 = owner(fo, co_y, co_z), nb1 = owner(fo1, co_y, co_z);
           const int64_t tr = (int64_t)(bx + 1) * ((cj - co_y * by) + (int64_t)by * (ck - co_z * bz));
-          bxl = nb0 >= 0 ? a.B[(int64_t)nb0 * a.nface + (x0 + i - fo * bx) + tr] : 0.0;
-          bxr = nb1 >= 0 ? a.B[(int64_t)nb1 * a.nface + (x0 + i + 1 - fo1 * bx) + tr] : 0.0;
+          bxl = nb0 >= 0 ? bsrc(nb0)[(x0 + i - fo * bx) + tr] : 0.0;
+          bxr = nb1 >= 0 ? bsrc(nb1)[(x0 + i + 1 - fo1 * bx) + tr] : 0.0;
         }
         {
           const int fo = face_off(y0 + j, by), fo1 = face_off(y0 + j + 1, by);
           const int co_x = cell_off(ci, bx), co_z = D3 ? cell_off(ck, bz) : 0;
           const int nb0 = owner(co_x, fo, co_z), nb1 = owner(co_x, fo1, co_z);
           const int64_t base = a.nfx + (ci - co_x * bx);
-          byl = nb0 >= 0 ? a.B[(int64_t)nb0 * a.nface + base + (int64_t)bx * ((y0 + j - fo * by) + (int64_t)(by + 1) * (ck - co_z * bz))] : 0.0;
-          byr = nb1 >= 0 ? a.B[(int64_t)nb1 * a.nface + base + (int64_t)bx * ((y0 + j + 1 - fo1 * by) + (int64_t)(by + 1) * (ck - co_z * bz))] : 0.0;
+          byl = nb0 >= 0 ? bsrc(nb0)[base + (int64_t)bx * ((y0 + j - fo * by) + (int64_t)(by + 1) * (ck - co_z * bz))] : 0.0;
+          byr = nb1 >= 0 ? bsrc(nb1)[base + (int64_t)bx * ((y0 + j + 1 - fo1 * by) + (int64_t)(by + 1) * (ck - co_z * bz))] : 0.0;
         }
         if (D3)
         {
@@ -644,14 +964,15 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
           const int co_x = cell_off(ci, bx), co_y = cell_off(cj, by);
           const int nb0 = owner(co_x, co_y, fo), nb1 = owner(co_x, co_y, fo1);
           const int64_t base = a.nfx + a.nfy + (ci - co_x * bx) + (int64_t)bx * (cj - co_y * by);
-          bzl = nb0 >= 0 ? a.B[(int64_t)nb0 * a.nface + base + (int64_t)bx * by * (z0 + k - fo * bz)] : 0.0;
-          bzr = nb1 >= 0 ? a.B[(int64_t)nb1 * a.nface + base + (int64_t)bx * by * (z0 + k + 1 - fo1 * bz)] : 0.0;
+          bzl = nb0 >= 0 ? bsrc(nb0)[base + (int64_t)bx * by * (z0 + k - fo * bz)] : 0.0;
+          bzr = nb1 >= 0 ? bsrc(nb1)[base + (int64_t)bx * by * (z0 + k + 1 - fo1 * bz)] : 0.0;
         }
         else
         {
           bzl = bzr = (double)Bzc;
         }
-        const double Bx2 = 0.5 * (bxl + bxr), By2 = 0.5 * (byl + byr), Bz2 = 0.5 * (bzl + bzr);
+        const double Bx2 = cc ? bcc[0] : 0.5 * (bxl + bxr), By2 = cc ? bcc[1] : 0.5 * (byl + byr),
+                     Bz2 = cc ? bcc[2] : 0.5 * (bzl + bzr);
         const double rd = fmax(u[ID], a.smallr);
         const double emag_d = 0.5 * (Bx2 * Bx2 + By2 * By2 + Bz2 * Bz2);
         const double ekin_d = 0.5 * (u[IU] * u[IU] + u[IV] * u[IV] + u[IW] * u[IW]) / rd;
@@ -874,6 +1195,18 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
     tv.by = by;
     tv.bz = bz;
     tv.n_owned = a.n_owned;
+    if constexpr (C::AMR)
+    {
+      tv.s_kind = s_kind;
+      tv.blk = blk;
+      tv.pass = a.pass;
+      tv.fine = a.fine;
+      tv.emf_side = a.emf_side;
+      tv.emf_slot = a.emf_slot;
+      tv.emf_self = (a.pass == 1 && a.emf_slot[blk] >= 0)
+                      ? a.emf_side + (int64_t)a.emf_slot[blk] * C::NECOMP * ((int64_t)(bx + 1) * (by + 1) * (D3 ? bz + 1 : 1))
+                      : nullptr;
+    }
     edge_pass<C, 2>(tv, tid);
     if constexpr (DIM == 3)
     {
@@ -886,6 +1219,13 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       flux_pass<C, 2>(tv, tid);
   }
   __syncthreads();
+  if constexpr (C::AMR)
+  {
+    amr_border_fluxes<C>(a, fl, s_kind, blk, x0, y0, z0, tid);
+    __syncthreads();
+    if (side_only)
+      return; // this tile's update runs in pass 2
+  }
 
   // ---- phase 6: CT update (ReadEmfAndUpdateFunctor.cpp:58-163) on faces [0, T] along each
   // normal; a tile writes faces [0, T) and face T when it ends at the block border, and keeps all

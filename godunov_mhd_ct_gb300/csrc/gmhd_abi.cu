@@ -2,7 +2,9 @@
 // the CFL reduction, the outside-block fill and a graph-captured multi-step driver.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -53,6 +55,23 @@ struct gmhd_ctx
   int             mesh_version = 0, graph_mesh_version = -1;
   uint64_t        bytes = 0;
   int             last_cuda = 0;
+  // coarse/fine meshes: virtual neighbour blocks, two-pass tile lists, fine-side data
+  bool      amr = false;
+  int       n_virtual = 0, n_list1 = 0, n_list2 = 0, flux_face_stride = 0;
+  int8_t *  d_kind = nullptr;
+  int32_t * d_fine = nullptr;
+  int32_t * d_coord = nullptr;
+  int32_t * d_vmap = nullptr;
+  int32_t * d_nbr_real = nullptr;
+  int32_t * d_list1 = nullptr;
+  int32_t * d_list2 = nullptr;
+  int32_t * d_flux_slot = nullptr;
+  int32_t * d_emf_slot = nullptr;
+  double *  d_Uv = nullptr;
+  double *  d_Bv = nullptr;
+  double *  d_Bccv = nullptr;
+  double *  d_flux_side = nullptr;
+  double *  d_emf_side = nullptr;
 };
 
 namespace
@@ -120,6 +139,15 @@ free_mesh(gmhd_ctx * c)
   c->d_dt = c->d_t = c->d_tend = c->d_dtlog = nullptr;
   c->d_counter = nullptr;
   c->d_U = c->d_U2 = c->d_B = c->d_B2 = nullptr;
+  for (void * p : {(void *)c->d_kind, (void *)c->d_fine, (void *)c->d_coord, (void *)c->d_vmap, (void *)c->d_nbr_real,
+                   (void *)c->d_list1, (void *)c->d_list2, (void *)c->d_flux_slot, (void *)c->d_emf_slot,
+                   (void *)c->d_Uv, (void *)c->d_Bv, (void *)c->d_Bccv, (void *)c->d_flux_side, (void *)c->d_emf_side})
+    dfree(p);
+  c->d_kind = nullptr;
+  c->d_fine = c->d_coord = c->d_vmap = c->d_nbr_real = c->d_list1 = c->d_list2 = c->d_flux_slot = c->d_emf_slot = nullptr;
+  c->d_Uv = c->d_Bv = c->d_Bccv = c->d_flux_side = c->d_emf_side = nullptr;
+  c->amr = false;
+  c->n_virtual = c->n_list1 = c->n_list2 = c->flux_face_stride = 0;
   c->dtlog_cap = 0;
   c->bytes = sizeof(unsigned int);
   if (c->graph_exec)
@@ -159,11 +187,12 @@ make_args(const gmhd_ctx * c, const double * U, double * U2, const double * B, d
   a.cfl = c->p.cfl;
   a.riemann = c->p.riemann;
   a.health = c->d_health;
+  a.n_blocks = c->n_blocks;
   return a;
 }
 
 int
-launch_step(gmhd_ctx * ctx, const gmhd::StepArgs & a, cudaStream_t s)
+launch_one(gmhd_ctx * ctx, const gmhd::StepArgs & a, cudaStream_t s)
 {
   const int rc = ctx->p.precision == GMHD_PRECISION_MIXED ? gmhd::launch_step_mixed(a, ctx->dim, s)
                                                           : gmhd::launch_step_fp64(a, ctx->dim, s);
@@ -171,6 +200,71 @@ launch_step(gmhd_ctx * ctx, const gmhd::StepArgs & a, cudaStream_t s)
     return GMHD_ERR_ARGUMENT;
   if (rc != 0)
     return cuda_fail(ctx, (cudaError_t)rc);
+  return GMHD_OK;
+}
+
+// One do_time_step. On coarse/fine meshes: the ghost prepass (virtual neighbour blocks from U, B),
+// then pass 1 (tiles without finer neighbours; fine-side fluxes and EMFs) and pass 2 (tiles next to
+// finer blocks, reading them).
+int
+launch_step(gmhd_ctx * ctx, const gmhd::StepArgs & a0, cudaStream_t s)
+{
+  if (!ctx->amr)
+    return launch_one(ctx, a0, s);
+  gmhd::GhostArgs g;
+  std::memset(&g, 0, sizeof g);
+  g.U = a0.U;
+  g.B = a0.B;
+  g.Uv = ctx->d_Uv;
+  g.Bv = ctx->d_Bv;
+  g.Bccv = ctx->d_Bccv;
+  g.vmap = ctx->d_vmap;
+  g.neighbor = ctx->d_nbr_real;
+  g.kind = ctx->d_kind;
+  g.fine = ctx->d_fine;
+  g.coord = ctx->d_coord;
+  g.n_virtual = ctx->n_virtual;
+  g.dim = ctx->dim;
+  g.bx = ctx->bx;
+  g.by = ctx->by;
+  g.bz = ctx->bz;
+  g.prolongation = ctx->p.prolongation;
+  g.ncell = ctx->ncell;
+  g.nfx = ctx->nfx;
+  g.nfy = ctx->nfy;
+  g.nface = ctx->nface;
+  g.health = ctx->d_health;
+  int rc = gmhd::launch_ghost_prepass(g, s);
+  if (rc != 0)
+    return cuda_fail(ctx, (cudaError_t)rc);
+  gmhd::StepArgs a = a0;
+  a.kind = ctx->d_kind;
+  a.fine = ctx->d_fine;
+  a.Uv = ctx->d_Uv;
+  a.Bv = ctx->d_Bv;
+  a.Bccv = ctx->d_Bccv;
+  a.prolongation = ctx->p.prolongation;
+  a.flux_side = ctx->d_flux_side;
+  a.flux_slot = ctx->d_flux_slot;
+  a.flux_face_stride = ctx->flux_face_stride;
+  a.emf_side = ctx->d_emf_side;
+  a.emf_slot = ctx->d_emf_slot;
+  if (ctx->n_list1 > 0)
+  {
+    a.pass = 1;
+    a.tile_list = ctx->d_list1;
+    a.n_list = ctx->n_list1;
+    if ((rc = launch_one(ctx, a, s)))
+      return rc;
+  }
+  if (ctx->n_list2 > 0)
+  {
+    a.pass = 2;
+    a.tile_list = ctx->d_list2;
+    a.n_list = ctx->n_list2;
+    if ((rc = launch_one(ctx, a, s)))
+      return rc;
+  }
   return GMHD_OK;
 }
 
@@ -383,6 +477,146 @@ check_health(gmhd_ctx * ctx, cudaStream_t s, unsigned int * flags_out)
   return GMHD_OK;
 }
 
+// Coarse/fine tables: virtual blocks for every neighbour region read through the ghost prepass,
+// the kernel's neighbour table pointing at them, fine-side data slots and the two tile lists.
+int
+setup_amr(gmhd_ctx * ctx, const gmhd_mesh * m, const std::vector<int8_t> & kind)
+{
+  auto lev = [](int k) { return k == gmhd::RK_COARSER ? -1 : (k == gmhd::RK_FINER ? 1 : (k == gmhd::RK_MISSING ? -100 : 0)); };
+  auto slot_of = [](const int * o) { return (o[2] + 1) * 9 + (o[1] + 1) * 3 + (o[0] + 1); };
+  const int            nown = m->n_owned;
+  std::vector<int32_t> knbr(m->neighbor, m->neighbor + (size_t)m->n_blocks * 27);
+  std::vector<int32_t> vmap;
+  std::vector<int32_t> flux_slot(nown, -1), emf_slot(nown, -1);
+  int                  n_flux = 0, n_emf = 0;
+  for (int b = 0; b < nown; ++b)
+  {
+    bool coarser_face = false, coarser_any = false;
+    for (int s = 0; s < 27; ++s)
+    {
+      if (s == 13 || (m->dim == 2 && s / 9 != 1))
+        continue;
+      const int o[3] = {s % 3 - 1, (s / 3) % 3 - 1, s / 9 - 1};
+      const int k = kind[(size_t)b * 27 + s];
+      bool      virt = k == gmhd::RK_COARSER || k == gmhd::RK_FINER;
+      if (k == gmhd::RK_COARSER)
+      {
+        coarser_any = true;
+        coarser_face = coarser_face || (std::abs(o[0]) + std::abs(o[1]) + std::abs(o[2]) == 1);
+      }
+      // a same-level region whose border faces (along a normal) must come from a finer region
+      if (!virt && (k == gmhd::RK_SAME || k == gmhd::RK_OUTSIDE))
+        for (int c = 0; c < m->dim && !virt; ++c)
+        {
+          if (o[c] != 0)
+            continue;
+          for (int sg = -1; sg <= 1 && !virt; sg += 2)
+          {
+            int o1[3] = {o[0], o[1], o[2]};
+            o1[c] = sg;
+            virt = lev(kind[(size_t)b * 27 + slot_of(o1)]) > lev(k);
+          }
+        }
+      if (virt)
+      {
+        knbr[(size_t)b * 27 + s] = m->n_blocks + (int32_t)(vmap.size() / 2);
+        vmap.push_back(b);
+        vmap.push_back(s);
+      }
+    }
+    if (coarser_face)
+      flux_slot[b] = n_flux++;
+    if (coarser_any)
+      emf_slot[b] = n_emf++;
+  }
+  // two-pass tile lists
+  int T[3];
+  if (ctx->p.precision == GMHD_PRECISION_MIXED)
+    gmhd::tile_shape_mixed(m->dim, ctx->bx, ctx->by, ctx->bz, T);
+  else
+    gmhd::tile_shape_fp64(m->dim, ctx->bx, ctx->by, ctx->bz, T);
+  const int            nt[3] = {ctx->bx / T[0], ctx->by / T[1], m->dim == 3 ? ctx->bz / T[2] : 1};
+  const int            tpb = nt[0] * nt[1] * nt[2];
+  std::vector<int32_t> list1, list2;
+  for (int b = 0; b < nown; ++b)
+    for (int t = 0; t < tpb; ++t)
+    {
+      const int tc[3] = {t % nt[0], (t / nt[0]) % nt[1], t / (nt[0] * nt[1])};
+      bool      fin = false, coa = false;
+      for (int s = 0; s < 27; ++s)
+      {
+        if (s == 13 || (m->dim == 2 && s / 9 != 1))
+          continue;
+        const int o[3] = {s % 3 - 1, (s / 3) % 3 - 1, s / 9 - 1};
+        bool      touch = true;
+        for (int d = 0; d < 3; ++d)
+          if (o[d] != 0 && tc[d] != (o[d] < 0 ? 0 : nt[d] - 1))
+            touch = false;
+        if (!touch)
+          continue;
+        fin = fin || kind[(size_t)b * 27 + s] == gmhd::RK_FINER;
+        coa = coa || kind[(size_t)b * 27 + s] == gmhd::RK_COARSER;
+      }
+      const int32_t id = b * tpb + t;
+      if (!fin)
+        list1.push_back(id);
+      else
+      {
+        if (coa)
+          list1.push_back(~id);
+        list2.push_back(id);
+      }
+    }
+  const int     nv = (int)(vmap.size() / 2);
+  const int     ncomp = m->dim == 3 ? 3 : 1;
+  const int64_t ne = (int64_t)(ctx->bx + 1) * (ctx->by + 1) * (m->dim == 3 ? ctx->bz + 1 : 1);
+  const int     nfv = m->dim == 3 ? 5 : 6;
+  ctx->flux_face_stride = m->dim == 3 ? std::max(ctx->by * ctx->bz, std::max(ctx->bx * ctx->bz, ctx->bx * ctx->by))
+                                      : std::max(ctx->bx, ctx->by);
+  int rc;
+  if ((rc = dalloc(ctx, &ctx->d_kind, kind.size())) || (rc = dalloc(ctx, &ctx->d_nbr_real, knbr.size())) ||
+      (rc = dalloc(ctx, &ctx->d_vmap, vmap.size())) || (rc = dalloc(ctx, &ctx->d_list1, list1.size())) ||
+      (rc = dalloc(ctx, &ctx->d_list2, list2.size())) || (rc = dalloc(ctx, &ctx->d_flux_slot, (size_t)nown)) ||
+      (rc = dalloc(ctx, &ctx->d_emf_slot, (size_t)nown)) || (rc = dalloc(ctx, &ctx->d_coord, (size_t)m->n_blocks * 3)) ||
+      (rc = dalloc(ctx, &ctx->d_fine, (size_t)m->n_blocks * 27 * 8)) ||
+      (rc = dalloc(ctx, &ctx->d_Uv, (size_t)nv * 5 * ctx->ncell)) || (rc = dalloc(ctx, &ctx->d_Bv, (size_t)nv * ctx->nface)) ||
+      (rc = dalloc(ctx, &ctx->d_Bccv, (size_t)nv * 3 * ctx->ncell)) ||
+      (rc = dalloc(ctx, &ctx->d_flux_side, (size_t)n_flux * 2 * m->dim * nfv * ctx->flux_face_stride)) ||
+      (rc = dalloc(ctx, &ctx->d_emf_side, (size_t)n_emf * ncomp * ne)))
+    return rc;
+  GMHD_CUDA(cudaMemcpy(ctx->d_kind, kind.data(), kind.size(), cudaMemcpyHostToDevice));
+  // the real table for the prepass; the kernel's table with the virtual ids
+  GMHD_CUDA(cudaMemcpy(ctx->d_nbr_real, m->neighbor, sizeof(int32_t) * knbr.size(), cudaMemcpyHostToDevice));
+  GMHD_CUDA(cudaMemcpy(ctx->d_neighbor, knbr.data(), sizeof(int32_t) * knbr.size(), cudaMemcpyHostToDevice));
+  if (nv)
+    GMHD_CUDA(cudaMemcpy(ctx->d_vmap, vmap.data(), sizeof(int32_t) * vmap.size(), cudaMemcpyHostToDevice));
+  if (!list1.empty())
+    GMHD_CUDA(cudaMemcpy(ctx->d_list1, list1.data(), sizeof(int32_t) * list1.size(), cudaMemcpyHostToDevice));
+  if (!list2.empty())
+    GMHD_CUDA(cudaMemcpy(ctx->d_list2, list2.data(), sizeof(int32_t) * list2.size(), cudaMemcpyHostToDevice));
+  GMHD_CUDA(cudaMemcpy(ctx->d_flux_slot, flux_slot.data(), sizeof(int32_t) * nown, cudaMemcpyHostToDevice));
+  GMHD_CUDA(cudaMemcpy(ctx->d_emf_slot, emf_slot.data(), sizeof(int32_t) * nown, cudaMemcpyHostToDevice));
+  if (m->coord)
+    GMHD_CUDA(cudaMemcpy(ctx->d_coord, m->coord, sizeof(int32_t) * m->n_blocks * 3, cudaMemcpyHostToDevice));
+  else
+    GMHD_CUDA(cudaMemset(ctx->d_coord, 0, sizeof(int32_t) * m->n_blocks * 3));
+  if (m->fine_neighbor)
+    GMHD_CUDA(cudaMemcpy(ctx->d_fine, m->fine_neighbor, sizeof(int32_t) * m->n_blocks * 27 * 8, cudaMemcpyHostToDevice));
+  else
+    GMHD_CUDA(cudaMemset(ctx->d_fine, 0xff, sizeof(int32_t) * m->n_blocks * 27 * 8));
+  if (nv)
+  {
+    GMHD_CUDA(cudaMemset(ctx->d_Uv, 0, sizeof(double) * (size_t)nv * 5 * ctx->ncell));
+    GMHD_CUDA(cudaMemset(ctx->d_Bv, 0, sizeof(double) * (size_t)nv * ctx->nface));
+    GMHD_CUDA(cudaMemset(ctx->d_Bccv, 0, sizeof(double) * (size_t)nv * 3 * ctx->ncell));
+  }
+  ctx->amr = true;
+  ctx->n_virtual = nv;
+  ctx->n_list1 = (int)list1.size();
+  ctx->n_list2 = (int)list2.size();
+  return GMHD_OK;
+}
+
 } // namespace
 
 extern "C" {
@@ -460,15 +694,66 @@ gmhd_set_mesh(gmhd_ctx * ctx, const gmhd_mesh * m)
     if (m->problem && (m->problem[b] < 0 || m->problem[b] >= np))
       return GMHD_ERR_MESH;
   }
+  if (m->fine_neighbor)
+    for (int64_t i = 0; i < (int64_t)m->n_blocks * 27 * 8; ++i)
+      if (m->fine_neighbor[i] < -1 || m->fine_neighbor[i] >= m->n_owned)
+        return GMHD_ERR_MESH;
+  // kind of every neighbour region of the owned blocks (same level, one coarser, one finer, outside)
+  std::vector<int8_t> kind((size_t)m->n_owned * 27, (int8_t)gmhd::RK_MISSING);
+  bool                amr = false;
   for (int b = 0; b < m->n_owned; ++b)
     for (int s = 0; s < 27; ++s)
     {
+      int8_t & k = kind[(size_t)b * 27 + s];
+      if (s == 13)
+      {
+        k = gmhd::RK_SAME;
+        continue;
+      }
+      if (m->dim == 2 && s / 9 != 1)
+        continue;
       const int nb = m->neighbor[(int64_t)b * 27 + s];
-      if (nb >= 0 && m->level[nb] != m->level[b])
-        return GMHD_ERR_MESH; // coarse/fine interfaces are not supported by this path
-      if (nb >= 0 && m->problem && m->problem[nb] != m->problem[b])
-        return GMHD_ERR_MESH;
+      if (nb >= 0)
+      {
+        if (m->problem && m->problem[nb] != m->problem[b])
+          return GMHD_ERR_MESH;
+        if (nb >= m->n_owned)
+        {
+          if (m->level[nb] != m->level[b])
+            return GMHD_ERR_MESH; // outside blocks are at the level of the block they serve
+          k = gmhd::RK_OUTSIDE;
+        }
+        else if (m->level[nb] == m->level[b])
+          k = gmhd::RK_SAME;
+        else if (m->level[nb] == m->level[b] - 1 && m->coord)
+        {
+          k = gmhd::RK_COARSER;
+          amr = true;
+        }
+        else
+          return GMHD_ERR_MESH; // not 2:1 balanced, or a coarser neighbour without coordinates
+        continue;
+      }
+      if (!m->fine_neighbor)
+        continue;
+      bool any = false;
+      for (int c = 0; c < (1 << m->dim); ++c)
+      {
+        const int id = m->fine_neighbor[((int64_t)b * 27 + s) * 8 + c];
+        if (id < 0)
+          continue;
+        if (m->level[id] != m->level[b] + 1 || (m->problem && m->problem[id] != m->problem[b]))
+          return GMHD_ERR_MESH;
+        any = true;
+      }
+      if (any)
+      {
+        k = gmhd::RK_FINER;
+        amr = true;
+      }
     }
+  if (amr && (m->bx % 2 || m->by % 2 || (m->dim == 3 && m->bz % 2)))
+    return GMHD_ERR_MESH;
   for (int o = 0; o < n_out; ++o)
     if (m->outside_src[o] < 0 || m->outside_src[o] >= m->n_owned)
       return GMHD_ERR_MESH;
@@ -510,6 +795,8 @@ gmhd_set_mesh(gmhd_ctx * ctx, const gmhd_mesh * m)
     GMHD_CUDA(cudaMemcpy(ctx->d_out_src, m->outside_src, sizeof(int32_t) * n_out, cudaMemcpyHostToDevice));
     GMHD_CUDA(cudaMemcpy(ctx->d_out_normal, m->outside_normal, sizeof(int32_t) * 3 * n_out, cudaMemcpyHostToDevice));
   }
+  if (amr && (rc = setup_amr(ctx, m, kind)))
+    return rc;
   ctx->has_mesh = true;
   ctx->mesh_version++;
   return GMHD_OK;

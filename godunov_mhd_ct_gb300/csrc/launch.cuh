@@ -19,7 +19,7 @@ launch_fused(StepArgs a, cudaStream_t stream)
   a.tiles_x = a.bx / C::TX;
   a.tiles_y = a.by / C::TY;
   a.tiles_z = C::DIM == 3 ? a.bz / C::TZ : 1;
-  const long long nblocks = (long long)a.n_owned * a.tiles_x * a.tiles_y * a.tiles_z;
+  const long long nblocks = a.tile_list ? (long long)a.n_list : (long long)a.n_owned * a.tiles_x * a.tiles_y * a.tiles_z;
   if (nblocks <= 0)
     return 0;
   fused_step_kernel<C><<<(unsigned)nblocks, C::NT, C::SMEM_BYTES, stream>>>(a);
@@ -39,7 +39,30 @@ prepare_fused()
 // Tile choice: the largest configured tile that divides the block.
 int launch_step_fp64(const StepArgs & a, int dim, cudaStream_t stream);
 int launch_step_mixed(const StepArgs & a, int dim, cudaStream_t stream);
+// the tile extents launch_step_* uses for these block sizes
+void tile_shape_fp64(int dim, int bx, int by, int bz, int * t);
+void tile_shape_mixed(int dim, int bx, int by, int bz, int * t);
 int prepare_fp64();
 int prepare_mixed();
+
+// coarse/fine ghost prepass (amr.cu): fills the virtual neighbour blocks read by the fused step
+struct GhostArgs
+{
+  const double *  U;
+  const double *  B;
+  double *        Uv;
+  double *        Bv;
+  double *        Bccv;
+  const int32_t * vmap;     // [n_virtual][2]: owner block, neighbour slot
+  const int32_t * neighbor; // [n_blocks * 27] real ids (same-level, coarser or outside block)
+  const int8_t *  kind;     // [n_owned * 27]
+  const int32_t * fine;     // [n_blocks * 27 * 8]
+  const int32_t * coord;    // [n_blocks * 3]
+  int             n_virtual, dim, bx, by, bz, prolongation;
+  int64_t         ncell, nfx, nfy, nface;
+  unsigned int *  health;
+};
+
+int launch_ghost_prepass(const GhostArgs & g, cudaStream_t stream);
 
 } // namespace gmhd

@@ -1,5 +1,7 @@
 // FP64 instantiations of the fused step: the drop-in path. This unit is compiled with
 // --fmad=false so that every a*b+c stays unfused, matching the reference formulas' FP64 rounding.
+#include <type_traits>
+
 #include "launch.cuh"
 
 namespace gmhd
@@ -9,21 +11,49 @@ using F64_3D_444 = Cfg<double, 3, 4, 4, 4, 64, true>;
 using F64_2D_16 = Cfg<double, 2, 16, 16, 1, 256, true>;
 using F64_2D_8 = Cfg<double, 2, 8, 8, 1, 64, true>;
 using F64_2D_4 = Cfg<double, 2, 4, 4, 1, 32, true>;
+using F64_3D_844_AMR = Cfg<double, 3, 8, 4, 4, 128, true, true>;
+using F64_3D_444_AMR = Cfg<double, 3, 4, 4, 4, 64, true, true>;
+using F64_2D_16_AMR = Cfg<double, 2, 16, 16, 1, 256, true, true>;
+using F64_2D_8_AMR = Cfg<double, 2, 8, 8, 1, 64, true, true>;
+using F64_2D_4_AMR = Cfg<double, 2, 4, 4, 1, 32, true, true>;
 
+template <bool AMR>
 int
-launch_step_fp64(const StepArgs & a, int dim, cudaStream_t stream)
+launch_step_fp64_cfg(const StepArgs & a, int dim, cudaStream_t stream)
 {
   if (dim == 3)
   {
     if (a.bx % 8 == 0 && a.by % 4 == 0 && a.bz % 4 == 0)
-      return launch_fused<F64_3D_844>(a, stream);
-    return launch_fused<F64_3D_444>(a, stream);
+      return launch_fused<std::conditional_t<AMR, F64_3D_844_AMR, F64_3D_844>>(a, stream);
+    return launch_fused<std::conditional_t<AMR, F64_3D_444_AMR, F64_3D_444>>(a, stream);
   }
   if (a.bx % 16 == 0 && a.by % 16 == 0)
-    return launch_fused<F64_2D_16>(a, stream);
+    return launch_fused<std::conditional_t<AMR, F64_2D_16_AMR, F64_2D_16>>(a, stream);
   if (a.bx % 8 == 0 && a.by % 8 == 0)
-    return launch_fused<F64_2D_8>(a, stream);
-  return launch_fused<F64_2D_4>(a, stream);
+    return launch_fused<std::conditional_t<AMR, F64_2D_8_AMR, F64_2D_8>>(a, stream);
+  return launch_fused<std::conditional_t<AMR, F64_2D_4_AMR, F64_2D_4>>(a, stream);
+}
+
+int
+launch_step_fp64(const StepArgs & a, int dim, cudaStream_t stream)
+{
+  return a.kind ? launch_step_fp64_cfg<true>(a, dim, stream) : launch_step_fp64_cfg<false>(a, dim, stream);
+}
+
+void
+tile_shape_fp64(int dim, int bx, int by, int bz, int * t)
+{
+  if (dim == 3)
+  {
+    const bool big = bx % 8 == 0 && by % 4 == 0 && bz % 4 == 0;
+    t[0] = big ? 8 : 4;
+    t[1] = 4;
+    t[2] = 4;
+    return;
+  }
+  const int n = (bx % 16 == 0 && by % 16 == 0) ? 16 : ((bx % 8 == 0 && by % 8 == 0) ? 8 : 4);
+  t[0] = t[1] = n;
+  t[2] = 1;
 }
 
 int
@@ -35,6 +65,11 @@ prepare_fp64()
   rc = rc ? rc : prepare_fused<F64_2D_16>();
   rc = rc ? rc : prepare_fused<F64_2D_8>();
   rc = rc ? rc : prepare_fused<F64_2D_4>();
+  rc = rc ? rc : prepare_fused<F64_3D_844_AMR>();
+  rc = rc ? rc : prepare_fused<F64_3D_444_AMR>();
+  rc = rc ? rc : prepare_fused<F64_2D_16_AMR>();
+  rc = rc ? rc : prepare_fused<F64_2D_8_AMR>();
+  rc = rc ? rc : prepare_fused<F64_2D_4_AMR>();
   return rc;
 }
 } // namespace gmhd

@@ -1,5 +1,7 @@
 // Mixed-precision instantiations of the fused step: FP32 slopes, predictor, Riemann solvers and
 // EMFs; FP64 conserved/face-B accumulation, CT curl and low-beta pressure recovery.
+#include <type_traits>
+
 #include "launch.cuh"
 
 namespace gmhd
@@ -9,21 +11,47 @@ using MX_3D_444 = Cfg<float, 3, 4, 4, 4, 64, false>;
 using MX_2D_16 = Cfg<float, 2, 16, 16, 1, 256, false>;
 using MX_2D_8 = Cfg<float, 2, 8, 8, 1, 64, false>;
 using MX_2D_4 = Cfg<float, 2, 4, 4, 1, 32, false>;
+using MX_3D_888_AMR = Cfg<float, 3, 8, 8, 8, 512, false, true>;
+using MX_3D_444_AMR = Cfg<float, 3, 4, 4, 4, 64, false, true>;
+using MX_2D_16_AMR = Cfg<float, 2, 16, 16, 1, 256, false, true>;
+using MX_2D_8_AMR = Cfg<float, 2, 8, 8, 1, 64, false, true>;
+using MX_2D_4_AMR = Cfg<float, 2, 4, 4, 1, 32, false, true>;
 
+template <bool AMR>
 int
-launch_step_mixed(const StepArgs & a, int dim, cudaStream_t stream)
+launch_step_mixed_cfg(const StepArgs & a, int dim, cudaStream_t stream)
 {
   if (dim == 3)
   {
     if (a.bx % 8 == 0 && a.by % 8 == 0 && a.bz % 8 == 0)
-      return launch_fused<MX_3D_888>(a, stream);
-    return launch_fused<MX_3D_444>(a, stream);
+      return launch_fused<std::conditional_t<AMR, MX_3D_888_AMR, MX_3D_888>>(a, stream);
+    return launch_fused<std::conditional_t<AMR, MX_3D_444_AMR, MX_3D_444>>(a, stream);
   }
   if (a.bx % 16 == 0 && a.by % 16 == 0)
-    return launch_fused<MX_2D_16>(a, stream);
+    return launch_fused<std::conditional_t<AMR, MX_2D_16_AMR, MX_2D_16>>(a, stream);
   if (a.bx % 8 == 0 && a.by % 8 == 0)
-    return launch_fused<MX_2D_8>(a, stream);
-  return launch_fused<MX_2D_4>(a, stream);
+    return launch_fused<std::conditional_t<AMR, MX_2D_8_AMR, MX_2D_8>>(a, stream);
+  return launch_fused<std::conditional_t<AMR, MX_2D_4_AMR, MX_2D_4>>(a, stream);
+}
+
+int
+launch_step_mixed(const StepArgs & a, int dim, cudaStream_t stream)
+{
+  return a.kind ? launch_step_mixed_cfg<true>(a, dim, stream) : launch_step_mixed_cfg<false>(a, dim, stream);
+}
+
+void
+tile_shape_mixed(int dim, int bx, int by, int bz, int * t)
+{
+  if (dim == 3)
+  {
+    const int n = (bx % 8 == 0 && by % 8 == 0 && bz % 8 == 0) ? 8 : 4;
+    t[0] = t[1] = t[2] = n;
+    return;
+  }
+  const int n = (bx % 16 == 0 && by % 16 == 0) ? 16 : ((bx % 8 == 0 && by % 8 == 0) ? 8 : 4);
+  t[0] = t[1] = n;
+  t[2] = 1;
 }
 
 int
@@ -35,6 +63,11 @@ prepare_mixed()
   rc = rc ? rc : prepare_fused<MX_2D_16>();
   rc = rc ? rc : prepare_fused<MX_2D_8>();
   rc = rc ? rc : prepare_fused<MX_2D_4>();
+  rc = rc ? rc : prepare_fused<MX_3D_888_AMR>();
+  rc = rc ? rc : prepare_fused<MX_3D_444_AMR>();
+  rc = rc ? rc : prepare_fused<MX_2D_16_AMR>();
+  rc = rc ? rc : prepare_fused<MX_2D_8_AMR>();
+  rc = rc ? rc : prepare_fused<MX_2D_4_AMR>();
   return rc;
 }
 } // namespace gmhd

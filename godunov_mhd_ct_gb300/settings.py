@@ -22,6 +22,7 @@ class MHDSettings:
     small_beta: float = 1e-3
     scaling_factor: float = 1.0
     implementation_version: int = 0
+    prolongation: str = "SIMPLE_COPY"  # [amr] cell_centered_prolongation_type
 
     @property
     def smallp(self) -> float:
@@ -60,4 +61,5 @@ class MHDSettings:
             small_beta=get("mhd", "small_beta", 1e-3, float),
             scaling_factor=get("mesh", "scaling_factor", 1.0, float),
             implementation_version=get("hydro", "implementation_version", 0, int),
+            prolongation=get("amr", "cell_centered_prolongation_type", "SIMPLE_COPY", str),
         )

@@ -55,9 +55,12 @@ class GodunovImplemGB300:
             raise ValueError("only implementation_version=0 exists in the reference")
         self.settings = settings
         self.precision = precision
+        prol = settings.prolongation.upper()
+        if prol not in nat.PROLONGATION:
+            raise ValueError(f"unsupported [amr] cell_centered_prolongation_type {settings.prolongation!r}")
         p = nat.GmhdParams(settings.gamma0, settings.cfl, settings.slope_type, settings.smallr, settings.smallc,
                            settings.scaling_factor if mesh is None else mesh.scaling_factor,
-                           settings.riemann_id, nat.PRECISION[precision])
+                           settings.riemann_id, nat.PRECISION[precision], nat.PROLONGATION[prol])
         self._lib = nat.lib()
         self._ctx = self._lib.gmhd_create(ctypes.byref(p))
         if not self._ctx:

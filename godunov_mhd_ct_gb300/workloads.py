@@ -38,21 +38,34 @@ def uniform01(seed: int, ids: np.ndarray) -> np.ndarray:
 
 
 def _faces_from_az(mesh: BlockMesh, B: np.ndarray, az, x0=0.0, y0=0.0):
-    """Face B = curl(A_z e_z) on the faces of every block; az(x, y) evaluated at edges."""
+    """Face B = curl(A_z e_z) on the faces of every block; az(x, y) evaluated at edges. Edge
+    positions are wrapped on periodic axes, so the two copies of a face shared across a periodic
+    border hold the same value (the shared-face agreement SolverGodunovMHD.cpp:506-513 checks)."""
     bx, by, bz = mesh.block
-    dx = mesh.block_dx()[:, None, None, None]  # per block (AMR meshes mix levels)
+    dxb = mesh.block_dx()
+    dx = dxb[:, None, None, None]  # per block (AMR meshes mix levels)
     Bx, By, Bz = mesh.split_faces(B)
     c = mesh.coords
+    # cells per axis across the domain at each block's level
+    n_x = np.rint(mesh.domain_length(0) / dxb).astype(np.int64)[:, None, None, None]
+    n_y = np.rint(mesh.domain_length(1) / dxb).astype(np.int64)[:, None, None, None]
+
+    def wx(g):
+        return (np.mod(g, n_x) if mesh.periodic[0] else g).astype(np.float64)
+
+    def wy(g):
+        return (np.mod(g, n_y) if mesh.periodic[1] else g).astype(np.float64)
+
     # x faces: Bx(i, j) = (Az(x_i, y_{j+1}) - Az(x_i, y_j)) / dy
     k, j, i = np.meshgrid(np.arange(bz), np.arange(by), np.arange(bx + 1), indexing="ij")
-    gi = (c[:, 0, None, None, None] * bx + i[None]).astype(np.float64)
-    gj = (c[:, 1, None, None, None] * by + j[None]).astype(np.float64)
-    Bx[...] = (az(x0 + gi * dx, y0 + (gj + 1) * dx) - az(x0 + gi * dx, y0 + gj * dx)) / dx
+    gi = c[:, 0, None, None, None] * bx + i[None]
+    gj = c[:, 1, None, None, None] * by + j[None]
+    Bx[...] = (az(x0 + wx(gi) * dx, y0 + wy(gj + 1) * dx) - az(x0 + wx(gi) * dx, y0 + wy(gj) * dx)) / dx
     # y faces: By(i, j) = -(Az(x_{i+1}, y_j) - Az(x_i, y_j)) / dx
     k, j, i = np.meshgrid(np.arange(bz), np.arange(by + 1), np.arange(bx), indexing="ij")
-    gi = (c[:, 0, None, None, None] * bx + i[None]).astype(np.float64)
-    gj = (c[:, 1, None, None, None] * by + j[None]).astype(np.float64)
-    By[...] = -(az(x0 + (gi + 1) * dx, y0 + gj * dx) - az(x0 + gi * dx, y0 + gj * dx)) / dx
+    gi = c[:, 0, None, None, None] * bx + i[None]
+    gj = c[:, 1, None, None, None] * by + j[None]
+    By[...] = -(az(x0 + wx(gi + 1) * dx, y0 + wy(gj) * dx) - az(x0 + wx(gi) * dx, y0 + wy(gj) * dx)) / dx
     Bz[...] = 0.0
 
 
@@ -203,15 +216,18 @@ def kelvin_helmholtz(mesh: BlockMesh, gamma=1.4, p0=2.5, bx0=0.1, width=0.01, no
     n = mesh.n_owned
     gi, gj, gk = mesh.global_cell_index()
     gi, gj, gk = gi[:n], gj[:n], gk[:n]
-    dx = mesh.cell_length()
+    dx = mesh.block_dx()[:n, None, None, None]
     x = (gi + 0.5) * dx
     y = (gj + 0.5) * dx
     s = 0.5 * (1.0 + np.tanh((0.25 - np.abs(y - 0.5)) / width))
     rho = 1.0 + s
     vx = -0.5 + s
+    # noise id: the cell's lower corner on the finest level's grid (unique across levels)
+    top = int(mesh.level[:n].max())
+    sh = (top - mesh.level[:n]).astype(np.int64)[:, None, None, None]
     gx = mesh.grid[0] * mesh.block[0]
     gy = mesh.grid[1] * mesh.block[1]
-    ids = gi + gx * (gj + gy * gk)
+    ids = (gi << sh) + gx * ((gj << sh) + gy * (gk << sh))
     vy = 0.01 * np.sin(4.0 * math.pi * x) + noise * gaussian01(seed, ids)
     vz = np.zeros_like(x)
     _fill_energy(mesh, U, B, rho, np.full(x.shape, p0), vx, vy, vz, gamma)

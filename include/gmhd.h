@@ -62,6 +62,13 @@ enum gmhd_bc
   GMHD_BC_WALL = 3
 };
 
+enum gmhd_prolongation
+{ /* [amr] cell_centered_prolongation_type: hydro ghosts taken from a coarser neighbour
+   * (scheme/ConvertToPrimitivesVariablesFunctor.cpp:699-718) */
+  GMHD_PROLONG_SIMPLE_COPY = 0,
+  GMHD_PROLONG_LINEAR_MINMOD = 1 /* EXTRAPOLATE_LINEAR_MINMOD */
+};
+
 /* Health flags reported by gmhd_last_status. */
 enum gmhd_health_flags
 {
@@ -85,12 +92,23 @@ typedef struct gmhd_params
   double  scaling_factor;
   int32_t riemann;   /* enum gmhd_riemann */
   int32_t precision; /* enum gmhd_precision */
+  int32_t prolongation; /* [amr] cell_centered_prolongation_type: enum gmhd_prolongation */
 } gmhd_params;
 
 /* Leaf-block mesh (HOST pointers; copied by gmhd_set_mesh). Blocks [0, n_owned) are updated;
  * blocks [n_owned, n_blocks) are outside blocks filled by gmhd_fill_outside.
  * neighbor[b*27 + (oz+1)*9 + (oy+1)*3 + (ox+1)] is the block across face/edge/corner (ox,oy,oz)
- * of block b, or -1. cell size of block b = scaling_factor / (bx * 2^level[b]). */
+ * of block b, or -1. cell size of block b = scaling_factor / (bx * 2^level[b]).
+ *
+ * Coarse/fine meshes (2:1 balanced across faces, edges and corners, as p4est's full balance;
+ * the reference's AMR, scheme/ConvertToPrimitivesVariablesFunctor.cpp:699-718,
+ * scheme/ReadFluxesAndConservativeUpdateFunctor.cpp:141-172,
+ * scheme/CorrectEmfAtBlockBorderFunctor.cpp:94-360): the block-sized region next to b in
+ * direction (ox,oy,oz) at b's level is either a leaf at that level (neighbor = it), part of a leaf
+ * one level coarser (neighbor = that leaf; coord gives the position inside it), or split into
+ * leaves one level finer (neighbor = -1 and fine_neighbor[(b*27 + slot)*8 + cx + 2cy + 4cz] = the
+ * children, -1 where absent). Outside blocks are at the level of the block they serve, with a
+ * same-level inside block across the border. Bx, by, bz must be even. */
 typedef struct gmhd_mesh
 {
   int32_t         dim;   /* 2 or 3 */
@@ -105,6 +123,10 @@ typedef struct gmhd_mesh
   const int32_t * outside_normal; /* [3 * (n_blocks - n_owned)] per axis: +1 below the domain,
                                      -1 above it, 0 inside its range (points into the domain) */
   int32_t         bc[6];          /* enum gmhd_bc for XMIN, XMAX, YMIN, YMAX, ZMIN, ZMAX */
+  const int32_t * coord;          /* [3 * n_blocks] block coordinates at the block's level, or NULL
+                                     (needed when a neighbour is coarser; orchard-key position) */
+  const int32_t * fine_neighbor;  /* [27 * 8 * n_blocks] children of refined neighbour regions, or
+                                     NULL on meshes without finer neighbours */
 } gmhd_mesh;
 
 typedef struct gmhd_ctx gmhd_ctx;

@@ -24,12 +24,14 @@
 // leaf at L (same), part of a leaf at L-1 (coarser), split into 2^d leaves at L+1 (finer), or an
 // outside block at L (non-periodic borders).
 //   * face-B ghost layer (core FillBlockGhostFacesFunctor): faces with normal index 0..b and
-//     transverse cells inside the block are the block's own; a same-level or outside region copies
+//     transverse cells inside the block are the block's own, except that a face shared with a finer
+//     region takes that region's value (below); a same-level or outside region copies
 //     the neighbour's face; a finer region takes the mean of the 2^(d-1) fine faces covering the face
 //     (sum with the first transverse axis fastest, then divide); a coarser region takes the coarse
 //     face containing the face when the face lies on a coarse face, else the mean of the two coarse
 //     faces bounding the coarse cell along the normal. 2D Bz is cell-centred: mean of the 4 fine
-//     cells (x fastest) / the coarse cell value;
+//     cells (x fastest) / the coarse cell value. A face on the border between two regions along its
+//     normal is taken from the finer one, so that all blocks see one value for every face;
 //   * cell-centred hydro ghosts follow ConvertToPrimitivesVariablesFunctor.cpp:217-283, 471-719:
 //     same level copies U and takes B_cc from the ghost faces (equal to the neighbour's faces when
 //     shared faces agree); finer takes the mean of the 2^d fine cells (core compute_siblings_average:
@@ -346,9 +348,9 @@ region_face(const Mesh & m, const Fields & f, const Region & r, int comp, const 
 
 // Value of face component comp at (i, j, k) of block blk's ghosted face space (2D comp 2: the
 // cell-centred Bz), following the face-B ghost definition at the top of this file. A face lying on
-// the border between two neighbour regions along its normal is taken from the finer of the two (the
-// first when they are at the same level), so every block sees the same value for it. Returns false
-// when the neighbour region is missing.
+// the border between two regions along its normal (the block itself included) is taken from the
+// finer of the two (the first when they are at the same level), so every block sees the same value
+// for it. Returns false when the neighbour region is missing.
 static bool
 ghost_face(const Mesh & m, const Fields & f, int blk, int comp, int i, int j, int k, double & out)
 {
@@ -360,7 +362,7 @@ ghost_face(const Mesh & m, const Fields & f, int blk, int comp, int i, int j, in
     o[d] = (d == comp && !cellc) ? (idx[d] < 0 ? -1 : (idx[d] > b[d] ? 1 : 0)) : region_axis(idx[d], b[d]);
   Region r = region_of(m, blk, o[0], o[1], o[2]);
   int    q[3] = {idx[0] - o[0] * b[0], idx[1] - o[1] * b[1], idx[2] - o[2] * b[2]};
-  if (!cellc && (o[0] != 0 || o[1] != 0 || o[2] != 0) && (idx[comp] == 0 || idx[comp] == b[comp]))
+  if (!cellc && (idx[comp] == 0 || idx[comp] == b[comp]))
   {
     int o1[3] = {o[0], o[1], o[2]};
     o1[comp] = idx[comp] == 0 ? -1 : 1;

@@ -62,3 +62,26 @@ def shared_face_mismatch(mesh: BlockMesh, B):
         ok = right_z >= 0
         worst = max(worst, float(np.max(np.abs(Bz[:n][ok, -1] - Bz[right_z[ok], 0]), initial=0.0)))
     return worst
+
+
+def same_level_face_mismatch(mesh: BlockMesh, B):
+    """Max |difference| between the two copies of faces shared by same-level neighbours (AMR meshes
+    included; coarse/fine borders are skipped)."""
+    from godunov_mhd_ct_gb300.mesh import nb_slot
+
+    faces = mesh.split_faces(np.asarray(B))
+    n = mesh.n_owned
+    worst = 0.0
+    for d in range(mesh.dim):
+        o = [0, 0, 0]
+        o[d] = 1
+        right = mesh.neighbor[:n, nb_slot(*o)]
+        ok = (right >= 0) & (right < n)
+        ok[ok] &= mesh.level[right[ok]] == mesh.level[:n][ok]
+        if not ok.any():
+            continue
+        F = faces[d]
+        a = np.take(F[:n][ok], -1, axis=3 - d)
+        b = np.take(F[right[ok]], 0, axis=3 - d)
+        worst = max(worst, float(np.max(np.abs(a - b))))
+    return worst

@@ -16,6 +16,8 @@ import pytest
 from godunov_mhd_ct_gb300 import workloads as wl
 from godunov_mhd_ct_gb300.mesh import BlockMesh, nb_slot
 
+from .helpers import same_level_face_mismatch
+
 orc = pytest.importorskip("oracle.oracle")
 
 
@@ -124,6 +126,9 @@ def test_conservation_and_div_b(dim, prolongation):
     assert abs(t1[1] - t0[1]) <= 1e-13 * abs(t0[1])
     assert div_b(m, B2) < 1e-11
     assert coarse_fine_face_gap(m, B2) < 1e-14
+    # every block sees one value per face, so same-level copies of shared faces stay identical
+    assert same_level_face_mismatch(m, B) == 0.0
+    assert same_level_face_mismatch(m, B2) == 0.0
 
 
 def test_prolongation_types_differ():
