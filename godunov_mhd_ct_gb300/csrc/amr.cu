@@ -226,154 +226,178 @@ minmod_slope(double u, double ur, double ul)
   return dl > 0.0 ? fmin(dl, dr) : fmax(dl, dr);
 }
 
-// One thread per (virtual block, cell or face). Only items within two cells of the owner block
-// are filled; the fused step reads no others.
+// Cells (or faces, along their normal) of region o that lie within two cells of the block: the
+// only ones the fused step reads. o < 0: the last two (faces: b-2 .. b), o > 0: the first two (faces:
+// 0 .. 2), o == 0: all.
+__device__ static void
+near_range(int o, int n, bool normal, int & lo, int & len)
+{
+  if (o == 0)
+  {
+    lo = 0;
+    len = n + (normal ? 1 : 0);
+  }
+  else
+  {
+    lo = o < 0 ? n - 2 : 0;
+    len = normal ? 3 : 2;
+  }
+}
+
+// One CTA per virtual block (grid-stride), its threads over the cells and faces of the region's
+// near layer.
 __global__ void __launch_bounds__(256)
 ghost_prepass_kernel(const GhostArgs g)
 {
-  const int64_t per = g.ncell + g.nface;
-  const int64_t total = (int64_t)g.n_virtual * per;
-  const int     b[3] = {g.bx, g.by, g.bz};
-  for (int64_t it = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; it < total; it += (int64_t)gridDim.x * blockDim.x)
+  const int b[3] = {g.bx, g.by, g.bz};
+  for (int v = blockIdx.x; v < g.n_virtual; v += gridDim.x)
   {
-    const int     v = (int)(it / per);
-    const int64_t item = it - (int64_t)v * per;
     const int     blk = g.vmap[2 * v], slot = g.vmap[2 * v + 1];
     const int     o[3] = {slot % 3 - 1, (slot / 3) % 3 - 1, slot / 9 - 1};
     const DRegion r = region_of(g, blk, o[0], o[1], o[2]);
-    if (item < g.ncell)
+    // near boxes: cells, then faces of each component
+    int lo[4][3], len[4][3], cnt[4];
+    for (int c = 0; c < 4; ++c)
     {
-      const int q[3] = {(int)(item % g.bx), (int)((item / g.bx) % g.by), (int)(item / ((int64_t)g.bx * g.by))};
-      bool      near = true;
+      cnt[c] = 1;
+      for (int d = 0; d < 3; ++d)
+      {
+        if (d >= g.dim)
+        {
+          lo[c][d] = 0;
+          len[c][d] = 1;
+        }
+        else
+          near_range(o[d], b[d], c < 3 && c == d && !(g.dim == 2 && c == 2), lo[c][d], len[c][d]);
+        cnt[c] *= len[c][d];
+      }
+    }
+    // cnt[3] (cells) first, then faces x, y, z
+    const int total = cnt[3] + cnt[0] + cnt[1] + cnt[2];
+    for (int it = threadIdx.x; it < total; it += blockDim.x)
+    {
+      if (it < cnt[3])
+      {
+        const int     q[3] = {lo[3][0] + it % len[3][0], lo[3][1] + (it / len[3][0]) % len[3][1],
+                              lo[3][2] + it / (len[3][0] * len[3][1])};
+        const int64_t item = q[0] + (int64_t)g.bx * (q[1] + (int64_t)g.by * q[2]);
+        double        u[5] = {0, 0, 0, 0, 0}, bc[3] = {0, 0, 0};
+        bool   ok = true;
+        switch (r.kind)
+        {
+          case RK_SAME:
+          case RK_OUTSIDE:
+            for (int n = 0; n < 5; ++n)
+              u[n] = u_at(g, r.id, n, q[0], q[1], q[2]);
+            break;
+          case RK_FINER:
+            for (int n = 0; n < 5 && ok; ++n)
+              ok = restrict_cell(g, r, q, n, u[n]);
+            break;
+          case RK_COARSER:
+          {
+            const int I[3] = {(r.sub[0] * b[0] + q[0]) >> 1, (r.sub[1] * b[1] + q[1]) >> 1, (r.sub[2] * b[2] + q[2]) >> 1};
+            if (g.prolongation == 0)
+            {
+              for (int n = 0; n < 5; ++n)
+                u[n] = u_at(g, r.id, n, I[0], I[1], I[2]);
+              bc[0] = 0.5 * (face_at(g, r.id, 0, I[0], I[1], I[2]) + face_at(g, r.id, 0, I[0] + 1, I[1], I[2]));
+              bc[1] = 0.5 * (face_at(g, r.id, 1, I[0], I[1], I[2]) + face_at(g, r.id, 1, I[0], I[1] + 1, I[2]));
+              bc[2] = g.dim == 3
+                        ? 0.5 * (face_at(g, r.id, 2, I[0], I[1], I[2]) + face_at(g, r.id, 2, I[0], I[1], I[2] + 1))
+                        : 0.5 * (face_at(g, r.id, 2, I[0], I[1], 0) + face_at(g, r.id, 2, I[0], I[1], 0));
+            }
+            else
+            {
+              const int sgn[3] = {2 * (q[0] & 1) - 1, 2 * (q[1] & 1) - 1, 2 * (q[2] & 1) - 1};
+              for (int n = 0; n < 5 && ok; ++n)
+              {
+                const double uc = u_at(g, r.id, n, I[0], I[1], I[2]);
+                double       sl[3] = {0, 0, 0};
+                for (int d = 0; d < g.dim && ok; ++d)
+                {
+                  int    ip[3] = {I[0], I[1], I[2]}, im[3] = {I[0], I[1], I[2]};
+                  double ur = 0.0, ul = 0.0;
+                  ip[d] += 1;
+                  im[d] -= 1;
+                  ok = level_cell_value(g, r.id, n, ip[0], ip[1], ip[2], ur) &&
+                       level_cell_value(g, r.id, n, im[0], im[1], im[2], ul);
+                  sl[d] = minmod_slope(uc, ur, ul);
+                }
+                double val = uc + 0.25 * (double)sgn[0] * sl[0] + 0.25 * (double)sgn[1] * sl[1];
+                if (g.dim == 3)
+                  val = val + 0.25 * (double)sgn[2] * sl[2];
+                u[n] = val;
+              }
+            }
+            break;
+          }
+          default:
+            ok = false;
+        }
+        if (!ok)
+        {
+          atomicOr(g.health, (unsigned)HEALTH_MISSING_NEIGHBOR);
+          continue;
+        }
+        for (int n = 0; n < 5; ++n)
+          g.Uv[((int64_t)v * 5 + n) * g.ncell + item] = u[n];
+        for (int n = 0; n < 3; ++n)
+          g.Bccv[((int64_t)v * 3 + n) * g.ncell + item] = bc[n];
+        continue;
+      }
+      int comp = 0, f = it - cnt[3];
+      while (f >= cnt[comp])
+        f -= cnt[comp++];
+      int q[3] = {lo[comp][0] + f % len[comp][0], lo[comp][1] + (f / len[comp][0]) % len[comp][1],
+                  lo[comp][2] + f / (len[comp][0] * len[comp][1])};
+      int64_t fi;
+      if (comp == 0)
+        fi = q[0] + (int64_t)(g.bx + 1) * (q[1] + (int64_t)g.by * q[2]);
+      else if (comp == 1)
+        fi = g.nfx + q[0] + (int64_t)g.bx * (q[1] + (int64_t)(g.by + 1) * q[2]);
+      else
+        fi = g.nfx + g.nfy + q[0] + (int64_t)g.bx * (q[1] + (int64_t)g.by * q[2]);
+      const bool cellc = g.dim == 2 && comp == 2;
+      // block-frame index and the region the block's gather assigns this face to
+      int  idx[3] = {0, 0, 0};
+      bool mine = true;
       for (int d = 0; d < g.dim; ++d)
       {
-        const int x = o[d] * b[d] + q[d];
-        near = near && x >= -2 && x < b[d] + 2;
+        idx[d] = o[d] * b[d] + q[d];
+        const bool normal = d == comp && !cellc;
+        if (idx[d] < -2 || idx[d] > (normal ? b[d] + 2 : b[d] + 1))
+          mine = false;
+        const int od = normal ? (idx[d] < 0 ? -1 : (idx[d] > b[d] ? 1 : 0)) : axis_off(idx[d], b[d]);
+        if (od != o[d])
+          mine = false;
       }
-      if (!near)
+      // the block's own border face shared with a finer face neighbour is read from here too
+      if (!mine && !cellc && r.kind == RK_FINER && o[comp] != 0 &&
+          (o[0] != 0) + (o[1] != 0) + (o[2] != 0) == 1 && q[comp] == (o[comp] < 0 ? b[comp] : 0))
+        mine = true;
+      if (!mine)
         continue;
-      double u[5] = {0, 0, 0, 0, 0}, bc[3] = {0, 0, 0};
-      bool   ok = true;
-      switch (r.kind)
+      DRegion rf = r;
+      if (!cellc && (idx[comp] == 0 || idx[comp] == b[comp]))
       {
-        case RK_SAME:
-        case RK_OUTSIDE:
-          for (int n = 0; n < 5; ++n)
-            u[n] = u_at(g, r.id, n, q[0], q[1], q[2]);
-          break;
-        case RK_FINER:
-          for (int n = 0; n < 5 && ok; ++n)
-            ok = restrict_cell(g, r, q, n, u[n]);
-          break;
-        case RK_COARSER:
+        int o1[3] = {o[0], o[1], o[2]};
+        o1[comp] = idx[comp] == 0 ? -1 : 1;
+        const DRegion r1 = region_of(g, blk, o1[0], o1[1], o1[2]);
+        if (region_level(r1) > region_level(rf))
         {
-          const int I[3] = {(r.sub[0] * b[0] + q[0]) >> 1, (r.sub[1] * b[1] + q[1]) >> 1, (r.sub[2] * b[2] + q[2]) >> 1};
-          if (g.prolongation == 0)
-          {
-            for (int n = 0; n < 5; ++n)
-              u[n] = u_at(g, r.id, n, I[0], I[1], I[2]);
-            bc[0] = 0.5 * (face_at(g, r.id, 0, I[0], I[1], I[2]) + face_at(g, r.id, 0, I[0] + 1, I[1], I[2]));
-            bc[1] = 0.5 * (face_at(g, r.id, 1, I[0], I[1], I[2]) + face_at(g, r.id, 1, I[0], I[1] + 1, I[2]));
-            bc[2] = g.dim == 3
-                      ? 0.5 * (face_at(g, r.id, 2, I[0], I[1], I[2]) + face_at(g, r.id, 2, I[0], I[1], I[2] + 1))
-                      : 0.5 * (face_at(g, r.id, 2, I[0], I[1], 0) + face_at(g, r.id, 2, I[0], I[1], 0));
-          }
-          else
-          {
-            const int sgn[3] = {2 * (q[0] & 1) - 1, 2 * (q[1] & 1) - 1, 2 * (q[2] & 1) - 1};
-            for (int n = 0; n < 5 && ok; ++n)
-            {
-              const double uc = u_at(g, r.id, n, I[0], I[1], I[2]);
-              double       sl[3] = {0, 0, 0};
-              for (int d = 0; d < g.dim && ok; ++d)
-              {
-                int    ip[3] = {I[0], I[1], I[2]}, im[3] = {I[0], I[1], I[2]};
-                double ur = 0.0, ul = 0.0;
-                ip[d] += 1;
-                im[d] -= 1;
-                ok = level_cell_value(g, r.id, n, ip[0], ip[1], ip[2], ur) &&
-                     level_cell_value(g, r.id, n, im[0], im[1], im[2], ul);
-                sl[d] = minmod_slope(uc, ur, ul);
-              }
-              double val = uc + 0.25 * (double)sgn[0] * sl[0] + 0.25 * (double)sgn[1] * sl[1];
-              if (g.dim == 3)
-                val = val + 0.25 * (double)sgn[2] * sl[2];
-              u[n] = val;
-            }
-          }
-          break;
+          rf = r1;
+          q[comp] = idx[comp] == 0 ? b[comp] : 0;
         }
-        default:
-          ok = false;
       }
-      if (!ok)
+      double val = 0.0;
+      if (!region_face(g, rf, comp, q, val))
       {
         atomicOr(g.health, (unsigned)HEALTH_MISSING_NEIGHBOR);
         continue;
       }
-      for (int n = 0; n < 5; ++n)
-        g.Uv[((int64_t)v * 5 + n) * g.ncell + item] = u[n];
-      for (int n = 0; n < 3; ++n)
-        g.Bccv[((int64_t)v * 3 + n) * g.ncell + item] = bc[n];
-      continue;
+      g.Bv[(int64_t)v * g.nface + fi] = val;
     }
-    // faces
-    const int64_t f = item - g.ncell;
-    int           comp, nx, ny;
-    int64_t       rr;
-    if (f < g.nfx)
-    {
-      comp = 0; rr = f; nx = g.bx + 1; ny = g.by;
-    }
-    else if (f < g.nfx + g.nfy)
-    {
-      comp = 1; rr = f - g.nfx; nx = g.bx; ny = g.by + 1;
-    }
-    else
-    {
-      comp = 2; rr = f - g.nfx - g.nfy; nx = g.bx; ny = g.by;
-    }
-    int        q[3] = {(int)(rr % nx), (int)((rr / nx) % ny), (int)(rr / ((int64_t)nx * ny))};
-    const bool cellc = g.dim == 2 && comp == 2;
-    // block-frame index and the region the block's gather assigns this face to
-    int  idx[3] = {0, 0, 0};
-    bool mine = true;
-    for (int d = 0; d < g.dim; ++d)
-    {
-      idx[d] = o[d] * b[d] + q[d];
-      const bool normal = d == comp && !cellc;
-      const int  lo = -2, hi = normal ? b[d] + 2 : b[d] + 1;
-      if (idx[d] < lo || idx[d] > hi)
-        mine = false;
-      const int od = normal ? (idx[d] < 0 ? -1 : (idx[d] > b[d] ? 1 : 0)) : axis_off(idx[d], b[d]);
-      if (od != o[d])
-        mine = false;
-    }
-    // the block's own border face shared with a finer face neighbour is read from here too
-    if (!mine && !cellc && r.kind == RK_FINER && o[comp] != 0 &&
-        (o[0] != 0) + (o[1] != 0) + (o[2] != 0) == 1 && q[comp] == (o[comp] < 0 ? b[comp] : 0))
-      mine = true;
-    if (!mine)
-      continue;
-    DRegion rf = r;
-    if (!cellc && (idx[comp] == 0 || idx[comp] == b[comp]))
-    {
-      int o1[3] = {o[0], o[1], o[2]};
-      o1[comp] = idx[comp] == 0 ? -1 : 1;
-      const DRegion r1 = region_of(g, blk, o1[0], o1[1], o1[2]);
-      if (region_level(r1) > region_level(rf))
-      {
-        rf = r1;
-        q[comp] = idx[comp] == 0 ? b[comp] : 0;
-      }
-    }
-    double val = 0.0;
-    if (!region_face(g, rf, comp, q, val))
-    {
-      atomicOr(g.health, (unsigned)HEALTH_MISSING_NEIGHBOR);
-      continue;
-    }
-    g.Bv[(int64_t)v * g.nface + f] = val;
   }
 }
 
@@ -382,9 +406,7 @@ launch_ghost_prepass(const GhostArgs & g, cudaStream_t stream)
 {
   if (g.n_virtual <= 0)
     return 0;
-  const int64_t total = (int64_t)g.n_virtual * (g.ncell + g.nface);
-  const int64_t want = (total + 255) / 256;
-  const int     grid = (int)(want < 152 * 16 ? want : 152 * 16);
+  const int grid = g.n_virtual < 152 * 32 ? g.n_virtual : 152 * 32;
   ghost_prepass_kernel<<<grid, 256, 0, stream>>>(g);
   return (int)cudaGetLastError();
 }

@@ -1,7 +1,9 @@
-"""Run W warm-up steps and one measured do_time_step of the fused kernel on a 3D Orszag-Tang
-mesh, for profiling a single launch (e.g. under ncu -k regex:fused_step -s W -c 1).
+"""Run W warm-up steps and measured do_time_steps of the fused step on a uniform 3D Orszag-Tang
+mesh or an AMR workload, for timing and for profiling single launches (e.g. under
+ncu -k regex:fused_step -s W -c 1).
 
     python -m godunov_mhd_ct_gb300.profile_step --precision mixed --side-blocks 4 --block 32
+    python -m godunov_mhd_ct_gb300.profile_step --workload blast --levels 5:9 --block 16
 """
 from __future__ import annotations
 
@@ -15,6 +17,9 @@ def main():
     ap.add_argument("--side-blocks", type=int, default=4)
     ap.add_argument("--block", type=int, default=32)
     ap.add_argument("--dim", type=int, default=3, choices=[2, 3])
+    ap.add_argument("--workload", default="ot", choices=["ot", "blast", "kh"],
+                    help="ot: uniform Orszag-Tang; blast: 2D AMR blast; kh: 3D AMR shear layers with walls")
+    ap.add_argument("--levels", default="5:8", help="base:max level of the AMR workloads")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--repeat", type=int, default=1)
     args = ap.parse_args()
@@ -27,14 +32,29 @@ def main():
     from .settings import MHDSettings
     from .solver import GodunovImplemGB300
 
-    level = int(np.log2(args.side_blocks))
-    blk = (args.block, args.block, args.block if args.dim == 3 else 1)
-    mesh = BlockMesh.uniform(args.dim, level=level, block=blk)
     st = MHDSettings(gamma0=5.0 / 3.0, cfl=0.5, slope_type=2.0, riemann="HLLD")
-    U, B = wl.orszag_tang(mesh, gamma=st.gamma0, rho_perturbation=1e-3, seed=12345)
-    impl = GodunovImplemGB300(st, mesh, precision=args.precision)
+    bc = None
+    if args.workload == "ot":
+        level = int(np.log2(args.side_blocks))
+        blk = (args.block, args.block, args.block if args.dim == 3 else 1)
+        mesh = BlockMesh.uniform(args.dim, level=level, block=blk)
+        U, B = wl.orszag_tang(mesh, gamma=st.gamma0, rho_perturbation=1e-3, seed=12345)
+    else:
+        lo, hi = (int(v) for v in args.levels.split(":"))
+        if args.workload == "blast":
+            mesh = wl.blast_mesh(lo, hi, block=args.block)
+            U, B = wl.blast(mesh, gamma=st.gamma0)
+        else:
+            st = MHDSettings(gamma0=1.4, cfl=0.5, slope_type=2.0, riemann="HLLD")
+            mesh = wl.kh_amr_mesh(lo, hi, block=args.block)
+            U, B = wl.kelvin_helmholtz(mesh, gamma=st.gamma0, seed=12345)
+            bc = (1, 1, 3, 3, 1, 1)
+        print(f"{args.workload}: {mesh.n_owned} leaves, levels {np.bincount(mesh.level[: mesh.n_owned])[lo:]}")
+    impl = GodunovImplemGB300(st, mesh, precision=args.precision, bc=bc)
     dU, dB = torch.from_numpy(U).cuda(), torch.from_numpy(B).cuda()
     dU2, dB2 = torch.empty_like(dU), torch.empty_like(dB)
+    if bc is not None:
+        impl.fill_outside(dU, dB)
     dt = impl.compute_dt(dU, dB)
     for _ in range(args.warmup):
         impl.do_time_step(dU, dU2, dB, dB2, dt)
@@ -46,7 +66,7 @@ def main():
     el = (time.perf_counter() - t0) / args.repeat
     cells = mesh.n_owned * mesh.ncell
     flags = impl.last_status()
-    print(f"{args.precision} {args.dim}D {cells} cells: {el * 1e3:.3f} ms/step, {cells / el / 1e9:.3f} Gcell/s, "
+    print(f"{args.precision} {mesh.dim}D {cells} cells: {el * 1e3:.3f} ms/step, {cells / el / 1e9:.3f} Gcell/s, "
           f"health flags {flags}")
 
 

@@ -257,3 +257,59 @@ def field_loop_batch(n_problems: int, seed: int = 0, sizes=(32, 64, 128, 256), b
         states.append((U, B))
         params.append({"N": n, "radius": radius, "speed": speed, "angle": angle})
     return meshes, states, params
+
+
+# ---- coarse/fine (AMR) workloads -------------------------------------------------------------
+def refine_band(center, r_lo, r_hi, axes=2):
+    """Refinement predicate for BlockMesh.amr: leaves whose box meets the shell r_lo <= |x - c| <= r_hi
+    (distance over the first `axes` coordinates, unit-brick coordinates)."""
+    c = np.asarray(center, dtype=np.float64)
+
+    def f(level, lo, hi):
+        p = np.clip(c, lo, hi)
+        near = float(np.sqrt(((p - c)[:axes] ** 2).sum()))
+        far = float(np.sqrt((np.maximum(np.abs(lo - c), np.abs(hi - c))[:axes] ** 2).sum()))
+        return near <= r_hi and far >= r_lo
+
+    return f
+
+
+def blast_mesh(base_level: int = 5, max_level: int = 9, block: int = 16, radius: float = 0.1,
+               band: float = 0.02) -> BlockMesh:
+    """2D magnetised blast mesh on [-0.5, 0.5]^2 (periodic): leaves within `band` of the initial
+    front r = radius refined to max_level, 2:1 balanced (the shape of app/test_mhd_blast_2d.ini with
+    levels 5-10; the mesh is static here)."""
+    return BlockMesh.amr(2, refine_band((0.5, 0.5, 0.5), radius - band, radius + band), base_level=base_level,
+                         max_level=max_level, block=(block, block, 1))
+
+
+def blast(mesh: BlockMesh, gamma=5.0 / 3.0, radius=0.1, p_in=10.0, p_out=0.1, x0=-0.5, y0=-0.5):
+    """rho = 1, p = p_in for r < radius else p_out, v = 0, B = (1/sqrt 2, 1/sqrt 2, 0)
+    (init/InitBlast, MHD variant with a uniform oblique field)."""
+    U, B = mesh.alloc_state()
+    Bx, By, Bz = mesh.split_faces(B)
+    b0 = 1.0 / math.sqrt(2.0)
+    Bx[...] = b0
+    By[...] = b0
+    Bz[...] = 0.0
+    n = mesh.n_owned
+    gi, gj, _ = mesh.global_cell_index()
+    dx = mesh.block_dx()[:n, None, None, None]
+    x = x0 + (gi[:n] + 0.5) * dx
+    y = y0 + (gj[:n] + 0.5) * dx
+    r = np.sqrt(x * x + y * y)
+    p = np.where(r < radius, p_in, p_out)
+    z = np.zeros_like(x)
+    _fill_energy(mesh, U, B, np.ones_like(x), p, z, z, z, gamma)
+    return U, B
+
+
+def kh_amr_mesh(base_level: int = 5, max_level: int = 7, block: int = 16, band: float = 0.02) -> BlockMesh:
+    """3D shear-layer mesh on [0,1]^3, periodic in x and z, reflecting in y: leaves within `band` of
+    the layers |y - 0.5| = 0.25 refined to max_level (the shape of the 3D Kelvin-Helmholtz
+    configuration with levels 6-9; the mesh is static here)."""
+    def refine(level, lo, hi):
+        return any(lo[1] - band <= yl <= hi[1] + band for yl in (0.25, 0.75))
+
+    return BlockMesh.amr(3, refine, base_level=base_level, max_level=max_level, block=(block, block, block),
+                         periodic=(True, False, True))

@@ -143,3 +143,20 @@ def test_amr_walls_fp64_bit_exact(oracle_lib):
     assert np.array_equal(dtg[:, 0], dto)
     assert np.array_equal(dU.cpu().numpy()[:n], Uo[:n])
     assert np.array_equal(dB.cpu().numpy()[:n], Bo[:n])
+
+
+def test_amr_blast_fp64_bit_exact(oracle_lib):
+    """Magnetised blast (strong pressure jump on the refined front), solver loop, bit for bit."""
+    mesh = wl.blast_mesh(base_level=2, max_level=4, block=8, radius=0.15, band=0.05)
+    st = settings(gamma0=5.0 / 3.0, cfl=0.5)
+    U, B = wl.blast(mesh, gamma=st.gamma0, radius=0.15)
+    nsteps = 8
+    om = oracle_lib.Mesh.from_block_mesh(mesh)
+    Uo, Bo, dto = oracle_lib.run(om, oracle_settings(oracle_lib, st), U, B, nsteps)
+    impl = GodunovImplemGB300(st, mesh, precision="fp64")
+    dU, dB = _dev(U), _dev(B)
+    dtg, _ = impl.advance(dU, torch.empty_like(dU), dB, torch.empty_like(dB), nsteps)
+    n = mesh.n_owned
+    assert np.array_equal(dtg[:, 0], dto)
+    assert np.array_equal(dU.cpu().numpy()[:n], Uo[:n])
+    assert np.array_equal(dB.cpu().numpy()[:n], Bo[:n])
