@@ -66,6 +66,7 @@ def lib():
     L.gmhd_fill_outside.argtypes = [vp, vp, vp, vp]
     L.gmhd_advance.argtypes = [vp, vp, vp, vp, vp, ctypes.c_int32, dp, dp, dp, ctypes.c_int32, vp]
     L.gmhd_step_host.argtypes = [vp, vp, vp, vp, vp, ctypes.c_double, vp]
+    L.gmhd_step_host_async.argtypes = [vp, vp, vp, vp, vp, ctypes.c_double, vp]
     L.gmhd_last_status.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32)]
     L.gmhd_last_cuda_error.argtypes = [vp]
     L.gmhd_error_string.restype = ctypes.c_char_p
@@ -89,7 +90,7 @@ def exported_symbols():
     """Names declared in include/gmhd.h, for the ABI tests."""
     return ["gmhd_create", "gmhd_destroy", "gmhd_set_mesh", "gmhd_mem_bytes", "gmhd_step", "gmhd_inv_dt",
             "gmhd_fill_outside", "gmhd_advance", "gmhd_step_host", "gmhd_last_status", "gmhd_last_cuda_error",
-            "gmhd_error_string", "gmhd_layout_check", "gmhd_inv_dt_noalloc"]
+            "gmhd_error_string", "gmhd_layout_check", "gmhd_inv_dt_noalloc", "gmhd_step_host_async"]
 
 
 class MeshTables:

@@ -47,6 +47,12 @@ struct gmhd_ctx
   int64_t              dtlog_cap = 0;
   // host-variant staging
   double *d_U = nullptr, *d_U2 = nullptr, *d_B = nullptr, *d_B2 = nullptr;
+  // asynchronous host-variant pipeline: two staging sets, copy-in / step / copy-out streams
+  double *     a_U[2] = {nullptr, nullptr}, *a_U2[2] = {nullptr, nullptr};
+  double *     a_B[2] = {nullptr, nullptr}, *a_B2[2] = {nullptr, nullptr};
+  cudaStream_t a_in = nullptr, a_run = nullptr, a_out = nullptr;
+  cudaEvent_t  a_in_done[2] = {nullptr, nullptr}, a_run_done[2] = {nullptr, nullptr}, a_out_done[2] = {nullptr, nullptr};
+  int          a_next = 0;
   // own stream for graph capture when the caller passes the legacy stream
   cudaStream_t own_stream = nullptr;
   // cached graph of two steps
@@ -139,6 +145,14 @@ free_mesh(gmhd_ctx * c)
   c->d_dt = c->d_t = c->d_tend = c->d_dtlog = nullptr;
   c->d_counter = nullptr;
   c->d_U = c->d_U2 = c->d_B = c->d_B2 = nullptr;
+  for (int k = 0; k < 2; ++k)
+  {
+    dfree(c->a_U[k]);
+    dfree(c->a_U2[k]);
+    dfree(c->a_B[k]);
+    dfree(c->a_B2[k]);
+    c->a_U[k] = c->a_U2[k] = c->a_B[k] = c->a_B2[k] = nullptr;
+  }
   for (void * p : {(void *)c->d_kind, (void *)c->d_fine, (void *)c->d_coord, (void *)c->d_vmap, (void *)c->d_nbr_real,
                    (void *)c->d_list1, (void *)c->d_list2, (void *)c->d_flux_slot, (void *)c->d_emf_slot,
                    (void *)c->d_Uv, (void *)c->d_Bv, (void *)c->d_Bccv, (void *)c->d_flux_side, (void *)c->d_emf_side})
@@ -660,10 +674,23 @@ gmhd_destroy(gmhd_ctx * ctx)
 {
   if (!ctx)
     return;
+  if (ctx->a_in)
+    cudaStreamSynchronize(ctx->a_in);
+  if (ctx->a_run)
+    cudaStreamSynchronize(ctx->a_run);
+  if (ctx->a_out)
+    cudaStreamSynchronize(ctx->a_out);
   free_mesh(ctx);
   dfree(ctx->d_health);
   if (ctx->own_stream)
     cudaStreamDestroy(ctx->own_stream);
+  for (cudaStream_t st : {ctx->a_in, ctx->a_run, ctx->a_out})
+    if (st)
+      cudaStreamDestroy(st);
+  for (int k = 0; k < 2; ++k)
+    for (cudaEvent_t ev : {ctx->a_in_done[k], ctx->a_run_done[k], ctx->a_out_done[k]})
+      if (ev)
+        cudaEventDestroy(ev);
   delete ctx;
 }
 
@@ -998,6 +1025,64 @@ gmhd_step_host(gmhd_ctx * ctx, const double * U, double * U2, const double * B, 
   GMHD_CUDA(cudaMemcpyAsync(U2, ctx->d_U2, nu_own * sizeof(double), cudaMemcpyDeviceToHost, s));
   GMHD_CUDA(cudaMemcpyAsync(B2, ctx->d_B2, nb_own * sizeof(double), cudaMemcpyDeviceToHost, s));
   GMHD_CUDA(cudaStreamSynchronize(s));
+  return GMHD_OK;
+}
+
+int
+gmhd_step_host_async(gmhd_ctx * ctx, const double * U, double * U2, const double * B, double * B2, double dt,
+                     void * stream)
+{
+  if (!ctx || !U || !U2 || !B || !B2)
+    return GMHD_ERR_ARGUMENT;
+  if (!ctx->has_mesh)
+    return GMHD_ERR_MESH;
+  if (!(dt >= 0.0))
+    return GMHD_ERR_ARGUMENT;
+  const size_t nu = (size_t)ctx->n_blocks * 5 * ctx->ncell;
+  const size_t nb = (size_t)ctx->n_blocks * ctx->nface;
+  int          rc;
+  if (!ctx->a_in)
+  {
+    GMHD_CUDA(cudaStreamCreateWithFlags(&ctx->a_in, cudaStreamNonBlocking));
+    GMHD_CUDA(cudaStreamCreateWithFlags(&ctx->a_run, cudaStreamNonBlocking));
+    GMHD_CUDA(cudaStreamCreateWithFlags(&ctx->a_out, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k)
+    {
+      GMHD_CUDA(cudaEventCreateWithFlags(&ctx->a_in_done[k], cudaEventDisableTiming));
+      GMHD_CUDA(cudaEventCreateWithFlags(&ctx->a_run_done[k], cudaEventDisableTiming));
+      GMHD_CUDA(cudaEventCreateWithFlags(&ctx->a_out_done[k], cudaEventDisableTiming));
+    }
+  }
+  const int k = ctx->a_next;
+  if (!ctx->a_U[k])
+  {
+    if ((rc = dalloc(ctx, &ctx->a_U[k], nu)) || (rc = dalloc(ctx, &ctx->a_U2[k], nu)) ||
+        (rc = dalloc(ctx, &ctx->a_B[k], nb)) || (rc = dalloc(ctx, &ctx->a_B2[k], nb)))
+      return rc;
+  }
+  cudaStream_t caller = (cudaStream_t)stream;
+  // copy in (U, B are complete in host memory when the call is made), after the staging set's last
+  // copy-out
+  GMHD_CUDA(cudaStreamWaitEvent(ctx->a_in, ctx->a_out_done[k], 0));
+  GMHD_CUDA(cudaMemcpyAsync(ctx->a_U[k], U, nu * sizeof(double), cudaMemcpyHostToDevice, ctx->a_in));
+  GMHD_CUDA(cudaMemcpyAsync(ctx->a_B[k], B, nb * sizeof(double), cudaMemcpyHostToDevice, ctx->a_in));
+  GMHD_CUDA(cudaEventRecord(ctx->a_in_done[k], ctx->a_in));
+  // the step
+  GMHD_CUDA(cudaStreamWaitEvent(ctx->a_run, ctx->a_in_done[k], 0));
+  gmhd::StepArgs a = make_args(ctx, ctx->a_U[k], ctx->a_U2[k], ctx->a_B[k], ctx->a_B2[k]);
+  a.dt = dt;
+  if ((rc = launch_step(ctx, a, ctx->a_run)))
+    return rc;
+  GMHD_CUDA(cudaEventRecord(ctx->a_run_done[k], ctx->a_run));
+  // copy out the owned blocks, then order the caller's stream after it
+  GMHD_CUDA(cudaStreamWaitEvent(ctx->a_out, ctx->a_run_done[k], 0));
+  GMHD_CUDA(cudaMemcpyAsync(U2, ctx->a_U2[k], (size_t)ctx->n_owned * 5 * ctx->ncell * sizeof(double),
+                            cudaMemcpyDeviceToHost, ctx->a_out));
+  GMHD_CUDA(cudaMemcpyAsync(B2, ctx->a_B2[k], (size_t)ctx->n_owned * ctx->nface * sizeof(double),
+                            cudaMemcpyDeviceToHost, ctx->a_out));
+  GMHD_CUDA(cudaEventRecord(ctx->a_out_done[k], ctx->a_out));
+  GMHD_CUDA(cudaStreamWaitEvent(caller, ctx->a_out_done[k], 0));
+  ctx->a_next = 1 - k;
   return GMHD_OK;
 }
 

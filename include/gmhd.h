@@ -196,6 +196,18 @@ int gmhd_inv_dt_noalloc(const gmhd_params * params, int32_t dim, int32_t bx, int
 int gmhd_step_host(gmhd_ctx * ctx, const double * U, double * U2, const double * B, double * B2, double dt,
                    void * stream);
 
+/* Stream-ordered gmhd_step_host (no counterpart in the reference; it exists for callers that keep the
+ * state in host memory): copies U, B in, runs the step and copies the owned blocks of U2, B2 out, then
+ * returns without waiting; the results are in U2/B2 once `stream` has completed the work enqueued
+ * before this call returns (synchronise `stream`). Consecutive calls overlap: the host->device copy of
+ * one call, the step of the previous call and the device->host copy of the one before run at the same
+ * time (two device staging sets and three streams owned by ctx). U and B are read as they are in host
+ * memory when the call is made (the copy-in does not wait for work on `stream`: synchronise `stream`
+ * first when they are the results of an earlier call). Until the call completes, U and B must stay
+ * unchanged and U2, B2 must not be read. Host buffers should be page-locked for the copies to overlap. */
+int gmhd_step_host_async(gmhd_ctx * ctx, const double * U, double * U2, const double * B, double * B2, double dt,
+                         void * stream);
+
 /* --- diagnostics ---------------------------------------------------------------------------- */
 
 /* Health flags accumulated since the last call (clears them). Synchronises the context stream. */
