@@ -16,6 +16,7 @@ STATUS = {0: "ok", -1: "invalid argument", -2: "mesh not set or not supported", 
 
 PRECISION = {"fp64": 0, "mixed": 1}
 PROLONGATION = {"SIMPLE_COPY": 0, "EXTRAPOLATE_LINEAR_MINMOD": 1}
+TIME_INTEGRATOR = {"HANCOCK": 0, "RK2_SSP": 1}
 RIEMANN = {"LLF": 2, "HLL": 3, "HLLC": 4, "HLLD": 5}
 BC = {"NONE": 0, "PERIODIC": 1, "ZERO_GRADIENT": 2, "WALL": 3}
 HEALTH = {1: "missing neighbour", 2: "level jump", 4: "density <= 0", 8: "non-finite value",
@@ -25,7 +26,8 @@ HEALTH = {1: "missing neighbour", 2: "level jump", 4: "density <= 0", 8: "non-fi
 class GmhdParams(ctypes.Structure):
     _fields_ = [("gamma0", ctypes.c_double), ("cfl", ctypes.c_double), ("slope_type", ctypes.c_double),
                 ("smallr", ctypes.c_double), ("smallc", ctypes.c_double), ("scaling_factor", ctypes.c_double),
-                ("riemann", ctypes.c_int32), ("precision", ctypes.c_int32), ("prolongation", ctypes.c_int32)]
+                ("riemann", ctypes.c_int32), ("precision", ctypes.c_int32), ("prolongation", ctypes.c_int32),
+                ("time_integrator", ctypes.c_int32)]
 
 
 _ip = ctypes.POINTER(ctypes.c_int32)

@@ -37,6 +37,7 @@ struct StepArgs
   int64_t ncell, nfx, nfy, nface;
   double  gamma0, smallr, smallc, smallp, slope_type, scaling_factor, cfl;
   int     riemann;
+  int     rk2;                                  // [amr] time_integrator RK2_SSP: no Hancock half step
   double  dt;                                   // used when dt_dev is null
   const double *             dt_dev;            // per problem dt on the device, or null
   unsigned long long *       invdt_out;         // per problem: fused CFL of U2/B2 (max), or null
@@ -198,6 +199,7 @@ struct TileView
   Phys<R>     ph;
   R           dtdx;
   int         x0, y0, z0, bx, by, bz, n_owned;
+  int         rk2;
   // coarse/fine meshes (s_kind null otherwise)
   const int *     s_kind;
   int             blk, pass;
@@ -448,8 +450,11 @@ recon_edge(const TileView<C> & t, int sc, int fb0, int fb1, typename C::R * q)
   const R * F1 = t.fb[D1];
   R         B0 = F0[f0];
   R         B1 = F1[f1];
-  B0 += t.sf[D0 * NS + sc + (sh0 ? s_stride<C>(D0) : 0)];
-  B1 += t.sf[D1 * NS + sc + (sh1 ? s_stride<C>(D1) : 0)];
+  if (!t.rk2) // the half-step face source only with HANCOCK (ComputeEmfAndStoreFunctor.cpp:189-193, 297-301)
+  {
+    B0 += t.sf[D0 * NS + sc + (sh0 ? s_stride<C>(D0) : 0)];
+    B1 += t.sf[D1 * NS + sc + (sh1 ? s_stride<C>(D1) : 0)];
+  }
   const R   dB0d1 = slope1<R>(F0[f0], F0[f0 + f_stride<C>(D0, D1)], F0[f0 - f_stride<C>(D0, D1)], t.ph.slope_type);
   const R   dB1d0 = slope1<R>(F1[f1], F1[f1 + f_stride<C>(D1, D0)], F1[f1 - f_stride<C>(D1, D0)], t.ph.slope_type);
   const R * S0 = t.sl + D0 * 8 * NS + sc;
@@ -1058,6 +1063,19 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
     const R r = qh[0 * C::NQ + q0], p = qh[1 * C::NQ + q0], u = qh[2 * C::NQ + q0],
             v = qh[3 * C::NQ + q0], w = qh[4 * C::NQ + q0];
     const R A = (AL + AR) * R(0.5), B = (BL + BR) * R(0.5), Cc = (CL + CR) * R(0.5);
+    if (a.rk2)
+    {
+      // RK2_SSP: Q2 = Q (ComputeUpdatedPrimitiveVariablesFunctor.cpp:396-407, 531-542)
+      q2[ID * C::NS + n] = r;
+      q2[IU * C::NS + n] = u;
+      q2[IV * C::NS + n] = v;
+      q2[IW * C::NS + n] = w;
+      q2[IP * C::NS + n] = p;
+      q2[IA * C::NS + n] = A;
+      q2[IB * C::NS + n] = B;
+      q2[IC * C::NS + n] = Cc;
+      continue;
+    }
     const R gamma = ph.gamma0;
     const R dtdy = dtdx, dtdz = dtdx;
     const R drx = dq[0][ID], dpx = dq[0][IP], dux = dq[0][IU], dvx = dq[0][IV], dwx = dq[0][IW],
@@ -1195,6 +1213,7 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
     tv.by = by;
     tv.bz = bz;
     tv.n_owned = a.n_owned;
+    tv.rk2 = a.rk2;
     if constexpr (C::AMR)
     {
       tv.s_kind = s_kind;

@@ -47,6 +47,8 @@ struct gmhd_ctx
   int64_t              dtlog_cap = 0;
   // host-variant staging
   double *d_U = nullptr, *d_U2 = nullptr, *d_B = nullptr, *d_B2 = nullptr;
+  // RK2_SSP stage buffers of gmhd_advance
+  double *d_Urk = nullptr, *d_Brk = nullptr;
   // asynchronous host-variant pipeline: two staging sets, copy-in / step / copy-out streams
   double *     a_U[2] = {nullptr, nullptr}, *a_U2[2] = {nullptr, nullptr};
   double *     a_B[2] = {nullptr, nullptr}, *a_B2[2] = {nullptr, nullptr};
@@ -145,6 +147,9 @@ free_mesh(gmhd_ctx * c)
   c->d_dt = c->d_t = c->d_tend = c->d_dtlog = nullptr;
   c->d_counter = nullptr;
   c->d_U = c->d_U2 = c->d_B = c->d_B2 = nullptr;
+  dfree(c->d_Urk);
+  dfree(c->d_Brk);
+  c->d_Urk = c->d_Brk = nullptr;
   for (int k = 0; k < 2; ++k)
   {
     dfree(c->a_U[k]);
@@ -200,6 +205,7 @@ make_args(const gmhd_ctx * c, const double * U, double * U2, const double * B, d
   a.scaling_factor = c->p.scaling_factor;
   a.cfl = c->p.cfl;
   a.riemann = c->p.riemann;
+  a.rk2 = c->p.time_integrator == GMHD_TIME_RK2_SSP;
   a.health = c->d_health;
   a.n_blocks = c->n_blocks;
   return a;
@@ -458,11 +464,64 @@ enqueue_inv_dt(gmhd_ctx * ctx, const double * U, const double * B, unsigned long
   return GMHD_OK;
 }
 
+// LinearCombination (core; SolverGodunovMHD.cpp:617-621): out = c0 * a + c1 * out over the owned blocks
+__global__ void
+lincomb_kernel(const double * __restrict__ a, double * __restrict__ out, int64_t n, double c0, double c1)
+{
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = c0 * a[i] + c1 * out[i];
+}
+
+int
+enqueue_lincomb(gmhd_ctx * ctx, const double * a, double * out, int64_t n, double c0, double c1, cudaStream_t s)
+{
+  if (n <= 0)
+    return GMHD_OK;
+  const int64_t want = (n + 255) / 256;
+  lincomb_kernel<<<(int)(want < 152 * 64 ? want : 152 * 64), 256, 0, s>>>(a, out, n, c0, c1);
+  GMHD_CUDA(cudaGetLastError());
+  return GMHD_OK;
+}
+
+// one RK2_SSP iteration of gmhd_advance (SolverGodunovMHD.cpp:551-647): U_RK = U + L(U);
+// U2 = U_RK + L(U_RK); U2 = 1/2 U + 1/2 U2; CFL of U2 for the next iteration. The stage-1 combination
+// (coefficients 0 and 1) leaves U_RK unchanged and is not launched.
+int
+enqueue_iteration_rk2(gmhd_ctx * ctx, const double * Uc, double * Un, const double * Bc, double * Bn, int slot_in,
+                      cudaStream_t s, bool has_tend)
+{
+  const int np = ctx->n_problems;
+  advance_time_kernel<<<1, 256, 0, s>>>(ctx->d_invdt + (size_t)slot_in * np, ctx->p.cfl, ctx->d_t,
+                                        has_tend ? ctx->d_tend : nullptr, ctx->d_dt, ctx->d_dtlog, ctx->d_counter,
+                                        np, ctx->dtlog_cap);
+  GMHD_CUDA(cudaGetLastError());
+  int rc = enqueue_fill(ctx, const_cast<double *>(Uc), const_cast<double *>(Bc), s);
+  if (rc)
+    return rc;
+  gmhd::StepArgs a = make_args(ctx, Uc, ctx->d_Urk, Bc, ctx->d_Brk);
+  a.dt_dev = ctx->d_dt;
+  if ((rc = launch_step(ctx, a, s)))
+    return rc;
+  if ((rc = enqueue_fill(ctx, ctx->d_Urk, ctx->d_Brk, s)))
+    return rc;
+  a = make_args(ctx, ctx->d_Urk, Un, ctx->d_Brk, Bn);
+  a.dt_dev = ctx->d_dt;
+  if ((rc = launch_step(ctx, a, s)))
+    return rc;
+  if ((rc = enqueue_lincomb(ctx, Uc, Un, (int64_t)ctx->n_owned * 5 * ctx->ncell, 0.5, 0.5, s)) ||
+      (rc = enqueue_lincomb(ctx, Bc, Bn, (int64_t)ctx->n_owned * ctx->nface, 0.5, 0.5, s)))
+    return rc;
+  return enqueue_inv_dt(ctx, Un, Bn, ctx->d_invdt + (size_t)(1 - slot_in) * np, s,
+                        ctx->p.precision != GMHD_PRECISION_MIXED);
+}
+
 // one solver iteration of gmhd_advance: time control, outside fill, fused step + CFL
 int
 enqueue_iteration(gmhd_ctx * ctx, const double * Uc, double * Un, const double * Bc, double * Bn, int slot_in,
                   cudaStream_t s, bool has_tend)
 {
+  if (ctx->p.time_integrator == GMHD_TIME_RK2_SSP)
+    return enqueue_iteration_rk2(ctx, Uc, Un, Bc, Bn, slot_in, s, has_tend);
   const int np = ctx->n_problems;
   advance_time_kernel<<<1, 256, 0, s>>>(ctx->d_invdt + (size_t)slot_in * np, ctx->p.cfl, ctx->d_t,
                                         has_tend ? ctx->d_tend : nullptr, ctx->d_dt, ctx->d_dtlog, ctx->d_counter,
@@ -643,6 +702,10 @@ gmhd_create(const gmhd_params * params)
   if (params->riemann < GMHD_RIEMANN_LLF || params->riemann > GMHD_RIEMANN_HLLD)
     return nullptr;
   if (params->precision != GMHD_PRECISION_FP64 && params->precision != GMHD_PRECISION_MIXED)
+    return nullptr;
+  if (params->prolongation != GMHD_PROLONG_SIMPLE_COPY && params->prolongation != GMHD_PROLONG_LINEAR_MINMOD)
+    return nullptr;
+  if (params->time_integrator != GMHD_TIME_HANCOCK && params->time_integrator != GMHD_TIME_RK2_SSP)
     return nullptr;
   gmhd_ctx * c = new (std::nothrow) gmhd_ctx();
   if (!c)
@@ -923,6 +986,12 @@ gmhd_advance(gmhd_ctx * ctx, double * U, double * U2, double * B, double * B2, i
       cudaGraphExecDestroy(ctx->graph_exec);
       ctx->graph_exec = nullptr;
     }
+  }
+  if (ctx->p.time_integrator == GMHD_TIME_RK2_SSP && !ctx->d_Urk)
+  {
+    if ((rc = dalloc(ctx, &ctx->d_Urk, (size_t)ctx->n_blocks * 5 * ctx->ncell)) ||
+        (rc = dalloc(ctx, &ctx->d_Brk, (size_t)ctx->n_blocks * ctx->nface)))
+      return rc;
   }
   std::vector<double> zeros(np, 0.0);
   GMHD_CUDA(cudaMemcpyAsync(ctx->d_t, t ? t : zeros.data(), sizeof(double) * np, cudaMemcpyHostToDevice, s));

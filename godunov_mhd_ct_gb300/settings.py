@@ -23,6 +23,7 @@ class MHDSettings:
     scaling_factor: float = 1.0
     implementation_version: int = 0
     prolongation: str = "SIMPLE_COPY"  # [amr] cell_centered_prolongation_type
+    time_integrator: str = "HANCOCK"  # [amr] time_integrator (HANCOCK or RK2_SSP)
 
     @property
     def smallp(self) -> float:
@@ -62,4 +63,5 @@ class MHDSettings:
             scaling_factor=get("mesh", "scaling_factor", 1.0, float),
             implementation_version=get("hydro", "implementation_version", 0, int),
             prolongation=get("amr", "cell_centered_prolongation_type", "SIMPLE_COPY", str),
+            time_integrator=get("amr", "time_integrator", "HANCOCK", str),
         )

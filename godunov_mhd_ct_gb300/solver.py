@@ -58,9 +58,14 @@ class GodunovImplemGB300:
         prol = settings.prolongation.upper()
         if prol not in nat.PROLONGATION:
             raise ValueError(f"unsupported [amr] cell_centered_prolongation_type {settings.prolongation!r}")
+        integ = settings.time_integrator.upper()
+        if integ not in nat.TIME_INTEGRATOR:
+            # RK3_SSP aborts in the reference (SolverGodunovMHD.cpp:174-177)
+            raise ValueError(f"unsupported [amr] time_integrator {settings.time_integrator!r}")
         p = nat.GmhdParams(settings.gamma0, settings.cfl, settings.slope_type, settings.smallr, settings.smallc,
                            settings.scaling_factor if mesh is None else mesh.scaling_factor,
-                           settings.riemann_id, nat.PRECISION[precision], nat.PROLONGATION[prol])
+                           settings.riemann_id, nat.PRECISION[precision], nat.PROLONGATION[prol],
+                           nat.TIME_INTEGRATOR[integ])
         self._lib = nat.lib()
         self._ctx = self._lib.gmhd_create(ctypes.byref(p))
         if not self._ctx:

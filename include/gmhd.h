@@ -69,6 +69,12 @@ enum gmhd_prolongation
   GMHD_PROLONG_LINEAR_MINMOD = 1 /* EXTRAPOLATE_LINEAR_MINMOD */
 };
 
+enum gmhd_time_integrator
+{ /* [amr] time_integrator (SolverGodunovMHD.cpp:488-647) */
+  GMHD_TIME_HANCOCK = 0, /* MUSCL-Hancock: one stage with the half-step predictor */
+  GMHD_TIME_RK2_SSP = 1  /* two stages without the predictor, U = 1/2 U + 1/2 U2 (gmhd_advance) */
+};
+
 /* Health flags reported by gmhd_last_status. */
 enum gmhd_health_flags
 {
@@ -93,6 +99,7 @@ typedef struct gmhd_params
   int32_t riemann;   /* enum gmhd_riemann */
   int32_t precision; /* enum gmhd_precision */
   int32_t prolongation; /* [amr] cell_centered_prolongation_type: enum gmhd_prolongation */
+  int32_t time_integrator; /* [amr] time_integrator: enum gmhd_time_integrator */
 } gmhd_params;
 
 /* Leaf-block mesh (HOST pointers; copied by gmhd_set_mesh). Blocks [0, n_owned) are updated;

@@ -33,6 +33,7 @@ class OracleSettings(ctypes.Structure):
     _fields_ = [
         ("gamma0", ctypes.c_double), ("cfl", ctypes.c_double), ("slope_type", ctypes.c_double),
         ("smallr", ctypes.c_double), ("smallc", ctypes.c_double), ("riemann", ctypes.c_int32),
+        ("time_integrator", ctypes.c_int32),
     ]
 
 
@@ -85,8 +86,10 @@ def _dp(a: np.ndarray):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
-def settings(gamma0=1.4, cfl=0.5, slope_type=1.0, smallr=1e-10, smallc=1e-10, riemann=5) -> OracleSettings:
-    return OracleSettings(gamma0, cfl, slope_type, smallr, smallc, riemann)
+def settings(gamma0=1.4, cfl=0.5, slope_type=1.0, smallr=1e-10, smallc=1e-10, riemann=5,
+             time_integrator=0) -> OracleSettings:
+    """time_integrator: 0 HANCOCK, 1 RK2_SSP ([amr] time_integrator)."""
+    return OracleSettings(gamma0, cfl, slope_type, smallr, smallc, riemann, time_integrator)
 
 
 class Mesh:

@@ -50,6 +50,7 @@ struct Settings
   double smallpp; // smallr * smallp
   double cIso;    // always 0 in the reference (HydroSettings.cpp:27)
   int    riemann;
+  int    rk2 = 0; // [amr] time_integrator: 0 HANCOCK, 1 RK2_SSP
 };
 
 inline Settings

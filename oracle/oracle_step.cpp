@@ -683,6 +683,19 @@ compute_predictor(const Mesh & m, const Settings & s, double dtdx, StepWork & w)
           sB0 = (v * dAx + A * dvx - u * dBx - B * dux) * dtdx + (v * dCz + C * dvz - ww * dBz - B * dwz) * dtdz;
           sC0 = (ww * dAx + A * dwx - u * dCx - C * dux) * dtdx + (ww * dBy + B * dwy - v * dCy - C * dvy) * dtdy;
         }
+        if (s.rk2)
+        {
+          // RK2_SSP: no Hancock half step (ComputeUpdatedPrimitiveVariablesFunctor.cpp:396-407, 531-542)
+          w.Q2(i, j, k, ID) = r;
+          w.Q2(i, j, k, IU) = u;
+          w.Q2(i, j, k, IV) = v;
+          w.Q2(i, j, k, IW) = ww;
+          w.Q2(i, j, k, IP) = p;
+          w.Q2(i, j, k, IA) = A;
+          w.Q2(i, j, k, IB) = B;
+          w.Q2(i, j, k, IC) = C;
+          continue;
+        }
         w.Q2(i, j, k, ID) = r + 0.5 * sr0;
         w.Q2(i, j, k, IU) = u + 0.5 * su0;
         w.Q2(i, j, k, IV) = v + 0.5 * sv0;
@@ -987,8 +1000,11 @@ reconstruct_edge_2d(StepWork & w, const Settings & s, int is, int js, EdgeLoc lo
   }
   double A = w.Q(ia, ja, 0, IA);
   double B = w.Q(ib, jb, 0, IB);
-  A += w.SF(ia, ja, 0, 0);
-  B += w.SF(ib, jb, 0, 1);
+  if (!s.rk2) // the half-step face source only with HANCOCK (ComputeEmfAndStoreFunctor.cpp:189-193)
+  {
+    A += w.SF(ia, ja, 0, 0);
+    B += w.SF(ib, jb, 0, 1);
+  }
   const double dAy = face_slope(w, s, ia, ja, 0, IA, 1);
   const double dBx = face_slope(w, s, ib, jb, 0, IB, 0);
   const double fx = (double)sx, fy = (double)sy;
@@ -1022,8 +1038,11 @@ reconstruct_edge_3d(StepWork & w, const Settings & s, int is, int js, int ks, Ed
   }
   double B0 = w.Q(ijk0[0], ijk0[1], ijk0[2], IA + dir0);
   double B1 = w.Q(ijk1[0], ijk1[1], ijk1[2], IA + dir1);
-  B0 += w.SF(ijk0[0], ijk0[1], ijk0[2], dir0);
-  B1 += w.SF(ijk1[0], ijk1[1], ijk1[2], dir1);
+  if (!s.rk2) // the half-step face source only with HANCOCK (ComputeEmfAndStoreFunctor.cpp:297-301)
+  {
+    B0 += w.SF(ijk0[0], ijk0[1], ijk0[2], dir0);
+    B1 += w.SF(ijk1[0], ijk1[1], ijk1[2], dir1);
+  }
   const double dB0d1 = face_slope(w, s, ijk0[0], ijk0[1], ijk0[2], IA + dir0, dir1);
   const double dB1d0 = face_slope(w, s, ijk1[0], ijk1[1], ijk1[2], IA + dir1, dir0);
   Box &        S0 = slopes_dir(w, dir0);
@@ -1316,6 +1335,7 @@ struct oracle_settings
 {
   double  gamma0, cfl, slope_type, smallr, smallc;
   int32_t riemann;
+  int32_t time_integrator; // [amr] time_integrator: 0 HANCOCK, 1 RK2_SSP
 };
 
 static Mesh
@@ -1340,7 +1360,9 @@ to_mesh(const oracle_mesh * om)
 static Settings
 to_settings(const oracle_settings * os)
 {
-  return make_settings(os->gamma0, os->cfl, os->slope_type, os->smallr, os->smallc, os->riemann);
+  Settings st = make_settings(os->gamma0, os->cfl, os->slope_type, os->smallr, os->smallc, os->riemann);
+  st.rk2 = os->time_integrator == 1;
+  return st;
 }
 
 // One do_time_step: U2 and B2 must equal U and B on entry (SolverGodunovMHD.cpp:166-167, 545-548).
@@ -1600,6 +1622,29 @@ oracle_run_to(const oracle_mesh * om, const oracle_settings * os, double * U, do
     }
     if (dt_out)
       dt_out[n] = dt;
+    if (os->time_integrator == 1)
+    {
+      // RK2_SSP (SolverGodunovMHD.cpp:551-647): U_RK = U + L(U); U2 = U_RK + L(U_RK);
+      // U = 1/2 U + 1/2 U2. The stage-1 combination (core LinearCombination, coefficients 0 and 1)
+      // leaves U_RK unchanged.
+      std::vector<double> Urk(U, U + nu), Brk(B, B + nb);
+      int                 st = oracle_step(om, os, U, Urk.data(), B, Brk.data(), dt);
+      if (st != 0)
+        return st;
+      if (m.n_blocks > m.n_owned)
+        oracle_fill_outside(om, Urk.data(), Brk.data());
+      std::memcpy(U2.data(), Urk.data(), nu * sizeof(double));
+      std::memcpy(B2.data(), Brk.data(), nb * sizeof(double));
+      st = oracle_step(om, os, Urk.data(), U2.data(), Brk.data(), B2.data(), dt);
+      if (st != 0)
+        return st;
+      const size_t nuo = (size_t)m.n_owned * 5 * L.ncell, nbo = (size_t)m.n_owned * L.nface;
+      for (size_t i = 0; i < nuo; ++i)
+        U[i] = 0.5 * U[i] + 0.5 * U2[i];
+      for (size_t i = 0; i < nbo; ++i)
+        B[i] = 0.5 * B[i] + 0.5 * B2[i];
+      continue;
+    }
     const int st = oracle_step(om, os, U, U2.data(), B, B2.data(), dt);
     if (st != 0)
       return st;
