@@ -761,12 +761,17 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
   // ---- phase 1: gather face B at t^n (FillBlockGhostFaces equivalent) and the conservative state
   // of the Q region. Every global load of the phase is issued before any is consumed, so HBM latency
   // is paid once for the phase rather than once per loop trip.
+  // x faces one by one (rows of bx + 1 faces are not 16-byte aligned); y and z faces and the
+  // conservative state in 16-byte pairs of x-adjacent items: every tile starts at an even x and block
+  // sizes are even, so a pair never straddles two blocks and its address is 16-byte aligned.
   constexpr int ITX = (C::NFBX + NT - 1) / NT;
-  constexpr int ITY = (C::NFBY + NT - 1) / NT;
-  constexpr int ITZ = (C::NFBZ + NT - 1) / NT;
-  constexpr int ITQ = (C::NQ + NT - 1) / NT;
-  double        fvx[ITX], fvy[ITY], fvz[ITZ];
-  double        uq[ITQ][5];
+  constexpr int ITY = (C::NFBY / 2 + NT - 1) / NT;
+  constexpr int ITZ = (C::NFBZ / 2 + NT - 1) / NT;
+  constexpr int ITQ = (C::NQ / 2 + NT - 1) / NT;
+  static_assert(C::QX % 2 == 0, "pair loads need an even Q-region width");
+  double        fvx[ITX];
+  double2       fvy[ITY], fvz[ITZ];
+  double2       uq[ITQ][5];
 #pragma unroll
   for (int it = 0; it < ITX; ++it)
   {
@@ -789,8 +794,8 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
 #pragma unroll
   for (int it = 0; it < ITY; ++it)
   {
-    const int n = tid + it * NT;
-    fvy[it] = 0.0;
+    const int n = 2 * (tid + it * NT);
+    fvy[it] = make_double2(0.0, 0.0);
     if (n < C::NFBY)
     {
       const int i = n % C::QX - 2;
@@ -802,14 +807,15 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       int       fq = fj - oy * by;
       shared_face(1, fj, by, nb, fq);
       if (nb >= 0)
-        fvy[it] = bsrc(nb)[a.nfx + (ci - ox * bx) + (int64_t)bx * (fq + (int64_t)(by + 1) * (ck - oz * bz))];
+        fvy[it] = *reinterpret_cast<const double2 *>(
+          bsrc(nb) + a.nfx + (ci - ox * bx) + (int64_t)bx * (fq + (int64_t)(by + 1) * (ck - oz * bz)));
     }
   }
 #pragma unroll
   for (int it = 0; it < ITZ; ++it)
   {
-    const int n = tid + it * NT;
-    fvz[it] = 0.0;
+    const int n = 2 * (tid + it * NT);
+    fvz[it] = make_double2(0.0, 0.0);
     if (n < C::NFBZ)
     {
       const int i = n % C::QX - 2;
@@ -822,16 +828,16 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       if (D3)
         shared_face(2, fk, bz, nb, fq);
       if (nb >= 0)
-        fvz[it] = bsrc(nb)[a.nfx + a.nfy + (ci - ox * bx) + (int64_t)bx * ((cj - oy * by) + (int64_t)by * fq)];
+        fvz[it] = *reinterpret_cast<const double2 *>(
+          bsrc(nb) + a.nfx + a.nfy + (ci - ox * bx) + (int64_t)bx * ((cj - oy * by) + (int64_t)by * fq));
     }
   }
 #pragma unroll
   for (int it = 0; it < ITQ; ++it)
   {
-    const int n = tid + it * NT;
-    uq[it][0] = 1.0;
-    uq[it][1] = 1.0;
-    uq[it][2] = uq[it][3] = uq[it][4] = 0.0;
+    const int n = 2 * (tid + it * NT);
+    uq[it][0] = uq[it][1] = make_double2(1.0, 1.0);
+    uq[it][2] = uq[it][3] = uq[it][4] = make_double2(0.0, 0.0);
     if (n < C::NQ)
     {
       const int i = n % C::QX - 2;
@@ -845,7 +851,7 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
         const double * Ub = usrc(nb) + (ci - ox * bx) + (int64_t)bx * ((cj - oy * by) + (int64_t)by * (ck - oz * bz));
 #pragma unroll
         for (int v = 0; v < 5; ++v)
-          uq[it][v] = Ub[(int64_t)v * a.ncell];
+          uq[it][v] = *reinterpret_cast<const double2 *>(Ub + (int64_t)v * a.ncell);
       }
     }
   }
@@ -855,12 +861,24 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       fbx[tid + it * NT] = to_r<R>(fvx[it]);
 #pragma unroll
   for (int it = 0; it < ITY; ++it)
-    if (tid + it * NT < C::NFBY)
-      fby[tid + it * NT] = to_r<R>(fvy[it]);
+  {
+    const int n = 2 * (tid + it * NT);
+    if (n < C::NFBY)
+    {
+      fby[n] = to_r<R>(fvy[it].x);
+      fby[n + 1] = to_r<R>(fvy[it].y);
+    }
+  }
 #pragma unroll
   for (int it = 0; it < ITZ; ++it)
-    if (tid + it * NT < C::NFBZ)
-      fbz[tid + it * NT] = to_r<R>(fvz[it]);
+  {
+    const int n = 2 * (tid + it * NT);
+    if (n < C::NFBZ)
+    {
+      fbz[n] = to_r<R>(fvz[it].x);
+      fbz[n + 1] = to_r<R>(fvz[it].y);
+    }
+  }
   __syncthreads();
 
   // SIMPLE_COPY ghosts of a coarser neighbour take the coarse cell's own cell-centred B
@@ -881,18 +899,21 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
     return true;
   };
 
-  // primitive variables on the Q region (ConvertToPrimitivesVariablesFunctor)
+  // primitive variables on the Q region (ConvertToPrimitivesVariablesFunctor), two x-adjacent cells
+  // per thread and iteration
 #pragma unroll
-  for (int it = 0; it < ITQ; ++it)
+  for (int ie = 0; ie < 2 * ITQ; ++ie)
   {
-    const int n = tid + it * NT;
+    const int it = ie >> 1, e = ie & 1;
+    const int n = 2 * (tid + it * NT) + e;
     if (n >= C::NQ)
       continue;
     const int i = n % C::QX - 2;
     const int j = (n / C::QX) % C::QY - 2;
     const int k = D3 ? n / (C::QX * C::QY) - 2 : 0;
     const int ci = x0 + i, cj = y0 + j, ck = z0 + k;
-    const double * u = uq[it];
+    const double u[5] = {e ? uq[it][0].y : uq[it][0].x, e ? uq[it][1].y : uq[it][1].x, e ? uq[it][2].y : uq[it][2].x,
+                         e ? uq[it][3].y : uq[it][3].x, e ? uq[it][4].y : uq[it][4].x};
     const int qn = C::qi(i, j, k);
     if constexpr (C::EXACT)
     {

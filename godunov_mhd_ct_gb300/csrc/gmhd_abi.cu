@@ -288,6 +288,13 @@ launch_step(gmhd_ctx * ctx, const gmhd::StepArgs & a0, cudaStream_t s)
   return GMHD_OK;
 }
 
+// the fused step reads U and B in 16-byte pairs
+bool
+misaligned(const void * p)
+{
+  return ((uintptr_t)p & 15u) != 0;
+}
+
 bool
 overlaps(const void * a, size_t na, const void * b, size_t nb)
 {
@@ -905,7 +912,7 @@ gmhd_step(gmhd_ctx * ctx, const double * U, double * U2, const double * B, doubl
     return GMHD_ERR_ARGUMENT;
   if (!ctx->has_mesh)
     return GMHD_ERR_MESH;
-  if (!(dt >= 0.0))
+  if (!(dt >= 0.0) || misaligned(U) || misaligned(B))
     return GMHD_ERR_ARGUMENT;
   const size_t nu = sizeof(double) * (size_t)ctx->n_blocks * 5 * ctx->ncell;
   const size_t nb = sizeof(double) * (size_t)ctx->n_blocks * ctx->nface;
@@ -955,6 +962,8 @@ gmhd_advance(gmhd_ctx * ctx, double * U, double * U2, double * B, double * B2, i
              const double * t_end, double * dt_log, int32_t use_graph, void * stream)
 {
   if (!ctx || !U || !U2 || !B || !B2 || nsteps < 0)
+    return GMHD_ERR_ARGUMENT;
+  if (misaligned(U) || misaligned(U2) || misaligned(B) || misaligned(B2))
     return GMHD_ERR_ARGUMENT;
   if (!ctx->has_mesh)
     return GMHD_ERR_MESH;

@@ -158,7 +158,8 @@ uint64_t gmhd_mem_bytes(const gmhd_ctx * ctx);
 /* do_time_step (scheme/GodunovImplemBase.h:85-90, scheme/GodunovImplemV0.cpp:101-207).
  * Writes U2 = U + conservative update and B2 = B + CT update for the owned blocks. Unlike the
  * reference, U2/B2 need not equal U/B on entry (they are overwritten); they must not alias U/B.
- * Ghost/outside blocks of U and B must be filled (SolverGodunovMHD.cpp:497-498). */
+ * Ghost/outside blocks of U and B must be filled (SolverGodunovMHD.cpp:497-498). U and B must be
+ * 16-byte aligned (device allocations are); otherwise GMHD_ERR_ARGUMENT. */
 int gmhd_step(gmhd_ctx * ctx, const double * U, double * U2, const double * B, double * B2, double dt,
               void * stream);
 
