@@ -40,6 +40,15 @@ class GmhdMesh(ctypes.Structure):
                 ("bc", ctypes.c_int32 * 6), ("coord", _ip), ("fine_neighbor", _ip)]
 
 
+class GmhdRefineParams(ctypes.Structure):
+    _fields_ = [("criterion", ctypes.c_int32), ("level_min", ctypes.c_int32), ("level_max", ctypes.c_int32),
+                ("use_rho", ctypes.c_int32), ("use_pressure", ctypes.c_int32), ("eps_refine", ctypes.c_double),
+                ("eps_coarsen", ctypes.c_double), ("eps_lohner", ctypes.c_double)]
+
+
+REFINE_CRITERIA = {"SIMPLE_GRADIENT": 0, "LOHNER_UNSPLIT": 1}
+
+
 class NativeError(RuntimeError):
     pass
 
@@ -69,6 +78,8 @@ def lib():
     L.gmhd_advance.argtypes = [vp, vp, vp, vp, vp, ctypes.c_int32, dp, dp, dp, ctypes.c_int32, vp]
     L.gmhd_step_host.argtypes = [vp, vp, vp, vp, vp, ctypes.c_double, vp]
     L.gmhd_step_host_async.argtypes = [vp, vp, vp, vp, vp, ctypes.c_double, vp]
+    L.gmhd_refine_flags.argtypes = [vp, vp, vp, ctypes.POINTER(GmhdRefineParams), vp, vp]
+    L.gmhd_remap.argtypes = [ctypes.c_int32] * 6 + [vp] * 5 + [vp]
     L.gmhd_last_status.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32)]
     L.gmhd_last_cuda_error.argtypes = [vp]
     L.gmhd_error_string.restype = ctypes.c_char_p
@@ -92,7 +103,8 @@ def exported_symbols():
     """Names declared in include/gmhd.h, for the ABI tests."""
     return ["gmhd_create", "gmhd_destroy", "gmhd_set_mesh", "gmhd_mem_bytes", "gmhd_step", "gmhd_inv_dt",
             "gmhd_fill_outside", "gmhd_advance", "gmhd_step_host", "gmhd_last_status", "gmhd_last_cuda_error",
-            "gmhd_error_string", "gmhd_layout_check", "gmhd_inv_dt_noalloc", "gmhd_step_host_async"]
+            "gmhd_error_string", "gmhd_layout_check", "gmhd_inv_dt_noalloc", "gmhd_step_host_async",
+            "gmhd_refine_flags", "gmhd_remap"]
 
 
 class MeshTables:

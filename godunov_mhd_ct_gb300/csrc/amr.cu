@@ -412,3 +412,275 @@ launch_ghost_prepass(const GhostArgs & g, cudaStream_t stream)
 }
 
 } // namespace gmhd
+
+// ---- regrid: refinement indicator and remap ---------------------------------------------------
+// Definitions as in the CPU restatement (kalypsso-core's ComputeRefineFlags / UserDataRemapper are not
+// in the reference tree): indicator per cell and axis on rho and/or the pressure, neighbours clamped to
+// the block, SIMPLE_GRADIENT max(|q+ - q|, |q - q-|) / max(|q|, DBL_MIN) or LOHNER_UNSPLIT
+// |dp - dm| / (|dp| + |dm| + eps (|q+| + 2|q| + |q-|)); block error = max over cells.
+namespace gmhd
+{
+
+// quantity 0 (rho) or 1 (pressure) of every owned cell, into q[var][block][cell]
+__global__ void __launch_bounds__(256)
+refine_quantity_kernel(const double * __restrict__ U, const double * __restrict__ B, int n_owned, int dim, int bx,
+                       int by, int bz, int64_t ncell, int64_t nfx, int64_t nfy, int64_t nface, double gamma0,
+                       double smallr, double smallp, int use_rho, int use_pressure, double * __restrict__ q)
+{
+  const int64_t total = (int64_t)n_owned * ncell;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x)
+  {
+    const int64_t blk = g / ncell, c = g - blk * ncell;
+    const double *Ub = U + blk * 5 * ncell, *Bb = B + blk * nface;
+    if (use_rho)
+      q[g] = Ub[c];
+    if (use_pressure)
+    {
+      const int    i = (int)(c % bx), j = (int)((c / bx) % by), k = (int)(c / ((int64_t)bx * by));
+      const double Bxc = 0.5 * (Bb[i + (int64_t)(bx + 1) * (j + (int64_t)by * k)] + Bb[i + 1 + (int64_t)(bx + 1) * (j + (int64_t)by * k)]);
+      const double Byc = 0.5 * (Bb[nfx + i + (int64_t)bx * (j + (int64_t)(by + 1) * k)] +
+                                Bb[nfx + i + (int64_t)bx * (j + 1 + (int64_t)(by + 1) * k)]);
+      const double Bzc = dim == 3 ? 0.5 * (Bb[nfx + nfy + c] + Bb[nfx + nfy + c + (int64_t)bx * by])
+                                  : 0.5 * (Bb[nfx + nfy + c] + Bb[nfx + nfy + c]);
+      // compute_primitives (models/mhd_utils.h:449-515), cIso == 0
+      const double r = fmax(Ub[c], smallr);
+      const double vx = Ub[2 * ncell + c] / r, vy = Ub[3 * ncell + c] / r, vz = Ub[4 * ncell + c] / r;
+      const double eken = 0.5 * (vx * vx + vy * vy + vz * vz);
+      const double emag = 0.5 * (Bxc * Bxc + Byc * Byc + Bzc * Bzc);
+      const double eint = (Ub[ncell + c] - emag) / r - eken;
+      q[total * (use_rho ? 1 : 0) + g] = fmax((gamma0 - 1.0) * r * eint, r * smallp);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256)
+refine_flags_kernel(const double * __restrict__ q, int nvar, const int32_t * __restrict__ level, int n_owned, int dim,
+                    int bx, int by, int bz, int64_t ncell, int criterion, int level_min, int level_max,
+                    double eps_refine, double eps_coarsen, double eps_lohner, int8_t * __restrict__ flags)
+{
+  __shared__ double red[8];
+  const int blk = blockIdx.x;
+  const int b[3] = {bx, by, bz};
+  double    err = 0.0;
+  for (int var = 0; var < nvar; ++var)
+  {
+    const double * Q = q + ((int64_t)var * n_owned + blk) * ncell;
+    for (int64_t c = threadIdx.x; c < ncell; c += blockDim.x)
+    {
+      const int    idx[3] = {(int)(c % bx), (int)((c / bx) % by), (int)(c / ((int64_t)bx * by))};
+      const double v = Q[c];
+      for (int d = 0; d < dim; ++d)
+      {
+        const int64_t st = d == 0 ? 1 : (d == 1 ? bx : (int64_t)bx * by);
+        const double  qm = idx[d] > 0 ? Q[c - st] : v;
+        const double  qp = idx[d] < b[d] - 1 ? Q[c + st] : v;
+        double        e;
+        if (criterion == 0)
+          e = fmax(fabs(qp - v), fabs(v - qm)) / fmax(fabs(v), 2.2250738585072014e-308);
+        else
+        {
+          const double dp = qp - v, dm = v - qm;
+          const double den = fabs(dp) + fabs(dm) + eps_lohner * (fabs(qp) + 2.0 * fabs(v) + fabs(qm));
+          e = den > 0.0 ? fabs(dp - dm) / den : 0.0;
+        }
+        err = fmax(err, e);
+      }
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+    err = fmax(err, __shfl_xor_sync(0xffffffffu, err, off));
+  if ((threadIdx.x & 31) == 0)
+    red[threadIdx.x >> 5] = err;
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+      err = fmax(err, red[w]);
+    const int lv = level[blk];
+    flags[blk] = (err > eps_refine && lv < level_max) ? 1 : ((err < eps_coarsen && lv > level_min) ? -1 : 0);
+  }
+}
+
+int
+launch_refine_flags(const double * U, const double * B, const int32_t * level, int n_owned, int dim, int bx, int by,
+                    int bz, int64_t ncell, int64_t nfx, int64_t nfy, int64_t nface, double gamma0, double smallr,
+                    double smallp, int criterion, int level_min, int level_max, int use_rho, int use_pressure,
+                    double eps_refine, double eps_coarsen, double eps_lohner, double * scratch, int8_t * flags,
+                    cudaStream_t stream)
+{
+  if (n_owned <= 0)
+    return 0;
+  const int64_t total = (int64_t)n_owned * ncell;
+  const int64_t want = (total + 255) / 256;
+  refine_quantity_kernel<<<(int)(want < 152 * 64 ? want : 152 * 64), 256, 0, stream>>>(
+    U, B, n_owned, dim, bx, by, bz, ncell, nfx, nfy, nface, gamma0, smallr, smallp, use_rho, use_pressure, scratch);
+  refine_flags_kernel<<<n_owned, 256, 0, stream>>>(scratch, (use_rho ? 1 : 0) + (use_pressure ? 1 : 0), level, n_owned,
+                                                   dim, bx, by, bz, ncell, criterion, level_min, level_max, eps_refine,
+                                                   eps_coarsen, eps_lohner, flags);
+  return (int)cudaGetLastError();
+}
+
+// Face of refined-leaf child rm (remap row) of the new mesh at block-local idx: the ghost prolongation
+// of the parent, faces shared with a kept leaf copied from it, then the divergence corrections of the
+// borders in the order -x, +x, -y, +y, -z, +z (the CPU restatement's prolonged_face).
+__device__ static double
+prolonged_face(const GhostArgs & g, const int32_t * rm, int comp, const int * idx)
+{
+  const int b[3] = {g.bx, g.by, g.bz};
+  DRegion   r{RK_COARSER, rm[1], {rm[2] & 1, (rm[2] >> 1) & 1, (rm[2] >> 2) & 1}, nullptr};
+  auto      base = [&](int c, const int * q) {
+    double v = 0.0;
+    region_face(g, r, c, q, v);
+    return v;
+  };
+  auto border = [&](int c, const int * q, double & v) -> bool {
+    if (g.dim == 2 && c == 2)
+      return false;
+    for (int sd = 0; sd < 2; ++sd)
+    {
+      const int nb = rm[9 + 2 * c + sd];
+      if (nb < 0 || q[c] != (sd == 0 ? 0 : b[c]))
+        continue;
+      int qq[3] = {q[0], q[1], q[2]};
+      qq[c] = sd == 0 ? b[c] : 0;
+      v = face_at(g, nb, c, qq[0], qq[1], qq[2]);
+      return true;
+    }
+    return false;
+  };
+  double val;
+  if (!border(comp, idx, val))
+    val = base(comp, idx);
+  if (g.dim == 2 && comp == 2)
+    return val;
+  for (int n = 0; n < g.dim; ++n)
+    for (int sd = 0; sd < 2; ++sd)
+    {
+      const int nb = rm[9 + 2 * n + sd];
+      if (nb < 0 || comp == n)
+        continue;
+      const int p = sd == 0 ? 0 : b[n] - 1;
+      if (idx[n] != p || (idx[comp] & 1) == 0)
+        continue;
+      const double sgn = sd == 0 ? 1.0 : -1.0;
+      const int    t1 = n == 0 ? 1 : 0, t2 = n == 2 ? 1 : 2;
+      const int    A = idx[t1] >> 1, Cc = g.dim == 3 ? (idx[t2] >> 1) : 0;
+      double       d[2][2] = {{0, 0}, {0, 0}};
+      for (int a = 0; a < 2; ++a)
+        for (int c2 = 0; c2 < (g.dim == 3 ? 2 : 1); ++c2)
+        {
+          int q[3] = {0, 0, 0};
+          q[n] = sd == 0 ? 0 : b[n];
+          q[t1] = 2 * A + a;
+          if (g.dim == 3)
+            q[t2] = 2 * Cc + c2;
+          double bv = 0.0;
+          border(n, q, bv);
+          d[a][c2] = bv - base(n, q);
+        }
+      if (g.dim == 2)
+      {
+        val += sgn * d[0][0];
+        continue;
+      }
+      const double F = 0.5 * (d[0][0] + d[0][1]);
+      if (comp == t1)
+        val += sgn * F;
+      else
+      {
+        const int a = idx[t1] & 1;
+        val += sgn * (a == 0 ? d[0][0] - F : d[1][0] + F);
+      }
+    }
+  return val;
+}
+
+// one CTA per new owned block
+__global__ void __launch_bounds__(256)
+remap_kernel(const GhostArgs g, const int32_t * __restrict__ remap, double * __restrict__ Un,
+             double * __restrict__ Bn)
+{
+  const int       n = blockIdx.x;
+  const int32_t * rm = remap + (int64_t)n * 15;
+  const int       b[3] = {g.bx, g.by, g.bz};
+  double *        Ub = Un + (int64_t)n * 5 * g.ncell;
+  double *        Bb = Bn + (int64_t)n * g.nface;
+  const int       kind = rm[0];
+  if (kind == 0)
+  {
+    const double * Us = g.U + (int64_t)rm[1] * 5 * g.ncell;
+    const double * Bs = g.B + (int64_t)rm[1] * g.nface;
+    for (int64_t i = threadIdx.x; i < 5 * g.ncell; i += blockDim.x)
+      Ub[i] = Us[i];
+    for (int64_t i = threadIdx.x; i < g.nface; i += blockDim.x)
+      Bb[i] = Bs[i];
+    return;
+  }
+  const DRegion fine{RK_FINER, -1, {0, 0, 0}, rm + 1};
+  for (int64_t c = threadIdx.x; c < g.ncell; c += blockDim.x)
+  {
+    const int q[3] = {(int)(c % g.bx), (int)((c / g.bx) % g.by), (int)(c / ((int64_t)g.bx * g.by))};
+    for (int v = 0; v < 5; ++v)
+    {
+      double val = 0.0;
+      if (kind == 2)
+      {
+        if (!restrict_cell(g, fine, q, v, val))
+          atomicOr(g.health, (unsigned)HEALTH_MISSING_NEIGHBOR);
+      }
+      else
+      {
+        const int ch = rm[2];
+        val = u_at(g, rm[1], v, ((ch & 1) * b[0] + q[0]) >> 1, (((ch >> 1) & 1) * b[1] + q[1]) >> 1,
+                   g.dim == 3 ? ((((ch >> 2) & 1) * b[2] + q[2]) >> 1) : 0);
+      }
+      Ub[(int64_t)v * g.ncell + c] = val;
+    }
+  }
+  for (int64_t fi = threadIdx.x; fi < g.nface; fi += blockDim.x)
+  {
+    int     comp, nx, ny;
+    int64_t rr;
+    if (fi < g.nfx)
+    {
+      comp = 0; rr = fi; nx = g.bx + 1; ny = g.by;
+    }
+    else if (fi < g.nfx + g.nfy)
+    {
+      comp = 1; rr = fi - g.nfx; nx = g.bx; ny = g.by + 1;
+    }
+    else
+    {
+      comp = 2; rr = fi - g.nfx - g.nfy; nx = g.bx; ny = g.by;
+    }
+    const int idx[3] = {(int)(rr % nx), (int)((rr / nx) % ny), (int)(rr / ((int64_t)nx * ny))};
+    double    val = 0.0;
+    if (kind == 2)
+    {
+      const int sd = (g.dim == 2 && comp == 2) ? -1 : (idx[comp] == 0 ? 0 : (idx[comp] == b[comp] ? 1 : -1));
+      if (sd >= 0 && rm[9 + 2 * comp + sd] >= 0)
+      {
+        int qq[3] = {idx[0], idx[1], idx[2]};
+        qq[comp] = sd == 0 ? b[comp] : 0;
+        val = face_at(g, rm[9 + 2 * comp + sd], comp, qq[0], qq[1], qq[2]);
+      }
+      else if (!region_face(g, fine, comp, idx, val))
+        atomicOr(g.health, (unsigned)HEALTH_MISSING_NEIGHBOR);
+    }
+    else
+      val = prolonged_face(g, rm, comp, idx);
+    Bb[fi] = val;
+  }
+}
+
+int
+launch_remap(const GhostArgs & g, const int32_t * remap, int n_new, double * Un, double * Bn, cudaStream_t stream)
+{
+  if (n_new <= 0)
+    return 0;
+  remap_kernel<<<n_new, 256, 0, stream>>>(g, remap, Un, Bn);
+  return (int)cudaGetLastError();
+}
+
+} // namespace gmhd

@@ -1165,6 +1165,105 @@ gmhd_step_host_async(gmhd_ctx * ctx, const double * U, double * U2, const double
 }
 
 int
+gmhd_refine_flags(gmhd_ctx * ctx, const double * U, const double * B, const gmhd_refine_params * params,
+                  int8_t * flags, void * stream)
+{
+  if (!ctx || !U || !B || !params || !flags)
+    return GMHD_ERR_ARGUMENT;
+  if (!ctx->has_mesh)
+    return GMHD_ERR_MESH;
+  if ((params->criterion != GMHD_REFINE_SIMPLE_GRADIENT && params->criterion != GMHD_REFINE_LOHNER_UNSPLIT) ||
+      (!params->use_rho && !params->use_pressure))
+    return GMHD_ERR_ARGUMENT;
+  const int     nvar = (params->use_rho ? 1 : 0) + (params->use_pressure ? 1 : 0);
+  const size_t  nq = (size_t)nvar * ctx->n_owned * ctx->ncell;
+  double *      q = nullptr;
+  int8_t *      dflags = nullptr;
+  cudaStream_t  s = (cudaStream_t)stream;
+  GMHD_CUDA(cudaMalloc((void **)&q, nq * sizeof(double)));
+  cudaError_t e = cudaMalloc((void **)&dflags, (size_t)ctx->n_owned > 0 ? (size_t)ctx->n_owned : 1);
+  if (e != cudaSuccess)
+  {
+    cudaFree(q);
+    return cuda_fail(ctx, e);
+  }
+  int rc = gmhd::launch_refine_flags(U, B, ctx->d_level, ctx->n_owned, ctx->dim, ctx->bx, ctx->by, ctx->bz, ctx->ncell,
+                                     ctx->nfx, ctx->nfy, ctx->nface, ctx->p.gamma0, ctx->p.smallr, ctx->smallp,
+                                     params->criterion, params->level_min, params->level_max, params->use_rho,
+                                     params->use_pressure, params->eps_refine, params->eps_coarsen, params->eps_lohner,
+                                     q, dflags, s);
+  if (rc == 0 && ctx->n_owned > 0)
+    rc = (int)cudaMemcpyAsync(flags, dflags, (size_t)ctx->n_owned, cudaMemcpyDeviceToHost, s);
+  if (rc == 0)
+    rc = (int)cudaStreamSynchronize(s);
+  cudaFree(q);
+  cudaFree(dflags);
+  return rc ? cuda_fail(ctx, (cudaError_t)rc) : GMHD_OK;
+}
+
+int
+gmhd_remap(int32_t dim, int32_t bx, int32_t by, int32_t bz, int32_t n_old_blocks, int32_t n_new_owned,
+           const int32_t * remap, const double * U_old, const double * B_old, double * U_new, double * B_new,
+           void * stream)
+{
+  if ((dim != 2 && dim != 3) || bx < 4 || by < 4 || (dim == 3 && bz < 4) || (dim == 2 && bz != 1) || bx % 2 ||
+      by % 2 || (dim == 3 && bz % 2) || n_new_owned < 0 || !remap || !U_old || !B_old || !U_new || !B_new)
+    return GMHD_ERR_ARGUMENT;
+  for (int64_t n = 0; n < n_new_owned; ++n)
+  {
+    const int32_t * rm = remap + n * 15;
+    if (rm[0] < 0 || rm[0] > 2 || rm[1] < 0 || rm[1] >= n_old_blocks ||
+        (rm[0] == 1 && (rm[2] < 0 || rm[2] >= (1 << dim))))
+      return GMHD_ERR_ARGUMENT;
+    if (rm[0] == 2)
+      for (int c = 0; c < (1 << dim); ++c)
+        if (rm[1 + c] < 0 || rm[1 + c] >= n_old_blocks)
+          return GMHD_ERR_ARGUMENT;
+    for (int f = 0; f < 6; ++f)
+      if (rm[9 + f] < -1 || rm[9 + f] >= n_old_blocks || (f >= 2 * dim && rm[9 + f] != -1))
+        return GMHD_ERR_ARGUMENT;
+  }
+  gmhd::GhostArgs g;
+  std::memset(&g, 0, sizeof g);
+  g.U = U_old;
+  g.B = B_old;
+  g.dim = dim;
+  g.bx = bx;
+  g.by = by;
+  g.bz = dim == 3 ? bz : 1;
+  g.ncell = (int64_t)bx * by * g.bz;
+  g.nfx = (int64_t)(bx + 1) * by * g.bz;
+  g.nfy = (int64_t)bx * (by + 1) * g.bz;
+  g.nface = g.nfx + g.nfy + (dim == 3 ? (int64_t)bx * by * (g.bz + 1) : g.ncell);
+  cudaStream_t s = (cudaStream_t)stream;
+  int32_t *    dmap = nullptr;
+  unsigned *   dh = nullptr;
+  if (cudaMalloc((void **)&dmap, sizeof(int32_t) * 15 * (size_t)(n_new_owned > 0 ? n_new_owned : 1)) != cudaSuccess)
+    return GMHD_ERR_CUDA;
+  if (cudaMalloc((void **)&dh, sizeof(unsigned)) != cudaSuccess)
+  {
+    cudaFree(dmap);
+    return GMHD_ERR_CUDA;
+  }
+  g.health = dh;
+  int      rc = (int)cudaMemsetAsync(dh, 0, sizeof(unsigned), s);
+  unsigned h = 0;
+  if (rc == 0)
+    rc = (int)cudaMemcpyAsync(dmap, remap, sizeof(int32_t) * 15 * (size_t)n_new_owned, cudaMemcpyHostToDevice, s);
+  if (rc == 0)
+    rc = gmhd::launch_remap(g, dmap, n_new_owned, U_new, B_new, s);
+  if (rc == 0)
+    rc = (int)cudaMemcpyAsync(&h, dh, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+  if (rc == 0)
+    rc = (int)cudaStreamSynchronize(s);
+  cudaFree(dmap);
+  cudaFree(dh);
+  if (rc)
+    return GMHD_ERR_CUDA;
+  return h ? GMHD_ERR_MESH : GMHD_OK;
+}
+
+int
 gmhd_last_status(gmhd_ctx * ctx, uint32_t * flags)
 {
   if (!ctx || !flags)

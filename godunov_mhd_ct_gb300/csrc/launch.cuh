@@ -65,4 +65,12 @@ struct GhostArgs
 
 int launch_ghost_prepass(const GhostArgs & g, cudaStream_t stream);
 
+// regrid (amr.cu): refinement flags of the owned blocks and the remap to an adapted mesh
+int launch_refine_flags(const double * U, const double * B, const int32_t * level, int n_owned, int dim, int bx,
+                        int by, int bz, int64_t ncell, int64_t nfx, int64_t nfy, int64_t nface, double gamma0,
+                        double smallr, double smallp, int criterion, int level_min, int level_max, int use_rho,
+                        int use_pressure, double eps_refine, double eps_coarsen, double eps_lohner, double * scratch,
+                        int8_t * flags, cudaStream_t stream);
+int launch_remap(const GhostArgs & g, const int32_t * remap, int n_new, double * Un, double * Bn, cudaStream_t stream);
+
 } // namespace gmhd

@@ -50,6 +50,7 @@ class BlockMesh:
     # [n_blocks, 27, 8] leaves covering a neighbour region one level finer (children x fastest,
     # -1 where absent); None on meshes without level jumps
     fine_neighbor: np.ndarray | None = None
+    bricks: tuple = (1, 1, 1)  # root trees per direction
 
     @property
     def n_blocks(self) -> int:
@@ -176,7 +177,8 @@ class BlockMesh:
                          neighbor=neighbor, coords=all_coords, n_owned=n_owned, grid=gsz, periodic=per,
                          scaling_factor=scaling_factor,
                          outside_src=np.array(out_src, dtype=np.int32),
-                         outside_normal=np.array(out_normal, dtype=np.int32).reshape(-1, 3))
+                         outside_normal=np.array(out_normal, dtype=np.int32).reshape(-1, 3),
+                         bricks=tuple(bricks))
 
     @staticmethod
     def amr(dim: int, refine, bricks=(1, 1, 1), base_level: int = 1, max_level: int = 2, block=(16, 16, 16),
@@ -190,27 +192,10 @@ class BlockMesh:
         ``fine_neighbor[b, slot]`` = the 2^d children, x fastest), or an outside block at L. Outside
         blocks need a same-level inside leaf across the border (FillOutside.cpp:134-145 looks the
         inside quadrant up at the outside quadrant's level)."""
-        if dim not in (2, 3):
-            raise ValueError("dim must be 2 or 3")
-        bx, by, bz = block
-        if dim == 2:
-            bz = 1
-            bricks = (bricks[0], bricks[1], 1)
-        if min(bx, by) < 4 or (dim == 3 and bz < 4) or bx % 2 or by % 2 or (dim == 3 and bz % 2):
-            raise ValueError("block sizes must be even and >= 4 on AMR meshes")
+        f = _Forest(dim, bricks, periodic, base_level, block)
         if not (0 <= base_level <= max_level):
             raise ValueError("need 0 <= base_level <= max_level")
-        per = tuple(bool(p) for p in periodic[:dim]) + (True,) * (3 - dim)
-
-        def ext(L):
-            return (bricks[0] << L, bricks[1] << L, (bricks[2] << L) if dim == 3 else 1)
-
-        def kids(key):
-            L, cx, cy, cz = key
-            return [(L + 1, 2 * cx + ex, 2 * cy + ey, 2 * cz + ez) for ez in ((0, 1) if dim == 3 else (0,))
-                    for ey in (0, 1) for ex in (0, 1)]
-
-        e0 = ext(base_level)
+        e0 = f.ext(base_level)
         leaves = {(base_level, cx, cy, cz) for cz in range(e0[2]) for cy in range(e0[1]) for cx in range(e0[0])}
         for L in range(base_level, max_level):
             h = 1.0 / (1 << L)
@@ -219,120 +204,79 @@ class BlockMesh:
                 hi = lo + np.array([h, h, h if dim == 3 else 1.0])
                 if refine(L, lo, hi):
                     leaves.remove(key)
-                    leaves.update(kids(key))
-        offs = [(ox, oy, oz) for oz in ((-1, 0, 1) if dim == 3 else (0,)) for oy in (-1, 0, 1) for ox in (-1, 0, 1)
-                if (ox, oy, oz) != (0, 0, 0)]
+                    leaves.update(f.kids(key))
+        f.balance(leaves)
+        return f.build(leaves, scaling_factor)
 
-        def wrap(L, c):
-            e = ext(L)
-            out = []
-            for d in range(3):
-                v = c[d]
-                if per[d]:
-                    v %= e[d]
-                elif not 0 <= v < e[d]:
-                    return None
-                out.append(v)
-            return tuple(out)
+    def leaf_keys(self):
+        """(level, cx, cy, cz) of the owned leaves, in block order."""
+        return [(int(self.level[b]),) + tuple(int(v) for v in self.coords[b]) for b in range(self.n_owned)]
 
-        changed = True
-        while changed:
-            changed = False
-            for key in sorted(leaves):
-                if key not in leaves or key[0] - 2 < base_level:
-                    continue
-                L = key[0]
-                for o in offs:
-                    r = wrap(L, (key[1] + o[0], key[2] + o[1], key[3] + o[2]))
-                    if r is None:
-                        continue
-                    for lv in range(L - 2, base_level - 1, -1):
-                        sh = L - lv
-                        anc = (lv, r[0] >> sh, r[1] >> sh, r[2] >> sh)
-                        if anc in leaves:
-                            leaves.remove(anc)
-                            leaves.update(kids(anc))
-                            changed = True
-                            break
-
-        # p4est order: trees x fastest, then Morton order of the anchor at max_level
-        def order_key(key):
-            L, cx, cy, cz = key
-            t = (cx >> L, cy >> L, cz >> L)
-            tid = t[0] + bricks[0] * (t[1] + bricks[1] * t[2])
-            sh = max_level - L
-            a = [((cx - (t[0] << L)) << sh), ((cy - (t[1] << L)) << sh), ((cz - (t[2] << L)) << sh)]
-            m = 0
-            for bit in range(max(max_level, 1)):
-                m |= ((a[0] >> bit) & 1) << (3 * bit) | ((a[1] >> bit) & 1) << (3 * bit + 1) | \
-                    ((a[2] >> bit) & 1) << (3 * bit + 2)
-            return (tid, m, L)
-
-        owned = sorted(leaves, key=order_key)
-        ids = {k: n for n, k in enumerate(owned)}
-        n_owned = len(owned)
-        out_keys, out_ids, out_src, out_normal = [], {}, [], []
-        for key in owned:
-            L = key[0]
-            e = ext(L)
-            for o in offs:
-                c = [key[1] + o[0], key[2] + o[1], key[3] + o[2]]
-                r = wrap(L, c)
-                if r is not None:
-                    continue
-                cw = [c[d] % e[d] if per[d] else c[d] for d in range(3)]
-                ok = (L, cw[0], cw[1], cw[2])
-                if ok in out_ids:
-                    continue
-                src = tuple(min(max(cw[d], 0), e[d] - 1) for d in range(3))
-                skey = (L,) + src
-                if skey not in ids:
-                    raise ValueError(f"outside block {ok} has no same-level inside leaf {skey}; keep the level "
-                                     "uniform along non-periodic borders")
-                out_ids[ok] = n_owned + len(out_keys)
-                out_keys.append(ok)
-                out_src.append(ids[skey])
-                out_normal.append(tuple(int(np.sign(src[d] - cw[d])) for d in range(3)))
-        all_keys = owned + out_keys
-        n_blocks = len(all_keys)
-        level = np.array([k[0] for k in all_keys], dtype=np.int32)
-        coords = np.array([k[1:] for k in all_keys], dtype=np.int64).reshape(-1, 3)
-        neighbor = -np.ones((n_blocks, 27), dtype=np.int32)
-        fine = -np.ones((n_blocks, 27, 8), dtype=np.int32)
-        any_jump = False
-        for b, key in enumerate(owned):
-            L = key[0]
-            e = ext(L)
-            for o in offs:
-                s_ = nb_slot(*o)
-                c = [key[1] + o[0], key[2] + o[1], key[3] + o[2]]
-                r = wrap(L, c)
-                if r is None:
-                    cw = tuple(c[d] % e[d] if per[d] else c[d] for d in range(3))
-                    neighbor[b, s_] = out_ids[(L,) + cw]
-                    continue
-                if (L,) + r in ids:
-                    neighbor[b, s_] = ids[(L,) + r]
-                    continue
-                if L - 1 >= base_level and (L - 1, r[0] >> 1, r[1] >> 1, r[2] >> 1) in ids:
-                    neighbor[b, s_] = ids[(L - 1, r[0] >> 1, r[1] >> 1, r[2] >> 1)]
-                    any_jump = True
-                    continue
-                ch = kids((L,) + r)
-                found = False
-                for n, kk in enumerate(ch):
-                    if kk in ids:
-                        fine[b, s_, n] = ids[kk]
-                        found = True
-                if not found:
-                    raise ValueError(f"neighbour region {r} of leaf {key} is not covered within one level")
-                any_jump = True
-        gsz = ext(max(k[0] for k in owned))
-        return BlockMesh(dim=dim, block=(bx, by, bz), level=level, neighbor=neighbor, coords=coords,
-                         n_owned=n_owned, grid=gsz, periodic=per, scaling_factor=scaling_factor,
-                         outside_src=np.array(out_src, dtype=np.int32),
-                         outside_normal=np.array(out_normal, dtype=np.int32).reshape(-1, 3),
-                         fine_neighbor=fine if any_jump else None)
+    def adapt(self, flags, level_min: int, level_max: int):
+        """Refine (flag > 0) and coarsen (flag < 0, whole families only) the owned leaves, then
+        2:1-balance (refinement wins; a family is not coarsened if balance would refine its parent
+        again). Returns (new mesh, remap) with remap[n] for new owned leaf n:
+        [kind, s0, ..., s7, f0, ..., f5] where kind 0 keeps old leaf s0, kind 1 is child s1 (x fastest)
+        of old leaf s0, kind 2 is the parent of old leaves s0..s(2^d - 1) (x fastest); f0..f5 (kinds 1
+        and 2) are the kept old leaves of the same level across the faces -x, +x, -y, +y, -z, +z (-1
+        otherwise). Plays p4est's adapt + balance and the reference's AMR cycle
+        (SolverGodunovMHD.cpp:263-319)."""
+        f = _Forest(self.dim, self.bricks, self.periodic, level_min, self.block)
+        old = self.leaf_keys()
+        old_id = {k: n for n, k in enumerate(old)}
+        flags = np.asarray(flags).reshape(-1)
+        leaves = set(old)
+        refined = {k for n, k in enumerate(old) if flags[n] > 0 and k[0] < level_max}
+        nch = 1 << self.dim
+        parents = {}
+        for n, k in enumerate(old):
+            if flags[n] < 0 and k[0] > level_min:
+                par = (k[0] - 1, k[1] >> 1, k[2] >> 1, k[3] >> 1)
+                parents.setdefault(par, []).append(k)
+        coarsen = {p_ for p_, ch in parents.items() if len(ch) == nch}
+        while True:
+            cand = set(leaves)
+            for k in refined:
+                cand.discard(k)
+                cand.update(f.kids(k))
+            for p_ in coarsen:
+                for c in f.kids(p_):
+                    cand.discard(c)
+                cand.add(p_)
+            f.balance(cand)
+            undone = {p_ for p_ in coarsen if p_ not in cand}
+            if not undone:
+                break
+            coarsen -= undone
+        mesh = f.build(cand, self.scaling_factor)
+        new = mesh.leaf_keys()
+        new_set = set(new)
+        remap = -np.ones((len(new), 15), dtype=np.int32)
+        for n, k in enumerate(new):
+            if k in old_id:
+                remap[n, 0] = 0
+                remap[n, 1] = old_id[k]
+                continue
+            if (k[0] - 1, k[1] >> 1, k[2] >> 1, k[3] >> 1) in old_id:
+                par = (k[0] - 1, k[1] >> 1, k[2] >> 1, k[3] >> 1)
+                remap[n, 0] = 1
+                remap[n, 1] = old_id[par]
+                remap[n, 2] = (k[1] & 1) + 2 * (k[2] & 1) + 4 * (k[3] & 1)
+            else:
+                ch = f.kids(k)
+                if not all(c in old_id for c in ch):
+                    raise ValueError(f"new leaf {k} is neither kept, refined from nor coarsened to the old mesh")
+                remap[n, 0] = 2
+                for c_i, c in enumerate(ch):
+                    remap[n, 1 + c_i] = old_id[c]
+            # kept leaves at this level across the faces: their faces are copied
+            for fc in range(2 * self.dim):
+                o = [0, 0, 0]
+                o[fc // 2] = -1 if fc % 2 == 0 else 1
+                r = f.wrap(k[0], (k[1] + o[0], k[2] + o[1], k[3] + o[2]))
+                if r is not None and (k[0],) + r in old_id and (k[0],) + r in new_set:
+                    remap[n, 9 + fc] = old_id[(k[0],) + r]
+        return mesh, remap
 
     @staticmethod
     def batch(meshes) -> tuple["BlockMesh", np.ndarray]:
@@ -409,3 +353,147 @@ class BlockMesh:
         gj = c[:, 1, None, None, None] * by + j[None]
         gk = c[:, 2, None, None, None] * bz + k[None]
         return gi, gj, gk
+
+
+class _Forest:
+    """Leaf-set operations of a brick forest: children, periodic wrap, 2:1 balance (faces, edges,
+    corners) and the construction of a BlockMesh (p4est order, neighbour and outside tables)."""
+
+    def __init__(self, dim, bricks, periodic, base_level, block):
+        if dim not in (2, 3):
+            raise ValueError("dim must be 2 or 3")
+        bx, by, bz = block
+        if dim == 2:
+            bz = 1
+            bricks = (bricks[0], bricks[1], 1)
+        if min(bx, by) < 4 or (dim == 3 and bz < 4) or bx % 2 or by % 2 or (dim == 3 and bz % 2):
+            raise ValueError("block sizes must be even and >= 4 on AMR meshes")
+        self.dim, self.bricks, self.base_level, self.block = dim, tuple(bricks), base_level, (bx, by, bz)
+        self.per = tuple(bool(p) for p in periodic[:dim]) + (True,) * (3 - dim)
+        self.offs = [(ox, oy, oz) for oz in ((-1, 0, 1) if dim == 3 else (0,)) for oy in (-1, 0, 1)
+                     for ox in (-1, 0, 1) if (ox, oy, oz) != (0, 0, 0)]
+
+    def ext(self, L):
+        b = self.bricks
+        return (b[0] << L, b[1] << L, (b[2] << L) if self.dim == 3 else 1)
+
+    def kids(self, key):
+        L, cx, cy, cz = key
+        return [(L + 1, 2 * cx + ex, 2 * cy + ey, 2 * cz + ez) for ez in ((0, 1) if self.dim == 3 else (0,))
+                for ey in (0, 1) for ex in (0, 1)]
+
+    def wrap(self, L, c):
+        e = self.ext(L)
+        out = []
+        for d in range(3):
+            v = c[d]
+            if self.per[d]:
+                v %= e[d]
+            elif not 0 <= v < e[d]:
+                return None
+            out.append(v)
+        return tuple(out)
+
+    def balance(self, leaves):
+        """Refine leaves (in place) until every leaf's face/edge/corner neighbours are within one level."""
+        changed = True
+        while changed:
+            changed = False
+            for key in sorted(leaves):
+                if key not in leaves or key[0] - 2 < self.base_level:
+                    continue
+                L = key[0]
+                for o in self.offs:
+                    r = self.wrap(L, (key[1] + o[0], key[2] + o[1], key[3] + o[2]))
+                    if r is None:
+                        continue
+                    for lv in range(L - 2, self.base_level - 1, -1):
+                        sh = L - lv
+                        anc = (lv, r[0] >> sh, r[1] >> sh, r[2] >> sh)
+                        if anc in leaves:
+                            leaves.remove(anc)
+                            leaves.update(self.kids(anc))
+                            changed = True
+                            break
+
+    def build(self, leaves, scaling_factor):
+        dim, bricks, per = self.dim, self.bricks, self.per
+        bx, by, bz = self.block
+        max_level = max(k[0] for k in leaves)
+
+        # p4est order: trees x fastest, then Morton order of the anchor at the finest level
+        def order_key(key):
+            L, cx, cy, cz = key
+            t = (cx >> L, cy >> L, cz >> L)
+            tid = t[0] + bricks[0] * (t[1] + bricks[1] * t[2])
+            sh = max_level - L
+            a = [((cx - (t[0] << L)) << sh), ((cy - (t[1] << L)) << sh), ((cz - (t[2] << L)) << sh)]
+            m = 0
+            for bit in range(max(max_level, 1)):
+                m |= ((a[0] >> bit) & 1) << (3 * bit) | ((a[1] >> bit) & 1) << (3 * bit + 1) | \
+                    ((a[2] >> bit) & 1) << (3 * bit + 2)
+            return (tid, m, L)
+
+        owned = sorted(leaves, key=order_key)
+        ids = {k: n for n, k in enumerate(owned)}
+        n_owned = len(owned)
+        out_keys, out_ids, out_src, out_normal = [], {}, [], []
+        for key in owned:
+            L = key[0]
+            e = self.ext(L)
+            for o in self.offs:
+                c = [key[1] + o[0], key[2] + o[1], key[3] + o[2]]
+                if self.wrap(L, c) is not None:
+                    continue
+                cw = [c[d] % e[d] if per[d] else c[d] for d in range(3)]
+                ok = (L, cw[0], cw[1], cw[2])
+                if ok in out_ids:
+                    continue
+                src = tuple(min(max(cw[d], 0), e[d] - 1) for d in range(3))
+                skey = (L,) + src
+                if skey not in ids:
+                    raise ValueError(f"outside block {ok} has no same-level inside leaf {skey}; keep the level "
+                                     "uniform along non-periodic borders")
+                out_ids[ok] = n_owned + len(out_keys)
+                out_keys.append(ok)
+                out_src.append(ids[skey])
+                out_normal.append(tuple(int(np.sign(src[d] - cw[d])) for d in range(3)))
+        all_keys = owned + out_keys
+        n_blocks = len(all_keys)
+        level = np.array([k[0] for k in all_keys], dtype=np.int32)
+        coords = np.array([k[1:] for k in all_keys], dtype=np.int64).reshape(-1, 3)
+        neighbor = -np.ones((n_blocks, 27), dtype=np.int32)
+        fine = -np.ones((n_blocks, 27, 8), dtype=np.int32)
+        any_jump = False
+        for b, key in enumerate(owned):
+            L = key[0]
+            e = self.ext(L)
+            for o in self.offs:
+                s_ = nb_slot(*o)
+                c = [key[1] + o[0], key[2] + o[1], key[3] + o[2]]
+                r = self.wrap(L, c)
+                if r is None:
+                    cw = tuple(c[d] % e[d] if per[d] else c[d] for d in range(3))
+                    neighbor[b, s_] = out_ids[(L,) + cw]
+                    continue
+                if (L,) + r in ids:
+                    neighbor[b, s_] = ids[(L,) + r]
+                    continue
+                par = (L - 1, r[0] >> 1, r[1] >> 1, r[2] >> 1)
+                if L - 1 >= 0 and par in ids:
+                    neighbor[b, s_] = ids[par]
+                    any_jump = True
+                    continue
+                found = False
+                for n, kk in enumerate(self.kids((L,) + r)):
+                    if kk in ids:
+                        fine[b, s_, n] = ids[kk]
+                        found = True
+                if not found:
+                    raise ValueError(f"neighbour region {r} of leaf {key} is not covered within one level")
+                any_jump = True
+        return BlockMesh(dim=dim, block=(bx, by, bz), level=level, neighbor=neighbor, coords=coords,
+                         n_owned=n_owned, grid=self.ext(max_level), periodic=per, scaling_factor=scaling_factor,
+                         outside_src=np.array(out_src, dtype=np.int32),
+                         outside_normal=np.array(out_normal, dtype=np.int32).reshape(-1, 3),
+                         fine_neighbor=fine if any_jump else None, bricks=bricks)

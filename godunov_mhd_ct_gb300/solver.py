@@ -80,6 +80,7 @@ class GodunovImplemGB300:
             self.mesh = mesh
             self._tables = nat.MeshTables(mesh, problem=problem, n_problems=n_problems, bc=bc)
             self.n_problems = n_problems
+            self._bc = bc
         nat.check(self._lib.gmhd_set_mesh(self._ctx, ctypes.byref(self._tables.c)), "gmhd_set_mesh", self._ctx)
 
     def total_mem_size_in_bytes(self) -> int:
@@ -127,6 +128,39 @@ class GodunovImplemGB300:
         nat.check(self._lib.gmhd_step_host(self._ctx, U.ctypes.data, U2.ctypes.data, B.ctypes.data, B2.ctypes.data,
                                            float(dt), None), "gmhd_step_host", self._ctx)
         return U2, B2
+
+    # --- AMR cycle (SolverGodunovMHD::do_amr_cycle, SolverGodunovMHD.cpp:263-319) -------------------
+    def refine_flags(self, U, B, criterion="LOHNER_UNSPLIT", level_min=0, level_max=30, eps_refine=0.16,
+                     eps_coarsen=0.02, eps_lohner=0.02, variables=("rho",), stream=None):
+        """Flags (-1 coarsen, 0 keep, +1 refine) of the owned blocks (compute_refine_flags)."""
+        vs = {v.lower() for v in variables}
+        p = nat.GmhdRefineParams(nat.REFINE_CRITERIA[criterion.upper()], level_min, level_max, int("rho" in vs),
+                                 int("pressure" in vs), eps_refine, eps_coarsen, eps_lohner)
+        flags = np.zeros(self.mesh.n_owned, dtype=np.int8)
+        nat.check(self._lib.gmhd_refine_flags(self._ctx, _ptr(U), _ptr(B), ctypes.byref(p), flags.ctypes.data,
+                                              _stream_ptr(stream)), "gmhd_refine_flags", self._ctx)
+        return flags
+
+    def regrid(self, U, B, level_min: int, level_max: int, stream=None, **criterion):
+        """One AMR cycle: refinement flags on the device, mesh adaptation + 2:1 balance on the host
+        (BlockMesh.adapt, p4est's part), remap of U and B on the device, new mesh tables
+        (resize_auxiliary_data). Returns (new mesh, new U, new B); U, B stay valid until released."""
+        import torch
+
+        if self.n_problems != 1:
+            raise ValueError("regrid works on single-problem meshes")
+        flags = self.refine_flags(U, B, level_min=level_min, level_max=level_max, stream=stream, **criterion)
+        new_mesh, table = self.mesh.adapt(flags, level_min, level_max)
+        us, bs = new_mesh.alloc_state()
+        Un = torch.zeros(us.shape, dtype=torch.float64, device=U.device)
+        Bn = torch.zeros(bs.shape, dtype=torch.float64, device=U.device)
+        table = np.ascontiguousarray(table, dtype=np.int32)
+        bx, by, bz = self.mesh.block
+        nat.check(self._lib.gmhd_remap(self.mesh.dim, bx, by, bz, self.mesh.n_blocks, new_mesh.n_owned,
+                                       table.ctypes.data, _ptr(U), _ptr(B), _ptr(Un), _ptr(Bn), _stream_ptr(stream)),
+                  "gmhd_remap")
+        self.resize_auxiliary_data(new_mesh, bc=self._bc)
+        return new_mesh, Un, Bn
 
     def last_status(self) -> int:
         flags = ctypes.c_uint32(0)

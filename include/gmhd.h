@@ -75,6 +75,22 @@ enum gmhd_time_integrator
   GMHD_TIME_RK2_SSP = 1  /* two stages without the predictor, U = 1/2 U + 1/2 U2 (gmhd_advance) */
 };
 
+/* Regrid refinement criterion ([amr] refine_criterion, epsilon_refine, epsilon_coarsen, epsilon_lohner,
+ * level_min, level_max, variable_used_to_compute_refine_criterion; SolverGodunovMHD.cpp:1092-1186). */
+enum gmhd_refine_criterion
+{
+  GMHD_REFINE_SIMPLE_GRADIENT = 0,
+  GMHD_REFINE_LOHNER_UNSPLIT = 1
+};
+
+typedef struct gmhd_refine_params
+{
+  int32_t criterion; /* enum gmhd_refine_criterion */
+  int32_t level_min, level_max;
+  int32_t use_rho, use_pressure; /* quantities the indicator is taken on (max over them) */
+  double  eps_refine, eps_coarsen, eps_lohner;
+} gmhd_refine_params;
+
 /* Health flags reported by gmhd_last_status. */
 enum gmhd_health_flags
 {
@@ -203,6 +219,28 @@ int gmhd_inv_dt_noalloc(const gmhd_params * params, int32_t dim, int32_t bx, int
 /* gmhd_step on HOST arrays: copies U, B to the device, runs the step, copies U2, B2 back. */
 int gmhd_step_host(gmhd_ctx * ctx, const double * U, double * U2, const double * B, double * B2, double dt,
                    void * stream);
+
+/* Refinement flags of the owned blocks (-1 coarsen, 0 keep, +1 refine) of the state U, B on the mesh
+ * set in ctx (compute_refine_flags, SolverGodunovMHD.cpp:1092-1186; the indicator of kalypsso-core's
+ * ComputeRefineFlags restated: per cell and axis, neighbours clamped to the block, SIMPLE_GRADIENT
+ * max(|q+ - q|, |q - q-|) / |q| or LOHNER_UNSPLIT |dp - dm| / (|dp| + |dm| + eps (|q+| + 2|q| + |q-|)),
+ * block error = max; +1 when error > eps_refine and level < level_max, -1 when error < eps_coarsen and
+ * level > level_min). flags: HOST array of n_owned bytes. Synchronises `stream`. */
+int gmhd_refine_flags(gmhd_ctx * ctx, const double * U, const double * B, const gmhd_refine_params * params,
+                      int8_t * flags, void * stream);
+
+/* Remap of the conservative state and face B to an adapted mesh (map_userdata_after_adapt,
+ * SolverGodunovMHD.cpp:1189-1262; kalypsso-core's UserDataRemapper restated). remap: HOST array of
+ * 15 ints per new owned block: kind (0 kept, 1 refined child, 2 coarsened parent), sources (kind 0:
+ * old block; 1: old parent, child index x fastest; 2: the 2^d old children, x fastest), then the old
+ * blocks of the same level kept across the faces -x, +x, -y, +y, -z, +z (-1 otherwise). Kept blocks are
+ * copied; coarsened ones take the mean of their children (faces shared with a kept block copy it);
+ * refined ones copy the parent cell and prolong face B divergence-free (faces shared with a kept block
+ * copy it and the faces inside each parent cell absorb the difference). Writes the owned blocks of
+ * U_new, B_new (device); synchronises `stream`. */
+int gmhd_remap(int32_t dim, int32_t bx, int32_t by, int32_t bz, int32_t n_old_blocks, int32_t n_new_owned,
+               const int32_t * remap, const double * U_old, const double * B_old, double * U_new, double * B_new,
+               void * stream);
 
 /* Stream-ordered gmhd_step_host (no counterpart in the reference; it exists for callers that keep the
  * state in host memory): copies U, B in, runs the step and copies the owned blocks of U2, B2 out, then

@@ -209,3 +209,41 @@ def find_speed_info(st, q, dim):
 def find_speed_fast(st, q, d):
     q = np.ascontiguousarray(q, dtype=np.float64)
     return np.array([lib().oracle_find_speed_fast(ctypes.byref(st), _dp(q[i]), d) for i in range(q.shape[0])])
+
+
+REFINE_CRITERIA = {"SIMPLE_GRADIENT": 0, "LOHNER_UNSPLIT": 1}
+
+
+def refine_flags(mesh: Mesh, st: OracleSettings, U, B, criterion="LOHNER_UNSPLIT", level_min=0, level_max=30,
+                 eps_refine=0.16, eps_coarsen=0.02, eps_lohner=0.02, use_rho=True, use_pressure=False):
+    """Refinement flags (-1, 0, +1) of the owned blocks."""
+    L = lib()
+    L.oracle_refine_flags.argtypes = [ctypes.POINTER(OracleMesh), ctypes.POINTER(OracleSettings),
+                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_void_p]
+    pi = np.array([REFINE_CRITERIA[criterion], level_min, level_max, int(use_rho), int(use_pressure)], np.int32)
+    pd = np.array([eps_refine, eps_coarsen, eps_lohner], np.float64)
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    flags = np.zeros(mesh.c.n_owned, np.int8)
+    L.oracle_refine_flags(ctypes.byref(mesh.c), ctypes.byref(st), U.ctypes.data, B.ctypes.data, pi.ctypes.data,
+                          pd.ctypes.data, flags.ctypes.data)
+    return flags
+
+
+def remap(old: Mesh, new: Mesh, table, U, B, new_shapes):
+    """U, B of the new mesh from the old one (table: BlockMesh.adapt's remap)."""
+    L = lib()
+    L.oracle_remap.restype = ctypes.c_int
+    L.oracle_remap.argtypes = [ctypes.POINTER(OracleMesh), ctypes.POINTER(OracleMesh), ctypes.c_void_p,
+                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    t = np.ascontiguousarray(table, dtype=np.int32)
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    Un = np.zeros(new_shapes[0], np.float64)
+    Bn = np.zeros(new_shapes[1], np.float64)
+    rc = L.oracle_remap(ctypes.byref(old.c), ctypes.byref(new.c), t.ctypes.data, U.ctypes.data, B.ctypes.data,
+                        Un.ctypes.data, Bn.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"oracle_remap failed: {rc}")
+    return Un, Bn

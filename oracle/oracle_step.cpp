@@ -1311,6 +1311,167 @@ cell_length(const Mesh & m, int level)
   return (1.0 / (double)((int64_t)m.bx << level)) * m.scaling_factor;
 }
 
+
+// ---- regrid: refinement indicator and remap (SolverGodunovMHD.cpp:263-319, 1092-1262) --------
+// kalypsso-core's ComputeRefineFlags and UserDataRemapper are not in the reference tree; these are
+// this restatement's definitions (mirrored by the GPU kernels in amr.cu):
+//   * indicator per cell and axis on rho and/or the pressure (compute_primitives with the cell-centred
+//     B of the faces), neighbours clamped to the block: SIMPLE_GRADIENT
+//     max(|q+ - q|, |q - q-|) / max(|q|, DBL_MIN); LOHNER_UNSPLIT |dp - dm| / (|dp| + |dm| +
+//     eps_lohner (|q+| + 2|q| + |q-|)) with dp = q+ - q, dm = q - q-; block error = max; flag +1
+//     if error > epsilon_refine and level < level_max, -1 if error < epsilon_coarsen and level >
+//     level_min;
+//   * remap: kept leaves copy; a coarsened leaf takes the mean of its children (cells and faces, as
+//     the ghost restriction; a face shared with a kept leaf of its level copies that leaf's face);
+//     a refined leaf copies the parent cell (SIMPLE_COPY) and prolongs faces
+//     as the ghost prolongation, except that faces shared with a leaf that stays at the child's level
+//     copy that leaf's faces, the resulting divergence of each adjacent fine cell being cancelled on
+//     the faces inside its coarse cell (2D: + or - d0 on the middle face; 3D: F = (d00 + d01)/2 on
+//     the two faces normal to the first transverse axis, d00 - F and d10 + F on those normal to the
+//     second), borders applied in the order -x, +x, -y, +y, -z, +z.
+struct RefineParams
+{
+  int32_t criterion; // 0 SIMPLE_GRADIENT, 1 LOHNER_UNSPLIT
+  int32_t level_min, level_max;
+  int32_t use_rho, use_pressure;
+  double  eps_refine, eps_coarsen, eps_lohner;
+};
+
+static double
+refine_quantity(const Mesh & m, const Fields & f, const Settings & s, int blk, int var, int i, int j, int k)
+{
+  if (var == 0)
+    return f.u(blk, ID, i, j, k);
+  double u[8], q[8];
+  for (int n = 0; n < 5; ++n)
+    u[n] = f.u(blk, n, i, j, k);
+  u[IA] = 0.5 * (f.bx(blk, i, j, k) + f.bx(blk, i + 1, j, k));
+  u[IB] = 0.5 * (f.by(blk, i, j, k) + f.by(blk, i, j + 1, k));
+  if (m.dim == 3)
+    u[IC] = 0.5 * (f.bz(blk, i, j, k) + f.bz(blk, i, j, k + 1));
+  else
+    u[IC] = 0.5 * (f.bz(blk, i, j, 0) + f.bz(blk, i, j, 0));
+  compute_primitives(u, q, nullptr, s);
+  return q[IP];
+}
+
+static double
+block_refine_error(const Mesh & m, const Fields & f, const Settings & s, const RefineParams & rp, int blk)
+{
+  const int b[3] = {m.bx, m.by, m.bz};
+  double    err = 0.0;
+  for (int var = 0; var < 2; ++var)
+  {
+    if ((var == 0 && !rp.use_rho) || (var == 1 && !rp.use_pressure))
+      continue;
+    for (int k = 0; k < m.bz; ++k)
+      for (int j = 0; j < m.by; ++j)
+        for (int i = 0; i < m.bx; ++i)
+        {
+          const double q = refine_quantity(m, f, s, blk, var, i, j, k);
+          for (int d = 0; d < m.dim; ++d)
+          {
+            int im[3] = {i, j, k}, ip[3] = {i, j, k};
+            im[d] = std::max(im[d] - 1, 0);
+            ip[d] = std::min(ip[d] + 1, b[d] - 1);
+            const double qm = refine_quantity(m, f, s, blk, var, im[0], im[1], im[2]);
+            const double qp = refine_quantity(m, f, s, blk, var, ip[0], ip[1], ip[2]);
+            double       e;
+            if (rp.criterion == 0)
+              e = std::fmax(std::fabs(qp - q), std::fabs(q - qm)) / std::fmax(std::fabs(q), 2.2250738585072014e-308);
+            else
+            {
+              const double dp = qp - q, dm = q - qm;
+              const double den = std::fabs(dp) + std::fabs(dm) +
+                                 rp.eps_lohner * (std::fabs(qp) + 2.0 * std::fabs(q) + std::fabs(qm));
+              e = den > 0.0 ? std::fabs(dp - dm) / den : 0.0;
+            }
+            err = std::fmax(err, e);
+          }
+        }
+  }
+  return err;
+}
+
+// Face value (component comp, block-local idx) of refined-leaf child n of the new mesh: the ghost
+// prolongation of the parent, faces shared with a kept leaf copied from it, then the divergence
+// corrections of the borders in order.
+static double
+prolonged_face(const Mesh & mo, const Fields & fo, const int32_t * rm, int comp, const int * idx)
+{
+  const int b[3] = {mo.bx, mo.by, mo.bz};
+  const int parent = rm[1], child = rm[2];
+  Region    r{RK_COARSER, parent, {child & 1, (child >> 1) & 1, (child >> 2) & 1}, nullptr};
+  auto      base = [&](int c, const int * q) {
+    double v = 0.0;
+    region_face(mo, fo, r, c, q, v);
+    return v;
+  };
+  const bool cellc = mo.dim == 2 && comp == 2;
+  // border replacement
+  auto border = [&](int c, const int * q, double & v) {
+    if (mo.dim == 2 && c == 2)
+      return false;
+    for (int sd = 0; sd < 2; ++sd)
+    {
+      const int nb = rm[9 + 2 * c + sd];
+      if (nb < 0 || q[c] != (sd == 0 ? 0 : b[c]))
+        continue;
+      int qq[3] = {q[0], q[1], q[2]};
+      qq[c] = sd == 0 ? b[c] : 0;
+      v = fo.face(nb, c, qq[0], qq[1], qq[2]);
+      return true;
+    }
+    return false;
+  };
+  double val;
+  if (!border(comp, idx, val))
+    val = base(comp, idx);
+  if (cellc)
+    return val;
+  for (int n = 0; n < mo.dim; ++n)
+    for (int sd = 0; sd < 2; ++sd)
+    {
+      const int nb = rm[9 + 2 * n + sd];
+      if (nb < 0 || comp == n)
+        continue;
+      const int p = sd == 0 ? 0 : b[n] - 1;
+      if (idx[n] != p || (idx[comp] & 1) == 0)
+        continue;
+      const double sgn = sd == 0 ? 1.0 : -1.0;
+      const int    t1 = n == 0 ? 1 : 0, t2 = n == 2 ? 1 : 2;
+      // deltas of the border faces of this coarse cell, d[a][c] at (t1: 2A + a, t2: 2C + c)
+      const int A = idx[t1] >> 1, Cc = mo.dim == 3 ? (idx[t2] >> 1) : 0;
+      double    d[2][2] = {{0, 0}, {0, 0}};
+      for (int a = 0; a < 2; ++a)
+        for (int c2 = 0; c2 < (mo.dim == 3 ? 2 : 1); ++c2)
+        {
+          int q[3] = {0, 0, 0};
+          q[n] = sd == 0 ? 0 : b[n];
+          q[t1] = 2 * A + a;
+          if (mo.dim == 3)
+            q[t2] = 2 * Cc + c2;
+          double bv = 0.0;
+          border(n, q, bv);
+          d[a][c2] = bv - base(n, q);
+        }
+      if (mo.dim == 2)
+      {
+        val += sgn * d[0][0];
+        continue;
+      }
+      const double F = 0.5 * (d[0][0] + d[0][1]);
+      if (comp == t1)
+        val += sgn * F;
+      else
+      {
+        const int a = idx[t1] & 1;
+        val += sgn * (a == 0 ? d[0][0] - F : d[1][0] + F);
+      }
+    }
+  return val;
+}
+
 } // namespace oracle
 
 using namespace oracle;
@@ -1652,6 +1813,122 @@ oracle_run_to(const oracle_mesh * om, const oracle_settings * os, double * U, do
     std::memcpy(B, B2.data(), nb * sizeof(double));
   }
   return 0;
+}
+
+// Refinement flags of the owned blocks (-1 coarsen, 0 keep, +1 refine); see RefineParams.
+void
+oracle_refine_flags(const oracle_mesh * om, const oracle_settings * os, const double * U, const double * B,
+                    const int32_t * params_i, const double * params_d, int8_t * flags)
+{
+  const Mesh     m = to_mesh(om);
+  const Settings s = to_settings(os);
+  Fields         f;
+  f.m = &m;
+  f.L = block_layout(m);
+  f.U = U;
+  f.B = B;
+  RefineParams rp{params_i[0], params_i[1], params_i[2], params_i[3], params_i[4], params_d[0], params_d[1],
+                  params_d[2]};
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int blk = 0; blk < m.n_owned; ++blk)
+  {
+    const double err = block_refine_error(m, f, s, rp, blk);
+    const int    lv = m.level[blk];
+    flags[blk] = (err > rp.eps_refine && lv < rp.level_max) ? 1 : ((err < rp.eps_coarsen && lv > rp.level_min) ? -1 : 0);
+  }
+}
+
+// Remap U, B of the old mesh to the new one (remap rows of BlockMesh.adapt: kind, sources, fine
+// face neighbours); owned blocks of the new arrays are written.
+int
+oracle_remap(const oracle_mesh * om_old, const oracle_mesh * om_new, const int32_t * remap, const double * Uo,
+             const double * Bo, double * Un, double * Bn)
+{
+  const Mesh mo = to_mesh(om_old), mn = to_mesh(om_new);
+  Fields     fo;
+  fo.m = &mo;
+  fo.L = block_layout(mo);
+  fo.U = Uo;
+  fo.B = Bo;
+  const BlockLayout L = fo.L;
+  int               status = 0;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int n = 0; n < mn.n_owned; ++n)
+  {
+    const int32_t * rm = remap + (int64_t)n * 15;
+    double *        Ub = Un + (int64_t)n * 5 * L.ncell;
+    double *        Bb = Bn + (int64_t)n * L.nface;
+    if (rm[0] == 0)
+    {
+      std::memcpy(Ub, Uo + (int64_t)rm[1] * 5 * L.ncell, sizeof(double) * 5 * L.ncell);
+      std::memcpy(Bb, Bo + (int64_t)rm[1] * L.nface, sizeof(double) * L.nface);
+      continue;
+    }
+    // cells
+    for (int k = 0; k < mo.bz; ++k)
+      for (int j = 0; j < mo.by; ++j)
+        for (int i = 0; i < mo.bx; ++i)
+        {
+          const int     q[3] = {i, j, k};
+          const int64_t c = i + (int64_t)mo.bx * (j + (int64_t)mo.by * k);
+          for (int v = 0; v < 5; ++v)
+          {
+            double val = 0.0;
+            if (rm[0] == 2)
+            {
+              Region r{RK_FINER, -1, {0, 0, 0}, rm + 1};
+              if (!restrict_cell(mo, fo, r, q, v, val))
+                status = -1;
+            }
+            else
+            {
+              const int ch = rm[2];
+              const int I[3] = {((ch & 1) * mo.bx + i) >> 1, (((ch >> 1) & 1) * mo.by + j) >> 1,
+                                (mo.dim == 3 ? (((ch >> 2) & 1) * mo.bz + k) >> 1 : 0)};
+              val = fo.u(rm[1], v, I[0], I[1], I[2]);
+            }
+            Ub[v * L.ncell + c] = val;
+          }
+        }
+    // faces
+    for (int64_t fi = 0; fi < L.nface; ++fi)
+    {
+      int     comp, nx, ny;
+      int64_t rr;
+      if (fi < L.nfx)
+      {
+        comp = 0; rr = fi; nx = mo.bx + 1; ny = mo.by;
+      }
+      else if (fi < L.nfx + L.nfy)
+      {
+        comp = 1; rr = fi - L.nfx; nx = mo.bx; ny = mo.by + 1;
+      }
+      else
+      {
+        comp = 2; rr = fi - L.nfx - L.nfy; nx = mo.bx; ny = mo.by;
+      }
+      const int idx[3] = {(int)(rr % nx), (int)((rr / nx) % ny), (int)(rr / ((int64_t)nx * ny))};
+      double    val = 0.0;
+      if (rm[0] == 2)
+      {
+        // mean of the children's faces; a face shared with a kept leaf of the same level is its copy
+        Region r{RK_FINER, -1, {0, 0, 0}, rm + 1};
+        const int sd = (mo.dim == 2 && comp == 2) ? -1 : (idx[comp] == 0 ? 0 : (idx[comp] == (comp == 0 ? mo.bx : (comp == 1 ? mo.by : mo.bz)) ? 1 : -1));
+        if (sd >= 0 && rm[9 + 2 * comp + sd] >= 0)
+        {
+          int qq[3] = {idx[0], idx[1], idx[2]};
+          qq[comp] = sd == 0 ? (comp == 0 ? mo.bx : (comp == 1 ? mo.by : mo.bz)) : 0;
+          val = fo.face(rm[9 + 2 * comp + sd], comp, qq[0], qq[1], qq[2]);
+        }
+        else if (!region_face(mo, fo, r, comp, idx, val))
+          status = -1;
+      }
+      else
+        val = prolonged_face(mo, fo, rm, comp, idx);
+      Bb[fi] = val;
+    }
+  }
+  return status;
 }
 
 // Per-call entry points for the known-answer tests.
