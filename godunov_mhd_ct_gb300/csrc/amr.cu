@@ -132,7 +132,13 @@ region_face(const GhostArgs & g, const DRegion & r, int comp, const int * q, dou
             F[t2] = 2 * q[t2] + e2;
             c[t2] = F[t2] >= b[t2];
           }
-          const int id = r.child[c[0] + 2 * c[1] + 4 * c[2]];
+          int id = r.child[c[0] + 2 * c[1] + 4 * c[2]];
+          if (id < 0 && F[comp] == b[comp])
+          {
+            // a face between the two children along its normal: the other child holds it too
+            c[comp] = 0;
+            id = r.child[c[0] + 2 * c[1] + 4 * c[2]];
+          }
           if (id < 0)
             return false;
           acc += face_at(g, id, comp, F[0] - c[0] * b[0], F[1] - c[1] * b[1], F[2] - c[2] * b[2]);
