@@ -80,6 +80,11 @@ def lib():
     L.gmhd_step_host_async.argtypes = [vp, vp, vp, vp, vp, ctypes.c_double, vp]
     L.gmhd_refine_flags.argtypes = [vp, vp, vp, ctypes.POINTER(GmhdRefineParams), vp, vp]
     L.gmhd_remap.argtypes = [ctypes.c_int32] * 6 + [vp] * 5 + [vp]
+    L.gmhd_forest_build.restype = vp
+    L.gmhd_forest_build.argtypes = [ctypes.c_int32, vp, vp] + [ctypes.c_int32] * 6 + [vp, vp]
+    L.gmhd_forest_sizes.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
+    L.gmhd_forest_tables.argtypes = [vp] * 8
+    L.gmhd_forest_destroy.argtypes = [vp]
     L.gmhd_last_status.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32)]
     L.gmhd_last_cuda_error.argtypes = [vp]
     L.gmhd_error_string.restype = ctypes.c_char_p
@@ -104,7 +109,8 @@ def exported_symbols():
     return ["gmhd_create", "gmhd_destroy", "gmhd_set_mesh", "gmhd_mem_bytes", "gmhd_step", "gmhd_inv_dt",
             "gmhd_fill_outside", "gmhd_advance", "gmhd_step_host", "gmhd_last_status", "gmhd_last_cuda_error",
             "gmhd_error_string", "gmhd_layout_check", "gmhd_inv_dt_noalloc", "gmhd_step_host_async",
-            "gmhd_refine_flags", "gmhd_remap"]
+            "gmhd_refine_flags", "gmhd_remap", "gmhd_forest_build", "gmhd_forest_sizes", "gmhd_forest_tables",
+            "gmhd_forest_destroy"]
 
 
 class MeshTables:
@@ -138,3 +144,34 @@ class MeshTables:
         self.fine = None if fine is None else np.ascontiguousarray(fine, dtype=np.int32).reshape(-1)
         c.fine_neighbor = self.fine.ctypes.data_as(_ip) if self.fine is not None else ctypes.cast(None, _ip)
         self.c = c
+
+
+def forest_build(dim, bricks, periodic, block, level_min, level_max, keys, flags=None):
+    """Native leaf forest (gmhd_forest_build): returns a dict of numpy tables (level, coord, neighbor,
+    fine_neighbor [n_blocks, 27, 8], outside_src, outside_normal, remap [n_owned, 15], n_owned)."""
+    L = lib()
+    keys = np.ascontiguousarray(np.asarray(keys, dtype=np.int32).reshape(-1, 4))
+    br = np.ascontiguousarray(np.asarray(bricks, dtype=np.int32)[:3])
+    pe = np.ascontiguousarray(np.asarray([int(bool(p)) for p in periodic[:3]], dtype=np.int32))
+    fl = None if flags is None else np.ascontiguousarray(np.asarray(flags, dtype=np.int8).reshape(-1))
+    h = L.gmhd_forest_build(int(dim), br.ctypes.data, pe.ctypes.data, int(block[0]), int(block[1]), int(block[2]),
+                            int(level_min), int(level_max), keys.shape[0], keys.ctypes.data,
+                            fl.ctypes.data if fl is not None else None)
+    if not h:
+        raise ValueError("gmhd_forest_build failed (invalid keys, or an outside block without a same-level inside "
+                         "block: keep the level uniform along non-periodic borders)")
+    try:
+        no, nb = ctypes.c_int32(), ctypes.c_int32()
+        check(L.gmhd_forest_sizes(h, ctypes.byref(no), ctypes.byref(nb)), "gmhd_forest_sizes")
+        no, nb = no.value, nb.value
+        t = {"level": np.zeros(nb, np.int32), "coord": np.zeros((nb, 3), np.int32),
+             "neighbor": np.zeros((nb, 27), np.int32), "fine_neighbor": np.zeros((nb, 27, 8), np.int32),
+             "outside_src": np.zeros(nb - no, np.int32), "outside_normal": np.zeros((nb - no, 3), np.int32),
+             "remap": np.zeros((no, 15), np.int32)}
+        check(L.gmhd_forest_tables(h, *(t[k].ctypes.data if t[k].size else None for k in
+                                        ("level", "coord", "neighbor", "fine_neighbor", "outside_src",
+                                         "outside_normal", "remap"))), "gmhd_forest_tables")
+        t["n_owned"] = no
+        return t
+    finally:
+        L.gmhd_forest_destroy(h)

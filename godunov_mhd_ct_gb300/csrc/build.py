@@ -25,6 +25,7 @@ UNITS = {
     "gmhd_abi.cu": ["--fmad=false"],
     "noalloc.cu": ["--fmad=false"],
     "amr.cu": ["--fmad=false"],
+    "forest.cpp": [],
 }
 HEADERS = ["mhd_math.cuh", "fused_step.cuh", "launch.cuh", os.path.join("..", "..", "include", "gmhd.h")]
 
@@ -49,7 +50,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     jobs = []
     for unit, flags in UNITS.items():
         src = os.path.join(HERE, unit)
-        obj = os.path.join(OBJDIR, unit.replace(".cu", ".o"))
+        obj = os.path.join(OBJDIR, unit.rsplit(".", 1)[0] + ".o")
         if force or _stale(obj, [src, __file__] + headers):
             cmd = [nvcc()] + ARCH + COMMON + flags + ["-c", src, "-o", obj]
             jobs.append(cmd)
@@ -61,7 +62,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
             print(r.stdout + r.stderr)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {cmd[-3]}")
-    objs = [os.path.join(OBJDIR, u.replace(".cu", ".o")) for u in UNITS]
+    objs = [os.path.join(OBJDIR, u.rsplit(".", 1)[0] + ".o") for u in UNITS]
     if force or jobs or _stale(LIB, objs):
         cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -1,0 +1,477 @@
+// Host-side leaf forest: refinement / coarsening of the leaf blocks, 2:1 balance across faces, edges
+// and corners, and the mesh tables the kernels read (p4est's adapt + balance + the reference's
+// orchard-key hashmap lookups, SolverGodunovMHD.cpp:263-319; p4est_balance with full connectivity).
+//
+// Leaves are keyed by (level, x, y, z) with x, y, z the block position at that level over a brick of
+// bricks[0] x bricks[1] x bricks[2] trees. Block order is p4est's: trees x fastest, then the Morton
+// order of the block's anchor at the finest level present.
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <new>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+#include "../../include/gmhd.h"
+
+namespace
+{
+struct Key
+{
+  int32_t L, x, y, z;
+};
+
+inline uint64_t
+pack(int L, int x, int y, int z)
+{
+  return ((uint64_t)(uint32_t)L << 57) | ((uint64_t)(uint32_t)x << 38) | ((uint64_t)(uint32_t)y << 19) |
+         (uint64_t)(uint32_t)z;
+}
+
+inline Key
+unpack(uint64_t k)
+{
+  return Key{(int)(k >> 57), (int)((k >> 38) & 0x7ffff), (int)((k >> 19) & 0x7ffff), (int)(k & 0x7ffff)};
+}
+
+struct Forest
+{
+  int dim = 3, bricks[3] = {1, 1, 1}, per[3] = {1, 1, 1}, base = 0;
+  int offs[26][3];
+  int noffs = 0;
+
+  void
+  init()
+  {
+    noffs = 0;
+    for (int oz = (dim == 3 ? -1 : 0); oz <= (dim == 3 ? 1 : 0); ++oz)
+      for (int oy = -1; oy <= 1; ++oy)
+        for (int ox = -1; ox <= 1; ++ox)
+          if (ox || oy || oz)
+          {
+            offs[noffs][0] = ox;
+            offs[noffs][1] = oy;
+            offs[noffs][2] = oz;
+            ++noffs;
+          }
+  }
+  int
+  ext(int L, int d) const
+  {
+    return d < dim ? bricks[d] << L : 1;
+  }
+  // wrap c (level L) on periodic axes; false when outside a non-periodic border
+  bool
+  wrap(int L, int * c) const
+  {
+    for (int d = 0; d < 3; ++d)
+    {
+      const int e = ext(L, d);
+      if (per[d])
+        c[d] = ((c[d] % e) + e) % e;
+      else if (c[d] < 0 || c[d] >= e)
+        return false;
+    }
+    return true;
+  }
+  int
+  nkids() const
+  {
+    return 1 << dim;
+  }
+  uint64_t
+  kid(const Key & k, int c) const
+  {
+    return pack(k.L + 1, 2 * k.x + (c & 1), 2 * k.y + ((c >> 1) & 1), 2 * k.z + ((c >> 2) & 1));
+  }
+
+  // refine leaves until every leaf's face/edge/corner neighbours are within one level
+  void
+  balance(std::unordered_set<uint64_t> & leaves) const
+  {
+    std::vector<uint64_t> work(leaves.begin(), leaves.end());
+    std::sort(work.begin(), work.end());
+    while (!work.empty())
+    {
+      const uint64_t kk = work.back();
+      work.pop_back();
+      if (!leaves.count(kk))
+        continue;
+      const Key k = unpack(kk);
+      if (k.L - 2 < base)
+        continue;
+      for (int o = 0; o < noffs; ++o)
+      {
+        int r[3] = {k.x + offs[o][0], k.y + offs[o][1], k.z + offs[o][2]};
+        if (!wrap(k.L, r))
+          continue;
+        for (int lv = k.L - 2; lv >= base; --lv)
+        {
+          const int      sh = k.L - lv;
+          const uint64_t anc = pack(lv, r[0] >> sh, r[1] >> sh, r[2] >> sh);
+          if (leaves.count(anc))
+          {
+            leaves.erase(anc);
+            const Key a = unpack(anc);
+            for (int c = 0; c < nkids(); ++c)
+            {
+              leaves.insert(kid(a, c));
+              work.push_back(kid(a, c));
+            }
+            work.push_back(kk);
+            break;
+          }
+        }
+      }
+    }
+  }
+};
+
+} // namespace
+
+struct gmhd_forest
+{
+  int                   dim = 3, bx = 0, by = 0, bz = 0;
+  int                   n_owned = 0, n_blocks = 0;
+  std::vector<int32_t>  level, coord, neighbor, fine, out_src, out_normal, remap;
+  std::vector<Key>      owned;
+};
+
+namespace
+{
+// mesh tables of a balanced leaf set
+void
+build(const Forest & f, const std::unordered_set<uint64_t> & leaves, gmhd_forest & out)
+{
+  int max_level = 0;
+  for (uint64_t k : leaves)
+    max_level = std::max(max_level, unpack(k).L);
+  struct Ord
+  {
+    uint64_t tree, morton;
+    int      L;
+    uint64_t key;
+  };
+  std::vector<Ord> ord;
+  ord.reserve(leaves.size());
+  for (uint64_t kk : leaves)
+  {
+    const Key k = unpack(kk);
+    const int t[3] = {k.x >> k.L, k.y >> k.L, k.z >> k.L};
+    const uint64_t tid = (uint64_t)t[0] + (uint64_t)f.bricks[0] * ((uint64_t)t[1] + (uint64_t)f.bricks[1] * t[2]);
+    const int      sh = max_level - k.L;
+    const uint64_t a[3] = {(uint64_t)(k.x - (t[0] << k.L)) << sh, (uint64_t)(k.y - (t[1] << k.L)) << sh,
+                           (uint64_t)(k.z - (t[2] << k.L)) << sh};
+    uint64_t m = 0;
+    for (int bit = 0; bit < std::max(max_level, 1); ++bit)
+      m |= ((a[0] >> bit) & 1) << (3 * bit) | ((a[1] >> bit) & 1) << (3 * bit + 1) | ((a[2] >> bit) & 1) << (3 * bit + 2);
+    ord.push_back(Ord{tid, m, k.L, kk});
+  }
+  std::sort(ord.begin(), ord.end(), [](const Ord & p, const Ord & q) {
+    if (p.tree != q.tree)
+      return p.tree < q.tree;
+    if (p.morton != q.morton)
+      return p.morton < q.morton;
+    return p.L < q.L;
+  });
+  std::unordered_map<uint64_t, int32_t> ids;
+  ids.reserve(ord.size() * 2);
+  out.owned.clear();
+  for (size_t n = 0; n < ord.size(); ++n)
+  {
+    ids[ord[n].key] = (int32_t)n;
+    out.owned.push_back(unpack(ord[n].key));
+  }
+  const int n_owned = (int)ord.size();
+  // outside blocks at the level of the block they serve, sourced from the same-level inside block
+  std::unordered_map<uint64_t, int32_t> out_ids;
+  std::vector<Key>                      out_keys;
+  out.out_src.clear();
+  out.out_normal.clear();
+  for (int b = 0; b < n_owned; ++b)
+  {
+    const Key k = out.owned[b];
+    for (int o = 0; o < f.noffs; ++o)
+    {
+      int c[3] = {k.x + f.offs[o][0], k.y + f.offs[o][1], k.z + f.offs[o][2]};
+      int w[3] = {c[0], c[1], c[2]};
+      if (f.wrap(k.L, w))
+        continue;
+      for (int d = 0; d < 3; ++d)
+        if (f.per[d])
+        {
+          const int e = f.ext(k.L, d);
+          w[d] = ((c[d] % e) + e) % e;
+        }
+        else
+          w[d] = c[d];
+      // outside coordinates can be -1: keep them in a separate map keyed by the signed triple
+      const uint64_t ok = pack(k.L, w[0] + 1, w[1] + 1, w[2] + 1);
+      if (out_ids.count(ok))
+        continue;
+      int src[3];
+      for (int d = 0; d < 3; ++d)
+        src[d] = std::min(std::max(w[d], 0), f.ext(k.L, d) - 1);
+      const auto it = ids.find(pack(k.L, src[0], src[1], src[2]));
+      if (it == ids.end())
+      {
+        out.n_owned = -1; // an outside block without a same-level inside block
+        return;
+      }
+      out_ids[ok] = n_owned + (int32_t)out_keys.size();
+      out_keys.push_back(Key{k.L, w[0], w[1], w[2]});
+      out.out_src.push_back(it->second);
+      for (int d = 0; d < 3; ++d)
+        out.out_normal.push_back(src[d] > w[d] ? 1 : (src[d] < w[d] ? -1 : 0));
+    }
+  }
+  const int n_blocks = n_owned + (int)out_keys.size();
+  out.n_owned = n_owned;
+  out.n_blocks = n_blocks;
+  out.level.assign(n_blocks, 0);
+  out.coord.assign((size_t)n_blocks * 3, 0);
+  out.neighbor.assign((size_t)n_blocks * 27, -1);
+  out.fine.assign((size_t)n_blocks * 27 * 8, -1);
+  for (int b = 0; b < n_blocks; ++b)
+  {
+    const Key k = b < n_owned ? out.owned[b] : out_keys[b - n_owned];
+    out.level[b] = k.L;
+    out.coord[3 * b] = k.x;
+    out.coord[3 * b + 1] = k.y;
+    out.coord[3 * b + 2] = k.z;
+  }
+  for (int b = 0; b < n_owned; ++b)
+  {
+    const Key k = out.owned[b];
+    out.neighbor[(size_t)b * 27 + 13] = b; // the block itself
+    for (int o = 0; o < f.noffs; ++o)
+    {
+      const int s = (f.offs[o][2] + 1) * 9 + (f.offs[o][1] + 1) * 3 + (f.offs[o][0] + 1);
+      int       r[3] = {k.x + f.offs[o][0], k.y + f.offs[o][1], k.z + f.offs[o][2]};
+      int       c[3] = {r[0], r[1], r[2]};
+      if (!f.wrap(k.L, r))
+      {
+        int w[3];
+        for (int d = 0; d < 3; ++d)
+        {
+          const int e = f.ext(k.L, d);
+          w[d] = f.per[d] ? ((c[d] % e) + e) % e : c[d];
+        }
+        out.neighbor[(size_t)b * 27 + s] = out_ids[pack(k.L, w[0] + 1, w[1] + 1, w[2] + 1)];
+        continue;
+      }
+      auto it = ids.find(pack(k.L, r[0], r[1], r[2]));
+      if (it != ids.end())
+      {
+        out.neighbor[(size_t)b * 27 + s] = it->second;
+        continue;
+      }
+      if (k.L >= 1)
+      {
+        it = ids.find(pack(k.L - 1, r[0] >> 1, r[1] >> 1, r[2] >> 1));
+        if (it != ids.end())
+        {
+          out.neighbor[(size_t)b * 27 + s] = it->second;
+          continue;
+        }
+      }
+      bool      found = false;
+      const Key rk{k.L, r[0], r[1], r[2]};
+      for (int ch = 0; ch < f.nkids(); ++ch)
+      {
+        it = ids.find(f.kid(rk, ch));
+        if (it != ids.end())
+        {
+          out.fine[((size_t)b * 27 + s) * 8 + ch] = it->second;
+          found = true;
+        }
+      }
+      if (!found)
+      {
+        out.n_owned = -2; // not 2:1 balanced
+        return;
+      }
+    }
+  }
+}
+
+} // namespace
+
+extern "C" {
+
+gmhd_forest *
+gmhd_forest_build(int32_t dim, const int32_t * bricks, const int32_t * periodic, int32_t bx, int32_t by, int32_t bz,
+                  int32_t level_min, int32_t level_max, int32_t n_leaves, const int32_t * keys, const int8_t * flags)
+{
+  if ((dim != 2 && dim != 3) || !bricks || !periodic || n_leaves <= 0 || !keys || level_min < 0 ||
+      level_max < level_min || level_max > 18 || bx < 4 || by < 4 || (dim == 3 && bz < 4) || bx % 2 || by % 2 ||
+      (dim == 3 && bz % 2))
+    return nullptr;
+  gmhd_forest * out = new (std::nothrow) gmhd_forest();
+  if (!out)
+    return nullptr;
+  Forest f;
+  f.dim = dim;
+  for (int d = 0; d < 3; ++d)
+  {
+    f.bricks[d] = d < dim ? bricks[d] : 1;
+    f.per[d] = d < dim ? (periodic[d] != 0) : 1;
+    if (f.bricks[d] < 1)
+    {
+      delete out;
+      return nullptr;
+    }
+  }
+  f.base = level_min;
+  f.init();
+  out->dim = dim;
+  out->bx = bx;
+  out->by = by;
+  out->bz = dim == 3 ? bz : 1;
+  std::vector<uint64_t>                old(n_leaves);
+  std::unordered_map<uint64_t, int32_t> old_id;
+  old_id.reserve((size_t)n_leaves * 2);
+  for (int n = 0; n < n_leaves; ++n)
+  {
+    const int32_t * k = keys + 4 * n;
+    if (k[0] < 0 || k[0] > 18 || k[1] < 0 || k[2] < 0 || k[3] < 0)
+    {
+      delete out;
+      return nullptr;
+    }
+    old[n] = pack(k[0], k[1], k[2], dim == 3 ? k[3] : 0);
+    old_id[old[n]] = n;
+  }
+  std::unordered_set<uint64_t> cand(old.begin(), old.end());
+  if (flags)
+  {
+    // refine flagged leaves, coarsen whole flagged families; undo a coarsening that balance refines again
+    std::unordered_set<uint64_t>                              refined;
+    std::unordered_map<uint64_t, std::vector<uint64_t>>       families;
+    for (int n = 0; n < n_leaves; ++n)
+    {
+      const Key k = unpack(old[n]);
+      if (flags[n] > 0 && k.L < level_max)
+        refined.insert(old[n]);
+      else if (flags[n] < 0 && k.L > level_min)
+        families[pack(k.L - 1, k.x >> 1, k.y >> 1, k.z >> 1)].push_back(old[n]);
+    }
+    std::unordered_set<uint64_t> coarsen;
+    for (auto & fam : families)
+      if ((int)fam.second.size() == f.nkids())
+        coarsen.insert(fam.first);
+    while (true)
+    {
+      cand = std::unordered_set<uint64_t>(old.begin(), old.end());
+      for (uint64_t kk : refined)
+      {
+        cand.erase(kk);
+        for (int c = 0; c < f.nkids(); ++c)
+          cand.insert(f.kid(unpack(kk), c));
+      }
+      for (uint64_t p : coarsen)
+      {
+        for (int c = 0; c < f.nkids(); ++c)
+          cand.erase(f.kid(unpack(p), c));
+        cand.insert(p);
+      }
+      f.balance(cand);
+      std::vector<uint64_t> undone;
+      for (uint64_t p : coarsen)
+        if (!cand.count(p))
+          undone.push_back(p);
+      if (undone.empty())
+        break;
+      for (uint64_t p : undone)
+        coarsen.erase(p);
+    }
+  }
+  else
+    f.balance(cand);
+  build(f, cand, *out);
+  if (out->n_owned < 0)
+  {
+    delete out;
+    return nullptr;
+  }
+  // remap rows: kind, sources, kept same-level leaves across the faces
+  out->remap.assign((size_t)out->n_owned * 15, -1);
+  for (int n = 0; n < out->n_owned; ++n)
+  {
+    int32_t * rm = &out->remap[(size_t)n * 15];
+    const Key k = out->owned[n];
+    const uint64_t kk = pack(k.L, k.x, k.y, k.z);
+    auto       it = old_id.find(kk);
+    if (it != old_id.end())
+    {
+      rm[0] = 0;
+      rm[1] = it->second;
+      continue;
+    }
+    if (k.L >= 1 && (it = old_id.find(pack(k.L - 1, k.x >> 1, k.y >> 1, k.z >> 1))) != old_id.end())
+    {
+      rm[0] = 1;
+      rm[1] = it->second;
+      rm[2] = (k.x & 1) + 2 * (k.y & 1) + 4 * (k.z & 1);
+    }
+    else
+    {
+      rm[0] = 2;
+      for (int c = 0; c < f.nkids(); ++c)
+      {
+        it = old_id.find(f.kid(k, c));
+        rm[1 + c] = it != old_id.end() ? it->second : -1;
+      }
+    }
+    for (int fc = 0; fc < 2 * dim; ++fc)
+    {
+      int r[3] = {k.x, k.y, k.z};
+      r[fc / 2] += fc % 2 == 0 ? -1 : 1;
+      if (!f.wrap(k.L, r))
+        continue;
+      const uint64_t rk = pack(k.L, r[0], r[1], r[2]);
+      if (old_id.count(rk) && cand.count(rk))
+        rm[9 + fc] = old_id[rk];
+    }
+  }
+  return out;
+}
+
+int
+gmhd_forest_sizes(const gmhd_forest * f, int32_t * n_owned, int32_t * n_blocks)
+{
+  if (!f || !n_owned || !n_blocks)
+    return GMHD_ERR_ARGUMENT;
+  *n_owned = f->n_owned;
+  *n_blocks = f->n_blocks;
+  return GMHD_OK;
+}
+
+int
+gmhd_forest_tables(const gmhd_forest * f, int32_t * level, int32_t * coord, int32_t * neighbor, int32_t * fine_neighbor,
+                   int32_t * outside_src, int32_t * outside_normal, int32_t * remap)
+{
+  if (!f)
+    return GMHD_ERR_ARGUMENT;
+  auto put = [](int32_t * dst, const std::vector<int32_t> & src) {
+    if (dst && !src.empty())
+      std::memcpy(dst, src.data(), src.size() * sizeof(int32_t));
+  };
+  put(level, f->level);
+  put(coord, f->coord);
+  put(neighbor, f->neighbor);
+  put(fine_neighbor, f->fine);
+  put(outside_src, f->out_src);
+  put(outside_normal, f->out_normal);
+  put(remap, f->remap);
+  return GMHD_OK;
+}
+
+void
+gmhd_forest_destroy(gmhd_forest * f)
+{
+  delete f;
+}
+
+} // extern "C"

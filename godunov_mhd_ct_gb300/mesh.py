@@ -205,8 +205,7 @@ class BlockMesh:
                 if refine(L, lo, hi):
                     leaves.remove(key)
                     leaves.update(f.kids(key))
-        f.balance(leaves)
-        return f.build(leaves, scaling_factor)
+        return f.native(sorted(leaves), None, base_level, max(max_level, base_level), scaling_factor)[0]
 
     def leaf_keys(self):
         """(level, cx, cy, cz) of the owned leaves, in block order."""
@@ -222,61 +221,7 @@ class BlockMesh:
         otherwise). Plays p4est's adapt + balance and the reference's AMR cycle
         (SolverGodunovMHD.cpp:263-319)."""
         f = _Forest(self.dim, self.bricks, self.periodic, level_min, self.block)
-        old = self.leaf_keys()
-        old_id = {k: n for n, k in enumerate(old)}
-        flags = np.asarray(flags).reshape(-1)
-        leaves = set(old)
-        refined = {k for n, k in enumerate(old) if flags[n] > 0 and k[0] < level_max}
-        nch = 1 << self.dim
-        parents = {}
-        for n, k in enumerate(old):
-            if flags[n] < 0 and k[0] > level_min:
-                par = (k[0] - 1, k[1] >> 1, k[2] >> 1, k[3] >> 1)
-                parents.setdefault(par, []).append(k)
-        coarsen = {p_ for p_, ch in parents.items() if len(ch) == nch}
-        while True:
-            cand = set(leaves)
-            for k in refined:
-                cand.discard(k)
-                cand.update(f.kids(k))
-            for p_ in coarsen:
-                for c in f.kids(p_):
-                    cand.discard(c)
-                cand.add(p_)
-            f.balance(cand)
-            undone = {p_ for p_ in coarsen if p_ not in cand}
-            if not undone:
-                break
-            coarsen -= undone
-        mesh = f.build(cand, self.scaling_factor)
-        new = mesh.leaf_keys()
-        new_set = set(new)
-        remap = -np.ones((len(new), 15), dtype=np.int32)
-        for n, k in enumerate(new):
-            if k in old_id:
-                remap[n, 0] = 0
-                remap[n, 1] = old_id[k]
-                continue
-            if (k[0] - 1, k[1] >> 1, k[2] >> 1, k[3] >> 1) in old_id:
-                par = (k[0] - 1, k[1] >> 1, k[2] >> 1, k[3] >> 1)
-                remap[n, 0] = 1
-                remap[n, 1] = old_id[par]
-                remap[n, 2] = (k[1] & 1) + 2 * (k[2] & 1) + 4 * (k[3] & 1)
-            else:
-                ch = f.kids(k)
-                if not all(c in old_id for c in ch):
-                    raise ValueError(f"new leaf {k} is neither kept, refined from nor coarsened to the old mesh")
-                remap[n, 0] = 2
-                for c_i, c in enumerate(ch):
-                    remap[n, 1 + c_i] = old_id[c]
-            # kept leaves at this level across the faces: their faces are copied
-            for fc in range(2 * self.dim):
-                o = [0, 0, 0]
-                o[fc // 2] = -1 if fc % 2 == 0 else 1
-                r = f.wrap(k[0], (k[1] + o[0], k[2] + o[1], k[3] + o[2]))
-                if r is not None and (k[0],) + r in old_id and (k[0],) + r in new_set:
-                    remap[n, 9 + fc] = old_id[(k[0],) + r]
-        return mesh, remap
+        return f.native(self.leaf_keys(), np.asarray(flags).reshape(-1), level_min, level_max, self.scaling_factor)
 
     @staticmethod
     def batch(meshes) -> tuple["BlockMesh", np.ndarray]:
@@ -356,8 +301,8 @@ class BlockMesh:
 
 
 class _Forest:
-    """Leaf-set operations of a brick forest: children, periodic wrap, 2:1 balance (faces, edges,
-    corners) and the construction of a BlockMesh (p4est order, neighbour and outside tables)."""
+    """Leaf-set helpers of a brick forest (children, periodic wrap); balance and the mesh tables come
+    from the native forest of libgmhd.so (gmhd_forest_build)."""
 
     def __init__(self, dim, bricks, periodic, base_level, block):
         if dim not in (2, 3):
@@ -394,106 +339,23 @@ class _Forest:
             out.append(v)
         return tuple(out)
 
-    def balance(self, leaves):
-        """Refine leaves (in place) until every leaf's face/edge/corner neighbours are within one level."""
-        changed = True
-        while changed:
-            changed = False
-            for key in sorted(leaves):
-                if key not in leaves or key[0] - 2 < self.base_level:
-                    continue
-                L = key[0]
-                for o in self.offs:
-                    r = self.wrap(L, (key[1] + o[0], key[2] + o[1], key[3] + o[2]))
-                    if r is None:
-                        continue
-                    for lv in range(L - 2, self.base_level - 1, -1):
-                        sh = L - lv
-                        anc = (lv, r[0] >> sh, r[1] >> sh, r[2] >> sh)
-                        if anc in leaves:
-                            leaves.remove(anc)
-                            leaves.update(self.kids(anc))
-                            changed = True
-                            break
+    def native(self, keys, flags, level_min, level_max, scaling_factor):
+        """Adapt (flags) or just balance the leaf set with the native forest (gmhd_forest_build) and
+        wrap its tables in a BlockMesh. Returns (mesh, remap rows)."""
+        from . import _native
 
-    def build(self, leaves, scaling_factor):
-        dim, bricks, per = self.dim, self.bricks, self.per
-        bx, by, bz = self.block
-        max_level = max(k[0] for k in leaves)
-
-        # p4est order: trees x fastest, then Morton order of the anchor at the finest level
-        def order_key(key):
-            L, cx, cy, cz = key
-            t = (cx >> L, cy >> L, cz >> L)
-            tid = t[0] + bricks[0] * (t[1] + bricks[1] * t[2])
-            sh = max_level - L
-            a = [((cx - (t[0] << L)) << sh), ((cy - (t[1] << L)) << sh), ((cz - (t[2] << L)) << sh)]
-            m = 0
-            for bit in range(max(max_level, 1)):
-                m |= ((a[0] >> bit) & 1) << (3 * bit) | ((a[1] >> bit) & 1) << (3 * bit + 1) | \
-                    ((a[2] >> bit) & 1) << (3 * bit + 2)
-            return (tid, m, L)
-
-        owned = sorted(leaves, key=order_key)
-        ids = {k: n for n, k in enumerate(owned)}
-        n_owned = len(owned)
-        out_keys, out_ids, out_src, out_normal = [], {}, [], []
-        for key in owned:
-            L = key[0]
-            e = self.ext(L)
-            for o in self.offs:
-                c = [key[1] + o[0], key[2] + o[1], key[3] + o[2]]
-                if self.wrap(L, c) is not None:
-                    continue
-                cw = [c[d] % e[d] if per[d] else c[d] for d in range(3)]
-                ok = (L, cw[0], cw[1], cw[2])
-                if ok in out_ids:
-                    continue
-                src = tuple(min(max(cw[d], 0), e[d] - 1) for d in range(3))
-                skey = (L,) + src
-                if skey not in ids:
-                    raise ValueError(f"outside block {ok} has no same-level inside leaf {skey}; keep the level "
-                                     "uniform along non-periodic borders")
-                out_ids[ok] = n_owned + len(out_keys)
-                out_keys.append(ok)
-                out_src.append(ids[skey])
-                out_normal.append(tuple(int(np.sign(src[d] - cw[d])) for d in range(3)))
-        all_keys = owned + out_keys
-        n_blocks = len(all_keys)
-        level = np.array([k[0] for k in all_keys], dtype=np.int32)
-        coords = np.array([k[1:] for k in all_keys], dtype=np.int64).reshape(-1, 3)
-        neighbor = -np.ones((n_blocks, 27), dtype=np.int32)
-        fine = -np.ones((n_blocks, 27, 8), dtype=np.int32)
-        any_jump = False
-        for b, key in enumerate(owned):
-            L = key[0]
-            e = self.ext(L)
-            for o in self.offs:
-                s_ = nb_slot(*o)
-                c = [key[1] + o[0], key[2] + o[1], key[3] + o[2]]
-                r = self.wrap(L, c)
-                if r is None:
-                    cw = tuple(c[d] % e[d] if per[d] else c[d] for d in range(3))
-                    neighbor[b, s_] = out_ids[(L,) + cw]
-                    continue
-                if (L,) + r in ids:
-                    neighbor[b, s_] = ids[(L,) + r]
-                    continue
-                par = (L - 1, r[0] >> 1, r[1] >> 1, r[2] >> 1)
-                if L - 1 >= 0 and par in ids:
-                    neighbor[b, s_] = ids[par]
-                    any_jump = True
-                    continue
-                found = False
-                for n, kk in enumerate(self.kids((L,) + r)):
-                    if kk in ids:
-                        fine[b, s_, n] = ids[kk]
-                        found = True
-                if not found:
-                    raise ValueError(f"neighbour region {r} of leaf {key} is not covered within one level")
-                any_jump = True
-        return BlockMesh(dim=dim, block=(bx, by, bz), level=level, neighbor=neighbor, coords=coords,
-                         n_owned=n_owned, grid=self.ext(max_level), periodic=per, scaling_factor=scaling_factor,
-                         outside_src=np.array(out_src, dtype=np.int32),
-                         outside_normal=np.array(out_normal, dtype=np.int32).reshape(-1, 3),
-                         fine_neighbor=fine if any_jump else None, bricks=bricks)
+        t = _native.forest_build(self.dim, self.bricks, self.per, self.block, level_min, level_max,
+                                 np.asarray(keys, dtype=np.int32).reshape(-1, 4), flags)
+        no = t["n_owned"]
+        lv = t["level"]
+        jump = bool(np.any(t["fine_neighbor"] >= 0))
+        if not jump:
+            own = t["neighbor"][:no]
+            ok = own >= 0
+            jump = bool(np.any(lv[own[ok]] != np.broadcast_to(lv[:no, None], own.shape)[ok]))
+        mesh = BlockMesh(dim=self.dim, block=self.block, level=lv, neighbor=t["neighbor"],
+                         coords=t["coord"].astype(np.int64), n_owned=no, grid=self.ext(int(lv[:no].max())),
+                         periodic=self.per, scaling_factor=scaling_factor, outside_src=t["outside_src"],
+                         outside_normal=t["outside_normal"], fine_neighbor=t["fine_neighbor"] if jump else None,
+                         bricks=self.bricks)
+        return mesh, t["remap"]

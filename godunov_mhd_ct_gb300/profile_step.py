@@ -21,6 +21,8 @@ def main():
                     help="ot: uniform Orszag-Tang; blast: 2D AMR blast; kh: 3D AMR shear layers with walls")
     ap.add_argument("--levels", default="5:8", help="base:max level of the AMR workloads")
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--regrid", type=int, default=0,
+                    help="AMR workloads: run --repeat solver iterations with an AMR cycle every REGRID steps")
     ap.add_argument("--repeat", type=int, default=1)
     args = ap.parse_args()
 
@@ -59,6 +61,28 @@ def main():
     for _ in range(args.warmup):
         impl.do_time_step(dU, dU2, dB, dB2, dt)
     torch.cuda.synchronize()
+    if args.regrid > 0 and args.workload != "ot":
+        # solver loop with AMR cycles (SolverGodunovMHD::next_iteration_impl): cell-updates over wall time
+        lo, hi = (int(v) for v in args.levels.split(":"))
+        crit = dict(criterion="LOHNER_UNSPLIT", eps_refine=0.16, eps_coarsen=0.02, eps_lohner=0.02,
+                    variables=("rho", "pressure"))
+        updates, done, t_regrid = 0, 0, 0.0
+        t0 = time.perf_counter()
+        while done < args.repeat:
+            n = min(args.regrid, args.repeat - done)
+            impl.advance(dU, torch.empty_like(dU), dB, torch.empty_like(dB), n)
+            updates += n * mesh.n_owned * mesh.ncell
+            done += n
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            mesh, dU, dB = impl.regrid(dU, dB, lo, hi, **crit)
+            t_regrid += time.perf_counter() - t1
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        print(f"{args.precision} {mesh.dim}D with an AMR cycle every {args.regrid} steps: {args.repeat} steps, "
+              f"{updates / el / 1e9:.3f} G cell-updates/s, regrid {t_regrid / el * 100:.1f} % of the time, "
+              f"final {mesh.n_owned} leaves, levels {np.bincount(mesh.level[: mesh.n_owned])[lo:]}")
+        return
     t0 = time.perf_counter()
     for _ in range(args.repeat):
         impl.do_time_step(dU, dU2, dB, dB2, dt)

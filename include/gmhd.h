@@ -242,6 +242,28 @@ int gmhd_remap(int32_t dim, int32_t bx, int32_t by, int32_t bz, int32_t n_old_bl
                const int32_t * remap, const double * U_old, const double * B_old, double * U_new, double * B_new,
                void * stream);
 
+/* --- host-side leaf forest (p4est's adapt + balance and the mesh tables; SolverGodunovMHD.cpp:263-319) --- */
+
+typedef struct gmhd_forest gmhd_forest;
+
+/* Leaves keys[n] = (level, x, y, z) (position at the level over bricks[0..2] root trees). With flags
+ * (one per leaf, -1 coarsen / 0 keep / +1 refine) the leaves are adapted first: flagged leaves below
+ * level_max are refined, complete families flagged above level_min are coarsened; then the set is
+ * 2:1 balanced across faces, edges and corners (refinement wins; a coarsening that balance would undo is
+ * dropped) and the tables of gmhd_mesh are built (p4est order, outside blocks for non-periodic axes).
+ * Without flags the keys are balanced and tabulated as given. Returns NULL on invalid input, on an
+ * outside block without a same-level inside block, or on exhaustion. */
+gmhd_forest * gmhd_forest_build(int32_t dim, const int32_t * bricks, const int32_t * periodic, int32_t bx, int32_t by,
+                                 int32_t bz, int32_t level_min, int32_t level_max, int32_t n_leaves,
+                                 const int32_t * keys, const int8_t * flags);
+int gmhd_forest_sizes(const gmhd_forest * forest, int32_t * n_owned, int32_t * n_blocks);
+/* Copies the tables (HOST arrays sized by gmhd_forest_sizes; any may be NULL): level[n_blocks],
+ * coord[3 n_blocks], neighbor[27 n_blocks], fine_neighbor[27 * 8 n_blocks], outside_src[n_blocks - n_owned],
+ * outside_normal[3 (n_blocks - n_owned)], remap[15 n_owned] (the rows gmhd_remap takes). */
+int  gmhd_forest_tables(const gmhd_forest * forest, int32_t * level, int32_t * coord, int32_t * neighbor,
+                        int32_t * fine_neighbor, int32_t * outside_src, int32_t * outside_normal, int32_t * remap);
+void gmhd_forest_destroy(gmhd_forest * forest);
+
 /* Stream-ordered gmhd_step_host (no counterpart in the reference; it exists for callers that keep the
  * state in host memory): copies U, B in, runs the step and copies the owned blocks of U2, B2 out, then
  * returns without waiting; the results are in U2/B2 once `stream` has completed the work enqueued

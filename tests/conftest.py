@@ -18,3 +18,12 @@ def oracle_lib():
 
     orc.build()
     return orc
+
+
+@pytest.fixture(scope="session", autouse=True)
+def native_library():
+    """libgmhd.so (the kernels, the C ABI and the host leaf forest the AMR mesh builders call);
+    compiled here when missing or stale (nvcc cross-compiles without a GPU)."""
+    from godunov_mhd_ct_gb300.csrc import build
+
+    build.build()

@@ -129,3 +129,41 @@ def test_workload_divergence_free_and_reproducible():
     rho0 = 25.0 / (36.0 * np.pi)
     r = U[:, 0] / rho0 - 1.0
     assert np.all(np.abs(r) <= 1e-3 + 1e-15) and np.std(r) > 2e-4
+
+
+@pytest.mark.parametrize("dim,periodic", [(2, (True, True, True)), (3, (True, True, True)), (2, (False, True, True)),
+                                          (3, (True, False, True))])
+def test_native_forest_matches_uniform_builder(native, dim, periodic):
+    """gmhd_forest_build on a uniform leaf set gives the uniform builder's tables (order, neighbours,
+    outside blocks)."""
+    block = (8, 8, 8 if dim == 3 else 1)
+    u = BlockMesh.uniform(dim, level=2, block=block, periodic=periodic)
+    t = native.forest_build(dim, u.bricks, u.periodic, u.block, 2, 2, np.array(u.leaf_keys(), np.int32))
+    n = u.n_owned
+    assert t["n_owned"] == n and len(t["level"]) == u.n_blocks
+    np.testing.assert_array_equal(t["coord"][:n], u.coords[:n])
+    np.testing.assert_array_equal(t["level"], u.level)
+    # owned neighbours by id; outside blocks (numbered differently) by their coordinates, source, normal
+    a, b = t["neighbor"][:n], u.neighbor[:n]
+    inside = b < n
+    np.testing.assert_array_equal(a[inside], b[inside])
+    ca = {tuple(t["coord"][x]) + (int(t["outside_src"][x - n]),) + tuple(t["outside_normal"][x - n]) for x in a[~inside]}
+    cb = {tuple(u.coords[x]) + (int(u.outside_src[x - n]),) + tuple(u.outside_normal[x - n]) for x in b[~inside]}
+    assert ca == cb
+    assert (t["fine_neighbor"] < 0).all()
+    np.testing.assert_array_equal(t["remap"][:, 0], 0)
+
+
+def test_native_forest_adapt_balances(native):
+    """Refining one leaf twice forces its neighbours to refine (2:1 across faces, edges, corners)."""
+    u = BlockMesh.uniform(2, level=2, block=(8, 8, 1))
+    m, _ = u.adapt(np.where(np.arange(u.n_owned) == 5, 1, 0), 2, 4)
+    m2, table = m.adapt(np.where(m.level[: m.n_owned] == 3, 1, 0), 2, 4)
+    for b in range(m2.n_owned):
+        for s in range(27):
+            n = m2.neighbor[b, s]
+            if n >= 0:
+                assert abs(int(m2.level[n]) - int(m2.level[b])) <= 1
+    assert set(np.unique(table[:, 0])) <= {0, 1}
+    assert np.bincount(m2.level[: m2.n_owned]).tolist()[2:] == [np.count_nonzero(m2.level == 2),
+                                                                np.count_nonzero(m2.level == 3), 16]
