@@ -82,7 +82,7 @@ def lib():
     L.gmhd_remap.argtypes = [ctypes.c_int32] * 6 + [vp] * 5 + [vp]
     L.gmhd_forest_build.restype = vp
     L.gmhd_forest_build.argtypes = [ctypes.c_int32, vp, vp] + [ctypes.c_int32] * 6 + [vp, vp]
-    L.gmhd_forest_sizes.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
+    L.gmhd_forest_sizes.argtypes = [vp] + [ctypes.POINTER(ctypes.c_int32)] * 3
     L.gmhd_forest_tables.argtypes = [vp] * 8
     L.gmhd_forest_destroy.argtypes = [vp]
     L.gmhd_last_status.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32)]
@@ -148,7 +148,8 @@ class MeshTables:
 
 def forest_build(dim, bricks, periodic, block, level_min, level_max, keys, flags=None):
     """Native leaf forest (gmhd_forest_build): returns a dict of numpy tables (level, coord, neighbor,
-    fine_neighbor [n_blocks, 27, 8], outside_src, outside_normal, remap [n_owned, 15], n_owned)."""
+    fine_neighbor [n_blocks, 27, 8] or None on a single-level leaf set, outside_src, outside_normal,
+    remap [n_owned, 15], n_owned)."""
     L = lib()
     keys = np.ascontiguousarray(np.asarray(keys, dtype=np.int32).reshape(-1, 4))
     br = np.ascontiguousarray(np.asarray(bricks, dtype=np.int32)[:3])
@@ -161,16 +162,17 @@ def forest_build(dim, bricks, periodic, block, level_min, level_max, keys, flags
         raise ValueError("gmhd_forest_build failed (invalid keys, or an outside block without a same-level inside "
                          "block: keep the level uniform along non-periodic borders)")
     try:
-        no, nb = ctypes.c_int32(), ctypes.c_int32()
-        check(L.gmhd_forest_sizes(h, ctypes.byref(no), ctypes.byref(nb)), "gmhd_forest_sizes")
+        no, nb, fine = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        check(L.gmhd_forest_sizes(h, ctypes.byref(no), ctypes.byref(nb), ctypes.byref(fine)), "gmhd_forest_sizes")
         no, nb = no.value, nb.value
-        t = {"level": np.zeros(nb, np.int32), "coord": np.zeros((nb, 3), np.int32),
-             "neighbor": np.zeros((nb, 27), np.int32), "fine_neighbor": np.zeros((nb, 27, 8), np.int32),
-             "outside_src": np.zeros(nb - no, np.int32), "outside_normal": np.zeros((nb - no, 3), np.int32),
-             "remap": np.zeros((no, 15), np.int32)}
-        check(L.gmhd_forest_tables(h, *(t[k].ctypes.data if t[k].size else None for k in
-                                        ("level", "coord", "neighbor", "fine_neighbor", "outside_src",
-                                         "outside_normal", "remap"))), "gmhd_forest_tables")
+        t = {"level": np.empty(nb, np.int32), "coord": np.empty((nb, 3), np.int32),
+             "neighbor": np.empty((nb, 27), np.int32),
+             "fine_neighbor": np.empty((nb, 27, 8), np.int32) if fine.value else None,
+             "outside_src": np.empty(nb - no, np.int32), "outside_normal": np.empty((nb - no, 3), np.int32),
+             "remap": np.empty((no, 15), np.int32)}
+        keys = ("level", "coord", "neighbor", "fine_neighbor", "outside_src", "outside_normal", "remap")
+        check(L.gmhd_forest_tables(h, *(t[k].ctypes.data if t[k] is not None and t[k].size else None
+                                        for k in keys)), "gmhd_forest_tables")
         t["n_owned"] = no
         return t
     finally:

@@ -9,8 +9,6 @@
 #include <cstdint>
 #include <cstring>
 #include <new>
-#include <unordered_map>
-#include <unordered_set>
 #include <vector>
 
 #include "../../include/gmhd.h"
@@ -34,6 +32,131 @@ unpack(uint64_t k)
 {
   return Key{(int)(k >> 57), (int)((k >> 38) & 0x7ffff), (int)((k >> 19) & 0x7ffff), (int)(k & 0x7ffff)};
 }
+
+// Open-addressing table of packed keys -> int32 (linear probing, Fibonacci hashing, backward-shift
+// erase). The all-ones key never occurs (levels stop at 18), so it marks an empty slot.
+class KeyTable
+{
+public:
+  explicit KeyTable(size_t n = 0) { rehash(capacity_for(n)); }
+
+  size_t
+  size() const
+  {
+    return n_;
+  }
+  const int32_t *
+  find(uint64_t k) const
+  {
+    for (size_t i = home(k);; i = (i + 1) & mask_)
+    {
+      if (keys_[i] == k)
+        return &vals_[i];
+      if (keys_[i] == EMPTY)
+        return nullptr;
+    }
+  }
+  bool
+  contains(uint64_t k) const
+  {
+    return find(k) != nullptr;
+  }
+  // insert, or overwrite the value of a present key; true when the key was new
+  bool
+  put(uint64_t k, int32_t v = 0)
+  {
+    if (2 * (n_ + 1) > keys_.size())
+      rehash(2 * keys_.size());
+    size_t i = home(k);
+    for (; keys_[i] != EMPTY; i = (i + 1) & mask_)
+      if (keys_[i] == k)
+      {
+        vals_[i] = v;
+        return false;
+      }
+    keys_[i] = k;
+    vals_[i] = v;
+    ++n_;
+    return true;
+  }
+  bool
+  erase(uint64_t k)
+  {
+    size_t i = home(k);
+    for (; keys_[i] != k; i = (i + 1) & mask_)
+      if (keys_[i] == EMPTY)
+        return false;
+    // shift the rest of the probe run back so that no lookup stops early at the hole
+    for (size_t j = (i + 1) & mask_; keys_[j] != EMPTY; j = (j + 1) & mask_)
+    {
+      const size_t h = home(keys_[j]);
+      const bool   stays = (i <= j) ? (i < h && h <= j) : (i < h || h <= j);
+      if (stays)
+        continue;
+      keys_[i] = keys_[j];
+      vals_[i] = vals_[j];
+      i = j;
+    }
+    keys_[i] = EMPTY;
+    --n_;
+    return true;
+  }
+  template <typename F>
+  void
+  for_each(F && f) const
+  {
+    for (size_t i = 0; i < keys_.size(); ++i)
+      if (keys_[i] != EMPTY)
+        f(keys_[i], vals_[i]);
+  }
+  std::vector<uint64_t>
+  keys() const
+  {
+    std::vector<uint64_t> out;
+    out.reserve(n_);
+    for_each([&](uint64_t k, int32_t) { out.push_back(k); });
+    return out;
+  }
+
+private:
+  static constexpr uint64_t EMPTY = ~0ull;
+  std::vector<uint64_t>     keys_;
+  std::vector<int32_t>      vals_;
+  size_t                    mask_ = 0, n_ = 0;
+  int                       shift_ = 60;
+
+  static size_t
+  capacity_for(size_t n)
+  {
+    size_t c = 16;
+    while (c < 2 * n + 2)
+      c <<= 1;
+    return c;
+  }
+  size_t
+  home(uint64_t k) const
+  {
+    return (size_t)((k * 0x9E3779B97F4A7C15ull) >> shift_);
+  }
+  void
+  rehash(size_t cap)
+  {
+    std::vector<uint64_t> ok;
+    std::vector<int32_t>  ov;
+    ok.swap(keys_);
+    ov.swap(vals_);
+    keys_.assign(cap, EMPTY);
+    vals_.assign(cap, 0);
+    mask_ = cap - 1;
+    shift_ = 64;
+    for (size_t c = cap; c > 1; c >>= 1)
+      --shift_;
+    n_ = 0;
+    for (size_t i = 0; i < ok.size(); ++i)
+      if (ok[i] != EMPTY)
+        put(ok[i], ov[i]);
+  }
+};
 
 struct Forest
 {
@@ -61,6 +184,16 @@ struct Forest
   {
     return d < dim ? bricks[d] << L : 1;
   }
+  // c mod e for the coordinates of neighbour regions (at most one block width outside [0, e))
+  static int
+  periodic(int c, int e)
+  {
+    if (c < 0)
+      c += e;
+    else if (c >= e)
+      c -= e;
+    return (c >= 0 && c < e) ? c : ((c % e) + e) % e;
+  }
   // wrap c (level L) on periodic axes; false when outside a non-periodic border
   bool
   wrap(int L, int * c) const
@@ -69,7 +202,7 @@ struct Forest
     {
       const int e = ext(L, d);
       if (per[d])
-        c[d] = ((c[d] % e) + e) % e;
+        c[d] = periodic(c[d], e);
       else if (c[d] < 0 || c[d] >= e)
         return false;
     }
@@ -88,15 +221,15 @@ struct Forest
 
   // refine leaves until every leaf's face/edge/corner neighbours are within one level
   void
-  balance(std::unordered_set<uint64_t> & leaves) const
+  balance(KeyTable & leaves) const
   {
-    std::vector<uint64_t> work(leaves.begin(), leaves.end());
+    std::vector<uint64_t> work = leaves.keys();
     std::sort(work.begin(), work.end());
     while (!work.empty())
     {
       const uint64_t kk = work.back();
       work.pop_back();
-      if (!leaves.count(kk))
+      if (!leaves.contains(kk))
         continue;
       const Key k = unpack(kk);
       if (k.L - 2 < base)
@@ -106,17 +239,19 @@ struct Forest
         int r[3] = {k.x + offs[o][0], k.y + offs[o][1], k.z + offs[o][2]};
         if (!wrap(k.L, r))
           continue;
+        // a leaf at L or L-1 covering r rules out a coarser one
+        if (leaves.contains(pack(k.L, r[0], r[1], r[2])) || leaves.contains(pack(k.L - 1, r[0] >> 1, r[1] >> 1, r[2] >> 1)))
+          continue;
         for (int lv = k.L - 2; lv >= base; --lv)
         {
           const int      sh = k.L - lv;
           const uint64_t anc = pack(lv, r[0] >> sh, r[1] >> sh, r[2] >> sh);
-          if (leaves.count(anc))
+          if (leaves.erase(anc))
           {
-            leaves.erase(anc);
             const Key a = unpack(anc);
             for (int c = 0; c < nkids(); ++c)
             {
-              leaves.insert(kid(a, c));
+              leaves.put(kid(a, c));
               work.push_back(kid(a, c));
             }
             work.push_back(kk);
@@ -134,7 +269,10 @@ struct gmhd_forest
 {
   int                   dim = 3, bx = 0, by = 0, bz = 0;
   int                   n_owned = 0, n_blocks = 0;
-  std::vector<int32_t>  level, coord, neighbor, fine, out_src, out_normal, remap;
+  bool                  has_fine = false;
+  std::vector<int32_t>  level, coord, neighbor, out_src, out_normal, remap;
+  std::vector<int64_t>  fine_at; // entries of the [n_blocks][27][8] children table that are not -1 ...
+  std::vector<int32_t>  fine_id; // ... and their values
   std::vector<Key>      owned;
 };
 
@@ -142,10 +280,11 @@ namespace
 {
 // mesh tables of a balanced leaf set
 void
-build(const Forest & f, const std::unordered_set<uint64_t> & leaves, gmhd_forest & out)
+build(const Forest & f, const KeyTable & leaves, gmhd_forest & out)
 {
-  int max_level = 0;
-  for (uint64_t k : leaves)
+  const std::vector<uint64_t> keys = leaves.keys();
+  int                         max_level = 0;
+  for (uint64_t k : keys)
     max_level = std::max(max_level, unpack(k).L);
   struct Ord
   {
@@ -154,8 +293,8 @@ build(const Forest & f, const std::unordered_set<uint64_t> & leaves, gmhd_forest
     uint64_t key;
   };
   std::vector<Ord> ord;
-  ord.reserve(leaves.size());
-  for (uint64_t kk : leaves)
+  ord.reserve(keys.size());
+  for (uint64_t kk : keys)
   {
     const Key k = unpack(kk);
     const int t[3] = {k.x >> k.L, k.y >> k.L, k.z >> k.L};
@@ -175,18 +314,18 @@ build(const Forest & f, const std::unordered_set<uint64_t> & leaves, gmhd_forest
       return p.morton < q.morton;
     return p.L < q.L;
   });
-  std::unordered_map<uint64_t, int32_t> ids;
-  ids.reserve(ord.size() * 2);
+  KeyTable ids(ord.size());
   out.owned.clear();
+  out.owned.reserve(ord.size());
   for (size_t n = 0; n < ord.size(); ++n)
   {
-    ids[ord[n].key] = (int32_t)n;
+    ids.put(ord[n].key, (int32_t)n);
     out.owned.push_back(unpack(ord[n].key));
   }
   const int n_owned = (int)ord.size();
   // outside blocks at the level of the block they serve, sourced from the same-level inside block
-  std::unordered_map<uint64_t, int32_t> out_ids;
-  std::vector<Key>                      out_keys;
+  KeyTable         out_ids;
+  std::vector<Key> out_keys;
   out.out_src.clear();
   out.out_normal.clear();
   for (int b = 0; b < n_owned; ++b)
@@ -200,28 +339,25 @@ build(const Forest & f, const std::unordered_set<uint64_t> & leaves, gmhd_forest
         continue;
       for (int d = 0; d < 3; ++d)
         if (f.per[d])
-        {
-          const int e = f.ext(k.L, d);
-          w[d] = ((c[d] % e) + e) % e;
-        }
+          w[d] = Forest::periodic(c[d], f.ext(k.L, d));
         else
           w[d] = c[d];
       // outside coordinates can be -1: keep them in a separate map keyed by the signed triple
       const uint64_t ok = pack(k.L, w[0] + 1, w[1] + 1, w[2] + 1);
-      if (out_ids.count(ok))
+      if (out_ids.contains(ok))
         continue;
       int src[3];
       for (int d = 0; d < 3; ++d)
         src[d] = std::min(std::max(w[d], 0), f.ext(k.L, d) - 1);
-      const auto it = ids.find(pack(k.L, src[0], src[1], src[2]));
-      if (it == ids.end())
+      const int32_t * it = ids.find(pack(k.L, src[0], src[1], src[2]));
+      if (!it)
       {
         out.n_owned = -1; // an outside block without a same-level inside block
         return;
       }
-      out_ids[ok] = n_owned + (int32_t)out_keys.size();
+      out_ids.put(ok, n_owned + (int32_t)out_keys.size());
       out_keys.push_back(Key{k.L, w[0], w[1], w[2]});
-      out.out_src.push_back(it->second);
+      out.out_src.push_back(*it);
       for (int d = 0; d < 3; ++d)
         out.out_normal.push_back(src[d] > w[d] ? 1 : (src[d] < w[d] ? -1 : 0));
     }
@@ -232,7 +368,8 @@ build(const Forest & f, const std::unordered_set<uint64_t> & leaves, gmhd_forest
   out.level.assign(n_blocks, 0);
   out.coord.assign((size_t)n_blocks * 3, 0);
   out.neighbor.assign((size_t)n_blocks * 27, -1);
-  out.fine.assign((size_t)n_blocks * 27 * 8, -1);
+  out.fine_at.clear();
+  out.fine_id.clear();
   for (int b = 0; b < n_blocks; ++b)
   {
     const Key k = b < n_owned ? out.owned[b] : out_keys[b - n_owned];
@@ -255,38 +392,32 @@ build(const Forest & f, const std::unordered_set<uint64_t> & leaves, gmhd_forest
         int w[3];
         for (int d = 0; d < 3; ++d)
         {
-          const int e = f.ext(k.L, d);
-          w[d] = f.per[d] ? ((c[d] % e) + e) % e : c[d];
+          w[d] = f.per[d] ? Forest::periodic(c[d], f.ext(k.L, d)) : c[d];
         }
-        out.neighbor[(size_t)b * 27 + s] = out_ids[pack(k.L, w[0] + 1, w[1] + 1, w[2] + 1)];
+        out.neighbor[(size_t)b * 27 + s] = *out_ids.find(pack(k.L, w[0] + 1, w[1] + 1, w[2] + 1));
         continue;
       }
-      auto it = ids.find(pack(k.L, r[0], r[1], r[2]));
-      if (it != ids.end())
+      const int32_t * it = ids.find(pack(k.L, r[0], r[1], r[2]));
+      if (it)
       {
-        out.neighbor[(size_t)b * 27 + s] = it->second;
+        out.neighbor[(size_t)b * 27 + s] = *it;
         continue;
       }
-      if (k.L >= 1)
+      if (k.L >= 1 && (it = ids.find(pack(k.L - 1, r[0] >> 1, r[1] >> 1, r[2] >> 1))))
       {
-        it = ids.find(pack(k.L - 1, r[0] >> 1, r[1] >> 1, r[2] >> 1));
-        if (it != ids.end())
-        {
-          out.neighbor[(size_t)b * 27 + s] = it->second;
-          continue;
-        }
+        out.neighbor[(size_t)b * 27 + s] = *it;
+        continue;
       }
       bool      found = false;
       const Key rk{k.L, r[0], r[1], r[2]};
       for (int ch = 0; ch < f.nkids(); ++ch)
-      {
-        it = ids.find(f.kid(rk, ch));
-        if (it != ids.end())
+        if ((it = ids.find(f.kid(rk, ch))))
         {
-          out.fine[((size_t)b * 27 + s) * 8 + ch] = it->second;
+          out.fine_at.push_back(((int64_t)b * 27 + s) * 8 + ch);
+          out.fine_id.push_back(*it);
           found = true;
         }
-      }
+      out.has_fine = out.has_fine || found;
       if (!found)
       {
         out.n_owned = -2; // not 2:1 balanced
@@ -329,9 +460,8 @@ gmhd_forest_build(int32_t dim, const int32_t * bricks, const int32_t * periodic,
   out->bx = bx;
   out->by = by;
   out->bz = dim == 3 ? bz : 1;
-  std::vector<uint64_t>                old(n_leaves);
-  std::unordered_map<uint64_t, int32_t> old_id;
-  old_id.reserve((size_t)n_leaves * 2);
+  std::vector<uint64_t> old(n_leaves);
+  KeyTable              old_id(n_leaves);
   for (int n = 0; n < n_leaves; ++n)
   {
     const int32_t * k = keys + 4 * n;
@@ -341,54 +471,62 @@ gmhd_forest_build(int32_t dim, const int32_t * bricks, const int32_t * periodic,
       return nullptr;
     }
     old[n] = pack(k[0], k[1], k[2], dim == 3 ? k[3] : 0);
-    old_id[old[n]] = n;
+    old_id.put(old[n], n);
   }
-  std::unordered_set<uint64_t> cand(old.begin(), old.end());
+  KeyTable cand(n_leaves);
   if (flags)
   {
     // refine flagged leaves, coarsen whole flagged families; undo a coarsening that balance refines again
-    std::unordered_set<uint64_t>                              refined;
-    std::unordered_map<uint64_t, std::vector<uint64_t>>       families;
+    std::vector<uint64_t> refined, coarsen;
+    KeyTable              family;
     for (int n = 0; n < n_leaves; ++n)
     {
       const Key k = unpack(old[n]);
       if (flags[n] > 0 && k.L < level_max)
-        refined.insert(old[n]);
+        refined.push_back(old[n]);
       else if (flags[n] < 0 && k.L > level_min)
-        families[pack(k.L - 1, k.x >> 1, k.y >> 1, k.z >> 1)].push_back(old[n]);
+      {
+        const uint64_t  p = pack(k.L - 1, k.x >> 1, k.y >> 1, k.z >> 1);
+        const int32_t * c = family.find(p);
+        family.put(p, c ? *c + 1 : 1);
+      }
     }
-    std::unordered_set<uint64_t> coarsen;
-    for (auto & fam : families)
-      if ((int)fam.second.size() == f.nkids())
-        coarsen.insert(fam.first);
+    family.for_each([&](uint64_t p, int32_t c) {
+      if (c == f.nkids())
+        coarsen.push_back(p);
+    });
+    std::sort(coarsen.begin(), coarsen.end());
     while (true)
     {
-      cand = std::unordered_set<uint64_t>(old.begin(), old.end());
+      cand = KeyTable(n_leaves + refined.size() * f.nkids());
+      for (uint64_t kk : old)
+        cand.put(kk);
       for (uint64_t kk : refined)
       {
         cand.erase(kk);
         for (int c = 0; c < f.nkids(); ++c)
-          cand.insert(f.kid(unpack(kk), c));
+          cand.put(f.kid(unpack(kk), c));
       }
       for (uint64_t p : coarsen)
       {
         for (int c = 0; c < f.nkids(); ++c)
           cand.erase(f.kid(unpack(p), c));
-        cand.insert(p);
+        cand.put(p);
       }
       f.balance(cand);
-      std::vector<uint64_t> undone;
-      for (uint64_t p : coarsen)
-        if (!cand.count(p))
-          undone.push_back(p);
-      if (undone.empty())
+      const size_t before = coarsen.size();
+      coarsen.erase(std::remove_if(coarsen.begin(), coarsen.end(), [&](uint64_t p) { return !cand.contains(p); }),
+                    coarsen.end());
+      if (coarsen.size() == before)
         break;
-      for (uint64_t p : undone)
-        coarsen.erase(p);
     }
   }
   else
+  {
+    for (uint64_t kk : old)
+      cand.put(kk);
     f.balance(cand);
+  }
   build(f, cand, *out);
   if (out->n_owned < 0)
   {
@@ -402,17 +540,17 @@ gmhd_forest_build(int32_t dim, const int32_t * bricks, const int32_t * periodic,
     int32_t * rm = &out->remap[(size_t)n * 15];
     const Key k = out->owned[n];
     const uint64_t kk = pack(k.L, k.x, k.y, k.z);
-    auto       it = old_id.find(kk);
-    if (it != old_id.end())
+    const int32_t * it = old_id.find(kk);
+    if (it)
     {
       rm[0] = 0;
-      rm[1] = it->second;
+      rm[1] = *it;
       continue;
     }
-    if (k.L >= 1 && (it = old_id.find(pack(k.L - 1, k.x >> 1, k.y >> 1, k.z >> 1))) != old_id.end())
+    if (k.L >= 1 && (it = old_id.find(pack(k.L - 1, k.x >> 1, k.y >> 1, k.z >> 1))))
     {
       rm[0] = 1;
-      rm[1] = it->second;
+      rm[1] = *it;
       rm[2] = (k.x & 1) + 2 * (k.y & 1) + 4 * (k.z & 1);
     }
     else
@@ -421,7 +559,7 @@ gmhd_forest_build(int32_t dim, const int32_t * bricks, const int32_t * periodic,
       for (int c = 0; c < f.nkids(); ++c)
       {
         it = old_id.find(f.kid(k, c));
-        rm[1 + c] = it != old_id.end() ? it->second : -1;
+        rm[1 + c] = it ? *it : -1;
       }
     }
     for (int fc = 0; fc < 2 * dim; ++fc)
@@ -431,20 +569,23 @@ gmhd_forest_build(int32_t dim, const int32_t * bricks, const int32_t * periodic,
       if (!f.wrap(k.L, r))
         continue;
       const uint64_t rk = pack(k.L, r[0], r[1], r[2]);
-      if (old_id.count(rk) && cand.count(rk))
-        rm[9 + fc] = old_id[rk];
+      const int32_t * kept = old_id.find(rk);
+      if (kept && cand.contains(rk))
+        rm[9 + fc] = *kept;
     }
   }
   return out;
 }
 
 int
-gmhd_forest_sizes(const gmhd_forest * f, int32_t * n_owned, int32_t * n_blocks)
+gmhd_forest_sizes(const gmhd_forest * f, int32_t * n_owned, int32_t * n_blocks, int32_t * has_fine)
 {
   if (!f || !n_owned || !n_blocks)
     return GMHD_ERR_ARGUMENT;
   *n_owned = f->n_owned;
   *n_blocks = f->n_blocks;
+  if (has_fine)
+    *has_fine = f->has_fine ? 1 : 0;
   return GMHD_OK;
 }
 
@@ -461,7 +602,12 @@ gmhd_forest_tables(const gmhd_forest * f, int32_t * level, int32_t * coord, int3
   put(level, f->level);
   put(coord, f->coord);
   put(neighbor, f->neighbor);
-  put(fine_neighbor, f->fine);
+  if (fine_neighbor)
+  {
+    std::memset(fine_neighbor, 0xff, sizeof(int32_t) * (size_t)f->n_blocks * 27 * 8);
+    for (size_t i = 0; i < f->fine_at.size(); ++i)
+      fine_neighbor[f->fine_at[i]] = f->fine_id[i];
+  }
   put(outside_src, f->out_src);
   put(outside_normal, f->out_normal);
   put(remap, f->remap);

@@ -7,6 +7,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/gmhd.h"
@@ -63,6 +64,8 @@ struct gmhd_ctx
   int             mesh_version = 0, graph_mesh_version = -1;
   uint64_t        bytes = 0;
   int             last_cuda = 0;
+  // bytes reserved behind every device buffer of the context (buffers are reused across meshes)
+  std::unordered_map<const void *, size_t> cap;
   // coarse/fine meshes: virtual neighbour blocks, two-pass tile lists, fine-side data
   bool      amr = false;
   int       n_virtual = 0, n_list1 = 0, n_list2 = 0, flux_face_stride = 0;
@@ -102,79 +105,94 @@ cuda_fail(gmhd_ctx * c, cudaError_t e)
   } while (0)
 
 template <typename T>
+void
+drelease(gmhd_ctx * ctx, T ** ptr)
+{
+  if (!*ptr)
+    return;
+  auto it = ctx->cap.find((const void *)*ptr);
+  if (it != ctx->cap.end())
+  {
+    ctx->bytes -= it->second;
+    ctx->cap.erase(it);
+  }
+  cudaFree((void *)*ptr);
+  *ptr = nullptr;
+}
+
+// Device buffers outlive a mesh: a buffer is reallocated only when the new size does not fit, then
+// with a quarter of headroom, so that an AMR cycle every few steps costs no cudaMalloc / cudaFree.
+template <typename T>
 int
 dalloc(gmhd_ctx * ctx, T ** ptr, size_t count)
 {
+  const size_t need = count * sizeof(T);
+  size_t       take = need;
   if (*ptr)
   {
-    cudaFree(*ptr);
-    *ptr = nullptr;
+    const auto   it = ctx->cap.find((const void *)*ptr);
+    const size_t have = it != ctx->cap.end() ? it->second : 0;
+    if (need <= have)
+      return GMHD_OK;
+    take = need + need / 4;
+    drelease(ctx, ptr);
   }
   if (count == 0)
     return GMHD_OK;
-  GMHD_CUDA(cudaMalloc((void **)ptr, count * sizeof(T)));
-  ctx->bytes += count * sizeof(T);
+  GMHD_CUDA(cudaMalloc((void **)ptr, take));
+  ctx->cap[(const void *)*ptr] = take;
+  ctx->bytes += take;
   return GMHD_OK;
 }
 
 void
-dfree(void * p)
+release_amr(gmhd_ctx * c)
 {
-  if (p)
-    cudaFree(p);
+  drelease(c, &c->d_kind);
+  drelease(c, &c->d_fine);
+  drelease(c, &c->d_coord);
+  drelease(c, &c->d_vmap);
+  drelease(c, &c->d_nbr_real);
+  drelease(c, &c->d_list1);
+  drelease(c, &c->d_list2);
+  drelease(c, &c->d_flux_slot);
+  drelease(c, &c->d_emf_slot);
+  drelease(c, &c->d_Uv);
+  drelease(c, &c->d_Bv);
+  drelease(c, &c->d_Bccv);
+  drelease(c, &c->d_flux_side);
+  drelease(c, &c->d_emf_side);
 }
 
+// forget the mesh (tables, graph, coarse/fine state) but keep the device buffers
 void
-free_mesh(gmhd_ctx * c)
+reset_mesh(gmhd_ctx * c)
 {
-  dfree(c->d_neighbor);
-  dfree(c->d_level);
-  dfree(c->d_problem);
-  dfree(c->d_out_src);
-  dfree(c->d_out_normal);
-  dfree(c->d_invdt);
-  dfree(c->d_dt);
-  dfree(c->d_t);
-  dfree(c->d_tend);
-  dfree(c->d_counter);
-  dfree(c->d_dtlog);
-  dfree(c->d_U);
-  dfree(c->d_U2);
-  dfree(c->d_B);
-  dfree(c->d_B2);
-  c->d_neighbor = c->d_level = c->d_problem = c->d_out_src = c->d_out_normal = nullptr;
-  c->d_invdt = nullptr;
-  c->d_dt = c->d_t = c->d_tend = c->d_dtlog = nullptr;
-  c->d_counter = nullptr;
-  c->d_U = c->d_U2 = c->d_B = c->d_B2 = nullptr;
-  dfree(c->d_Urk);
-  dfree(c->d_Brk);
-  c->d_Urk = c->d_Brk = nullptr;
-  for (int k = 0; k < 2; ++k)
-  {
-    dfree(c->a_U[k]);
-    dfree(c->a_U2[k]);
-    dfree(c->a_B[k]);
-    dfree(c->a_B2[k]);
-    c->a_U[k] = c->a_U2[k] = c->a_B[k] = c->a_B2[k] = nullptr;
-  }
-  for (void * p : {(void *)c->d_kind, (void *)c->d_fine, (void *)c->d_coord, (void *)c->d_vmap, (void *)c->d_nbr_real,
-                   (void *)c->d_list1, (void *)c->d_list2, (void *)c->d_flux_slot, (void *)c->d_emf_slot,
-                   (void *)c->d_Uv, (void *)c->d_Bv, (void *)c->d_Bccv, (void *)c->d_flux_side, (void *)c->d_emf_side})
-    dfree(p);
-  c->d_kind = nullptr;
-  c->d_fine = c->d_coord = c->d_vmap = c->d_nbr_real = c->d_list1 = c->d_list2 = c->d_flux_slot = c->d_emf_slot = nullptr;
-  c->d_Uv = c->d_Bv = c->d_Bccv = c->d_flux_side = c->d_emf_side = nullptr;
   c->amr = false;
   c->n_virtual = c->n_list1 = c->n_list2 = c->flux_face_stride = 0;
-  c->dtlog_cap = 0;
-  c->bytes = sizeof(unsigned int);
   if (c->graph_exec)
   {
     cudaGraphExecDestroy(c->graph_exec);
     c->graph_exec = nullptr;
   }
   c->has_mesh = false;
+}
+
+void
+release_all(gmhd_ctx * c)
+{
+  reset_mesh(c);
+  for (int32_t ** p : {&c->d_neighbor, &c->d_level, &c->d_problem, &c->d_out_src, &c->d_out_normal, &c->d_counter})
+    drelease(c, p);
+  drelease(c, &c->d_invdt);
+  for (double ** p : {&c->d_dt, &c->d_t, &c->d_tend, &c->d_dtlog, &c->d_U, &c->d_U2, &c->d_B, &c->d_B2, &c->d_Urk,
+                      &c->d_Brk})
+    drelease(c, p);
+  for (int k = 0; k < 2; ++k)
+    for (double ** p : {&c->a_U[k], &c->a_U2[k], &c->a_B[k], &c->a_B2[k]})
+      drelease(c, p);
+  release_amr(c);
+  c->dtlog_cap = 0;
 }
 
 gmhd::StepArgs
@@ -750,8 +768,9 @@ gmhd_destroy(gmhd_ctx * ctx)
     cudaStreamSynchronize(ctx->a_run);
   if (ctx->a_out)
     cudaStreamSynchronize(ctx->a_out);
-  free_mesh(ctx);
-  dfree(ctx->d_health);
+  release_all(ctx);
+  if (ctx->d_health)
+    cudaFree(ctx->d_health);
   if (ctx->own_stream)
     cudaStreamDestroy(ctx->own_stream);
   for (cudaStream_t st : {ctx->a_in, ctx->a_run, ctx->a_out})
@@ -855,7 +874,13 @@ gmhd_set_mesh(gmhd_ctx * ctx, const gmhd_mesh * m)
     if (m->outside_src[o] < 0 || m->outside_src[o] >= m->n_owned)
       return GMHD_ERR_MESH;
 
-  free_mesh(ctx);
+  // work queued on any stream may still read the old tables: wait for it before reusing the buffers
+  GMHD_CUDA(cudaDeviceSynchronize());
+  reset_mesh(ctx);
+  if (!amr)
+    release_amr(ctx);
+  if (!m->problem)
+    drelease(ctx, &ctx->d_problem);
   ctx->dim = m->dim;
   ctx->bx = m->bx;
   ctx->by = m->by;
@@ -996,7 +1021,7 @@ gmhd_advance(gmhd_ctx * ctx, double * U, double * U2, double * B, double * B2, i
       ctx->graph_exec = nullptr;
     }
   }
-  if (ctx->p.time_integrator == GMHD_TIME_RK2_SSP && !ctx->d_Urk)
+  if (ctx->p.time_integrator == GMHD_TIME_RK2_SSP)
   {
     if ((rc = dalloc(ctx, &ctx->d_Urk, (size_t)ctx->n_blocks * 5 * ctx->ncell)) ||
         (rc = dalloc(ctx, &ctx->d_Brk, (size_t)ctx->n_blocks * ctx->nface)))
@@ -1087,7 +1112,6 @@ gmhd_step_host(gmhd_ctx * ctx, const double * U, double * U2, const double * B, 
   const size_t nu = (size_t)ctx->n_blocks * 5 * ctx->ncell;
   const size_t nb = (size_t)ctx->n_blocks * ctx->nface;
   int          rc;
-  if (!ctx->d_U)
   {
     if ((rc = dalloc(ctx, &ctx->d_U, nu)) || (rc = dalloc(ctx, &ctx->d_U2, nu)) || (rc = dalloc(ctx, &ctx->d_B, nb)) ||
         (rc = dalloc(ctx, &ctx->d_B2, nb)))
@@ -1132,7 +1156,6 @@ gmhd_step_host_async(gmhd_ctx * ctx, const double * U, double * U2, const double
     }
   }
   const int k = ctx->a_next;
-  if (!ctx->a_U[k])
   {
     if ((rc = dalloc(ctx, &ctx->a_U[k], nu)) || (rc = dalloc(ctx, &ctx->a_U2[k], nu)) ||
         (rc = dalloc(ctx, &ctx->a_B[k], nb)) || (rc = dalloc(ctx, &ctx->a_B2[k], nb)))

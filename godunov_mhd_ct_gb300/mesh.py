@@ -208,8 +208,9 @@ class BlockMesh:
         return f.native(sorted(leaves), None, base_level, max(max_level, base_level), scaling_factor)[0]
 
     def leaf_keys(self):
-        """(level, cx, cy, cz) of the owned leaves, in block order."""
-        return [(int(self.level[b]),) + tuple(int(v) for v in self.coords[b]) for b in range(self.n_owned)]
+        """int32 [n_owned, 4]: (level, cx, cy, cz) of the owned leaves, in block order."""
+        n = self.n_owned
+        return np.concatenate([self.level[:n, None].astype(np.int32), self.coords[:n].astype(np.int32)], axis=1)
 
     def adapt(self, flags, level_min: int, level_max: int):
         """Refine (flag > 0) and coarsen (flag < 0, whole families only) the owned leaves, then
@@ -271,11 +272,15 @@ class BlockMesh:
         return bm, problem
 
     # ---- layout helpers -------------------------------------------------------------------------
-    def alloc_state(self):
-        """Zeroed U [n_blocks, 5, bz, by, bx] and B [n_blocks, nface] (C-ABI layout, FP64)."""
+    def state_shapes(self):
+        """Shapes of U [n_blocks, 5, bz, by, bx] and B [n_blocks, nface] (C-ABI layout)."""
         bx, by, bz = self.block
-        return (np.zeros((self.n_blocks, 5, bz, by, bx), dtype=np.float64),
-                np.zeros((self.n_blocks, self.nface), dtype=np.float64))
+        return (self.n_blocks, 5, bz, by, bx), (self.n_blocks, self.nface)
+
+    def alloc_state(self):
+        """Zeroed U and B of state_shapes() (FP64)."""
+        us, bs = self.state_shapes()
+        return np.zeros(us, dtype=np.float64), np.zeros(bs, dtype=np.float64)
 
     def split_faces(self, B: np.ndarray):
         """Views (Bx, By, Bz) of a face array [n_blocks, nface] with shapes (z, y, x)."""
@@ -348,14 +353,11 @@ class _Forest:
                                  np.asarray(keys, dtype=np.int32).reshape(-1, 4), flags)
         no = t["n_owned"]
         lv = t["level"]
-        jump = bool(np.any(t["fine_neighbor"] >= 0))
-        if not jump:
-            own = t["neighbor"][:no]
-            ok = own >= 0
-            jump = bool(np.any(lv[own[ok]] != np.broadcast_to(lv[:no, None], own.shape)[ok]))
+        # in a 2:1-balanced leaf set every coarser neighbour sees this leaf's region as finer, so the
+        # fine table is present exactly when levels jump
         mesh = BlockMesh(dim=self.dim, block=self.block, level=lv, neighbor=t["neighbor"],
                          coords=t["coord"].astype(np.int64), n_owned=no, grid=self.ext(int(lv[:no].max())),
                          periodic=self.per, scaling_factor=scaling_factor, outside_src=t["outside_src"],
-                         outside_normal=t["outside_normal"], fine_neighbor=t["fine_neighbor"] if jump else None,
+                         outside_normal=t["outside_normal"], fine_neighbor=t["fine_neighbor"],
                          bricks=self.bricks)
         return mesh, t["remap"]

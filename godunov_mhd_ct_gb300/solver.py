@@ -151,9 +151,9 @@ class GodunovImplemGB300:
             raise ValueError("regrid works on single-problem meshes")
         flags = self.refine_flags(U, B, level_min=level_min, level_max=level_max, stream=stream, **criterion)
         new_mesh, table = self.mesh.adapt(flags, level_min, level_max)
-        us, bs = new_mesh.alloc_state()
-        Un = torch.zeros(us.shape, dtype=torch.float64, device=U.device)
-        Bn = torch.zeros(bs.shape, dtype=torch.float64, device=U.device)
+        us, bs = new_mesh.state_shapes()
+        Un = torch.zeros(us, dtype=torch.float64, device=U.device)
+        Bn = torch.zeros(bs, dtype=torch.float64, device=U.device)
         table = np.ascontiguousarray(table, dtype=np.int32)
         bx, by, bz = self.mesh.block
         nat.check(self._lib.gmhd_remap(self.mesh.dim, bx, by, bz, self.mesh.n_blocks, new_mesh.n_owned,

@@ -256,7 +256,9 @@ typedef struct gmhd_forest gmhd_forest;
 gmhd_forest * gmhd_forest_build(int32_t dim, const int32_t * bricks, const int32_t * periodic, int32_t bx, int32_t by,
                                  int32_t bz, int32_t level_min, int32_t level_max, int32_t n_leaves,
                                  const int32_t * keys, const int8_t * flags);
-int gmhd_forest_sizes(const gmhd_forest * forest, int32_t * n_owned, int32_t * n_blocks);
+/* Block counts of the tabulated leaf set; *has_fine (may be NULL) is 1 when some neighbour region is
+ * split into finer leaves (a coarse/fine mesh: fine_neighbor is needed), else 0. */
+int gmhd_forest_sizes(const gmhd_forest * forest, int32_t * n_owned, int32_t * n_blocks, int32_t * has_fine);
 /* Copies the tables (HOST arrays sized by gmhd_forest_sizes; any may be NULL): level[n_blocks],
  * coord[3 n_blocks], neighbor[27 n_blocks], fine_neighbor[27 * 8 n_blocks], outside_src[n_blocks - n_owned],
  * outside_normal[3 (n_blocks - n_owned)], remap[15 n_owned] (the rows gmhd_remap takes). */
