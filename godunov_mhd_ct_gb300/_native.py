@@ -27,7 +27,9 @@ class GmhdParams(ctypes.Structure):
     _fields_ = [("gamma0", ctypes.c_double), ("cfl", ctypes.c_double), ("slope_type", ctypes.c_double),
                 ("smallr", ctypes.c_double), ("smallc", ctypes.c_double), ("scaling_factor", ctypes.c_double),
                 ("riemann", ctypes.c_int32), ("precision", ctypes.c_int32), ("prolongation", ctypes.c_int32),
-                ("time_integrator", ctypes.c_int32)]
+                ("time_integrator", ctypes.c_int32), ("gravity_enabled", ctypes.c_int32),
+                ("gravity", ctypes.c_double * 3), ("viscosity_enabled", ctypes.c_int32),
+                ("viscosity_mu", ctypes.c_double), ("viscous_predictor", ctypes.c_int32)]
 
 
 _ip = ctypes.POINTER(ctypes.c_int32)

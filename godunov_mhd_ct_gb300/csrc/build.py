@@ -21,7 +21,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 UNITS = {
     "step_fp64.cu": ["--fmad=false"],
+    "step_fp64_visc.cu": ["--fmad=false"],
     "step_mixed.cu": ["--use_fast_math"],
+    "step_mixed_visc.cu": ["--use_fast_math"],
     "gmhd_abi.cu": ["--fmad=false"],
     "noalloc.cu": ["--fmad=false"],
     "amr.cu": ["--fmad=false"],

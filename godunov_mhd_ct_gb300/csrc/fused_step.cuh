@@ -43,6 +43,7 @@ struct StepArgs
   unsigned long long *       invdt_out;         // per problem: fused CFL of U2/B2 (max), or null
   unsigned int *             health;            // OR of HEALTH_* flags
   int                        n_blocks;          // ids >= n_blocks in `neighbor` are virtual blocks
+  Sources                    src;               // gravity / viscosity (viscous fluxes need C::VISC)
 
   // ---- coarse/fine meshes (all null / zero when no block has a neighbour at another level) ----
   // Neighbour regions at another level are presented to the gather as virtual same-level blocks
@@ -87,11 +88,13 @@ enum : unsigned int
   HEALTH_LOW_BETA_FP64 = 16u, // informational: FP64 pressure recovery was used (mixed path)
 };
 
-template <typename R_, int DIM_, int TX_, int TY_, int TZ_, int NT_, bool EXACT_, bool AMR_ = false>
+template <typename R_, int DIM_, int TX_, int TY_, int TZ_, int NT_, bool EXACT_, bool AMR_ = false,
+          bool VISC_ = false>
 struct Cfg
 {
   using R = R_;
-  static constexpr bool AMR = AMR_; // coarse/fine mesh support compiled in
+  static constexpr bool AMR = AMR_;   // coarse/fine mesh support compiled in
+  static constexpr bool VISC = VISC_; // viscous fluxes compiled in
   static constexpr int  DIM = DIM_;
   static constexpr int  TX = TX_;
   static constexpr int  TY = TY_;
@@ -125,6 +128,9 @@ struct Cfg
   static constexpr int NF_Z = TX * TY * (TZ + 1);
   static constexpr int NF = NF_X > NF_Y ? (NF_X > NF_Z ? NF_X : NF_Z) : (NF_Y > NF_Z ? NF_Y : NF_Z);
   static constexpr int NFV = DIM == 3 ? 5 : 6; // flux vars used by the update (2D adds Bz)
+  // vars per face of the coarse/fine flux side buffer: the NFV hydro fluxes, then the viscous fluxes
+  // of E, rho u, rho v, rho w
+  static constexpr int NFS = NFV + (VISC ? 4 : 0);
 
   // fluxes of all directions (one list: x faces, then y, then z)
   static constexpr int NFT = NF_X + NF_Y + (DIM == 3 ? NF_Z : 0);
@@ -148,7 +154,11 @@ struct Cfg
   static constexpr int OFF_SL = OFF_FBZ + NFBZ;
   static constexpr int OFF_Q2 = OFF_SL + NDIR * 8 * NS;
   static constexpr int OFF_SF = OFF_Q2 + 8 * NS;
-  static constexpr int OFF_U1 = ((OFF_SF + NSF * NS + 1) / 2) * 2; // 8-byte aligned
+  // t^n velocities (DIM components) of cells [-1, T] for the viscous fluxes, outside the union below
+  static constexpr int VX = TX + 2, VY = TY + 2, VZ = D3 ? TZ + 2 : 1;
+  static constexpr int NVEL = VISC ? VX * VY * VZ : 0;
+  static constexpr int OFF_VEL = OFF_SF + NSF * NS;
+  static constexpr int OFF_U1 = ((OFF_VEL + DIM * NVEL + 1) / 2) * 2; // 8-byte aligned
   static constexpr int U1_EARLY = 5 * NQ + NECOMP * NE;
   static constexpr int OFF_E = OFF_U1 + 5 * NQ;
   static constexpr int OFF_EMFD = OFF_U1;
@@ -168,7 +178,122 @@ struct Cfg
   __device__ static int si(int i, int j, int k) { return (i + 1) + SX * ((j + 1) + SY * (k + D3)); }
   __device__ static int ei(int i, int j, int k) { return (i + 1) + EX * ((j + 1) + EY * (k + D3)); }
   __device__ static int mi(int i, int j, int k) { return i + MX * (j + MY * k); }
+  __device__ static int vi(int i, int j, int k) { return (i + 1) + VX * ((j + 1) + VY * (k + D3)); }
 };
+
+// Viscous flux (times dt/dx) at the left face along dir of tile cell (i, j, k), from the t^n
+// velocities of cells [-1, T] (ComputeViscousFluxesAndStoreFunctor.cpp:168-344): the velocity
+// gradient is a backward difference from the cell (across the face along dir, inside the cell's row
+// along the others); out = E, rho u, rho v, rho w (rho and B fluxes are zero).
+template <class C>
+__device__ __forceinline__ void
+viscous_face_flux(const typename C::R * vel, int dir, int i, int j, int k, typename C::R mu, typename C::R dx,
+                  typename C::R dtdx, typename C::R * out)
+{
+  using R = typename C::R;
+  constexpr int NC = C::DIM;
+  R             v[3], g[3][3];
+  const int     c0 = C::vi(i, j, k);
+  const int     cx = C::vi(i - 1, j, k), cy = C::vi(i, j - 1, k), cz = C::D3 ? C::vi(i, j, k - 1) : c0;
+#pragma unroll
+  for (int c = 0; c < NC; ++c)
+  {
+    const R * V = vel + c * C::NVEL;
+    const R   qr = V[c0];
+    v[c] = qr;
+    g[c][0] = (qr - V[cx]) / dx;
+    g[c][1] = (qr - V[cy]) / dx;
+    if constexpr (C::DIM == 3)
+      g[c][2] = (qr - V[cz]) / dx;
+  }
+  R fu, fv, fw = R(0), fe;
+  if constexpr (C::DIM == 2)
+  {
+    const R div = g[0][0] + g[1][1];
+    const R txy = mu * (g[1][0] + g[0][1]);
+    if (dir == 0)
+    {
+      const R txx = R(2) * mu * (g[0][0] - R(0.5) * div);
+      fu = -txx;
+      fv = -txy;
+      fe = -v[0] * txx - v[1] * txy;
+    }
+    else
+    {
+      const R tyy = R(2) * mu * (g[1][1] - R(0.5) * div);
+      fu = -txy;
+      fv = -tyy;
+      fe = -v[0] * txy - v[1] * tyy;
+    }
+  }
+  else
+  {
+    const R third = R(1.0 / 3.0);
+    const R div = g[0][0] + g[1][1] + g[2][2];
+    R       t0, t1, t2;
+    if (dir == 0)
+    {
+      t0 = R(2) * mu * (g[0][0] - third * div);
+      t1 = mu * (g[1][0] + g[0][1]);
+      t2 = mu * (g[2][0] + g[0][2]);
+    }
+    else if (dir == 1)
+    {
+      t0 = mu * (g[0][1] + g[1][0]);
+      t1 = R(2) * mu * (g[1][1] - third * div);
+      t2 = mu * (g[2][1] + g[1][2]);
+    }
+    else
+    {
+      t0 = mu * (g[0][2] + g[2][0]);
+      t1 = mu * (g[1][2] + g[2][1]);
+      t2 = R(2) * mu * (g[2][2] - third * div);
+    }
+    fu = -t0;
+    fv = -t1;
+    fw = -t2;
+    fe = -v[0] * t0 - v[1] * t1 - v[2] * t2;
+  }
+  out[0] = fe * dtdx;
+  out[1] = fu * dtdx;
+  out[2] = fv * dtdx;
+  out[3] = fw * dtdx;
+}
+
+// Sum over the 2^(d-1) fine faces covering coarse face (g1, g2) of this block's border face toward
+// neighbour slot `slot` (direction d, side), of flux side variable `var`, divided by 2^d
+// (ReadFluxesAndConservativeUpdateFunctor.h:233-270). The fine blocks stored them in pass 1.
+template <class C>
+__device__ double
+fine_face_flux(const StepArgs & a, int blk, int slot, int d, int side, int g1, int g2, int var)
+{
+  const int bs[3] = {a.bx, a.by, a.bz};
+  const int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;
+  const int ff = 2 * d + (side < 0 ? 1 : 0); // the fine block's face toward this block
+  double    acc = 0.0;
+  for (int e2 = 0; e2 < (C::DIM == 3 ? 2 : 1); ++e2)
+    for (int e1 = 0; e1 < 2; ++e1)
+    {
+      int ch[3] = {0, 0, 0};
+      ch[d] = side < 0 ? 1 : 0;
+      int F1 = 2 * g1 + e1;
+      ch[t1] = F1 >= bs[t1] ? 1 : 0;
+      F1 -= ch[t1] * bs[t1];
+      int F2 = 0;
+      if (C::DIM == 3)
+      {
+        F2 = 2 * g2 + e2;
+        ch[t2] = F2 >= bs[t2] ? 1 : 0;
+        F2 -= ch[t2] * bs[t2];
+      }
+      const int id = a.fine[((int64_t)blk * 27 + slot) * 8 + ch[0] + 2 * ch[1] + 4 * ch[2]];
+      const int cs = id >= 0 ? a.flux_slot[id] : -1;
+      if (cs >= 0)
+        acc += a.flux_side[(((int64_t)cs * 2 * C::DIM + ff) * C::NFS + var) * a.flux_face_stride + F1 +
+                           (int64_t)bs[t1] * F2];
+    }
+  return acc / (double)(1 << C::DIM);
+}
 
 __device__ __forceinline__ int
 nb_slot(int ox, int oy, int oz)
@@ -348,7 +473,8 @@ amr_border_emf(const TileView<C> & t, const int * gi, int v0, int v1, typename C
 // the sum of the 2^(d-1) fine fluxes (first transverse axis fastest) / 2^d.
 template <class C>
 __device__ __forceinline__ void
-amr_border_fluxes(const StepArgs & a, typename C::R * fl, const int * s_kind, int blk, int x0, int y0, int z0, int tid)
+amr_border_fluxes(const StepArgs & a, typename C::R * fl, const int * s_kind, int blk, int x0, int y0, int z0, int tid,
+                  const typename C::R * vel, typename C::R dx, typename C::R dtdx)
 {
   using R = typename C::R;
   const int bs[3] = {a.bx, a.by, a.bz};
@@ -372,7 +498,10 @@ amr_border_fluxes(const StepArgs & a, typename C::R * fl, const int * s_kind, in
     const int n1 = T[t1], n2 = C::DIM == 3 ? T[t2] : 1;
     const int off = d == 0 ? 0 : (d == 1 ? C::NF_X : C::NF_X + C::NF_Y);
     const int nxd = C::TX + (d == 0), nyd = C::TY + (d == 1);
-    for (int m = tid; m < n1 * n2 * C::NFV; m += C::NT)
+    // pass 1 stores the hydro and viscous fluxes; pass 2 replaces the hydro fluxes here (the viscous
+    // ones are read in the update)
+    const int nvar = write ? C::NFS : C::NFV;
+    for (int m = tid; m < n1 * n2 * nvar; m += C::NT)
     {
       const int v = m / (n1 * n2), r = m - v * (n1 * n2);
       const int u1 = r % n1, u2 = r / n1;
@@ -385,34 +514,20 @@ amr_border_fluxes(const StepArgs & a, typename C::R * fl, const int * s_kind, in
       const int g1 = org[t1] + u1, g2 = C::DIM == 3 ? org[t2] + u2 : 0;
       if (write)
       {
-        a.flux_side[(((int64_t)my_slot * 2 * C::DIM + f) * C::NFV + v) * a.flux_face_stride + g1 + (int64_t)bs[t1] * g2] =
-          to_d<R>(fl[v * C::NFT + idx]);
+        double val;
+        if (v < C::NFV)
+          val = to_d<R>(fl[v * C::NFT + idx]);
+        else
+        {
+          R fv[4];
+          viscous_face_flux<C>(vel, d, li[0], li[1], li[2], (R)a.src.mu, dx, dtdx, fv);
+          val = to_d<R>(fv[v - C::NFV]);
+        }
+        a.flux_side[(((int64_t)my_slot * 2 * C::DIM + f) * C::NFS + v) * a.flux_face_stride + g1 + (int64_t)bs[t1] * g2] =
+          val;
         continue;
       }
-      const int ff = 2 * d + (side < 0 ? 1 : 0); // the fine block's face toward this block
-      double    acc = 0.0;
-      for (int e2 = 0; e2 < (C::DIM == 3 ? 2 : 1); ++e2)
-        for (int e1 = 0; e1 < 2; ++e1)
-        {
-          int ch[3] = {0, 0, 0};
-          ch[d] = side < 0 ? 1 : 0;
-          int F1 = 2 * g1 + e1;
-          ch[t1] = F1 >= bs[t1] ? 1 : 0;
-          F1 -= ch[t1] * bs[t1];
-          int F2 = 0;
-          if (C::DIM == 3)
-          {
-            F2 = 2 * g2 + e2;
-            ch[t2] = F2 >= bs[t2] ? 1 : 0;
-            F2 -= ch[t2] * bs[t2];
-          }
-          const int id = a.fine[((int64_t)blk * 27 + slot) * 8 + ch[0] + 2 * ch[1] + 4 * ch[2]];
-          const int cs = id >= 0 ? a.flux_slot[id] : -1;
-          if (cs >= 0)
-            acc += a.flux_side[(((int64_t)cs * 2 * C::DIM + ff) * C::NFV + v) * a.flux_face_stride + F1 +
-                               (int64_t)bs[t1] * F2];
-        }
-      fl[v * C::NFT + idx] = to_r<R>(acc / (double)(1 << C::DIM));
+      fl[v * C::NFT + idx] = to_r<R>(fine_face_flux<C>(a, blk, slot, d, side, g1, g2, v));
     }
   }
 }
@@ -643,6 +758,7 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
   double * emfd = reinterpret_cast<double *>(sm + C::OFF_EMFD); // FP64 EMFs for the CT curl
   R *      fl = sm + C::OFF_FL;
   R *      b2s = sm + C::OFF_B2;
+  R *      vel = sm + C::OFF_VEL; // viscous variants: t^n velocities of cells [-1, T]
   int * s_nbr = reinterpret_cast<int *>(sm + C::TOTAL);
   __shared__ double       s_red[NT / 32];
   __shared__ unsigned int s_health;
@@ -704,6 +820,7 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
   const double dx = (1.0 / (double)((int64_t)bx << mylevel)) * a.scaling_factor;
   const double dtdx_d = dt / dx;
   const R      dtdx = (R)dtdx_d;
+  const R      dxr = (R)dx;
 
   Phys<R> ph;
   ph.gamma0 = (R)a.gamma0;
@@ -1017,6 +1134,19 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
 
   // ---- phase 2: limited slopes + Hancock predictor on the S region ---------------------------
   // (ComputeLimitedSlopesFunctor.cpp:121-314, ComputeUpdatedPrimitiveVariablesFunctor.cpp:284-546)
+  if constexpr (C::VISC)
+  {
+    // keep the t^n velocities the viscous fluxes need past the reuse of the primitive region
+    for (int n = tid; n < C::NVEL; n += NT)
+    {
+      const int i = n % C::VX - 1;
+      const int j = (n / C::VX) % C::VY - 1;
+      const int k = D3 ? n / (C::VX * C::VY) - 1 : 0;
+#pragma unroll
+      for (int c = 0; c < DIM; ++c)
+        vel[c * C::NVEL + n] = qh[(IU + c) * C::NQ + C::qi(i, j, k)];
+    }
+  }
   for (int n = tid; n < C::NS; n += NT)
   {
     const int i = n % C::SX - 1;
@@ -1132,10 +1262,47 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       sB0 = (v * dAx + A * dvx - u * dBx - B * dux) * dtdx + (v * dCz + Cc * dvz - w * dBz - B * dwz) * dtdz;
       sC0 = (w * dAx + A * dwx - u * dCx - Cc * dux) * dtdx + (w * dBy + B * dwy - v * dCy - Cc * dvy) * dtdy;
     }
+    // half-step gravity kick and viscous predictor on the velocity, after the sources
+    // (ComputeUpdatedPrimitiveVariablesFunctor.cpp:372-383, 505-517)
+    R ug = u, vg = v, wg = w;
+    if (a.src.gravity)
+    {
+      const R hdt = (R)dt;
+      ug += (R)a.src.g[0] * R(0.5) * hdt;
+      vg += (R)a.src.g[1] * R(0.5) * hdt;
+      if constexpr (DIM == 3)
+        wg += (R)a.src.g[2] * R(0.5) * hdt;
+    }
+    if constexpr (C::VISC)
+    {
+      if (a.src.visc_predictor)
+      {
+        // (ComputeUpdatedPrimitiveVariablesFunctor.cpp:174-280): half a step of nu * Laplacian per axis
+        const R nu = (R)a.src.mu / r;
+        auto    vp = [&](int var, R val) {
+          const R * Q = qh + var * C::NQ;
+          const R   q0v = Q[q0];
+          const R   d2x = Q[qxp] + Q[qxm] - R(2) * q0v;
+          val += R(0.5) * nu * d2x / dxr * dtdx;
+          const R d2y = Q[qyp] + Q[qym] - R(2) * q0v;
+          val += R(0.5) * nu * d2y / dxr * dtdx;
+          if constexpr (DIM == 3)
+          {
+            const R d2z = Q[qzp] + Q[qzm] - R(2) * q0v;
+            val += R(0.5) * nu * d2z / dxr * dtdx;
+          }
+          return val;
+        };
+        ug = vp(IU, ug);
+        vg = vp(IV, vg);
+        if constexpr (DIM == 3)
+          wg = vp(IW, wg);
+      }
+    }
     q2[ID * C::NS + n] = r + R(0.5) * sr0;
-    q2[IU * C::NS + n] = u + R(0.5) * su0;
-    q2[IV * C::NS + n] = v + R(0.5) * sv0;
-    q2[IW * C::NS + n] = w + R(0.5) * sw0;
+    q2[IU * C::NS + n] = ug + R(0.5) * su0;
+    q2[IV * C::NS + n] = vg + R(0.5) * sv0;
+    q2[IW * C::NS + n] = wg + R(0.5) * sw0;
     q2[IP * C::NS + n] = p + R(0.5) * sp0;
     q2[IA * C::NS + n] = A + R(0.5) * sA0;
     q2[IB * C::NS + n] = B + R(0.5) * sB0;
@@ -1261,7 +1428,7 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
   __syncthreads();
   if constexpr (C::AMR)
   {
-    amr_border_fluxes<C>(a, fl, s_kind, blk, x0, y0, z0, tid);
+    amr_border_fluxes<C>(a, fl, s_kind, blk, x0, y0, z0, tid, vel, dxr, dtdx);
     __syncthreads();
     if (side_only)
       return; // this tile's update runs in pass 2
@@ -1432,6 +1599,87 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       for (int v = 0; v < C::NFV; ++v)
         u2[v] += to_d<R>(dU[v]);
     }
+    if constexpr (C::VISC)
+    {
+      // viscous fluxes through the same update, after the three hydro directions
+      // (GodunovImplemV0.cpp:179-192); a coarse cell next to finer blocks takes their flux sum
+      const int lc[3] = {i, j, k};
+      const int org[3] = {x0, y0, z0};
+      const int bsz[3] = {bx, by, bz};
+      R         dV[4] = {R(0), R(0), R(0), R(0)};
+#pragma unroll
+      for (int dir = 0; dir < DIM; ++dir)
+      {
+        R fL[4], fR[4];
+        viscous_face_flux<C>(vel, dir, i, j, k, (R)a.src.mu, dxr, dtdx, fL);
+        viscous_face_flux<C>(vel, dir, i + (dir == 0), j + (dir == 1), k + (dir == 2), (R)a.src.mu, dxr, dtdx, fR);
+        if constexpr (C::AMR)
+        {
+          if (a.pass == 2)
+          {
+            const int t1 = dir == 0 ? 1 : 0, t2 = dir == 2 ? 1 : 2;
+            const int g1 = org[t1] + lc[t1], g2 = DIM == 3 ? org[t2] + lc[t2] : 0;
+#pragma unroll
+            for (int side = -1; side <= 1; side += 2)
+            {
+              const int gc = org[dir] + lc[dir];
+              if (side < 0 ? gc != 0 : gc != bsz[dir] - 1)
+                continue;
+              const int sl = nb_slot(dir == 0 ? side : 0, dir == 1 ? side : 0, dir == 2 ? side : 0);
+              if (s_kind[sl] != RK_FINER)
+                continue;
+#pragma unroll
+              for (int v = 0; v < 4; ++v)
+              {
+                const R fv = to_r<R>(fine_face_flux<C>(a, blk, sl, dir, side, g1, g2, C::NFV + v));
+                if (side < 0)
+                  fL[v] = fv;
+                else
+                  fR[v] = fv;
+              }
+            }
+          }
+        }
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+        {
+          R acc = R(0);
+          acc = acc + fL[v];
+          acc = acc - fR[v];
+          if constexpr (C::EXACT)
+            u2[IP + v] += (double)acc;
+          else
+            dV[v] += acc;
+        }
+      }
+      if constexpr (!C::EXACT)
+      {
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+          u2[IP + v] += to_d<R>(dV[v]);
+      }
+    }
+    if (a.src.gravity)
+    {
+      // AddGravitySourceTerm (AddGravitySourceTerm.cpp:47-99), FP64
+      const double rho_old = upre[c][ID], rho_new = u2[ID];
+      double       ru = u2[IU], rv = u2[IV], rw = DIM == 3 ? u2[IW] : 0.0;
+      double       ekin_old = 0.5 * (ru * ru + rv * rv) / rho_new;
+      if constexpr (DIM == 3)
+        ekin_old += 0.5 * (rw * rw) / rho_new;
+      ru += dt * a.src.g[0] * (rho_old + rho_new) / 2;
+      rv += dt * a.src.g[1] * (rho_old + rho_new) / 2;
+      if constexpr (DIM == 3)
+        rw += dt * a.src.g[2] * (rho_old + rho_new) / 2;
+      u2[IU] = ru;
+      u2[IV] = rv;
+      if constexpr (DIM == 3)
+        u2[IW] = rw;
+      double ekin_new = 0.5 * (ru * ru + rv * rv) / rho_new;
+      if constexpr (DIM == 3)
+        ekin_new += 0.5 * (rw * rw) / rho_new;
+      u2[IP] += (ekin_new - ekin_old);
+    }
 #pragma unroll
     for (int v = 0; v < 5; ++v)
       a.U2[((int64_t)blk * 5 + v) * a.ncell + cell] = u2[v];
@@ -1467,13 +1715,10 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
         const double d2 = 0.5 * (b2 / r + c2);
         const double cfx = sqrt(d2 + sqrt(d2 * d2 - c2 * Ax * Ax / r)) + fabs(vx);
         const double cfy = sqrt(d2 + sqrt(d2 * d2 - c2 * Ay * Ay / r)) + fabs(vy);
+        double cfz = 0.0;
         if constexpr (DIM == 3)
-        {
-          const double cfz = sqrt(d2 + sqrt(d2 * d2 - c2 * Az * Az / r)) + fabs(vz);
-          val = cfx / dx + cfy / dx + cfz / dx;
-        }
-        else
-          val = cfx / dx + cfy / dx;
+          cfz = sqrt(d2 + sqrt(d2 * d2 - c2 * Az * Az / r)) + fabs(vz);
+        val = cfl_inv_dt_fp64(DIM, cfx, cfy, cfz, dx, u2[ID], a.src);
       }
       else
       {
@@ -1497,10 +1742,10 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
         const float d2 = 0.5f * (b2 * ir + c2);
         const float cfx = sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * bxf * bxf * ir, 0.0f))) + fabsf(vx);
         const float cfy = sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * byf * byf * ir, 0.0f))) + fabsf(vy);
-        float       sum = cfx + cfy;
+        float       cfz = 0.0f;
         if constexpr (DIM == 3)
-          sum += sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * bzf * bzf * ir, 0.0f))) + fabsf(vz);
-        val = to_d<R>(sum * (float)(1.0 / dx));
+          cfz = sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * bzf * bzf * ir, 0.0f))) + fabsf(vz);
+        val = to_d<R>(cfl_inv_dt_fp32(DIM, cfx, cfy, cfz, (float)dx, (float)(1.0 / dx), to_r<R>(u2[ID]), a.src));
       }
       my_invdt = fmax(my_invdt, val);
     }

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -18,11 +19,11 @@ namespace gmhd
 int launch_inv_dt(const double * U, const double * B, const int32_t * level, const int32_t * problem,
                   int n_owned, int dim, int bx, int by, int bz, int64_t ncell, int64_t nfx, int64_t nfy,
                   int64_t nface, double gamma0, double smallr, double smallp, double scaling_factor,
-                  unsigned long long * invdt, cudaStream_t stream);
+                  const Sources & src, unsigned long long * invdt, cudaStream_t stream);
 int launch_inv_dt_mixed(const double * U, const double * B, const int32_t * level, const int32_t * problem,
                         int n_owned, int dim, int bx, int by, int bz, int64_t ncell, int64_t nfx, int64_t nfy,
                         int64_t nface, double gamma0, double smallr, double smallp, double scaling_factor,
-                        unsigned long long * invdt, cudaStream_t stream);
+                        const Sources & src, unsigned long long * invdt, cudaStream_t stream);
 } // namespace gmhd
 
 struct gmhd_ctx
@@ -195,6 +196,20 @@ release_all(gmhd_ctx * c)
   c->dtlog_cap = 0;
 }
 
+gmhd::Sources
+sources_of(const gmhd_params & p)
+{
+  gmhd::Sources src;
+  std::memset(&src, 0, sizeof src);
+  src.gravity = p.gravity_enabled != 0;
+  for (int d = 0; d < 3; ++d)
+    src.g[d] = src.gravity ? p.gravity[d] : 0.0;
+  src.viscosity = p.viscosity_enabled != 0;
+  src.mu = src.viscosity ? p.viscosity_mu : 0.0;
+  src.visc_predictor = src.viscosity && p.viscous_predictor != 0;
+  return src;
+}
+
 gmhd::StepArgs
 make_args(const gmhd_ctx * c, const double * U, double * U2, const double * B, double * B2)
 {
@@ -226,6 +241,7 @@ make_args(const gmhd_ctx * c, const double * U, double * U2, const double * B, d
   a.rk2 = c->p.time_integrator == GMHD_TIME_RK2_SSP;
   a.health = c->d_health;
   a.n_blocks = c->n_blocks;
+  a.src = sources_of(c->p);
   return a;
 }
 
@@ -483,7 +499,7 @@ enqueue_inv_dt(gmhd_ctx * ctx, const double * U, const double * B, unsigned long
   auto launch = (exact || ctx->p.precision != GMHD_PRECISION_MIXED) ? gmhd::launch_inv_dt : gmhd::launch_inv_dt_mixed;
   const int rc = launch(U, B, ctx->d_level, ctx->d_problem, ctx->n_owned, ctx->dim, ctx->bx, ctx->by,
                                      ctx->bz, ctx->ncell, ctx->nfx, ctx->nfy, ctx->nface, ctx->p.gamma0,
-                                     ctx->p.smallr, ctx->smallp, ctx->p.scaling_factor, slot, s);
+                                     ctx->p.smallr, ctx->smallp, ctx->p.scaling_factor, sources_of(ctx->p), slot, s);
   if (rc != 0)
     return cuda_fail(ctx, (cudaError_t)rc);
   return GMHD_OK;
@@ -630,9 +646,9 @@ setup_amr(gmhd_ctx * ctx, const gmhd_mesh * m, const std::vector<int8_t> & kind)
   // two-pass tile lists
   int T[3];
   if (ctx->p.precision == GMHD_PRECISION_MIXED)
-    gmhd::tile_shape_mixed(m->dim, ctx->bx, ctx->by, ctx->bz, T);
+    gmhd::tile_shape_mixed(m->dim, ctx->bx, ctx->by, ctx->bz, ctx->p.viscosity_enabled != 0, T);
   else
-    gmhd::tile_shape_fp64(m->dim, ctx->bx, ctx->by, ctx->bz, T);
+    gmhd::tile_shape_fp64(m->dim, ctx->bx, ctx->by, ctx->bz, ctx->p.viscosity_enabled != 0, T);
   const int            nt[3] = {ctx->bx / T[0], ctx->by / T[1], m->dim == 3 ? ctx->bz / T[2] : 1};
   const int            tpb = nt[0] * nt[1] * nt[2];
   std::vector<int32_t> list1, list2;
@@ -668,7 +684,8 @@ setup_amr(gmhd_ctx * ctx, const gmhd_mesh * m, const std::vector<int8_t> & kind)
   const int     nv = (int)(vmap.size() / 2);
   const int     ncomp = m->dim == 3 ? 3 : 1;
   const int64_t ne = (int64_t)(ctx->bx + 1) * (ctx->by + 1) * (m->dim == 3 ? ctx->bz + 1 : 1);
-  const int     nfv = m->dim == 3 ? 5 : 6;
+  // hydro flux vars of the update, plus the 4 viscous ones (E and the momenta) with viscosity
+  const int     nfv = (m->dim == 3 ? 5 : 6) + (ctx->p.viscosity_enabled ? 4 : 0);
   ctx->flux_face_stride = m->dim == 3 ? std::max(ctx->by * ctx->bz, std::max(ctx->bx * ctx->bz, ctx->bx * ctx->by))
                                       : std::max(ctx->bx, ctx->by);
   int rc;
@@ -732,6 +749,11 @@ gmhd_create(const gmhd_params * params)
     return nullptr;
   if (params->time_integrator != GMHD_TIME_HANCOCK && params->time_integrator != GMHD_TIME_RK2_SSP)
     return nullptr;
+  if (params->gravity_enabled &&
+      !(std::isfinite(params->gravity[0]) && std::isfinite(params->gravity[1]) && std::isfinite(params->gravity[2])))
+    return nullptr;
+  if (params->viscosity_enabled && !(params->viscosity_mu >= 0.0 && std::isfinite(params->viscosity_mu)))
+    return nullptr;
   gmhd_ctx * c = new (std::nothrow) gmhd_ctx();
   if (!c)
     return nullptr;
@@ -747,7 +769,8 @@ gmhd_create(const gmhd_params * params)
     return nullptr;
   }
   c->bytes = sizeof(unsigned int);
-  if (gmhd::prepare_fp64() != 0 || gmhd::prepare_mixed() != 0)
+  if (gmhd::prepare_fp64() != 0 || gmhd::prepare_mixed() != 0 || gmhd::prepare_fp64_visc() != 0 ||
+      gmhd::prepare_mixed_visc() != 0)
   {
     cudaFree(c->d_health);
     cudaStreamDestroy(c->own_stream);

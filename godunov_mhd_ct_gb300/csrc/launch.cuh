@@ -36,14 +36,19 @@ prepare_fused()
                                    (int)C::SMEM_BYTES);
 }
 
-// Tile choice: the largest configured tile that divides the block.
+// Tile choice: the largest configured tile that divides the block. With a.src.viscosity the
+// viscous variants run (launch_step_*_visc).
 int launch_step_fp64(const StepArgs & a, int dim, cudaStream_t stream);
 int launch_step_mixed(const StepArgs & a, int dim, cudaStream_t stream);
+int launch_step_fp64_visc(const StepArgs & a, int dim, cudaStream_t stream);
+int launch_step_mixed_visc(const StepArgs & a, int dim, cudaStream_t stream);
 // the tile extents launch_step_* uses for these block sizes
-void tile_shape_fp64(int dim, int bx, int by, int bz, int * t);
-void tile_shape_mixed(int dim, int bx, int by, int bz, int * t);
+void tile_shape_fp64(int dim, int bx, int by, int bz, bool visc, int * t);
+void tile_shape_mixed(int dim, int bx, int by, int bz, bool visc, int * t);
 int prepare_fp64();
 int prepare_mixed();
+int prepare_fp64_visc();
+int prepare_mixed_visc();
 
 // coarse/fine ghost prepass (amr.cu): fills the virtual neighbour blocks read by the fused step
 struct GhostArgs

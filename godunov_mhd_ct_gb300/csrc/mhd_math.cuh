@@ -32,6 +32,76 @@ enum : int
   RS_HLLD = 5
 };
 
+// Source terms of the step (all off by default): uniform gravity and viscosity.
+struct Sources
+{
+  int    gravity;        // [gravity] enabled
+  double g[3];           // [gravity] uniform_gx, uniform_gy, uniform_gz
+  int    viscosity;      // [viscosity] enabled
+  double mu;             // [viscosity] mu
+  int    visc_predictor; // viscous term of the Hancock predictor
+};
+
+// One cell's 1/dt from its fast speeds v_d = c_f,d + |u_d| (ComputeDtMHDFunctor.cpp:86-151): sum of
+// v_d / dx; with gravity each term is scaled by k / (sqrt(1 + 2k) - 1), k = sum|g| dx / sum v_d^2
+// floored at 1e-4 (:155-249); with viscosity at least 4 nu / dx^2, nu = mu / rho of the conservative
+// density (:144-148). FP64 with the reference's operand order.
+__device__ __forceinline__ double
+cfl_inv_dt_fp64(int dim, double vx, double vy, double vz, double dx, double rho, const Sources & s)
+{
+  double val;
+  if (s.gravity)
+  {
+    double v2 = vx * vx + vy * vy;
+    if (dim == 3)
+      v2 += vz * vz;
+    double k = fabs(s.g[0]) + fabs(s.g[1]);
+    if (dim == 3)
+      k += fabs(s.g[2]);
+    k *= dx / v2;
+    k = fmax(k, 1e-4);
+    const double factor = k / (sqrt(1.0 + 2.0 * k) - 1.0);
+    val = 0.0;
+    val += (vx * factor) / dx;
+    val += (vy * factor) / dx;
+    if (dim == 3)
+      val += (vz * factor) / dx;
+  }
+  else
+    val = dim == 3 ? vx / dx + vy / dx + vz / dx : vx / dx + vy / dx;
+  if (s.viscosity)
+  {
+    const double nu = s.mu / rho;
+    val = fmax(val, 4 * nu / (dx * dx));
+  }
+  return val;
+}
+
+// FP32 estimate of cfl_inv_dt_fp64 for the mixed path. The gravity factor is evaluated as
+// (sqrt(1 + 2k) + 1) / 2, equal to k / (sqrt(1 + 2k) - 1) but without its cancellation at small k.
+__device__ __forceinline__ float
+cfl_inv_dt_fp32(int dim, float vx, float vy, float vz, float dx, float idx, float rho, const Sources & s)
+{
+  float sum = vx + vy;
+  if (dim == 3)
+    sum += vz;
+  if (s.gravity)
+  {
+    float v2 = vx * vx + vy * vy;
+    if (dim == 3)
+      v2 += vz * vz;
+    float gs = fabsf((float)s.g[0]) + fabsf((float)s.g[1]);
+    if (dim == 3)
+      gs += fabsf((float)s.g[2]);
+    const float k = fmaxf(gs * dx / v2, 1e-4f);
+    sum *= 0.5f * (sqrtf(1.0f + 2.0f * k) + 1.0f);
+  }
+  float val = sum * idx;
+  if (s.viscosity)
+    val = fmaxf(val, 4.0f * ((float)s.mu / rho) * idx * idx);
+  return val;
+}
+
 template <typename R>
 struct Phys
 {

@@ -19,9 +19,13 @@
 #include <mutex>
 
 #include "../../include/gmhd.h"
+#include "mhd_math.cuh"
 
 namespace
 {
+using gmhd::cfl_inv_dt_fp64;
+using gmhd::Sources;
+
 __device__ __align__(256) unsigned long long g_inv_dt_scratch[GMHD_NOALLOC_MAX_PROBLEMS];
 
 constexpr int kMaxDevices = 64;
@@ -61,7 +65,7 @@ __global__ void __launch_bounds__(256)
 inv_dt_noalloc_kernel(const double * __restrict__ U, const double * __restrict__ B,
                       const int32_t * __restrict__ problem, int dim, int bx, int by, int bz, int64_t ncell,
                       int64_t nfx, int64_t nfy, int64_t nface, double dx, double gamma0, double smallr,
-                      double smallp, unsigned long long * slots)
+                      double smallp, Sources src, unsigned long long * slots)
 {
   const int     blk = blockIdx.x;
   const double *Ub = U + (int64_t)blk * 5 * ncell;
@@ -92,15 +96,8 @@ inv_dt_noalloc_kernel(const double * __restrict__ U, const double * __restrict__
     const double d2 = 0.5 * (b2 / r + c2);
     const double cfx = sqrt(d2 + sqrt(d2 * d2 - c2 * Ax * Ax / r)) + fabs(vx);
     const double cfy = sqrt(d2 + sqrt(d2 * d2 - c2 * Ay * Ay / r)) + fabs(vy);
-    double       val;
-    if (dim == 3)
-    {
-      const double cfz = sqrt(d2 + sqrt(d2 * d2 - c2 * Az * Az / r)) + fabs(vz);
-      val = cfx / dx + cfy / dx + cfz / dx;
-    }
-    else
-      val = cfx / dx + cfy / dx;
-    m = fmax(m, val);
+    const double cfz = dim == 3 ? sqrt(d2 + sqrt(d2 * d2 - c2 * Az * Az / r)) + fabs(vz) : 0.0;
+    m = fmax(m, cfl_inv_dt_fp64(dim, cfx, cfy, cfz, dx, Ub[c], src));
   }
   __shared__ double red[8];
 #pragma unroll
@@ -154,10 +151,17 @@ gmhd_inv_dt_noalloc(const gmhd_params * params, int32_t dim, int32_t bx, int32_t
   const int64_t        nface = nfx + nfy + nfz;
   const double         dx = (1.0 / (double)((int64_t)bx << level)) * params->scaling_factor;
   const double         smallp = params->smallc * params->smallc / params->gamma0;
+  Sources src;
+  src.gravity = params->gravity_enabled != 0;
+  for (int d = 0; d < 3; ++d)
+    src.g[d] = src.gravity ? params->gravity[d] : 0.0;
+  src.viscosity = params->viscosity_enabled != 0;
+  src.mu = src.viscosity ? params->viscosity_mu : 0.0;
+  src.visc_predictor = 0;
   clear_slots_kernel<<<(np + 255) / 256, 256, 0, s>>>(slots, np);
   if (n_blocks > 0)
     inv_dt_noalloc_kernel<<<n_blocks, 256, 0, s>>>(U, B, problem, dim, bx, by, bz, ncell, nfx, nfy, nface, dx,
-                                                   params->gamma0, params->smallr, smallp, slots);
+                                                   params->gamma0, params->smallr, smallp, src, slots);
   write_out_kernel<<<(np + 255) / 256, 256, 0, s>>>(slots, inv_dt, np);
   return cudaGetLastError() == cudaSuccess ? GMHD_OK : GMHD_ERR_CUDA;
 }

@@ -37,11 +37,13 @@ launch_step_fp64_cfg(const StepArgs & a, int dim, cudaStream_t stream)
 int
 launch_step_fp64(const StepArgs & a, int dim, cudaStream_t stream)
 {
+  if (a.src.viscosity)
+    return launch_step_fp64_visc(a, dim, stream);
   return a.kind ? launch_step_fp64_cfg<true>(a, dim, stream) : launch_step_fp64_cfg<false>(a, dim, stream);
 }
 
 void
-tile_shape_fp64(int dim, int bx, int by, int bz, int * t)
+tile_shape_fp64(int dim, int bx, int by, int bz, bool /*visc: same tiles*/, int * t)
 {
   if (dim == 3)
   {
@@ -82,7 +84,7 @@ __global__ void __launch_bounds__(256)
 inv_dt_kernel(const double * __restrict__ U, const double * __restrict__ B, const int32_t * __restrict__ level,
               const int32_t * __restrict__ problem, int dim, int bx, int by, int bz, int64_t ncell, int64_t nfx,
               int64_t nfy, int64_t nface, double gamma0, double smallr, double smallp, double scaling_factor,
-              unsigned long long * invdt)
+              Sources src, unsigned long long * invdt)
 {
   const int     blk = blockIdx.x;
   const double  dx = (1.0 / (double)((int64_t)bx << level[blk])) * scaling_factor;
@@ -113,15 +115,8 @@ inv_dt_kernel(const double * __restrict__ U, const double * __restrict__ B, cons
     const double d2 = 0.5 * (b2 / r + c2);
     const double cfx = sqrt(d2 + sqrt(d2 * d2 - c2 * Ax * Ax / r)) + fabs(vx);
     const double cfy = sqrt(d2 + sqrt(d2 * d2 - c2 * Ay * Ay / r)) + fabs(vy);
-    double       val;
-    if (dim == 3)
-    {
-      const double cfz = sqrt(d2 + sqrt(d2 * d2 - c2 * Az * Az / r)) + fabs(vz);
-      val = cfx / dx + cfy / dx + cfz / dx;
-    }
-    else
-      val = cfx / dx + cfy / dx;
-    m = fmax(m, val);
+    const double cfz = dim == 3 ? sqrt(d2 + sqrt(d2 * d2 - c2 * Az * Az / r)) + fabs(vz) : 0.0;
+    m = fmax(m, cfl_inv_dt_fp64(dim, cfx, cfy, cfz, dx, Ub[c], src));
   }
   __shared__ double red[8];
 #pragma unroll
@@ -141,12 +136,13 @@ inv_dt_kernel(const double * __restrict__ U, const double * __restrict__ B, cons
 int
 launch_inv_dt(const double * U, const double * B, const int32_t * level, const int32_t * problem, int n_owned, int dim,
               int bx, int by, int bz, int64_t ncell, int64_t nfx, int64_t nfy, int64_t nface, double gamma0,
-              double smallr, double smallp, double scaling_factor, unsigned long long * invdt, cudaStream_t stream)
+              double smallr, double smallp, double scaling_factor, const Sources & src, unsigned long long * invdt,
+              cudaStream_t stream)
 {
   if (n_owned <= 0)
     return 0;
   inv_dt_kernel<<<n_owned, 256, 0, stream>>>(U, B, level, problem, dim, bx, by, bz, ncell, nfx, nfy, nface, gamma0,
-                                             smallr, smallp, scaling_factor, invdt);
+                                             smallr, smallp, scaling_factor, src, invdt);
   return (int)cudaGetLastError();
 }
 } // namespace gmhd

@@ -37,14 +37,23 @@ launch_step_mixed_cfg(const StepArgs & a, int dim, cudaStream_t stream)
 int
 launch_step_mixed(const StepArgs & a, int dim, cudaStream_t stream)
 {
+  if (a.src.viscosity)
+    return launch_step_mixed_visc(a, dim, stream);
   return a.kind ? launch_step_mixed_cfg<true>(a, dim, stream) : launch_step_mixed_cfg<false>(a, dim, stream);
 }
 
 void
-tile_shape_mixed(int dim, int bx, int by, int bz, int * t)
+tile_shape_mixed(int dim, int bx, int by, int bz, bool visc, int * t)
 {
   if (dim == 3)
   {
+    if (visc)
+    {
+      const bool big = bx % 8 == 0 && by % 8 == 0 && bz % 4 == 0;
+      t[0] = t[1] = big ? 8 : 4;
+      t[2] = 4;
+      return;
+    }
     const int n = (bx % 8 == 0 && by % 8 == 0 && bz % 8 == 0) ? 8 : 4;
     t[0] = t[1] = t[2] = n;
     return;
@@ -80,7 +89,7 @@ __global__ void __launch_bounds__(256)
 inv_dt_mixed_kernel(const double * __restrict__ U, const double * __restrict__ B, const int32_t * __restrict__ level,
                     const int32_t * __restrict__ problem, int dim, int bx, int by, int bz, int64_t ncell,
                     int64_t nfx, int64_t nfy, int64_t nface, float gamma0, float smallr, float smallp,
-                    double scaling_factor, unsigned long long * invdt)
+                    double scaling_factor, Sources src, unsigned long long * invdt)
 {
   const int     blk = blockIdx.x;
   const double  dx = (1.0 / (double)((int64_t)bx << level[blk])) * scaling_factor;
@@ -107,11 +116,10 @@ inv_dt_mixed_kernel(const double * __restrict__ U, const double * __restrict__ B
     const float p = fmaxf((gamma0 - 1.0f) * (d2f_bits(Ub[ncell + c]) - emag - ekin), r * smallp);
     const float c2 = gamma0 * p * ir;
     const float d2 = 0.5f * (2.0f * emag * ir + c2);
-    float       sum = sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * Ax * Ax * ir, 0.0f))) + fabsf(vx) +
-                sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * Ay * Ay * ir, 0.0f))) + fabsf(vy);
-    if (dim == 3)
-      sum += sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * Az * Az * ir, 0.0f))) + fabsf(vz);
-    m = fmaxf(m, sum * idx);
+    const float cfx = sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * Ax * Ax * ir, 0.0f))) + fabsf(vx);
+    const float cfy = sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * Ay * Ay * ir, 0.0f))) + fabsf(vy);
+    const float cfz = dim == 3 ? sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * Az * Az * ir, 0.0f))) + fabsf(vz) : 0.0f;
+    m = fmaxf(m, cfl_inv_dt_fp32(dim, cfx, cfy, cfz, (float)dx, idx, d2f_bits(Ub[c]), src));
   }
   __shared__ float red[8];
 #pragma unroll
@@ -131,13 +139,14 @@ inv_dt_mixed_kernel(const double * __restrict__ U, const double * __restrict__ B
 int
 launch_inv_dt_mixed(const double * U, const double * B, const int32_t * level, const int32_t * problem, int n_owned,
                     int dim, int bx, int by, int bz, int64_t ncell, int64_t nfx, int64_t nfy, int64_t nface,
-                    double gamma0, double smallr, double smallp, double scaling_factor, unsigned long long * invdt,
-                    cudaStream_t stream)
+                    double gamma0, double smallr, double smallp, double scaling_factor, const Sources & src,
+                    unsigned long long * invdt, cudaStream_t stream)
 {
   if (n_owned <= 0)
     return 0;
   inv_dt_mixed_kernel<<<n_owned, 256, 0, stream>>>(U, B, level, problem, dim, bx, by, bz, ncell, nfx, nfy, nface,
-                                                   (float)gamma0, (float)smallr, (float)smallp, scaling_factor, invdt);
+                                                   (float)gamma0, (float)smallr, (float)smallp, scaling_factor, src,
+                                                   invdt);
   return (int)cudaGetLastError();
 }
 } // namespace gmhd

@@ -1,7 +1,11 @@
 """Hot-path settings read from the reference's .ini decks.
 
 Mirrors HydroSettings / MHDSettings (models/HydroSettings.cpp:18-31, models/MHDSettings.cpp:20):
-same sections, keys and defaults, so an existing deck configures this path unchanged.
+same sections, keys and defaults, so an existing deck configures this path unchanged. The source
+terms of the step read [gravity] enabled / uniform_gx, uniform_gy, uniform_gz (the keys of
+app/test_mhd_rayleigh_taylor_3d.ini, read by kalypsso-core's get_uniform_gravity_vector) and
+[viscosity] enabled / mu (app/test_mhd_kelvin_helmholtz_2d.ini, kalypsso-core's ViscosityParams);
+the viscous Hancock predictor switch is [viscosity] hancock_predictor_enabled (off by default).
 """
 from __future__ import annotations
 
@@ -24,6 +28,9 @@ class MHDSettings:
     implementation_version: int = 0
     prolongation: str = "SIMPLE_COPY"  # [amr] cell_centered_prolongation_type
     time_integrator: str = "HANCOCK"  # [amr] time_integrator (HANCOCK or RK2_SSP)
+    gravity: tuple | None = None  # [gravity] uniform (gx, gy, gz) when enabled
+    viscosity_mu: float | None = None  # [viscosity] mu when enabled
+    viscous_predictor: bool = False  # [viscosity] hancock_predictor_enabled
 
     @property
     def smallp(self) -> float:
@@ -52,6 +59,16 @@ class MHDSettings:
                 return conv(cp.get(sec, key).strip())
             return default
 
+        def flag(v):
+            return str(v).strip().lower() in ("1", "yes", "true", "on")
+
+        gravity = None
+        if flag(get("gravity", "enabled", "no", str)):
+            gravity = tuple(get("gravity", "uniform_g" + c, 0.0, float) for c in "xyz")
+        viscosity_mu = None
+        if flag(get("viscosity", "enabled", "no", str)):
+            viscosity_mu = get("viscosity", "mu", 0.0, float)
+
         return cls(
             gamma0=get("hydro", "gamma0", 1.4, float),
             cfl=get("hydro", "cfl", 0.5, float),
@@ -64,4 +81,7 @@ class MHDSettings:
             implementation_version=get("hydro", "implementation_version", 0, int),
             prolongation=get("amr", "cell_centered_prolongation_type", "SIMPLE_COPY", str),
             time_integrator=get("amr", "time_integrator", "HANCOCK", str),
+            gravity=gravity,
+            viscosity_mu=viscosity_mu,
+            viscous_predictor=flag(get("viscosity", "hancock_predictor_enabled", "no", str)),
         )

@@ -66,6 +66,14 @@ class GodunovImplemGB300:
                            settings.scaling_factor if mesh is None else mesh.scaling_factor,
                            settings.riemann_id, nat.PRECISION[precision], nat.PROLONGATION[prol],
                            nat.TIME_INTEGRATOR[integ])
+        if settings.gravity is not None:
+            g = tuple(float(v) for v in settings.gravity) + (0.0,) * (3 - len(settings.gravity))
+            p.gravity_enabled = 1
+            p.gravity = (ctypes.c_double * 3)(*g[:3])
+        if settings.viscosity_mu is not None:
+            p.viscosity_enabled = 1
+            p.viscosity_mu = float(settings.viscosity_mu)
+            p.viscous_predictor = int(bool(settings.viscous_predictor))
         self._lib = nat.lib()
         self._ctx = self._lib.gmhd_create(ctypes.byref(p))
         if not self._ctx:

@@ -116,6 +116,19 @@ typedef struct gmhd_params
   int32_t precision; /* enum gmhd_precision */
   int32_t prolongation; /* [amr] cell_centered_prolongation_type: enum gmhd_prolongation */
   int32_t time_integrator; /* [amr] time_integrator: enum gmhd_time_integrator */
+  /* Uniform gravity ([gravity] enabled, uniform_gx/gy/gz): the half-step velocity kick of the Hancock
+   * predictor (scheme/ComputeUpdatedPrimitiveVariablesFunctor.cpp:372-377, 505-511), the momentum and
+   * energy source after the update (scheme/AddGravitySourceTerm.cpp:47-99) and the CFL with gravity
+   * (scheme/ComputeDtMHDFunctor.cpp:155-249). gravity[2] is ignored in 2D. */
+  int32_t gravity_enabled;
+  double  gravity[3];
+  /* Viscosity ([viscosity] enabled, mu): viscous face fluxes applied after the hydro fluxes
+   * (scheme/ComputeViscousFluxesAndStoreFunctor.cpp:168-344, scheme/GodunovImplemV0.cpp:179-192),
+   * the CFL bound 4 mu / (rho dx^2) (scheme/ComputeDtMHDFunctor.cpp:144-148) and, with
+   * viscous_predictor, the Hancock predictor term (ComputeUpdatedPrimitiveVariablesFunctor.cpp:174-280). */
+  int32_t viscosity_enabled;
+  double  viscosity_mu;
+  int32_t viscous_predictor;
 } gmhd_params;
 
 /* Leaf-block mesh (HOST pointers; copied by gmhd_set_mesh). Blocks [0, n_owned) are updated;

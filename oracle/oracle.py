@@ -33,7 +33,8 @@ class OracleSettings(ctypes.Structure):
     _fields_ = [
         ("gamma0", ctypes.c_double), ("cfl", ctypes.c_double), ("slope_type", ctypes.c_double),
         ("smallr", ctypes.c_double), ("smallc", ctypes.c_double), ("riemann", ctypes.c_int32),
-        ("time_integrator", ctypes.c_int32),
+        ("time_integrator", ctypes.c_int32), ("gravity_enabled", ctypes.c_int32), ("gravity", ctypes.c_double * 3),
+        ("viscosity_enabled", ctypes.c_int32), ("viscosity_mu", ctypes.c_double), ("viscous_predictor", ctypes.c_int32),
     ]
 
 
@@ -87,9 +88,14 @@ def _dp(a: np.ndarray):
 
 
 def settings(gamma0=1.4, cfl=0.5, slope_type=1.0, smallr=1e-10, smallc=1e-10, riemann=5,
-             time_integrator=0) -> OracleSettings:
-    """time_integrator: 0 HANCOCK, 1 RK2_SSP ([amr] time_integrator)."""
-    return OracleSettings(gamma0, cfl, slope_type, smallr, smallc, riemann, time_integrator)
+             time_integrator=0, gravity=None, viscosity_mu=None, viscous_predictor=False) -> OracleSettings:
+    """time_integrator: 0 HANCOCK, 1 RK2_SSP ([amr] time_integrator). gravity: (gx, gy, gz) of a uniform
+    field ([gravity] enabled + uniform_g*) or None; viscosity_mu: [viscosity] mu or None (disabled);
+    viscous_predictor: the viscous Hancock predictor term."""
+    g = (0.0, 0.0, 0.0) if gravity is None else tuple(float(v) for v in gravity) + (0.0,) * (3 - len(gravity))
+    return OracleSettings(gamma0, cfl, slope_type, smallr, smallc, riemann, time_integrator,
+                          int(gravity is not None), (ctypes.c_double * 3)(*g[:3]), int(viscosity_mu is not None),
+                          0.0 if viscosity_mu is None else float(viscosity_mu), int(bool(viscous_predictor)))
 
 
 class Mesh:

@@ -51,6 +51,13 @@ struct Settings
   double cIso;    // always 0 in the reference (HydroSettings.cpp:27)
   int    riemann;
   int    rk2 = 0; // [amr] time_integrator: 0 HANCOCK, 1 RK2_SSP
+  // uniform gravity ([gravity] enabled, uniform_gx/gy/gz; kalypsso-core get_uniform_gravity_vector)
+  int    gravity = 0;
+  double grav[3] = {0.0, 0.0, 0.0};
+  // viscosity ([viscosity] enabled, mu; kalypsso-core ViscosityParams) and its Hancock predictor term
+  int    viscosity = 0;
+  double mu = 0.0;
+  int    visc_predictor = 0;
 };
 
 inline Settings

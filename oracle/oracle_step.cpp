@@ -633,8 +633,29 @@ compute_slopes(const Mesh & m, const Settings & s, StepWork & w)
 }
 
 // update_primitive_variables, Hancock branch (scheme/ComputeUpdatedPrimitiveVariablesFunctor.cpp:284-546)
+// Viscous force predictor (ComputeUpdatedPrimitiveVariablesFunctor.cpp:174-280): velocity component
+// `var` at cell (i, j, k) gets half a step of nu * Laplacian, one axis after the other; nu = mu / rho
+// of the cell's primitive density.
+static double
+viscous_predictor(const Mesh & m, const Settings & s, StepWork & w, int i, int j, int k, int var, double dtdx,
+                  double dx, double vel)
+{
+  const double nu = s.mu / w.Q(i, j, k, ID);
+  const double q0 = w.Q(i, j, k, var);
+  const double d2x = w.Q(i + 1, j, k, var) + w.Q(i - 1, j, k, var) - 2 * q0;
+  vel += 0.5 * nu * d2x / dx * dtdx;
+  const double d2y = w.Q(i, j + 1, k, var) + w.Q(i, j - 1, k, var) - 2 * q0;
+  vel += 0.5 * nu * d2y / dx * dtdx;
+  if (m.dim == 3)
+  {
+    const double d2z = w.Q(i, j, k + 1, var) + w.Q(i, j, k - 1, var) - 2 * q0;
+    vel += 0.5 * nu * d2z / dx * dtdx;
+  }
+  return vel;
+}
+
 static void
-compute_predictor(const Mesh & m, const Settings & s, double dtdx, StepWork & w)
+compute_predictor(const Mesh & m, const Settings & s, double dt, double dtdx, double dx, StepWork & w)
 {
   const int g = 1;
   const int gz = m.dim == 3 ? 1 : 0;
@@ -647,9 +668,9 @@ compute_predictor(const Mesh & m, const Settings & s, double dtdx, StepWork & w)
       {
         const double r = w.Q(i, j, k, ID);
         const double p = w.Q(i, j, k, IP);
-        const double u = w.Q(i, j, k, IU);
-        const double v = w.Q(i, j, k, IV);
-        const double ww = w.Q(i, j, k, IW);
+        double       u = w.Q(i, j, k, IU);
+        double       v = w.Q(i, j, k, IV);
+        double       ww = w.Q(i, j, k, IW);
         const double A = (w.Q(i, j, k, IA) + w.Q(i, j, k, IAR)) * 0.5;
         const double B = (w.Q(i, j, k, IB) + w.Q(i, j, k, IBR)) * 0.5;
         const double C = (w.Q(i, j, k, IC) + w.Q(i, j, k, ICR)) * 0.5;
@@ -701,6 +722,22 @@ compute_predictor(const Mesh & m, const Settings & s, double dtdx, StepWork & w)
           w.Q2(i, j, k, IB) = B;
           w.Q2(i, j, k, IC) = C;
           continue;
+        }
+        // half-step gravity kick and viscous predictor on the velocity, after the sources
+        // (ComputeUpdatedPrimitiveVariablesFunctor.cpp:372-383, 505-517)
+        if (s.gravity)
+        {
+          u += s.grav[0] * 0.5 * dt;
+          v += s.grav[1] * 0.5 * dt;
+          if (m.dim == 3)
+            ww += s.grav[2] * 0.5 * dt;
+        }
+        if (s.viscosity && s.visc_predictor)
+        {
+          u = viscous_predictor(m, s, w, i, j, k, IU, dtdx, dx, u);
+          v = viscous_predictor(m, s, w, i, j, k, IV, dtdx, dx, v);
+          if (m.dim == 3)
+            ww = viscous_predictor(m, s, w, i, j, k, IW, dtdx, dx, ww);
         }
         w.Q2(i, j, k, ID) = r + 0.5 * sr0;
         w.Q2(i, j, k, IU) = u + 0.5 * su0;
@@ -878,6 +915,123 @@ compute_fluxes(const Mesh & m, const Settings & s, double dtdx, int dir, StepWor
 
 // get_flux_from_fine_neighbor (scheme/ReadFluxesAndConservativeUpdateFunctor.h:233-270): sum of the
 // 2^(d-1) fine fluxes through the face of cell q on side `side` (-1 left, +1 right) along dir.
+// Viscous face fluxes along dir (ComputeViscousFluxesAndStoreFunctor.cpp:168-344): at the left face
+// of cell (i, j, k), the velocity gradient is a backward difference from the cell (normal: across the
+// face; transverse: inside the cell's row), the stress tensor uses it with the cell's velocity; the
+// flux (times dt/dx) goes to E and the momenta, zero for rho and B. Same layout as compute_fluxes.
+static void
+compute_viscous_fluxes(const Mesh & m, const Settings & s, double dtdx, double dx, int dir, StepWork & w,
+                       double * Fblk)
+{
+  const FluxLayout FL = flux_layout(m);
+  const int        nx = m.bx + (dir == 0), ny = m.by + (dir == 1), nz = m.bz + (dir == 2);
+  const double     mu = s.mu;
+  const int        nv = m.dim;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i)
+      {
+        double vel[3] = {0.0, 0.0, 0.0}, g[3][3] = {}; // g[c][d]: d(velocity c)/d(axis d)
+        for (int c = 0; c < nv; ++c)
+        {
+          const int    var = IU + c;
+          const double qr = w.Q(i, j, k, var);
+          vel[c] = qr;
+          g[c][0] = (qr - w.Q(i - 1, j, k, var)) / dx;
+          g[c][1] = (qr - w.Q(i, j - 1, k, var)) / dx;
+          if (m.dim == 3)
+            g[c][2] = (qr - w.Q(i, j, k - 1, var)) / dx;
+        }
+        double fu, fv, fw = 0.0, fe;
+        if (m.dim == 2)
+        {
+          const double div = g[0][0] + g[1][1];
+          const double txy = mu * (g[1][0] + g[0][1]);
+          if (dir == 0)
+          {
+            const double txx = 2 * mu * (g[0][0] - 0.5 * div);
+            fu = -txx;
+            fv = -txy;
+            fe = -vel[0] * txx - vel[1] * txy;
+          }
+          else
+          {
+            const double tyy = 2 * mu * (g[1][1] - 0.5 * div);
+            fu = -txy;
+            fv = -tyy;
+            fe = -vel[0] * txy - vel[1] * tyy;
+          }
+        }
+        else
+        {
+          const double third = 1.0 / 3.0;
+          const double div = g[0][0] + g[1][1] + g[2][2];
+          double       t0, t1, t2;
+          if (dir == 0)
+          {
+            t0 = 2 * mu * (g[0][0] - third * div);
+            t1 = mu * (g[1][0] + g[0][1]);
+            t2 = mu * (g[2][0] + g[0][2]);
+          }
+          else if (dir == 1)
+          {
+            t0 = mu * (g[0][1] + g[1][0]);
+            t1 = 2 * mu * (g[1][1] - third * div);
+            t2 = mu * (g[2][1] + g[1][2]);
+          }
+          else
+          {
+            t0 = mu * (g[0][2] + g[2][0]);
+            t1 = mu * (g[1][2] + g[2][1]);
+            t2 = 2 * mu * (g[2][2] - third * div);
+          }
+          fu = -t0;
+          fv = -t1;
+          fw = -t2;
+          fe = -vel[0] * t0 - vel[1] * t1 - vel[2] * t2;
+        }
+        const int64_t f = i + (int64_t)nx * (j + (int64_t)ny * k);
+        double *      F = Fblk + FL.off[dir];
+        F[ID * FL.n[dir] + f] = 0.0 * dtdx;
+        F[IP * FL.n[dir] + f] = fe * dtdx; // energy (IE == IP)
+        F[IU * FL.n[dir] + f] = fu * dtdx;
+        F[IV * FL.n[dir] + f] = fv * dtdx;
+        F[IW * FL.n[dir] + f] = fw * dtdx;
+        if (m.dim == 2)
+          F[IC * FL.n[dir] + f] = 0.0 * dtdx;
+      }
+}
+
+// AddGravitySourceTerm (scheme/AddGravitySourceTerm.cpp:47-99) on one owned block: momentum gets
+// dt g times the mean of the old and new densities, the energy the resulting change of kinetic energy.
+static void
+add_gravity_source(const Mesh & m, const Settings & s, double dt, const double * Ublk, double * U2blk, int64_t ncell)
+{
+  for (int64_t c = 0; c < ncell; ++c)
+  {
+    const double rho_old = Ublk[ID * ncell + c];
+    const double rho_new = U2blk[ID * ncell + c];
+    double       ru = U2blk[IU * ncell + c], rv = U2blk[IV * ncell + c], rw = 0.0;
+    if (m.dim == 3)
+      rw = U2blk[IW * ncell + c];
+    double ekin_old = 0.5 * (ru * ru + rv * rv) / rho_new;
+    if (m.dim == 3)
+      ekin_old += 0.5 * (rw * rw) / rho_new;
+    ru += dt * s.grav[0] * (rho_old + rho_new) / 2;
+    rv += dt * s.grav[1] * (rho_old + rho_new) / 2;
+    if (m.dim == 3)
+      rw += dt * s.grav[2] * (rho_old + rho_new) / 2;
+    U2blk[IU * ncell + c] = ru;
+    U2blk[IV * ncell + c] = rv;
+    if (m.dim == 3)
+      U2blk[IW * ncell + c] = rw;
+    double ekin_new = 0.5 * (ru * ru + rv * rv) / rho_new;
+    if (m.dim == 3)
+      ekin_new += 0.5 * (rw * rw) / rho_new;
+    U2blk[IP * ncell + c] += (ekin_new - ekin_old); // total energy (IE == IP)
+  }
+}
+
 static bool
 fine_flux_sum(const Mesh & m, const std::vector<std::vector<double>> & flux_all, const Region & r, int dir,
               int side, const int * q, int v, double & out)
@@ -1503,6 +1657,11 @@ struct oracle_settings
   double  gamma0, cfl, slope_type, smallr, smallc;
   int32_t riemann;
   int32_t time_integrator; // [amr] time_integrator: 0 HANCOCK, 1 RK2_SSP
+  int32_t gravity_enabled; // [gravity] enabled
+  double  gravity[3];      // [gravity] uniform_gx, uniform_gy, uniform_gz
+  int32_t viscosity_enabled; // [viscosity] enabled
+  double  viscosity_mu;      // [viscosity] mu
+  int32_t viscous_predictor; // [viscosity] hancock_predictor_enabled
 };
 
 static Mesh
@@ -1529,6 +1688,12 @@ to_settings(const oracle_settings * os)
 {
   Settings st = make_settings(os->gamma0, os->cfl, os->slope_type, os->smallr, os->smallc, os->riemann);
   st.rk2 = os->time_integrator == 1;
+  st.gravity = os->gravity_enabled != 0;
+  for (int d = 0; d < 3; ++d)
+    st.grav[d] = os->gravity[d];
+  st.viscosity = os->viscosity_enabled != 0;
+  st.mu = os->viscosity_mu;
+  st.visc_predictor = os->viscous_predictor != 0;
   return st;
 }
 
@@ -1558,6 +1723,7 @@ oracle_step(const oracle_mesh * om, const oracle_settings * os, const double * U
   const FluxLayout                 FL = flux_layout(m);
   std::vector<double>              emf_all((size_t)m.n_owned * ne, 0.0);
   std::vector<std::vector<double>> flux_all((size_t)m.n_owned);
+  std::vector<std::vector<double>> visc_all(s.viscosity ? (size_t)m.n_owned : 0);
   int                              status = 0;
   // stages K2-K11 per block: everything up to the face fluxes and the raw edge EMFs
 #pragma omp parallel
@@ -1566,7 +1732,8 @@ oracle_step(const oracle_mesh * om, const oracle_settings * os, const double * U
 #pragma omp for schedule(dynamic, 1)
     for (int blk = 0; blk < m.n_owned; ++blk)
     {
-      const double dtdx = dt / cell_length(m, m.level[blk]);
+      const double dx = cell_length(m, m.level[blk]);
+      const double dtdx = dt / dx;
       flux_all[blk].assign((size_t)FL.total, 0.0);
       int st = fill_bface_ghosted(m, f, blk, w);
       if (st == 0)
@@ -1574,11 +1741,17 @@ oracle_step(const oracle_mesh * om, const oracle_settings * os, const double * U
       if (st == 0)
       {
         compute_slopes(m, s, w);
-        compute_predictor(m, s, dtdx, w);
+        compute_predictor(m, s, dt, dtdx, dx, w);
         compute_elec_field(m, w);
         compute_sfacemag(m, dtdx, w);
         for (int dir = 0; dir < m.dim && st == 0; ++dir)
           st = compute_fluxes(m, s, dtdx, dir, w, flux_all[blk].data());
+        if (s.viscosity)
+        {
+          visc_all[blk].assign((size_t)FL.total, 0.0);
+          for (int dir = 0; dir < m.dim; ++dir)
+            compute_viscous_fluxes(m, s, dtdx, dx, dir, w, visc_all[blk].data());
+        }
         if (st == 0)
           compute_emfs(m, s, dtdx, w, &emf_all[(size_t)blk * ne]);
       }
@@ -1601,8 +1774,14 @@ oracle_step(const oracle_mesh * om, const oracle_settings * os, const double * U
     double * U2blk = U2 + (int64_t)blk * 5 * f.L.ncell;
     double * B2blk = B2 + (int64_t)blk * f.L.nface;
     int      st = update_u(m, blk, flux_all, U2blk, B2blk + f.L.nfx + f.L.nfy);
+    // viscous fluxes through the same update, after the three hydro directions
+    // (GodunovImplemV0.cpp:179-192)
+    if (st == 0 && s.viscosity)
+      st = update_u(m, blk, visc_all, U2blk, B2blk + f.L.nfx + f.L.nfy);
     if (st == 0)
       st = correct_emf_and_update_b(m, blk, emf_all, B2blk);
+    if (st == 0 && s.gravity)
+      add_gravity_source(m, s, dt, U + (int64_t)blk * 5 * f.L.ncell, U2blk, f.L.ncell);
     if (st != 0)
     {
 #pragma omp critical
@@ -1622,6 +1801,40 @@ oracle_step_fluxes(const oracle_mesh * om, const oracle_settings * os, const dou
   const int st = oracle_step(om, os, U, U2, B, B2, dt);
   g_flux_sink = nullptr;
   return st;
+}
+
+// One cell's 1/dt (ComputeDtMHDFunctor.cpp:86-151; with gravity :155-249): the fast speeds v over dx,
+// with gravity corrected by k / (sqrt(1 + 2k) - 1), k = sum|g| dx / |v|^2 (floored at 1e-4); with
+// viscosity at least 4 nu / dx^2, nu = mu / rho (conservative density).
+static double
+cfl_inv_dt(const Mesh & m, const Settings & s, const double * v, double dx, double rho)
+{
+  double val;
+  if (s.gravity)
+  {
+    double v2 = v[0] * v[0] + v[1] * v[1];
+    if (m.dim == 3)
+      v2 += v[2] * v[2];
+    double k = std::fabs(s.grav[0]) + std::fabs(s.grav[1]);
+    if (m.dim == 3)
+      k += std::fabs(s.grav[2]);
+    k *= dx / v2;
+    k = std::fmax(k, 1e-4);
+    const double factor = k / (std::sqrt(1.0 + 2.0 * k) - 1.0);
+    val = 0.0;
+    val += (v[0] * factor) / dx;
+    val += (v[1] * factor) / dx;
+    if (m.dim == 3)
+      val += (v[2] * factor) / dx;
+  }
+  else
+    val = m.dim == 3 ? v[0] / dx + v[1] / dx + v[2] / dx : v[0] / dx + v[1] / dx;
+  if (s.viscosity)
+  {
+    const double nu = s.mu / rho;
+    val = std::fmax(val, 4 * nu / (dx * dx));
+  }
+  return val;
 }
 
 // ComputeDtMHDFunctor::apply over owned blocks; returns invDt (max over cells).
@@ -1644,7 +1857,7 @@ oracle_inv_dt(const oracle_mesh * om, const oracle_settings * os, const double *
       for (int j = 0; j < m.by; ++j)
         for (int i = 0; i < m.bx; ++i)
         {
-          double u[8], q[8], v[3];
+          double u[8], q[8], v[3] = {0.0, 0.0, 0.0};
           for (int n = 0; n < 5; ++n)
             u[n] = f.u(blk, n, i, j, k);
           u[IA] = 0.5 * (f.bx(blk, i, j, k) + f.bx(blk, i + 1, j, k));
@@ -1655,8 +1868,7 @@ oracle_inv_dt(const oracle_mesh * om, const oracle_settings * os, const double *
             u[IC] = 0.5 * (f.bz(blk, i, j, 0) + f.bz(blk, i, j, 0));
           compute_primitives(u, q, nullptr, s);
           find_speed_info(q, m.dim, v, s);
-          double val = m.dim == 3 ? v[0] / dx + v[1] / dx + v[2] / dx : v[0] / dx + v[1] / dx;
-          inv_dt = std::fmax(inv_dt, val);
+          inv_dt = std::fmax(inv_dt, cfl_inv_dt(m, s, v, dx, u[ID]));
         }
   }
   return inv_dt;

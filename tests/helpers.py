@@ -21,7 +21,8 @@ def oracle_mesh(orc, mesh: BlockMesh, bc=None):
 def oracle_settings(orc, st: MHDSettings):
     return orc.settings(gamma0=st.gamma0, cfl=st.cfl, slope_type=st.slope_type, smallr=st.smallr,
                         smallc=st.smallc, riemann=st.riemann_id,
-                        time_integrator=1 if st.time_integrator.upper() == "RK2_SSP" else 0)
+                        time_integrator=1 if st.time_integrator.upper() == "RK2_SSP" else 0,
+                        gravity=st.gravity, viscosity_mu=st.viscosity_mu, viscous_predictor=st.viscous_predictor)
 
 
 def max_rel_diff(a, b):
