@@ -36,6 +36,9 @@ struct StepArgs
   int     tiles_x, tiles_y, tiles_z;
   int64_t ncell, nfx, nfy, nface;
   double  gamma0, smallr, smallc, smallp, slope_type, scaling_factor, cfl;
+  // the same in FP32 for the mixed path (converted once on the host: each FP64 conversion in the
+  // kernel is an FP64-pipe instruction per warp)
+  float   gamma0_f, smallr_f, smallc_f, smallp_f, slope_type_f;
   int     riemann;
   int     rk2;                                  // [amr] time_integrator RK2_SSP: no Hancock half step
   double  dt;                                   // used when dt_dev is null
@@ -168,6 +171,16 @@ struct Cfg
   static constexpr int TOTAL = OFF_U1 + (U1_EARLY > U1_LATE ? U1_EARLY : U1_LATE);
   static constexpr size_t SMEM_BYTES = sizeof(R) * (size_t)TOTAL + 64 * sizeof(int);
 
+  // Persistent, software-pipelined variant (mixed precision, conforming 3D meshes): one CTA per SM
+  // loops over tiles; after phase 5 of a tile it stages the next tile's FP64 gather (face B and U of
+  // the Q region, in the layout of fbx|fby|fbz and of the primitives) into [OFF_SL, OFF_U1) with
+  // cp.async, and those copies land while phases 6-7 run.
+  static constexpr int  NFB = NFBX + NFBY + NFBZ;
+  static constexpr int  STAGE_DOUBLES = NFB + 5 * NQ;
+  static constexpr bool PIPE = !EXACT && !AMR && !VISC && DIM == 3 && NFBX % 2 == 0 && NFBY % 2 == 0 &&
+                               NFBZ % 2 == 0 && NQ % 2 == 0 && (OFF_SL * sizeof(R)) % 16 == 0 &&
+                               (size_t)STAGE_DOUBLES * 8 <= (size_t)(OFF_U1 - OFF_SL) * sizeof(R);
+
   static constexpr int NCELL = TX * TY * TZ;
   static constexpr int CPT = (NCELL + NT - 1) / NT;
 
@@ -293,6 +306,30 @@ fine_face_flux(const StepArgs & a, int blk, int slot, int d, int side, int g1, i
                            (int64_t)bs[t1] * F2];
     }
   return acc / (double)(1 << C::DIM);
+}
+
+// Asynchronous global -> shared copies (cp.async, sm_80+): 8 bytes through L1, 16 bytes bypassing it.
+__device__ __forceinline__ void
+cp_async8(void * smem_dst, const void * gmem_src)
+{
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void
+cp_async16(void * smem_dst, const void * gmem_src)
+{
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void
+cp_async_commit()
+{
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void
+cp_async_wait_all()
+{
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
 __device__ __forceinline__ int
@@ -759,15 +796,158 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
   R *      fl = sm + C::OFF_FL;
   R *      b2s = sm + C::OFF_B2;
   R *      vel = sm + C::OFF_VEL; // viscous variants: t^n velocities of cells [-1, T]
-  int * s_nbr = reinterpret_cast<int *>(sm + C::TOTAL);
+  int * s_nbr0 = reinterpret_cast<int *>(sm + C::TOTAL); // [32] neighbours (+ [32] region kinds or a 2nd table)
   __shared__ double       s_red[NT / 32];
   __shared__ unsigned int s_health;
+  __shared__ unsigned int s_stage_health[2]; // PIPE: missing / level-jump flags of a staged tile
+  __shared__ unsigned int s_stage_jump[2];   // PIPE: neighbour slots at another level
 
   const int tid = threadIdx.x;
   const int tiles_per_block = a.tiles_x * a.tiles_y * a.tiles_z;
-  int       tile = blockIdx.x;
+  const int bx = a.bx, by = a.by, bz = a.bz;
+  auto cell_off = [](int c, int n) { return c < 0 ? -1 : (c >= n ? 1 : 0); };
+  auto face_off = [](int f, int n) { return f < 0 ? -1 : (f > n ? 1 : 0); };
+
+  // ---- PIPE: staging of a tile's gather ----------------------------------------------------------
+  double *  stage = reinterpret_cast<double *>(sm + C::OFF_SL);
+  const int n_work = C::PIPE ? a.n_owned * tiles_per_block : 0;
+  // neighbour table of tile w into buffer buf (warp 0), with the slots whose block is at another level
+  auto load_nbr = [&](int w, int buf) {
+    if (tid < 32)
+    {
+      const int b = w / tiles_per_block;
+      int       nb = -1;
+      bool      jump = false;
+      if (tid < 27)
+      {
+        nb = a.neighbor[(int64_t)b * 27 + tid];
+        jump = nb >= 0 && nb < a.n_blocks && a.level[nb] != a.level[b];
+        s_nbr0[32 * buf + tid] = nb;
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, jump);
+      if (tid == 0)
+      {
+        s_stage_jump[buf] = m;
+        s_stage_health[buf] = 0u;
+      }
+    }
+  };
+  // issue the cp.async copies of tile w's face B and U (Q region) into the staging area; absent
+  // neighbours give 0 (faces) and rho = E = 1, momenta 0 (as the direct gather)
+  auto stage_tile = [&](int w, int buf) {
+    const int   b = w / tiles_per_block;
+    int         t = w - b * tiles_per_block;
+    const int   sx0 = (t % a.tiles_x) * TX;
+    t /= a.tiles_x;
+    const int   sy0 = (t % a.tiles_y) * TY, sz0 = (t / a.tiles_y) * TZ;
+    const int * nbr = s_nbr0 + 32 * buf;
+    const unsigned jm = s_stage_jump[buf];
+    unsigned    fl = 0u;
+    auto        own = [&](int ox, int oy, int oz) -> int {
+      if ((ox | oy | oz) == 0)
+        return b;
+      const int sl = nb_slot(ox, oy, oz);
+      const int nb = nbr[sl];
+      if (nb < 0)
+        fl |= HEALTH_MISSING_NEIGHBOR;
+      else if ((jm >> sl) & 1u)
+        fl |= HEALTH_LEVEL_JUMP;
+      return nb;
+    };
+    for (int n = tid; n < C::NFBX; n += NT)
+    {
+      const int i = n % (TX + 5) - 2;
+      const int j = (n / (TX + 5)) % C::QY - 2;
+      const int k = n / ((TX + 5) * C::QY) - 2;
+      const int fi = sx0 + i, cj = sy0 + j, ck = sz0 + k;
+      const int ox = face_off(fi, bx), oy = cell_off(cj, by), oz = cell_off(ck, bz);
+      const int nb = own(ox, oy, oz);
+      if (nb >= 0)
+        cp_async8(stage + n, a.B + (int64_t)nb * a.nface + (fi - ox * bx) +
+                               (int64_t)(bx + 1) * ((cj - oy * by) + (int64_t)by * (ck - oz * bz)));
+      else
+        stage[n] = 0.0;
+    }
+    for (int m = tid; m < C::NFBY / 2; m += NT)
+    {
+      const int n = 2 * m;
+      const int i = n % C::QX - 2;
+      const int j = (n / C::QX) % (TY + 5) - 2;
+      const int k = n / (C::QX * (TY + 5)) - 2;
+      const int ci = sx0 + i, fj = sy0 + j, ck = sz0 + k;
+      const int ox = cell_off(ci, bx), oy = face_off(fj, by), oz = cell_off(ck, bz);
+      const int nb = own(ox, oy, oz);
+      double *  d = stage + C::NFBX + n;
+      if (nb >= 0)
+        cp_async16(d, a.B + (int64_t)nb * a.nface + a.nfx + (ci - ox * bx) +
+                        (int64_t)bx * ((fj - oy * by) + (int64_t)(by + 1) * (ck - oz * bz)));
+      else
+        d[0] = d[1] = 0.0;
+    }
+    for (int m = tid; m < C::NFBZ / 2; m += NT)
+    {
+      const int n = 2 * m;
+      const int i = n % C::QX - 2;
+      const int j = (n / C::QX) % C::QY - 2;
+      const int k = n / (C::QX * C::QY) - 2;
+      const int ci = sx0 + i, cj = sy0 + j, fk = sz0 + k;
+      const int ox = cell_off(ci, bx), oy = cell_off(cj, by), oz = face_off(fk, bz);
+      const int nb = own(ox, oy, oz);
+      double *  d = stage + C::NFBX + C::NFBY + n;
+      if (nb >= 0)
+        cp_async16(d, a.B + (int64_t)nb * a.nface + a.nfx + a.nfy + (ci - ox * bx) +
+                        (int64_t)bx * ((cj - oy * by) + (int64_t)by * (fk - oz * bz)));
+      else
+        d[0] = d[1] = 0.0;
+    }
+    for (int m = tid; m < C::NQ / 2; m += NT)
+    {
+      const int n = 2 * m;
+      const int i = n % C::QX - 2;
+      const int j = (n / C::QX) % C::QY - 2;
+      const int k = n / (C::QX * C::QY) - 2;
+      const int ci = sx0 + i, cj = sy0 + j, ck = sz0 + k;
+      const int ox = cell_off(ci, bx), oy = cell_off(cj, by), oz = cell_off(ck, bz);
+      const int nb = own(ox, oy, oz);
+      double *  d = stage + C::NFB + n;
+      if (nb >= 0)
+      {
+        const double * Ub = a.U + (int64_t)nb * 5 * a.ncell + (ci - ox * bx) +
+                            (int64_t)bx * ((cj - oy * by) + (int64_t)by * (ck - oz * bz));
+#pragma unroll
+        for (int v = 0; v < 5; ++v)
+          cp_async16(d + v * C::NQ, Ub + (int64_t)v * a.ncell);
+      }
+      else
+      {
+#pragma unroll
+        for (int v = 0; v < 5; ++v)
+          d[v * C::NQ] = d[v * C::NQ + 1] = v < 2 ? 1.0 : 0.0;
+      }
+    }
+    cp_async_commit();
+    if (fl)
+      atomicOr(&s_stage_health[buf], fl);
+  };
+  if constexpr (C::PIPE)
+  {
+    if ((int)blockIdx.x < n_work)
+    {
+      load_nbr(blockIdx.x, 0);
+      __syncthreads();
+      stage_tile(blockIdx.x, 0);
+    }
+  }
+
+  // one tile per CTA, or (PIPE) tiles blockIdx.x, blockIdx.x + gridDim.x, ...
+  for (int iter = 0, work = blockIdx.x; C::PIPE ? work < n_work : iter == 0; ++iter, work += gridDim.x)
+  {
+  const int buf = iter & 1;
+  const bool has_next = C::PIPE && work + (int)gridDim.x < n_work;
+  int *     s_nbr = s_nbr0 + (C::PIPE ? 32 * buf : 0);
+  int       tile = C::PIPE ? work : (int)blockIdx.x;
   bool      side_only = false; // pass 1 of a tile that also runs in pass 2: side data only
-  if (a.tile_list)
+  if (!C::PIPE && a.tile_list)
   {
     tile = a.tile_list[blockIdx.x];
     if (tile < 0)
@@ -785,23 +965,31 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
   const int ty = t % a.tiles_y;
   const int tz = t / a.tiles_y;
   const int x0 = tx * TX, y0 = ty * TY, z0 = tz * TZ;
-  const int bx = a.bx, by = a.by, bz = a.bz;
 
-  int * s_kind = s_nbr + 32;
-  if (tid < 27)
+  int * s_kind = s_nbr0 + 32;
+  if constexpr (C::PIPE)
   {
-    s_nbr[tid] = a.neighbor[(int64_t)blk * 27 + tid];
-    if constexpr (C::AMR)
-      s_kind[tid] = (int)a.kind[(int64_t)blk * 27 + tid];
+    cp_async_wait_all(); // this tile's staged gather (issued during the previous tile)
+    if (tid == 0)
+      s_health = s_stage_health[buf];
   }
-  if (tid == 0)
-    s_health = 0u;
+  else
+  {
+    if (tid < 27)
+    {
+      s_nbr[tid] = a.neighbor[(int64_t)blk * 27 + tid];
+      if constexpr (C::AMR)
+        s_kind[tid] = (int)a.kind[(int64_t)blk * 27 + tid];
+    }
+    if (tid == 0)
+      s_health = 0u;
+  }
   __syncthreads();
 
   const int myprob = a.problem ? a.problem[blk] : 0;
   const int mylevel = a.level[blk];
   const double dt = a.dt_dev ? a.dt_dev[myprob] : a.dt;
-  if (dt == 0.0)
+  if ((__double_as_longlong(dt) << 1) == 0) // dt == +-0 (integer test: no FP64 instruction per warp)
   {
     // a problem that has reached its end time: carry the tile over unchanged
     for (int n = tid; n < C::NCELL; n += NT)
@@ -815,19 +1003,47 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
     for (int64_t f = (int64_t)(tile - blk * tiles_per_block) * NT + tid; f < a.nface;
          f += (int64_t)tiles_per_block * NT)
       a.B2[(int64_t)blk * a.nface + f] = a.B[(int64_t)blk * a.nface + f];
-    return;
+    if constexpr (C::PIPE)
+    {
+      __syncthreads(); // staged data of this tile unused; the area takes the next tile's
+      if (has_next)
+        stage_tile(work + gridDim.x, buf ^ 1);
+      continue;
+    }
+    else
+      return;
   }
-  const double dx = (1.0 / (double)((int64_t)bx << mylevel)) * a.scaling_factor;
-  const double dtdx_d = dt / dx;
-  const R      dtdx = (R)dtdx_d;
-  const R      dxr = (R)dx;
+  // tile constants in FP64, computed by one thread (FP64 divisions issued by every warp would cost
+  // more than the whole gather on GB300) and read after the phase-1 barrier
+  __shared__ double s_tc[1]; // dx
+  __shared__ R      s_tr[3]; // (R)dx, (R)(dt/dx), (R)(1/dx)
+  if (tid == 0)
+  {
+    const double dx0 = (1.0 / (double)((int64_t)bx << mylevel)) * a.scaling_factor;
+    const double dtdx0 = dt / dx0;
+    s_tc[0] = dx0;
+    s_tr[0] = (R)dx0;
+    s_tr[1] = (R)dtdx0;
+    s_tr[2] = (R)(1.0 / dx0);
+  }
 
   Phys<R> ph;
-  ph.gamma0 = (R)a.gamma0;
-  ph.smallr = (R)a.smallr;
-  ph.smallc = (R)a.smallc;
-  ph.smallp = (R)a.smallp;
-  ph.slope_type = (R)a.slope_type;
+  if constexpr (std::is_same<R, float>::value)
+  {
+    ph.gamma0 = a.gamma0_f;
+    ph.smallr = a.smallr_f;
+    ph.smallc = a.smallc_f;
+    ph.smallp = a.smallp_f;
+    ph.slope_type = a.slope_type_f;
+  }
+  else
+  {
+    ph.gamma0 = a.gamma0;
+    ph.smallr = a.smallr;
+    ph.smallc = a.smallc;
+    ph.smallp = a.smallp;
+    ph.slope_type = a.slope_type;
+  }
   ph.riemann = a.riemann;
 
   unsigned int health = 0u;
@@ -872,9 +1088,6 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       }
     }
   };
-  auto cell_off = [](int c, int n) { return c < 0 ? -1 : (c >= n ? 1 : 0); };
-  auto face_off = [](int f, int n) { return f < 0 ? -1 : (f > n ? 1 : 0); };
-
   // ---- phase 1: gather face B at t^n (FillBlockGhostFaces equivalent) and the conservative state
   // of the Q region. Every global load of the phase is issued before any is consumed, so HBM latency
   // is paid once for the phase rather than once per loop trip.
@@ -886,9 +1099,17 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
   constexpr int ITZ = (C::NFBZ / 2 + NT - 1) / NT;
   constexpr int ITQ = (C::NQ / 2 + NT - 1) / NT;
   static_assert(C::QX % 2 == 0, "pair loads need an even Q-region width");
-  double        fvx[ITX];
-  double2       fvy[ITY], fvz[ITZ];
-  double2       uq[ITQ][5];
+  double        fvx[C::PIPE ? 1 : ITX];
+  double2       fvy[C::PIPE ? 1 : ITY], fvz[C::PIPE ? 1 : ITZ];
+  double2       uq[C::PIPE ? 1 : ITQ][5];
+  if constexpr (C::PIPE)
+  {
+    // the gather was staged by cp.async during the previous tile: convert the faces
+    for (int n = tid; n < C::NFB; n += NT)
+      fbx[n] = to_r<R>(stage[n]);
+  }
+  else
+  {
 #pragma unroll
   for (int it = 0; it < ITX; ++it)
   {
@@ -996,7 +1217,18 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       fbz[n + 1] = to_r<R>(fvz[it].y);
     }
   }
+  }
   __syncthreads();
+  const double dx = s_tc[0];
+  const R      dtdx = s_tr[1];
+  const R      dxr = s_tr[0];
+  const R      idxr = s_tr[2];
+  if constexpr (C::PIPE)
+  {
+    // the next tile's neighbour table: its loads have the rest of this tile to land
+    if (has_next)
+      load_nbr(work + gridDim.x, buf ^ 1);
+  }
 
   // SIMPLE_COPY ghosts of a coarser neighbour take the coarse cell's own cell-centred B
   // (ConvertToPrimitivesVariablesFunctor.cpp:439-446), kept by the ghost prepass in Bccv
@@ -1016,21 +1248,12 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
     return true;
   };
 
-  // primitive variables on the Q region (ConvertToPrimitivesVariablesFunctor), two x-adjacent cells
-  // per thread and iteration
-#pragma unroll
-  for (int ie = 0; ie < 2 * ITQ; ++ie)
-  {
-    const int it = ie >> 1, e = ie & 1;
-    const int n = 2 * (tid + it * NT) + e;
-    if (n >= C::NQ)
-      continue;
+  // primitive variables on the Q region (ConvertToPrimitivesVariablesFunctor) of cell item n
+  auto prim_cell = [&](int n, const double * u) {
     const int i = n % C::QX - 2;
     const int j = (n / C::QX) % C::QY - 2;
     const int k = D3 ? n / (C::QX * C::QY) - 2 : 0;
     const int ci = x0 + i, cj = y0 + j, ck = z0 + k;
-    const double u[5] = {e ? uq[it][0].y : uq[it][0].x, e ? uq[it][1].y : uq[it][1].x, e ? uq[it][2].y : uq[it][2].x,
-                         e ? uq[it][3].y : uq[it][3].x, e ? uq[it][4].y : uq[it][4].x};
     const int qn = C::qi(i, j, k);
     if constexpr (C::EXACT)
     {
@@ -1128,6 +1351,31 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       qh[2 * C::NQ + qn] = vx;
       qh[3 * C::NQ + qn] = vy;
       qh[4 * C::NQ + qn] = vz;
+    }
+  };
+  if constexpr (C::PIPE)
+  {
+    for (int n = tid; n < C::NQ; n += NT)
+    {
+      const double u[5] = {stage[C::NFB + n], stage[C::NFB + C::NQ + n], stage[C::NFB + 2 * C::NQ + n],
+                           stage[C::NFB + 3 * C::NQ + n], stage[C::NFB + 4 * C::NQ + n]};
+      prim_cell(n, u);
+    }
+  }
+  else
+  {
+    // two x-adjacent cells per thread and iteration
+#pragma unroll
+    for (int ie = 0; ie < 2 * ITQ; ++ie)
+    {
+      const int it = ie >> 1, e = ie & 1;
+      const int n = 2 * (tid + it * NT) + e;
+      if (n >= C::NQ)
+        continue;
+      const double u[5] = {e ? uq[it][0].y : uq[it][0].x, e ? uq[it][1].y : uq[it][1].x,
+                           e ? uq[it][2].y : uq[it][2].x, e ? uq[it][3].y : uq[it][3].x,
+                           e ? uq[it][4].y : uq[it][4].x};
+      prim_cell(n, u);
     }
   }
   __syncthreads();
@@ -1426,6 +1674,13 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       flux_pass<C, 2>(tv, tid);
   }
   __syncthreads();
+  if constexpr (C::PIPE)
+  {
+    // slopes, predictor and face source are dead: their area receives the next tile's gather while
+    // phases 6-7 run
+    if (has_next)
+      stage_tile(work + gridDim.x, buf ^ 1);
+  }
   if constexpr (C::AMR)
   {
     amr_border_fluxes<C>(a, fl, s_kind, blk, x0, y0, z0, tid, vel, dxr, dtdx);
@@ -1545,7 +1800,8 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
 
   // ---- phase 7: conservative update (ReadFluxesAndConservativeUpdateFunctor.cpp:240-436),
   // write U2 (and 2D Bz), fused CFL of the new state (ComputeDtMHDFunctor.cpp:86-151) ----------
-  double my_invdt = 0.0;
+  double my_invdt = 0.0;   // FP64 path
+  float  my_invdt_f = 0.0f; // mixed path: FP32 maximum, widened once per CTA
 #pragma unroll
   for (int c = 0; c < C::CPT; ++c)
   {
@@ -1685,16 +1941,21 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       a.U2[((int64_t)blk * 5 + v) * a.ncell + cell] = u2[v];
     if constexpr (DIM == 2)
       a.B2[(int64_t)blk * a.nface + a.nfx + a.nfy + cell] = u2[5];
-    if (!(u2[ID] > 0.0))
-      health |= HEALTH_BAD_DENSITY;
-    if (!isfinite(u2[IP]) || !isfinite(u2[IU]))
-      health |= HEALTH_NONFINITE;
+    // u2[ID] > 0 and finite E, rho u, as integer tests on the bit patterns
+    {
+      const long long bd = __double_as_longlong(u2[ID]);
+      if (!(bd > 0 && bd <= 0x7ff0000000000000LL))
+        health |= HEALTH_BAD_DENSITY;
+      const long long ex = 0x7ff0000000000000LL;
+      if ((__double_as_longlong(u2[IP]) & ex) == ex || (__double_as_longlong(u2[IU]) & ex) == ex)
+        health |= HEALTH_NONFINITE;
+    }
 
     if (a.invdt_out)
     {
       const R Axl = b2s[i + (TX + 1) * (j + TY * k)], Axr = b2s[i + 1 + (TX + 1) * (j + TY * k)];
       const R Ayl = b2s[C::NB2X + i + TX * (j + (TY + 1) * k)], Ayr = b2s[C::NB2X + i + TX * (j + 1 + (TY + 1) * k)];
-      double  val;
+      [[maybe_unused]] double val = 0.0; // FP64 path
       if constexpr (C::EXACT)
       {
         const double Ax = 0.5 * (Axl + Axr);
@@ -1745,9 +2006,10 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
         float       cfz = 0.0f;
         if constexpr (DIM == 3)
           cfz = sqrtf(d2 + sqrtf(fmaxf(d2 * d2 - c2 * bzf * bzf * ir, 0.0f))) + fabsf(vz);
-        val = to_d<R>(cfl_inv_dt_fp32(DIM, cfx, cfy, cfz, (float)dx, (float)(1.0 / dx), to_r<R>(u2[ID]), a.src));
+        my_invdt_f = fmaxf(my_invdt_f, cfl_inv_dt_fp32(DIM, cfx, cfy, cfz, dxr, idxr, to_r<R>(u2[ID]), a.src));
       }
-      my_invdt = fmax(my_invdt, val);
+      if constexpr (C::EXACT)
+        my_invdt = fmax(my_invdt, val);
     }
   }
 
@@ -1755,25 +2017,48 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
     atomicOr(&s_health, health);
   if (a.invdt_out)
   {
+    if constexpr (C::EXACT)
+    {
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1)
-      my_invdt = fmax(my_invdt, __shfl_xor_sync(0xffffffffu, my_invdt, off));
-    if ((tid & 31) == 0)
-      s_red[tid >> 5] = my_invdt;
+      for (int off = 16; off > 0; off >>= 1)
+        my_invdt = fmax(my_invdt, __shfl_xor_sync(0xffffffffu, my_invdt, off));
+      if ((tid & 31) == 0)
+        s_red[tid >> 5] = my_invdt;
+    }
+    else
+    {
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1)
+        my_invdt_f = fmaxf(my_invdt_f, __shfl_xor_sync(0xffffffffu, my_invdt_f, off));
+      if ((tid & 31) == 0)
+        reinterpret_cast<float *>(s_red)[tid >> 5] = my_invdt_f;
+    }
   }
   __syncthreads();
   if (tid == 0)
   {
     if (a.invdt_out)
     {
-      double m = s_red[0];
-      for (int w = 1; w < NT / 32; ++w)
-        m = fmax(m, s_red[w]);
+      double m;
+      if constexpr (C::EXACT)
+      {
+        m = s_red[0];
+        for (int w = 1; w < NT / 32; ++w)
+          m = fmax(m, s_red[w]);
+      }
+      else
+      {
+        float mf = reinterpret_cast<const float *>(s_red)[0];
+        for (int w = 1; w < NT / 32; ++w)
+          mf = fmaxf(mf, reinterpret_cast<const float *>(s_red)[w]);
+        m = f2d_bits(mf);
+      }
       atomic_max_pos_double(&a.invdt_out[myprob], m);
     }
     if (s_health)
       atomicOr(a.health, s_health);
   }
+  } // tile loop
 }
 
 } // namespace gmhd

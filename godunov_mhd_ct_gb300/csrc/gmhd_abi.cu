@@ -238,6 +238,11 @@ make_args(const gmhd_ctx * c, const double * U, double * U2, const double * B, d
   a.scaling_factor = c->p.scaling_factor;
   a.cfl = c->p.cfl;
   a.riemann = c->p.riemann;
+  a.gamma0_f = (float)a.gamma0;
+  a.smallr_f = (float)a.smallr;
+  a.smallc_f = (float)a.smallc;
+  a.smallp_f = (float)a.smallp;
+  a.slope_type_f = (float)a.slope_type;
   a.rk2 = c->p.time_integrator == GMHD_TIME_RK2_SSP;
   a.health = c->d_health;
   a.n_blocks = c->n_blocks;

@@ -10,6 +10,15 @@ namespace gmhd
 
 // Launch the fused step for configuration C. Returns a cudaError_t (0 on success) or -1 when the
 // tile does not divide the block.
+// Resident CTAs of configuration C on the whole device (persistent variants), set by prepare_fused.
+template <class C>
+int &
+resident_ctas()
+{
+  static int n = 0;
+  return n;
+}
+
 template <class C>
 int
 launch_fused(StepArgs a, cudaStream_t stream)
@@ -19,21 +28,39 @@ launch_fused(StepArgs a, cudaStream_t stream)
   a.tiles_x = a.bx / C::TX;
   a.tiles_y = a.by / C::TY;
   a.tiles_z = C::DIM == 3 ? a.bz / C::TZ : 1;
-  const long long nblocks = a.tile_list ? (long long)a.n_list : (long long)a.n_owned * a.tiles_x * a.tiles_y * a.tiles_z;
+  long long nblocks = a.tile_list ? (long long)a.n_list : (long long)a.n_owned * a.tiles_x * a.tiles_y * a.tiles_z;
   if (nblocks <= 0)
     return 0;
+  if constexpr (C::PIPE)
+  {
+    // one persistent CTA per resident slot, each looping over tiles
+    if (a.tile_list || resident_ctas<C>() <= 0)
+      return -1;
+    nblocks = nblocks < resident_ctas<C>() ? nblocks : resident_ctas<C>();
+  }
   fused_step_kernel<C><<<(unsigned)nblocks, C::NT, C::SMEM_BYTES, stream>>>(a);
   return (int)cudaGetLastError();
 }
 
-// Opt configuration C into its dynamic shared-memory size on the current device. Called when a
-// context is created, so that no attribute call happens while a stream is being captured.
+// Opt configuration C into its dynamic shared-memory size on the current device and record how
+// many CTAs of it the device holds. Called when a context is created, so that no attribute call
+// happens while a stream is being captured.
 template <class C>
 int
 prepare_fused()
 {
-  return (int)cudaFuncSetAttribute(fused_step_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)C::SMEM_BYTES);
+  cudaError_t e = cudaFuncSetAttribute(fused_step_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)C::SMEM_BYTES);
+  if (e != cudaSuccess || !C::PIPE)
+    return (int)e;
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
+      (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
+      (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fused_step_kernel<C>, C::NT, C::SMEM_BYTES)) !=
+        cudaSuccess)
+    return (int)e;
+  resident_ctas<C>() = sms * (per_sm > 0 ? per_sm : 1);
+  return 0;
 }
 
 // Tile choice: the largest configured tile that divides the block. With a.src.viscosity the
