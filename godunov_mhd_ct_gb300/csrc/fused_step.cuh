@@ -648,7 +648,30 @@ recon_edge(const TileView<C> & t, int sc, int fb0, int fb1, typename C::R * q)
 
 // EMFs along direction CD on the tile's edges [0, T] (ComputeEmfAndStoreFunctor.cpp:371-590), with
 // the border averaging of CorrectEmfAtBlockBorderFunctor (uniform level, .cpp:298-356)
+// Items of the phase-5 passes are dealt round-robin to the threads, each pass starting where the
+// previous one stopped (START = items dealt before, mod NT), so that no thread gets the remainder
+// of every pass.
+template <class C>
+__device__ __forceinline__ int
+first_item(int tid, int start)
+{
+  const int m0 = tid - start;
+  return m0 < 0 ? m0 + C::NT : m0;
+}
 template <class C, int CD>
+__device__ constexpr int
+edge_count()
+{
+  return (CD == 0 ? C::TX : C::TX + 1) * (CD == 1 ? C::TY : C::TY + 1) * (C::DIM == 3 ? (CD == 2 ? C::TZ : C::TZ + 1) : 1);
+}
+template <class C, int D>
+__device__ constexpr int
+face_count()
+{
+  return (C::TX + (D == 0)) * (C::TY + (D == 1)) * (C::TZ + (D == 2 && C::D3));
+}
+
+template <class C, int CD, int START>
 __device__ __forceinline__ void
 edge_pass(const TileView<C> & t, int tid)
 {
@@ -661,7 +684,7 @@ edge_pass(const TileView<C> & t, int tid)
   constexpr int s0 = s_stride<C>(D0), s1 = s_stride<C>(D1);
   constexpr int f00 = f_stride<C>(D0, D0), f01 = f_stride<C>(D0, D1);
   constexpr int f10 = f_stride<C>(D1, D0), f11 = f_stride<C>(D1, D1);
-  for (int m = tid; m < NX * NY * NZ; m += C::NT)
+  for (int m = first_item<C>(tid, START); m < NX * NY * NZ; m += C::NT)
   {
     const int i = m % NX, j = (m / NX) % NY, k = m / (NX * NY);
     const int sc = C::si(i, j, k);
@@ -723,7 +746,7 @@ edge_pass(const TileView<C> & t, int tid)
 
 // Fluxes through the tile's faces normal to D (ComputeHydroFluxesAndStoreFunctor.cpp:335-503):
 // left state from cell i-1, right state from cell i, normal B = face value + sFaceMag.
-template <class C, int D>
+template <class C, int D, int START>
 __device__ __forceinline__ void
 flux_pass(const TileView<C> & t, int tid)
 {
@@ -734,7 +757,7 @@ flux_pass(const TileView<C> & t, int tid)
   constexpr int imag = D == 0 ? IA : (D == 1 ? IB : IC);
   constexpr int NS = C::NS;
   const R *     S = t.sl + D * 8 * NS;
-  for (int m = tid; m < NX * NY * NZ; m += C::NT)
+  for (int m = first_item<C>(tid, START); m < NX * NY * NZ; m += C::NT)
   {
     const int i = m % NX, j = (m / NX) % NY, k = m / (NX * NY);
     const int snR = C::si(i, j, k);
@@ -1662,16 +1685,20 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
                       ? a.emf_side + (int64_t)a.emf_slot[blk] * C::NECOMP * ((int64_t)(bx + 1) * (by + 1) * (D3 ? bz + 1 : 1))
                       : nullptr;
     }
-    edge_pass<C, 2>(tv, tid);
+    constexpr int E2 = edge_count<C, 2>();
+    constexpr int E1 = DIM == 3 ? edge_count<C, 1>() : 0;
+    constexpr int E0 = DIM == 3 ? edge_count<C, 0>() : 0;
+    constexpr int F0 = face_count<C, 0>(), F1 = face_count<C, 1>();
+    edge_pass<C, 2, 0>(tv, tid);
     if constexpr (DIM == 3)
     {
-      edge_pass<C, 1>(tv, tid);
-      edge_pass<C, 0>(tv, tid);
+      edge_pass<C, 1, E2 % NT>(tv, tid);
+      edge_pass<C, 0, (E2 + E1) % NT>(tv, tid);
     }
-    flux_pass<C, 0>(tv, tid);
-    flux_pass<C, 1>(tv, tid);
+    flux_pass<C, 0, (E2 + E1 + E0) % NT>(tv, tid);
+    flux_pass<C, 1, (E2 + E1 + E0 + F0) % NT>(tv, tid);
     if constexpr (DIM == 3)
-      flux_pass<C, 2>(tv, tid);
+      flux_pass<C, 2, (E2 + E1 + E0 + F0 + F1) % NT>(tv, tid);
   }
   __syncthreads();
   if constexpr (C::PIPE)
