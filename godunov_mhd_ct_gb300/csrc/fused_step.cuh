@@ -1701,13 +1701,6 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       flux_pass<C, 2, (E2 + E1 + E0 + F0 + F1) % NT>(tv, tid);
   }
   __syncthreads();
-  if constexpr (C::PIPE)
-  {
-    // slopes, predictor and face source are dead: their area receives the next tile's gather while
-    // phases 6-7 run
-    if (has_next)
-      stage_tile(work + gridDim.x, buf ^ 1);
-  }
   if constexpr (C::AMR)
   {
     amr_border_fluxes<C>(a, fl, s_kind, blk, x0, y0, z0, tid, vel, dxr, dtdx);
@@ -1770,6 +1763,13 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
         if constexpr (DIM == 2)
           upre[c][5] = a.B[(int64_t)blk * a.nface + a.nfx + a.nfy + cell];
       }
+    }
+    if constexpr (C::PIPE)
+    {
+      // slopes, predictor and face source are dead: their area receives the next tile's gather while
+      // the loads above are in flight and phases 6-7 run
+      if (has_next)
+        stage_tile(work + gridDim.x, buf ^ 1);
     }
 #pragma unroll
     for (int it = 0; it < ITB; ++it)
