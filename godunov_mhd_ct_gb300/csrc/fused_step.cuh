@@ -648,6 +648,24 @@ recon_edge(const TileView<C> & t, int sc, int fb0, int fb1, typename C::R * q)
 
 // EMFs along direction CD on the tile's edges [0, T] (ComputeEmfAndStoreFunctor.cpp:371-590), with
 // the border averaging of CorrectEmfAtBlockBorderFunctor (uniform level, .cpp:298-356)
+// Face increment of the CT update from two EMF differences: the reference's "d = 0; d += a; d -= b"
+// (ReadEmfAndUpdateFunctor.cpp:118-161) on the FP64 path; a - b on the mixed path, the same value
+// up to the sign of a zero, one FP64 instruction less per face.
+template <bool EXACT>
+__device__ __forceinline__ double
+curl2(double a, double b)
+{
+  if constexpr (EXACT)
+  {
+    double d = 0;
+    d += a;
+    d -= b;
+    return d;
+  }
+  else
+    return a - b;
+}
+
 // Items of the phase-5 passes are dealt round-robin to the threads, each pass starting where the
 // previous one stopped (START = items dealt before, mod NT), so that no thread gets the remainder
 // of every pass.
@@ -1782,14 +1800,11 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       if (n < C::NB2X)
       {
         const int i = n % (TX + 1), j = (n / (TX + 1)) % TY, k = n / ((TX + 1) * TY);
-        double    d = 0;
+        double d;
         if constexpr (DIM == 2)
-          d += (Mz[C::mi(i, j + 1, 0)] - Mz[C::mi(i, j, 0)]);
+          d = curl2<C::EXACT>(Mz[C::mi(i, j + 1, 0)] - Mz[C::mi(i, j, 0)], 0.0);
         else
-        {
-          d += (Mz[C::mi(i, j + 1, k)] - Mz[C::mi(i, j, k)]);
-          d -= (My[C::mi(i, j, k + 1)] - My[C::mi(i, j, k)]);
-        }
+          d = curl2<C::EXACT>(Mz[C::mi(i, j + 1, k)] - Mz[C::mi(i, j, k)], My[C::mi(i, j, k + 1)] - My[C::mi(i, j, k)]);
         bnew = bold[it] + d;
         owned = i < TX || ex;
       }
@@ -1801,9 +1816,8 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
           bnew = bold[it] - (Mz[C::mi(i + 1, j, 0)] - Mz[C::mi(i, j, 0)]);
         else
         {
-          double d = 0;
-          d += (Mx[C::mi(i, j, k + 1)] - Mx[C::mi(i, j, k)]);
-          d -= (Mz[C::mi(i + 1, j, k)] - Mz[C::mi(i, j, k)]);
+          const double d =
+            curl2<C::EXACT>(Mx[C::mi(i, j, k + 1)] - Mx[C::mi(i, j, k)], Mz[C::mi(i + 1, j, k)] - Mz[C::mi(i, j, k)]);
           bnew = bold[it] + d;
         }
         owned = j < TY || ey;
@@ -1812,9 +1826,8 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       {
         const int nn = n - C::NB2X - C::NB2Y;
         const int i = nn % TX, j = (nn / TX) % TY, k = nn / (TX * TY);
-        double    d = 0;
-        d += (My[C::mi(i + 1, j, k)] - My[C::mi(i, j, k)]);
-        d -= (Mx[C::mi(i, j + 1, k)] - Mx[C::mi(i, j, k)]);
+        const double d =
+          curl2<C::EXACT>(My[C::mi(i + 1, j, k)] - My[C::mi(i, j, k)], Mx[C::mi(i, j + 1, k)] - Mx[C::mi(i, j, k)]);
         bnew = bold[it] + d;
         owned = k < TZ || ez;
       }

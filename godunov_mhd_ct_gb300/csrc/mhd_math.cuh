@@ -723,14 +723,22 @@ d2f_bits(double x)
   const unsigned hi = (unsigned)__double2hiint(x);
   const unsigned lo = (unsigned)__double2loint(x);
   const unsigned sign = hi & 0x80000000u;
-  const unsigned e = (hi >> 20) & 0x7ffu;
-  const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
-  const int      ef = (int)e - 896; // rebias 1023 -> 127
-  unsigned       bits = sign | (((unsigned)ef << 23) + m + ((lo >> 28) & 1u));
-  bits = ef <= 0 ? sign : bits;
-  const bool nan = e == 0x7ffu && ((hi & 0xfffffu) | lo) != 0u;
-  bits = ef >= 255 ? (sign | 0x7f800000u | (nan ? 0x400000u : 0u)) : bits;
-  return __uint_as_float(bits);
+  const unsigned mag = hi & 0x7fffffffu;
+  // the low 8 exponent bits and the top 23 mantissa bits in place (one funnel shift); for exponents
+  // 897..1150 (the float normal range) e - 896 == (e & 0xff) ^ 0x80, so the rebias 1023 -> 127 is a
+  // flip of the field's top bit; then the first dropped bit rounds, a carry out of the mantissa
+  // moving into the exponent as it should
+  const unsigned bits = ((__funnelshift_l(lo, hi, 3) & 0x7fffffffu) ^ 0x40000000u) + ((lo >> 28) & 1u);
+  // |x| below the float normal range (exponent <= 896) -> signed zero; at or above 2^128
+  // (exponent >= 1151), infinity or NaN -> infinity / quiet NaN
+  if (mag < 0x38100000u)
+    return __uint_as_float(sign);
+  if (mag >= 0x47f00000u)
+  {
+    const bool nan = mag > 0x7ff00000u || (mag == 0x7ff00000u && lo != 0u);
+    return __uint_as_float(sign | 0x7f800000u | (nan ? 0x400000u : 0u));
+  }
+  return __uint_as_float(sign | bits);
 }
 
 // float -> double, exact for normal numbers, zero, infinity and NaN (subnormals flush to zero).
