@@ -59,3 +59,38 @@ def test_batch_rejects_cross_problem_neighbours():
     bad[0] = 1  # block 0 now claims problem 1 while its neighbours belong to problem 0
     with pytest.raises(NativeError):
         GodunovImplemGB300(settings(), mesh, problem=bad, n_problems=3)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_3d_batch_with_staggered_end_times(oracle_lib, precision):
+    """3D problems of 8^3 tiles (the mixed path's persistent kernel) ending at different times: a
+    finished problem's tiles are carried over unchanged while the others keep stepping."""
+    st = settings(gamma0=1.4, cfl=0.4, slope_type=2.0)
+    meshes = [BlockMesh.uniform(3, level=1, block=(16, 16, 16)), BlockMesh.uniform(3, level=1, block=(16, 16, 16)),
+              BlockMesh.uniform(3, level=2, block=(16, 16, 16))]
+    states = [wl.random_smooth(m, seed=40 + p) for p, m in enumerate(meshes)]
+    mesh, problem = BlockMesh.batch(meshes)
+    U = np.concatenate([s[0] for s in states])
+    B = np.concatenate([s[1] for s in states])
+    t_end = np.array([5e-3, 1.5e-2, 1e-2])  # about 2, 6 and 8 steps
+    nsteps = 12
+    impl = GodunovImplemGB300(st, mesh, precision=precision, problem=problem, n_problems=len(meshes))
+    dU, dB = torch.from_numpy(U).cuda(), torch.from_numpy(B).cuda()
+    dtlog, t = impl.advance(dU, torch.empty_like(dU), dB, torch.empty_like(dB), nsteps, t=0.0, t_end=t_end)
+    Ug, Bg = dU.cpu().numpy(), dB.cpu().numpy()
+    assert np.allclose(t, t_end, rtol=0, atol=1e-15)
+    off = 0
+    for p, (m, (Up, Bp)) in enumerate(zip(meshes, states)):
+        Uo, Bo, dto, to = oracle_lib.run_to(oracle_mesh(oracle_lib, m), oracle_settings(oracle_lib, st), Up, Bp,
+                                            nsteps, 0.0, t_end[p])
+        sl = slice(off, off + m.n_owned)
+        off += m.n_owned
+        n_active = int(np.count_nonzero(dto))
+        assert n_active < nsteps  # finished inside the step budget, later steps carried the state over
+        if precision == "fp64":
+            assert max_rel_diff(Ug[sl], Uo) <= TOL_FP64
+            assert max_rel_diff(Bg[sl], Bo) <= TOL_FP64
+        else:
+            l1 = float(np.abs(Ug[sl, 0] - Uo[:, 0]).sum() / np.abs(Uo[:, 0]).sum())
+            assert l1 <= 1e-6
+            assert np.count_nonzero(dtlog[:, p]) == n_active
