@@ -1046,7 +1046,10 @@ __global__ void __launch_bounds__(C::NT, 1) fused_step_kernel(const StepArgs a)
       a.B2[(int64_t)blk * a.nface + f] = a.B[(int64_t)blk * a.nface + f];
     if constexpr (C::PIPE)
     {
-      __syncthreads(); // staged data of this tile unused; the area takes the next tile's
+      // staged data of this tile unused; the area takes the next tile's gather
+      if (has_next)
+        load_nbr(work + gridDim.x, buf ^ 1);
+      __syncthreads();
       if (has_next)
         stage_tile(work + gridDim.x, buf ^ 1);
       continue;
