@@ -84,6 +84,9 @@ struct gmhd_ctx
   double *  d_Bccv = nullptr;
   double *  d_flux_side = nullptr;
   double *  d_emf_side = nullptr;
+  // gmhd_refine_flags scratch
+  double * d_rf_q = nullptr;
+  int8_t * d_rf_flags = nullptr;
 };
 
 namespace
@@ -193,6 +196,8 @@ release_all(gmhd_ctx * c)
     for (double ** p : {&c->a_U[k], &c->a_U2[k], &c->a_B[k], &c->a_B2[k]})
       drelease(c, p);
   release_amr(c);
+  drelease(c, &c->d_rf_q);
+  drelease(c, &c->d_rf_flags);
   c->dtlog_cap = 0;
 }
 
@@ -1228,27 +1233,21 @@ gmhd_refine_flags(gmhd_ctx * ctx, const double * U, const double * B, const gmhd
     return GMHD_ERR_ARGUMENT;
   const int     nvar = (params->use_rho ? 1 : 0) + (params->use_pressure ? 1 : 0);
   const size_t  nq = (size_t)nvar * ctx->n_owned * ctx->ncell;
-  double *      q = nullptr;
-  int8_t *      dflags = nullptr;
   cudaStream_t  s = (cudaStream_t)stream;
-  GMHD_CUDA(cudaMalloc((void **)&q, nq * sizeof(double)));
-  cudaError_t e = cudaMalloc((void **)&dflags, (size_t)ctx->n_owned > 0 ? (size_t)ctx->n_owned : 1);
-  if (e != cudaSuccess)
-  {
-    cudaFree(q);
-    return cuda_fail(ctx, e);
-  }
-  int rc = gmhd::launch_refine_flags(U, B, ctx->d_level, ctx->n_owned, ctx->dim, ctx->bx, ctx->by, ctx->bz, ctx->ncell,
-                                     ctx->nfx, ctx->nfy, ctx->nface, ctx->p.gamma0, ctx->p.smallr, ctx->smallp,
-                                     params->criterion, params->level_min, params->level_max, params->use_rho,
-                                     params->use_pressure, params->eps_refine, params->eps_coarsen, params->eps_lohner,
-                                     q, dflags, s);
+  // scratch kept in the context (an AMR cycle every few steps allocates nothing)
+  int rc;
+  if ((rc = dalloc(ctx, &ctx->d_rf_q, nq > 0 ? nq : 1)) ||
+      (rc = dalloc(ctx, &ctx->d_rf_flags, (size_t)(ctx->n_owned > 0 ? ctx->n_owned : 1))))
+    return rc;
+  rc = gmhd::launch_refine_flags(U, B, ctx->d_level, ctx->n_owned, ctx->dim, ctx->bx, ctx->by, ctx->bz, ctx->ncell,
+                                 ctx->nfx, ctx->nfy, ctx->nface, ctx->p.gamma0, ctx->p.smallr, ctx->smallp,
+                                 params->criterion, params->level_min, params->level_max, params->use_rho,
+                                 params->use_pressure, params->eps_refine, params->eps_coarsen, params->eps_lohner,
+                                 ctx->d_rf_q, ctx->d_rf_flags, s);
   if (rc == 0 && ctx->n_owned > 0)
-    rc = (int)cudaMemcpyAsync(flags, dflags, (size_t)ctx->n_owned, cudaMemcpyDeviceToHost, s);
+    rc = (int)cudaMemcpyAsync(flags, ctx->d_rf_flags, (size_t)ctx->n_owned, cudaMemcpyDeviceToHost, s);
   if (rc == 0)
     rc = (int)cudaStreamSynchronize(s);
-  cudaFree(q);
-  cudaFree(dflags);
   return rc ? cuda_fail(ctx, (cudaError_t)rc) : GMHD_OK;
 }
 

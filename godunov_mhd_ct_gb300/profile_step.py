@@ -17,7 +17,9 @@ def main():
     ap.add_argument("--side-blocks", type=int, default=4)
     ap.add_argument("--block", type=int, default=32)
     ap.add_argument("--dim", type=int, default=3, choices=[2, 3])
-    ap.add_argument("--workload", default="ot", choices=["ot", "blast", "kh"],
+    ap.add_argument("--problems", type=int, default=1024, help="fieldloops: number of independent problems")
+    ap.add_argument("--t-end", type=float, default=0.5, help="fieldloops: end time of every problem")
+    ap.add_argument("--workload", default="ot", choices=["ot", "blast", "kh", "fieldloops"],
                     help="ot: uniform Orszag-Tang; blast: 2D AMR blast; kh: 3D AMR shear layers with walls")
     ap.add_argument("--levels", default="5:8", help="base:max level of the AMR workloads")
     ap.add_argument("--warmup", type=int, default=3)
@@ -36,6 +38,35 @@ def main():
 
     st = MHDSettings(gamma0=5.0 / 3.0, cfl=0.5, slope_type=2.0, riemann="HLLD")
     bc = None
+    if args.workload == "fieldloops":
+        # independent 2D field loops of log-uniform sizes (2N x N cells, N = 32..512) batched in one
+        # launch per step, each with its own dt, run until every problem reaches t_end
+        t0 = time.perf_counter()
+        meshes, states, _ = wl.field_loop_batch(args.problems, seed=12345, sizes=(32, 64, 128, 256, 512))
+        mesh, problem = BlockMesh.batch(meshes)
+        U = np.concatenate([s_[0] for s_ in states])
+        B = np.concatenate([s_[1] for s_ in states])
+        del states
+        cells = np.array([m.n_owned * m.ncell for m in meshes], dtype=np.float64)
+        print(f"fieldloops: {len(meshes)} problems, {cells.sum() / 1e6:.1f} M cells, {mesh.n_owned} blocks "
+              f"(setup {time.perf_counter() - t0:.1f} s)")
+        impl = GodunovImplemGB300(st, mesh, precision=args.precision, problem=problem, n_problems=len(meshes))
+        dU, dB = torch.from_numpy(U).cuda(), torch.from_numpy(B).cuda()
+        dU2, dB2 = torch.empty_like(dU), torch.empty_like(dB)
+        t = np.zeros(len(meshes))
+        updates, steps = 0.0, 0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        while (t < args.t_end).any():
+            dtlog, t = impl.advance(dU, dU2, dB, dB2, 100, t=t, t_end=args.t_end)
+            updates += float(((dtlog > 0) * cells[None, :]).sum())
+            steps += 100
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        print(f"{args.precision} field loops to t={args.t_end}: {steps} launches of the batch, "
+              f"{updates / 1e9:.2f} G cell-updates in {el:.2f} s: {updates / el / 1e9:.3f} G cell-updates/s, "
+              f"health flags {impl.last_status()}")
+        return
     if args.workload == "ot":
         level = int(np.log2(args.side_blocks))
         blk = (args.block, args.block, args.block if args.dim == 3 else 1)
