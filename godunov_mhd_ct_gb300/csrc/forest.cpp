@@ -50,9 +50,9 @@ public:
   {
     for (size_t i = home(k);; i = (i + 1) & mask_)
     {
-      if (keys_[i] == k)
-        return &vals_[i];
-      if (keys_[i] == EMPTY)
+      if (slots_[i].key == k)
+        return &slots_[i].val;
+      if (slots_[i].key == EMPTY)
         return nullptr;
     }
   }
@@ -65,17 +65,16 @@ public:
   bool
   put(uint64_t k, int32_t v = 0)
   {
-    if (2 * (n_ + 1) > keys_.size())
-      rehash(2 * keys_.size());
+    if (2 * (n_ + 1) > slots_.size())
+      rehash(2 * slots_.size());
     size_t i = home(k);
-    for (; keys_[i] != EMPTY; i = (i + 1) & mask_)
-      if (keys_[i] == k)
+    for (; slots_[i].key != EMPTY; i = (i + 1) & mask_)
+      if (slots_[i].key == k)
       {
-        vals_[i] = v;
+        slots_[i].val = v;
         return false;
       }
-    keys_[i] = k;
-    vals_[i] = v;
+    slots_[i] = Slot{k, v};
     ++n_;
     return true;
   }
@@ -83,21 +82,20 @@ public:
   erase(uint64_t k)
   {
     size_t i = home(k);
-    for (; keys_[i] != k; i = (i + 1) & mask_)
-      if (keys_[i] == EMPTY)
+    for (; slots_[i].key != k; i = (i + 1) & mask_)
+      if (slots_[i].key == EMPTY)
         return false;
     // shift the rest of the probe run back so that no lookup stops early at the hole
-    for (size_t j = (i + 1) & mask_; keys_[j] != EMPTY; j = (j + 1) & mask_)
+    for (size_t j = (i + 1) & mask_; slots_[j].key != EMPTY; j = (j + 1) & mask_)
     {
-      const size_t h = home(keys_[j]);
+      const size_t h = home(slots_[j].key);
       const bool   stays = (i <= j) ? (i < h && h <= j) : (i < h || h <= j);
       if (stays)
         continue;
-      keys_[i] = keys_[j];
-      vals_[i] = vals_[j];
+      slots_[i] = slots_[j];
       i = j;
     }
-    keys_[i] = EMPTY;
+    slots_[i].key = EMPTY;
     --n_;
     return true;
   }
@@ -105,9 +103,9 @@ public:
   void
   for_each(F && f) const
   {
-    for (size_t i = 0; i < keys_.size(); ++i)
-      if (keys_[i] != EMPTY)
-        f(keys_[i], vals_[i]);
+    for (const Slot & sl : slots_)
+      if (sl.key != EMPTY)
+        f(sl.key, sl.val);
   }
   std::vector<uint64_t>
   keys() const
@@ -120,10 +118,14 @@ public:
 
 private:
   static constexpr uint64_t EMPTY = ~0ull;
-  std::vector<uint64_t>     keys_;
-  std::vector<int32_t>      vals_;
-  size_t                    mask_ = 0, n_ = 0;
-  int                       shift_ = 60;
+  struct Slot
+  {
+    uint64_t key; // key and value side by side: one cache line per probe
+    int32_t  val;
+  };
+  std::vector<Slot> slots_;
+  size_t            mask_ = 0, n_ = 0;
+  int               shift_ = 60;
 
   static size_t
   capacity_for(size_t n)
@@ -141,20 +143,17 @@ private:
   void
   rehash(size_t cap)
   {
-    std::vector<uint64_t> ok;
-    std::vector<int32_t>  ov;
-    ok.swap(keys_);
-    ov.swap(vals_);
-    keys_.assign(cap, EMPTY);
-    vals_.assign(cap, 0);
+    std::vector<Slot> old;
+    old.swap(slots_);
+    slots_.assign(cap, Slot{EMPTY, 0});
     mask_ = cap - 1;
     shift_ = 64;
     for (size_t c = cap; c > 1; c >>= 1)
       --shift_;
     n_ = 0;
-    for (size_t i = 0; i < ok.size(); ++i)
-      if (ok[i] != EMPTY)
-        put(ok[i], ov[i]);
+    for (const Slot & sl : old)
+      if (sl.key != EMPTY)
+        put(sl.key, sl.val);
   }
 };
 
@@ -213,18 +212,41 @@ struct Forest
   {
     return 1 << dim;
   }
+  // leaves of `leaves` two levels below coarsened parent p and next to it: the only old leaves that can
+  // now be out of balance (before the coarsening they touched p's children)
+  void
+  fine_neighbours_of(const KeyTable & leaves, uint64_t p, std::vector<uint64_t> & out) const
+  {
+    const Key k = unpack(p);
+    const int n2 = dim == 3 ? 4 : 1; // grandchildren per axis: 4 in x and y, 4 or 1 in z
+    for (int o = 0; o < noffs; ++o)
+    {
+      int r[3] = {k.x + offs[o][0], k.y + offs[o][1], k.z + offs[o][2]};
+      if (!wrap(k.L, r))
+        continue;
+      for (int gz = 0; gz < n2; ++gz)
+        for (int gy = 0; gy < 4; ++gy)
+          for (int gx = 0; gx < 4; ++gx)
+          {
+            const uint64_t g = pack(k.L + 2, 4 * r[0] + gx, 4 * r[1] + gy, dim == 3 ? 4 * r[2] + gz : 0);
+            if (leaves.contains(g))
+              out.push_back(g);
+          }
+    }
+  }
   uint64_t
   kid(const Key & k, int c) const
   {
     return pack(k.L + 1, 2 * k.x + (c & 1), 2 * k.y + ((c >> 1) & 1), 2 * k.z + ((c >> 2) & 1));
   }
 
-  // refine leaves until every leaf's face/edge/corner neighbours are within one level
+  // refine leaves until every leaf's face/edge/corner neighbours are within one level. The work list
+  // starts from `seeds` when given (the leaves that can break the balance of an already balanced
+  // set), else from every leaf; the result (the coarsest balanced refinement) does not depend on it.
   void
-  balance(KeyTable & leaves) const
+  balance(KeyTable & leaves, const std::vector<uint64_t> * seeds = nullptr) const
   {
-    std::vector<uint64_t> work = leaves.keys();
-    std::sort(work.begin(), work.end());
+    std::vector<uint64_t> work = seeds ? *seeds : leaves.keys();
     while (!work.empty())
     {
       const uint64_t kk = work.back();
@@ -279,6 +301,19 @@ struct gmhd_forest
 namespace
 {
 // mesh tables of a balanced leaf set
+// every third bit of v (v < 2^21): the usual "part 1 by 2" interleave by shifts and masks
+inline uint64_t
+spread3(uint64_t v)
+{
+  v &= 0x1fffffull;
+  v = (v | v << 32) & 0x1f00000000ffffull;
+  v = (v | v << 16) & 0x1f0000ff0000ffull;
+  v = (v | v << 8) & 0x100f00f00f00f00full;
+  v = (v | v << 4) & 0x10c30c30c30c30c3ull;
+  v = (v | v << 2) & 0x1249249249249249ull;
+  return v;
+}
+
 void
 build(const Forest & f, const KeyTable & leaves, gmhd_forest & out)
 {
@@ -286,10 +321,11 @@ build(const Forest & f, const KeyTable & leaves, gmhd_forest & out)
   int                         max_level = 0;
   for (uint64_t k : keys)
     max_level = std::max(max_level, unpack(k).L);
+  // p4est order: tree (bricks x fastest), then the Morton code of the leaf's anchor at max_level
+  // (leaves of a leaf set never share an anchor)
   struct Ord
   {
     uint64_t tree, morton;
-    int      L;
     uint64_t key;
   };
   std::vector<Ord> ord;
@@ -300,20 +336,23 @@ build(const Forest & f, const KeyTable & leaves, gmhd_forest & out)
     const int t[3] = {k.x >> k.L, k.y >> k.L, k.z >> k.L};
     const uint64_t tid = (uint64_t)t[0] + (uint64_t)f.bricks[0] * ((uint64_t)t[1] + (uint64_t)f.bricks[1] * t[2]);
     const int      sh = max_level - k.L;
-    const uint64_t a[3] = {(uint64_t)(k.x - (t[0] << k.L)) << sh, (uint64_t)(k.y - (t[1] << k.L)) << sh,
-                           (uint64_t)(k.z - (t[2] << k.L)) << sh};
-    uint64_t m = 0;
-    for (int bit = 0; bit < std::max(max_level, 1); ++bit)
-      m |= ((a[0] >> bit) & 1) << (3 * bit) | ((a[1] >> bit) & 1) << (3 * bit + 1) | ((a[2] >> bit) & 1) << (3 * bit + 2);
-    ord.push_back(Ord{tid, m, k.L, kk});
+    const uint64_t m = spread3((uint64_t)(k.x - (t[0] << k.L)) << sh) |
+                       spread3((uint64_t)(k.y - (t[1] << k.L)) << sh) << 1 |
+                       spread3((uint64_t)(k.z - (t[2] << k.L)) << sh) << 2;
+    ord.push_back(Ord{tid, m, kk});
   }
-  std::sort(ord.begin(), ord.end(), [](const Ord & p, const Ord & q) {
-    if (p.tree != q.tree)
-      return p.tree < q.tree;
-    if (p.morton != q.morton)
-      return p.morton < q.morton;
-    return p.L < q.L;
-  });
+  const uint64_t ntrees = (uint64_t)f.bricks[0] * f.bricks[1] * f.bricks[2];
+  if (3 * max_level + 64 - __builtin_clzll(ntrees | 1) <= 64)
+  {
+    // one 64-bit sort key: tree id above the Morton bits
+    for (Ord & o : ord)
+      o.morton |= o.tree << (3 * max_level);
+    std::sort(ord.begin(), ord.end(), [](const Ord & p, const Ord & q) { return p.morton < q.morton; });
+  }
+  else
+    std::sort(ord.begin(), ord.end(), [](const Ord & p, const Ord & q) {
+      return p.tree != q.tree ? p.tree < q.tree : p.morton < q.morton;
+    });
   KeyTable ids(ord.size());
   out.owned.clear();
   out.owned.reserve(ord.size());
@@ -513,7 +552,15 @@ gmhd_forest_build(int32_t dim, const int32_t * bricks, const int32_t * periodic,
           cand.erase(f.kid(unpack(p), c));
         cand.put(p);
       }
-      f.balance(cand);
+      // the input set is balanced (it comes from an earlier build): only new children and the leaves
+      // next to new parents can break the balance
+      std::vector<uint64_t> seeds;
+      for (uint64_t kk : refined)
+        for (int c = 0; c < f.nkids(); ++c)
+          seeds.push_back(f.kid(unpack(kk), c));
+      for (uint64_t p : coarsen)
+        f.fine_neighbours_of(cand, p, seeds);
+      f.balance(cand, &seeds);
       const size_t before = coarsen.size();
       coarsen.erase(std::remove_if(coarsen.begin(), coarsen.end(), [&](uint64_t p) { return !cand.contains(p); }),
                     coarsen.end());
