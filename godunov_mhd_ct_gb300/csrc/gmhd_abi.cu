@@ -952,6 +952,9 @@ gmhd_set_mesh(gmhd_ctx * ctx, const gmhd_mesh * m)
   }
   if (amr && (rc = setup_amr(ctx, m, kind)))
     return rc;
+  // the memsets above ran on the legacy stream: finish them before any step on another stream reads
+  // the tables
+  GMHD_CUDA(cudaStreamSynchronize(0));
   ctx->has_mesh = true;
   ctx->mesh_version++;
   return GMHD_OK;
