@@ -6,12 +6,12 @@
 
 namespace gmhd
 {
-using F64_3D_844 = Cfg<double, 3, 8, 4, 4, 128, true>;
+using F64_3D_844 = Cfg<double, 3, 8, 4, 4, 256, true>;
 using F64_3D_444 = Cfg<double, 3, 4, 4, 4, 64, true>;
 using F64_2D_16 = Cfg<double, 2, 16, 16, 1, 256, true>;
 using F64_2D_8 = Cfg<double, 2, 8, 8, 1, 64, true>;
 using F64_2D_4 = Cfg<double, 2, 4, 4, 1, 32, true>;
-using F64_3D_844_AMR = Cfg<double, 3, 8, 4, 4, 128, true, true>;
+using F64_3D_844_AMR = Cfg<double, 3, 8, 4, 4, 256, true, true>;
 using F64_3D_444_AMR = Cfg<double, 3, 4, 4, 4, 64, true, true>;
 using F64_2D_16_AMR = Cfg<double, 2, 16, 16, 1, 256, true, true>;
 using F64_2D_8_AMR = Cfg<double, 2, 8, 8, 1, 64, true, true>;
