@@ -1020,16 +1020,29 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
   }
   else
   {
-    if (tid < 27)
+    if (tid < 32)
     {
-      s_nbr[tid] = a.neighbor[(int64_t)blk * 27 + tid];
-      if constexpr (C::AMR)
-        s_kind[tid] = (int)a.kind[(int64_t)blk * 27 + tid];
+      // neighbour table, region kinds, and the slots whose (real) block is at another level
+      int  nb = -1;
+      bool jump = false;
+      if (tid < 27)
+      {
+        nb = a.neighbor[(int64_t)blk * 27 + tid];
+        s_nbr[tid] = nb;
+        if constexpr (C::AMR)
+          s_kind[tid] = (int)a.kind[(int64_t)blk * 27 + tid];
+        jump = nb >= 0 && nb < a.n_blocks && a.level[nb] != a.level[blk];
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, jump);
+      if (tid == 0)
+      {
+        s_stage_jump[0] = m;
+        s_health = 0u;
+      }
     }
-    if (tid == 0)
-      s_health = 0u;
   }
   __syncthreads();
+  const unsigned jump_mask = s_stage_jump[C::PIPE ? buf : 0];
 
   const int myprob = a.problem ? a.problem[blk] : 0;
   const int mylevel = a.level[blk];
@@ -1100,10 +1113,11 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
   auto owner = [&](int ox, int oy, int oz) -> int {
     if ((ox | oy | oz) == 0)
       return blk;
-    const int nb = s_nbr[nb_slot(ox, oy, oz)];
+    const int sl = nb_slot(ox, oy, oz);
+    const int nb = s_nbr[sl];
     if (nb < 0)
       health |= HEALTH_MISSING_NEIGHBOR;
-    else if (nb < a.n_blocks && a.level[nb] != mylevel)
+    else if ((jump_mask >> sl) & 1u)
       health |= HEALTH_LEVEL_JUMP;
     return nb;
   };
