@@ -154,6 +154,25 @@ def inv_dt(mesh: Mesh, st: OracleSettings, U, B) -> float:
     return lib().oracle_inv_dt(ctypes.byref(mesh.c), ctypes.byref(st), _dp(U), _dp(B))
 
 
+def block_stages(mesh: Mesh, st: OracleSettings, U, B, dt, blk):
+    """Stage arrays of one block (oracle_block_stages): ghosted primitives q, slopes, predictor q2,
+    edge field e and face source sf, flat, variable-major, x fastest."""
+    c = mesh.c
+    dim = c.dim
+    b = (c.bx, c.by, c.bz if dim == 3 else 1)
+    n2 = int(np.prod([v + 4 for v in b[:dim]]))
+    n1 = int(np.prod([v + 2 for v in b[:dim]]))
+    out = {"q": np.zeros(11 * n2), "slopes": np.zeros(dim * 8 * n1), "q2": np.zeros(8 * n1),
+           "e": np.zeros((3 if dim == 3 else 1) * n2), "sf": np.zeros((3 if dim == 3 else 2) * n1)}
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    rc = lib().oracle_block_stages(ctypes.byref(c), ctypes.byref(st), _dp(U), _dp(B), ctypes.c_double(dt), int(blk),
+                                   *(_dp(out[k]) for k in ("q", "slopes", "q2", "e", "sf")))
+    if rc != 0:
+        raise RuntimeError(f"oracle_block_stages failed: {rc}")
+    return out
+
+
 def run(mesh: Mesh, st: OracleSettings, U, B, nsteps):
     """nsteps of CFL + step, in place on copies; returns (U, B, dts)."""
     U = np.array(U, dtype=np.float64, copy=True, order="C")

@@ -1791,6 +1791,54 @@ oracle_step(const oracle_mesh * om, const oracle_settings * os, const double * U
   return status;
 }
 
+// The per-block stage arrays of oracle_step for block blk (for checks against the reference's own
+// stage functors): ghosted primitives q [11][(b+4)^d], slopes [dim][8][(b+2)^d], predictor
+// q2 [8][(b+2)^d], edge electric field e [1|3][(b+4)^d], face source sf [2|3][(b+2)^d]; each array
+// variable-major, x fastest (2D: one z layer). Returns 0 or the stage error.
+int
+oracle_block_stages(const oracle_mesh * om, const oracle_settings * os, const double * U, const double * B, double dt,
+                    int blk, double * q, double * slopes, double * q2, double * e, double * sf)
+{
+  const Mesh     m = to_mesh(om);
+  const Settings s = to_settings(os);
+  if (blk < 0 || blk >= m.n_owned)
+    return -1;
+  Fields f;
+  f.m = &m;
+  f.L = block_layout(m);
+  f.U = U;
+  f.B = B;
+  StepWork     w;
+  const double dx = cell_length(m, m.level[blk]);
+  const double dtdx = dt / dx;
+  int          st = fill_bface_ghosted(m, f, blk, w);
+  if (st == 0)
+    st = convert_to_primitives(m, f, s, blk, w);
+  if (st != 0)
+    return st;
+  compute_slopes(m, s, w);
+  compute_predictor(m, s, dt, dtdx, dx, w);
+  compute_elec_field(m, w);
+  compute_sfacemag(m, dtdx, w);
+  auto put = [](double * dst, const Box & bx) {
+    if (dst)
+      std::memcpy(dst, bx.a.data(), sizeof(double) * bx.a.size());
+  };
+  put(q, w.Q);
+  if (slopes)
+  {
+    const size_t ns = w.Sx.a.size();
+    std::memcpy(slopes, w.Sx.a.data(), sizeof(double) * ns);
+    std::memcpy(slopes + ns, w.Sy.a.data(), sizeof(double) * ns);
+    if (m.dim == 3)
+      std::memcpy(slopes + 2 * ns, w.Sz.a.data(), sizeof(double) * ns);
+  }
+  put(q2, w.Q2);
+  put(e, w.E);
+  put(sf, w.SF);
+  return 0;
+}
+
 // oracle_step that also copies the per-block face fluxes (flux * dt/dx, [block][dir][var][face]) to
 // fluxes_out, for checks of the coarse/fine flux correction.
 int

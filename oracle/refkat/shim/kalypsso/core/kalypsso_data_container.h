@@ -1,0 +1,73 @@
+// Stub of kalypsso-core's block data containers for the functor bridge (test infrastructure):
+// host arrays of n octants x nvar variables x (b + 2 g)^d cells, variable-major per octant, x fastest
+// (the octant-contiguous SoA the reference slices, scheme/GodunovImplemV0.cpp:304-319). Element
+// (i, j[, k], var, oct) counts i, j, k from the first interior cell, -g .. b + g - 1. Copies share
+// storage, as Kokkos views do.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <memory>
+#include <vector>
+
+#include <kalypsso/core/kokkos_shared.h>
+
+namespace kalypsso
+{
+template <std::size_t dim>
+using block_size_t = Kokkos::Array<int32_t, dim>;
+
+template <std::size_t dim, typename T, typename device_t>
+class DataArrayGhostedBlock
+{
+public:
+  DataArrayGhostedBlock() = default;
+  DataArrayGhostedBlock(block_size_t<dim> bs, int ghost, int nvar, int noct)
+    : m_bs(bs), m_g(ghost), m_nvar(nvar), m_noct(noct)
+  {
+    m_ncell = 1;
+    for (std::size_t d = 0; d < dim; ++d)
+      m_ncell *= bs[d] + 2 * ghost;
+    m_data = std::make_shared<std::vector<T>>((std::size_t)m_ncell * nvar * noct, T(0));
+  }
+  template <std::size_t D = dim, std::enable_if_t<D == 2, int> = 0>
+  T &
+  operator()(int i, int j, int var, int oct) const
+  {
+    const int nx = m_bs[0] + 2 * m_g;
+    return (*m_data)[(std::size_t)(i + m_g) + nx * (j + m_g) + (std::size_t)m_ncell * (var + (std::size_t)m_nvar * oct)];
+  }
+  template <std::size_t D = dim, std::enable_if_t<D == 3, int> = 0>
+  T &
+  operator()(int i, int j, int k, int var, int oct) const
+  {
+    const int nx = m_bs[0] + 2 * m_g, ny = m_bs[1] + 2 * m_g;
+    return (*m_data)[(std::size_t)(i + m_g) + nx * ((j + m_g) + (std::size_t)ny * (k + m_g)) +
+                     (std::size_t)m_ncell * (var + (std::size_t)m_nvar * oct)];
+  }
+  int32_t num_cells() const { return m_ncell; }
+  int32_t num_quadrants() const { return m_noct; }
+  int32_t shift() const { return m_g; }
+  block_size_t<dim> block_size() const { return m_bs; }
+  block_size_t<dim>
+  ghosted_block_size() const
+  {
+    block_size_t<dim> g;
+    for (std::size_t d = 0; d < dim; ++d)
+      g[d] = m_bs[d] + 2 * m_g;
+    return g;
+  }
+  T * data() const { return m_data->data(); }
+
+private:
+  block_size_t<dim>               m_bs{};
+  int                             m_g = 0, m_nvar = 0, m_noct = 0, m_ncell = 0;
+  std::shared_ptr<std::vector<T>> m_data;
+};
+
+template <std::size_t dim, typename T, typename device_t>
+using DataArrayBlock = DataArrayGhostedBlock<dim, T, device_t>;
+// face-centred arrays appear in the functors' type aliases only (the bridge does not call the
+// stages that read them)
+template <std::size_t dim, typename T, typename device_t>
+using FaceDataArrayBlock = DataArrayGhostedBlock<dim, T, device_t>;
+} // namespace kalypsso

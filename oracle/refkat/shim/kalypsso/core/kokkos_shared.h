@@ -4,6 +4,7 @@
 #include <cstddef>
 #include <cstdio>
 #include <cstdlib>
+#include <type_traits>
 #include <kalypsso/core/real_type.h>
 
 #define KOKKOS_INLINE_FUNCTION inline
@@ -25,10 +26,33 @@ abort(const char * msg)
   std::fprintf(stderr, "Kokkos::abort: %s\n", msg);
   std::abort();
 }
+// serial stand-ins for the range policy and parallel_for the scheme functors use
+template <class Exec, class Tag = void>
+struct RangePolicy
+{
+  long long b, e;
+  RangePolicy(long long b_, long long e_) : b(b_), e(e_) {}
+};
+template <class F, class Exec, class Tag>
+void
+parallel_for(const char *, RangePolicy<Exec, Tag> p, const F & f)
+{
+  for (long long i = p.b; i < p.e; ++i)
+  {
+    if constexpr (std::is_void_v<Tag>)
+      f(i);
+    else
+      f(Tag{}, i);
+  }
+}
 } // namespace Kokkos
 
 namespace kalypsso
 {
+struct DefaultDevice
+{
+  using execution_space = int;
+};
 enum ComponentIndex3D : int
 {
   IX = 0,

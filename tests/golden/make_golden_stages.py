@@ -1,0 +1,113 @@
+"""Record golden stage arrays from the reference's own stage functors.
+
+Runs the functor bridge (oracle/refkat/functor_bridge.cpp: the reference's
+ComputeLimitedSlopesFunctor, ComputeUpdatedPrimitiveVariablesFunctor, ComputeElectricFieldFunctor
+and ComputeSourceFaceMagFunctor compiled unmodified against stub headers) on the ghosted primitive
+variables the oracle builds for one block, and writes ``functor_stages.npz`` next to this script:
+per case the mesh and state (U, B), dt, the block, the settings, and the reference's slopes,
+predictor, edge field and face source. Needs the reference tree (default /root/reference, or
+$GMHD_REFERENCE_TREE); the committed npz is what tests use.
+
+    python tests/golden/make_golden_stages.py
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from godunov_mhd_ct_gb300 import workloads as wl  # noqa: E402
+from godunov_mhd_ct_gb300.mesh import BlockMesh  # noqa: E402
+from oracle import oracle as orc  # noqa: E402
+
+BRIDGE = os.path.join(ROOT, "oracle", "_ref", "libref_functors.so")
+
+# name: dim, state, gamma, slope_type, rk2, gravity, viscosity mu (None: off), viscous predictor
+CASES = {
+    "2d_smooth_mc": (2, "smooth", 1.4, 2.0, 0, None, None, False),
+    "2d_ot_minmod": (2, "ot", 5.0 / 3.0, 1.0, 0, None, None, False),
+    "2d_blast_mc_grav_visc": (2, "blast", 5.0 / 3.0, 2.0, 0, (0.3, -0.7, 0.0), 2e-3, True),
+    "2d_smooth_rk2": (2, "smooth", 1.4, 2.0, 1, None, None, False),
+    "3d_smooth_mc": (3, "smooth", 1.4, 2.0, 0, None, None, False),
+    "3d_ot_minmod_grav": (3, "ot", 5.0 / 3.0, 1.0, 0, (0.2, 0.1, -0.4), None, False),
+    "3d_smooth_visc_pred": (3, "smooth", 1.4, 2.0, 0, None, 3e-3, True),
+    "3d_smooth_rk2": (3, "smooth", 1.4, 2.0, 1, None, None, False),
+}
+
+
+def case_mesh(dim):
+    if dim == 2:
+        return BlockMesh.uniform(2, level=1, block=(8, 8, 1))
+    return BlockMesh.uniform(3, level=1, block=(4, 4, 4))
+
+
+def case_state(mesh, kind, gamma):
+    if kind == "smooth":
+        return wl.random_smooth(mesh, gamma=gamma, seed=17)
+    if kind == "ot":
+        return wl.orszag_tang(mesh, gamma=gamma, rho_perturbation=1e-3, seed=5)
+    # front r = 0.3 around the domain centre (it crosses every block), three oracle steps on: the
+    # initial step profile has zero limited slopes
+    U, B = wl.blast(mesh, gamma=gamma, radius=0.3)
+    st = orc.settings(gamma0=gamma, cfl=0.4, slope_type=2.0, riemann=5)
+    U, B, _ = orc.run(orc.Mesh.from_block_mesh(mesh), st, U, B, 3)
+    return U, B
+
+
+def oracle_settings(gamma, slope, rk2, grav, mu, pred):
+    return orc.settings(gamma0=gamma, cfl=0.4, slope_type=slope, riemann=5, time_integrator=rk2, gravity=grav,
+                        viscosity_mu=mu, viscous_predictor=pred)
+
+
+def reference_stages(dim, block, level, gamma, slope, rk2, grav, mu, pred, dt, q):
+    """The reference functors on the oracle's ghosted primitives q of one block."""
+    L = ctypes.CDLL(BRIDGE)
+    dp = ctypes.POINTER(ctypes.c_double)
+    b = (ctypes.c_int * 3)(*block)
+    prm = (ctypes.c_double * 6)(gamma, slope, 1e-10, 1e-10, 1.0, 0.0 if mu is None else mu)
+    flags = (ctypes.c_int * 5)(5, rk2, int(grav is not None), int(mu is not None), int(bool(pred)))
+    g = (ctypes.c_double * 3)(*(tuple(grav) + (0.0,) * 3)[:3] if grav is not None else (0.0, 0.0, 0.0))
+    n1 = int(np.prod([v + 2 for v in block[:dim]]))
+    n2 = int(np.prod([v + 4 for v in block[:dim]]))
+    out = {"slopes": np.zeros(dim * 8 * n1), "q2": np.zeros(8 * n1), "e": np.zeros((3 if dim == 3 else 1) * n2),
+           "sf": np.zeros((3 if dim == 3 else 2) * n1)}
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    rc = L.ref_block_stages(dim, b, level, prm, flags, g, ctypes.c_double(dt), q.ctypes.data_as(dp),
+                            *(out[k].ctypes.data_as(dp) for k in ("slopes", "q2", "e", "sf")))
+    if rc != 0:
+        raise RuntimeError(f"ref_block_stages failed: {rc}")
+    return out
+
+
+def main():
+    if not orc.build_refkat() or not os.path.exists(BRIDGE):
+        sys.exit("the reference tree is needed to record the golden stages")
+    out = {}
+    for name, (dim, kind, gamma, slope, rk2, grav, mu, pred) in CASES.items():
+        mesh = case_mesh(dim)
+        U, B = case_state(mesh, kind, gamma)
+        om = orc.Mesh.from_block_mesh(mesh)
+        st = oracle_settings(gamma, slope, rk2, grav, mu, pred)
+        dt = 0.4 / orc.inv_dt(om, st, U, B)
+        blk = 1
+        q = orc.block_stages(om, st, U, B, dt, blk)["q"]
+        ref = reference_stages(dim, mesh.block, int(mesh.level[blk]), gamma, slope, rk2, grav, mu, pred, dt, q)
+        out[f"{name}_U"] = U
+        out[f"{name}_B"] = B
+        out[f"{name}_dt"] = np.float64(dt)
+        out[f"{name}_q"] = q
+        for k, v in ref.items():
+            out[f"{name}_{k}"] = v
+    path = os.path.join(HERE, "functor_stages.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {path} ({len(CASES)} cases)")
+
+
+if __name__ == "__main__":
+    main()

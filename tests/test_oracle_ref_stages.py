@@ -1,0 +1,71 @@
+"""Pin the oracle's per-block stages against the reference's own stage functors.
+
+The golden arrays (tests/golden/functor_stages.npz, recorded by tests/golden/make_golden_stages.py)
+are the output of the reference's ComputeLimitedSlopesFunctor, ComputeUpdatedPrimitiveVariablesFunctor
+(Hancock predictor with the gravity and viscous terms, and the RK2_SSP identity),
+ComputeElectricFieldFunctor and ComputeSourceFaceMagFunctor, compiled unmodified, on the ghosted
+primitive variables the oracle builds for one block. The oracle must reproduce the slopes, the
+predictor, the edge electric field and the half-step face source bit for bit. Where the reference tree
+is present the same comparison also runs live on further states.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from godunov_mhd_ct_gb300.mesh import BlockMesh  # noqa: F401
+
+orc = pytest.importorskip("oracle.oracle")
+HERE = os.path.dirname(__file__)
+GOLDEN = os.path.join(HERE, "golden", "functor_stages.npz")
+
+import importlib.util  # noqa: E402
+
+_spec = importlib.util.spec_from_file_location("make_golden_stages", os.path.join(HERE, "golden", "make_golden_stages.py"))
+gen = importlib.util.module_from_spec(_spec)
+_spec.loader.exec_module(gen)
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return np.load(GOLDEN)
+
+
+@pytest.mark.parametrize("name", sorted(gen.CASES))
+def test_oracle_stages_match_reference_functors(golden, name):
+    dim, kind, gamma, slope, rk2, grav, mu, pred = gen.CASES[name]
+    mesh = gen.case_mesh(dim)
+    om = orc.Mesh.from_block_mesh(mesh)
+    st = gen.oracle_settings(gamma, slope, rk2, grav, mu, pred)
+    out = orc.block_stages(om, st, golden[f"{name}_U"], golden[f"{name}_B"], float(golden[f"{name}_dt"]), 1)
+    assert np.array_equal(out["q"], golden[f"{name}_q"])
+    for k in ("slopes", "q2", "e", "sf"):
+        assert np.array_equal(out[k], golden[f"{name}_{k}"]), k
+
+
+@pytest.mark.skipif(not os.path.isdir(os.environ.get("GMHD_REFERENCE_TREE", "/root/reference")),
+                    reason="needs the reference tree")
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_oracle_stages_match_reference_functors_live(dim, seed):
+    from godunov_mhd_ct_gb300 import workloads as wl
+
+    if not orc.build_refkat() or not os.path.exists(gen.BRIDGE):
+        pytest.skip("functor bridge not built")
+    rng = np.random.default_rng(seed)
+    mesh = gen.case_mesh(dim)
+    gamma = [1.4, 5.0 / 3.0][seed % 2]
+    slope = [1.0, 2.0][seed % 2]
+    grav = tuple(rng.uniform(-1, 1, 3)) if seed == 2 else None
+    mu, pred = (1e-3 * seed, seed != 1) if seed >= 2 else (None, False)
+    rk2 = int(seed == 3)
+    U, B = wl.random_smooth(mesh, gamma=gamma, seed=100 + seed, amp=0.4)
+    om = orc.Mesh.from_block_mesh(mesh)
+    st = gen.oracle_settings(gamma, slope, rk2, grav, mu, pred)
+    dt = 0.4 / orc.inv_dt(om, st, U, B)
+    for blk in range(mesh.n_owned):
+        out = orc.block_stages(om, st, U, B, dt, blk)
+        ref = gen.reference_stages(dim, mesh.block, int(mesh.level[blk]), gamma, slope, rk2, grav, mu, pred, dt,
+                                   out["q"])
+        for k in ("slopes", "q2", "e", "sf"):
+            assert np.array_equal(out[k], ref[k]), (blk, k)
