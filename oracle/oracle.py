@@ -173,6 +173,25 @@ def block_stages(mesh: Mesh, st: OracleSettings, U, B, dt, blk):
     return out
 
 
+def block_fluxes_emf(mesh: Mesh, st: OracleSettings, U, B, dt, blk):
+    """Face fluxes (per direction [8][faces], concatenated) and raw edge EMFs ([1|3][(b+1)^d]) of one
+    block (oracle_block_fluxes_emf), both times dt/dx."""
+    c = mesh.c
+    dim = c.dim
+    b = (c.bx, c.by, c.bz if dim == 3 else 1)
+    nf = sum(int(np.prod([b[d] + (d == dr) for d in range(dim)])) for dr in range(dim))
+    ne = int(np.prod([v + 1 for v in b[:dim]]))
+    fl = np.zeros(8 * nf)
+    emf = np.zeros((3 if dim == 3 else 1) * ne)
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    rc = lib().oracle_block_fluxes_emf(ctypes.byref(c), ctypes.byref(st), _dp(U), _dp(B), ctypes.c_double(dt),
+                                       int(blk), _dp(fl), _dp(emf))
+    if rc != 0:
+        raise RuntimeError(f"oracle_block_fluxes_emf failed: {rc}")
+    return fl, emf
+
+
 def run(mesh: Mesh, st: OracleSettings, U, B, nsteps):
     """nsteps of CFL + step, in place on copies; returns (U, B, dts)."""
     U = np.array(U, dtype=np.float64, copy=True, order="C")

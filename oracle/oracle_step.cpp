@@ -1839,6 +1839,44 @@ oracle_block_stages(const oracle_mesh * om, const oracle_settings * os, const do
   return 0;
 }
 
+// Face fluxes [dir][8][faces] (times dt/dx) and raw edge EMFs [1|3][(b+1)^d] (times dt/dx, before the
+// border correction) of block blk, as oracle_step computes them.
+int
+oracle_block_fluxes_emf(const oracle_mesh * om, const oracle_settings * os, const double * U, const double * B,
+                        double dt, int blk, double * fluxes, double * emf)
+{
+  const Mesh     m = to_mesh(om);
+  const Settings s = to_settings(os);
+  if (blk < 0 || blk >= m.n_owned)
+    return -1;
+  Fields f;
+  f.m = &m;
+  f.L = block_layout(m);
+  f.U = U;
+  f.B = B;
+  StepWork     w;
+  const double dx = cell_length(m, m.level[blk]);
+  const double dtdx = dt / dx;
+  int          st = fill_bface_ghosted(m, f, blk, w);
+  if (st == 0)
+    st = convert_to_primitives(m, f, s, blk, w);
+  if (st != 0)
+    return st;
+  compute_slopes(m, s, w);
+  compute_predictor(m, s, dt, dtdx, dx, w);
+  compute_elec_field(m, w);
+  compute_sfacemag(m, dtdx, w);
+  const FluxLayout FL = flux_layout(m);
+  std::vector<double> F((size_t)FL.total, 0.0);
+  for (int dir = 0; dir < m.dim && st == 0; ++dir)
+    st = compute_fluxes(m, s, dtdx, dir, w, F.data());
+  if (st != 0)
+    return st;
+  std::memcpy(fluxes, F.data(), sizeof(double) * F.size());
+  compute_emfs(m, s, dtdx, w, emf);
+  return 0;
+}
+
 // oracle_step that also copies the per-block face fluxes (flux * dt/dx, [block][dir][var][face]) to
 // fluxes_out, for checks of the coarse/fine flux correction.
 int

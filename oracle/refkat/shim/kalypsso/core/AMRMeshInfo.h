@@ -1,0 +1,9 @@
+// Stub of kalypsso-core's mesh counts for the functor bridge (the conforming-mesh stages use none).
+#pragma once
+namespace kalypsso
+{
+struct AMRMeshInfo
+{
+  int nb_owned = 1, nb_ghosts = 0, nb_outside = 0;
+};
+} // namespace kalypsso

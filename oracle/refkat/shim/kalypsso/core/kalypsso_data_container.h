@@ -10,11 +10,22 @@
 #include <vector>
 
 #include <kalypsso/core/kokkos_shared.h>
+#include <kalypsso/utils/config/ConfigMap.h>
 
 namespace kalypsso
 {
 template <std::size_t dim>
 using block_size_t = Kokkos::Array<int32_t, dim>;
+template <std::size_t dim, typename T = int32_t>
+using coord_t = Kokkos::Array<T, dim>;
+// the four edges of a cell seen by the 2D magnetic Riemann problem
+enum class MHDEdgeLocation : int
+{
+  LB = 0,
+  RT = 1,
+  RB = 2,
+  LT = 3
+};
 
 template <std::size_t dim, typename T, typename device_t>
 class DataArrayGhostedBlock
@@ -48,6 +59,7 @@ public:
   int32_t num_quadrants() const { return m_noct; }
   int32_t shift() const { return m_g; }
   block_size_t<dim> block_size() const { return m_bs; }
+  block_size_t<dim> shape() const { return m_bs; }
   block_size_t<dim>
   ghosted_block_size() const
   {
@@ -70,4 +82,46 @@ using DataArrayBlock = DataArrayGhostedBlock<dim, T, device_t>;
 // stages that read them)
 template <std::size_t dim, typename T, typename device_t>
 using FaceDataArrayBlock = DataArrayGhostedBlock<dim, T, device_t>;
+} // namespace kalypsso
+
+// ---- block index helpers (kalypsso-core utils) ----
+namespace kalypsso
+{
+// (i, j[, k]) of cell `cell_index` of a ghosted block (x fastest), counted from the first interior cell
+template <std::size_t dim>
+KOKKOS_INLINE_FUNCTION Kokkos::Array<int32_t, dim>
+cellindex_to_coord(int32_t cell_index, block_size_t<dim> ghosted, int32_t shift)
+{
+  Kokkos::Array<int32_t, dim> c;
+  c[0] = cell_index % ghosted[0] - shift;
+  c[1] = (cell_index / ghosted[0]) % ghosted[1] - shift;
+  if constexpr (dim == 3)
+    c[2] = cell_index / (ghosted[0] * ghosted[1]) - shift;
+  return c;
+}
+// (i, j[, k]) of cell `cell_index` of an unghosted block of `shape` (x fastest)
+template <std::size_t dim>
+KOKKOS_INLINE_FUNCTION Kokkos::Array<int32_t, dim>
+cellindex_to_coord(int32_t cell_index, block_size_t<dim> shape)
+{
+  return cellindex_to_coord<dim>(cell_index, shape, 0);
+}
+template <std::size_t dim>
+KOKKOS_INLINE_FUNCTION Kokkos::Array<int32_t, dim>
+cell_index_unravel(int32_t cell_index, block_size_t<dim> shape)
+{
+  return cellindex_to_coord<dim>(cell_index, shape, 0);
+}
+// cell length of a leaf at `level` with `bx` cells along x over a unit brick (before the scaling factor)
+template <std::size_t dim>
+KOKKOS_INLINE_FUNCTION real_t
+compute_cell_length(int level, int bx)
+{
+  return 1.0 / (double)((int64_t)bx << level);
+}
+inline real_t
+get_scaling_factor(ConfigMap const & cm)
+{
+  return cm.getReal("mesh", "scaling_factor", 1.0);
+}
 } // namespace kalypsso

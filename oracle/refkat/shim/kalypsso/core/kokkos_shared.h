@@ -26,6 +26,33 @@ abort(const char * msg)
   std::fprintf(stderr, "Kokkos::abort: %s\n", msg);
   std::abort();
 }
+template <typename T, std::size_t N>
+inline bool
+operator==(const Array<T, N> & a, const Array<T, N> & b)
+{
+  for (std::size_t i = 0; i < N; ++i)
+    if (a[i] != b[i])
+      return false;
+  return true;
+}
+template <typename T, std::size_t N>
+inline Array<T, N>
+operator*(const Array<T, N> & a, T s)
+{
+  Array<T, N> r;
+  for (std::size_t i = 0; i < N; ++i)
+    r[i] = a[i] * s;
+  return r;
+}
+template <typename T, std::size_t N>
+inline T
+dim_prod(const Array<T, N> & a)
+{
+  T p = 1;
+  for (std::size_t i = 0; i < N; ++i)
+    p *= a[i];
+  return p;
+}
 // serial stand-ins for the range policy and parallel_for the scheme functors use
 template <class Exec, class Tag = void>
 struct RangePolicy
@@ -52,6 +79,21 @@ namespace kalypsso
 struct DefaultDevice
 {
   using execution_space = int;
+};
+template <typename T>
+KOKKOS_INLINE_FUNCTION void
+my_swap(T & a, T & b)
+{
+  T t = a;
+  a = b;
+  b = t;
+}
+// component of an edge-centred array by edge direction
+enum EdgeAlong : int
+{
+  ALONG_X = 0,
+  ALONG_Y = 1,
+  ALONG_Z = 2
 };
 enum ComponentIndex3D : int
 {

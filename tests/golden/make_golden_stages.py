@@ -1,11 +1,12 @@
 """Record golden stage arrays from the reference's own stage functors.
 
 Runs the functor bridge (oracle/refkat/functor_bridge.cpp: the reference's
-ComputeLimitedSlopesFunctor, ComputeUpdatedPrimitiveVariablesFunctor, ComputeElectricFieldFunctor
-and ComputeSourceFaceMagFunctor compiled unmodified against stub headers) on the ghosted primitive
-variables the oracle builds for one block, and writes ``functor_stages.npz`` next to this script:
-per case the mesh and state (U, B), dt, the block, the settings, and the reference's slopes,
-predictor, edge field and face source. Needs the reference tree (default /root/reference, or
+ComputeLimitedSlopesFunctor, ComputeUpdatedPrimitiveVariablesFunctor, ComputeElectricFieldFunctor,
+ComputeSourceFaceMagFunctor, ComputeHydroFluxesAndStoreFunctor and ComputeEmfAndStoreFunctor
+compiled unmodified against stub headers) on the ghosted primitive variables the oracle builds for
+one block, and writes ``functor_stages.npz`` next to this script: per case the mesh and state
+(U, B), dt, the settings, and the reference's slopes, predictor, edge field, face source, face
+fluxes and raw edge EMFs (the fluxes and EMFs computed from the reference's own stage arrays). Needs the reference tree (default /root/reference, or
 $GMHD_REFERENCE_TREE); the committed npz is what tests use.
 
     python tests/golden/make_golden_stages.py
@@ -85,6 +86,27 @@ def reference_stages(dim, block, level, gamma, slope, rk2, grav, mu, pred, dt, q
     return out
 
 
+def reference_fluxes_emf(dim, block, level, gamma, slope, rk2, grav, mu, pred, dt, stages):
+    """The reference flux and EMF functors on the stage arrays `stages` (q, q2, slopes, sf) of one
+    block: fluxes per direction [8][faces] concatenated, EMFs [3][(b+1)^d] by edge direction."""
+    L = ctypes.CDLL(BRIDGE)
+    dp = ctypes.POINTER(ctypes.c_double)
+    b = (ctypes.c_int * 3)(*block)
+    prm = (ctypes.c_double * 6)(gamma, slope, 1e-10, 1e-10, 1.0, 0.0 if mu is None else mu)
+    flags = (ctypes.c_int * 5)(5, rk2, int(grav is not None), int(mu is not None), int(bool(pred)))
+    g = (ctypes.c_double * 3)(*(tuple(grav) + (0.0,) * 3)[:3] if grav is not None else (0.0, 0.0, 0.0))
+    nf = sum(int(np.prod([block[d] + (d == dr) for d in range(dim)])) for dr in range(dim))
+    ne = int(np.prod([v + 1 for v in block[:dim]]))
+    fl = np.zeros(8 * nf)
+    emf = np.zeros(3 * ne)
+    arrs = [np.ascontiguousarray(stages[k], dtype=np.float64) for k in ("q", "q2", "slopes", "sf")]
+    rc = L.ref_block_fluxes_emf(dim, b, level, prm, flags, g, ctypes.c_double(dt), *(a.ctypes.data_as(dp) for a in arrs),
+                                fl.ctypes.data_as(dp), emf.ctypes.data_as(dp))
+    if rc != 0:
+        raise RuntimeError(f"ref_block_fluxes_emf failed: {rc}")
+    return fl, emf
+
+
 def main():
     if not orc.build_refkat() or not os.path.exists(BRIDGE):
         sys.exit("the reference tree is needed to record the golden stages")
@@ -98,6 +120,8 @@ def main():
         blk = 1
         q = orc.block_stages(om, st, U, B, dt, blk)["q"]
         ref = reference_stages(dim, mesh.block, int(mesh.level[blk]), gamma, slope, rk2, grav, mu, pred, dt, q)
+        ref["fluxes"], ref["emf"] = reference_fluxes_emf(dim, mesh.block, int(mesh.level[blk]), gamma, slope, rk2,
+                                                         grav, mu, pred, dt, dict(ref, q=q))
         out[f"{name}_U"] = U
         out[f"{name}_B"] = B
         out[f"{name}_dt"] = np.float64(dt)

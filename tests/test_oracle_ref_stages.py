@@ -3,9 +3,11 @@
 The golden arrays (tests/golden/functor_stages.npz, recorded by tests/golden/make_golden_stages.py)
 are the output of the reference's ComputeLimitedSlopesFunctor, ComputeUpdatedPrimitiveVariablesFunctor
 (Hancock predictor with the gravity and viscous terms, and the RK2_SSP identity),
-ComputeElectricFieldFunctor and ComputeSourceFaceMagFunctor, compiled unmodified, on the ghosted
+ComputeElectricFieldFunctor, ComputeSourceFaceMagFunctor, ComputeHydroFluxesAndStoreFunctor (HLLD)
+and ComputeEmfAndStoreFunctor (edge reconstruction + 2D HLLD), compiled unmodified, on the ghosted
 primitive variables the oracle builds for one block. The oracle must reproduce the slopes, the
-predictor, the edge electric field and the half-step face source bit for bit. Where the reference tree
+predictor, the edge electric field, the half-step face source, the face fluxes and the raw edge EMFs
+bit for bit (2D fluxes: the variables the reference stores, rho, E, rho u, rho v, rho w, Bz). Where the reference tree
 is present the same comparison also runs live on further states.
 """
 import os
@@ -13,7 +15,6 @@ import os
 import numpy as np
 import pytest
 
-from godunov_mhd_ct_gb300.mesh import BlockMesh  # noqa: F401
 
 orc = pytest.importorskip("oracle.oracle")
 HERE = os.path.dirname(__file__)
@@ -41,6 +42,26 @@ def test_oracle_stages_match_reference_functors(golden, name):
     assert np.array_equal(out["q"], golden[f"{name}_q"])
     for k in ("slopes", "q2", "e", "sf"):
         assert np.array_equal(out[k], golden[f"{name}_{k}"]), k
+    fl, emf = orc.block_fluxes_emf(om, st, golden[f"{name}_U"], golden[f"{name}_B"], float(golden[f"{name}_dt"]), 1)
+    _same_fluxes_emf(dim, fl, emf, golden[f"{name}_fluxes"], golden[f"{name}_emf"])
+
+
+def _same_fluxes_emf(dim, fl, emf, ref_fl, ref_emf, block=None):
+    """Oracle fluxes / EMFs against the reference's: per direction a [8][faces] block; in 2D the
+    reference stores six flux variables, and its single EMF component is the z one of its edge array."""
+    block = block or ((8, 8, 1) if dim == 2 else (4, 4, 4))
+    stored = list(range(8)) if dim == 3 else [0, 1, 2, 3, 4, 7]
+    off = 0
+    for dr in range(dim):
+        n = int(np.prod([block[d] + (d == dr) for d in range(dim)]))
+        a = fl[off:off + 8 * n].reshape(8, n)
+        b = ref_fl[off:off + 8 * n].reshape(8, n)
+        for v in stored:
+            assert np.array_equal(a[v], b[v]), ("flux", dr, v)
+        off += 8 * n
+    ne = emf.size // (3 if dim == 3 else 1)
+    want = ref_emf[2 * ne:3 * ne] if dim == 2 else ref_emf
+    assert np.array_equal(emf, want), "emf"
 
 
 @pytest.mark.skipif(not os.path.isdir(os.environ.get("GMHD_REFERENCE_TREE", "/root/reference")),
@@ -69,3 +90,7 @@ def test_oracle_stages_match_reference_functors_live(dim, seed):
                                    out["q"])
         for k in ("slopes", "q2", "e", "sf"):
             assert np.array_equal(out[k], ref[k]), (blk, k)
+        fl, emf = orc.block_fluxes_emf(om, st, U, B, dt, blk)
+        rfl, remf = gen.reference_fluxes_emf(dim, mesh.block, int(mesh.level[blk]), gamma, slope, rk2, grav, mu, pred,
+                                             dt, out)
+        _same_fluxes_emf(dim, fl, emf, rfl, remf)
