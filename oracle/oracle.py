@@ -78,6 +78,8 @@ def lib():
         L.oracle_find_speed_fast.restype = ctypes.c_double
         L.oracle_find_speed_fast.argtypes = [ctypes.POINTER(OracleSettings), dp, ctypes.c_int]
         L.oracle_fill_outside.argtypes = [ctypes.POINTER(OracleMesh), dp, dp]
+        L.oracle_ct_update.restype = ctypes.c_int
+        L.oracle_ct_update.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int, dp, dp]
         _lib = L
     return _lib
 
@@ -190,6 +192,48 @@ def block_fluxes_emf(mesh: Mesh, st: OracleSettings, U, B, dt, blk):
     if rc != 0:
         raise RuntimeError(f"oracle_block_fluxes_emf failed: {rc}")
     return fl, emf
+
+
+def block_viscous_fluxes(mesh: Mesh, st: OracleSettings, U, B, dt, blk):
+    """Viscous face fluxes of one block (oracle_block_viscous_fluxes), times dt/dx, per direction
+    [8][faces] concatenated."""
+    c = mesh.c
+    dim = c.dim
+    b = (c.bx, c.by, c.bz if dim == 3 else 1)
+    nf = sum(int(np.prod([b[d] + (d == dr) for d in range(dim)])) for dr in range(dim))
+    fl = np.zeros(8 * nf)
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    rc = lib().oracle_block_viscous_fluxes(ctypes.byref(c), ctypes.byref(st), _dp(U), _dp(B), ctypes.c_double(dt),
+                                           int(blk), _dp(fl))
+    if rc != 0:
+        raise RuntimeError(f"oracle_block_viscous_fluxes failed: {rc}")
+    return fl
+
+
+def gravity_source(dim, block, gravity, dt, Uold, Unew):
+    """AddGravitySourceTerm alone (oracle_gravity_source) on a copy of Unew [n][5][cells]."""
+    Unew = np.array(Unew, dtype=np.float64, copy=True, order="C")
+    Uold = np.ascontiguousarray(Uold, dtype=np.float64)
+    b = (ctypes.c_int * 3)(*(tuple(block) + (1, 1))[:3])
+    g = (ctypes.c_double * 3)(*(tuple(float(v) for v in gravity) + (0.0, 0.0, 0.0))[:3])
+    rc = lib().oracle_gravity_source(int(dim), b, int(Unew.shape[0]), g, ctypes.c_double(dt), _dp(Uold), _dp(Unew))
+    if rc != 0:
+        raise RuntimeError(f"oracle_gravity_source failed: {rc}")
+    return Unew
+
+
+def ct_update(dim, block, emf, B):
+    """The CT update alone (oracle_ct_update) on copies: B [n][faces] += curl of emf
+    [n][1|3][(b+1)^d] (already times dt/dx). Returns the updated B."""
+    B = np.array(B, dtype=np.float64, copy=True, order="C")
+    emf = np.ascontiguousarray(emf, dtype=np.float64)
+    n = int(B.shape[0]) if B.ndim > 1 else 1
+    b = (ctypes.c_int * 3)(*(tuple(block) + (1, 1))[:3])
+    rc = lib().oracle_ct_update(int(dim), b, n, _dp(emf), _dp(B))
+    if rc != 0:
+        raise RuntimeError(f"oracle_ct_update failed: {rc}")
+    return B
 
 
 def run(mesh: Mesh, st: OracleSettings, U, B, nsteps):

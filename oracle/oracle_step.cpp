@@ -1291,6 +1291,57 @@ emf_count(const Mesh & m)
   return (int64_t)(m.bx + 1) * (m.by + 1) * (m.dim == 3 ? m.bz + 1 : 1);
 }
 
+// read_emf_and_update_{2d,3d} (scheme/ReadEmfAndUpdateFunctor.cpp:58-163): B of one block (faces,
+// C ABI layout) += curl of the block's edge EMFs emf2 [ncomp][(b+1)^d] (2D: the z component only).
+static void
+read_emf_and_update(const Mesh & m, const double * emf2, double * B2blk)
+{
+  const int     ex = m.bx + 1, ey = m.by + 1;
+  const int64_t ne = emf_count(m);
+  const BlockLayout L = block_layout(m);
+  double *          Bx = B2blk;
+  double *          By = B2blk + L.nfx;
+  double *          Bz = B2blk + L.nfx + L.nfy;
+  auto              E = [&](int c, int i, int j, int k) { return emf2[c * ne + i + (int64_t)ex * (j + (int64_t)ey * k)]; };
+  if (m.dim == 2)
+  {
+    for (int j = 0; j < m.by; ++j)
+      for (int i = 0; i <= m.bx; ++i)
+        Bx[i + (int64_t)(m.bx + 1) * j] += (E(0, i, j + 1, 0) - E(0, i, j, 0));
+    for (int j = 0; j <= m.by; ++j)
+      for (int i = 0; i < m.bx; ++i)
+        By[i + (int64_t)m.bx * j] -= (E(0, i + 1, j, 0) - E(0, i, j, 0));
+    return;
+  }
+  for (int k = 0; k < m.bz; ++k)
+    for (int j = 0; j < m.by; ++j)
+      for (int i = 0; i <= m.bx; ++i)
+      {
+        double d = 0;
+        d += (E(2, i, j + 1, k) - E(2, i, j, k));
+        d -= (E(1, i, j, k + 1) - E(1, i, j, k));
+        Bx[i + (int64_t)(m.bx + 1) * (j + (int64_t)m.by * k)] += d;
+      }
+  for (int k = 0; k < m.bz; ++k)
+    for (int j = 0; j <= m.by; ++j)
+      for (int i = 0; i < m.bx; ++i)
+      {
+        double d = 0;
+        d += (E(0, i, j, k + 1) - E(0, i, j, k));
+        d -= (E(2, i + 1, j, k) - E(2, i, j, k));
+        By[i + (int64_t)m.bx * (j + (int64_t)(m.by + 1) * k)] += d;
+      }
+  for (int k = 0; k <= m.bz; ++k)
+    for (int j = 0; j < m.by; ++j)
+      for (int i = 0; i < m.bx; ++i)
+      {
+        double d = 0;
+        d += (E(1, i + 1, j, k) - E(1, i, j, k));
+        d -= (E(0, i, j + 1, k) - E(0, i, j, k));
+        Bz[i + (int64_t)m.bx * (j + (int64_t)m.by * k)] += d;
+      }
+}
+
 // correct_emf, uniform-level branch (scheme/CorrectEmfAtBlockBorderFunctor.cpp:94-360) followed by
 // read_emf_and_update_{2d,3d} (scheme/ReadEmfAndUpdateFunctor.cpp:58-163) for block blk.
 static int
@@ -1420,48 +1471,7 @@ correct_emf_and_update_b(const Mesh & m, int blk, const std::vector<double> & em
         }
   }
   // CT update
-  const BlockLayout L = block_layout(m);
-  double *          Bx = B2blk;
-  double *          By = B2blk + L.nfx;
-  double *          Bz = B2blk + L.nfx + L.nfy;
-  auto              E = [&](int c, int i, int j, int k) { return emf2[c * ne + i + (int64_t)ex * (j + (int64_t)ey * k)]; };
-  if (m.dim == 2)
-  {
-    for (int j = 0; j < m.by; ++j)
-      for (int i = 0; i <= m.bx; ++i)
-        Bx[i + (int64_t)(m.bx + 1) * j] += (E(0, i, j + 1, 0) - E(0, i, j, 0));
-    for (int j = 0; j <= m.by; ++j)
-      for (int i = 0; i < m.bx; ++i)
-        By[i + (int64_t)m.bx * j] -= (E(0, i + 1, j, 0) - E(0, i, j, 0));
-    return 0;
-  }
-  for (int k = 0; k < m.bz; ++k)
-    for (int j = 0; j < m.by; ++j)
-      for (int i = 0; i <= m.bx; ++i)
-      {
-        double d = 0;
-        d += (E(2, i, j + 1, k) - E(2, i, j, k));
-        d -= (E(1, i, j, k + 1) - E(1, i, j, k));
-        Bx[i + (int64_t)(m.bx + 1) * (j + (int64_t)m.by * k)] += d;
-      }
-  for (int k = 0; k < m.bz; ++k)
-    for (int j = 0; j <= m.by; ++j)
-      for (int i = 0; i < m.bx; ++i)
-      {
-        double d = 0;
-        d += (E(0, i, j, k + 1) - E(0, i, j, k));
-        d -= (E(2, i + 1, j, k) - E(2, i, j, k));
-        By[i + (int64_t)m.bx * (j + (int64_t)(m.by + 1) * k)] += d;
-      }
-  for (int k = 0; k <= m.bz; ++k)
-    for (int j = 0; j < m.by; ++j)
-      for (int i = 0; i < m.bx; ++i)
-      {
-        double d = 0;
-        d += (E(1, i + 1, j, k) - E(1, i, j, k));
-        d -= (E(0, i, j + 1, k) - E(0, i, j, k));
-        Bz[i + (int64_t)m.bx * (j + (int64_t)m.by * k)] += d;
-      }
+  read_emf_and_update(m, emf2.data(), B2blk);
   return 0;
 }
 
@@ -1877,6 +1887,36 @@ oracle_block_fluxes_emf(const oracle_mesh * om, const oracle_settings * os, cons
   return 0;
 }
 
+// Viscous face fluxes of one owned block (compute_viscous_fluxes on the block's t^n primitives),
+// times dt/dx, per direction [8][faces] concatenated.
+int
+oracle_block_viscous_fluxes(const oracle_mesh * om, const oracle_settings * os, const double * U, const double * B,
+                            double dt, int blk, double * fluxes)
+{
+  const Mesh     m = to_mesh(om);
+  const Settings s = to_settings(os);
+  if (blk < 0 || blk >= m.n_owned)
+    return -1;
+  Fields f;
+  f.m = &m;
+  f.L = block_layout(m);
+  f.U = U;
+  f.B = B;
+  StepWork     w;
+  const double dx = cell_length(m, m.level[blk]);
+  int          st = fill_bface_ghosted(m, f, blk, w);
+  if (st == 0)
+    st = convert_to_primitives(m, f, s, blk, w);
+  if (st != 0)
+    return st;
+  const FluxLayout    FL = flux_layout(m);
+  std::vector<double> F((size_t)FL.total, 0.0);
+  for (int dir = 0; dir < m.dim; ++dir)
+    compute_viscous_fluxes(m, s, dt / dx, dx, dir, w, F.data());
+  std::memcpy(fluxes, F.data(), sizeof(double) * F.size());
+  return 0;
+}
+
 // oracle_step that also copies the per-block face fluxes (flux * dt/dx, [block][dir][var][face]) to
 // fluxes_out, for checks of the coarse/fine flux correction.
 int
@@ -1921,6 +1961,48 @@ cfl_inv_dt(const Mesh & m, const Settings & s, const double * v, double dx, doub
     val = std::fmax(val, 4 * nu / (dx * dx));
   }
   return val;
+}
+
+// AddGravitySourceTerm alone on n_blocks blocks of size b: Unew [n][5][cells] updated in place from
+// Uold (same layout), with gravity g[3] and time step dt.
+int
+oracle_gravity_source(int dim, const int * b, int n_blocks, const double * g, double dt, const double * Uold,
+                      double * Unew)
+{
+  if (dim != 2 && dim != 3)
+    return -1;
+  Mesh m{};
+  m.dim = dim;
+  m.bx = b[0];
+  m.by = b[1];
+  m.bz = dim == 3 ? b[2] : 1;
+  Settings s{};
+  s.gravity = 1;
+  for (int d = 0; d < 3; ++d)
+    s.grav[d] = g[d];
+  const int64_t ncell = block_layout(m).ncell;
+  for (int n = 0; n < n_blocks; ++n)
+    add_gravity_source(m, s, dt, Uold + (size_t)n * 5 * ncell, Unew + (size_t)n * 5 * ncell, ncell);
+  return 0;
+}
+
+// CT update alone on n_blocks blocks of size b (read_emf_and_update): B [n][faces] updated in place by
+// emf [n][ncomp][(b+1)^d] (ncomp 3 in 3D, 1 in 2D).
+int
+oracle_ct_update(int dim, const int * b, int n_blocks, const double * emf, double * B)
+{
+  if (dim != 2 && dim != 3)
+    return -1;
+  Mesh m{};
+  m.dim = dim;
+  m.bx = b[0];
+  m.by = b[1];
+  m.bz = dim == 3 ? b[2] : 1;
+  const BlockLayout L = block_layout(m);
+  const int64_t     ne = emf_count(m) * (dim == 3 ? 3 : 1);
+  for (int n = 0; n < n_blocks; ++n)
+    read_emf_and_update(m, emf + (size_t)n * ne, B + (size_t)n * L.nface);
+  return 0;
 }
 
 // ComputeDtMHDFunctor::apply over owned blocks; returns invDt (max over cells).

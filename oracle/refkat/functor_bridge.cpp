@@ -1,5 +1,6 @@
 // Functor bridge (test infrastructure): runs the reference's own stage functors — limited slopes,
-// Hancock predictor, edge electric field, half-step face source, face fluxes and edge EMFs
+// Hancock predictor, edge electric field, half-step face source, face fluxes, edge EMFs, the CT
+// update of the face field, the CFL reduction, the viscous face fluxes and the gravity source term
 // (scheme/*Functor.cpp, compiled unmodified from the reference tree against the stub headers in
 // shim/) — on one block whose ghosted stage inputs come from the caller, so that tests can compare the oracle's
 // restatement of those stages with the reference code itself. Built only where the reference tree
@@ -14,6 +15,10 @@
 #include <godunov_mhd_ct/scheme/ComputeLimitedSlopesFunctor.h>
 #include <godunov_mhd_ct/scheme/ComputeSourceFaceMagFunctor.h>
 #include <godunov_mhd_ct/scheme/ComputeUpdatedPrimitiveVariablesFunctor.h>
+#include <godunov_mhd_ct/scheme/AddGravitySourceTerm.h>
+#include <godunov_mhd_ct/scheme/ComputeDtMHDFunctor.h>
+#include <godunov_mhd_ct/scheme/ComputeViscousFluxesAndStoreFunctor.h>
+#include <godunov_mhd_ct/scheme/ReadEmfAndUpdateFunctor.h>
 
 using namespace kalypsso;
 using namespace kalypsso::godunov_mhd_ct;
@@ -153,9 +158,157 @@ run_fluxes(const int * b, int level, const double * prm, const int * flags, cons
   std::memcpy(emf, e.data(), sizeof(double) * e.num_cells() * 3);
   return 0;
 }
+template <std::size_t dim>
+int
+run_viscous(const int * b, int level, const double * prm, const int * flags, const double * grav, double dt,
+            const double * q_in, double * fluxes)
+{
+  const ConfigMap       cm = config_of(prm, flags, grav);
+  const ViscosityParams visc(cm);
+  FieldMap<models::MHD> fm;
+  AMRMeshInfo           info;
+  using Arr = DataArrayGhostedBlock<dim, real_t, DefaultDevice>;
+  block_size_t<dim> bs;
+  for (std::size_t d = 0; d < dim; ++d)
+    bs[d] = b[d];
+  Arr q(bs, 2, 11, 1);
+  std::memcpy(q.data(), q_in, sizeof(double) * q.num_cells() * 11);
+  typename orchard_key_base_t<DefaultDevice>::view_t keys;
+  keys.keys->push_back((uint64_t)level);
+  std::size_t off = 0;
+  for (int dir = 0; dir < (int)dim; ++dir)
+  {
+    block_size_t<dim> fs = bs;
+    fs[dir]++;
+    Arr f(fs, 0, 8, 1);
+    ComputeViscousFluxesAndStoreFunctor<dim, DefaultDevice>::apply(cm, keys, info, f, q, fm, 0, 1, dir, visc, dt);
+    std::memcpy(fluxes + off, f.data(), sizeof(double) * f.num_cells() * 8);
+    off += (std::size_t)f.num_cells() * 8;
+  }
+  return 0;
+}
+
+template <std::size_t dim>
+int
+run_inv_dt(const int * b, int n_blocks, const int * levels, const double * prm, const int * flags,
+           const double * grav, const double * U_in, const double * B_in, double * inv_dt)
+{
+  const ConfigMap       cm = config_of(prm, flags, grav);
+  const MHDSettings     st(cm);
+  FieldMap<models::MHD> fm;
+  block_size_t<dim>     bs;
+  for (std::size_t d = 0; d < dim; ++d)
+    bs[d] = b[d];
+  DataArrayBlock<dim, real_t, DefaultDevice>     U(bs, 0, 5, n_blocks);
+  FaceDataArrayBlock<dim, real_t, DefaultDevice> B(bs, n_blocks);
+  std::memcpy(U.data(), U_in, sizeof(double) * (std::size_t)U.num_cells() * 5 * n_blocks);
+  std::memcpy(B.data(), B_in, sizeof(double) * (std::size_t)B.num_elements_per_octant() * n_blocks);
+  typename orchard_key_base_t<DefaultDevice>::view_t keys;
+  for (int i = 0; i < n_blocks; ++i)
+    keys.keys->push_back((uint64_t)levels[i]);
+  real_t v = 0;
+  ComputeDtMHDFunctor<dim, DefaultDevice>::apply(cm, keys, n_blocks, st, fm, bs, U, B, v);
+  *inv_dt = v;
+  return 0;
+}
+
+template <std::size_t dim>
+int
+run_gravity(const int * b, int n_blocks, const double * grav, double dt, const double * Uold_in, double * Unew_io)
+{
+  const double prm[6] = {1.4, 1.0, 1e-10, 1e-10, 1.0, 0.0};
+  const int    flags[5] = {5, 0, 1, 0, 0};
+  const ConfigMap       cm = config_of(prm, flags, grav);
+  FieldMap<models::MHD> fm;
+  block_size_t<dim>     bs;
+  for (std::size_t d = 0; d < dim; ++d)
+    bs[d] = b[d];
+  DataArrayBlock<dim, real_t, DefaultDevice> Uold(bs, 0, 5, n_blocks), Unew(bs, 0, 5, n_blocks);
+  const std::size_t                          n = (std::size_t)Uold.num_cells() * 5 * n_blocks;
+  std::memcpy(Uold.data(), Uold_in, sizeof(double) * n);
+  std::memcpy(Unew.data(), Unew_io, sizeof(double) * n);
+  AddGravitySourceTerm<dim, DefaultDevice>::apply(cm, Uold, Unew, fm, n_blocks, dt);
+  std::memcpy(Unew_io, Unew.data(), sizeof(double) * n);
+  return 0;
+}
+
+template <std::size_t dim>
+int
+run_ct(const int * b, int n_blocks, const double * emf_in, double * B_io)
+{
+  block_size_t<dim> bs, es;
+  for (std::size_t d = 0; d < dim; ++d)
+  {
+    bs[d] = b[d];
+    es[d] = b[d] + 1;
+  }
+  FaceDataArrayBlock<dim, real_t, DefaultDevice> B(bs, n_blocks);
+  DataArrayBlock<dim, real_t, DefaultDevice>     emf(es, 0, 3, n_blocks);
+  const std::size_t                              nf = (std::size_t)B.num_elements_per_octant() * n_blocks;
+  std::memcpy(B.data(), B_io, sizeof(double) * nf);
+  std::memcpy(emf.data(), emf_in, sizeof(double) * (std::size_t)emf.num_cells() * 3 * n_blocks);
+  AMRMeshInfo info;
+  info.nb_owned = n_blocks;
+  ReadEmfAndUpdateFunctor<dim, DefaultDevice>::apply(info, B, emf);
+  std::memcpy(B_io, B.data(), sizeof(double) * nf);
+  return 0;
+}
 } // namespace
 
 extern "C" {
+
+// One block: ghosted primitives q [11][(b+4)^d] (as ref_block_stages takes them) in, the reference's
+// viscous face fluxes (times dt/dx; per direction [8][faces], directions concatenated) out.
+int
+ref_block_viscous_fluxes(int dim, const int * b, int level, const double * prm, const int * flags,
+                         const double * grav, double dt, const double * q, double * fluxes)
+{
+  if (dim == 2)
+    return run_viscous<2>(b, level, prm, flags, grav, dt, q, fluxes);
+  if (dim == 3)
+    return run_viscous<3>(b, level, prm, flags, grav, dt, q, fluxes);
+  return -1;
+}
+
+// The reference's CFL reduction (ComputeDtMHDFunctor::apply) over n_blocks unghosted blocks of the
+// C ABI layout: U [n_blocks][5][cells], B [n_blocks][Bx|By|Bz faces], block levels on the unit
+// brick. Writes max over cells of the inverse time step (before the CFL number).
+int
+ref_inv_dt(int dim, const int * b, int n_blocks, const int * levels, const double * prm, const int * flags,
+           const double * grav, const double * U, const double * B, double * inv_dt)
+{
+  if (dim == 2)
+    return run_inv_dt<2>(b, n_blocks, levels, prm, flags, grav, U, B, inv_dt);
+  if (dim == 3)
+    return run_inv_dt<3>(b, n_blocks, levels, prm, flags, grav, U, B, inv_dt);
+  return -1;
+}
+
+// The reference's gravity source term (AddGravitySourceTerm::apply): Unew [n_blocks][5][cells]
+// updated in place from Uold, uniform field grav[3], time step dt.
+int
+ref_gravity_source(int dim, const int * b, int n_blocks, const double * grav, double dt, const double * Uold,
+                   double * Unew)
+{
+  if (dim == 2)
+    return run_gravity<2>(b, n_blocks, grav, dt, Uold, Unew);
+  if (dim == 3)
+    return run_gravity<3>(b, n_blocks, grav, dt, Uold, Unew);
+  return -1;
+}
+
+// The reference's CT update (ReadEmfAndUpdateFunctor::apply): B [n_blocks][Bx|By|Bz faces] (C ABI
+// layout) updated in place by the curl of emf [n_blocks][3][(b+1)^d] (components by edge direction;
+// 2D: along z), which already carries dt/dx.
+int
+ref_ct_update(int dim, const int * b, int n_blocks, const double * emf, double * B)
+{
+  if (dim == 2)
+    return run_ct<2>(b, n_blocks, emf, B);
+  if (dim == 3)
+    return run_ct<3>(b, n_blocks, emf, B);
+  return -1;
+}
 
 // One block: the ghosted stage arrays (as ref_block_stages returns them) in, the reference's face
 // fluxes (times dt/dx; per direction [8][faces], directions concatenated) and raw edge EMFs (times

@@ -5,5 +5,6 @@ namespace kalypsso
 struct AMRMeshInfo
 {
   int nb_owned = 1, nb_ghosts = 0, nb_outside = 0;
+  int local_num_quadrants() const { return nb_owned; }
 };
 } // namespace kalypsso

@@ -68,6 +68,12 @@ public:
       g[d] = m_bs[d] + 2 * m_g;
     return g;
   }
+  // element (cell, var, oct) of an unghosted block
+  T &
+  operator()(int cell, int var, int oct) const
+  {
+    return (*m_data)[(std::size_t)cell + (std::size_t)m_ncell * (var + (std::size_t)m_nvar * oct)];
+  }
   T * data() const { return m_data->data(); }
 
 private:
@@ -78,10 +84,59 @@ private:
 
 template <std::size_t dim, typename T, typename device_t>
 using DataArrayBlock = DataArrayGhostedBlock<dim, T, device_t>;
-// face-centred arrays appear in the functors' type aliases only (the bridge does not call the
-// stages that read them)
+// Face-centred B of n octants: per octant Bx on (bx+1) x by [x bz], By on bx x (by+1) [x bz], and Bz on
+// bx x by x (bz+1) (3D) or cell-centred (2D), each x fastest, components concatenated (the layout of
+// the C ABI's face arrays). Element (i, j[, k], comp, oct).
 template <std::size_t dim, typename T, typename device_t>
-using FaceDataArrayBlock = DataArrayGhostedBlock<dim, T, device_t>;
+class FaceDataArrayBlock
+{
+public:
+  FaceDataArrayBlock() = default;
+  FaceDataArrayBlock(block_size_t<dim> cells, int noct) : m_cells(cells), m_noct(noct)
+  {
+    int off = 0;
+    for (int c = 0; c < 3; ++c)
+    {
+      int n = 1;
+      for (std::size_t d = 0; d < dim; ++d)
+        n *= cells[d] + ((int)d == c ? 1 : 0);
+      m_off[c] = off;
+      off += n;
+    }
+    m_per = off;
+    m_data = std::make_shared<std::vector<T>>((std::size_t)m_per * noct, T(0));
+  }
+  template <std::size_t D = dim, std::enable_if_t<D == 2, int> = 0>
+  T &
+  operator()(int i, int j, int c, int oct) const
+  {
+    const int nx = m_cells[0] + (c == 0);
+    return (*m_data)[(std::size_t)m_per * oct + m_off[c] + i + (std::size_t)nx * j];
+  }
+  template <std::size_t D = dim, std::enable_if_t<D == 3, int> = 0>
+  T &
+  operator()(int i, int j, int k, int c, int oct) const
+  {
+    const int nx = m_cells[0] + (c == 0), ny = m_cells[1] + (c == 1);
+    return (*m_data)[(std::size_t)m_per * oct + m_off[c] + i + (std::size_t)nx * (j + (std::size_t)ny * k)];
+  }
+  block_size_t<dim>       cell_block_size() const { return m_cells; }
+  int32_t                 num_elements_per_octant() const { return m_per; }
+  Kokkos::Array<int32_t, 3> offsets() const
+  {
+    Kokkos::Array<int32_t, 3> o;
+    for (int c = 0; c < 3; ++c)
+      o[c] = m_off[c];
+    return o;
+  }
+  int32_t shift() const { return 0; }
+  T *     data() const { return m_data->data(); }
+
+private:
+  block_size_t<dim>               m_cells{};
+  int                             m_noct = 0, m_per = 0, m_off[3] = {0, 0, 0};
+  std::shared_ptr<std::vector<T>> m_data;
+};
 } // namespace kalypsso
 
 // ---- block index helpers (kalypsso-core utils) ----
@@ -123,5 +178,24 @@ inline real_t
 get_scaling_factor(ConfigMap const & cm)
 {
   return cm.getReal("mesh", "scaling_factor", 1.0);
+}
+// (i, j[, k], comp) of face `idx` of a face block (components concatenated at `offsets`)
+template <std::size_t dim, typename O>
+KOKKOS_INLINE_FUNCTION Kokkos::Array<int32_t, dim + 1>
+face_flat_index_unravel(int32_t idx, block_size_t<dim> cells, O const & offsets, int32_t shift)
+{
+  int c = 2;
+  while (c > 0 && idx < offsets[c])
+    --c;
+  int32_t r = idx - offsets[c];
+  Kokkos::Array<int32_t, dim + 1> out;
+  for (std::size_t d = 0; d < dim; ++d)
+  {
+    const int32_t n = cells[d] + ((int)d == c ? 1 : 0);
+    out[d] = r % n - shift;
+    r /= n;
+  }
+  out[dim] = c;
+  return out;
 }
 } // namespace kalypsso

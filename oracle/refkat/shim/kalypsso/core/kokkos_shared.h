@@ -4,6 +4,7 @@
 #include <cstddef>
 #include <cstdio>
 #include <cstdlib>
+#include <limits>
 #include <type_traits>
 #include <kalypsso/core/real_type.h>
 
@@ -45,6 +46,21 @@ operator*(const Array<T, N> & a, T s)
   return r;
 }
 template <typename T, std::size_t N>
+inline Array<T, N>
+operator+(const Array<T, N> & a, T s)
+{
+  Array<T, N> r;
+  for (std::size_t i = 0; i < N; ++i)
+    r[i] = a[i] + s;
+  return r;
+}
+template <typename T>
+struct Max
+{
+  T & ref;
+  explicit Max(T & r) : ref(r) {}
+};
+template <typename T, std::size_t N>
 inline T
 dim_prod(const Array<T, N> & a)
 {
@@ -71,6 +87,15 @@ parallel_for(const char *, RangePolicy<Exec, Tag> p, const F & f)
     else
       f(Tag{}, i);
   }
+}
+template <class F, class Exec, class Tag, typename T>
+void
+parallel_reduce(const char *, RangePolicy<Exec, Tag> p, const F & f, Max<T> red)
+{
+  T v = std::numeric_limits<T>::lowest();
+  for (long long i = p.b; i < p.e; ++i)
+    f(i, v);
+  red.ref = v;
 }
 } // namespace Kokkos
 

@@ -2,11 +2,16 @@
 
 Runs the functor bridge (oracle/refkat/functor_bridge.cpp: the reference's
 ComputeLimitedSlopesFunctor, ComputeUpdatedPrimitiveVariablesFunctor, ComputeElectricFieldFunctor,
-ComputeSourceFaceMagFunctor, ComputeHydroFluxesAndStoreFunctor and ComputeEmfAndStoreFunctor
-compiled unmodified against stub headers) on the ghosted primitive variables the oracle builds for
-one block, and writes ``functor_stages.npz`` next to this script: per case the mesh and state
-(U, B), dt, the settings, and the reference's slopes, predictor, edge field, face source, face
-fluxes and raw edge EMFs (the fluxes and EMFs computed from the reference's own stage arrays). Needs the reference tree (default /root/reference, or
+ComputeSourceFaceMagFunctor, ComputeHydroFluxesAndStoreFunctor, ComputeEmfAndStoreFunctor,
+ReadEmfAndUpdateFunctor, ComputeDtMHDFunctor, ComputeViscousFluxesAndStoreFunctor and
+AddGravitySourceTerm compiled unmodified against stub headers) on the
+ghosted primitive variables the oracle builds for one block, and writes ``functor_stages.npz`` next
+to this script: per case the mesh and state (U, B), dt, the settings, and the reference's slopes,
+predictor, edge field, face source, face fluxes and raw edge EMFs (the fluxes and EMFs computed from
+the reference's own stage arrays), the block's faces after the reference's CT update by those EMFs
+(``ct_B``), the reference's CFL reduction over the mesh (``inv_dt``), with viscosity its viscous
+face fluxes (``visc``) and with gravity its source term on the owned blocks (``grav_U``, inputs from
+``gravity_inputs``). Needs the reference tree (default /root/reference, or
 $GMHD_REFERENCE_TREE); the committed npz is what tests use.
 
     python tests/golden/make_golden_stages.py
@@ -107,6 +112,87 @@ def reference_fluxes_emf(dim, block, level, gamma, slope, rk2, grav, mu, pred, d
     return fl, emf
 
 
+def _bridge_args(gamma, slope, rk2, grav, mu, pred):
+    prm = (ctypes.c_double * 6)(gamma, slope, 1e-10, 1e-10, 1.0, 0.0 if mu is None else mu)
+    flags = (ctypes.c_int * 5)(5, rk2, int(grav is not None), int(mu is not None), int(bool(pred)))
+    g = (ctypes.c_double * 3)(*(tuple(grav) + (0.0,) * 3)[:3] if grav is not None else (0.0, 0.0, 0.0))
+    return prm, flags, g
+
+
+def reference_viscous_fluxes(dim, block, level, gamma, slope, rk2, grav, mu, pred, dt, q):
+    """The reference viscous flux functor (ComputeViscousFluxesAndStoreFunctor) on the ghosted
+    primitives q of one block: per direction [8][faces], concatenated."""
+    L = ctypes.CDLL(BRIDGE)
+    dp = ctypes.POINTER(ctypes.c_double)
+    b = (ctypes.c_int * 3)(*block)
+    nf = sum(int(np.prod([block[d] + (d == dr) for d in range(dim)])) for dr in range(dim))
+    fl = np.zeros(8 * nf)
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    rc = L.ref_block_viscous_fluxes(dim, b, level, *_bridge_args(gamma, slope, rk2, grav, mu, pred), ctypes.c_double(dt),
+                                    q.ctypes.data_as(dp), fl.ctypes.data_as(dp))
+    if rc != 0:
+        raise RuntimeError(f"ref_block_viscous_fluxes failed: {rc}")
+    return fl
+
+
+def gravity_inputs(mesh, U):
+    """(Uold, Unew) for the gravity source check: the owned blocks of U, and a copy with the density
+    raised by 1 % and the momenta shifted (a stand-in for the hydro update)."""
+    n = mesh.n_owned
+    Uold = np.ascontiguousarray(U[:n], dtype=np.float64)
+    Unew = Uold.copy()
+    Unew[:, 0] *= 1.01
+    Unew[:, 2:5] += 0.05
+    return Uold, Unew
+
+
+def reference_gravity(dim, block, grav, dt, Uold, Unew):
+    """The reference gravity source term (AddGravitySourceTerm) on a copy of Unew."""
+    L = ctypes.CDLL(BRIDGE)
+    dp = ctypes.POINTER(ctypes.c_double)
+    b = (ctypes.c_int * 3)(*block)
+    g = (ctypes.c_double * 3)(*(tuple(grav) + (0.0,) * 3)[:3])
+    Unew = np.array(Unew, dtype=np.float64, copy=True)
+    Uold = np.ascontiguousarray(Uold, dtype=np.float64)
+    rc = L.ref_gravity_source(dim, b, int(Unew.shape[0]), g, ctypes.c_double(dt), Uold.ctypes.data_as(dp),
+                              Unew.ctypes.data_as(dp))
+    if rc != 0:
+        raise RuntimeError(f"ref_gravity_source failed: {rc}")
+    return Unew
+
+
+def reference_inv_dt(mesh, gamma, slope, rk2, grav, mu, pred, U, B):
+    """The reference CFL reduction (ComputeDtMHDFunctor) over the owned blocks of `mesh`."""
+    L = ctypes.CDLL(BRIDGE)
+    dp = ctypes.POINTER(ctypes.c_double)
+    n = mesh.n_owned
+    b = (ctypes.c_int * 3)(*mesh.block)
+    lev = np.ascontiguousarray(mesh.level[:n], dtype=np.int32)
+    Uo = np.ascontiguousarray(U[:n], dtype=np.float64)
+    Bo = np.ascontiguousarray(B[:n], dtype=np.float64)
+    out = ctypes.c_double(0.0)
+    rc = L.ref_inv_dt(mesh.dim, b, n, lev.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                      *_bridge_args(gamma, slope, rk2, grav, mu, pred), Uo.ctypes.data_as(dp), Bo.ctypes.data_as(dp),
+                      ctypes.byref(out))
+    if rc != 0:
+        raise RuntimeError(f"ref_inv_dt failed: {rc}")
+    return out.value
+
+
+def reference_ct(dim, block, emf, B):
+    """The reference CT update (ReadEmfAndUpdateFunctor) of one block's faces B by its edge EMFs
+    emf [3][(b+1)^d] (2D: component 2 is the z one). Returns the updated B."""
+    L = ctypes.CDLL(BRIDGE)
+    dp = ctypes.POINTER(ctypes.c_double)
+    b = (ctypes.c_int * 3)(*block)
+    B = np.array(B, dtype=np.float64, copy=True)
+    emf = np.ascontiguousarray(emf, dtype=np.float64)
+    rc = L.ref_ct_update(dim, b, 1, emf.ctypes.data_as(dp), B.ctypes.data_as(dp))
+    if rc != 0:
+        raise RuntimeError(f"ref_ct_update failed: {rc}")
+    return B
+
+
 def main():
     if not orc.build_refkat() or not os.path.exists(BRIDGE):
         sys.exit("the reference tree is needed to record the golden stages")
@@ -122,6 +208,13 @@ def main():
         ref = reference_stages(dim, mesh.block, int(mesh.level[blk]), gamma, slope, rk2, grav, mu, pred, dt, q)
         ref["fluxes"], ref["emf"] = reference_fluxes_emf(dim, mesh.block, int(mesh.level[blk]), gamma, slope, rk2,
                                                          grav, mu, pred, dt, dict(ref, q=q))
+        if mu is not None:
+            ref["visc"] = reference_viscous_fluxes(dim, mesh.block, int(mesh.level[blk]), gamma, slope, rk2, grav, mu,
+                                                   pred, dt, q)
+        if grav is not None:
+            ref["grav_U"] = reference_gravity(dim, mesh.block, grav, dt, *gravity_inputs(mesh, U))
+        ref["inv_dt"] = np.float64(reference_inv_dt(mesh, gamma, slope, rk2, grav, mu, pred, U, B))
+        ref["ct_B"] = reference_ct(dim, mesh.block, ref["emf"], B[blk])
         out[f"{name}_U"] = U
         out[f"{name}_B"] = B
         out[f"{name}_dt"] = np.float64(dt)
