@@ -223,6 +223,18 @@ def gravity_source(dim, block, gravity, dt, Uold, Unew):
     return Unew
 
 
+def block_update(mesh: Mesh, blk, fluxes, U2blk, B2blk):
+    """Conservative update alone (oracle_block_update) of block blk by its face fluxes, on copies of
+    the block's U2 [5][cells] and faces B2; returns (U2blk, B2blk)."""
+    U2blk = np.array(U2blk, dtype=np.float64, copy=True, order="C")
+    B2blk = np.array(B2blk, dtype=np.float64, copy=True, order="C")
+    fluxes = np.ascontiguousarray(fluxes, dtype=np.float64)
+    rc = lib().oracle_block_update(ctypes.byref(mesh.c), int(blk), _dp(fluxes), _dp(U2blk), _dp(B2blk))
+    if rc != 0:
+        raise RuntimeError(f"oracle_block_update failed: {rc}")
+    return U2blk, B2blk
+
+
 def ct_update(dim, block, emf, B):
     """The CT update alone (oracle_ct_update) on copies: B [n][faces] += curl of emf
     [n][1|3][(b+1)^d] (already times dt/dx). Returns the updated B."""

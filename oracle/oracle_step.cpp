@@ -1986,6 +1986,22 @@ oracle_gravity_source(int dim, const int * b, int n_blocks, const double * g, do
   return 0;
 }
 
+// Conservative update alone (update_u) of owned block blk with its face fluxes `fluxes` (per
+// direction [8][faces] concatenated, times dt/dx): U2blk [5][cells] and the block's faces B2blk (2D:
+// the cell-centred Bz) updated in place. Blocks with finer neighbours need their fluxes too: -1.
+int
+oracle_block_update(const oracle_mesh * om, int blk, const double * fluxes, double * U2blk, double * B2blk)
+{
+  const Mesh m = to_mesh(om);
+  if (blk < 0 || blk >= m.n_owned)
+    return -1;
+  const FluxLayout                 FL = flux_layout(m);
+  const BlockLayout                L = block_layout(m);
+  std::vector<std::vector<double>> flux_all((size_t)m.n_blocks);
+  flux_all[blk].assign(fluxes, fluxes + FL.total);
+  return update_u(m, blk, flux_all, U2blk, B2blk + L.nfx + L.nfy);
+}
+
 // CT update alone on n_blocks blocks of size b (read_emf_and_update): B [n][faces] updated in place by
 // emf [n][ncomp][(b+1)^d] (ncomp 3 in 3D, 1 in 2D).
 int

@@ -1,6 +1,7 @@
 // Functor bridge (test infrastructure): runs the reference's own stage functors — limited slopes,
 // Hancock predictor, edge electric field, half-step face source, face fluxes, edge EMFs, the CT
-// update of the face field, the CFL reduction, the viscous face fluxes and the gravity source term
+// update of the face field, the CFL reduction, the viscous face fluxes, the gravity source term and
+// the conservative update by face fluxes
 // (scheme/*Functor.cpp, compiled unmodified from the reference tree against the stub headers in
 // shim/) — on one block whose ghosted stage inputs come from the caller, so that tests can compare the oracle's
 // restatement of those stages with the reference code itself. Built only where the reference tree
@@ -19,6 +20,7 @@
 #include <godunov_mhd_ct/scheme/ComputeDtMHDFunctor.h>
 #include <godunov_mhd_ct/scheme/ComputeViscousFluxesAndStoreFunctor.h>
 #include <godunov_mhd_ct/scheme/ReadEmfAndUpdateFunctor.h>
+#include <godunov_mhd_ct/scheme/ReadFluxesAndConservativeUpdateFunctor.h>
 
 using namespace kalypsso;
 using namespace kalypsso::godunov_mhd_ct;
@@ -234,6 +236,49 @@ run_gravity(const int * b, int n_blocks, const double * grav, double dt, const d
 
 template <std::size_t dim>
 int
+run_update(const int * b, const double * prm, const int * flags, const double * grav, double dt,
+           const double * fluxes, double * U_io, double * B_io)
+{
+  const ConfigMap       cm = config_of(prm, flags, grav);
+  const MHDSettings     st(cm);
+  FieldMap<models::MHD> fm;
+  AMRMeshInfo           info;
+  block_size_t<dim>     bs;
+  brick_size_t<dim>     bricks;
+  Kokkos::Array<bool, dim> periodic;
+  for (std::size_t d = 0; d < dim; ++d)
+  {
+    bs[d] = b[d];
+    bricks[d] = 1;
+    periodic[d] = true;
+  }
+  DataArrayBlock<dim, real_t, DefaultDevice>     U(bs, 0, 5, 1);
+  FaceDataArrayBlock<dim, real_t, DefaultDevice> B(bs, 1);
+  std::memcpy(U.data(), U_io, sizeof(double) * (std::size_t)U.num_cells() * 5);
+  std::memcpy(B.data(), B_io, sizeof(double) * (std::size_t)B.num_elements_per_octant());
+  typename orchard_key_base_t<DefaultDevice>::view_t keys;
+  keys.keys->push_back(0);
+  conformal_status_view_t<dim, DefaultDevice> status;
+  status.bits->push_back(0); // conforming: no finer neighbour across any face
+  typename hashmap_base_t<DefaultDevice>::map_t map;
+  std::size_t                                   off = 0;
+  for (int dir = 0; dir < (int)dim; ++dir)
+  {
+    block_size_t<dim> fs = bs;
+    fs[dir]++;
+    DataArrayBlock<dim, real_t, DefaultDevice> f(fs, 0, 8, 1);
+    std::memcpy(f.data(), fluxes + off, sizeof(double) * f.num_cells() * 8);
+    off += (std::size_t)f.num_cells() * 8;
+    ReadFluxesAndConservativeUpdateFunctor<dim, DefaultDevice>::apply(cm, map, keys, status, info, U, B, f, fm, dir,
+                                                                      bricks, periodic, st, dt);
+  }
+  std::memcpy(U_io, U.data(), sizeof(double) * (std::size_t)U.num_cells() * 5);
+  std::memcpy(B_io, B.data(), sizeof(double) * (std::size_t)B.num_elements_per_octant());
+  return 0;
+}
+
+template <std::size_t dim>
+int
 run_ct(const int * b, int n_blocks, const double * emf_in, double * B_io)
 {
   block_size_t<dim> bs, es;
@@ -294,6 +339,20 @@ ref_gravity_source(int dim, const int * b, int n_blocks, const double * grav, do
     return run_gravity<2>(b, n_blocks, grav, dt, Uold, Unew);
   if (dim == 3)
     return run_gravity<3>(b, n_blocks, grav, dt, Uold, Unew);
+  return -1;
+}
+
+// The reference's conservative update (ReadFluxesAndConservativeUpdateFunctor::apply, direction by
+// direction) of one conforming block: U [5][cells] and faces B (2D: the cell-centred Bz) updated in
+// place by the face fluxes (per direction [8][faces] concatenated, times dt/dx).
+int
+ref_block_update(int dim, const int * b, const double * prm, const int * flags, const double * grav, double dt,
+                 const double * fluxes, double * U, double * B)
+{
+  if (dim == 2)
+    return run_update<2>(b, prm, flags, grav, dt, fluxes, U, B);
+  if (dim == 3)
+    return run_update<3>(b, prm, flags, grav, dt, fluxes, U, B);
   return -1;
 }
 

@@ -18,6 +18,18 @@ template <std::size_t dim>
 using block_size_t = Kokkos::Array<int32_t, dim>;
 template <std::size_t dim, typename T = int32_t>
 using coord_t = Kokkos::Array<T, dim>;
+template <std::size_t dim>
+using brick_size_t = Kokkos::Array<int32_t, dim>;
+// an array with every element v
+template <typename T, std::size_t N>
+KOKKOS_INLINE_FUNCTION Kokkos::Array<T, N>
+init_kokkos_array(T v)
+{
+  Kokkos::Array<T, N> a;
+  for (std::size_t i = 0; i < N; ++i)
+    a[i] = v;
+  return a;
+}
 // the four edges of a cell seen by the 2D magnetic Riemann problem
 enum class MHDEdgeLocation : int
 {

@@ -54,6 +54,33 @@ operator+(const Array<T, N> & a, T s)
     r[i] = a[i] + s;
   return r;
 }
+template <typename T, std::size_t N>
+inline Array<T, N>
+operator+(const Array<T, N> & a, const Array<T, N> & b)
+{
+  Array<T, N> r;
+  for (std::size_t i = 0; i < N; ++i)
+    r[i] = a[i] + b[i];
+  return r;
+}
+template <typename T, std::size_t N>
+inline Array<T, N>
+operator-(const Array<T, N> & a, const Array<T, N> & b)
+{
+  Array<T, N> r;
+  for (std::size_t i = 0; i < N; ++i)
+    r[i] = a[i] - b[i];
+  return r;
+}
+template <typename T, std::size_t N, typename S>
+inline Array<T, N>
+operator/(const Array<T, N> & a, S s)
+{
+  Array<T, N> r;
+  for (std::size_t i = 0; i < N; ++i)
+    r[i] = a[i] / s;
+  return r;
+}
 template <typename T>
 struct Max
 {

@@ -3,15 +3,16 @@
 Runs the functor bridge (oracle/refkat/functor_bridge.cpp: the reference's
 ComputeLimitedSlopesFunctor, ComputeUpdatedPrimitiveVariablesFunctor, ComputeElectricFieldFunctor,
 ComputeSourceFaceMagFunctor, ComputeHydroFluxesAndStoreFunctor, ComputeEmfAndStoreFunctor,
-ReadEmfAndUpdateFunctor, ComputeDtMHDFunctor, ComputeViscousFluxesAndStoreFunctor and
-AddGravitySourceTerm compiled unmodified against stub headers) on the
+ReadEmfAndUpdateFunctor, ComputeDtMHDFunctor, ComputeViscousFluxesAndStoreFunctor,
+AddGravitySourceTerm and ReadFluxesAndConservativeUpdateFunctor compiled unmodified against stub headers) on the
 ghosted primitive variables the oracle builds for one block, and writes ``functor_stages.npz`` next
 to this script: per case the mesh and state (U, B), dt, the settings, and the reference's slopes,
 predictor, edge field, face source, face fluxes and raw edge EMFs (the fluxes and EMFs computed from
 the reference's own stage arrays), the block's faces after the reference's CT update by those EMFs
 (``ct_B``), the reference's CFL reduction over the mesh (``inv_dt``), with viscosity its viscous
 face fluxes (``visc``) and with gravity its source term on the owned blocks (``grav_U``, inputs from
-``gravity_inputs``). Needs the reference tree (default /root/reference, or
+``gravity_inputs``), and the block's U and faces after the reference's conservative update by
+those fluxes, then by the viscous ones (``upd_U``, ``upd_B``). Needs the reference tree (default /root/reference, or
 $GMHD_REFERENCE_TREE); the committed npz is what tests use.
 
     python tests/golden/make_golden_stages.py
@@ -135,6 +136,22 @@ def reference_viscous_fluxes(dim, block, level, gamma, slope, rk2, grav, mu, pre
     return fl
 
 
+def reference_update(dim, block, gamma, slope, rk2, grav, mu, pred, dt, fluxes, Ublk, Bblk):
+    """The reference conservative update (ReadFluxesAndConservativeUpdateFunctor, direction by
+    direction) of one conforming block by its face fluxes, on copies; returns (U, B)."""
+    L = ctypes.CDLL(BRIDGE)
+    dp = ctypes.POINTER(ctypes.c_double)
+    b = (ctypes.c_int * 3)(*block)
+    U = np.array(Ublk, dtype=np.float64, copy=True)
+    B = np.array(Bblk, dtype=np.float64, copy=True)
+    fl = np.ascontiguousarray(fluxes, dtype=np.float64)
+    rc = L.ref_block_update(dim, b, *_bridge_args(gamma, slope, rk2, grav, mu, pred), ctypes.c_double(dt),
+                            fl.ctypes.data_as(dp), U.ctypes.data_as(dp), B.ctypes.data_as(dp))
+    if rc != 0:
+        raise RuntimeError(f"ref_block_update failed: {rc}")
+    return U, B
+
+
 def gravity_inputs(mesh, U):
     """(Uold, Unew) for the gravity source check: the owned blocks of U, and a copy with the density
     raised by 1 % and the momenta shifted (a stand-in for the hydro update)."""
@@ -213,6 +230,10 @@ def main():
                                                    pred, dt, q)
         if grav is not None:
             ref["grav_U"] = reference_gravity(dim, mesh.block, grav, dt, *gravity_inputs(mesh, U))
+        args = (dim, mesh.block, gamma, slope, rk2, grav, mu, pred, dt)
+        ref["upd_U"], ref["upd_B"] = reference_update(*args, ref["fluxes"], U[blk], B[blk])
+        if mu is not None:
+            ref["upd_U"], ref["upd_B"] = reference_update(*args, ref["visc"], ref["upd_U"], ref["upd_B"])
         ref["inv_dt"] = np.float64(reference_inv_dt(mesh, gamma, slope, rk2, grav, mu, pred, U, B))
         ref["ct_B"] = reference_ct(dim, mesh.block, ref["emf"], B[blk])
         out[f"{name}_U"] = U

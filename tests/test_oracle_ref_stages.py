@@ -6,10 +6,10 @@ are the output of the reference's ComputeLimitedSlopesFunctor, ComputeUpdatedPri
 ComputeElectricFieldFunctor, ComputeSourceFaceMagFunctor, ComputeHydroFluxesAndStoreFunctor (HLLD),
 ComputeEmfAndStoreFunctor (edge reconstruction + 2D HLLD), ComputeViscousFluxesAndStoreFunctor,
 ReadEmfAndUpdateFunctor (CT update), ComputeDtMHDFunctor (CFL with the gravity and viscous
-limits) and AddGravitySourceTerm, compiled unmodified, on the ghosted primitive variables the oracle builds for one block. The
+limits), AddGravitySourceTerm and ReadFluxesAndConservativeUpdateFunctor, compiled unmodified, on the ghosted primitive variables the oracle builds for one block. The
 oracle must reproduce the slopes, the predictor, the edge electric field, the half-step face source,
-the face fluxes, the raw edge EMFs, the viscous fluxes, the CT update, the CFL reduction and the
-gravity source bit for bit (2D fluxes: the variables the reference stores, rho, E, rho u, rho v, rho w, Bz). Where the reference tree
+the face fluxes, the raw edge EMFs, the viscous fluxes, the conservative update by the fluxes, the CT
+update, the CFL reduction and the gravity source bit for bit (2D fluxes: the variables the reference stores, rho, E, rho u, rho v, rho w, Bz). Where the reference tree
 is present the same comparison also runs live on further states.
 """
 import os
@@ -53,6 +53,10 @@ def test_oracle_stages_match_reference_functors(golden, name):
     if mu is not None:
         vf = orc.block_viscous_fluxes(om, st, golden[f"{name}_U"], golden[f"{name}_B"], float(golden[f"{name}_dt"]), 1)
         _same_fluxes(dim, vf, golden[f"{name}_visc"])
+    U1, B1 = orc.block_update(om, 1, golden[f"{name}_fluxes"], golden[f"{name}_U"][1], golden[f"{name}_B"][1])
+    if mu is not None:
+        U1, B1 = orc.block_update(om, 1, golden[f"{name}_visc"], U1, B1)
+    assert np.array_equal(U1, golden[f"{name}_upd_U"]) and np.array_equal(B1, golden[f"{name}_upd_B"])
     if grav is not None:
         Uold, Unew = gen.gravity_inputs(mesh, golden[f"{name}_U"])
         got = orc.gravity_source(dim, mesh.block, grav, float(golden[f"{name}_dt"]), Uold, Unew)
@@ -133,6 +137,10 @@ def test_oracle_stages_match_reference_functors_live(dim, seed):
             vf = orc.block_viscous_fluxes(om, st, U, B, dt, blk)
             _same_fluxes(dim, vf, gen.reference_viscous_fluxes(dim, mesh.block, int(mesh.level[blk]), gamma, slope, rk2,
                                                                grav, mu, pred, dt, out["q"]))
+        args = (dim, mesh.block, gamma, slope, rk2, grav, mu, pred, dt)
+        want = gen.reference_update(*args, rfl, U[blk], B[blk])
+        got = orc.block_update(om, blk, rfl, U[blk], B[blk])
+        assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1]), blk
 
 
 @pytest.mark.skipif(not os.path.isdir(os.environ.get("GMHD_REFERENCE_TREE", "/root/reference")),
