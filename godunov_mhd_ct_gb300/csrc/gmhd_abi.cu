@@ -1198,14 +1198,16 @@ gmhd_step_host_async(gmhd_ctx * ctx, const double * U, double * U2, const double
       return rc;
   }
   cudaStream_t caller = (cudaStream_t)stream;
-  // copy in (U, B are complete in host memory when the call is made), after the staging set's last
-  // copy-out
-  GMHD_CUDA(cudaStreamWaitEvent(ctx->a_in, ctx->a_out_done[k], 0));
+  // copy in (U, B are complete in host memory when the call is made) once the step that last read this
+  // input set is done; the input and output sets are released separately, so that the copy-in of one
+  // call runs beside the copy-out of the call before it
+  GMHD_CUDA(cudaStreamWaitEvent(ctx->a_in, ctx->a_run_done[k], 0));
   GMHD_CUDA(cudaMemcpyAsync(ctx->a_U[k], U, nu * sizeof(double), cudaMemcpyHostToDevice, ctx->a_in));
   GMHD_CUDA(cudaMemcpyAsync(ctx->a_B[k], B, nb * sizeof(double), cudaMemcpyHostToDevice, ctx->a_in));
   GMHD_CUDA(cudaEventRecord(ctx->a_in_done[k], ctx->a_in));
-  // the step
+  // the step, once its inputs are in and the output set's last copy-out is done
   GMHD_CUDA(cudaStreamWaitEvent(ctx->a_run, ctx->a_in_done[k], 0));
+  GMHD_CUDA(cudaStreamWaitEvent(ctx->a_run, ctx->a_out_done[k], 0));
   gmhd::StepArgs a = make_args(ctx, ctx->a_U[k], ctx->a_U2[k], ctx->a_B[k], ctx->a_B2[k]);
   a.dt = dt;
   if ((rc = launch_step(ctx, a, ctx->a_run)))

@@ -284,7 +284,8 @@ void gmhd_forest_destroy(gmhd_forest * forest);
  * returns without waiting; the results are in U2/B2 once `stream` has completed the work enqueued
  * before this call returns (synchronise `stream`). Consecutive calls overlap: the host->device copy of
  * one call, the step of the previous call and the device->host copy of the one before run at the same
- * time (two device staging sets and three streams owned by ctx). U and B are read as they are in host
+ * time (two device input sets and two output sets, released independently, and three streams owned by
+ * ctx). U and B are read as they are in host
  * memory when the call is made (the copy-in does not wait for work on `stream`: synchronise `stream`
  * first when they are the results of an earlier call). Until the call completes, U and B must stay
  * unchanged and U2, B2 must not be read. Host buffers should be page-locked for the copies to overlap. */

@@ -169,7 +169,7 @@ def test_step_host_async_matches_step(oracle_lib):
     torch.cuda.synchronize()
     ref_U, ref_B = dU2.cpu().numpy(), dB2.cpu().numpy()
     hU, hB = torch.from_numpy(U).pin_memory(), torch.from_numpy(B).pin_memory()
-    outs = [(torch.zeros_like(hU).pin_memory(), torch.zeros_like(hB).pin_memory()) for _ in range(3)]
+    outs = [(torch.zeros_like(hU).pin_memory(), torch.zeros_like(hB).pin_memory()) for _ in range(5)]
     s = torch.cuda.current_stream()
     for hU2, hB2 in outs:
         nat.check(nat.lib().gmhd_step_host_async(impl._ctx, hU.data_ptr(), hU2.data_ptr(), hB.data_ptr(),
