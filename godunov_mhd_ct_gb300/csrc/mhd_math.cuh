@@ -6,6 +6,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 
 namespace gmhd
 {
@@ -175,17 +176,55 @@ rcopysign<float>(float a, float b)
   return copysignf(a, b);
 }
 
+// Divisions that share a divisor. FP64 keeps the reference's x / y (bit-exact parity); the FP32
+// path multiplies by one reciprocal inv = recip(y) computed for all of them (unused, and removed,
+// on the FP64 path).
+template <typename R>
+__device__ __forceinline__ R
+recip(R y)
+{
+  return R(1) / y;
+}
+template <typename R>
+__device__ __forceinline__ R
+qdiv(R x, R y, R inv)
+{
+  (void)inv;
+  return x / y;
+}
+template <>
+__device__ __forceinline__ float
+qdiv<float>(float x, float y, float inv)
+{
+  (void)y;
+  return x * inv;
+}
+// x / sqrt(r): FP64 as written, FP32 as x * rsqrt(r)
+template <typename R>
+__device__ __forceinline__ R
+div_sqrt(R x, R r)
+{
+  return x / dsqrt<R>(r);
+}
+template <>
+__device__ __forceinline__ float
+div_sqrt<float>(float x, float r)
+{
+  return x * rsqrtf(r);
+}
+
 // find_speed_fast<dir> (models/mhd_utils.h:93-122)
 template <typename R>
 __device__ __forceinline__ R
 speed_fast(const R * q, int dir, const Phys<R> & s)
 {
   const R d = q[ID], p = q[IP], a = q[IA], b = q[IB], c = q[IC];
+  const R id = recip<R>(d);
   const R b2 = a * a + b * b + c * c;
-  const R c2 = s.gamma0 * p / d;
-  const R d2 = R(0.5) * (b2 / d + c2);
+  const R c2 = qdiv<R>(s.gamma0 * p, d, id);
+  const R d2 = R(0.5) * (qdiv<R>(b2, d, id) + c2);
   const R bn = dir == 0 ? a : (dir == 1 ? b : c);
-  return dsqrt<R>(d2 + dsqrt<R>(d2 * d2 - c2 * bn * bn / d));
+  return dsqrt<R>(d2 + dsqrt<R>(d2 * d2 - qdiv<R>(c2 * bn * bn, d, id)));
 }
 
 // find_mhd_flux (models/mhd_utils.h:182-245), cIso == 0
@@ -358,10 +397,12 @@ riemann_hlld(R * qL, R * qR, R * flux, const Phys<R> & s)
   const R sr = rmax<R>(ul, ur) + rmax<R>(cfastl, cfastr);
   const R rcl = rl * (ul - sl);
   const R rcr = rr * (sr - ur);
-  const R ustar = (rcr * ur + rcl * ul + (ptotl - ptotr)) / (rcr + rcl);
-  const R ptotstar = (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) / (rcr + rcl);
+  const R irc = recip<R>(rcr + rcl);
+  const R ustar = qdiv<R>(rcr * ur + rcl * ul + (ptotl - ptotr), rcr + rcl, irc);
+  const R ptotstar = qdiv<R>(rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur), rcr + rcl, irc);
 
-  const R rstarl = rl * (sl - ul) / (sl - ustar);
+  const R isl = recip<R>(sl - ustar);
+  const R rstarl = qdiv<R>(rl * (sl - ul), sl - ustar, isl);
   R       estar = rl * (sl - ul) * (sl - ustar) - a * a;
   const R el = rl * (sl - ul) * (sl - ul) - a * a;
   R       vstarl, wstarl, bstarl, cstarl;
@@ -371,19 +412,31 @@ riemann_hlld(R * qL, R * qR, R * flux, const Phys<R> & s)
   }
   else
   {
-    vstarl = vl - a * bl * (ustar - ul) / estar;
-    bstarl = bl * el / estar;
-    wstarl = wl - a * cl * (ustar - ul) / estar;
-    cstarl = cl * el / estar;
+    const R ie = recip<R>(estar);
+    vstarl = vl - qdiv<R>(a * bl * (ustar - ul), estar, ie);
+    bstarl = qdiv<R>(bl * el, estar, ie);
+    wstarl = wl - qdiv<R>(a * cl * (ustar - ul), estar, ie);
+    cstarl = qdiv<R>(cl * el, estar, ie);
   }
   const R vdotbstarl = ustar * a + vstarl * bstarl + wstarl * cstarl;
   const R etotstarl =
-    ((sl - ul) * etotl - ptotl * ul + ptotstar * ustar + a * (vdotbl - vdotbstarl)) / (sl - ustar);
-  const R sqrrstarl = dsqrt<R>(rstarl);
-  const R calfvenl = rabs<R>(a) / sqrrstarl;
+    qdiv<R>((sl - ul) * etotl - ptotl * ul + ptotstar * ustar + a * (vdotbl - vdotbstarl), sl - ustar, isl);
+  R sqrrstarl, calfvenl;
+  if constexpr (std::is_same<R, float>::value)
+  {
+    const float rs = rsqrtf(rstarl);
+    sqrrstarl = rstarl * rs;
+    calfvenl = rabs<R>(a) * rs;
+  }
+  else
+  {
+    sqrrstarl = dsqrt<R>(rstarl);
+    calfvenl = rabs<R>(a) / sqrrstarl;
+  }
   const R sal = ustar - calfvenl;
 
-  const R rstarr = rr * (sr - ur) / (sr - ustar);
+  const R isr = recip<R>(sr - ustar);
+  const R rstarr = qdiv<R>(rr * (sr - ur), sr - ustar, isr);
   estar = rr * (sr - ur) * (sr - ustar) - a * a;
   const R er = rr * (sr - ur) * (sr - ur) - a * a;
   R       vstarr, wstarr, bstarr, cstarr;
@@ -393,28 +446,40 @@ riemann_hlld(R * qL, R * qR, R * flux, const Phys<R> & s)
   }
   else
   {
-    vstarr = vr - a * br * (ustar - ur) / estar;
-    bstarr = br * er / estar;
-    wstarr = wr - a * cr * (ustar - ur) / estar;
-    cstarr = cr * er / estar;
+    const R ie = recip<R>(estar);
+    vstarr = vr - qdiv<R>(a * br * (ustar - ur), estar, ie);
+    bstarr = qdiv<R>(br * er, estar, ie);
+    wstarr = wr - qdiv<R>(a * cr * (ustar - ur), estar, ie);
+    cstarr = qdiv<R>(cr * er, estar, ie);
   }
   const R vdotbstarr = ustar * a + vstarr * bstarr + wstarr * cstarr;
   const R etotstarr =
-    ((sr - ur) * etotr - ptotr * ur + ptotstar * ustar + a * (vdotbr - vdotbstarr)) / (sr - ustar);
-  const R sqrrstarr = dsqrt<R>(rstarr);
-  const R calfvenr = rabs<R>(a) / sqrrstarr;
+    qdiv<R>((sr - ur) * etotr - ptotr * ur + ptotstar * ustar + a * (vdotbr - vdotbstarr), sr - ustar, isr);
+  R sqrrstarr, calfvenr;
+  if constexpr (std::is_same<R, float>::value)
+  {
+    const float rs = rsqrtf(rstarr);
+    sqrrstarr = rstarr * rs;
+    calfvenr = rabs<R>(a) * rs;
+  }
+  else
+  {
+    sqrrstarr = dsqrt<R>(rstarr);
+    calfvenr = rabs<R>(a) / sqrrstarr;
+  }
   const R sar = ustar + calfvenr;
 
+  const R isq = recip<R>(sqrrstarl + sqrrstarr);
   const R vstarstar =
-    (sqrrstarl * vstarl + sqrrstarr * vstarr + sgnm * (bstarr - bstarl)) / (sqrrstarl + sqrrstarr);
+    qdiv<R>(sqrrstarl * vstarl + sqrrstarr * vstarr + sgnm * (bstarr - bstarl), sqrrstarl + sqrrstarr, isq);
   const R wstarstar =
-    (sqrrstarl * wstarl + sqrrstarr * wstarr + sgnm * (cstarr - cstarl)) / (sqrrstarl + sqrrstarr);
+    qdiv<R>(sqrrstarl * wstarl + sqrrstarr * wstarr + sgnm * (cstarr - cstarl), sqrrstarl + sqrrstarr, isq);
   const R bstarstar =
-    (sqrrstarl * bstarr + sqrrstarr * bstarl + sgnm * sqrrstarl * sqrrstarr * (vstarr - vstarl)) /
-    (sqrrstarl + sqrrstarr);
+    qdiv<R>(sqrrstarl * bstarr + sqrrstarr * bstarl + sgnm * sqrrstarl * sqrrstarr * (vstarr - vstarl),
+            sqrrstarl + sqrrstarr, isq);
   const R cstarstar =
-    (sqrrstarl * cstarr + sqrrstarr * cstarl + sgnm * sqrrstarl * sqrrstarr * (wstarr - wstarl)) /
-    (sqrrstarl + sqrrstarr);
+    qdiv<R>(sqrrstarl * cstarr + sqrrstarr * cstarl + sgnm * sqrrstarl * sqrrstarr * (wstarr - wstarl),
+            sqrrstarl + sqrrstarr, isq);
   const R vdotbstarstar = ustar * a + vstarstar * bstarstar + wstarstar * cstarstar;
   const R etotstarstarl = etotstarl - sgnm * sqrrstarl * (vdotbstarl - vdotbstarstar);
   const R etotstarstarr = etotstarr + sgnm * sqrrstarr * (vdotbstarr - vdotbstarstar);
@@ -565,10 +630,11 @@ edge_emf(const R (*qe)[8], const Phys<R> & s)
 
   // find_speed_fast<IX>/<IY> for the 4 states (models/mhd_utils.h:93-122)
   auto fast = [&](R d, R p, R a, R b, R c, R bn) {
+    const R id = recip<R>(d);
     const R b2 = a * a + b * b + c * c;
-    const R c2 = s.gamma0 * p / d;
-    const R d2 = R(0.5) * (b2 / d + c2);
-    return dsqrt<R>(d2 + dsqrt<R>(d2 * d2 - c2 * bn * bn / d));
+    const R c2 = qdiv<R>(s.gamma0 * p, d, id);
+    const R d2 = R(0.5) * (qdiv<R>(b2, d, id) + c2);
+    return dsqrt<R>(d2 + dsqrt<R>(d2 * d2 - qdiv<R>(c2 * bn * bn, d, id)));
   };
   const R cFastLLx = fast(rLL, pLL, aLL, bLL, cLL, aLL);
   const R cFastLRx = fast(rLR, pLR, aLR, bLR, cLR, aLR);
@@ -605,60 +671,66 @@ edge_emf(const R (*qe)[8], const Phys<R> & s)
     (rcLLy * vLL + rcLRy * vLR + rcRLy * vRL + rcRRy * vRR + (PtotLL - PtotLR + PtotRL - PtotRR)) /
     (rcLLy + rcLRy + rcRLy + rcRRy);
 
-  const R rstarLLx = rLL * (SL - uLL) / (SL - ustar);
-  const R BstarLL = bLL * (SL - uLL) / (SL - ustar);
-  const R rstarLLy = rLL * (SB - vLL) / (SB - vstar);
-  const R AstarLL = aLL * (SB - vLL) / (SB - vstar);
-  const R rstarLL = rLL * (SL - uLL) / (SL - ustar) * (SB - vLL) / (SB - vstar);
+  // shared divisors of the star states
+  const R dLu = SL - ustar, dRu = SR - ustar, dBv = SB - vstar, dTv = ST - vstar;
+  const R iLu = recip<R>(dLu), iRu = recip<R>(dRu), iBv = recip<R>(dBv), iTv = recip<R>(dTv);
+
+  const R rstarLLx = qdiv<R>(rLL * (SL - uLL), dLu, iLu);
+  const R BstarLL = qdiv<R>(bLL * (SL - uLL), dLu, iLu);
+  const R rstarLLy = qdiv<R>(rLL * (SB - vLL), dBv, iBv);
+  const R AstarLL = qdiv<R>(aLL * (SB - vLL), dBv, iBv);
+  const R rstarLL = qdiv<R>(qdiv<R>(rLL * (SL - uLL), dLu, iLu) * (SB - vLL), dBv, iBv);
   const R EstarLLx = ustar * BstarLL - vLL * aLL;
   const R EstarLLy = uLL * bLL - vstar * AstarLL;
   const R EstarLL = ustar * BstarLL - vstar * AstarLL;
 
-  const R rstarLRx = rLR * (SL - uLR) / (SL - ustar);
-  const R BstarLR = bLR * (SL - uLR) / (SL - ustar);
-  const R rstarLRy = rLR * (ST - vLR) / (ST - vstar);
-  const R AstarLR = aLR * (ST - vLR) / (ST - vstar);
-  const R rstarLR = rLR * (SL - uLR) / (SL - ustar) * (ST - vLR) / (ST - vstar);
+  const R rstarLRx = qdiv<R>(rLR * (SL - uLR), dLu, iLu);
+  const R BstarLR = qdiv<R>(bLR * (SL - uLR), dLu, iLu);
+  const R rstarLRy = qdiv<R>(rLR * (ST - vLR), dTv, iTv);
+  const R AstarLR = qdiv<R>(aLR * (ST - vLR), dTv, iTv);
+  const R rstarLR = qdiv<R>(qdiv<R>(rLR * (SL - uLR), dLu, iLu) * (ST - vLR), dTv, iTv);
   const R EstarLRx = ustar * BstarLR - vLR * aLR;
   const R EstarLRy = uLR * bLR - vstar * AstarLR;
   const R EstarLR = ustar * BstarLR - vstar * AstarLR;
 
-  const R rstarRLx = rRL * (SR - uRL) / (SR - ustar);
-  const R BstarRL = bRL * (SR - uRL) / (SR - ustar);
-  const R rstarRLy = rRL * (SB - vRL) / (SB - vstar);
-  const R AstarRL = aRL * (SB - vRL) / (SB - vstar);
-  const R rstarRL = rRL * (SR - uRL) / (SR - ustar) * (SB - vRL) / (SB - vstar);
+  const R rstarRLx = qdiv<R>(rRL * (SR - uRL), dRu, iRu);
+  const R BstarRL = qdiv<R>(bRL * (SR - uRL), dRu, iRu);
+  const R rstarRLy = qdiv<R>(rRL * (SB - vRL), dBv, iBv);
+  const R AstarRL = qdiv<R>(aRL * (SB - vRL), dBv, iBv);
+  const R rstarRL = qdiv<R>(qdiv<R>(rRL * (SR - uRL), dRu, iRu) * (SB - vRL), dBv, iBv);
   const R EstarRLx = ustar * BstarRL - vRL * aRL;
   const R EstarRLy = uRL * bRL - vstar * AstarRL;
   const R EstarRL = ustar * BstarRL - vstar * AstarRL;
 
-  const R rstarRRx = rRR * (SR - uRR) / (SR - ustar);
-  const R BstarRR = bRR * (SR - uRR) / (SR - ustar);
-  const R rstarRRy = rRR * (ST - vRR) / (ST - vstar);
-  const R AstarRR = aRR * (ST - vRR) / (ST - vstar);
-  const R rstarRR = rRR * (SR - uRR) / (SR - ustar) * (ST - vRR) / (ST - vstar);
+  const R rstarRRx = qdiv<R>(rRR * (SR - uRR), dRu, iRu);
+  const R BstarRR = qdiv<R>(bRR * (SR - uRR), dRu, iRu);
+  const R rstarRRy = qdiv<R>(rRR * (ST - vRR), dTv, iTv);
+  const R AstarRR = qdiv<R>(aRR * (ST - vRR), dTv, iTv);
+  const R rstarRR = qdiv<R>(qdiv<R>(rRR * (SR - uRR), dRu, iRu) * (ST - vRR), dTv, iTv);
   const R EstarRRx = ustar * BstarRR - vRR * aRR;
   const R EstarRRy = uRR * bRR - vstar * AstarRR;
   const R EstarRR = ustar * BstarRR - vstar * AstarRR;
 
-  const R calfvenL = max5<R>(rabs<R>(aLR) / dsqrt<R>(rstarLRx), rabs<R>(AstarLR) / dsqrt<R>(rstarLR),
-                             rabs<R>(aLL) / dsqrt<R>(rstarLLx), rabs<R>(AstarLL) / dsqrt<R>(rstarLL), s.smallc);
-  const R calfvenR = max5<R>(rabs<R>(aRR) / dsqrt<R>(rstarRRx), rabs<R>(AstarRR) / dsqrt<R>(rstarRR),
-                             rabs<R>(aRL) / dsqrt<R>(rstarRLx), rabs<R>(AstarRL) / dsqrt<R>(rstarRL), s.smallc);
-  const R calfvenB = max5<R>(rabs<R>(bLL) / dsqrt<R>(rstarLLy), rabs<R>(BstarLL) / dsqrt<R>(rstarLL),
-                             rabs<R>(bRL) / dsqrt<R>(rstarRLy), rabs<R>(BstarRL) / dsqrt<R>(rstarRL), s.smallc);
-  const R calfvenT = max5<R>(rabs<R>(bLR) / dsqrt<R>(rstarLRy), rabs<R>(BstarLR) / dsqrt<R>(rstarLR),
-                             rabs<R>(bRR) / dsqrt<R>(rstarRRy), rabs<R>(BstarRR) / dsqrt<R>(rstarRR), s.smallc);
+  const R calfvenL = max5<R>(div_sqrt<R>(rabs<R>(aLR), rstarLRx), div_sqrt<R>(rabs<R>(AstarLR), rstarLR),
+                             div_sqrt<R>(rabs<R>(aLL), rstarLLx), div_sqrt<R>(rabs<R>(AstarLL), rstarLL), s.smallc);
+  const R calfvenR = max5<R>(div_sqrt<R>(rabs<R>(aRR), rstarRRx), div_sqrt<R>(rabs<R>(AstarRR), rstarRR),
+                             div_sqrt<R>(rabs<R>(aRL), rstarRLx), div_sqrt<R>(rabs<R>(AstarRL), rstarRL), s.smallc);
+  const R calfvenB = max5<R>(div_sqrt<R>(rabs<R>(bLL), rstarLLy), div_sqrt<R>(rabs<R>(BstarLL), rstarLL),
+                             div_sqrt<R>(rabs<R>(bRL), rstarRLy), div_sqrt<R>(rabs<R>(BstarRL), rstarRL), s.smallc);
+  const R calfvenT = max5<R>(div_sqrt<R>(rabs<R>(bLR), rstarLRy), div_sqrt<R>(rabs<R>(BstarLR), rstarLR),
+                             div_sqrt<R>(rabs<R>(bRR), rstarRRy), div_sqrt<R>(rabs<R>(BstarRR), rstarRR), s.smallc);
 
   const R SAL = rmin<R>(ustar - calfvenL, R(0));
   const R SAR = rmax<R>(ustar + calfvenR, R(0));
   const R SAB = rmin<R>(vstar - calfvenB, R(0));
   const R SAT = rmax<R>(vstar + calfvenT, R(0));
 
-  const R AstarT = (SAR * AstarRR - SAL * AstarLR) / (SAR - SAL);
-  const R AstarB = (SAR * AstarRL - SAL * AstarLL) / (SAR - SAL);
-  const R BstarR = (SAT * BstarRR - SAB * BstarRL) / (SAT - SAB);
-  const R BstarL = (SAT * BstarLR - SAB * BstarLL) / (SAT - SAB);
+  const R dRL = SAR - SAL, dTB = SAT - SAB;
+  const R iRL = recip<R>(dRL), iTB = recip<R>(dTB);
+  const R AstarT = qdiv<R>(SAR * AstarRR - SAL * AstarLR, dRL, iRL);
+  const R AstarB = qdiv<R>(SAR * AstarRL - SAL * AstarLL, dRL, iRL);
+  const R BstarR = qdiv<R>(SAT * BstarRR - SAB * BstarRL, dTB, iTB);
+  const R BstarL = qdiv<R>(SAT * BstarLR - SAB * BstarLL, dTB, iTB);
 
   R       E = 0, tmpE = 0;
   const R SB_pos = (1 + rcopysign<R>(R(1), SB)) / 2, SB_neg = 1 - SB_pos;
@@ -666,23 +738,24 @@ edge_emf(const R (*qe)[8], const Phys<R> & s)
   const R SL_pos = (1 + rcopysign<R>(R(1), SL)) / 2, SL_neg = 1 - SL_pos;
   const R SR_pos = (1 + rcopysign<R>(R(1), SR)) / 2, SR_neg = 1 - SR_pos;
 
-  tmpE = (SAL * SAB * EstarRR - SAL * SAT * EstarRL - SAR * SAB * EstarLR + SAR * SAT * EstarLL) /
-           (SAR - SAL) / (SAT - SAB) -
-         SAT * SAB / (SAT - SAB) * (AstarT - AstarB) + SAR * SAL / (SAR - SAL) * (BstarR - BstarL);
+  tmpE = qdiv<R>(qdiv<R>(SAL * SAB * EstarRR - SAL * SAT * EstarRL - SAR * SAB * EstarLR + SAR * SAT * EstarLL, dRL,
+                         iRL),
+                 dTB, iTB) -
+         qdiv<R>(SAT * SAB, dTB, iTB) * (AstarT - AstarB) + qdiv<R>(SAR * SAL, dRL, iRL) * (BstarR - BstarL);
   E += (SB_neg * ST_pos * SL_neg * SR_pos) * tmpE;
 
-  tmpE = (SAR * EstarLLx - SAL * EstarRLx + SAR * SAL * (bRL - bLL)) / (SAR - SAL);
+  tmpE = qdiv<R>(SAR * EstarLLx - SAL * EstarRLx + SAR * SAL * (bRL - bLL), dRL, iRL);
   tmpE = SL_pos * ELL + SL_neg * SR_neg * ERL + SL_neg * SR_pos * tmpE;
   E += SB_pos * tmpE;
 
-  tmpE = (SAR * EstarLRx - SAL * EstarRRx + SAR * SAL * (bRR - bLR)) / (SAR - SAL);
+  tmpE = qdiv<R>(SAR * EstarLRx - SAL * EstarRRx + SAR * SAL * (bRR - bLR), dRL, iRL);
   tmpE = SL_pos * ELR + SL_neg * SR_neg * ERR + SL_neg * SR_pos * tmpE;
   E += (SB_neg * ST_neg) * tmpE;
 
-  tmpE = (SAT * EstarLLy - SAB * EstarLRy - SAT * SAB * (aLR - aLL)) / (SAT - SAB);
+  tmpE = qdiv<R>(SAT * EstarLLy - SAB * EstarLRy - SAT * SAB * (aLR - aLL), dTB, iTB);
   E += (SB_neg * ST_pos * SL_pos) * tmpE;
 
-  tmpE = (SAT * EstarRLy - SAB * EstarRRy - SAT * SAB * (aRR - aRL)) / (SAT - SAB);
+  tmpE = qdiv<R>(SAT * EstarRLy - SAB * EstarRRy - SAT * SAB * (aRR - aRL), dTB, iTB);
   E += (SB_neg * ST_pos * SL_neg * SR_neg) * tmpE;
 
   return E;
