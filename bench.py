@@ -6,8 +6,9 @@ roofline of the fused step kernel, an end-to-end host-buffer number and the CPU 
 
 A step is one solver iteration (CFL reduction + do_time_step) over the whole 256^3 mesh. Inputs
 (U, B: 2.2 GB in FP64) are far larger than L2 (129 MB), so no L2 flush is needed between steps.
-Under torchrun each rank runs an independent replica of the workload (replicas only; the driver
-reports the aggregate). Prints one JSON line on rank 0.
+Under torchrun each rank runs an independent replica of the workload (replicas only): the timed
+duration is the max over ranks and the value the cell-updates of all ranks over it. Prints one JSON
+line on rank 0.
 """
 from __future__ import annotations
 
@@ -100,6 +101,22 @@ class ClockSampler:
                 continue
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def max_over_ranks(ms, dist, device):
+    """The timed duration of the slowest rank, on every rank (ms itself without a process group)."""
+    if dist is None:
+        return ms
+    import torch
+
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(cells_per_rank, steps, world, ms):
+    """Cell-updates per second of all ranks together over the max-over-ranks duration ms."""
+    return world * cells_per_rank * steps / (ms * 1e-3)
 
 
 def make_workload(side_blocks=8, block=32, seed=12345):
@@ -217,12 +234,8 @@ def main():
     if dist:
         dist.barrier()
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * cells * args.steps / (ms * 1e-3)
+    ms = max_over_ranks(e0.elapsed_time(e1), dist, "cuda")
+    value = whole_job_rate(cells, args.steps, world, ms)
 
     # ---- dominant kernel: the fused step, timed alone with CUDA events on its stream ----------
     nk = 20

@@ -1,5 +1,5 @@
 // C ABI of the GB300 MHD stage (declared in include/gmhd.h): context, mesh tables, the step,
-// the CFL reduction, the outside-block fill and a graph-captured multi-step driver.
+// the CFL reduction, the outside-block fill and a graph-captured multi-step loop.
 #include <cuda_runtime.h>
 
 #include <algorithm>

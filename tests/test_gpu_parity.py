@@ -1,9 +1,8 @@
 """GPU parity: the CUDA path, called through the C ABI (libgmhd.so), against the FP64 oracle.
 
 FP64 path: the oracle restates the reference in FP64 with its operand order; the kernel is built
-without FMA contraction, so results are expected to be identical. The bar written here is the
-spec tolerance, 1e-12 relative per field; the test also records whether they are
-bit-identical. Mixed path: L1(rho) <= 1e-6 relative to FP64 and max|div B| <= 1e-12.
+without FMA contraction, so results are expected to be identical. The bar written here is
+1e-12 relative per field; the test also records whether they are bit-identical. Mixed path: L1(rho) <= 1e-6 relative to FP64 and max|div B| <= 1e-12.
 """
 import numpy as np
 import pytest
