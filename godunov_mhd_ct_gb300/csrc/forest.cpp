@@ -344,10 +344,33 @@ build(const Forest & f, const KeyTable & leaves, gmhd_forest & out)
   const uint64_t ntrees = (uint64_t)f.bricks[0] * f.bricks[1] * f.bricks[2];
   if (3 * max_level + 64 - __builtin_clzll(ntrees | 1) <= 64)
   {
-    // one 64-bit sort key: tree id above the Morton bits
+    // one 64-bit sort key: tree id above the Morton bits; least-significant-digit radix sort over
+    // the bits in use, 11 bits per pass (keys are distinct, so stability only orders the passes)
+    uint64_t top = 0;
     for (Ord & o : ord)
+    {
       o.morton |= o.tree << (3 * max_level);
-    std::sort(ord.begin(), ord.end(), [](const Ord & p, const Ord & q) { return p.morton < q.morton; });
+      top |= o.morton;
+    }
+    const int        nbits = top ? 64 - __builtin_clzll(top) : 1;
+    std::vector<Ord> tmp(ord.size());
+    std::vector<uint32_t> cnt(1u << 11);
+    for (int shift = 0; shift < nbits; shift += 11)
+    {
+      std::fill(cnt.begin(), cnt.end(), 0u);
+      for (const Ord & o : ord)
+        ++cnt[(o.morton >> shift) & 0x7ff];
+      uint32_t sum = 0;
+      for (uint32_t & c : cnt)
+      {
+        const uint32_t c0 = c;
+        c = sum;
+        sum += c0;
+      }
+      for (const Ord & o : ord)
+        tmp[cnt[(o.morton >> shift) & 0x7ff]++] = o;
+      ord.swap(tmp);
+    }
   }
   else
     std::sort(ord.begin(), ord.end(), [](const Ord & p, const Ord & q) {
@@ -370,6 +393,13 @@ build(const Forest & f, const KeyTable & leaves, gmhd_forest & out)
   for (int b = 0; b < n_owned; ++b)
   {
     const Key k = out.owned[b];
+    // only a leaf on a non-periodic border has outside neighbours
+    const int kc[3] = {k.x, k.y, k.z};
+    bool      border = false;
+    for (int d = 0; d < f.dim; ++d)
+      border = border || (!f.per[d] && (kc[d] == 0 || kc[d] == f.ext(k.L, d) - 1));
+    if (!border)
+      continue;
     for (int o = 0; o < f.noffs; ++o)
     {
       int c[3] = {k.x + f.offs[o][0], k.y + f.offs[o][1], k.z + f.offs[o][2]};
