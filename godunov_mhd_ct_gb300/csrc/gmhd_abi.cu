@@ -87,6 +87,21 @@ struct gmhd_ctx
   // gmhd_refine_flags scratch
   double * d_rf_q = nullptr;
   int8_t * d_rf_flags = nullptr;
+  // gmhd_set_mesh uploads: recorded, then staged through one page-locked buffer (kept, grown as
+  // needed) and issued asynchronously on own_stream, which set_mesh waits for before it returns
+  struct Upload
+  {
+    void *       dst;
+    const void * src; // null: a memset of `fill`
+    size_t       bytes;
+    int          fill;
+  };
+  std::vector<Upload> uploads;
+  char *              h_stage = nullptr;
+  size_t              h_stage_cap = 0;
+  // host tables of the coarse/fine setup (kept so that their storage outlives the upload)
+  std::vector<int8_t>  h_kind;
+  std::vector<int32_t> h_knbr, h_vmap, h_list1, h_list2, h_flux_slot, h_emf_slot;
 };
 
 namespace
@@ -98,6 +113,63 @@ cuda_fail(gmhd_ctx * c, cudaError_t e)
     return GMHD_OK;
   c->last_cuda = (int)e;
   return GMHD_ERR_CUDA;
+}
+
+// record a host->device copy / a memset for the batched upload of gmhd_set_mesh
+void
+up_copy(gmhd_ctx * c, void * dst, const void * src, size_t bytes)
+{
+  if (bytes)
+    c->uploads.push_back(gmhd_ctx::Upload{dst, src, bytes, 0});
+}
+void
+up_set(gmhd_ctx * c, void * dst, int fill, size_t bytes)
+{
+  if (bytes)
+    c->uploads.push_back(gmhd_ctx::Upload{dst, nullptr, bytes, fill});
+}
+// stage the recorded copies through the page-locked buffer, issue everything on own_stream and wait
+int
+up_flush(gmhd_ctx * c)
+{
+  auto   rounded = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  size_t total = 0;
+  for (const gmhd_ctx::Upload & u : c->uploads)
+    if (u.src)
+      total += rounded(u.bytes);
+  cudaError_t e = cudaSuccess;
+  if (total > c->h_stage_cap)
+  {
+    if (c->h_stage)
+      cudaFreeHost(c->h_stage);
+    c->h_stage = nullptr;
+    c->h_stage_cap = 0;
+    const size_t cap = total + total / 4;
+    if ((e = cudaHostAlloc((void **)&c->h_stage, cap, cudaHostAllocDefault)) != cudaSuccess)
+    {
+      c->h_stage = nullptr;
+      c->uploads.clear();
+      return cuda_fail(c, e);
+    }
+    c->h_stage_cap = cap;
+  }
+  size_t off = 0;
+  for (const gmhd_ctx::Upload & u : c->uploads)
+  {
+    if (!u.src)
+      e = cudaMemsetAsync(u.dst, u.fill, u.bytes, c->own_stream);
+    else
+    {
+      std::memcpy(c->h_stage + off, u.src, u.bytes);
+      e = cudaMemcpyAsync(u.dst, c->h_stage + off, u.bytes, cudaMemcpyHostToDevice, c->own_stream);
+      off += rounded(u.bytes);
+    }
+    if (e != cudaSuccess)
+      break;
+  }
+  c->uploads.clear();
+  const cudaError_t e2 = cudaStreamSynchronize(c->own_stream);
+  return cuda_fail(c, e != cudaSuccess ? e : e2);
 }
 
 #define GMHD_CUDA(call)                                                                           \
@@ -608,11 +680,16 @@ setup_amr(gmhd_ctx * ctx, const gmhd_mesh * m, const std::vector<int8_t> & kind)
 {
   auto lev = [](int k) { return k == gmhd::RK_COARSER ? -1 : (k == gmhd::RK_FINER ? 1 : (k == gmhd::RK_MISSING ? -100 : 0)); };
   auto slot_of = [](const int * o) { return (o[2] + 1) * 9 + (o[1] + 1) * 3 + (o[0] + 1); };
-  const int            nown = m->n_owned;
-  std::vector<int32_t> knbr(m->neighbor, m->neighbor + (size_t)m->n_blocks * 27);
-  std::vector<int32_t> vmap;
-  std::vector<int32_t> flux_slot(nown, -1), emf_slot(nown, -1);
-  int                  n_flux = 0, n_emf = 0;
+  const int              nown = m->n_owned;
+  std::vector<int32_t> & knbr = ctx->h_knbr;
+  std::vector<int32_t> & vmap = ctx->h_vmap;
+  std::vector<int32_t> & flux_slot = ctx->h_flux_slot;
+  std::vector<int32_t> & emf_slot = ctx->h_emf_slot;
+  knbr.assign(m->neighbor, m->neighbor + (size_t)m->n_blocks * 27);
+  vmap.clear();
+  flux_slot.assign(nown, -1);
+  emf_slot.assign(nown, -1);
+  int n_flux = 0, n_emf = 0;
   for (int b = 0; b < nown; ++b)
   {
     bool coarser_face = false, coarser_any = false;
@@ -660,8 +737,11 @@ setup_amr(gmhd_ctx * ctx, const gmhd_mesh * m, const std::vector<int8_t> & kind)
   else
     gmhd::tile_shape_fp64(m->dim, ctx->bx, ctx->by, ctx->bz, ctx->p.viscosity_enabled != 0, T);
   const int            nt[3] = {ctx->bx / T[0], ctx->by / T[1], m->dim == 3 ? ctx->bz / T[2] : 1};
-  const int            tpb = nt[0] * nt[1] * nt[2];
-  std::vector<int32_t> list1, list2;
+  const int              tpb = nt[0] * nt[1] * nt[2];
+  std::vector<int32_t> & list1 = ctx->h_list1;
+  std::vector<int32_t> & list2 = ctx->h_list2;
+  list1.clear();
+  list2.clear();
   for (int b = 0; b < nown; ++b)
     for (int t = 0; t < tpb; ++t)
     {
@@ -709,32 +789,26 @@ setup_amr(gmhd_ctx * ctx, const gmhd_mesh * m, const std::vector<int8_t> & kind)
       (rc = dalloc(ctx, &ctx->d_flux_side, (size_t)n_flux * 2 * m->dim * nfv * ctx->flux_face_stride)) ||
       (rc = dalloc(ctx, &ctx->d_emf_side, (size_t)n_emf * ncomp * ne)))
     return rc;
-  GMHD_CUDA(cudaMemcpy(ctx->d_kind, kind.data(), kind.size(), cudaMemcpyHostToDevice));
+  up_copy(ctx, ctx->d_kind, kind.data(), kind.size());
   // the real table for the prepass; the kernel's table with the virtual ids
-  GMHD_CUDA(cudaMemcpy(ctx->d_nbr_real, m->neighbor, sizeof(int32_t) * knbr.size(), cudaMemcpyHostToDevice));
-  GMHD_CUDA(cudaMemcpy(ctx->d_neighbor, knbr.data(), sizeof(int32_t) * knbr.size(), cudaMemcpyHostToDevice));
-  if (nv)
-    GMHD_CUDA(cudaMemcpy(ctx->d_vmap, vmap.data(), sizeof(int32_t) * vmap.size(), cudaMemcpyHostToDevice));
-  if (!list1.empty())
-    GMHD_CUDA(cudaMemcpy(ctx->d_list1, list1.data(), sizeof(int32_t) * list1.size(), cudaMemcpyHostToDevice));
-  if (!list2.empty())
-    GMHD_CUDA(cudaMemcpy(ctx->d_list2, list2.data(), sizeof(int32_t) * list2.size(), cudaMemcpyHostToDevice));
-  GMHD_CUDA(cudaMemcpy(ctx->d_flux_slot, flux_slot.data(), sizeof(int32_t) * nown, cudaMemcpyHostToDevice));
-  GMHD_CUDA(cudaMemcpy(ctx->d_emf_slot, emf_slot.data(), sizeof(int32_t) * nown, cudaMemcpyHostToDevice));
+  up_copy(ctx, ctx->d_nbr_real, m->neighbor, sizeof(int32_t) * knbr.size());
+  up_copy(ctx, ctx->d_neighbor, knbr.data(), sizeof(int32_t) * knbr.size());
+  up_copy(ctx, ctx->d_vmap, vmap.data(), sizeof(int32_t) * vmap.size());
+  up_copy(ctx, ctx->d_list1, list1.data(), sizeof(int32_t) * list1.size());
+  up_copy(ctx, ctx->d_list2, list2.data(), sizeof(int32_t) * list2.size());
+  up_copy(ctx, ctx->d_flux_slot, flux_slot.data(), sizeof(int32_t) * nown);
+  up_copy(ctx, ctx->d_emf_slot, emf_slot.data(), sizeof(int32_t) * nown);
   if (m->coord)
-    GMHD_CUDA(cudaMemcpy(ctx->d_coord, m->coord, sizeof(int32_t) * m->n_blocks * 3, cudaMemcpyHostToDevice));
+    up_copy(ctx, ctx->d_coord, m->coord, sizeof(int32_t) * m->n_blocks * 3);
   else
-    GMHD_CUDA(cudaMemset(ctx->d_coord, 0, sizeof(int32_t) * m->n_blocks * 3));
+    up_set(ctx, ctx->d_coord, 0, sizeof(int32_t) * m->n_blocks * 3);
   if (m->fine_neighbor)
-    GMHD_CUDA(cudaMemcpy(ctx->d_fine, m->fine_neighbor, sizeof(int32_t) * m->n_blocks * 27 * 8, cudaMemcpyHostToDevice));
+    up_copy(ctx, ctx->d_fine, m->fine_neighbor, sizeof(int32_t) * m->n_blocks * 27 * 8);
   else
-    GMHD_CUDA(cudaMemset(ctx->d_fine, 0xff, sizeof(int32_t) * m->n_blocks * 27 * 8));
-  if (nv)
-  {
-    GMHD_CUDA(cudaMemset(ctx->d_Uv, 0, sizeof(double) * (size_t)nv * 5 * ctx->ncell));
-    GMHD_CUDA(cudaMemset(ctx->d_Bv, 0, sizeof(double) * (size_t)nv * ctx->nface));
-    GMHD_CUDA(cudaMemset(ctx->d_Bccv, 0, sizeof(double) * (size_t)nv * 3 * ctx->ncell));
-  }
+    up_set(ctx, ctx->d_fine, 0xff, sizeof(int32_t) * m->n_blocks * 27 * 8);
+  up_set(ctx, ctx->d_Uv, 0, sizeof(double) * (size_t)nv * 5 * ctx->ncell);
+  up_set(ctx, ctx->d_Bv, 0, sizeof(double) * (size_t)nv * ctx->nface);
+  up_set(ctx, ctx->d_Bccv, 0, sizeof(double) * (size_t)nv * 3 * ctx->ncell);
   ctx->amr = true;
   ctx->n_virtual = nv;
   ctx->n_list1 = (int)list1.size();
@@ -802,6 +876,8 @@ gmhd_destroy(gmhd_ctx * ctx)
   if (ctx->a_out)
     cudaStreamSynchronize(ctx->a_out);
   release_all(ctx);
+  if (ctx->h_stage)
+    cudaFreeHost(ctx->h_stage);
   if (ctx->d_health)
     cudaFree(ctx->d_health);
   if (ctx->own_stream)
@@ -843,13 +919,13 @@ gmhd_set_mesh(gmhd_ctx * ctx, const gmhd_mesh * m)
     if (m->problem && (m->problem[b] < 0 || m->problem[b] >= np))
       return GMHD_ERR_MESH;
   }
-  if (m->fine_neighbor)
-    for (int64_t i = 0; i < (int64_t)m->n_blocks * 27 * 8; ++i)
-      if (m->fine_neighbor[i] < -1 || m->fine_neighbor[i] >= m->n_owned)
-        return GMHD_ERR_MESH;
-  // kind of every neighbour region of the owned blocks (same level, one coarser, one finer, outside)
-  std::vector<int8_t> kind((size_t)m->n_owned * 27, (int8_t)gmhd::RK_MISSING);
-  bool                amr = false;
+  // kind of every neighbour region of the owned blocks (same level, one coarser, one finer, outside);
+  // the fine-neighbour entries are checked where they are read (regions without a same-level or
+  // coarser neighbour)
+  ctx->uploads.clear();
+  std::vector<int8_t> & kind = ctx->h_kind;
+  kind.assign((size_t)m->n_owned * 27, (int8_t)gmhd::RK_MISSING);
+  bool amr = false;
   for (int b = 0; b < m->n_owned; ++b)
     for (int s = 0; s < 27; ++s)
     {
@@ -889,6 +965,8 @@ gmhd_set_mesh(gmhd_ctx * ctx, const gmhd_mesh * m)
       for (int c = 0; c < (1 << m->dim); ++c)
       {
         const int id = m->fine_neighbor[((int64_t)b * 27 + s) * 8 + c];
+        if (id < -1 || id >= m->n_owned)
+          return GMHD_ERR_MESH;
         if (id < 0)
           continue;
         if (m->level[id] != m->level[b] + 1 || (m->problem && m->problem[id] != m->problem[b]))
@@ -935,26 +1013,29 @@ gmhd_set_mesh(gmhd_ctx * ctx, const gmhd_mesh * m)
       (rc = dalloc(ctx, &ctx->d_t, (size_t)np)) || (rc = dalloc(ctx, &ctx->d_tend, (size_t)np)) ||
       (rc = dalloc(ctx, &ctx->d_counter, 1)))
     return rc;
-  GMHD_CUDA(cudaMemcpy(ctx->d_neighbor, m->neighbor, sizeof(int32_t) * m->n_blocks * 27, cudaMemcpyHostToDevice));
-  GMHD_CUDA(cudaMemcpy(ctx->d_level, m->level, sizeof(int32_t) * m->n_blocks, cudaMemcpyHostToDevice));
+  up_copy(ctx, ctx->d_neighbor, m->neighbor, sizeof(int32_t) * m->n_blocks * 27);
+  up_copy(ctx, ctx->d_level, m->level, sizeof(int32_t) * m->n_blocks);
   if (m->problem)
   {
     if ((rc = dalloc(ctx, &ctx->d_problem, (size_t)m->n_blocks)))
       return rc;
-    GMHD_CUDA(cudaMemcpy(ctx->d_problem, m->problem, sizeof(int32_t) * m->n_blocks, cudaMemcpyHostToDevice));
+    up_copy(ctx, ctx->d_problem, m->problem, sizeof(int32_t) * m->n_blocks);
   }
   if (n_out > 0)
   {
     if ((rc = dalloc(ctx, &ctx->d_out_src, (size_t)n_out)) || (rc = dalloc(ctx, &ctx->d_out_normal, (size_t)3 * n_out)))
       return rc;
-    GMHD_CUDA(cudaMemcpy(ctx->d_out_src, m->outside_src, sizeof(int32_t) * n_out, cudaMemcpyHostToDevice));
-    GMHD_CUDA(cudaMemcpy(ctx->d_out_normal, m->outside_normal, sizeof(int32_t) * 3 * n_out, cudaMemcpyHostToDevice));
+    up_copy(ctx, ctx->d_out_src, m->outside_src, sizeof(int32_t) * n_out);
+    up_copy(ctx, ctx->d_out_normal, m->outside_normal, sizeof(int32_t) * 3 * n_out);
   }
   if (amr && (rc = setup_amr(ctx, m, kind)))
+  {
+    ctx->uploads.clear();
     return rc;
-  // the memsets above ran on the legacy stream: finish them before any step on another stream reads
-  // the tables
-  GMHD_CUDA(cudaStreamSynchronize(0));
+  }
+  // all tables in one staged batch on own_stream, complete before any step reads them
+  if ((rc = up_flush(ctx)))
+    return rc;
   ctx->has_mesh = true;
   ctx->mesh_version++;
   return GMHD_OK;

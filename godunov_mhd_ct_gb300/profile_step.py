@@ -100,7 +100,8 @@ def main():
         # warm-up: one AMR cycle outside the timed region (first use of the allocator and fill kernels)
         mesh, dU, dB = impl.regrid(dU, dB, lo, hi, **crit)
         torch.cuda.synchronize()
-        updates, done, t_regrid = 0, 0, 0.0
+        impl.regrid_seconds = [0.0] * 4
+        updates, done, t_regrid, cycles = 0, 0, 0.0, 0
         t0 = time.perf_counter()
         while done < args.repeat:
             n = min(args.regrid, args.repeat - done)
@@ -111,8 +112,12 @@ def main():
             t1 = time.perf_counter()
             mesh, dU, dB = impl.regrid(dU, dB, lo, hi, **crit)
             t_regrid += time.perf_counter() - t1
+            cycles += 1
         torch.cuda.synchronize()
         el = time.perf_counter() - t0
+        parts = ", ".join(f"{k} {1e3 * v / cycles:.3f} ms" for k, v in
+                          zip(("flags", "adapt", "remap", "set_mesh"), impl.regrid_seconds))
+        print(f"per cycle ({cycles}): {parts}; steps {1e3 * (el - t_regrid) / cycles:.3f} ms per {args.regrid} steps")
         print(f"{args.precision} {mesh.dim}D with an AMR cycle every {args.regrid} steps: {args.repeat} steps, "
               f"{updates / el / 1e9:.3f} G cell-updates/s, regrid {t_regrid / el * 100:.1f} % of the time, "
               f"final {mesh.n_owned} leaves, levels {np.bincount(mesh.level[: mesh.n_owned])[lo:]}")

@@ -153,12 +153,17 @@ class GodunovImplemGB300:
         """One AMR cycle: refinement flags on the device, mesh adaptation + 2:1 balance on the host
         (BlockMesh.adapt, p4est's part), remap of U and B on the device, new mesh tables
         (resize_auxiliary_data). Returns (new mesh, new U, new B); U, B stay valid until released."""
+        import time
+
         import torch
 
         if self.n_problems != 1:
             raise ValueError("regrid works on single-problem meshes")
+        t0 = time.perf_counter()
         flags = self.refine_flags(U, B, level_min=level_min, level_max=level_max, stream=stream, **criterion)
+        t1 = time.perf_counter()
         new_mesh, table = self.mesh.adapt(flags, level_min, level_max)
+        t2 = time.perf_counter()
         us, bs = new_mesh.state_shapes()
         Un = torch.zeros(us, dtype=torch.float64, device=U.device)
         Bn = torch.zeros(bs, dtype=torch.float64, device=U.device)
@@ -167,7 +172,13 @@ class GodunovImplemGB300:
         nat.check(self._lib.gmhd_remap(self.mesh.dim, bx, by, bz, self.mesh.n_blocks, new_mesh.n_owned,
                                        table.ctypes.data, _ptr(U), _ptr(B), _ptr(Un), _ptr(Bn), _stream_ptr(stream)),
                   "gmhd_remap")
+        t3 = time.perf_counter()
         self.resize_auxiliary_data(new_mesh, bc=self._bc)
+        t4 = time.perf_counter()
+        # host wall time per part of the cycle, accumulated: flags (incl. their device->host copy),
+        # adapt + balance + tables, remap enqueue, new mesh tables (waits for the remap)
+        self.regrid_seconds = [a + b for a, b in zip(getattr(self, "regrid_seconds", [0.0] * 4),
+                                                     (t1 - t0, t2 - t1, t3 - t2, t4 - t3))]
         return new_mesh, Un, Bn
 
     def last_status(self) -> int:
