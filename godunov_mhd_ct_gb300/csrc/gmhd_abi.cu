@@ -1226,6 +1226,8 @@ gmhd_step_host(gmhd_ctx * ctx, const double * U, double * U2, const double * B, 
     return GMHD_ERR_ARGUMENT;
   if (!ctx->has_mesh)
     return GMHD_ERR_MESH;
+  if (ctx->n_blocks == 0)
+    return GMHD_OK; // nothing to copy or step
   const size_t nu = (size_t)ctx->n_blocks * 5 * ctx->ncell;
   const size_t nb = (size_t)ctx->n_blocks * ctx->nface;
   int          rc;
@@ -1257,6 +1259,8 @@ gmhd_step_host_async(gmhd_ctx * ctx, const double * U, double * U2, const double
     return GMHD_ERR_MESH;
   if (!(dt >= 0.0))
     return GMHD_ERR_ARGUMENT;
+  if (ctx->n_blocks == 0)
+    return GMHD_OK; // nothing to copy or step
   const size_t nu = (size_t)ctx->n_blocks * 5 * ctx->ncell;
   const size_t nb = (size_t)ctx->n_blocks * ctx->nface;
   int          rc;

@@ -75,7 +75,9 @@ class BlockMesh:
 
     @property
     def is_amr(self) -> bool:
-        return self.fine_neighbor is not None or bool(np.any(self.level[: self.n_owned] != self.level[0]))
+        if self.fine_neighbor is not None:
+            return True
+        return self.n_owned > 0 and bool(np.any(self.level[: self.n_owned] != self.level[0]))
 
     def domain_length(self, d: int) -> float:
         """Extent of the domain along axis d (``grid`` counts blocks at the finest level)."""

@@ -179,3 +179,24 @@ def test_step_host_async_matches_step(oracle_lib):
     for hU2, hB2 in outs:
         assert np.array_equal(hU2.numpy()[:n], ref_U[:n])
         assert np.array_equal(hB2.numpy()[:n], ref_B[:n])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_empty_mesh_is_a_no_op(precision):
+    """A mesh without blocks (a rank that owns no leaves): every call succeeds and touches nothing."""
+    mesh = BlockMesh(dim=3, block=(8, 8, 8), level=np.zeros(0, np.int32), neighbor=np.zeros((0, 27), np.int32),
+                     coords=np.zeros((0, 3), np.int64), n_owned=0, grid=(1, 1, 1), periodic=(True, True, True))
+    assert not mesh.is_amr
+    impl = GodunovImplemGB300(settings(), mesh, precision=precision)
+    sentinel = torch.full((16,), 7.0, dtype=torch.float64, device="cuda")
+    U, U2, B, B2 = (sentinel.clone() for _ in range(4))
+    impl.do_time_step(U, U2, B, B2, 1e-3)
+    impl.fill_outside(U, B)
+    assert impl.compute_inv_dt(U, B) == 0.0
+    torch.cuda.synchronize()
+    for x in (U, U2, B, B2):
+        assert torch.equal(x, sentinel)
+    assert impl.last_status() == 0
+    hU2, hB2 = impl.step_host(np.zeros(0), np.zeros(0), 1e-3)
+    assert hU2.size == 0 and hB2.size == 0
+    impl.close()
