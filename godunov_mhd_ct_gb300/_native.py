@@ -80,6 +80,9 @@ def lib():
     L.gmhd_advance.argtypes = [vp, vp, vp, vp, vp, ctypes.c_int32, dp, dp, dp, ctypes.c_int32, vp]
     L.gmhd_step_host.argtypes = [vp, vp, vp, vp, vp, ctypes.c_double, vp]
     L.gmhd_step_host_async.argtypes = [vp, vp, vp, vp, vp, ctypes.c_double, vp]
+    L.gmhd_autotune.argtypes = [vp, vp, vp, vp, vp, ctypes.c_double, ctypes.POINTER(ctypes.c_int32),
+                                ctypes.POINTER(ctypes.c_double), vp]
+    L.gmhd_set_tile.argtypes = [vp, ctypes.c_int32]
     L.gmhd_refine_flags.argtypes = [vp, vp, vp, ctypes.POINTER(GmhdRefineParams), vp, vp]
     L.gmhd_remap.argtypes = [ctypes.c_int32] * 6 + [vp] * 5 + [vp]
     L.gmhd_forest_build.restype = vp
@@ -112,7 +115,7 @@ def exported_symbols():
             "gmhd_fill_outside", "gmhd_advance", "gmhd_step_host", "gmhd_last_status", "gmhd_last_cuda_error",
             "gmhd_error_string", "gmhd_layout_check", "gmhd_inv_dt_noalloc", "gmhd_step_host_async",
             "gmhd_refine_flags", "gmhd_remap", "gmhd_forest_build", "gmhd_forest_sizes", "gmhd_forest_tables",
-            "gmhd_forest_destroy"]
+            "gmhd_forest_destroy", "gmhd_autotune", "gmhd_set_tile"]
 
 
 class MeshTables:

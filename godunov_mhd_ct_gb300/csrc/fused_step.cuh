@@ -47,6 +47,7 @@ struct StepArgs
   unsigned int *             health;            // OR of HEALTH_* flags
   int                        n_blocks;          // ids >= n_blocks in `neighbor` are virtual blocks
   Sources                    src;               // gravity / viscosity (viscous fluxes need C::VISC)
+  int                        tile;              // host dispatch: tile x extent asked for (0: largest that fits)
 
   // ---- coarse/fine meshes (all null / zero when no block has a neighbour at another level) ----
   // Neighbour regions at another level are presented to the gather as virtual same-level blocks

@@ -102,6 +102,9 @@ struct gmhd_ctx
   // host tables of the coarse/fine setup (kept so that their storage outlives the upload)
   std::vector<int8_t>  h_kind;
   std::vector<int32_t> h_knbr, h_vmap, h_list1, h_list2, h_flux_slot, h_emf_slot;
+  // tile x extent the step asks for (0: the largest configured tile that divides the block; set by
+  // gmhd_autotune, kept across meshes)
+  int tile = 0;
 };
 
 namespace
@@ -300,6 +303,7 @@ make_args(const gmhd_ctx * c, const double * U, double * U2, const double * B, d
   a.level = c->d_level;
   a.problem = c->d_problem;
   a.n_owned = c->n_owned;
+  a.tile = c->tile;
   a.bx = c->bx;
   a.by = c->by;
   a.bz = c->bz;
@@ -673,6 +677,73 @@ check_health(gmhd_ctx * ctx, cudaStream_t s, unsigned int * flags_out)
   return GMHD_OK;
 }
 
+// The two-pass tile lists of a coarse/fine mesh for the context's tile choice: pass 1 takes the tiles
+// without finer neighbours (and, marked ~id, the coarse-side stores of tiles that also border finer
+// blocks), pass 2 the tiles next to finer blocks. Host side only (ctx->h_list1, ctx->h_list2).
+void
+build_tile_lists(gmhd_ctx * ctx, int dim, const std::vector<int8_t> & kind)
+{
+  int T[3];
+  if (ctx->p.precision == GMHD_PRECISION_MIXED)
+    gmhd::tile_shape_mixed(dim, ctx->bx, ctx->by, ctx->bz, ctx->p.viscosity_enabled != 0, ctx->tile, T);
+  else
+    gmhd::tile_shape_fp64(dim, ctx->bx, ctx->by, ctx->bz, ctx->p.viscosity_enabled != 0, ctx->tile, T);
+  const int              nt[3] = {ctx->bx / T[0], ctx->by / T[1], dim == 3 ? ctx->bz / T[2] : 1};
+  const int              tpb = nt[0] * nt[1] * nt[2];
+  std::vector<int32_t> & list1 = ctx->h_list1;
+  std::vector<int32_t> & list2 = ctx->h_list2;
+  list1.clear();
+  list2.clear();
+  for (int b = 0; b < ctx->n_owned; ++b)
+    for (int t = 0; t < tpb; ++t)
+    {
+      const int tc[3] = {t % nt[0], (t / nt[0]) % nt[1], t / (nt[0] * nt[1])};
+      bool      fin = false, coa = false;
+      for (int s = 0; s < 27; ++s)
+      {
+        if (s == 13 || (dim == 2 && s / 9 != 1))
+          continue;
+        const int o[3] = {s % 3 - 1, (s / 3) % 3 - 1, s / 9 - 1};
+        bool      touch = true;
+        for (int d = 0; d < 3; ++d)
+          if (o[d] != 0 && tc[d] != (o[d] < 0 ? 0 : nt[d] - 1))
+            touch = false;
+        if (!touch)
+          continue;
+        fin = fin || kind[(size_t)b * 27 + s] == gmhd::RK_FINER;
+        coa = coa || kind[(size_t)b * 27 + s] == gmhd::RK_COARSER;
+      }
+      const int32_t id = b * tpb + t;
+      if (!fin)
+        list1.push_back(id);
+      else
+      {
+        if (coa)
+          list1.push_back(~id);
+        list2.push_back(id);
+      }
+    }
+}
+
+// Make `tile` the context's tile request; on a coarse/fine mesh rebuild and upload the tile lists for
+// it (the caller has made sure no step still reads them).
+int
+apply_tile(gmhd_ctx * ctx, int tile)
+{
+  ctx->tile = tile;
+  if (!ctx->has_mesh || !ctx->amr)
+    return GMHD_OK;
+  build_tile_lists(ctx, ctx->dim, ctx->h_kind);
+  int rc;
+  if ((rc = dalloc(ctx, &ctx->d_list1, ctx->h_list1.size())) || (rc = dalloc(ctx, &ctx->d_list2, ctx->h_list2.size())))
+    return rc;
+  up_copy(ctx, ctx->d_list1, ctx->h_list1.data(), sizeof(int32_t) * ctx->h_list1.size());
+  up_copy(ctx, ctx->d_list2, ctx->h_list2.data(), sizeof(int32_t) * ctx->h_list2.size());
+  ctx->n_list1 = (int)ctx->h_list1.size();
+  ctx->n_list2 = (int)ctx->h_list2.size();
+  return up_flush(ctx);
+}
+
 // Coarse/fine tables: virtual blocks for every neighbour region read through the ghost prepass,
 // the kernel's neighbour table pointing at them, fine-side data slots and the two tile lists.
 int
@@ -730,47 +801,7 @@ setup_amr(gmhd_ctx * ctx, const gmhd_mesh * m, const std::vector<int8_t> & kind)
     if (coarser_any)
       emf_slot[b] = n_emf++;
   }
-  // two-pass tile lists
-  int T[3];
-  if (ctx->p.precision == GMHD_PRECISION_MIXED)
-    gmhd::tile_shape_mixed(m->dim, ctx->bx, ctx->by, ctx->bz, ctx->p.viscosity_enabled != 0, T);
-  else
-    gmhd::tile_shape_fp64(m->dim, ctx->bx, ctx->by, ctx->bz, ctx->p.viscosity_enabled != 0, T);
-  const int            nt[3] = {ctx->bx / T[0], ctx->by / T[1], m->dim == 3 ? ctx->bz / T[2] : 1};
-  const int              tpb = nt[0] * nt[1] * nt[2];
-  std::vector<int32_t> & list1 = ctx->h_list1;
-  std::vector<int32_t> & list2 = ctx->h_list2;
-  list1.clear();
-  list2.clear();
-  for (int b = 0; b < nown; ++b)
-    for (int t = 0; t < tpb; ++t)
-    {
-      const int tc[3] = {t % nt[0], (t / nt[0]) % nt[1], t / (nt[0] * nt[1])};
-      bool      fin = false, coa = false;
-      for (int s = 0; s < 27; ++s)
-      {
-        if (s == 13 || (m->dim == 2 && s / 9 != 1))
-          continue;
-        const int o[3] = {s % 3 - 1, (s / 3) % 3 - 1, s / 9 - 1};
-        bool      touch = true;
-        for (int d = 0; d < 3; ++d)
-          if (o[d] != 0 && tc[d] != (o[d] < 0 ? 0 : nt[d] - 1))
-            touch = false;
-        if (!touch)
-          continue;
-        fin = fin || kind[(size_t)b * 27 + s] == gmhd::RK_FINER;
-        coa = coa || kind[(size_t)b * 27 + s] == gmhd::RK_COARSER;
-      }
-      const int32_t id = b * tpb + t;
-      if (!fin)
-        list1.push_back(id);
-      else
-      {
-        if (coa)
-          list1.push_back(~id);
-        list2.push_back(id);
-      }
-    }
+  build_tile_lists(ctx, m->dim, kind);
   const int     nv = (int)(vmap.size() / 2);
   const int     ncomp = m->dim == 3 ? 3 : 1;
   const int64_t ne = (int64_t)(ctx->bx + 1) * (ctx->by + 1) * (m->dim == 3 ? ctx->bz + 1 : 1);
@@ -780,8 +811,8 @@ setup_amr(gmhd_ctx * ctx, const gmhd_mesh * m, const std::vector<int8_t> & kind)
                                       : std::max(ctx->bx, ctx->by);
   int rc;
   if ((rc = dalloc(ctx, &ctx->d_kind, kind.size())) || (rc = dalloc(ctx, &ctx->d_nbr_real, knbr.size())) ||
-      (rc = dalloc(ctx, &ctx->d_vmap, vmap.size())) || (rc = dalloc(ctx, &ctx->d_list1, list1.size())) ||
-      (rc = dalloc(ctx, &ctx->d_list2, list2.size())) || (rc = dalloc(ctx, &ctx->d_flux_slot, (size_t)nown)) ||
+      (rc = dalloc(ctx, &ctx->d_vmap, vmap.size())) || (rc = dalloc(ctx, &ctx->d_list1, ctx->h_list1.size())) ||
+      (rc = dalloc(ctx, &ctx->d_list2, ctx->h_list2.size())) || (rc = dalloc(ctx, &ctx->d_flux_slot, (size_t)nown)) ||
       (rc = dalloc(ctx, &ctx->d_emf_slot, (size_t)nown)) || (rc = dalloc(ctx, &ctx->d_coord, (size_t)m->n_blocks * 3)) ||
       (rc = dalloc(ctx, &ctx->d_fine, (size_t)m->n_blocks * 27 * 8)) ||
       (rc = dalloc(ctx, &ctx->d_Uv, (size_t)nv * 5 * ctx->ncell)) || (rc = dalloc(ctx, &ctx->d_Bv, (size_t)nv * ctx->nface)) ||
@@ -794,8 +825,8 @@ setup_amr(gmhd_ctx * ctx, const gmhd_mesh * m, const std::vector<int8_t> & kind)
   up_copy(ctx, ctx->d_nbr_real, m->neighbor, sizeof(int32_t) * knbr.size());
   up_copy(ctx, ctx->d_neighbor, knbr.data(), sizeof(int32_t) * knbr.size());
   up_copy(ctx, ctx->d_vmap, vmap.data(), sizeof(int32_t) * vmap.size());
-  up_copy(ctx, ctx->d_list1, list1.data(), sizeof(int32_t) * list1.size());
-  up_copy(ctx, ctx->d_list2, list2.data(), sizeof(int32_t) * list2.size());
+  up_copy(ctx, ctx->d_list1, ctx->h_list1.data(), sizeof(int32_t) * ctx->h_list1.size());
+  up_copy(ctx, ctx->d_list2, ctx->h_list2.data(), sizeof(int32_t) * ctx->h_list2.size());
   up_copy(ctx, ctx->d_flux_slot, flux_slot.data(), sizeof(int32_t) * nown);
   up_copy(ctx, ctx->d_emf_slot, emf_slot.data(), sizeof(int32_t) * nown);
   if (m->coord)
@@ -811,8 +842,8 @@ setup_amr(gmhd_ctx * ctx, const gmhd_mesh * m, const std::vector<int8_t> & kind)
   up_set(ctx, ctx->d_Bccv, 0, sizeof(double) * (size_t)nv * 3 * ctx->ncell);
   ctx->amr = true;
   ctx->n_virtual = nv;
-  ctx->n_list1 = (int)list1.size();
-  ctx->n_list2 = (int)list2.size();
+  ctx->n_list1 = (int)ctx->h_list1.size();
+  ctx->n_list2 = (int)ctx->h_list2.size();
   return GMHD_OK;
 }
 
@@ -1063,6 +1094,96 @@ gmhd_step(gmhd_ctx * ctx, const double * U, double * U2, const double * B, doubl
   gmhd::StepArgs a = make_args(ctx, U, U2, B, B2);
   a.dt = dt;
   return launch_step(ctx, a, (cudaStream_t)stream);
+}
+
+int
+gmhd_set_tile(gmhd_ctx * ctx, int32_t tile)
+{
+  if (!ctx || tile < 0)
+    return GMHD_ERR_ARGUMENT;
+  GMHD_CUDA(cudaDeviceSynchronize());
+  const int rc = apply_tile(ctx, tile);
+  ctx->mesh_version++; // cached step graphs hold the previous kernels
+  return rc;
+}
+
+int
+gmhd_autotune(gmhd_ctx * ctx, const double * U, double * U2, const double * B, double * B2, double dt,
+              int32_t * tile_out, double * ms_out, void * stream)
+{
+  if (!ctx || !U || !U2 || !B || !B2)
+    return GMHD_ERR_ARGUMENT;
+  if (!ctx->has_mesh)
+    return GMHD_ERR_MESH;
+  if (!(dt >= 0.0) || misaligned(U) || misaligned(B))
+    return GMHD_ERR_ARGUMENT;
+  const size_t nu = sizeof(double) * (size_t)ctx->n_blocks * 5 * ctx->ncell;
+  const size_t nb = sizeof(double) * (size_t)ctx->n_blocks * ctx->nface;
+  if (overlaps(U, nu, U2, nu) || overlaps(B, nb, B2, nb) || overlaps(U2, nu, B, nb) || overlaps(B2, nb, U, nu))
+    return GMHD_ERR_ALIAS;
+  int       cand[3];
+  const bool visc = ctx->p.viscosity_enabled != 0;
+  const int n = ctx->p.precision == GMHD_PRECISION_MIXED
+                  ? gmhd::tile_candidates_mixed(ctx->dim, ctx->bx, ctx->by, ctx->bz, visc, cand)
+                  : gmhd::tile_candidates_fp64(ctx->dim, ctx->bx, ctx->by, ctx->bz, visc, cand);
+  if (n == 0)
+    return GMHD_ERR_ARGUMENT;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaEvent_t  e0 = nullptr, e1 = nullptr;
+  // no step may still read the tile lists that a candidate replaces
+  GMHD_CUDA(cudaDeviceSynchronize());
+  GMHD_CUDA(cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess)
+  {
+    cudaEventDestroy(e0);
+    return cuda_fail(ctx, cudaErrorMemoryAllocation);
+  }
+  const int  prev = ctx->tile;
+  int        best = cand[0], rc = GMHD_OK;
+  double     best_ms = 0.0;
+  auto       use_tile = [&](int tile) { return apply_tile(ctx, tile); };
+  // every candidate: two steps to warm up, then five timed with events on the stream
+  for (int i = 0; i < n && rc == GMHD_OK; ++i)
+  {
+    if ((rc = use_tile(cand[i])))
+      break;
+    gmhd::StepArgs a = make_args(ctx, U, U2, B, B2);
+    a.dt = dt;
+    for (int w = 0; w < 2 && rc == GMHD_OK; ++w)
+      rc = launch_step(ctx, a, s);
+    if (rc == GMHD_OK && (rc = cuda_fail(ctx, cudaEventRecord(e0, s))) == GMHD_OK)
+    {
+      for (int r = 0; r < 5 && rc == GMHD_OK; ++r)
+        rc = launch_step(ctx, a, s);
+    }
+    if (rc == GMHD_OK && (rc = cuda_fail(ctx, cudaEventRecord(e1, s))) == GMHD_OK &&
+        (rc = cuda_fail(ctx, cudaEventSynchronize(e1))) == GMHD_OK)
+    {
+      float ms = 0.0f;
+      if ((rc = cuda_fail(ctx, cudaEventElapsedTime(&ms, e0, e1))) == GMHD_OK && (i == 0 || ms / 5.0 < best_ms))
+      {
+        best = cand[i];
+        best_ms = ms / 5.0;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const cudaError_t es = cudaDeviceSynchronize();
+  if (rc == GMHD_OK && es != cudaSuccess)
+    rc = cuda_fail(ctx, es);
+  const int rc2 = use_tile(rc == GMHD_OK ? best : prev);
+  ctx->mesh_version++; // cached step graphs hold the previous kernels
+  if (rc == GMHD_OK)
+    rc = rc2;
+  if (rc == GMHD_OK)
+  {
+    if (tile_out)
+      *tile_out = best;
+    if (ms_out)
+      *ms_out = best_ms;
+  }
+  return rc;
 }
 
 int

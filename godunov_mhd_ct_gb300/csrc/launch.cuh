@@ -63,15 +63,29 @@ prepare_fused()
   return 0;
 }
 
-// Tile choice: the largest configured tile that divides the block. With a.src.viscosity the
-// viscous variants run (launch_step_*_visc).
+// Tile choice: a.tile when it is one of the configured tiles that divide the block (named by their
+// x extent), else the largest that does. With a.src.viscosity the viscous variants run
+// (launch_step_*_visc).
 int launch_step_fp64(const StepArgs & a, int dim, cudaStream_t stream);
 int launch_step_mixed(const StepArgs & a, int dim, cudaStream_t stream);
 int launch_step_fp64_visc(const StepArgs & a, int dim, cudaStream_t stream);
 int launch_step_mixed_visc(const StepArgs & a, int dim, cudaStream_t stream);
-// the tile extents launch_step_* uses for these block sizes
-void tile_shape_fp64(int dim, int bx, int by, int bz, bool visc, int * t);
-void tile_shape_mixed(int dim, int bx, int by, int bz, bool visc, int * t);
+// configured tiles (x extents, largest first) that divide these blocks; returns their count (<= 3)
+int tile_candidates_fp64(int dim, int bx, int by, int bz, bool visc, int * out);
+int tile_candidates_mixed(int dim, int bx, int by, int bz, bool visc, int * out);
+// the tile extents launch_step_* uses for these block sizes and request
+void tile_shape_fp64(int dim, int bx, int by, int bz, bool visc, int tile, int * t);
+void tile_shape_mixed(int dim, int bx, int by, int bz, bool visc, int tile, int * t);
+
+// the requested tile when it is a candidate, else the first (largest) candidate, 0 when none fits
+inline int
+pick_tile(const int * cand, int n, int req)
+{
+  for (int i = 0; i < n; ++i)
+    if (cand[i] == req)
+      return req;
+  return n > 0 ? cand[0] : 0;
+}
 int prepare_fp64();
 int prepare_mixed();
 int prepare_fp64_visc();

@@ -21,15 +21,17 @@ template <bool AMR>
 int
 launch_step_fp64_cfg(const StepArgs & a, int dim, cudaStream_t stream)
 {
+  int       cand[3];
+  const int x = pick_tile(cand, tile_candidates_fp64(dim, a.bx, a.by, a.bz, false, cand), a.tile);
   if (dim == 3)
   {
-    if (a.bx % 8 == 0 && a.by % 4 == 0 && a.bz % 4 == 0)
+    if (x == 8)
       return launch_fused<std::conditional_t<AMR, F64_3D_844_AMR, F64_3D_844>>(a, stream);
     return launch_fused<std::conditional_t<AMR, F64_3D_444_AMR, F64_3D_444>>(a, stream);
   }
-  if (a.bx % 16 == 0 && a.by % 16 == 0)
+  if (x == 16)
     return launch_fused<std::conditional_t<AMR, F64_2D_16_AMR, F64_2D_16>>(a, stream);
-  if (a.bx % 8 == 0 && a.by % 8 == 0)
+  if (x == 8)
     return launch_fused<std::conditional_t<AMR, F64_2D_8_AMR, F64_2D_8>>(a, stream);
   return launch_fused<std::conditional_t<AMR, F64_2D_4_AMR, F64_2D_4>>(a, stream);
 }
@@ -42,18 +44,38 @@ launch_step_fp64(const StepArgs & a, int dim, cudaStream_t stream)
   return a.kind ? launch_step_fp64_cfg<true>(a, dim, stream) : launch_step_fp64_cfg<false>(a, dim, stream);
 }
 
-void
-tile_shape_fp64(int dim, int bx, int by, int bz, bool /*visc: same tiles*/, int * t)
+int
+tile_candidates_fp64(int dim, int bx, int by, int bz, bool /*visc: same tiles*/, int * out)
 {
+  int n = 0;
   if (dim == 3)
   {
-    const bool big = bx % 8 == 0 && by % 4 == 0 && bz % 4 == 0;
-    t[0] = big ? 8 : 4;
+    // 8x4x4 tiles, then 4x4x4
+    if (bx % 8 == 0 && by % 4 == 0 && bz % 4 == 0)
+      out[n++] = 8;
+    if (bx % 4 == 0 && by % 4 == 0 && bz % 4 == 0)
+      out[n++] = 4;
+    return n;
+  }
+  for (int t : {16, 8, 4})
+    if (bx % t == 0 && by % t == 0)
+      out[n++] = t;
+  return n;
+}
+
+void
+tile_shape_fp64(int dim, int bx, int by, int bz, bool visc, int tile, int * t)
+{
+  int       cand[3];
+  const int x = pick_tile(cand, tile_candidates_fp64(dim, bx, by, bz, visc, cand), tile);
+  if (dim == 3)
+  {
+    t[0] = x == 8 ? 8 : 4;
     t[1] = 4;
     t[2] = 4;
     return;
   }
-  const int n = (bx % 16 == 0 && by % 16 == 0) ? 16 : ((bx % 8 == 0 && by % 8 == 0) ? 8 : 4);
+  const int n = x ? x : 4;
   t[0] = t[1] = n;
   t[2] = 1;
 }

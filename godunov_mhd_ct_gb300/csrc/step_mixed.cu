@@ -21,15 +21,17 @@ template <bool AMR>
 int
 launch_step_mixed_cfg(const StepArgs & a, int dim, cudaStream_t stream)
 {
+  int       cand[3];
+  const int x = pick_tile(cand, tile_candidates_mixed(dim, a.bx, a.by, a.bz, false, cand), a.tile);
   if (dim == 3)
   {
-    if (a.bx % 8 == 0 && a.by % 8 == 0 && a.bz % 8 == 0)
+    if (x == 8)
       return launch_fused<std::conditional_t<AMR, MX_3D_888_AMR, MX_3D_888>>(a, stream);
     return launch_fused<std::conditional_t<AMR, MX_3D_444_AMR, MX_3D_444>>(a, stream);
   }
-  if (a.bx % 16 == 0 && a.by % 16 == 0)
+  if (x == 16)
     return launch_fused<std::conditional_t<AMR, MX_2D_16_AMR, MX_2D_16>>(a, stream);
-  if (a.bx % 8 == 0 && a.by % 8 == 0)
+  if (x == 8)
     return launch_fused<std::conditional_t<AMR, MX_2D_8_AMR, MX_2D_8>>(a, stream);
   return launch_fused<std::conditional_t<AMR, MX_2D_4_AMR, MX_2D_4>>(a, stream);
 }
@@ -42,23 +44,38 @@ launch_step_mixed(const StepArgs & a, int dim, cudaStream_t stream)
   return a.kind ? launch_step_mixed_cfg<true>(a, dim, stream) : launch_step_mixed_cfg<false>(a, dim, stream);
 }
 
-void
-tile_shape_mixed(int dim, int bx, int by, int bz, bool visc, int * t)
+int
+tile_candidates_mixed(int dim, int bx, int by, int bz, bool visc, int * out)
 {
+  int n = 0;
   if (dim == 3)
   {
-    if (visc)
-    {
-      const bool big = bx % 8 == 0 && by % 8 == 0 && bz % 4 == 0;
-      t[0] = t[1] = big ? 8 : 4;
-      t[2] = 4;
-      return;
-    }
-    const int n = (bx % 8 == 0 && by % 8 == 0 && bz % 8 == 0) ? 8 : 4;
-    t[0] = t[1] = t[2] = n;
+    // 8x8x8 tiles (8x8x4 with the viscous velocities), then 4x4x4
+    if (bx % 8 == 0 && by % 8 == 0 && bz % (visc ? 4 : 8) == 0)
+      out[n++] = 8;
+    if (bx % 4 == 0 && by % 4 == 0 && bz % 4 == 0)
+      out[n++] = 4;
+    return n;
+  }
+  for (int t : {16, 8, 4})
+    if (bx % t == 0 && by % t == 0)
+      out[n++] = t;
+  return n;
+}
+
+void
+tile_shape_mixed(int dim, int bx, int by, int bz, bool visc, int tile, int * t)
+{
+  int       cand[3];
+  const int x = pick_tile(cand, tile_candidates_mixed(dim, bx, by, bz, visc, cand), tile);
+  if (dim == 3)
+  {
+    const int n = x == 8 ? 8 : 4;
+    t[0] = t[1] = n;
+    t[2] = visc ? 4 : n;
     return;
   }
-  const int n = (bx % 16 == 0 && by % 16 == 0) ? 16 : ((bx % 8 == 0 && by % 8 == 0) ? 8 : 4);
+  const int n = x ? x : 4;
   t[0] = t[1] = n;
   t[2] = 1;
 }

@@ -22,15 +22,17 @@ template <bool AMR>
 int
 launch_step_mixed_visc_cfg(const StepArgs & a, int dim, cudaStream_t stream)
 {
+  int       cand[3];
+  const int x = pick_tile(cand, tile_candidates_mixed(dim, a.bx, a.by, a.bz, true, cand), a.tile);
   if (dim == 3)
   {
-    if (a.bx % 8 == 0 && a.by % 8 == 0 && a.bz % 4 == 0)
+    if (x == 8)
       return launch_fused<std::conditional_t<AMR, VMX_3D_884_AMR, VMX_3D_884>>(a, stream);
     return launch_fused<std::conditional_t<AMR, VMX_3D_444_AMR, VMX_3D_444>>(a, stream);
   }
-  if (a.bx % 16 == 0 && a.by % 16 == 0)
+  if (x == 16)
     return launch_fused<std::conditional_t<AMR, VMX_2D_16_AMR, VMX_2D_16>>(a, stream);
-  if (a.bx % 8 == 0 && a.by % 8 == 0)
+  if (x == 8)
     return launch_fused<std::conditional_t<AMR, VMX_2D_8_AMR, VMX_2D_8>>(a, stream);
   return launch_fused<std::conditional_t<AMR, VMX_2D_4_AMR, VMX_2D_4>>(a, stream);
 }

@@ -98,6 +98,19 @@ class GodunovImplemGB300:
         nat.check(self._lib.gmhd_step(self._ctx, _ptr(U), _ptr(U2), _ptr(Bface), _ptr(Bface2), float(dt),
                                       _stream_ptr(stream)), "gmhd_step", self._ctx)
 
+    def autotune(self, U, U2, B, B2, dt: float, stream=None):
+        """Pick the fastest shared-memory tile for this mesh's block size (gmhd_autotune): U2, B2 are
+        scratch. Returns (tile x extent, ms per step)."""
+        tile = ctypes.c_int32(0)
+        ms = ctypes.c_double(0.0)
+        nat.check(self._lib.gmhd_autotune(self._ctx, _ptr(U), _ptr(U2), _ptr(B), _ptr(B2), float(dt), ctypes.byref(tile),
+                                          ctypes.byref(ms), _stream_ptr(stream)), "gmhd_autotune", self._ctx)
+        return int(tile.value), float(ms.value)
+
+    def set_tile(self, tile: int) -> None:
+        """Tile request by hand (gmhd_set_tile): an x extent the step has for this block size, or 0."""
+        nat.check(self._lib.gmhd_set_tile(self._ctx, int(tile)), "gmhd_set_tile", self._ctx)
+
     # --- solver-side device calls of the path ------------------------------------------------------
     def compute_inv_dt(self, U, Bface, stream=None):
         out = np.zeros(self.n_problems, dtype=np.float64)

@@ -227,6 +227,19 @@ int gmhd_inv_dt_noalloc(const gmhd_params * params, int32_t dim, int32_t bx, int
                         int32_t n_blocks, int32_t level, const int32_t * problem, int32_t n_problems,
                         const double * U, const double * B, double * inv_dt, void * stream);
 
+/* Tile autotuner (no counterpart in the reference): runs the step (U -> U2, B -> B2, time step dt; U2
+ * and B2 are scratch here) with every shared-memory tile configuration compiled for this context's
+ * precision and block size (x extents 8 and 4 in 3D, 16, 8 and 4 in 2D, where they divide the block),
+ * two warm-up and five timed launches each on `stream`, and keeps the fastest for the context's
+ * later steps, across gmhd_set_mesh calls with the same block size (the coarse/fine tile lists are
+ * rebuilt for it). Results do not depend on the tile. Writes the chosen x extent and its time per step
+ * in ms (either pointer may be NULL). Synchronises the device. */
+int gmhd_autotune(gmhd_ctx * ctx, const double * U, double * U2, const double * B, double * B2, double dt,
+                  int32_t * tile_out, double * ms_out, void * stream);
+/* Sets the tile request by hand: an x extent from the list above (one that does not divide the block
+ * falls back to the largest that does), or 0 for that default. Synchronises the device. */
+int gmhd_set_tile(gmhd_ctx * ctx, int32_t tile);
+
 /* --- host-buffer variants ------------------------------------------------------------------- */
 
 /* gmhd_step on HOST arrays: copies U, B to the device, runs the step, copies U2, B2 back. */

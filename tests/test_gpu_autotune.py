@@ -1,0 +1,113 @@
+"""Tile choice and the autotuner (gmhd_set_tile, gmhd_autotune).
+
+Every tile configuration computes the same cells with the same formulas. On the FP64 path (no FMA
+contraction) a step must give bit-identical U2, B2 whatever tile runs it, on uniform and coarse/fine
+meshes, equal to the oracle's. On the mixed path each tile is its own compiled kernel whose FP32
+contractions may differ in the last bits: results must agree to 1e-6 relative (L1) and 1e-5 (max) per
+field. The autotuner must return one of the configured tiles and keep it for the following steps and
+across a new mesh of the same block size.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from godunov_mhd_ct_gb300 import workloads as wl  # noqa: E402
+from godunov_mhd_ct_gb300.mesh import BlockMesh  # noqa: E402
+from godunov_mhd_ct_gb300.solver import GodunovImplemGB300  # noqa: E402
+
+from .helpers import oracle_mesh, oracle_settings, settings  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _same(precision, got, ref, n):
+    for a, b in zip(got, ref):
+        a, b = a[:n], b[:n]
+        if precision == "fp64":
+            assert np.array_equal(a, b)
+        else:
+            assert np.abs(a - b).sum() <= 1e-6 * np.abs(b).sum()
+            assert np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-3)) <= 1e-5
+
+
+def _step(impl, U, B, dt):
+    dU, dB = torch.from_numpy(U).cuda(), torch.from_numpy(B).cuda()
+    dU2, dB2 = dU.clone(), dB.clone()
+    impl.do_time_step(dU, dU2, dB, dB2, dt)
+    torch.cuda.synchronize()
+    assert impl.last_status() & ~16 == 0
+    return dU2.cpu().numpy(), dB2.cpu().numpy()
+
+
+CASES = [
+    # dim, block, tiles the block admits
+    (3, (16, 16, 16), (8, 4)),
+    (2, (16, 16, 1), (16, 8, 4)),
+]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("dim,block,tiles", CASES)
+def test_results_do_not_depend_on_the_tile(oracle_lib, precision, dim, block, tiles):
+    mesh = BlockMesh.uniform(dim, level=1, block=block)
+    st = settings()
+    U, B = wl.random_smooth(mesh, gamma=st.gamma0, seed=3, amp=0.3)
+    impl = GodunovImplemGB300(st, mesh, precision=precision)
+    dt = 0.5 * impl.compute_dt(torch.from_numpy(U).cuda(), torch.from_numpy(B).cuda())
+    outs = []
+    for t in tiles:
+        impl.set_tile(t)
+        outs.append(_step(impl, U, B, dt))
+    n = mesh.n_owned
+    for out in outs[1:]:
+        _same(precision, out, outs[0], n)
+    if precision == "fp64":
+        U2o, B2o = oracle_lib.step(oracle_mesh(oracle_lib, mesh), oracle_settings(oracle_lib, st), U, B, dt)
+        assert np.array_equal(outs[0][0][:n], U2o[:n]) and np.array_equal(outs[0][1][:n], B2o[:n])
+    impl.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_tile_choice_on_a_coarse_fine_mesh(oracle_lib, precision):
+    """2D two-level mesh: the two-pass tile lists are rebuilt for each tile; steps agree bit for bit."""
+    mesh = BlockMesh.amr(2, wl.refine_band((0.5, 0.5, 0.5), 0.1, 0.2), base_level=2, max_level=3, block=(16, 16, 1))
+    assert mesh.is_amr
+    st = settings()
+    U, B = wl.random_smooth(mesh, gamma=st.gamma0, seed=5, amp=0.2)
+    impl = GodunovImplemGB300(st, mesh, precision=precision)
+    dt = 0.5 * impl.compute_dt(torch.from_numpy(U).cuda(), torch.from_numpy(B).cuda())
+    outs = []
+    for t in (16, 8, 4):
+        impl.set_tile(t)
+        outs.append(_step(impl, U, B, dt))
+    n = mesh.n_owned
+    for out in outs[1:]:
+        _same(precision, out, outs[0], n)
+    if precision == "fp64":
+        om = oracle_lib.Mesh.from_block_mesh(mesh)
+        U2o, B2o = oracle_lib.step(om, oracle_settings(oracle_lib, st), U, B, dt)
+        assert np.array_equal(outs[0][0][:n], U2o[:n]) and np.array_equal(outs[0][1][:n], B2o[:n])
+    impl.close()
+
+
+def test_autotune_picks_a_configured_tile_and_keeps_it():
+    mesh = BlockMesh.uniform(3, level=1, block=(32, 32, 32))
+    st = settings()
+    U, B = wl.orszag_tang(mesh, gamma=st.gamma0)
+    impl = GodunovImplemGB300(st, mesh, precision="mixed")
+    dU, dB = torch.from_numpy(U).cuda(), torch.from_numpy(B).cuda()
+    dU2, dB2 = torch.empty_like(dU), torch.empty_like(dB)
+    dt = impl.compute_dt(dU, dB)
+    ref = _step(impl, U, B, dt)
+    tile, ms = impl.autotune(dU, dU2, dB, dB2, dt)
+    assert tile in (8, 4) and ms > 0.0
+    tuned = _step(impl, U, B, dt)
+    _same("mixed", tuned, ref, mesh.n_owned)
+    # a graph-replayed loop after the tuning (the cached graph is rebuilt for the chosen kernel), and a
+    # new mesh of the same block size keep the choice: the same bits as right after the tuning
+    impl.advance(dU, dU2, dB, dB2, 3)
+    impl.resize_auxiliary_data(mesh)
+    got = _step(impl, U, B, dt)
+    assert np.array_equal(got[0], tuned[0]) and np.array_equal(got[1], tuned[1])
+    impl.close()
