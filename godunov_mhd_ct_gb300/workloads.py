@@ -204,33 +204,47 @@ def gaussian01(seed: int, ids: np.ndarray) -> np.ndarray:
     return np.sqrt(-2.0 * np.log1p(-u1)) * np.cos(2.0 * math.pi * u2)
 
 
-def kelvin_helmholtz(mesh: BlockMesh, gamma=1.4, p0=2.5, bx0=0.1, width=0.01, noise=1e-3, seed=0):
+def kelvin_helmholtz(mesh: BlockMesh, gamma=1.4, p0=2.5, bx0=0.1, width=0.01, noise=1e-3, seed=0,
+                     chunk_blocks: int = 2048):
     """Magnetised shear layer on [0,1]^d (init/InitKelvinHelmholtz.cpp): rho = 2, vx = +0.5 for
     |y - 0.5| < 0.25 and rho = 1, vx = -0.5 outside, tanh-smoothed with `width`; vy = 0.01 sin(4 pi x)
-    plus seeded Gaussian noise of amplitude `noise`; p = p0; uniform Bx = bx0."""
+    plus seeded Gaussian noise of amplitude `noise`; p = p0; uniform Bx = bx0. The cells are filled
+    `chunk_blocks` blocks at a time, so that the temporaries stay small next to U and B on large meshes."""
     U, B = mesh.alloc_state()
     Bx, By, Bz = mesh.split_faces(B)
     Bx[...] = bx0
     By[...] = 0.0
     Bz[...] = 0.0
     n = mesh.n_owned
-    gi, gj, gk = mesh.global_cell_index()
-    gi, gj, gk = gi[:n], gj[:n], gk[:n]
-    dx = mesh.block_dx()[:n, None, None, None]
-    x = (gi + 0.5) * dx
-    y = (gj + 0.5) * dx
-    s = 0.5 * (1.0 + np.tanh((0.25 - np.abs(y - 0.5)) / width))
-    rho = 1.0 + s
-    vx = -0.5 + s
-    # noise id: the cell's lower corner on the finest level's grid (unique across levels)
+    bx, by, bz = mesh.block
+    k, j, i = np.meshgrid(np.arange(bz), np.arange(by), np.arange(bx), indexing="ij")
     top = int(mesh.level[:n].max())
-    sh = (top - mesh.level[:n]).astype(np.int64)[:, None, None, None]
     gx = mesh.grid[0] * mesh.block[0]
     gy = mesh.grid[1] * mesh.block[1]
-    ids = (gi << sh) + gx * ((gj << sh) + gy * (gk << sh))
-    vy = 0.01 * np.sin(4.0 * math.pi * x) + noise * gaussian01(seed, ids)
-    vz = np.zeros_like(x)
-    _fill_energy(mesh, U, B, rho, np.full(x.shape, p0), vx, vy, vz, gamma)
+    for b0 in range(0, n, chunk_blocks):
+        b1 = min(n, b0 + chunk_blocks)
+        c = mesh.coords[b0:b1]
+        gi = c[:, 0, None, None, None] * bx + i[None]
+        gj = c[:, 1, None, None, None] * by + j[None]
+        gk = c[:, 2, None, None, None] * bz + k[None]
+        dx = mesh.block_dx()[b0:b1, None, None, None]
+        x = (gi + 0.5) * dx
+        y = (gj + 0.5) * dx
+        s = 0.5 * (1.0 + np.tanh((0.25 - np.abs(y - 0.5)) / width))
+        rho = 1.0 + s
+        vx = -0.5 + s
+        # noise id: the cell's lower corner on the finest level's grid (unique across levels)
+        sh = (top - mesh.level[b0:b1]).astype(np.int64)[:, None, None, None]
+        ids = (gi << sh) + gx * ((gj << sh) + gy * (gk << sh))
+        vy = 0.01 * np.sin(4.0 * math.pi * x) + noise * gaussian01(seed, ids)
+        vz = np.zeros_like(x)
+        bcx, bcy, bcz = _cell_centred_b(mesh, B[b0:b1])
+        U[b0:b1, 0] = rho
+        U[b0:b1, 2] = rho * vx
+        U[b0:b1, 3] = rho * vy
+        U[b0:b1, 4] = rho * vz
+        U[b0:b1, 1] = np.full(x.shape, p0) / (gamma - 1.0) + 0.5 * rho * (vx * vx + vy * vy + vz * vz) + 0.5 * (
+            bcx ** 2 + bcy ** 2 + bcz ** 2)
     return U, B
 
 
