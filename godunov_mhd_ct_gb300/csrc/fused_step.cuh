@@ -174,17 +174,20 @@ struct Cfg
   static constexpr int OFF_B2 = OFF_FL + NFV * NFT;
   static constexpr int U1_LATE = RPD * NECOMP * NM + NFV * NFT + NB2;
   static constexpr int TOTAL = OFF_U1 + (U1_EARLY > U1_LATE ? U1_EARLY : U1_LATE);
-  static constexpr size_t SMEM_BYTES = sizeof(R) * (size_t)TOTAL + 64 * sizeof(int);
 
-  // Persistent, software-pipelined variant (mixed precision, conforming 3D meshes): one CTA per SM
-  // loops over tiles; after phase 5 of a tile it stages the next tile's FP64 gather (face B and U of
-  // the Q region, in the layout of fbx|fby|fbz and of the primitives) into [OFF_SL, OFF_U1) with
-  // cp.async, and those copies land while phases 6-7 run.
+  // Persistent, software-pipelined variant (mixed precision, 3D, conforming or coarse/fine meshes):
+  // one CTA per SM loops over tiles (all tiles of the owned blocks, or a pass's tile list); after
+  // phase 5 of a tile it stages the next tile's FP64 gather (face B and U of the Q region, in the
+  // layout of fbx|fby|fbz and of the primitives) into [OFF_SL, OFF_U1) with cp.async, and those copies
+  // land while phases 6-7 run.
   static constexpr int  NFB = NFBX + NFBY + NFBZ;
   static constexpr int  STAGE_DOUBLES = NFB + 5 * NQ;
-  static constexpr bool PIPE = !EXACT && !AMR && !VISC && DIM == 3 && NFBX % 2 == 0 && NFBY % 2 == 0 &&
+  static constexpr bool PIPE = !EXACT && !VISC && DIM == 3 && NFBX % 2 == 0 && NFBY % 2 == 0 &&
                                NFBZ % 2 == 0 && NQ % 2 == 0 && (OFF_SL * sizeof(R)) % 16 == 0 &&
                                (size_t)STAGE_DOUBLES * 8 <= (size_t)(OFF_U1 - OFF_SL) * sizeof(R);
+  // after the tile arrays: neighbour tables and region kinds, [32] each, two of each with PIPE
+  static constexpr int    NBR_INTS = (PIPE ? 2 : 1) * 32 * (AMR ? 2 : 1) < 64 ? 64 : (PIPE ? 2 : 1) * 32 * (AMR ? 2 : 1);
+  static constexpr size_t SMEM_BYTES = sizeof(R) * (size_t)TOTAL + NBR_INTS * sizeof(int);
 
   static constexpr int NCELL = TX * TY * TZ;
   static constexpr int CPT = (NCELL + NT - 1) / NT;
@@ -842,7 +845,9 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
   R *      fl = sm + C::OFF_FL;
   R *      b2s = sm + C::OFF_B2;
   R *      vel = sm + C::OFF_VEL; // viscous variants: t^n velocities of cells [-1, T]
-  int * s_nbr0 = reinterpret_cast<int *>(sm + C::TOTAL); // [32] neighbours (+ [32] region kinds or a 2nd table)
+  // neighbour tables ([32] per staged tile), then region kinds of coarse/fine meshes ([32] per staged tile)
+  int * s_nbr0 = reinterpret_cast<int *>(sm + C::TOTAL);
+  int * s_kind0 = s_nbr0 + (C::PIPE ? 64 : 32);
   __shared__ double       s_red[NT / 32];
   __shared__ unsigned int s_health;
   __shared__ unsigned int s_stage_health[2]; // PIPE: missing / level-jump flags of a staged tile
@@ -856,12 +861,18 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
 
   // ---- PIPE: staging of a tile's gather ----------------------------------------------------------
   double *  stage = reinterpret_cast<double *>(sm + C::OFF_SL);
-  const int n_work = C::PIPE ? a.n_owned * tiles_per_block : 0;
-  // neighbour table of tile w into buffer buf (warp 0), with the slots whose block is at another level
+  const int n_work = C::PIPE ? (a.tile_list ? a.n_list : a.n_owned * tiles_per_block) : 0;
+  // tile of work item w (a pass's list entry: ~tile marks a side-data-only tile)
+  auto tile_at = [&](int w) { return a.tile_list ? a.tile_list[w] : w; };
+  // neighbour table (and region kinds) of work item w into buffer buf (warp 0), with the slots whose
+  // block is at another level
   auto load_nbr = [&](int w, int buf) {
     if (tid < 32)
     {
-      const int b = w / tiles_per_block;
+      int tl = tile_at(w);
+      if (tl < 0)
+        tl = ~tl;
+      const int b = tl / tiles_per_block;
       int       nb = -1;
       bool      jump = false;
       if (tid < 27)
@@ -869,6 +880,8 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
         nb = a.neighbor[(int64_t)b * 27 + tid];
         jump = nb >= 0 && nb < a.n_blocks && a.level[nb] != a.level[b];
         s_nbr0[32 * buf + tid] = nb;
+        if constexpr (C::AMR)
+          s_kind0[32 * buf + tid] = (int)a.kind[(int64_t)b * 27 + tid];
       }
       const unsigned m = __ballot_sync(0xffffffffu, jump);
       if (tid == 0)
@@ -881,14 +894,47 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
   // issue the cp.async copies of tile w's face B and U (Q region) into the staging area; absent
   // neighbours give 0 (faces) and rho = E = 1, momenta 0 (as the direct gather)
   auto stage_tile = [&](int w, int buf) {
-    const int   b = w / tiles_per_block;
-    int         t = w - b * tiles_per_block;
+    int tl = tile_at(w);
+    if (tl < 0)
+      tl = ~tl;
+    const int   b = tl / tiles_per_block;
+    int         t = tl - b * tiles_per_block;
     const int   sx0 = (t % a.tiles_x) * TX;
     t /= a.tiles_x;
     const int   sy0 = (t % a.tiles_y) * TY, sz0 = (t / a.tiles_y) * TZ;
     const int * nbr = s_nbr0 + 32 * buf;
+    const int * kinds = s_kind0 + 32 * buf;
     const unsigned jm = s_stage_jump[buf];
     unsigned    fl = 0u;
+    // face / conservative arrays of a real or virtual (coarse/fine ghost) block
+    auto bsrc_s = [&](int nb) -> const double * {
+      if constexpr (C::AMR)
+        return nb < a.n_blocks ? a.B + (int64_t)nb * a.nface : a.Bv + (int64_t)(nb - a.n_blocks) * a.nface;
+      else
+        return a.B + (int64_t)nb * a.nface;
+    };
+    auto usrc_s = [&](int nb) -> const double * {
+      if constexpr (C::AMR)
+        return nb < a.n_blocks ? a.U + (int64_t)nb * 5 * a.ncell : a.Uv + (int64_t)(nb - a.n_blocks) * 5 * a.ncell;
+      else
+        return a.U + (int64_t)nb * 5 * a.ncell;
+    };
+    // the block's own border face shared with a finer face neighbour: that neighbour's (restricted) value
+    auto shared_s = [&](int d, int f, int n, int & nb, int & fq) {
+      if constexpr (C::AMR)
+      {
+        if (nb == b && (f == 0 || f == n))
+        {
+          const int sl = nb_slot(d == 0 ? (f == 0 ? -1 : 1) : 0, d == 1 ? (f == 0 ? -1 : 1) : 0,
+                                 d == 2 ? (f == 0 ? -1 : 1) : 0);
+          if (kinds[sl] == RK_FINER)
+          {
+            nb = nbr[sl];
+            fq = f == 0 ? n : 0;
+          }
+        }
+      }
+    };
     auto        own = [&](int ox, int oy, int oz) -> int {
       if ((ox | oy | oz) == 0)
         return b;
@@ -907,10 +953,11 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
       const int k = n / ((TX + 5) * C::QY) - 2;
       const int fi = sx0 + i, cj = sy0 + j, ck = sz0 + k;
       const int ox = face_off(fi, bx), oy = cell_off(cj, by), oz = cell_off(ck, bz);
-      const int nb = own(ox, oy, oz);
+      int       nb = own(ox, oy, oz);
+      int       fq = fi - ox * bx;
+      shared_s(0, fi, bx, nb, fq);
       if (nb >= 0)
-        cp_async8(stage + n, a.B + (int64_t)nb * a.nface + (fi - ox * bx) +
-                               (int64_t)(bx + 1) * ((cj - oy * by) + (int64_t)by * (ck - oz * bz)));
+        cp_async8(stage + n, bsrc_s(nb) + fq + (int64_t)(bx + 1) * ((cj - oy * by) + (int64_t)by * (ck - oz * bz)));
       else
         stage[n] = 0.0;
     }
@@ -922,11 +969,12 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
       const int k = n / (C::QX * (TY + 5)) - 2;
       const int ci = sx0 + i, fj = sy0 + j, ck = sz0 + k;
       const int ox = cell_off(ci, bx), oy = face_off(fj, by), oz = cell_off(ck, bz);
-      const int nb = own(ox, oy, oz);
+      int       nb = own(ox, oy, oz);
+      int       fq = fj - oy * by;
+      shared_s(1, fj, by, nb, fq);
       double *  d = stage + C::NFBX + n;
       if (nb >= 0)
-        cp_async16(d, a.B + (int64_t)nb * a.nface + a.nfx + (ci - ox * bx) +
-                        (int64_t)bx * ((fj - oy * by) + (int64_t)(by + 1) * (ck - oz * bz)));
+        cp_async16(d, bsrc_s(nb) + a.nfx + (ci - ox * bx) + (int64_t)bx * (fq + (int64_t)(by + 1) * (ck - oz * bz)));
       else
         d[0] = d[1] = 0.0;
     }
@@ -938,11 +986,12 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
       const int k = n / (C::QX * C::QY) - 2;
       const int ci = sx0 + i, cj = sy0 + j, fk = sz0 + k;
       const int ox = cell_off(ci, bx), oy = cell_off(cj, by), oz = face_off(fk, bz);
-      const int nb = own(ox, oy, oz);
+      int       nb = own(ox, oy, oz);
+      int       fq = fk - oz * bz;
+      shared_s(2, fk, bz, nb, fq);
       double *  d = stage + C::NFBX + C::NFBY + n;
       if (nb >= 0)
-        cp_async16(d, a.B + (int64_t)nb * a.nface + a.nfx + a.nfy + (ci - ox * bx) +
-                        (int64_t)bx * ((cj - oy * by) + (int64_t)by * (fk - oz * bz)));
+        cp_async16(d, bsrc_s(nb) + a.nfx + a.nfy + (ci - ox * bx) + (int64_t)bx * ((cj - oy * by) + (int64_t)by * fq));
       else
         d[0] = d[1] = 0.0;
     }
@@ -958,8 +1007,7 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
       double *  d = stage + C::NFB + n;
       if (nb >= 0)
       {
-        const double * Ub = a.U + (int64_t)nb * 5 * a.ncell + (ci - ox * bx) +
-                            (int64_t)bx * ((cj - oy * by) + (int64_t)by * (ck - oz * bz));
+        const double * Ub = usrc_s(nb) + (ci - ox * bx) + (int64_t)bx * ((cj - oy * by) + (int64_t)by * (ck - oz * bz));
 #pragma unroll
         for (int v = 0; v < 5; ++v)
           cp_async16(d + v * C::NQ, Ub + (int64_t)v * a.ncell);
@@ -991,11 +1039,12 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
   const int buf = iter & 1;
   const bool has_next = C::PIPE && work + (int)gridDim.x < n_work;
   int *     s_nbr = s_nbr0 + (C::PIPE ? 32 * buf : 0);
-  int       tile = C::PIPE ? work : (int)blockIdx.x;
+  int       tile = C::PIPE ? tile_at(work) : (int)blockIdx.x;
   bool      side_only = false; // pass 1 of a tile that also runs in pass 2: side data only
-  if (!C::PIPE && a.tile_list)
+  if (a.tile_list)
   {
-    tile = a.tile_list[blockIdx.x];
+    if (!C::PIPE)
+      tile = a.tile_list[blockIdx.x];
     if (tile < 0)
     {
       tile = ~tile;
@@ -1012,7 +1061,7 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
   const int tz = t / a.tiles_y;
   const int x0 = tx * TX, y0 = ty * TY, z0 = tz * TZ;
 
-  int * s_kind = s_nbr0 + 32;
+  int * s_kind = s_kind0 + (C::PIPE ? 32 * buf : 0);
   if constexpr (C::PIPE)
   {
     cp_async_wait_all(); // this tile's staged gather (issued during the previous tile)
@@ -1746,7 +1795,18 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
     amr_border_fluxes<C>(a, fl, s_kind, blk, x0, y0, z0, tid, vel, dxr, dtdx);
     __syncthreads();
     if (side_only)
-      return; // this tile's update runs in pass 2
+    {
+      // this tile's update runs in pass 2; with PIPE the next tile's gather is issued here instead of
+      // in phase 6 (the staging area is dead: phase 5 and the border fluxes are done)
+      if constexpr (C::PIPE)
+      {
+        if (has_next)
+          stage_tile(work + gridDim.x, buf ^ 1);
+        continue;
+      }
+      else
+        return;
+    }
   }
 
   // ---- phase 6: CT update (ReadEmfAndUpdateFunctor.cpp:58-163) on faces [0, T] along each

@@ -33,8 +33,8 @@ launch_fused(StepArgs a, cudaStream_t stream)
     return 0;
   if constexpr (C::PIPE)
   {
-    // one persistent CTA per resident slot, each looping over tiles
-    if (a.tile_list || resident_ctas<C>() <= 0)
+    // one persistent CTA per resident slot, each looping over tiles (or over the pass's tile list)
+    if (resident_ctas<C>() <= 0)
       return -1;
     nblocks = nblocks < resident_ctas<C>() ? nblocks : resident_ctas<C>();
   }
