@@ -175,7 +175,8 @@ struct Cfg
   static constexpr int U1_LATE = RPD * NECOMP * NM + NFV * NFT + NB2;
   static constexpr int TOTAL = OFF_U1 + (U1_EARLY > U1_LATE ? U1_EARLY : U1_LATE);
 
-  // Persistent, software-pipelined variant (mixed precision, 3D, conforming or coarse/fine meshes):
+  // Persistent, software-pipelined variant (mixed precision, 3D, conforming or coarse/fine meshes; the
+  // FP64 path gains nothing from it, being bound by its FP64 pipe, and keeps one tile per CTA):
   // one CTA per SM loops over tiles (all tiles of the owned blocks, or a pass's tile list); after
   // phase 5 of a tile it stages the next tile's FP64 gather (face B and U of the Q region, in the
   // layout of fbx|fby|fbz and of the primitives) into [OFF_SL, OFF_U1) with cp.async, and those copies

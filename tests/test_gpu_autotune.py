@@ -3,8 +3,8 @@
 Every tile configuration computes the same cells with the same formulas. On the FP64 path (no FMA
 contraction) a step must give bit-identical U2, B2 whatever tile runs it, on uniform and coarse/fine
 meshes, equal to the oracle's. On the mixed path each tile is its own compiled kernel whose FP32
-contractions may differ in the last bits: results must agree to 1e-6 relative (L1) and 1e-5 (max) per
-field. The autotuner must return one of the configured tiles and keep it for the following steps and
+contractions may differ in the last bits: results must agree to 1e-6 relative (L1) and to 1e-5 of the
+field's largest magnitude. The autotuner must return one of the configured tiles and keep it for the following steps and
 across a new mesh of the same block size.
 """
 import numpy as np
@@ -28,7 +28,7 @@ def _same(precision, got, ref, n):
             assert np.array_equal(a, b)
         else:
             assert np.abs(a - b).sum() <= 1e-6 * np.abs(b).sum()
-            assert np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-3)) <= 1e-5
+            assert np.max(np.abs(a - b)) <= 1e-5 * np.max(np.abs(b))
 
 
 def _step(impl, U, B, dt):
@@ -69,16 +69,25 @@ def test_results_do_not_depend_on_the_tile(oracle_lib, precision, dim, block, ti
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_tile_choice_on_a_coarse_fine_mesh(oracle_lib, precision):
-    """2D two-level mesh: the two-pass tile lists are rebuilt for each tile; steps agree bit for bit."""
-    mesh = BlockMesh.amr(2, wl.refine_band((0.5, 0.5, 0.5), 0.1, 0.2), base_level=2, max_level=3, block=(16, 16, 1))
+@pytest.mark.parametrize("dim", [2, 3])
+def test_tile_choice_on_a_coarse_fine_mesh(oracle_lib, precision, dim):
+    """Two-level meshes: the two-pass tile lists are rebuilt for each tile (3D: the persistent kernel on
+    both tiles); FP64 steps agree bit for bit and with the oracle."""
+    if dim == 2:
+        mesh = BlockMesh.amr(2, wl.refine_band((0.5, 0.5, 0.5), 0.1, 0.2), base_level=2, max_level=3,
+                             block=(16, 16, 1))
+        tiles = (16, 8, 4)
+    else:
+        mesh = BlockMesh.amr(3, wl.refine_band((0.3, 0.3, 0.3), 0.0, 0.1, axes=3), base_level=2, max_level=3,
+                             block=(8, 8, 8))
+        tiles = (8, 4)
     assert mesh.is_amr
     st = settings()
     U, B = wl.random_smooth(mesh, gamma=st.gamma0, seed=5, amp=0.2)
     impl = GodunovImplemGB300(st, mesh, precision=precision)
     dt = 0.5 * impl.compute_dt(torch.from_numpy(U).cuda(), torch.from_numpy(B).cuda())
     outs = []
-    for t in (16, 8, 4):
+    for t in tiles:
         impl.set_tile(t)
         outs.append(_step(impl, U, B, dt))
     n = mesh.n_owned
