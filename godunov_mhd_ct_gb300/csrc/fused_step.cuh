@@ -862,9 +862,15 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
 
   // ---- PIPE: staging of a tile's gather ----------------------------------------------------------
   double *  stage = reinterpret_cast<double *>(sm + C::OFF_SL);
-  const int n_work = C::PIPE ? (a.tile_list ? a.n_list : a.n_owned * tiles_per_block) : 0;
+  // tile lists exist on coarse/fine meshes only (the AMR instantiations)
+  const int n_work = C::PIPE ? ((C::AMR && a.tile_list) ? a.n_list : a.n_owned * tiles_per_block) : 0;
   // tile of work item w (a pass's list entry: ~tile marks a side-data-only tile)
-  auto tile_at = [&](int w) { return a.tile_list ? a.tile_list[w] : w; };
+  auto tile_at = [&](int w) {
+    if constexpr (C::AMR)
+      return a.tile_list ? a.tile_list[w] : w;
+    else
+      return w;
+  };
   // neighbour table (and region kinds) of work item w into buffer buf (warp 0), with the slots whose
   // block is at another level
   auto load_nbr = [&](int w, int buf) {
@@ -1042,7 +1048,7 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
   int *     s_nbr = s_nbr0 + (C::PIPE ? 32 * buf : 0);
   int       tile = C::PIPE ? tile_at(work) : (int)blockIdx.x;
   bool      side_only = false; // pass 1 of a tile that also runs in pass 2: side data only
-  if (a.tile_list)
+  if (C::AMR && a.tile_list)
   {
     if (!C::PIPE)
       tile = a.tile_list[blockIdx.x];
