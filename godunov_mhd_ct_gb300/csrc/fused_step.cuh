@@ -175,17 +175,18 @@ struct Cfg
   static constexpr int U1_LATE = RPD * NECOMP * NM + NFV * NFT + NB2;
   static constexpr int TOTAL = OFF_U1 + (U1_EARLY > U1_LATE ? U1_EARLY : U1_LATE);
 
-  // Persistent, software-pipelined variant (mixed precision, 3D, conforming or coarse/fine meshes; the
-  // FP64 path gains nothing from it, being bound by its FP64 pipe, and keeps one tile per CTA):
-  // one CTA per SM loops over tiles (all tiles of the owned blocks, or a pass's tile list); after
-  // phase 5 of a tile it stages the next tile's FP64 gather (face B and U of the Q region, in the
-  // layout of fbx|fby|fbz and of the primitives) into [OFF_SL, OFF_U1) with cp.async, and those copies
-  // land while phases 6-7 run.
+  // Persistent, software-pipelined variant (mixed precision, 3D, conforming or coarse/fine meshes, with
+  // or without viscosity; the FP64 path gains nothing from it, being bound by its FP64 pipe, and keeps
+  // one tile per CTA): one CTA per SM loops over tiles (all tiles of the owned blocks, or a pass's tile
+  // list); after phase 5 of a tile it stages the next tile's FP64 gather (face B and U of the Q region,
+  // in the layout of fbx|fby|fbz and of the primitives) into [OFF_SL, OFF_VEL) with cp.async, and those
+  // copies land while phases 6-7 run. The area ends before the viscous variants' t^n velocities, which
+  // phase 7 still reads.
   static constexpr int  NFB = NFBX + NFBY + NFBZ;
   static constexpr int  STAGE_DOUBLES = NFB + 5 * NQ;
-  static constexpr bool PIPE = !EXACT && !VISC && DIM == 3 && NFBX % 2 == 0 && NFBY % 2 == 0 &&
-                               NFBZ % 2 == 0 && NQ % 2 == 0 && (OFF_SL * sizeof(R)) % 16 == 0 &&
-                               (size_t)STAGE_DOUBLES * 8 <= (size_t)(OFF_U1 - OFF_SL) * sizeof(R);
+  static constexpr bool PIPE = !EXACT && DIM == 3 && NFBX % 2 == 0 && NFBY % 2 == 0 && NFBZ % 2 == 0 &&
+                               NQ % 2 == 0 && (OFF_SL * sizeof(R)) % 16 == 0 &&
+                               (size_t)STAGE_DOUBLES * 8 <= (size_t)(OFF_VEL - OFF_SL) * sizeof(R);
   // after the tile arrays: neighbour tables and region kinds, [32] each, two of each with PIPE
   static constexpr int    NBR_INTS = (PIPE ? 2 : 1) * 32 * (AMR ? 2 : 1) < 64 ? 64 : (PIPE ? 2 : 1) * 32 * (AMR ? 2 : 1);
   static constexpr size_t SMEM_BYTES = sizeof(R) * (size_t)TOTAL + NBR_INTS * sizeof(int);
