@@ -176,8 +176,9 @@ struct Cfg
   static constexpr int TOTAL = OFF_U1 + (U1_EARLY > U1_LATE ? U1_EARLY : U1_LATE);
 
   // Persistent, software-pipelined variant (mixed precision, 3D, conforming or coarse/fine meshes, with
-  // or without viscosity; the FP64 path gains nothing from it, being bound by its FP64 pipe, and keeps
-  // one tile per CTA): one CTA per SM loops over tiles (all tiles of the owned blocks, or a pass's tile
+  // or without viscosity; the FP64 path gains nothing from it, being bound by its FP64 pipe, and the 2D
+  // kernels, whose four CTAs per SM already overlap one another's gathers, run 6 % slower with it: both
+  // keep one tile per CTA): one CTA per SM loops over tiles (all tiles of the owned blocks, or a pass's tile
   // list); after phase 5 of a tile it stages the next tile's FP64 gather (face B and U of the Q region,
   // in the layout of fbx|fby|fbz and of the primitives) into [OFF_SL, OFF_VEL) with cp.async, and those
   // copies land while phases 6-7 run. The area ends before the viscous variants' t^n velocities, which
@@ -958,9 +959,9 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
     {
       const int i = n % (TX + 5) - 2;
       const int j = (n / (TX + 5)) % C::QY - 2;
-      const int k = n / ((TX + 5) * C::QY) - 2;
+      const int k = D3 ? n / ((TX + 5) * C::QY) - 2 : 0;
       const int fi = sx0 + i, cj = sy0 + j, ck = sz0 + k;
-      const int ox = face_off(fi, bx), oy = cell_off(cj, by), oz = cell_off(ck, bz);
+      const int ox = face_off(fi, bx), oy = cell_off(cj, by), oz = D3 ? cell_off(ck, bz) : 0;
       int       nb = own(ox, oy, oz);
       int       fq = fi - ox * bx;
       shared_s(0, fi, bx, nb, fq);
@@ -974,9 +975,9 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
       const int n = 2 * m;
       const int i = n % C::QX - 2;
       const int j = (n / C::QX) % (TY + 5) - 2;
-      const int k = n / (C::QX * (TY + 5)) - 2;
+      const int k = D3 ? n / (C::QX * (TY + 5)) - 2 : 0;
       const int ci = sx0 + i, fj = sy0 + j, ck = sz0 + k;
-      const int ox = cell_off(ci, bx), oy = face_off(fj, by), oz = cell_off(ck, bz);
+      const int ox = cell_off(ci, bx), oy = face_off(fj, by), oz = D3 ? cell_off(ck, bz) : 0;
       int       nb = own(ox, oy, oz);
       int       fq = fj - oy * by;
       shared_s(1, fj, by, nb, fq);
@@ -991,12 +992,14 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
       const int n = 2 * m;
       const int i = n % C::QX - 2;
       const int j = (n / C::QX) % C::QY - 2;
-      const int k = n / (C::QX * C::QY) - 2;
+      const int k = D3 ? n / (C::QX * C::QY) - 2 : 0;
       const int ci = sx0 + i, cj = sy0 + j, fk = sz0 + k;
-      const int ox = cell_off(ci, bx), oy = cell_off(cj, by), oz = face_off(fk, bz);
+      // 3D z faces; 2D: the cell-centred Bz of the same cells
+      const int ox = cell_off(ci, bx), oy = cell_off(cj, by), oz = D3 ? face_off(fk, bz) : 0;
       int       nb = own(ox, oy, oz);
       int       fq = fk - oz * bz;
-      shared_s(2, fk, bz, nb, fq);
+      if (D3)
+        shared_s(2, fk, bz, nb, fq);
       double *  d = stage + C::NFBX + C::NFBY + n;
       if (nb >= 0)
         cp_async16(d, bsrc_s(nb) + a.nfx + a.nfy + (ci - ox * bx) + (int64_t)bx * ((cj - oy * by) + (int64_t)by * fq));
@@ -1008,9 +1011,9 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
       const int n = 2 * m;
       const int i = n % C::QX - 2;
       const int j = (n / C::QX) % C::QY - 2;
-      const int k = n / (C::QX * C::QY) - 2;
+      const int k = D3 ? n / (C::QX * C::QY) - 2 : 0;
       const int ci = sx0 + i, cj = sy0 + j, ck = sz0 + k;
-      const int ox = cell_off(ci, bx), oy = cell_off(cj, by), oz = cell_off(ck, bz);
+      const int ox = cell_off(ci, bx), oy = cell_off(cj, by), oz = D3 ? cell_off(ck, bz) : 0;
       const int nb = own(ox, oy, oz);
       double *  d = stage + C::NFB + n;
       if (nb >= 0)
