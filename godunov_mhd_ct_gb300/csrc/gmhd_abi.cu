@@ -694,26 +694,44 @@ build_tile_lists(gmhd_ctx * ctx, int dim, const std::vector<int8_t> & kind)
   std::vector<int32_t> & list2 = ctx->h_list2;
   list1.clear();
   list2.clear();
+  // the neighbour slots a tile touches depend only on where it sits in the block along each axis (first,
+  // last, or both when the block is one tile wide, or neither): one 27-bit mask per position class
+  auto cls_of = [&](int c, int n) { return (c == 0 ? 1 : 0) | (c == n - 1 ? 2 : 0); };
+  uint32_t touch[64];
+  for (int cz = 0; cz < 4; ++cz)
+    for (int cy = 0; cy < 4; ++cy)
+      for (int cx = 0; cx < 4; ++cx)
+      {
+        const int cl[3] = {cx, cy, cz};
+        uint32_t  m = 0;
+        for (int s = 0; s < 27; ++s)
+        {
+          if (s == 13 || (dim == 2 && s / 9 != 1))
+            continue;
+          const int o[3] = {s % 3 - 1, (s / 3) % 3 - 1, s / 9 - 1};
+          bool      t = true;
+          for (int d = 0; d < 3; ++d)
+            if (o[d] != 0 && !(cl[d] & (o[d] < 0 ? 1 : 2)))
+              t = false;
+          if (t)
+            m |= 1u << s;
+        }
+        touch[cx + 4 * (cy + 4 * cz)] = m;
+      }
   for (int b = 0; b < ctx->n_owned; ++b)
+  {
+    uint32_t finer = 0, coarser = 0;
+    for (int s = 0; s < 27; ++s)
+    {
+      finer |= (kind[(size_t)b * 27 + s] == gmhd::RK_FINER ? 1u : 0u) << s;
+      coarser |= (kind[(size_t)b * 27 + s] == gmhd::RK_COARSER ? 1u : 0u) << s;
+    }
     for (int t = 0; t < tpb; ++t)
     {
-      const int tc[3] = {t % nt[0], (t / nt[0]) % nt[1], t / (nt[0] * nt[1])};
-      bool      fin = false, coa = false;
-      for (int s = 0; s < 27; ++s)
-      {
-        if (s == 13 || (dim == 2 && s / 9 != 1))
-          continue;
-        const int o[3] = {s % 3 - 1, (s / 3) % 3 - 1, s / 9 - 1};
-        bool      touch = true;
-        for (int d = 0; d < 3; ++d)
-          if (o[d] != 0 && tc[d] != (o[d] < 0 ? 0 : nt[d] - 1))
-            touch = false;
-        if (!touch)
-          continue;
-        fin = fin || kind[(size_t)b * 27 + s] == gmhd::RK_FINER;
-        coa = coa || kind[(size_t)b * 27 + s] == gmhd::RK_COARSER;
-      }
-      const int32_t id = b * tpb + t;
+      const int      tc[3] = {t % nt[0], (t / nt[0]) % nt[1], t / (nt[0] * nt[1])};
+      const uint32_t m = touch[cls_of(tc[0], nt[0]) + 4 * (cls_of(tc[1], nt[1]) + 4 * cls_of(tc[2], nt[2]))];
+      const bool     fin = (finer & m) != 0, coa = (coarser & m) != 0;
+      const int32_t  id = b * tpb + t;
       if (!fin)
         list1.push_back(id);
       else
@@ -723,6 +741,7 @@ build_tile_lists(gmhd_ctx * ctx, int dim, const std::vector<int8_t> & kind)
         list2.push_back(id);
       }
     }
+  }
 }
 
 // Make `tile` the context's tile request; on a coarse/fine mesh rebuild and upload the tile lists for
