@@ -120,3 +120,28 @@ def test_autotune_picks_a_configured_tile_and_keeps_it():
     got = _step(impl, U, B, dt)
     assert np.array_equal(got[0], tuned[0]) and np.array_equal(got[1], tuned[1])
     impl.close()
+
+
+def test_autotune_on_a_coarse_fine_mesh_keeps_fp64_exact(oracle_lib):
+    """The autotuner on a two-level 2D mesh (tile lists rebuilt per candidate): the FP64 step afterwards
+    still equals the oracle's bit for bit; an empty mesh tunes without work."""
+    mesh = BlockMesh.amr(2, wl.refine_band((0.5, 0.5, 0.5), 0.1, 0.2), base_level=2, max_level=3, block=(16, 16, 1))
+    st = settings()
+    U, B = wl.random_smooth(mesh, gamma=st.gamma0, seed=8, amp=0.2)
+    impl = GodunovImplemGB300(st, mesh, precision="fp64")
+    dU, dB = torch.from_numpy(U).cuda(), torch.from_numpy(B).cuda()
+    dt = 0.5 * impl.compute_dt(dU, dB)
+    tile, _ = impl.autotune(dU, torch.empty_like(dU), dB, torch.empty_like(dB), dt)
+    assert tile in (16, 8, 4)
+    U2, B2 = _step(impl, U, B, dt)
+    U2o, B2o = oracle_lib.step(oracle_lib.Mesh.from_block_mesh(mesh), oracle_settings(oracle_lib, st), U, B, dt)
+    n = mesh.n_owned
+    assert np.array_equal(U2[:n], U2o[:n]) and np.array_equal(B2[:n], B2o[:n])
+    impl.close()
+    empty = BlockMesh(dim=2, block=(16, 16, 1), level=np.zeros(0, np.int32), neighbor=np.zeros((0, 27), np.int32),
+                      coords=np.zeros((0, 3), np.int64), n_owned=0, grid=(1, 1, 1), periodic=(True, True, True))
+    impl = GodunovImplemGB300(st, empty, precision="mixed")
+    x = torch.zeros(16, dtype=torch.float64, device="cuda")
+    tile, _ = impl.autotune(x, x.clone(), x.clone(), x.clone(), 1e-3)
+    assert tile in (16, 8, 4)
+    impl.close()
