@@ -232,8 +232,9 @@ int gmhd_inv_dt_noalloc(const gmhd_params * params, int32_t dim, int32_t bx, int
  * precision and block size (x extents 8 and 4 in 3D, 16, 8 and 4 in 2D, where they divide the block),
  * two warm-up and five timed launches each on `stream`, and keeps the fastest for the context's
  * later steps, across gmhd_set_mesh calls with the same block size (the coarse/fine tile lists are
- * rebuilt for it). Results do not depend on the tile. Writes the chosen x extent and its time per step
- * in ms (either pointer may be NULL). Synchronises the device. */
+ * rebuilt for it). FP64 results do not depend on the tile; mixed-precision ones may differ in the last
+ * FP32 bits (each tile is a separately compiled kernel). Writes the chosen x extent and its time per
+ * step in ms (either pointer may be NULL). Synchronises the device. */
 int gmhd_autotune(gmhd_ctx * ctx, const double * U, double * U2, const double * B, double * B2, double dt,
                   int32_t * tile_out, double * ms_out, void * stream);
 /* Sets the tile request by hand: an x extent from the list above (one that does not divide the block
