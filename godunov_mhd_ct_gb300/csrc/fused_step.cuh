@@ -1074,11 +1074,7 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
 
   int * s_kind = s_kind0 + (C::PIPE ? 32 * buf : 0);
   if constexpr (C::PIPE)
-  {
     cp_async_wait_all(); // this tile's staged gather (issued during the previous tile)
-    if (tid == 0)
-      s_health = s_stage_health[buf];
-  }
   else
   {
     if (tid < 32)
@@ -1104,6 +1100,11 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
   }
   __syncthreads();
   const unsigned jump_mask = s_stage_jump[C::PIPE ? buf : 0];
+  // the staging flags of this tile, read after the barrier: the threads that issued the staging may have
+  // gone straight to this tile (skip and side-data-only paths) without one in between
+  if constexpr (C::PIPE)
+    if (tid == 0)
+      s_health = s_stage_health[buf];
 
   const int myprob = a.problem ? a.problem[blk] : 0;
   const int mylevel = a.level[blk];
