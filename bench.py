@@ -31,10 +31,26 @@ METRIC = "cell-updates/s on 1 GB300, mixed vs FP64 at L1(rho)<=1e-6; % of HBM ro
 UNIT = "cell-updates/s"
 BYTES_PER_CELL_UPDATE = 128.0  # read U(5)+B(3), write U2(5)+B2(3), FP64
 FALLBACK_HBM_GBS = 6800.0
-# DRAM bytes (read + write) of one mixed fused-step launch on the full 256^3 workload: the 128^3
-# capture summarised in profiles/fused_step_mixed_ot3d.md (266.3 MB for 2,097,152 cells) scaled by
-# the cell count (x8); traffic grows in proportion to the cells processed
-MEASURED_TRAFFIC_BYTES = 266.3e6 * 8
+# ncu counters of one mixed fused-step launch on a small case (key value lines: cells, dram bytes,
+# warp instructions); per-cell figures scale to the full launch by the cell count
+COUNTERS = os.path.join("profiles", "fused_step_mixed_ot3d_counters.txt")
+
+
+def read_counters(path=COUNTERS):
+    """Per-cell DRAM bytes and warp instructions of the dominant kernel from a committed ncu capture,
+    or None when the file is absent."""
+    try:
+        vals = {}
+        with open(os.path.join(ROOT, path)) as f:
+            for line in f:
+                line = line.split("#", 1)[0].split()
+                if len(line) == 2:
+                    vals[line[0]] = float(line[1])
+        cells = vals["cells"]
+        return {"dram_bytes_per_cell": (vals["dram_read_bytes"] + vals["dram_write_bytes"]) / cells,
+                "warp_inst_per_cell": vals["warp_instructions"] / cells, "source": path}
+    except (OSError, KeyError, ValueError):
+        return None
 
 
 def hbm_peak():
@@ -135,14 +151,14 @@ def settings():
     return MHDSettings(gamma0=5.0 / 3.0, cfl=0.5, slope_type=2.0, riemann="HLLD")
 
 
-def cpu_baseline_run(steps, warmup, seconds_cap=25.0):
+def cpu_baseline_run(steps, warmup, seconds_cap=25.0, side_blocks=8):
     """Time the FP64 oracle (the CPU restatement of the reference stage, OpenMP over blocks) on all host
-    cores on a 128^3 sample (64 blocks of 32^3, so that every core has blocks) of the same Orszag-Tang
-    workload: solver iterations (CFL + step) in one call, as many as fit in seconds_cap."""
+    cores on the same Orszag-Tang workload (256^3: 512 blocks of 32^3 by default): warm-up iterations,
+    then solver iterations (CFL + step) in one call, as many as fit in seconds_cap (at least one)."""
     from oracle import oracle as orc
 
     orc.build()
-    mesh, U, B = make_workload(side_blocks=4, block=32)
+    mesh, U, B = make_workload(side_blocks=side_blocks, block=32)
     st = settings()
     om = orc.Mesh(3, 32, 32, 32, mesh.level, mesh.neighbor, mesh.n_owned)
     os_ = orc.settings(gamma0=st.gamma0, cfl=st.cfl, slope_type=st.slope_type, riemann=st.riemann_id)
@@ -157,22 +173,23 @@ def cpu_baseline_run(steps, warmup, seconds_cap=25.0):
     orc.run(om, os_, U, B, done)
     el = time.perf_counter() - t0
     cells = mesh.n_owned * mesh.ncell
+    side = side_blocks * 32
     return {"value": cells * done / el, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-            "sample": f"3D Orszag-Tang 128^3 (64 blocks of 32^3), {done} oracle solver iterations in one call, "
-                      f"FP64, OpenMP over blocks",
-            "ms_per_step": 1e3 * el / done, "steps": done}
+            "sample": f"3D Orszag-Tang {side}^3 ({mesh.n_owned} blocks of 32^3), {done} oracle solver iterations "
+                      f"in one call after {max(warmup, 1)} warm-up, FP64, OpenMP over blocks",
+            "ms_per_step": 1e3 * el / done, "steps": done, "workload": f"3d_orszag_tang_{side}^3"}
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    cb = cpu_baseline_run(args.steps, args.warmup, seconds_cap=120.0)
+    cb = cpu_baseline_run(args.steps, min(args.warmup, 2), seconds_cap=120.0, side_blocks=args.side_blocks)
     line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": cb["steps"], "warmup": args.warmup, "ms_per_step": cb["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "3d_orszag_tang_256^3 (CPU sample: 128^3, 64 blocks of 32^3)",
+            "config": {"workload": cb["workload"],
                        "note": "the reference's Kokkos build needs kalypsso-core/Kokkos/p4est (absent); this arm "
-                               "times the FP64 CPU restatement of its stage"},
+                               "times the FP64 CPU restatement of its stage on the same workload"},
             "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -259,6 +276,7 @@ def main():
     kern_ms = k0.elapsed_time(k1) / nk
     peak, peak_src = hbm_peak()
     achieved = BYTES_PER_CELL_UPDATE * cells / (kern_ms * 1e-3) / 1e9
+    n_sm = torch.cuda.get_device_properties(local_rank).multi_processor_count
 
     out = {}
     if rank == 0:
@@ -306,40 +324,60 @@ def main():
         from godunov_mhd_ct_gb300 import _native as nat
 
         L = nat.lib()
-        ne = 5
-        L.gmhd_step_host(mixed._ctx, hU.data_ptr(), hU2.data_ptr(), hB.data_ptr(), hB2.data_ptr(), dt_fixed, None)
+        cstream = torch.cuda.current_stream()
+        sp = ctypes.c_void_p(cstream.cuda_stream)
+
+        def host_step(a_u, a_b, b_u, b_b, asynchronous):
+            fn = L.gmhd_step_host_async if asynchronous else L.gmhd_step_host
+            nat.check(fn(mixed._ctx, a_u.data_ptr(), b_u.data_ptr(), a_b.data_ptr(), b_b.data_ptr(),
+                         ctypes.c_double(dt_fixed), sp), "gmhd_step_host")
+
+        # dependent chain: every step's input is the previous step's host output (a solver that keeps its
+        # state in host memory); the call copies U, B in, steps and copies U2, B2 out before returning
+        ne = 6
+        host_step(hU, hB, hU2, hB2, False)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for _ in range(ne):
-            nat.check(L.gmhd_step_host(mixed._ctx, hU.data_ptr(), hU2.data_ptr(), hB.data_ptr(), hB2.data_ptr(),
-                                       ctypes.c_double(dt_fixed), None), "gmhd_step_host")
-        e2e_sync_s = (time.perf_counter() - t0) / ne
-        # stream-ordered variant: each step still copies its inputs in and its result out inside the timed
-        # region; consecutive steps overlap copy-in, step and copy-out (two device staging sets)
+        bufs = [(hU, hB), (hU2, hB2)]
+        for k in range(ne):
+            (a_u, a_b), (b_u, b_b) = bufs[k % 2], bufs[(k + 1) % 2]
+            host_step(a_u, a_b, b_u, b_b, False)
+        e2e_dep_s = (time.perf_counter() - t0) / ne
+        # independent steps (each step copies the same host input in and its result out), stream-ordered:
+        # the copy-in, the step and the copy-out of consecutive steps overlap
+        hU.copy_(torch.from_numpy(U))
+        hB.copy_(torch.from_numpy(B))
         ne_async = 10
-        stream = torch.cuda.current_stream()
         for _ in range(2):
-            nat.check(L.gmhd_step_host_async(mixed._ctx, hU.data_ptr(), hU2.data_ptr(), hB.data_ptr(), hB2.data_ptr(),
-                                             ctypes.c_double(dt_fixed), ctypes.c_void_p(stream.cuda_stream)),
-                      "gmhd_step_host_async")
+            host_step(hU, hB, hU2, hB2, True)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(ne_async):
-            nat.check(L.gmhd_step_host_async(mixed._ctx, hU.data_ptr(), hU2.data_ptr(), hB.data_ptr(), hB2.data_ptr(),
-                                             ctypes.c_double(dt_fixed), ctypes.c_void_p(stream.cuda_stream)),
-                      "gmhd_step_host_async")
+            host_step(hU, hB, hU2, hB2, True)
         torch.cuda.synchronize()
-        e2e_s = (time.perf_counter() - t0) / ne_async
-        out["e2e"] = {"value": cells / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(U.nbytes + B.nbytes),
+        e2e_ind_s = (time.perf_counter() - t0) / ne_async
+        out["e2e"] = {"value": cells / e2e_dep_s, "unit": UNIT, "h2d_bytes_per_step": int(U.nbytes + B.nbytes),
                       "d2h_bytes_per_step": int(U[:n].nbytes + B[:n].nbytes),
-                      "path": "gmhd_step_host_async (C ABI, pinned host buffers; copy-in, step and copy-out of "
-                              "consecutive steps overlap), mixed precision, dt fixed",
-                      "sync_value": cells / e2e_sync_s,
-                      "sync_path": "gmhd_step_host (copy in, step, copy out, wait; no overlap)"}
+                      "path": "gmhd_step_host (C ABI, pinned host buffers): copy in, step, copy out, return; a "
+                              "dependent chain, each step's input the previous step's host output; mixed, dt fixed",
+                      "independent_value": cells / e2e_ind_s,
+                      "independent_path": "gmhd_step_host_async: independent steps on the same host input, copy-in, "
+                                          "step and copy-out of consecutive steps overlapped"}
         if not args.no_cpu_baseline and world == 1:
-            cb = cpu_baseline_run(steps=1000, warmup=1, seconds_cap=15.0)
+            cb = cpu_baseline_run(steps=1000, warmup=1, seconds_cap=15.0, side_blocks=args.side_blocks)
             out["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
 
+        ctr = read_counters()
+        kern_name = f"fused_step_kernel<float,3,{tile},{tile},{tile}> (mixed, persistent)"
+        issue = None
+        if ctr and clk.get("sm_mhz"):
+            # warp instructions per cell (ncu) x cells / launch time, against 4 issue slots per SM per clock
+            inst = ctr["warp_inst_per_cell"] * cells
+            peak_issue = n_sm * 4 * clk["sm_mhz"] * 1e6
+            issue = {"bound": "issue", "achieved": inst / (kern_ms * 1e-3), "peak": peak_issue,
+                     "unit": "warp-instructions/s", "frac": inst / (kern_ms * 1e-3) / peak_issue,
+                     "warp_inst_per_cell": ctr["warp_inst_per_cell"], "sms": n_sm, "sm_mhz": clk["sm_mhz"],
+                     "source": ctr["source"]}
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -348,9 +386,14 @@ def main():
                        "block": list(mesh.block), "ghost": 2, "precision": "mixed", "riemann": "HLLD",
                        "slope": "MC", "cfl": st.cfl, "l2": "inputs (2.2 GB) larger than L2 (129 MB); no flush"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": MEASURED_TRAFFIC_BYTES, "peak_source": peak_src,
-                         "kernel": "fused_step_kernel<float,3,8,8,8>", "kernel_ms": kern_ms,
-                         "bytes_per_launch": BYTES_PER_CELL_UPDATE * cells},
+                         "frac": achieved / peak,
+                         "traffic": ctr["dram_bytes_per_cell"] * cells if ctr else None,
+                         "traffic_source": (ctr["source"] + " (ncu dram__bytes_read.sum + dram__bytes_write.sum of "
+                                            "a small case, per cell, times the cells of this launch)") if ctr else None,
+                         "peak_source": peak_src, "kernel": kern_name, "kernel_ms": kern_ms,
+                         "bytes_per_launch": BYTES_PER_CELL_UPDATE * cells,
+                         "limiter": "instruction issue (see issue_roofline), not HBM"},
+            "issue_roofline": issue,
             "gpu_launches": 2 * args.steps,
             "clocks": clk,
         }

@@ -10,8 +10,8 @@
 //
 // Template Cfg: compute type R (double: the FP64 drop-in, float: the mixed path), dimension,
 // tile extents and threads per CTA. EXACT selects the reference's FP64 accumulation order for
-// U2 (three rounded per-direction adds); otherwise the three direction increments are summed in
-// R and added once to U in FP64.
+// U2 (three rounded per-direction adds); otherwise the face terms are summed error-free in FP32
+// (TwoSum: a sum and its rounding error) and both are added to U in FP64.
 #pragma once
 
 #include <cstdint>
@@ -1948,10 +1948,13 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
 #pragma unroll
     for (int v = 0; v < C::NFV; ++v)
       u2[v] = upre[c][v];
-    R dU[C::NFV];
+    // mixed path: the 2 DIM face terms of each variable are summed without rounding loss (TwoSum into
+    // a sum and an error term, both FP32), then added to the FP64 state as two FP64 adds, so that the
+    // flux a face gives one cell and takes from the other cancel in the totals to FP64 round-off
+    float dU[C::NFV], eU[C::NFV];
 #pragma unroll
     for (int v = 0; v < C::NFV; ++v)
-      dU[v] = R(0);
+      dU[v] = eU[v] = 0.0f;
 #pragma unroll
     for (int dir = 0; dir < DIM; ++dir)
     {
@@ -1974,20 +1977,28 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
 #pragma unroll
       for (int v = 0; v < C::NFV; ++v)
       {
-        R acc = R(0);
-        acc = acc + fl[v * C::NFT + fL];
-        acc = acc - fl[v * C::NFT + fR];
         if constexpr (C::EXACT)
+        {
+          R acc = R(0);
+          acc = acc + fl[v * C::NFT + fL];
+          acc = acc - fl[v * C::NFT + fR];
           u2[v] += (double)acc;
+        }
         else
-          dU[v] += acc;
+        {
+          if (dir == 0)
+            dU[v] = fl[v * C::NFT + fL];
+          else
+            two_sum_acc(dU[v], eU[v], fl[v * C::NFT + fL]);
+          two_sum_acc(dU[v], eU[v], -fl[v * C::NFT + fR]);
+        }
       }
     }
     if constexpr (!C::EXACT)
     {
 #pragma unroll
       for (int v = 0; v < C::NFV; ++v)
-        u2[v] += to_d<R>(dU[v]);
+        u2[v] = (u2[v] + to_d<float>(dU[v])) + to_d<float>(eU[v]);
     }
     if constexpr (C::VISC)
     {

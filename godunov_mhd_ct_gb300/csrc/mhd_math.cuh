@@ -78,6 +78,41 @@ cfl_inv_dt_fp64(int dim, double vx, double vy, double vz, double dx, double rho,
   return val;
 }
 
+// compute_cfl (scheme/ComputeDtMHDFunctor.cpp:86-151) of cell (i, j, k) of one block in the C-ABI
+// layout, FP64 with the reference operand order: face B averaged to the cell centre, primitive
+// recovery (models/mhd_utils.h:449-515), fast speeds (find_speed_info, :340-394), then
+// cfl_inv_dt_fp64. Ub / Bb point at the block's U and face arrays; c is the cell's index in the block.
+// Units that call it are compiled with --fmad=false, so every caller gets the same bits.
+__device__ __forceinline__ double
+cell_inv_dt_fp64(const double * __restrict__ Ub, const double * __restrict__ Bb, int dim, int bx, int by, int i,
+                 int j, int k, int64_t c, int64_t ncell, int64_t nfx, int64_t nfy, double dx, double gamma0,
+                 double smallr, double smallp, const Sources & src)
+{
+  const double Ax = 0.5 * (Bb[i + (int64_t)(bx + 1) * (j + (int64_t)by * k)] +
+                           Bb[i + 1 + (int64_t)(bx + 1) * (j + (int64_t)by * k)]);
+  const double Ay = 0.5 * (Bb[nfx + i + (int64_t)bx * (j + (int64_t)(by + 1) * k)] +
+                           Bb[nfx + i + (int64_t)bx * (j + 1 + (int64_t)(by + 1) * k)]);
+  double Az;
+  if (dim == 3)
+    Az = 0.5 * (Bb[nfx + nfy + i + (int64_t)bx * (j + (int64_t)by * k)] +
+                Bb[nfx + nfy + i + (int64_t)bx * (j + (int64_t)by * (k + 1))]);
+  else
+    Az = 0.5 * (Bb[nfx + nfy + c] + Bb[nfx + nfy + c]);
+  const double r = fmax(Ub[c], smallr);
+  const double vx = Ub[2 * ncell + c] / r, vy = Ub[3 * ncell + c] / r, vz = Ub[4 * ncell + c] / r;
+  const double eken = 0.5 * (vx * vx + vy * vy + vz * vz);
+  const double emag = 0.5 * (Ax * Ax + Ay * Ay + Az * Az);
+  const double eint = (Ub[ncell + c] - emag) / r - eken;
+  const double p = fmax((gamma0 - 1.0) * r * eint, r * smallp);
+  const double b2 = Ax * Ax + Ay * Ay + Az * Az;
+  const double c2 = gamma0 * p / r;
+  const double d2 = 0.5 * (b2 / r + c2);
+  const double cfx = sqrt(d2 + sqrt(d2 * d2 - c2 * Ax * Ax / r)) + fabs(vx);
+  const double cfy = sqrt(d2 + sqrt(d2 * d2 - c2 * Ay * Ay / r)) + fabs(vy);
+  const double cfz = dim == 3 ? sqrt(d2 + sqrt(d2 * d2 - c2 * Az * Az / r)) + fabs(vz) : 0.0;
+  return cfl_inv_dt_fp64(dim, cfx, cfy, cfz, dx, Ub[c], src);
+}
+
 // FP32 estimate of cfl_inv_dt_fp64 for the mixed path. The gravity factor is evaluated as
 // (sqrt(1 + 2k) + 1) / 2, equal to k / (sqrt(1 + 2k) - 1) but without its cancellation at small k.
 __device__ __forceinline__ float
@@ -828,6 +863,20 @@ f2d_bits(float x)
   hi = e == 0u ? sign : hi;
   lo = e == 0u ? 0u : lo;
   return __hiloint2double((int)hi, (int)lo);
+}
+
+// Adds t to the running sum s and the rounding error of that addition to e (Knuth's TwoSum: six
+// FP32 operations, no branch, valid for any magnitudes; no multiply, so FMA contraction cannot
+// change it). After the last term, s + e holds the exact sum of the terms up to the rounding of e
+// itself, which is of order eps^2 relative to the terms.
+__device__ __forceinline__ void
+two_sum_acc(float & s, float & e, float t)
+{
+  const float u = s + t;
+  const float tb = u - s;
+  const float err = (s - (u - tb)) + (t - tb);
+  s = u;
+  e += err;
 }
 
 template <typename R>

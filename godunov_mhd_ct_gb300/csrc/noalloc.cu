@@ -7,12 +7,15 @@
 // needs neither: the caller passes the state (U, B), the per-block problem ids (or none) and a
 // device output buffer, and the reduction accumulator lives in the fixed array below.
 //
-// The array g_inv_dt_scratch has GMHD_NOALLOC_MAX_PROBLEMS 64-bit slots (8 KB). Every GPU that
-// loads this library holds it until the process exits. All calls on a device share it and it keeps
-// the last call's contents, so each call clears the slots it uses before reducing into them; calls
-// that overlap on the GPU (on different streams, without ordering between them) race on it.
-// Compiled with --fmad=false: the per-cell arithmetic is the FP64 reference formula order, so the
-// result equals gmhd_inv_dt's.
+// The array g_inv_dt_scratch has GMHD_NOALLOC_MAX_PROBLEMS 64-bit slots (8 KB) plus one flag slot.
+// Every GPU that loads this library holds it until the process exits. All calls on a device share it
+// and it keeps the last call's contents, so each call clears the slots it uses (and the flag) before
+// reducing into them; calls that overlap on the GPU (on different streams, without ordering between
+// them) race on it. A block whose problem id is outside [0, n_problems) is skipped and sets the flag
+// slot, and the call then writes NaN to every output: the ids live on the device, so the host cannot
+// check them without a copy, and the kernel never indexes the array with them.
+// Compiled with --fmad=false and sharing cell_inv_dt_fp64 with gmhd_inv_dt, so the result equals
+// gmhd_inv_dt's.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -23,22 +26,22 @@
 
 namespace
 {
-using gmhd::cfl_inv_dt_fp64;
 using gmhd::Sources;
 
-__device__ __align__(256) unsigned long long g_inv_dt_scratch[GMHD_NOALLOC_MAX_PROBLEMS];
+// [0, GMHD_NOALLOC_MAX_PROBLEMS): per-problem maxima; [GMHD_NOALLOC_MAX_PROBLEMS]: bad-id flag
+constexpr int kFlagSlot = GMHD_NOALLOC_MAX_PROBLEMS;
+__device__ __align__(256) unsigned long long g_inv_dt_scratch[GMHD_NOALLOC_MAX_PROBLEMS + 1];
 
 constexpr int kMaxDevices = 64;
 std::mutex    g_setup_mutex;
 void *        g_scratch_addr[kMaxDevices] = {};
 
-// Device address of g_inv_dt_scratch on the current device. Host code cannot use the symbol
-// itself (its host-side name is only a stand-in), so the address is looked up once per device.
+// Device address of g_inv_dt_scratch on device `dev` (the current device). Host code cannot use the
+// symbol itself (its host-side name is only a stand-in), so the address is looked up once per device.
 int
-scratch_address(void ** out)
+scratch_address(int dev, void ** out)
 {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+  if (dev < 0 || dev >= kMaxDevices)
     return GMHD_ERR_CUDA;
   std::lock_guard<std::mutex> lock(g_setup_mutex);
   if (!g_scratch_addr[dev])
@@ -52,52 +55,42 @@ scratch_address(void ** out)
   return GMHD_OK;
 }
 
+// Clears slots [0, n) and the bad-id flag.
 __global__ void
 clear_slots_kernel(unsigned long long * slots, int n)
 {
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
     slots[p] = 0ull;
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    slots[kFlagSlot] = 0ull;
 }
 
 // compute_cfl (scheme/ComputeDtMHDFunctor.cpp:86-151) per owned cell, one CTA per block, max per
-// problem into slots[]. All blocks at one level (cell size dx).
+// problem into slots[]. All blocks at one level (cell size dx). A block whose problem id is not in
+// [0, np) does no work and sets the flag slot.
 __global__ void __launch_bounds__(256)
 inv_dt_noalloc_kernel(const double * __restrict__ U, const double * __restrict__ B,
-                      const int32_t * __restrict__ problem, int dim, int bx, int by, int bz, int64_t ncell,
+                      const int32_t * __restrict__ problem, int np, int dim, int bx, int by, int bz, int64_t ncell,
                       int64_t nfx, int64_t nfy, int64_t nface, double dx, double gamma0, double smallr,
                       double smallp, Sources src, unsigned long long * slots)
 {
-  const int     blk = blockIdx.x;
+  const int blk = blockIdx.x;
+  const int pid = problem ? problem[blk] : 0;
+  if ((unsigned)pid >= (unsigned)np)
+  {
+    // uniform over the CTA: every thread leaves before any barrier
+    if (threadIdx.x == 0)
+      atomicExch(&slots[kFlagSlot], 1ull);
+    return;
+  }
   const double *Ub = U + (int64_t)blk * 5 * ncell;
   const double *Bb = B + (int64_t)blk * nface;
   double        m = 0.0;
   for (int64_t c = threadIdx.x; c < ncell; c += blockDim.x)
   {
     const int i = (int)(c % bx), j = (int)((c / bx) % by), k = (int)(c / ((int64_t)bx * by));
-    const double Ax = 0.5 * (Bb[i + (int64_t)(bx + 1) * (j + (int64_t)by * k)] +
-                             Bb[i + 1 + (int64_t)(bx + 1) * (j + (int64_t)by * k)]);
-    const double Ay = 0.5 * (Bb[nfx + i + (int64_t)bx * (j + (int64_t)(by + 1) * k)] +
-                             Bb[nfx + i + (int64_t)bx * (j + 1 + (int64_t)(by + 1) * k)]);
-    double Az;
-    if (dim == 3)
-      Az = 0.5 * (Bb[nfx + nfy + i + (int64_t)bx * (j + (int64_t)by * k)] +
-                  Bb[nfx + nfy + i + (int64_t)bx * (j + (int64_t)by * (k + 1))]);
-    else
-      Az = 0.5 * (Bb[nfx + nfy + c] + Bb[nfx + nfy + c]);
-    // compute_primitives (models/mhd_utils.h:449-515) and find_speed_info (:340-394)
-    const double r = fmax(Ub[c], smallr);
-    const double vx = Ub[2 * ncell + c] / r, vy = Ub[3 * ncell + c] / r, vz = Ub[4 * ncell + c] / r;
-    const double eken = 0.5 * (vx * vx + vy * vy + vz * vz);
-    const double emag = 0.5 * (Ax * Ax + Ay * Ay + Az * Az);
-    const double eint = (Ub[ncell + c] - emag) / r - eken;
-    const double p = fmax((gamma0 - 1.0) * r * eint, r * smallp);
-    const double b2 = Ax * Ax + Ay * Ay + Az * Az;
-    const double c2 = gamma0 * p / r;
-    const double d2 = 0.5 * (b2 / r + c2);
-    const double cfx = sqrt(d2 + sqrt(d2 * d2 - c2 * Ax * Ax / r)) + fabs(vx);
-    const double cfy = sqrt(d2 + sqrt(d2 * d2 - c2 * Ay * Ay / r)) + fabs(vy);
-    const double cfz = dim == 3 ? sqrt(d2 + sqrt(d2 * d2 - c2 * Az * Az / r)) + fabs(vz) : 0.0;
-    m = fmax(m, cfl_inv_dt_fp64(dim, cfx, cfy, cfz, dx, Ub[c], src));
+    m = fmax(m, gmhd::cell_inv_dt_fp64(Ub, Bb, dim, bx, by, i, j, k, c, ncell, nfx, nfy, dx, gamma0, smallr, smallp,
+                                       src));
   }
   __shared__ double red[8];
 #pragma unroll
@@ -111,15 +104,17 @@ inv_dt_noalloc_kernel(const double * __restrict__ U, const double * __restrict__
     for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
       m = fmax(m, red[w]);
     // positive doubles order like their bit patterns
-    atomicMax(&slots[problem ? problem[blk] : 0], (unsigned long long)__double_as_longlong(m));
+    atomicMax(&slots[pid], (unsigned long long)__double_as_longlong(m));
   }
 }
 
+// Per-problem results, or NaN everywhere when some block had a problem id out of range.
 __global__ void
 write_out_kernel(const unsigned long long * slots, double * out, int n)
 {
+  const bool bad = slots[kFlagSlot] != 0ull;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
-    out[p] = __longlong_as_double((long long)slots[p]);
+    out[p] = bad ? __longlong_as_double(0x7ff8000000000000LL) : __longlong_as_double((long long)slots[p]);
 }
 } // namespace
 
@@ -138,12 +133,18 @@ gmhd_inv_dt_noalloc(const gmhd_params * params, int32_t dim, int32_t bx, int32_t
     return GMHD_ERR_ARGUMENT;
   if (np > GMHD_NOALLOC_MAX_PROBLEMS)
     return GMHD_ERR_TOO_LARGE;
+  cudaStream_t s = (cudaStream_t)stream;
+  // the array looked up below is the current device's: the stream must belong to that device
+  int dev = -1, sdev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess)
+    return GMHD_ERR_CUDA;
+  if (s && (cudaStreamGetDevice(s, &sdev) != cudaSuccess || sdev != dev))
+    return GMHD_ERR_ARGUMENT;
   void * addr = nullptr;
-  int    rc = scratch_address(&addr);
+  int    rc = scratch_address(dev, &addr);
   if (rc != GMHD_OK)
     return rc;
   unsigned long long * slots = static_cast<unsigned long long *>(addr);
-  cudaStream_t         s = (cudaStream_t)stream;
   const int64_t        ncell = (int64_t)bx * by * bz;
   const int64_t        nfx = (int64_t)(bx + 1) * by * bz;
   const int64_t        nfy = (int64_t)bx * (by + 1) * bz;
@@ -158,9 +159,12 @@ gmhd_inv_dt_noalloc(const gmhd_params * params, int32_t dim, int32_t bx, int32_t
   src.viscosity = params->viscosity_enabled != 0;
   src.mu = src.viscosity ? params->viscosity_mu : 0.0;
   src.visc_predictor = 0;
+  // an error left by earlier, unrelated work is not this call's: clear it so that the check after the
+  // launches reports only these
+  (void)cudaGetLastError();
   clear_slots_kernel<<<(np + 255) / 256, 256, 0, s>>>(slots, np);
   if (n_blocks > 0)
-    inv_dt_noalloc_kernel<<<n_blocks, 256, 0, s>>>(U, B, problem, dim, bx, by, bz, ncell, nfx, nfy, nface, dx,
+    inv_dt_noalloc_kernel<<<n_blocks, 256, 0, s>>>(U, B, problem, np, dim, bx, by, bz, ncell, nfx, nfy, nface, dx,
                                                    params->gamma0, params->smallr, smallp, src, slots);
   write_out_kernel<<<(np + 255) / 256, 256, 0, s>>>(slots, inv_dt, np);
   return cudaGetLastError() == cudaSuccess ? GMHD_OK : GMHD_ERR_CUDA;

@@ -116,29 +116,7 @@ inv_dt_kernel(const double * __restrict__ U, const double * __restrict__ B, cons
   for (int64_t c = threadIdx.x; c < ncell; c += blockDim.x)
   {
     const int i = (int)(c % bx), j = (int)((c / bx) % by), k = (int)(c / ((int64_t)bx * by));
-    const double Ax = 0.5 * (Bb[i + (int64_t)(bx + 1) * (j + (int64_t)by * k)] +
-                             Bb[i + 1 + (int64_t)(bx + 1) * (j + (int64_t)by * k)]);
-    const double Ay = 0.5 * (Bb[nfx + i + (int64_t)bx * (j + (int64_t)(by + 1) * k)] +
-                             Bb[nfx + i + (int64_t)bx * (j + 1 + (int64_t)(by + 1) * k)]);
-    double Az;
-    if (dim == 3)
-      Az = 0.5 * (Bb[nfx + nfy + i + (int64_t)bx * (j + (int64_t)by * k)] +
-                  Bb[nfx + nfy + i + (int64_t)bx * (j + (int64_t)by * (k + 1))]);
-    else
-      Az = 0.5 * (Bb[nfx + nfy + c] + Bb[nfx + nfy + c]);
-    const double r = fmax(Ub[c], smallr);
-    const double vx = Ub[2 * ncell + c] / r, vy = Ub[3 * ncell + c] / r, vz = Ub[4 * ncell + c] / r;
-    const double eken = 0.5 * (vx * vx + vy * vy + vz * vz);
-    const double emag = 0.5 * (Ax * Ax + Ay * Ay + Az * Az);
-    const double eint = (Ub[ncell + c] - emag) / r - eken;
-    const double p = fmax((gamma0 - 1.0) * r * eint, r * smallp);
-    const double b2 = Ax * Ax + Ay * Ay + Az * Az;
-    const double c2 = gamma0 * p / r;
-    const double d2 = 0.5 * (b2 / r + c2);
-    const double cfx = sqrt(d2 + sqrt(d2 * d2 - c2 * Ax * Ax / r)) + fabs(vx);
-    const double cfy = sqrt(d2 + sqrt(d2 * d2 - c2 * Ay * Ay / r)) + fabs(vy);
-    const double cfz = dim == 3 ? sqrt(d2 + sqrt(d2 * d2 - c2 * Az * Az / r)) + fabs(vz) : 0.0;
-    m = fmax(m, cfl_inv_dt_fp64(dim, cfx, cfy, cfz, dx, Ub[c], src));
+    m = fmax(m, cell_inv_dt_fp64(Ub, Bb, dim, bx, by, i, j, k, c, ncell, nfx, nfy, dx, gamma0, smallr, smallp, src));
   }
   __shared__ double red[8];
 #pragma unroll

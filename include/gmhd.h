@@ -221,8 +221,13 @@ int gmhd_advance(gmhd_ctx * ctx, double * U, double * U2, double * B, double * B
  * on `stream`. The reduction uses a fixed array of GMHD_NOALLOC_MAX_PROBLEMS slots in the library
  * (8 KB per GPU, held until the process exits); larger n_problems returns GMHD_ERR_TOO_LARGE.
  * The first call on each device looks that array up (cudaGetSymbolAddress); make that first call
- * before any stream capture. Calls share the array and clear their slots first; calls that
- * overlap on the GPU race on it. Results equal gmhd_inv_dt's. */
+ * before any stream capture. `stream` must belong to the current device (the array used is the
+ * current device's); a stream of another device returns GMHD_ERR_ARGUMENT. Problem ids are read on
+ * the device and never used as indices unchecked: a block whose id is outside [0, n_problems) is
+ * skipped and every inv_dt[p] of that call is NaN. The call clears a CUDA error left by earlier work
+ * (cudaGetLastError) before launching, so GMHD_ERR_CUDA reports only its own launches. Calls share
+ * the array and clear their slots first; calls that overlap on the GPU race on it. Results equal
+ * gmhd_inv_dt's. */
 int gmhd_inv_dt_noalloc(const gmhd_params * params, int32_t dim, int32_t bx, int32_t by, int32_t bz,
                         int32_t n_blocks, int32_t level, const int32_t * problem, int32_t n_problems,
                         const double * U, const double * B, double * inv_dt, void * stream);
