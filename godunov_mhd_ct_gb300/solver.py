@@ -162,10 +162,12 @@ class GodunovImplemGB300:
                                               _stream_ptr(stream)), "gmhd_refine_flags", self._ctx)
         return flags
 
-    def regrid(self, U, B, level_min: int, level_max: int, stream=None, **criterion):
+    def regrid(self, U, B, level_min: int, level_max: int, stream=None, flags=None, **criterion):
         """One AMR cycle: refinement flags on the device, mesh adaptation + 2:1 balance on the host
         (BlockMesh.adapt, p4est's part), remap of U and B on the device, new mesh tables
-        (resize_auxiliary_data). Returns (new mesh, new U, new B); U, B stay valid until released."""
+        (resize_auxiliary_data). ``flags`` (one per owned block) replaces the flags of the criterion,
+        e.g. to repeat another run's mesh sequence. Returns (new mesh, new U, new B); U, B stay valid
+        until released. The flags used are kept in ``last_flags``."""
         import time
 
         import torch
@@ -173,7 +175,13 @@ class GodunovImplemGB300:
         if self.n_problems != 1:
             raise ValueError("regrid works on single-problem meshes")
         t0 = time.perf_counter()
-        flags = self.refine_flags(U, B, level_min=level_min, level_max=level_max, stream=stream, **criterion)
+        if flags is None:
+            flags = self.refine_flags(U, B, level_min=level_min, level_max=level_max, stream=stream, **criterion)
+        else:
+            flags = np.ascontiguousarray(flags, dtype=np.int8).reshape(-1)
+            if flags.shape[0] != self.mesh.n_owned:
+                raise ValueError("flags need one entry per owned block")
+        self.last_flags = flags
         t1 = time.perf_counter()
         new_mesh, table = self.mesh.adapt(flags, level_min, level_max)
         t2 = time.perf_counter()

@@ -87,3 +87,47 @@ def same_level_face_mismatch(mesh: BlockMesh, B):
         b = np.take(F[right[ok]], 0, axis=3 - d)
         worst = max(worst, float(np.max(np.abs(a - b))))
     return worst
+
+
+def div_b_per_block(mesh: BlockMesh, B):
+    """Discrete divergence per owned cell with each block's own cell length (AMR meshes)."""
+    Bx, By, Bz = mesh.split_faces(np.asarray(B))
+    n = mesh.n_owned
+    d = (Bx[:n, ..., 1:] - Bx[:n, ..., :-1]) + (By[:n, :, 1:, :] - By[:n, :, :-1, :])
+    if mesh.dim == 3:
+        d = d + (Bz[:n, 1:] - Bz[:n, :-1])
+    return d / mesh.block_dx()[:n, None, None, None]
+
+
+def totals(mesh: BlockMesh, U):
+    """Volume integrals of rho and E over the owned blocks (cell volume dx^d per block)."""
+    n = mesh.n_owned
+    vol = mesh.block_dx()[:n] ** mesh.dim
+    U = np.asarray(U)
+    return float((U[:n, 0].reshape(n, -1).sum(axis=1) * vol).sum()), float((U[:n, 1].reshape(n, -1).sum(axis=1) * vol).sum())
+
+
+def accuracy_block(mesh0: BlockMesh, U0, mesh: BlockMesh, U, B, Uref, Bref):
+    """The per-result report: L1 relative error of rho, E and face B against (Uref, Bref) on the same
+    mesh, max |div B| of (U, B), and the relative drift of the rho and E integrals from the initial
+    state (mesh0, U0)."""
+    n = mesh.n_owned
+    U, B, Uref, Bref = (np.asarray(x) for x in (U, B, Uref, Bref))
+    m0, e0 = totals(mesh0, U0)
+    m1, e1 = totals(mesh, U)
+    return {"l1_rho": l1_rel(U[:n, 0], Uref[:n, 0]), "l1_E": l1_rel(U[:n, 1], Uref[:n, 1]),
+            "l1_B": l1_rel(B[:n], Bref[:n]), "max_divB": float(np.max(np.abs(div_b_per_block(mesh, B)))),
+            "mass_drift": abs(m1 - m0) / abs(m0), "energy_drift": abs(e1 - e0) / abs(e0)}
+
+
+def record(name, **values):
+    """Append a result line (JSON) to the file named by GMHD_RESULTS_LOG, when set, and print it."""
+    import json
+    import os
+
+    line = json.dumps({"case": name, **values}, default=float)
+    print(line)
+    path = os.environ.get("GMHD_RESULTS_LOG")
+    if path:
+        with open(path, "a") as f:
+            f.write(line + "\n")
