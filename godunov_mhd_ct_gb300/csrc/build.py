@@ -24,12 +24,14 @@ UNITS = {
     "step_fp64_visc.cu": ["--fmad=false"],
     "step_mixed.cu": ["--use_fast_math"],
     "step_mixed_visc.cu": ["--use_fast_math"],
+    "step_column.cu": ["--use_fast_math"],
     "gmhd_abi.cu": ["--fmad=false"],
     "noalloc.cu": ["--fmad=false"],
     "amr.cu": ["--fmad=false"],
     "forest.cpp": [],
 }
-HEADERS = ["mhd_math.cuh", "fused_step.cuh", "launch.cuh", os.path.join("..", "..", "include", "gmhd.h")]
+HEADERS = ["mhd_math.cuh", "fused_step.cuh", "column_step.cuh", "launch.cuh",
+           os.path.join("..", "..", "include", "gmhd.h")]
 
 
 def nvcc() -> str:

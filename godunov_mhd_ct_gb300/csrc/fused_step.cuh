@@ -446,18 +446,22 @@ amr_border_emf(const TileView<C> & t, const int * gi, int v0, int v1, typename C
     all_same = all_same && valid && kd[n] != RK_COARSER && kd[n] != RK_FINER;
   }
   double out = to_d<R>(val);
+  // The averages of copies of the same value are taken in FP64 (the FP64 path: as the reference, in
+  // its order). On the mixed path FP64 makes them exact for an FP32 value (k v / k == v), so a fine
+  // block's corrected edge equals the raw value its coarse neighbour reads back, and the coarse / fine
+  // face copies stay consistent; in FP32, (3 v) / 3 can differ from v by one ulp.
   if (coarser)
   {
-    R   acc = val;
-    int count = 1;
+    double acc = to_d<R>(val);
+    int    count = 1;
 #pragma unroll
     for (int n = 0; n < 3; ++n)
       if (kd[n] == RK_SAME)
       {
-        acc += val;
+        acc += to_d<R>(val);
         ++count;
       }
-    out = to_d<R>(acc / (R)count);
+    out = acc / (double)count;
   }
   else if (finer)
   {
@@ -500,17 +504,17 @@ amr_border_emf(const TileView<C> & t, const int * gi, int v0, int v1, typename C
   }
   if (all_same)
   {
-    R   acc = R(0);
-    int count = 1;
-    acc += val;
+    double acc = 0.0;
+    int    count = 1;
+    acc += to_d<R>(val);
 #pragma unroll
     for (int n = 0; n < 3; ++n)
       if (kd[n] != RK_OUTSIDE)
       {
-        acc += val;
+        acc += to_d<R>(val);
         ++count;
       }
-    out = to_d<R>(acc / (R)count);
+    out = acc / (double)count;
   }
   return out;
 }
@@ -1991,6 +1995,41 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
           else
             two_sum_acc(dU[v], eU[v], fl[v * C::NFT + fL]);
           two_sum_acc(dU[v], eU[v], -fl[v * C::NFT + fR]);
+        }
+      }
+    }
+    if constexpr (!C::EXACT && C::AMR)
+    {
+      // A face toward finer neighbours carries the FP64 sum of their fluxes / 2^d, held in the FP32
+      // flux array rounded to `hi`; its remainder lo = sum - hi joins the error-free sum here, so the
+      // coarse cell gains exactly what the fine cells lose
+      if (a.pass == 2)
+      {
+        const int lc[3] = {i, j, k};
+        const int org[3] = {x0, y0, z0};
+        const int bsz[3] = {bx, by, bz};
+#pragma unroll
+        for (int dir = 0; dir < DIM; ++dir)
+        {
+          const int t1 = dir == 0 ? 1 : 0, t2 = dir == 2 ? 1 : 2;
+          const int g1 = org[t1] + lc[t1], g2 = DIM == 3 ? org[t2] + lc[t2] : 0;
+          const int gc = org[dir] + lc[dir];
+#pragma unroll
+          for (int side = -1; side <= 1; side += 2)
+          {
+            if (side < 0 ? gc != 0 : gc != bsz[dir] - 1)
+              continue;
+            const int sl = nb_slot(dir == 0 ? side : 0, dir == 1 ? side : 0, dir == 2 ? side : 0);
+            if (s_kind[sl] != RK_FINER)
+              continue;
+#pragma unroll
+            for (int v = 0; v < C::NFV; ++v)
+            {
+              const double sum = fine_face_flux<C>(a, blk, sl, dir, side, g1, g2, v);
+              const float  lo = to_r<float>(sum - to_d<float>(to_r<float>(sum)));
+              two_sum_acc(dU[v], eU[v], side < 0 ? lo : -lo);
+            }
+          }
         }
       }
     }

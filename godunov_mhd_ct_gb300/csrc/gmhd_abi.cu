@@ -685,7 +685,7 @@ build_tile_lists(gmhd_ctx * ctx, int dim, const std::vector<int8_t> & kind)
 {
   int T[3];
   if (ctx->p.precision == GMHD_PRECISION_MIXED)
-    gmhd::tile_shape_mixed(dim, ctx->bx, ctx->by, ctx->bz, ctx->p.viscosity_enabled != 0, ctx->tile, T);
+    gmhd::tile_shape_mixed(dim, ctx->bx, ctx->by, ctx->bz, ctx->p.viscosity_enabled != 0, true, ctx->tile, T);
   else
     gmhd::tile_shape_fp64(dim, ctx->bx, ctx->by, ctx->bz, ctx->p.viscosity_enabled != 0, ctx->tile, T);
   const int              nt[3] = {ctx->bx / T[0], ctx->by / T[1], dim == 3 ? ctx->bz / T[2] : 1};
@@ -1143,7 +1143,7 @@ gmhd_autotune(gmhd_ctx * ctx, const double * U, double * U2, const double * B, d
   int       cand[3];
   const bool visc = ctx->p.viscosity_enabled != 0;
   const int n = ctx->p.precision == GMHD_PRECISION_MIXED
-                  ? gmhd::tile_candidates_mixed(ctx->dim, ctx->bx, ctx->by, ctx->bz, visc, cand)
+                  ? gmhd::tile_candidates_mixed(ctx->dim, ctx->bx, ctx->by, ctx->bz, visc, ctx->amr, cand)
                   : gmhd::tile_candidates_fp64(ctx->dim, ctx->bx, ctx->by, ctx->bz, visc, cand);
   if (n == 0)
     return GMHD_ERR_ARGUMENT;

@@ -70,12 +70,17 @@ int launch_step_fp64(const StepArgs & a, int dim, cudaStream_t stream);
 int launch_step_mixed(const StepArgs & a, int dim, cudaStream_t stream);
 int launch_step_fp64_visc(const StepArgs & a, int dim, cudaStream_t stream);
 int launch_step_mixed_visc(const StepArgs & a, int dim, cudaStream_t stream);
-// configured tiles (x extents, largest first) that divide these blocks; returns their count (<= 3)
+// configured tiles (x extents, largest first) that divide these blocks; returns their count (<= 3).
+// Mixed 3D without viscosity on a conforming mesh (amr false) also offers 16: the column step
+// (column_step.cuh, 16 x 8 columns through the block's z extent), listed after the 3D tiles.
 int tile_candidates_fp64(int dim, int bx, int by, int bz, bool visc, int * out);
-int tile_candidates_mixed(int dim, int bx, int by, int bz, bool visc, int * out);
-// the tile extents launch_step_* uses for these block sizes and request
+int tile_candidates_mixed(int dim, int bx, int by, int bz, bool visc, bool amr, int * out);
+// the tile extents launch_step_* uses for these block sizes and request (column step: 16, 8, bz)
 void tile_shape_fp64(int dim, int bx, int by, int bz, bool visc, int tile, int * t);
-void tile_shape_mixed(int dim, int bx, int by, int bz, bool visc, int tile, int * t);
+void tile_shape_mixed(int dim, int bx, int by, int bz, bool visc, bool amr, int tile, int * t);
+// column step (step_column.cu): -1 when it does not apply to these blocks / this mesh
+int launch_column(const StepArgs & a, cudaStream_t stream);
+int prepare_column();
 
 // the requested tile when it is a candidate, else the first (largest) candidate, 0 when none fits
 inline int

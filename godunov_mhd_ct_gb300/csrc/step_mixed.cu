@@ -22,9 +22,11 @@ int
 launch_step_mixed_cfg(const StepArgs & a, int dim, cudaStream_t stream)
 {
   int       cand[3];
-  const int x = pick_tile(cand, tile_candidates_mixed(dim, a.bx, a.by, a.bz, false, cand), a.tile);
+  const int x = pick_tile(cand, tile_candidates_mixed(dim, a.bx, a.by, a.bz, false, AMR, cand), a.tile);
   if (dim == 3)
   {
+    if (x == 16)
+      return launch_column(a, stream);
     if (x == 8)
       return launch_fused<std::conditional_t<AMR, MX_3D_888_AMR, MX_3D_888>>(a, stream);
     return launch_fused<std::conditional_t<AMR, MX_3D_444_AMR, MX_3D_444>>(a, stream);
@@ -45,16 +47,18 @@ launch_step_mixed(const StepArgs & a, int dim, cudaStream_t stream)
 }
 
 int
-tile_candidates_mixed(int dim, int bx, int by, int bz, bool visc, int * out)
+tile_candidates_mixed(int dim, int bx, int by, int bz, bool visc, bool amr, int * out)
 {
   int n = 0;
   if (dim == 3)
   {
-    // 8x8x8 tiles (8x8x4 with the viscous velocities), then 4x4x4
+    // 8x8x8 tiles (8x8x4 with the viscous velocities), then 4x4x4, then 16 x 8 columns
     if (bx % 8 == 0 && by % 8 == 0 && bz % (visc ? 4 : 8) == 0)
       out[n++] = 8;
     if (bx % 4 == 0 && by % 4 == 0 && bz % 4 == 0)
       out[n++] = 4;
+    if (!visc && !amr && bx % 16 == 0 && by % 8 == 0)
+      out[n++] = 16;
     return n;
   }
   for (int t : {16, 8, 4})
@@ -64,12 +68,19 @@ tile_candidates_mixed(int dim, int bx, int by, int bz, bool visc, int * out)
 }
 
 void
-tile_shape_mixed(int dim, int bx, int by, int bz, bool visc, int tile, int * t)
+tile_shape_mixed(int dim, int bx, int by, int bz, bool visc, bool amr, int tile, int * t)
 {
   int       cand[3];
-  const int x = pick_tile(cand, tile_candidates_mixed(dim, bx, by, bz, visc, cand), tile);
+  const int x = pick_tile(cand, tile_candidates_mixed(dim, bx, by, bz, visc, amr, cand), tile);
   if (dim == 3)
   {
+    if (x == 16)
+    {
+      t[0] = 16;
+      t[1] = 8;
+      t[2] = bz;
+      return;
+    }
     const int n = x == 8 ? 8 : 4;
     t[0] = t[1] = n;
     t[2] = visc ? 4 : n;
@@ -94,6 +105,7 @@ prepare_mixed()
   rc = rc ? rc : prepare_fused<MX_2D_16_AMR>();
   rc = rc ? rc : prepare_fused<MX_2D_8_AMR>();
   rc = rc ? rc : prepare_fused<MX_2D_4_AMR>();
+  rc = rc ? rc : prepare_column();
   return rc;
 }
 } // namespace gmhd

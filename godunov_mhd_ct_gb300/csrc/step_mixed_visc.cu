@@ -23,7 +23,7 @@ int
 launch_step_mixed_visc_cfg(const StepArgs & a, int dim, cudaStream_t stream)
 {
   int       cand[3];
-  const int x = pick_tile(cand, tile_candidates_mixed(dim, a.bx, a.by, a.bz, true, cand), a.tile);
+  const int x = pick_tile(cand, tile_candidates_mixed(dim, a.bx, a.by, a.bz, true, AMR, cand), a.tile);
   if (dim == 3)
   {
     if (x == 8)

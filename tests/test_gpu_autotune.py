@@ -42,7 +42,7 @@ def _step(impl, U, B, dt):
 
 CASES = [
     # dim, block, tiles the block admits
-    (3, (16, 16, 16), (8, 4)),
+    (3, (16, 16, 16), (8, 4, 16)),
     (2, (16, 16, 1), (16, 8, 4)),
 ]
 
@@ -110,7 +110,7 @@ def test_autotune_picks_a_configured_tile_and_keeps_it():
     dt = impl.compute_dt(dU, dB)
     ref = _step(impl, U, B, dt)
     tile, ms = impl.autotune(dU, dU2, dB, dB2, dt)
-    assert tile in (8, 4) and ms > 0.0
+    assert tile in (8, 4, 16) and ms > 0.0
     tuned = _step(impl, U, B, dt)
     _same("mixed", tuned, ref, mesh.n_owned)
     # a graph-replayed loop after the tuning (the cached graph is rebuilt for the chosen kernel), and a

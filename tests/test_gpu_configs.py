@@ -148,12 +148,17 @@ def test_config2_blast_amr_regrid_every_10_steps(oracle_lib):
             _, mU, mB = mix.regrid(mU, mB, lmin, lmax, flags=flag_log[c])
     assert mix.last_status() & ~16 == 0
     acc = accuracy_block(mesh0, U0, om, mU.cpu().numpy(), mB.cpu().numpy(), Uo, Bo)
+    acc64 = accuracy_block(mesh0, U0, om, Ug, Bg, Uo, Bo)
     record("config2_blast_amr_l5_10_500", fp64_bit_identical=exact, leaves_initial=mesh0.n_owned,
            leaves_min=min(sizes), leaves_max=max(sizes), leaves_final=n,
            levels_final=np.bincount(om.level[:n], minlength=lmax + 1)[lmin:].tolist(), mixed_vs_oracle=acc,
-           fp64_vs_oracle=accuracy_block(mesh0, U0, om, Ug, Bg, Uo, Bo))
-    _check_mixed(acc)
-    assert acc["mass_drift"] <= 1e-12 and acc["energy_drift"] <= 1e-12
+           fp64_vs_oracle=acc64)
+    # at coarse/fine borders the reference's EMF average (k v) / k differs from v by an FP64 ulp now and
+    # then, so div B grows with the steps on the FP64 path too (as in the oracle): the mixed path must
+    # stay at or below the FP64 path's level there
+    assert acc["l1_rho"] <= 1e-6
+    assert acc["max_divB"] <= max(1e-12, acc64["max_divB"])
+    assert acc["mass_drift"] <= 1e-13 and acc["energy_drift"] <= 1e-13
 
 
 def test_config3_field_loop_batch_1024(oracle_lib):
@@ -238,4 +243,9 @@ def test_config4_kelvin_helmholtz_3d_amr_100_steps(oracle_lib):
            levels=np.bincount(mesh.level[:n])[2:].tolist(), fp64_bit_identical=exact, mixed_vs_oracle=acc,
            fp64_vs_oracle=accuracy_block(mesh, U, mesh, Ug, Bg, Uo, Bo))
     _check_mixed(acc)
-    assert acc["mass_drift"] <= 1e-12 and acc["energy_drift"] <= 1e-12
+    # the reflecting walls exchange mass and energy with the outside blocks (the face-B WALL fill of the
+    # reference copies the inside field, FillOutside.cpp:293-367), so the totals drift on every path:
+    # the mixed path must drift as the oracle does
+    ref = accuracy_block(mesh, U, mesh, Uo, Bo, Uo, Bo)
+    for k in ("mass_drift", "energy_drift"):
+        assert abs(acc[k] - ref[k]) <= max(1e-13, 1e-2 * ref[k])
