@@ -248,6 +248,57 @@ def ct_update(dim, block, emf, B):
     return B
 
 
+def step_fluxes(mesh: Mesh, st: OracleSettings, U, B, dt):
+    """One do_time_step from (U, B) that also returns the per-block face fluxes (flux * dt/dx,
+    [n_owned][dir][var][face] flattened per block). Returns (U2, B2, fluxes)."""
+    U2 = np.array(U, dtype=np.float64, copy=True, order="C")
+    B2 = np.array(B, dtype=np.float64, copy=True, order="C")
+    c = mesh.c
+    dim = c.dim
+    b = (c.bx, c.by, c.bz if dim == 3 else 1)
+    nf = sum(int(np.prod([b[d] + (d == dr) for d in range(dim)])) for dr in range(dim))
+    fl = np.zeros(c.n_owned * 8 * nf)
+    L = lib()
+    L.oracle_step_fluxes.restype = ctypes.c_int
+    L.oracle_step_fluxes.argtypes = [ctypes.POINTER(OracleMesh), ctypes.POINTER(OracleSettings)] + \
+        [ctypes.POINTER(ctypes.c_double)] * 4 + [ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
+    rc = L.oracle_step_fluxes(ctypes.byref(c), ctypes.byref(st), _dp(np.ascontiguousarray(U, dtype=np.float64)), _dp(U2),
+                              _dp(np.ascontiguousarray(B, dtype=np.float64)), _dp(B2), dt, _dp(fl))
+    if rc != 0:
+        raise RuntimeError(f"oracle_step_fluxes failed: {rc}")
+    return U2, B2, fl.reshape(c.n_owned, -1)
+
+
+def correct_emf(mesh: Mesh, emf):
+    """The border EMF correction alone (oracle_correct_emf) over the owned blocks: emf [n_owned][1|3][(b+1)^d]
+    raw EMFs (as block_fluxes_emf returns them). Returns the corrected copy."""
+    emf = np.ascontiguousarray(emf, dtype=np.float64)
+    out = np.zeros_like(emf)
+    L = lib()
+    L.oracle_correct_emf.restype = ctypes.c_int
+    L.oracle_correct_emf.argtypes = [ctypes.POINTER(OracleMesh), ctypes.POINTER(ctypes.c_double),
+                                     ctypes.POINTER(ctypes.c_double)]
+    rc = L.oracle_correct_emf(ctypes.byref(mesh.c), _dp(emf), _dp(out))
+    if rc != 0:
+        raise RuntimeError(f"oracle_correct_emf failed: {rc}")
+    return out
+
+
+def update_all(mesh: Mesh, fluxes, U2, B2):
+    """The conservative update alone (oracle_update_all) over the owned blocks, coarse/fine flux sums
+    included, on copies of U2 [n_owned][5][cells] and B2 [n_owned][faces]. Returns (U2, B2)."""
+    U2 = np.array(U2, dtype=np.float64, copy=True, order="C")
+    B2 = np.array(B2, dtype=np.float64, copy=True, order="C")
+    fl = np.ascontiguousarray(fluxes, dtype=np.float64)
+    L = lib()
+    L.oracle_update_all.restype = ctypes.c_int
+    L.oracle_update_all.argtypes = [ctypes.POINTER(OracleMesh)] + [ctypes.POINTER(ctypes.c_double)] * 3
+    rc = L.oracle_update_all(ctypes.byref(mesh.c), _dp(fl), _dp(U2), _dp(B2))
+    if rc != 0:
+        raise RuntimeError(f"oracle_update_all failed: {rc}")
+    return U2, B2
+
+
 def run(mesh: Mesh, st: OracleSettings, U, B, nsteps):
     """nsteps of CFL + step, in place on copies; returns (U, B, dts)."""
     U = np.array(U, dtype=np.float64, copy=True, order="C")

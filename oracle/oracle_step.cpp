@@ -1344,14 +1344,18 @@ read_emf_and_update(const Mesh & m, const double * emf2, double * B2blk)
 
 // correct_emf, uniform-level branch (scheme/CorrectEmfAtBlockBorderFunctor.cpp:94-360) followed by
 // read_emf_and_update_{2d,3d} (scheme/ReadEmfAndUpdateFunctor.cpp:58-163) for block blk.
+// CorrectEmfAtBlockBorderFunctor::correct_emf (CorrectEmfAtBlockBorderFunctor.cpp:94-360) over the edges
+// of block blk: emf2 receives the block's EMFs (deep_copy(emf2, emf), GodunovImplemV0.cpp:606) with its
+// border edges corrected from the sibling copies in emf_all. Returns 0 or -1 (a finer sibling that is
+// not an owned block).
 static int
-correct_emf_and_update_b(const Mesh & m, int blk, const std::vector<double> & emf_all, double * B2blk)
+correct_emf(const Mesh & m, int blk, const std::vector<double> & emf_all, std::vector<double> & emf2)
 {
   const int     ex = m.bx + 1, ey = m.by + 1, ez = m.dim == 3 ? m.bz + 1 : 1;
   const int64_t ne = emf_count(m);
   const int     ncomp = m.dim == 3 ? 3 : 1;
   const double *emf_self = &emf_all[(size_t)blk * ncomp * ne];
-  std::vector<double> emf2(emf_self, emf_self + ncomp * ne); // deep_copy(emf2, emf)
+  emf2.assign(emf_self, emf_self + ncomp * ne);
   const int bsz[3] = {m.bx, m.by, m.bz};
   for (int c = 0; c < ncomp; ++c)
   {
@@ -1470,7 +1474,17 @@ correct_emf_and_update_b(const Mesh & m, int blk, const std::vector<double> & em
           }
         }
   }
-  // CT update
+  return 0;
+}
+
+// border EMF correction, then the CT update of block blk's faces
+static int
+correct_emf_and_update_b(const Mesh & m, int blk, const std::vector<double> & emf_all, double * B2blk)
+{
+  std::vector<double> emf2;
+  const int           st = correct_emf(m, blk, emf_all, emf2);
+  if (st != 0)
+    return st;
   read_emf_and_update(m, emf2.data(), B2blk);
   return 0;
 }
@@ -2004,6 +2018,44 @@ oracle_block_update(const oracle_mesh * om, int blk, const double * fluxes, doub
 
 // CT update alone on n_blocks blocks of size b (read_emf_and_update): B [n][faces] updated in place by
 // emf [n][ncomp][(b+1)^d] (ncomp 3 in 3D, 1 in 2D).
+// The border EMF correction alone over the owned blocks: emf_in [n_owned][1|3][(b+1)^d] raw EMFs (as
+// oracle_block_fluxes_emf returns them), emf_out the same layout after correct_emf. Returns 0 or the
+// first error.
+int
+oracle_correct_emf(const oracle_mesh * om, const double * emf_in, double * emf_out)
+{
+  const Mesh          m = to_mesh(om);
+  const int64_t       ne = emf_count(m) * (m.dim == 3 ? 3 : 1);
+  std::vector<double> emf_all(emf_in, emf_in + (size_t)m.n_owned * ne);
+  int                 status = 0;
+  for (int blk = 0; blk < m.n_owned && status == 0; ++blk)
+  {
+    std::vector<double> emf2;
+    status = correct_emf(m, blk, emf_all, emf2);
+    if (status == 0)
+      std::memcpy(emf_out + (size_t)blk * ne, emf2.data(), sizeof(double) * ne);
+  }
+  return status;
+}
+
+// The conservative update alone over the owned blocks, coarse/fine flux sums included: fluxes
+// [n_owned][dir][var][face] (flux * dt/dx, as oracle_step_fluxes writes them), U2 [n_owned][5][cells] and
+// the faces B2 (2D: the cell-centred Bz) updated in place. Returns 0 or the first error.
+int
+oracle_update_all(const oracle_mesh * om, const double * fluxes, double * U2, double * B2)
+{
+  const Mesh        m = to_mesh(om);
+  const BlockLayout L = block_layout(m);
+  const FluxLayout  FL = flux_layout(m);
+  std::vector<std::vector<double>> flux_all((size_t)m.n_owned);
+  for (int blk = 0; blk < m.n_owned; ++blk)
+    flux_all[blk].assign(fluxes + (size_t)blk * FL.total, fluxes + (size_t)(blk + 1) * FL.total);
+  int status = 0;
+  for (int blk = 0; blk < m.n_owned && status == 0; ++blk)
+    status = update_u(m, blk, flux_all, U2 + (int64_t)blk * 5 * L.ncell, B2 + (int64_t)blk * L.nface + L.nfx + L.nfy);
+  return status;
+}
+
 int
 oracle_ct_update(int dim, const int * b, int n_blocks, const double * emf, double * B)
 {

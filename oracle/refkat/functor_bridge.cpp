@@ -1,7 +1,7 @@
 // Functor bridge (test infrastructure): runs the reference's own stage functors — limited slopes,
 // Hancock predictor, edge electric field, half-step face source, face fluxes, edge EMFs, the CT
-// update of the face field, the CFL reduction, the viscous face fluxes, the gravity source term and
-// the conservative update by face fluxes
+// update of the face field, the CFL reduction, the viscous face fluxes, the gravity source term, the
+// conservative update by face fluxes (on coarse/fine meshes too) and the border EMF correction
 // (scheme/*Functor.cpp, compiled unmodified from the reference tree against the stub headers in
 // shim/) — on one block whose ghosted stage inputs come from the caller, so that tests can compare the oracle's
 // restatement of those stages with the reference code itself. Built only where the reference tree
@@ -11,6 +11,7 @@
 #include <string>
 
 #include <godunov_mhd_ct/scheme/ComputeElectricFieldFunctor.h>
+#include <godunov_mhd_ct/scheme/CorrectEmfAtBlockBorderFunctor.h>
 #include <godunov_mhd_ct/scheme/ComputeEmfAndStoreFunctor.h>
 #include <godunov_mhd_ct/scheme/ComputeHydroFluxesAndStoreFunctor.h>
 #include <godunov_mhd_ct/scheme/ComputeLimitedSlopesFunctor.h>
@@ -298,9 +299,159 @@ run_ct(const int * b, int n_blocks, const double * emf_in, double * B_io)
   std::memcpy(B_io, B.data(), sizeof(double) * nf);
   return 0;
 }
+// the bridge's mesh tables and the per-block flags derived from them (orchard keys = levels; one
+// conformal-status bit per face whose neighbour region is split into finer leaves)
+template <std::size_t dim>
+struct MeshCtx
+{
+  BridgeMesh                                          mesh;
+  typename hashmap_base_t<DefaultDevice>::map_t       map;
+  typename orchard_key_base_t<DefaultDevice>::view_t  keys;
+  conformal_status_view_t<dim, DefaultDevice>         status;
+  AMRMeshInfo                                         info;
+  brick_size_t<dim>                                   bricks;
+  Kokkos::Array<bool, dim>                            periodic;
+
+  MeshCtx(int n_blocks, int n_owned, const int * level, const int * neighbor, const int * fine, const int * coord)
+  {
+    mesh.dim = (int)dim;
+    mesh.n_owned = n_owned;
+    mesh.n_blocks = n_blocks;
+    mesh.level = level;
+    mesh.neighbor = neighbor;
+    mesh.fine = fine;
+    mesh.coord = coord;
+    map.mesh = &mesh;
+    for (int b = 0; b < n_blocks; ++b)
+      keys.keys->push_back((uint64_t)level[b]);
+    for (int b = 0; b < n_blocks; ++b)
+    {
+      uint8_t bits = 0;
+      for (int f = 0; f < 2 * (int)dim; ++f)
+      {
+        int o[3] = {0, 0, 0};
+        o[f / 2] = (f & 1) ? 1 : -1;
+        const int s = (o[2] + 1) * 9 + (o[1] + 1) * 3 + (o[0] + 1);
+        bool      finer = false;
+        if (fine && b < n_owned && neighbor[(int64_t)b * 27 + s] < 0)
+          for (int c = 0; c < 8; ++c)
+            finer = finer || fine[((int64_t)b * 27 + s) * 8 + c] >= 0;
+        bits |= (uint8_t)((finer ? 1 : 0) << f);
+      }
+      status.bits->push_back(bits);
+    }
+    info.nb_owned = n_owned;
+    info.nb_ghosts = 0;
+    info.nb_outside = n_blocks - n_owned;
+    for (std::size_t d = 0; d < dim; ++d)
+    {
+      bricks[d] = 1;
+      periodic[d] = true;
+    }
+  }
+};
+
+template <std::size_t dim>
+int
+run_correct_emf(const int * b, int n_blocks, int n_owned, const int * level, const int * neighbor, const int * fine,
+                const int * coord, const double * emf_in, double * emf_out)
+{
+  MeshCtx<dim>      mc(n_blocks, n_owned, level, neighbor, fine, coord);
+  ConfigMap         cm;
+  block_size_t<dim> bs, es;
+  for (std::size_t d = 0; d < dim; ++d)
+  {
+    bs[d] = b[d];
+    es[d] = b[d] + 1;
+  }
+  DataArrayBlock<dim, real_t, DefaultDevice> emf(es, 0, 3, n_blocks), emf2(es, 0, 3, n_blocks);
+  const std::size_t                          n = (std::size_t)emf.num_cells() * 3 * n_blocks;
+  std::memcpy(emf.data(), emf_in, sizeof(double) * n);
+  std::memcpy(emf2.data(), emf_in, sizeof(double) * n); // deep_copy(emf2, emf), GodunovImplemV0.cpp:606
+  ParallelEnv pe;
+  CorrectEmfAtBlockBorderFunctor<dim, DefaultDevice>::apply(cm, mc.map, mc.keys, mc.status, mc.info, bs, emf, emf2,
+                                                            mc.bricks, mc.periodic, pe);
+  std::memcpy(emf_out, emf2.data(), sizeof(double) * n);
+  return 0;
+}
+
+template <std::size_t dim>
+int
+run_update_mesh(const int * b, int n_blocks, int n_owned, const int * level, const int * neighbor, const int * fine,
+                const int * coord, const double * prm, const int * flags, const double * grav, double dt,
+                const double * fluxes, double * U_io, double * B_io)
+{
+  MeshCtx<dim>          mc(n_blocks, n_owned, level, neighbor, fine, coord);
+  const ConfigMap       cm = config_of(prm, flags, grav);
+  const MHDSettings     st(cm);
+  FieldMap<models::MHD> fm;
+  block_size_t<dim>     bs;
+  for (std::size_t d = 0; d < dim; ++d)
+    bs[d] = b[d];
+  DataArrayBlock<dim, real_t, DefaultDevice>     U(bs, 0, 5, n_owned);
+  FaceDataArrayBlock<dim, real_t, DefaultDevice> B(bs, n_owned);
+  std::memcpy(U.data(), U_io, sizeof(double) * (std::size_t)U.num_cells() * 5 * n_owned);
+  std::memcpy(B.data(), B_io, sizeof(double) * (std::size_t)B.num_elements_per_octant() * n_owned);
+  // fluxes [block][dir][8][faces] of every owned block, regrouped per direction
+  std::size_t per_block = 0;
+  for (int dir = 0; dir < (int)dim; ++dir)
+  {
+    std::size_t nf = 1;
+    for (std::size_t d = 0; d < dim; ++d)
+      nf *= (std::size_t)(b[d] + ((int)d == dir ? 1 : 0));
+    per_block += 8 * nf;
+  }
+  std::size_t off = 0;
+  for (int dir = 0; dir < (int)dim; ++dir)
+  {
+    block_size_t<dim> fs = bs;
+    fs[dir]++;
+    DataArrayBlock<dim, real_t, DefaultDevice> f(fs, 0, 8, n_blocks);
+    const std::size_t                          nfb = (std::size_t)f.num_cells() * 8;
+    for (int blk = 0; blk < n_owned; ++blk)
+      std::memcpy(f.data() + nfb * blk, fluxes + per_block * blk + off, sizeof(double) * nfb);
+    off += nfb;
+    ReadFluxesAndConservativeUpdateFunctor<dim, DefaultDevice>::apply(cm, mc.map, mc.keys, mc.status, mc.info, U, B,
+                                                                      f, fm, dir, mc.bricks, mc.periodic, st, dt);
+  }
+  std::memcpy(U_io, U.data(), sizeof(double) * (std::size_t)U.num_cells() * 5 * n_owned);
+  std::memcpy(B_io, B.data(), sizeof(double) * (std::size_t)B.num_elements_per_octant() * n_owned);
+  return 0;
+}
 } // namespace
 
 extern "C" {
+
+// The reference's border EMF correction (CorrectEmfAtBlockBorderFunctor::apply) on a mesh given by its
+// tables (levels [n_blocks], neighbour table [n_blocks][27], children of finer regions [n_blocks][27][8]
+// or NULL, coordinates [n_blocks][3]): emf_in [n_blocks][3][(b+1)^d] raw EMFs (components by edge
+// direction, 2D: z), emf_out the corrected copy (only the owned blocks' border edges change).
+int
+ref_correct_emf(int dim, const int * b, int n_blocks, int n_owned, const int * level, const int * neighbor,
+                const int * fine, const int * coord, const double * emf_in, double * emf_out)
+{
+  if (dim == 2)
+    return run_correct_emf<2>(b, n_blocks, n_owned, level, neighbor, fine, coord, emf_in, emf_out);
+  if (dim == 3)
+    return run_correct_emf<3>(b, n_blocks, n_owned, level, neighbor, fine, coord, emf_in, emf_out);
+  return -1;
+}
+
+// The reference's conservative update (ReadFluxesAndConservativeUpdateFunctor::apply per direction) of
+// all owned blocks of a mesh given by its tables, coarse cells next to finer leaves taking the sum of
+// the fine face fluxes: fluxes [n_owned][dir][8][faces] (times dt/dx), U [n_owned][5][cells] and B
+// [n_owned][faces] (2D: the cell-centred Bz) updated in place.
+int
+ref_update_mesh(int dim, const int * b, int n_blocks, int n_owned, const int * level, const int * neighbor,
+                const int * fine, const int * coord, const double * prm, const int * flags, const double * grav,
+                double dt, const double * fluxes, double * U, double * B)
+{
+  if (dim == 2)
+    return run_update_mesh<2>(b, n_blocks, n_owned, level, neighbor, fine, coord, prm, flags, grav, dt, fluxes, U, B);
+  if (dim == 3)
+    return run_update_mesh<3>(b, n_blocks, n_owned, level, neighbor, fine, coord, prm, flags, grav, dt, fluxes, U, B);
+  return -1;
+}
 
 // One block: ghosted primitives q [11][(b+4)^d] (as ref_block_stages takes them) in, the reference's
 // viscous face fluxes (times dt/dx; per direction [8][faces], directions concatenated) out.

@@ -1,4 +1,5 @@
-// Stub of kalypsso-core's mesh counts for the functor bridge (the conforming-mesh stages use none).
+// Stub of kalypsso-core's mesh counts for the functor bridge: owned blocks first, no MPI ghosts,
+// outside blocks after them.
 #pragma once
 namespace kalypsso
 {
