@@ -15,7 +15,8 @@
 //     shared border face;
 //   * hydro (ConvertToPrimitivesVariablesFunctor.cpp:217-283, 439-446, 471-635): a finer region
 //     gives the mean of the 2^d fine cells (x fastest); a coarser region copies the coarse cell
-//     (SIMPLE_COPY, with the coarse cell's own cell-centred B in Bcc) or adds 0.25 * (+-1) *
+//     (SIMPLE_COPY, with the coarse cell's own cell-centred B in Bcc, from the coarse block's ghosted
+//     faces: a border face shared with a finer region is that region's) or adds 0.25 * (+-1) *
 //     minmod(u - u_left, u_right - u) per axis at the coarse level (EXTRAPOLATE_LINEAR_MINMOD).
 // Built with --fmad=false: the FP64 path reproduces the CPU restatement bit for bit.
 #include <cuda_runtime.h>
@@ -176,6 +177,30 @@ region_face(const GhostArgs & g, const DRegion & r, int comp, const int * q, dou
   }
 }
 
+// Face comp at inner index (i, j, k) of block blk as its ghosted face field holds it: the block's own
+// face, except that a border face shared (along its normal) with a finer neighbour region is that
+// region's value (false when a needed leaf is absent).
+__device__ static bool
+own_ghost_face(const GhostArgs & g, int blk, int comp, int i, int j, int k, double & out)
+{
+  const int b[3] = {g.bx, g.by, g.bz};
+  const int idx[3] = {i, j, k};
+  if (!(g.dim == 2 && comp == 2) && (idx[comp] == 0 || idx[comp] == b[comp]))
+  {
+    int o1[3] = {0, 0, 0};
+    o1[comp] = idx[comp] == 0 ? -1 : 1;
+    const DRegion r1 = region_of(g, blk, o1[0], o1[1], o1[2]);
+    if (r1.kind == RK_FINER)
+    {
+      int q[3] = {i, j, k};
+      q[comp] = idx[comp] == 0 ? b[comp] : 0;
+      return region_face(g, r1, comp, q, out);
+    }
+  }
+  out = face_at(g, blk, comp, i, j, k);
+  return true;
+}
+
 // Mean of the 2^d fine cells of variable v covering region-local cell q of a finer region.
 __device__ static bool
 restrict_cell(const GhostArgs & g, const DRegion & r, const int * q, int v, double & out)
@@ -305,13 +330,26 @@ ghost_prepass_kernel(const GhostArgs g)
             const int I[3] = {(r.sub[0] * b[0] + q[0]) >> 1, (r.sub[1] * b[1] + q[1]) >> 1, (r.sub[2] * b[2] + q[2]) >> 1};
             if (g.prolongation == 0)
             {
+              // the coarse cell's own cell-centred B, from the coarse block's ghosted faces
+              // (ConvertToPrimitivesVariablesFunctor.cpp:175-210 via fill_ghost_copy)
               for (int n = 0; n < 5; ++n)
                 u[n] = u_at(g, r.id, n, I[0], I[1], I[2]);
-              bc[0] = 0.5 * (face_at(g, r.id, 0, I[0], I[1], I[2]) + face_at(g, r.id, 0, I[0] + 1, I[1], I[2]));
-              bc[1] = 0.5 * (face_at(g, r.id, 1, I[0], I[1], I[2]) + face_at(g, r.id, 1, I[0], I[1] + 1, I[2]));
-              bc[2] = g.dim == 3
-                        ? 0.5 * (face_at(g, r.id, 2, I[0], I[1], I[2]) + face_at(g, r.id, 2, I[0], I[1], I[2] + 1))
-                        : 0.5 * (face_at(g, r.id, 2, I[0], I[1], 0) + face_at(g, r.id, 2, I[0], I[1], 0));
+              double fl[3] = {0, 0, 0}, fr[3] = {0, 0, 0};
+              for (int c = 0; c < 3 && ok; ++c)
+              {
+                if (g.dim == 2 && c == 2)
+                {
+                  fl[2] = fr[2] = face_at(g, r.id, 2, I[0], I[1], 0);
+                  continue;
+                }
+                int I1[3] = {I[0], I[1], I[2]};
+                I1[c] += 1;
+                ok = own_ghost_face(g, r.id, c, I[0], I[1], I[2], fl[c]) &&
+                     own_ghost_face(g, r.id, c, I1[0], I1[1], I1[2], fr[c]);
+              }
+              bc[0] = 0.5 * (fl[0] + fr[0]);
+              bc[1] = 0.5 * (fl[1] + fr[1]);
+              bc[2] = 0.5 * (fl[2] + fr[2]);
             }
             else
             {

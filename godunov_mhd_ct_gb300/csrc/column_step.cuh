@@ -774,8 +774,26 @@ __global__ void __launch_bounds__(K::NT, 2) column_step_kernel(const StepArgs a)
             fzt[K::bzp(i, j)] = fzr;
             if (s == -4)
               t.Bz(q)[K::bzp(i, j)] = fzl; // the first plane's bottom faces
+            // a cell inside an outside block takes its cell-centred B from that block's own faces
+            // (get_conservative_vars of the outside cell; FillOutside's copy of the shared border face)
+            if (nb >= a.n_owned && nb < a.n_blocks)
+            {
+              const int      li = gi - cox * bx, lj = gj - coy * by, lk = q - coz * bz;
+              const double * Bn = a.B + (int64_t)nb * a.nface;
+              const int64_t  xr = li + (int64_t)(bx + 1) * (lj + (int64_t)by * lk);
+              const int64_t  yr = a.nfx + li + (int64_t)bx * (lj + (int64_t)(by + 1) * lk);
+              const int64_t  zr = a.nfx + a.nfy + li + (int64_t)bx * (lj + (int64_t)by * lk);
+              bxl = Bn[xr];
+              bxr = Bn[xr + 1];
+              byl = Bn[yr];
+              byr = Bn[yr + bx];
+              bzl = Bn[zr];
+              bzr = Bn[zr + (int64_t)bx * by];
+            }
             // FP32 recovery; FP64 when magnetic + kinetic energy dominate (low beta / high Mach)
-            const float Bxc = 0.5f * (fxl + fxr), Byc = 0.5f * (fyl + fyr), Bzc = 0.5f * (fzl + fzr);
+            const float Bxc = 0.5f * (to_r<float>(bxl) + to_r<float>(bxr)),
+                        Byc = 0.5f * (to_r<float>(byl) + to_r<float>(byr)),
+                        Bzc = 0.5f * (to_r<float>(bzl) + to_r<float>(bzr));
             const float r = rmax<float>(to_r<float>(u[ID]), ph.smallr);
             const float ir = 1.0f / r;
             const float vx = to_r<float>(u[IU]) * ir, vy = to_r<float>(u[IV]) * ir, vz = to_r<float>(u[IW]) * ir;

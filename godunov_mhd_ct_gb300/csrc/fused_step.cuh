@@ -1376,6 +1376,36 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
     return true;
   };
 
+  // A ghost cell inside an outside block takes its cell-centred B from that block's own faces
+  // (get_conservative_vars of the outside cell, ConvertToPrimitivesVariablesFunctor.cpp:175-221), whose
+  // copy of the shared border face is FillOutside's (a WALL copies the same face index)
+  const bool has_outside = a.n_blocks > a.n_owned;
+  auto       outside_bcc = [&](int ci, int cj, int ck, double * bc) -> bool {
+    const int ox = cell_off(ci, bx), oy = cell_off(cj, by), oz = D3 ? cell_off(ck, bz) : 0;
+    if ((ox | oy | oz) == 0)
+      return false;
+    const int nb = s_nbr[nb_slot(ox, oy, oz)];
+    if (nb < a.n_owned || nb >= a.n_blocks)
+      return false;
+    const int      li = ci - ox * bx, lj = cj - oy * by, lk = ck - oz * bz;
+    const double * Bn = a.B + (int64_t)nb * a.nface;
+    const int64_t  xr = li + (int64_t)(bx + 1) * (lj + (int64_t)by * lk);
+    const int64_t  yr = a.nfx + li + (int64_t)bx * (lj + (int64_t)(by + 1) * lk);
+    bc[0] = 0.5 * (Bn[xr] + Bn[xr + 1]);
+    bc[1] = 0.5 * (Bn[yr] + Bn[yr + bx]);
+    if (D3)
+    {
+      const int64_t zr = a.nfx + a.nfy + li + (int64_t)bx * (lj + (int64_t)by * lk);
+      bc[2] = 0.5 * (Bn[zr] + Bn[zr + (int64_t)bx * by]);
+    }
+    else
+    {
+      const double z = Bn[a.nfx + a.nfy + li + (int64_t)bx * lj];
+      bc[2] = 0.5 * (z + z);
+    }
+    return true;
+  };
+
   // primitive variables on the Q region (ConvertToPrimitivesVariablesFunctor) of cell item n
   auto prim_cell = [&](int n, const double * u) {
     const int i = n % C::QX - 2;
@@ -1390,10 +1420,10 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
       double Byc = 0.5 * (fby[C::fyi(i, j, k)] + fby[C::fyi(i, j + 1, k)]);
       double Bzc = D3 ? 0.5 * (fbz[C::fzi(i, j, k)] + fbz[C::fzi(i, j, k + 1)])
                       : 0.5 * (fbz[C::fzi(i, j, 0)] + fbz[C::fzi(i, j, 0)]);
-      if (coarse_copy)
+      if (coarse_copy || has_outside)
       {
         double bc[3];
-        if (coarse_bcc(ci, cj, ck, bc))
+        if ((coarse_copy && coarse_bcc(ci, cj, ck, bc)) || (has_outside && outside_bcc(ci, cj, ck, bc)))
         {
           Bxc = bc[0];
           Byc = bc[1];
@@ -1419,7 +1449,7 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
       R      Byc = R(0.5) * (fby[C::fyi(i, j, k)] + fby[C::fyi(i, j + 1, k)]);
       R      Bzc = D3 ? R(0.5) * (fbz[C::fzi(i, j, k)] + fbz[C::fzi(i, j, k + 1)]) : fbz[C::fzi(i, j, 0)];
       double bcc[3];
-      const bool cc = coarse_copy && coarse_bcc(ci, cj, ck, bcc);
+      const bool cc = (coarse_copy && coarse_bcc(ci, cj, ck, bcc)) || (has_outside && outside_bcc(ci, cj, ck, bcc));
       if (cc)
       {
         Bxc = to_r<R>(bcc[0]);

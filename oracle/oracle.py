@@ -269,6 +269,29 @@ def step_fluxes(mesh: Mesh, st: OracleSettings, U, B, dt):
     return U2, B2, fl.reshape(c.n_owned, -1)
 
 
+def block_ghost_faces(mesh: Mesh, U, B, blk):
+    """The ghosted face field of owned block blk (oracle_block_ghost_faces): Bx, By, Bz of a (b+4)^d cell
+    box whose first face has index -2 (2D: the cell-centred Bz), x fastest, concatenated."""
+    c = mesh.c
+    dim = c.dim
+    b = (c.bx, c.by, c.bz if dim == 3 else 1)
+    g = [v + 4 for v in b[:dim]]
+    n = 0
+    for comp in range(3):
+        n += int(np.prod([g[d] + (1 if d == comp else 0) for d in range(dim)]))
+    out = np.zeros(n)
+    L = lib()
+    L.oracle_block_ghost_faces.restype = ctypes.c_int
+    L.oracle_block_ghost_faces.argtypes = [ctypes.POINTER(OracleMesh), ctypes.POINTER(ctypes.c_double),
+                                           ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_double)]
+    rc = L.oracle_block_ghost_faces(ctypes.byref(c), _dp(np.ascontiguousarray(U, dtype=np.float64)),
+                                    _dp(np.ascontiguousarray(B, dtype=np.float64)), int(blk), _dp(out))
+    if rc != 0:
+        raise RuntimeError(f"oracle_block_ghost_faces failed: {rc}")
+    return out
+
+
 def correct_emf(mesh: Mesh, emf):
     """The border EMF correction alone (oracle_correct_emf) over the owned blocks: emf [n_owned][1|3][(b+1)^d]
     raw EMFs (as block_fluxes_emf returns them). Returns the corrected copy."""

@@ -34,9 +34,10 @@
 //     normal is taken from the finer one, so that all blocks see one value for every face;
 //   * cell-centred hydro ghosts follow ConvertToPrimitivesVariablesFunctor.cpp:217-283, 471-719:
 //     same level copies U and takes B_cc from the ghost faces (equal to the neighbour's faces when
-//     shared faces agree); finer takes the mean of the 2^d fine cells (core compute_siblings_average:
+//     shared faces agree), an outside block from its own faces (get_conservative_vars of the outside
+//     cell); finer takes the mean of the 2^d fine cells (core compute_siblings_average:
 //     x fastest, sum then divide) with B_cc from the ghost faces; coarser SIMPLE_COPY copies the
-//     coarse cell's U and its B_cc from the coarse block's faces; EXTRAPOLATE_LINEAR_MINMOD adds
+//     coarse cell's U and its B_cc from the coarse block's ghosted faces; EXTRAPOLATE_LINEAR_MINMOD adds
 //     0.25 * (+-1) * minmod slope per axis (core compute_minmod_slopes: minmod(u - u_left,
 //     u_right - u); neighbours at the coarse level, a refined one read as the mean of its fine cells,
 //     a coarser one as its containing cell) with B_cc from the ghost faces;
@@ -491,6 +492,18 @@ convert_to_primitives(const Mesh & m, const Fields & f, const Settings & s, int 
             // fill_inner / fill_ghost_copy at the same level (.cpp:373-468)
             for (int v = 0; v < 5; ++v)
               u[v] = f.u(r.id, v, q[0], q[1], q[2]);
+            if (r.kind == RK_OUTSIDE)
+            {
+              // get_conservative_vars(cell_loc_in) reads B_cc from the outside block's own faces, whose
+              // copy of the shared border face is FillOutside's (a WALL copies the same face index)
+              u[IA] = 0.5 * (f.bx(r.id, q[0], q[1], q[2]) + f.bx(r.id, q[0] + 1, q[1], q[2]));
+              u[IB] = 0.5 * (f.by(r.id, q[0], q[1], q[2]) + f.by(r.id, q[0], q[1] + 1, q[2]));
+              if (m.dim == 3)
+                u[IC] = 0.5 * (f.bz(r.id, q[0], q[1], q[2]) + f.bz(r.id, q[0], q[1], q[2] + 1));
+              else
+                u[IC] = 0.5 * (f.bz(r.id, q[0], q[1], 0) + f.bz(r.id, q[0], q[1], 0));
+              bcc_from_ghost_faces = false;
+            }
             break;
           case RK_FINER:
             // get_conservative_vars_restriction (.cpp:217-283)
@@ -504,15 +517,30 @@ convert_to_primitives(const Mesh & m, const Fields & f, const Settings & s, int 
                               (r.sub[2] * m.bz + q[2]) >> 1};
             if (m.prolongation == 0)
             {
-              // SIMPLE_COPY: fill_ghost_copy of the coarse cell with its own B_cc (.cpp:439-446)
+              // SIMPLE_COPY: fill_ghost_copy of the coarse cell with its own B_cc (.cpp:439-446), read
+              // from the coarse block's ghosted faces (a border face shared with a finer region is
+              // that region's)
               for (int v = 0; v < 5; ++v)
                 u[v] = f.u(r.id, v, I[0], I[1], I[2]);
-              u[IA] = 0.5 * (f.bx(r.id, I[0], I[1], I[2]) + f.bx(r.id, I[0] + 1, I[1], I[2]));
-              u[IB] = 0.5 * (f.by(r.id, I[0], I[1], I[2]) + f.by(r.id, I[0], I[1] + 1, I[2]));
-              if (m.dim == 3)
-                u[IC] = 0.5 * (f.bz(r.id, I[0], I[1], I[2]) + f.bz(r.id, I[0], I[1], I[2] + 1));
-              else
-                u[IC] = 0.5 * (f.bz(r.id, I[0], I[1], 0) + f.bz(r.id, I[0], I[1], 0));
+              double fl[3], fr[3];
+              for (int c = 0; c < 3; ++c)
+              {
+                if (m.dim == 2 && c == 2)
+                {
+                  if (!ghost_face(m, f, r.id, 2, I[0], I[1], 0, fl[2]))
+                    return -1;
+                  fr[2] = fl[2];
+                  continue;
+                }
+                int I1[3] = {I[0], I[1], I[2]};
+                I1[c] += 1;
+                if (!ghost_face(m, f, r.id, c, I[0], I[1], I[2], fl[c]) ||
+                    !ghost_face(m, f, r.id, c, I1[0], I1[1], I1[2], fr[c]))
+                  return -1;
+              }
+              u[IA] = 0.5 * (fl[0] + fr[0]);
+              u[IB] = 0.5 * (fl[1] + fr[1]);
+              u[IC] = 0.5 * (fl[2] + fr[2]);
               bcc_from_ghost_faces = false;
             }
             else
@@ -1860,6 +1888,32 @@ oracle_block_stages(const oracle_mesh * om, const oracle_settings * os, const do
   put(q2, w.Q2);
   put(e, w.E);
   put(sf, w.SF);
+  return 0;
+}
+
+// The ghosted face field of block blk (the face-B ghost layer oracle_step builds, fill_bface_ghosted):
+// Bx on faces [-2, bx+2] x cells [-2, b+2) of the other axes, By and Bz likewise (2D: the cell-centred Bz
+// on [-2, b+2)^2), x fastest, components concatenated. Returns 0 or -1 (missing neighbour).
+int
+oracle_block_ghost_faces(const oracle_mesh * om, const double * U, const double * B, int blk, double * out)
+{
+  const Mesh m = to_mesh(om);
+  if (blk < 0 || blk >= m.n_owned)
+    return -1;
+  Fields f;
+  f.m = &m;
+  f.L = block_layout(m);
+  f.U = U;
+  f.B = B;
+  StepWork w;
+  if (fill_bface_ghosted(m, f, blk, w) != 0)
+    return -1;
+  size_t off = 0;
+  for (const Box * bb : {&w.Bgx, &w.Bgy, &w.Bgz})
+  {
+    std::memcpy(out + off, bb->a.data(), sizeof(double) * bb->a.size());
+    off += bb->a.size();
+  }
   return 0;
 }
 

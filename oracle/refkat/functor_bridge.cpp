@@ -1,7 +1,8 @@
 // Functor bridge (test infrastructure): runs the reference's own stage functors — limited slopes,
 // Hancock predictor, edge electric field, half-step face source, face fluxes, edge EMFs, the CT
 // update of the face field, the CFL reduction, the viscous face fluxes, the gravity source term, the
-// conservative update by face fluxes (on coarse/fine meshes too) and the border EMF correction
+// conservative update by face fluxes (on coarse/fine meshes too), the border EMF correction and the
+// primitive variables of a ghosted block with its ghost cells from same-level, finer and coarser leaves
 // (scheme/*Functor.cpp, compiled unmodified from the reference tree against the stub headers in
 // shim/) — on one block whose ghosted stage inputs come from the caller, so that tests can compare the oracle's
 // restatement of those stages with the reference code itself. Built only where the reference tree
@@ -11,6 +12,7 @@
 #include <string>
 
 #include <godunov_mhd_ct/scheme/ComputeElectricFieldFunctor.h>
+#include <godunov_mhd_ct/scheme/ConvertToPrimitivesVariablesFunctor.h>
 #include <godunov_mhd_ct/scheme/CorrectEmfAtBlockBorderFunctor.h>
 #include <godunov_mhd_ct/scheme/ComputeEmfAndStoreFunctor.h>
 #include <godunov_mhd_ct/scheme/ComputeHydroFluxesAndStoreFunctor.h>
@@ -418,9 +420,55 @@ run_update_mesh(const int * b, int n_blocks, int n_owned, const int * level, con
   std::memcpy(B_io, B.data(), sizeof(double) * (std::size_t)B.num_elements_per_octant() * n_owned);
   return 0;
 }
+template <std::size_t dim>
+int
+run_primitives(const int * b, int n_blocks, int n_owned, const int * level, const int * neighbor, const int * fine,
+               const int * coord, const double * prm, int prolongation, const double * U_in, const double * Bg_in,
+               int blk, double * q_out)
+{
+  MeshCtx<dim> mc(n_blocks, n_owned, level, neighbor, fine, coord);
+  const int    flags[5] = {5, 0, 0, 0, 0};
+  const double grav[3] = {0.0, 0.0, 0.0};
+  ConfigMap    cm = config_of(prm, flags, grav);
+  cm.set("amr", "cell_centered_prolongation_type", prolongation ? "EXTRAPOLATE_LINEAR_MINMOD" : "SIMPLE_COPY");
+  const MHDSettings st(cm);
+  block_size_t<dim> bs, gs;
+  for (std::size_t d = 0; d < dim; ++d)
+  {
+    bs[d] = b[d];
+    gs[d] = b[d] + 4;
+  }
+  DataArrayBlock<dim, real_t, DefaultDevice>      U(bs, 0, 5, n_blocks);
+  FaceDataArrayBlock<dim, real_t, DefaultDevice>  Bg(gs, n_blocks, 2);
+  DataArrayGhostedBlock<dim, real_t, DefaultDevice> q(bs, 2, 11, 1);
+  std::memcpy(U.data(), U_in, sizeof(double) * (std::size_t)U.num_cells() * 5 * n_blocks);
+  std::memcpy(Bg.data(), Bg_in, sizeof(double) * (std::size_t)Bg.num_elements_per_octant() * n_blocks);
+  ParallelEnv pe;
+  ConvertToPrimitivesVariablesFunctor<dim, DefaultDevice>::apply_on_group(cm, mc.map, mc.keys, mc.info, blk, 1, U, Bg,
+                                                                          q, mc.bricks, mc.periodic, st, pe);
+  std::memcpy(q_out, q.data(), sizeof(double) * (std::size_t)q.num_cells() * 11);
+  return 0;
+}
 } // namespace
 
 extern "C" {
+
+// The reference's primitive variables of owned block blk on its (b+4)^d ghosted box
+// (ConvertToPrimitivesVariablesFunctor::apply_on_group, ghosts from same-level leaves, the sibling
+// average of finer ones, a coarser one copied or extrapolated with minmod slopes): mesh tables as for
+// ref_correct_emf, U [n_blocks][5][cells], Bg [n_blocks][ghosted faces] (per block the face arrays of a
+// (b+4)^d cell box, first face at index -2, components concatenated), q_out [11][(b+4)^d].
+int
+ref_block_primitives(int dim, const int * b, int n_blocks, int n_owned, const int * level, const int * neighbor,
+                     const int * fine, const int * coord, const double * prm, int prolongation, const double * U,
+                     const double * Bg, int blk, double * q_out)
+{
+  if (dim == 2)
+    return run_primitives<2>(b, n_blocks, n_owned, level, neighbor, fine, coord, prm, prolongation, U, Bg, blk, q_out);
+  if (dim == 3)
+    return run_primitives<3>(b, n_blocks, n_owned, level, neighbor, fine, coord, prm, prolongation, U, Bg, blk, q_out);
+  return -1;
+}
 
 // The reference's border EMF correction (CorrectEmfAtBlockBorderFunctor::apply) on a mesh given by its
 // tables (levels [n_blocks], neighbour table [n_blocks][27], children of finer regions [n_blocks][27][8]

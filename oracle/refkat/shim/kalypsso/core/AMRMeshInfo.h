@@ -8,5 +8,6 @@ struct AMRMeshInfo
   int nb_owned = 1, nb_ghosts = 0, nb_outside = 0;
   int local_num_quadrants() const { return nb_owned; }
   int local_num_ghosts() const { return nb_ghosts; }
+  int local_num_mirrors() const { return 0; }
 };
 } // namespace kalypsso

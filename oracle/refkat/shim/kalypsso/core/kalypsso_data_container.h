@@ -104,7 +104,8 @@ class FaceDataArrayBlock
 {
 public:
   FaceDataArrayBlock() = default;
-  FaceDataArrayBlock(block_size_t<dim> cells, int noct) : m_cells(cells), m_noct(noct)
+  // shift: ghost width (element (0, ...) is the first face of the inner block)
+  FaceDataArrayBlock(block_size_t<dim> cells, int noct, int shift = 0) : m_cells(cells), m_noct(noct), m_shift(shift)
   {
     int off = 0;
     for (int c = 0; c < 3; ++c)
@@ -123,6 +124,8 @@ public:
   operator()(int i, int j, int c, int oct) const
   {
     const int nx = m_cells[0] + (c == 0);
+    i += m_shift;
+    j += m_shift;
     return (*m_data)[(std::size_t)m_per * oct + m_off[c] + i + (std::size_t)nx * j];
   }
   template <std::size_t D = dim, std::enable_if_t<D == 3, int> = 0>
@@ -130,6 +133,9 @@ public:
   operator()(int i, int j, int k, int c, int oct) const
   {
     const int nx = m_cells[0] + (c == 0), ny = m_cells[1] + (c == 1);
+    i += m_shift;
+    j += m_shift;
+    k += m_shift;
     return (*m_data)[(std::size_t)m_per * oct + m_off[c] + i + (std::size_t)nx * (j + (std::size_t)ny * k)];
   }
   block_size_t<dim>       cell_block_size() const { return m_cells; }
@@ -141,12 +147,12 @@ public:
       o[c] = m_off[c];
     return o;
   }
-  int32_t shift() const { return 0; }
+  int32_t shift() const { return m_shift; }
   T *     data() const { return m_data->data(); }
 
 private:
   block_size_t<dim>               m_cells{};
-  int                             m_noct = 0, m_per = 0, m_off[3] = {0, 0, 0};
+  int                             m_noct = 0, m_shift = 0, m_per = 0, m_off[3] = {0, 0, 0};
   std::shared_ptr<std::vector<T>> m_data;
 };
 } // namespace kalypsso

@@ -12,7 +12,8 @@ struct orchard_key_base_t
   struct view_t
   {
     std::shared_ptr<std::vector<uint64_t>> keys = std::make_shared<std::vector<uint64_t>>();
-    uint64_t operator()(int i) const { return (*keys)[i]; }
+    uint64_t    operator()(int i) const { return (*keys)[i]; }
+    std::size_t extent(int) const { return keys->size(); }
   };
 };
 template <std::size_t dim>

@@ -8,7 +8,11 @@ oracle_block_fluxes_emf) and the face fluxes of one step (``fluxes``, oracle_ste
 ``functor_amr.npz`` next to this script: per case dt and the reference's results on the blocks next
 to a level change (``blocks``: owned blocks with a neighbour at another level), the corrected EMFs
 (``emf_ref``) and their U and faces after the conservative update from U, B (``upd_U``, ``upd_B``);
-the inputs are rebuilt from the seeded state (``case_inputs``). Needs the reference tree
+the inputs are rebuilt from the seeded state (``case_inputs``). The reference's ghosted primitive
+variables (ConvertToPrimitivesVariablesFunctor, SIMPLE_COPY and EXTRAPOLATE_LINEAR_MINMOD) of the
+blocks in ``prim_blocks`` (the level-change blocks, and on walled meshes also those next to outside
+blocks) are kept as SHA-256 digests of their bytes (``prim_sha_<prolongation>``), the first two
+of them in full (``prim_q_<prolongation>``). Needs the reference tree
 (default /root/reference, or $GMHD_REFERENCE_TREE); the committed npz is what tests use.
 
     python tests/golden/make_golden_amr.py
@@ -120,6 +124,43 @@ def reference_update(mesh, dt, fluxes, U, B):
     return Uo, Bo
 
 
+def reference_primitives(mesh, U, B, blk, prolongation, om):
+    """The reference's ConvertToPrimitivesVariablesFunctor on owned block blk: its primitive variables
+    [11][(b+4)^d] with the ghost cells filled from the neighbour leaves. The ghosted face field it reads
+    is the oracle's (block_ghost_faces) for owned blocks and the block's own faces for outside ones."""
+    L = ctypes.CDLL(BRIDGE)
+    dp = ctypes.POINTER(ctypes.c_double)
+    dim = mesh.dim
+    nbg = orc.block_ghost_faces(om, U, B, 0).size
+    Bg = np.zeros((mesh.n_blocks, nbg))
+    for k in range(mesh.n_owned):
+        Bg[k] = orc.block_ghost_faces(om, U, B, k)
+    # outside blocks: their own faces inside the ghosted box (the part the functor reads)
+    g = [v + 4 for v in mesh.block[:dim]]
+    faces = mesh.split_faces(B)
+    for k in range(mesh.n_owned, mesh.n_blocks):
+        off = 0
+        for comp in range(3):
+            shape = [g[d] + (1 if d == comp and not (dim == 2 and comp == 2) else 0) for d in range(dim)][::-1]
+            box = np.zeros(shape)
+            inner = faces[comp][k] if dim == 3 else faces[comp][k][0]
+            sl = tuple(slice(2, 2 + n) for n in inner.shape)
+            box[sl] = inner
+            Bg[k, off:off + box.size] = box.reshape(-1)
+            off += box.size
+    n2 = int(np.prod(g))
+    q = np.zeros(11 * n2)
+    keep, (lev, nbr, fine, coord) = _tables(mesh)
+    b = (ctypes.c_int * 3)(*mesh.block)
+    prm = (ctypes.c_double * 6)(GAMMA, SLOPE, 1e-10, 1e-10, 1.0, 0.0)
+    Uc = np.ascontiguousarray(U, dtype=np.float64)
+    rc = L.ref_block_primitives(dim, b, mesh.n_blocks, mesh.n_owned, lev, nbr, fine, coord, prm, int(prolongation),
+                                Uc.ctypes.data_as(dp), Bg.ctypes.data_as(dp), int(blk), q.ctypes.data_as(dp))
+    if rc != 0:
+        raise RuntimeError(f"ref_block_primitives failed: {rc}")
+    return q
+
+
 def level_change_blocks(mesh):
     """Owned blocks with a neighbour region at another level (coarser, or split into finer leaves)."""
     n = mesh.n_owned
@@ -135,6 +176,27 @@ def level_change_blocks(mesh):
     return np.nonzero(other)[0].astype(np.int32)
 
 
+def prim_blocks(mesh):
+    """Blocks whose ghost cells come from another level or from outside blocks."""
+    sel = set(level_change_blocks(mesh).tolist())
+    n = mesh.n_owned
+    for b in range(n):
+        if np.any((mesh.neighbor[b] >= n)):
+            sel.add(b)
+    return np.array(sorted(sel), dtype=np.int32)
+
+
+def digest(a):
+    import hashlib
+
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.float64).tobytes()).hexdigest()
+
+
+def oracle_mesh_of(mesh, prolongation):
+    bc = [1 if mesh.periodic[d // 2] else 3 for d in range(6)]
+    return orc.Mesh.from_block_mesh(mesh, bc=bc, prolongation=prolongation)
+
+
 def main():
     if not orc.build_refkat() or not os.path.exists(BRIDGE):
         sys.exit("the reference tree is needed to record the golden coarse/fine stages")
@@ -147,6 +209,13 @@ def main():
         out[f"{name}_emf_ref"] = reference_correct_emf(mesh, emf)[sel]
         Uu, Bu = reference_update(mesh, dt, fluxes, U, B)
         out[f"{name}_upd_U"], out[f"{name}_upd_B"] = Uu[sel], Bu[sel]
+        pb = prim_blocks(mesh)
+        out[f"{name}_prim_blocks"] = pb
+        for prol in (0, 1):
+            om2 = oracle_mesh_of(mesh, prol)
+            qs = [reference_primitives(mesh, U, B, int(b), prol, om2) for b in pb]
+            out[f"{name}_prim_sha_{prol}"] = np.array([digest(q) for q in qs])
+            out[f"{name}_prim_q_{prol}"] = np.array(qs[:2])
     path = os.path.join(HERE, "functor_amr.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({len(CASES)} cases)")
