@@ -1,6 +1,6 @@
 // Minimal stand-in for the better-enums BETTER_ENUM macro (the real library is not vendored in
-// the reference). Supports what riemann_solver_types.h uses: unary '+' to the enum class,
-// equality, _from_string_nothrow and _to_string, with implicit 0-based values.
+// the reference). Supports what the bridged reference code uses: unary '+' to the enum class,
+// equality, _from_string_nothrow, _to_string and _to_integral, with implicit 0-based values.
 #pragma once
 #include <cstring>
 #include <optional>
@@ -40,9 +40,13 @@ index_of(const char * list, const char * name)
       __VA_ARGS__                                                                                 \
     };                                                                                            \
     _enumerated v;                                                                                \
+    constexpr Name()                                                                              \
+      : v(static_cast<_enumerated>(0))                                                            \
+    {}                                                                                            \
     constexpr Name(_enumerated e)                                                                 \
       : v(e)                                                                                      \
     {}                                                                                            \
+    constexpr Underlying _to_integral() const { return static_cast<Underlying>(v); }             \
     constexpr operator _enumerated() const { return v; }                                          \
     static std::optional<Name> _from_string_nothrow(const char * s)                               \
     {                                                                                             \

@@ -1,9 +1,10 @@
 // Functor bridge (test infrastructure): runs the reference's own stage functors — limited slopes,
 // Hancock predictor, edge electric field, half-step face source, face fluxes, edge EMFs, the CT
 // update of the face field, the CFL reduction, the viscous face fluxes, the gravity source term, the
-// conservative update by face fluxes (on coarse/fine meshes too), the border EMF correction and the
+// conservative update by face fluxes (on coarse/fine meshes too), the border EMF correction, the
 // primitive variables of a ghosted block with its ghost cells from same-level, finer and coarser leaves
-// (scheme/*Functor.cpp, compiled unmodified from the reference tree against the stub headers in
+// and the fill of the leaves beyond non-periodic domain borders (scheme/*Functor.cpp and
+// border_conditions/FillOutside.cpp, compiled unmodified from the reference tree against the stub headers in
 // shim/) — on one block whose ghosted stage inputs come from the caller, so that tests can compare the oracle's
 // restatement of those stages with the reference code itself. Built only where the reference tree
 // is present; nothing in the product uses it.
@@ -24,6 +25,7 @@
 #include <godunov_mhd_ct/scheme/ComputeViscousFluxesAndStoreFunctor.h>
 #include <godunov_mhd_ct/scheme/ReadEmfAndUpdateFunctor.h>
 #include <godunov_mhd_ct/scheme/ReadFluxesAndConservativeUpdateFunctor.h>
+#include <godunov_mhd_ct/border_conditions/FillOutside.h>
 
 using namespace kalypsso;
 using namespace kalypsso::godunov_mhd_ct;
@@ -449,9 +451,81 @@ run_primitives(const int * b, int n_blocks, int n_owned, const int * level, cons
   std::memcpy(q_out, q.data(), sizeof(double) * (std::size_t)q.num_cells() * 11);
   return 0;
 }
+// keys of every block: level, coordinates at that level and, for the blocks beyond a non-periodic
+// border, the axes along which they lie outside [0, bricks << level)
+template <std::size_t dim>
+std::vector<uint64_t>
+block_keys(int n_blocks, const int * level, const int * coord, const int * bricks)
+{
+  std::vector<uint64_t> k((std::size_t)n_blocks);
+  for (int b = 0; b < n_blocks; ++b)
+  {
+    int64_t  c[3] = {0, 0, 0};
+    unsigned bits = 0;
+    for (int a = 0; a < (int)dim; ++a)
+    {
+      c[a] = coord[3 * b + a];
+      const int64_t e = (int64_t)bricks[a] << level[b];
+      if (c[a] < 0 || c[a] >= e)
+        bits |= 1u << a;
+    }
+    k[b] = orchard_key_t<dim>::pack(level[b], c, bits);
+  }
+  return k;
+}
+
+template <std::size_t dim>
+int
+run_fill_outside(const int * b, int n_blocks, int n_owned, const int * level, const int * neighbor, const int * coord,
+                 const int * bc, double * U_io, double * B_io)
+{
+  MeshCtx<dim>      mc(n_blocks, n_owned, level, neighbor, nullptr, coord);
+  const int         bricks[3] = {1, 1, 1};
+  std::vector<uint64_t> keys = block_keys<dim>(n_blocks, level, coord, bricks);
+  mc.mesh.keys = keys.data();
+  mc.keys.keys->assign(keys.begin(), keys.end());
+  ConfigMap    cm;
+  const char * names[5] = {"NONE", "PERIODIC", "ZERO_GRADIENT", "WALL", "CUSTOM"};
+  const char * faces[6] = {"xmin", "xmax", "ymin", "ymax", "zmin", "zmax"};
+  const char * per[3] = {"periodic_x", "periodic_y", "periodic_z"};
+  for (int f = 0; f < 2 * (int)dim; ++f)
+    cm.set("border_conditions", faces[f], names[bc[f] >= 0 && bc[f] < 5 ? bc[f] : 0]);
+  for (int a = 0; a < (int)dim; ++a)
+    cm.set("p4est_connectivity", per[a], bc[2 * a] == 1 ? "1" : "0");
+  block_size_t<dim> bs;
+  for (std::size_t d = 0; d < dim; ++d)
+    bs[d] = b[d];
+  DataArrayBlock<dim, real_t, DefaultDevice>     U(bs, 0, 5, n_blocks);
+  FaceDataArrayBlock<dim, real_t, DefaultDevice> B(bs, n_blocks);
+  const std::size_t nu = (std::size_t)U.num_cells() * 5 * n_blocks;
+  const std::size_t nb = (std::size_t)B.num_elements_per_octant() * n_blocks;
+  std::memcpy(U.data(), U_io, sizeof(double) * nu);
+  std::memcpy(B.data(), B_io, sizeof(double) * nb);
+  FieldMap<models::MHD> fm;
+  ParallelEnv           pe;
+  FillOutsideCellFunctor<dim, DefaultDevice>::apply(U, B, mc.info, mc.keys, mc.map, fm, cm, pe);
+  std::memcpy(U_io, U.data(), sizeof(double) * nu);
+  std::memcpy(B_io, B.data(), sizeof(double) * nb);
+  return 0;
+}
 } // namespace
 
 extern "C" {
+
+// The reference's fill of the leaves beyond non-periodic domain borders (FillOutsideCellFunctor::apply):
+// mesh tables as for ref_correct_emf, the outside blocks after the owned ones with their coordinates
+// beyond the domain (-1 or 2^level), border conditions bc[6] per domain face (0 NONE, 1 PERIODIC,
+// 2 ZERO_GRADIENT, 3 WALL, 4 CUSTOM); U [n_blocks][5][cells] and B [n_blocks][faces] updated in place.
+int
+ref_fill_outside(int dim, const int * b, int n_blocks, int n_owned, const int * level, const int * neighbor,
+                 const int * coord, const int * bc, double * U, double * B)
+{
+  if (dim == 2)
+    return run_fill_outside<2>(b, n_blocks, n_owned, level, neighbor, coord, bc, U, B);
+  if (dim == 3)
+    return run_fill_outside<3>(b, n_blocks, n_owned, level, neighbor, coord, bc, U, B);
+  return -1;
+}
 
 // The reference's primitive variables of owned block blk on its (b+4)^d ghosted box
 // (ConvertToPrimitivesVariablesFunctor::apply_on_group, ghosts from same-level leaves, the sibling

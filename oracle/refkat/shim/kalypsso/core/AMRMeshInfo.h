@@ -9,5 +9,7 @@ struct AMRMeshInfo
   int local_num_quadrants() const { return nb_owned; }
   int local_num_ghosts() const { return nb_ghosts; }
   int local_num_mirrors() const { return 0; }
+  int first_outside_quad_local_id() const { return nb_owned + nb_ghosts; }
+  int total_local_number_of_outside_quads() const { return nb_outside; }
 };
 } // namespace kalypsso

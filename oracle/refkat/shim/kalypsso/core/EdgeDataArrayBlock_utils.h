@@ -108,6 +108,6 @@ struct EdgeLocation
   int32_t                         iOct;
   bool                            is_ghost;
   bool                            is_valid = true;
-  KOKKOS_INLINE_FUNCTION int      level() const { return (int)key; }
+  KOKKOS_INLINE_FUNCTION int      level() const { return (int)(key & 63); }
 };
 } // namespace kalypsso

@@ -1,6 +1,6 @@
 // Stub of kalypsso-core's ghost-filling helpers used by ConvertToPrimitivesVariablesFunctor: a ghosted
 // cell coordinate (-2 .. b+1 per axis) wrapped into the block (coord_in) and the direction of the
-// neighbour region holding it (-1, 0, +1 per axis), and the flat index of an unghosted cell.
+// neighbour region holding it (-1, 0, +1 per axis).
 #pragma once
 #include <kalypsso/core/kokkos_shared.h>
 #include <kalypsso/core/kalypsso_data_container.h>
@@ -18,14 +18,5 @@ ghosted_coords_to_inner_coords(coord_t<dim> & coord_in, coord_t<dim> const & coo
     coord_in[a] = coord_out[a] - dir[a] * b[a];
   }
   return dir;
-}
-template <std::size_t dim>
-KOKKOS_INLINE_FUNCTION int32_t
-coord_to_cellindex(coord_t<dim> const & c, block_size_t<dim> const & b)
-{
-  int32_t i = c[dim - 1];
-  for (int a = (int)dim - 2; a >= 0; --a)
-    i = i * b[a] + c[a];
-  return i;
 }
 } // namespace kalypsso

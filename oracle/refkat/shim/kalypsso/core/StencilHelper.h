@@ -59,7 +59,7 @@ struct CellLocation
   bool                       is_ghost;
   int                        dir = -1;
   int                        side = 0;
-  KOKKOS_INLINE_FUNCTION int level() const { return (int)key; }
+  KOKKOS_INLINE_FUNCTION int level() const { return (int)(key & 63); }
   // index of the cell in an unghosted block of size b (x fastest)
   KOKKOS_INLINE_FUNCTION int32_t
   cellindex(block_size_t<dim> const & b) const

@@ -18,6 +18,7 @@ struct BridgeMesh
   const int32_t * neighbor = nullptr;
   const int32_t * fine = nullptr;
   const int32_t * coord = nullptr;
+  const uint64_t * keys = nullptr; // [n_blocks] orchard keys (outside leaves: coordinates beyond the domain)
 };
 template <typename device_t>
 struct hashmap_base_t

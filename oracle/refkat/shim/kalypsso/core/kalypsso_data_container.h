@@ -68,6 +68,7 @@ public:
                      (std::size_t)m_ncell * (var + (std::size_t)m_nvar * oct)];
   }
   int32_t num_cells() const { return m_ncell; }
+  int32_t num_vars() const { return m_nvar; }
   int32_t num_quadrants() const { return m_noct; }
   int32_t shift() const { return m_g; }
   block_size_t<dim> block_size() const { return m_bs; }
@@ -139,6 +140,15 @@ public:
     return (*m_data)[(std::size_t)m_per * oct + m_off[c] + i + (std::size_t)nx * (j + (std::size_t)ny * k)];
   }
   block_size_t<dim>       cell_block_size() const { return m_cells; }
+  // extents of face component c (2D c = 2: the cell-centred Bz)
+  block_size_t<dim>
+  face_block_size(int c) const
+  {
+    block_size_t<dim> s = m_cells;
+    if (c < (int)dim)
+      s[c] += 1;
+    return s;
+  }
   int32_t                 num_elements_per_octant() const { return m_per; }
   Kokkos::Array<int32_t, 3> offsets() const
   {
@@ -178,6 +188,37 @@ KOKKOS_INLINE_FUNCTION Kokkos::Array<int32_t, dim>
 cellindex_to_coord(int32_t cell_index, block_size_t<dim> shape)
 {
   return cellindex_to_coord<dim>(cell_index, shape, 0);
+}
+// flat index of cell c of an unghosted block of size b (x fastest)
+template <std::size_t dim>
+KOKKOS_INLINE_FUNCTION int32_t
+coord_to_cellindex(coord_t<dim> const & c, block_size_t<dim> const & b)
+{
+  int32_t i = c[dim - 1];
+  for (int a = (int)dim - 2; a >= 0; --a)
+    i = i * b[a] + c[a];
+  return i;
+}
+// (i, j[, k], comp) of element `flat` of one octant's face array (components at offsets[comp], each
+// x fastest; 2D comp 2 is the cell-centred Bz) of an unghosted face array (shift 0, as the outside
+// fill reads it)
+template <std::size_t dim>
+KOKKOS_INLINE_FUNCTION Kokkos::Array<int32_t, dim + 1>
+face_flat_index_unravel(int32_t flat, block_size_t<dim> const & cells, Kokkos::Array<int32_t, 3> const & offsets,
+                        int32_t shift)
+{
+  const int comp = flat < offsets[1] ? 0 : (flat < offsets[2] ? 1 : 2);
+  int32_t   r = flat - offsets[comp];
+  Kokkos::Array<int32_t, dim + 1> out;
+  for (std::size_t d = 0; d < dim; ++d)
+  {
+    const int32_t n = cells[d] + ((int)d == comp ? 1 : 0);
+    out[d] = r % n;
+    r /= n;
+  }
+  (void)shift;
+  out[dim] = comp;
+  return out;
 }
 template <std::size_t dim>
 KOKKOS_INLINE_FUNCTION Kokkos::Array<int32_t, dim>

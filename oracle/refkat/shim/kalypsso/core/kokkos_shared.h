@@ -20,6 +20,10 @@ struct Array
   T &       operator[](std::size_t i) { return m_data[i]; }
   const T & operator[](std::size_t i) const { return m_data[i]; }
   static constexpr std::size_t size() { return N; }
+  T *       begin() { return m_data; }
+  T *       end() { return m_data + N; }
+  const T * begin() const { return m_data; }
+  const T * end() const { return m_data + N; }
 };
 [[noreturn]] inline void
 abort(const char * msg)
