@@ -1,8 +1,10 @@
 """Benchmark: cell-updates/s of the MUSCL-Hancock + CT stage on 3D Orszag-Tang 256^3
 (512 leaf blocks of 32^3, periodic), mixed FP32/FP64 path vs the FP64 drop-in, with the HBM
-roofline of the fused step kernel, an end-to-end host-buffer number and the CPU baseline.
+roofline of the fused step kernel, an end-to-end host-buffer number and the CPU baseline; then one
+leg per other benchmark configuration (2D Orszag-Tang 128^2, the 2D AMR blast with regrids, 1024
+field loops, 3D Kelvin-Helmholtz shear layers on AMR) under "configs".
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gmhd|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gmhd|reference] [--legs 0,2,3,4]
 
 A step is one solver iteration (CFL reduction + do_time_step) over the whole 256^3 mesh. Inputs
 (U, B: 2.2 GB in FP64) are far larger than L2 (129 MB), so no L2 flush is needed between steps.
@@ -180,6 +182,241 @@ def cpu_baseline_run(steps, warmup, seconds_cap=25.0, side_blocks=8):
             "ms_per_step": 1e3 * el / done, "steps": done, "workload": f"3d_orszag_tang_{side}^3"}
 
 
+# ---- the other benchmark configurations (one leg each, after the headline) -----------------------
+def _accuracy(mesh0, U0, mesh, U, B, Uref, Bref):
+    """L1 relative error of rho, E and face B against (Uref, Bref), max|div B| (per block cell size) and
+    the drift of the rho and E volume integrals from (mesh0, U0)."""
+    n = mesh.n_owned
+
+    def l1(a, b):
+        return float(np.abs(a - b).sum() / np.abs(b).sum())
+
+    def totals(m, X):
+        k = m.n_owned
+        vol = m.block_dx()[:k] ** m.dim
+        return (X[:k, 0].reshape(k, -1).sum(axis=1) * vol).sum(), (X[:k, 1].reshape(k, -1).sum(axis=1) * vol).sum()
+
+    Bx, By, Bz = mesh.split_faces(B)
+    d = (Bx[:n, ..., 1:] - Bx[:n, ..., :-1]) + (By[:n, :, 1:, :] - By[:n, :, :-1, :])
+    if mesh.dim == 3:
+        d = d + (Bz[:n, 1:] - Bz[:n, :-1])
+    d = d / mesh.block_dx()[:n, None, None, None]
+    m0, e0 = totals(mesh0, U0)
+    m1, e1 = totals(mesh, U)
+    return {"l1_rho": l1(U[:n, 0], Uref[:n, 0]), "l1_E": l1(U[:n, 1], Uref[:n, 1]), "l1_B": l1(B[:n], Bref[:n]),
+            "max_divB": float(np.max(np.abs(d))), "mass_drift": float(abs(m1 - m0) / abs(m0)),
+            "energy_drift": float(abs(e1 - e0) / abs(e0))}
+
+
+def _run(st, mesh, U, B, nsteps, precision, bc=None, t_end=None, problem=None, n_problems=1, tile=None):
+    """nsteps graph-replayed solver iterations on the GPU; returns (U, B, dt_log, ms per step)."""
+    import torch
+
+    from godunov_mhd_ct_gb300.solver import GodunovImplemGB300
+
+    impl = GodunovImplemGB300(st, mesh, precision=precision, bc=bc, problem=problem, n_problems=n_problems)
+    if tile:
+        impl.set_tile(tile)
+    dU, dB = torch.from_numpy(U).cuda(), torch.from_numpy(B).cuda()
+    dU2, dB2 = torch.empty_like(dU), torch.empty_like(dB)
+    t0 = None if t_end is None else 0.0
+    impl.advance(dU.clone(), dU2, dB.clone(), dB2, 2, t=t0, t_end=t_end)  # warm-up and graph capture
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    dtlog, _ = impl.advance(dU, dU2, dB, dB2, nsteps, t=t0, t_end=t_end)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / nsteps
+    out = dU.cpu().numpy(), dB.cpu().numpy(), dtlog, ms
+    impl.close()
+    del dU, dB, dU2, dB2
+    torch.cuda.empty_cache()
+    return out
+
+
+def leg_config0(steps=200):
+    """2D Orszag-Tang 128^2 (64 blocks of 16^2), 200 steps: mixed and FP64 on the GPU (accuracy of the
+    mixed path against the FP64 one) and, as this configuration's CPU baseline, the FP64 oracle on all
+    host cores."""
+    from godunov_mhd_ct_gb300 import workloads as wl
+    from godunov_mhd_ct_gb300.mesh import BlockMesh
+    from oracle import oracle as orc
+
+    mesh = BlockMesh.uniform(2, level=3, block=(16, 16, 1))
+    st = settings()
+    U, B = wl.orszag_tang(mesh, gamma=st.gamma0)
+    cells = mesh.n_owned * mesh.ncell
+    Um, Bm, _, ms_m = _run(st, mesh, U, B, steps, "mixed")
+    Uf, Bf, _, ms_f = _run(st, mesh, U, B, steps, "fp64")
+    # CPU baseline of this configuration
+    orc.build()
+    om = orc.Mesh(2, 16, 16, 1, mesh.level, mesh.neighbor, mesh.n_owned)
+    os_ = orc.settings(gamma0=st.gamma0, cfl=st.cfl, slope_type=st.slope_type, riemann=st.riemann_id)
+    t0 = time.perf_counter()
+    orc.run(om, os_, U, B, steps)
+    cpu_s = (time.perf_counter() - t0) / steps
+    return {"workload": f"2d_orszag_tang_128^2 (64 blocks of 16^2), {steps} steps", "cells": cells,
+            "value": cells / (ms_m * 1e-3), "ms_per_step": ms_m, "fp64_value": cells / (ms_f * 1e-3),
+            "cpu_baseline": {"value": cells / cpu_s, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"the whole configuration, {steps} oracle solver iterations in one call"},
+            "accuracy": dict(_accuracy(mesh, U, mesh, Um, Bm, Uf, Bf), against="FP64 GPU path")}
+
+
+def leg_config1(side_blocks=4, steps=10, precision="mixed", tile=None):
+    """3D Orszag-Tang on (32 side_blocks)^3 cells (blocks of 32^3) at one precision and tile: the
+    headline workload's solver loop alone, at a size chosen for profiling single launches."""
+    mesh, U, B = make_workload(side_blocks=side_blocks)
+    cells = mesh.n_owned * mesh.ncell
+    _, _, _, ms = _run(settings(), mesh, U, B, steps, precision, tile=tile)
+    return {"workload": f"3d_orszag_tang_{32 * side_blocks}^3 ({mesh.n_owned} blocks of 32^3), {precision}, "
+                        f"tile {tile or 'default'}, {steps} steps", "cells": cells, "value": cells / (ms * 1e-3),
+            "ms_per_step": ms}
+
+
+def leg_config2(levels=(5, 10), steps=500, every=10):
+    """2D MHD blast, levels 5-10 of 16^2 blocks, an AMR cycle every 10 steps (SIMPLE_GRADIENT > 0.1 on rho
+    and p), 500 steps: the mixed solver loop with its regrids timed; accuracy against the FP64 GPU path
+    over the same mesh sequence (the FP64 path equals the oracle bit for bit in the tests)."""
+    import torch
+
+    from godunov_mhd_ct_gb300 import workloads as wl
+    from godunov_mhd_ct_gb300.mesh import BlockMesh
+    from godunov_mhd_ct_gb300.solver import GodunovImplemGB300
+
+    lmin, lmax = levels
+    cycles = max(1, steps // every)
+    crit = dict(criterion="SIMPLE_GRADIENT", eps_refine=0.1, eps_coarsen=0.02, eps_lohner=0.02)
+    st = settings()
+    mesh = BlockMesh.uniform(2, level=lmin, block=(16, 16, 1))
+    U, B = wl.blast(mesh, gamma=st.gamma0)
+    for _ in range(lmax - lmin):  # init-time refinement on the analytic state
+        impl = GodunovImplemGB300(st, mesh, precision="fp64")
+        fl = impl.refine_flags(torch.from_numpy(U).cuda(), torch.from_numpy(B).cuda(), level_min=lmin,
+                               level_max=lmax, variables=("rho", "pressure"), **crit)
+        impl.close()
+        mesh, _ = mesh.adapt(fl, lmin, lmax)
+        U, B = wl.blast(mesh, gamma=st.gamma0)
+    mesh0, U0, B0 = mesh, U, B
+
+    def loop(precision, flags=None):
+        impl = GodunovImplemGB300(st, mesh0, precision=precision)
+        dU, dB = torch.from_numpy(U0).cuda(), torch.from_numpy(B0).cuda()
+        log, updates = [], 0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m = mesh0
+        for c in range(cycles):
+            impl.advance(dU, torch.empty_like(dU), dB, torch.empty_like(dB), every)
+            updates += every * m.n_owned * m.ncell
+            if c < cycles - 1:
+                m, dU, dB = impl.regrid(dU, dB, lmin, lmax, flags=None if flags is None else flags[c],
+                                        variables=("rho", "pressure"), **crit)
+                log.append(impl.last_flags)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        out = m, dU.cpu().numpy(), dB.cpu().numpy(), updates / el, el, impl.regrid_seconds
+        impl.close()
+        return out, log
+
+    (mf, Uf, Bf, rate_f, _, _), flags = loop("fp64")
+    (mm, Um, Bm, rate_m, el_m, rs), _ = loop("mixed", flags)
+    return {"workload": f"2d_blast_amr levels {lmin}-{lmax} (16^2 blocks), regrid every {every} steps, "
+                        f"{cycles * every} steps",
+            "leaves_initial": mesh0.n_owned, "leaves_final": mm.n_owned, "value": rate_m,
+            "ms_per_step": 1e3 * el_m / (cycles * every), "regrid_share": float(sum(rs) / el_m),
+            "fp64_value": rate_f, "accuracy": dict(_accuracy(mesh0, U0, mm, Um, Bm, Uf, Bf),
+                                                   against="FP64 GPU path, same mesh sequence")}
+
+
+def leg_config3(steps=200, acc_steps=5, problems=1024):
+    """1024 independent 2D field loops ((2N) x N cells, N = 32..512 log-uniform in cell count; 110 M
+    cells) in one launch per step with per-problem dt and end time t = 0.5: `steps` graph-replayed
+    iterations timed (the whole run to t = 0.5 is about 2e11 cell-updates); accuracy of the mixed path
+    against the FP64 GPU path after acc_steps."""
+    from godunov_mhd_ct_gb300 import workloads as wl
+    from godunov_mhd_ct_gb300.mesh import BlockMesh
+
+    st = settings()
+    meshes, states, _ = wl.field_loop_batch(problems, seed=12345, sizes=(32, 64, 128, 256, 512))
+    mesh, problem = BlockMesh.batch(meshes)
+    U = np.concatenate([s_[0] for s_ in states])
+    B = np.concatenate([s_[1] for s_ in states])
+    del states
+    cells = np.array([m.n_owned * m.ncell for m in meshes], dtype=np.float64)
+    kw = dict(t_end=np.full(len(meshes), 0.5), problem=problem, n_problems=len(meshes))
+    _, _, dtlog, ms = _run(st, mesh, U, B, steps, "mixed", **kw)
+    updates = float(((dtlog > 0) * cells[None, :]).sum())
+    Um, Bm, _, _ = _run(st, mesh, U, B, acc_steps, "mixed", **kw)
+    Uf, Bf, _, ms_f = _run(st, mesh, U, B, acc_steps, "fp64", **kw)
+    return {"workload": f"{problems} field loops ({cells.sum() / 1e6:.0f} M cells, 16^2 blocks), {steps} steps of "
+                        "the batch",
+            "cells": int(cells.sum()), "value": updates / (steps * ms * 1e-3), "ms_per_step": ms,
+            "fp64_value": float(cells.sum()) / (ms_f * 1e-3),
+            "accuracy": dict(_accuracy(mesh, U, mesh, Um, Bm, Uf, Bf), steps=acc_steps, against="FP64 GPU path")}
+
+
+def leg_config4(levels=(4, 6), steps=100, acc_steps=2):
+    """3D magnetised shear layers (Kelvin-Helmholtz), periodic in x and z, reflecting walls in y, levels
+    4-6 of 16^3 blocks (1.64e8 cells), `steps` steps timed; accuracy of the mixed path against the FP64
+    GPU path after acc_steps (FP64 runs at about 4 s per step here)."""
+    from godunov_mhd_ct_gb300 import workloads as wl
+    from godunov_mhd_ct_gb300.settings import MHDSettings
+
+    st = MHDSettings(gamma0=1.4, cfl=0.5, slope_type=2.0, riemann="HLLD")
+    mesh = wl.kh_amr_mesh(levels[0], levels[1], block=16)
+    U, B = wl.kelvin_helmholtz(mesh, gamma=st.gamma0, seed=12345)
+    bc = (1, 1, 3, 3, 1, 1)
+    cells = mesh.n_owned * mesh.ncell
+    _, _, _, ms = _run(st, mesh, U, B, steps, "mixed", bc=bc)
+    Um, Bm, _, _ = _run(st, mesh, U, B, acc_steps, "mixed", bc=bc)
+    Uf, Bf, _, ms_f = _run(st, mesh, U, B, acc_steps, "fp64", bc=bc)
+    return {"workload": f"3d_kelvin_helmholtz_amr levels {levels[0]}-{levels[1]} (16^3 blocks, walls in y), "
+                        f"{steps} steps",
+            "cells": cells, "leaves": mesh.n_owned, "value": cells / (ms * 1e-3), "ms_per_step": ms,
+            "fp64_value": cells / (ms_f * 1e-3),
+            "accuracy": dict(_accuracy(mesh, U, mesh, Um, Bm, Uf, Bf), steps=acc_steps, against="FP64 GPU path")}
+
+
+LEGS = {"0": leg_config0, "1": leg_config1, "2": leg_config2, "3": leg_config3, "4": leg_config4}
+
+
+def run_legs(which, **kw):
+    out = {}
+    for k in [w for w in which.split(",") if w]:
+        t0 = time.perf_counter()
+        try:
+            out[f"config{k}"] = LEGS[k](**kw)
+        except Exception as e:  # noqa: BLE001 - a failing leg is reported, the headline line still prints
+            out[f"config{k}"] = {"error": f"{type(e).__name__}: {e}"}
+        out[f"config{k}"]["leg_seconds"] = time.perf_counter() - t0
+    return out
+
+
+def run_one_leg(args, rank):
+    """--config N: one configuration leg alone (stated sizes unless --levels / --leg-steps say otherwise)."""
+    if rank != 0:
+        return
+    from godunov_mhd_ct_gb300.csrc import build as cbuild
+
+    if not os.path.exists(cbuild.LIB):
+        cbuild.build()
+    kw = {}
+    if args.levels and args.config in ("2", "4"):
+        kw["levels"] = tuple(int(v) for v in args.levels.split(":"))
+    if args.config == "1":
+        kw.update(side_blocks=args.side_blocks, precision=args.precision, tile=args.tile)
+    if args.leg_steps:
+        kw["steps"] = args.leg_steps
+    t0 = time.perf_counter()
+    leg = LEGS[args.config](**kw)
+    line = {"metric": METRIC, "value": leg["value"], "unit": UNIT, "impl": "gmhd", "n_gpus": 1,
+            "higher_is_better": True, "dtype": "f32/f64 (mixed)", "data": "synthetic",
+            "config": {"workload": leg["workload"], "leg": f"config{args.config}"}, "leg": leg,
+            "leg_seconds": time.perf_counter() - t0}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -205,6 +442,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--accuracy-steps", type=int, default=50,
                     help="solver iterations of the mixed-vs-FP64 comparison (the workload's 50 steps)")
+    ap.add_argument("--legs", default="0,2,3,4",
+                    help="the other configurations to run after the headline (comma list of 0, 2, 3, 4; empty: none)")
+    ap.add_argument("--config", default=None, choices=sorted(LEGS),
+                    help="run one configuration leg alone and print its line (e.g. a small case under ncu)")
+    ap.add_argument("--levels", default=None, help="--config 2 or 4: lo:hi refinement levels instead of the stated ones")
+    ap.add_argument("--leg-steps", type=int, default=None, help="--config: solver iterations instead of the stated ones")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"], help="--config 1: the path to run")
+    ap.add_argument("--tile", type=int, default=None, help="--config 1: tile request instead of the default")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -213,6 +458,8 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.config is not None:
+        return run_one_leg(args, rank)
 
     import torch
 
@@ -368,7 +615,8 @@ def main():
             out["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
 
         ctr = read_counters()
-        kern_name = f"fused_step_kernel<float,3,{tile},{tile},{tile}> (mixed, persistent)"
+        kern_name = ("column_step_kernel<float> (mixed, 16x8 columns through the block)" if tile == 16 else
+                     f"fused_step_kernel<float,3,{tile},{tile},{tile}> (mixed, persistent)")
         issue = None
         if ctr and clk.get("sm_mhz"):
             # warp instructions per cell (ncu) x cells / launch time, against 4 issue slots per SM per clock
@@ -398,6 +646,10 @@ def main():
             "clocks": clk,
         }
         line.update(out)
+        if args.legs and world == 1:
+            del dU, dB, dU2, dB2, dU0, dB0
+            torch.cuda.empty_cache()
+            line["configs"] = run_legs(args.legs)
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
