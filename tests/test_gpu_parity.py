@@ -126,9 +126,8 @@ def test_mixed_precision_accuracy(dim, block, level, nsteps):
           f"max|divB|={divb:.3e}")
     assert l1_rho <= 1e-6
     assert divb <= 1e-12
-    # conservation on a periodic mesh: exact to FP64 round-off on the FP64 path; the mixed path
-    # adds each cell's FP32 sum of flux differences to U once in FP64, so its drift is the
-    # accumulated FP32 rounding of those increments
+    # conservation on a periodic mesh: exact to FP64 round-off on both paths (the mixed path sums each
+    # cell's face-flux terms error-free in FP32, a head and a tail, and adds both to U in FP64)
     for v in (0, 1):
         m0 = U[:n, v].sum()
         drift64 = abs(out["fp64"][0][:n, v].sum() - m0) / abs(m0)
