@@ -329,11 +329,35 @@ def leg_config2(levels=(5, 10), steps=500, every=10):
                                                    against="FP64 GPU path, same mesh sequence")}
 
 
-def leg_config3(steps=200, acc_steps=5, problems=1024):
+def _run_to_end(st, mesh, U, B, cells, t_end, problem, chunk=200):
+    """The mixed batch from t = 0 until every problem reaches t_end, in calls of `chunk` graph-replayed
+    iterations; returns (cell-updates of the active problems, seconds, launches)."""
+    import torch
+
+    from godunov_mhd_ct_gb300.solver import GodunovImplemGB300
+
+    impl = GodunovImplemGB300(st, mesh, precision="mixed", problem=problem, n_problems=len(cells))
+    dU, dB = torch.from_numpy(U).cuda(), torch.from_numpy(B).cuda()
+    dU2, dB2 = torch.empty_like(dU), torch.empty_like(dB)
+    t = np.zeros(len(cells))
+    updates, launches = 0.0, 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    while (t < t_end).any():
+        dtlog, t = impl.advance(dU, dU2, dB, dB2, chunk, t=t, t_end=t_end)
+        updates += float(((dtlog > 0) * cells[None, :]).sum())
+        launches += chunk
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    impl.close()
+    return updates, el, launches
+
+
+def leg_config3(steps=200, acc_steps=5, problems=1024, to_end=False):
     """1024 independent 2D field loops ((2N) x N cells, N = 32..512 log-uniform in cell count; 110 M
     cells) in one launch per step with per-problem dt and end time t = 0.5: `steps` graph-replayed
-    iterations timed (the whole run to t = 0.5 is about 2e11 cell-updates); accuracy of the mixed path
-    against the FP64 GPU path after acc_steps."""
+    iterations timed (the whole run to t = 0.5 is about 2e11 cell-updates; with to_end it is run and
+    timed too); accuracy of the mixed path against the FP64 GPU path after acc_steps."""
     from godunov_mhd_ct_gb300 import workloads as wl
     from godunov_mhd_ct_gb300.mesh import BlockMesh
 
@@ -349,11 +373,16 @@ def leg_config3(steps=200, acc_steps=5, problems=1024):
     updates = float(((dtlog > 0) * cells[None, :]).sum())
     Um, Bm, _, _ = _run(st, mesh, U, B, acc_steps, "mixed", **kw)
     Uf, Bf, _, ms_f = _run(st, mesh, U, B, acc_steps, "fp64", **kw)
-    return {"workload": f"{problems} field loops ({cells.sum() / 1e6:.0f} M cells, 16^2 blocks), {steps} steps of "
-                        "the batch",
-            "cells": int(cells.sum()), "value": updates / (steps * ms * 1e-3), "ms_per_step": ms,
-            "fp64_value": float(cells.sum()) / (ms_f * 1e-3),
-            "accuracy": dict(_accuracy(mesh, U, mesh, Um, Bm, Uf, Bf), steps=acc_steps, against="FP64 GPU path")}
+    out = {"workload": f"{problems} field loops ({cells.sum() / 1e6:.0f} M cells, 16^2 blocks), {steps} steps of "
+                       "the batch",
+           "cells": int(cells.sum()), "value": updates / (steps * ms * 1e-3), "ms_per_step": ms,
+           "fp64_value": float(cells.sum()) / (ms_f * 1e-3),
+           "accuracy": dict(_accuracy(mesh, U, mesh, Um, Bm, Uf, Bf), steps=acc_steps, against="FP64 GPU path")}
+    if to_end:
+        upd, el, launches = _run_to_end(st, mesh, U, B, cells, kw["t_end"], problem)
+        out["to_end"] = {"value": upd / el, "seconds": el, "cell_updates": upd, "launches": launches,
+                         "path": "the whole run to t = 0.5, wall time of chunks of 200 graph-replayed steps"}
+    return out
 
 
 def leg_config4(levels=(4, 6), steps=100, acc_steps=2):
@@ -406,6 +435,8 @@ def run_one_leg(args, rank):
         kw["levels"] = tuple(int(v) for v in args.levels.split(":"))
     if args.config == "1":
         kw.update(side_blocks=args.side_blocks, precision=args.precision, tile=args.tile)
+    if args.config == "3" and args.to_end:
+        kw["to_end"] = True
     if args.leg_steps:
         kw["steps"] = args.leg_steps
     t0 = time.perf_counter()
@@ -450,6 +481,7 @@ def main():
     ap.add_argument("--leg-steps", type=int, default=None, help="--config: solver iterations instead of the stated ones")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"], help="--config 1: the path to run")
     ap.add_argument("--tile", type=int, default=None, help="--config 1: tile request instead of the default")
+    ap.add_argument("--to-end", action="store_true", help="--config 3: also run and time the batch to t = 0.5")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 

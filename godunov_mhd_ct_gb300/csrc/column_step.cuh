@@ -378,7 +378,13 @@ __global__ void __launch_bounds__(K::NT, 2) column_step_kernel(const StepArgs a)
       s_tr[2] = (float)(1.0 / dx0);
     }
     __syncthreads();
-    if ((__double_as_longlong(dt) << 1) == 0)
+    if (__double_as_longlong(dt) == (long long)0x8000000000000000ull)
+    {
+      // dt = -0: an earlier step has carried this finished problem over; both buffers hold its state
+      __syncthreads();
+      continue;
+    }
+    if (__double_as_longlong(dt) == 0)
     {
       // a problem that has reached its end time: carry the column over unchanged
       for (int n = tid; n < TX * TY * bz; n += NT)

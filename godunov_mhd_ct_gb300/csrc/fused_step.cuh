@@ -1115,18 +1115,22 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
   const double dt = a.dt_dev ? a.dt_dev[myprob] : a.dt;
   if ((__double_as_longlong(dt) << 1) == 0) // dt == +-0 (integer test: no FP64 instruction per warp)
   {
-    // a problem that has reached its end time: carry the tile over unchanged
-    for (int n = tid; n < C::NCELL; n += NT)
+    // a problem that has reached its end time: carry the tile over unchanged (dt = +0), or, once an
+    // earlier step has done so and both buffers hold the final state, leave it (dt = -0)
+    if (__double_as_longlong(dt) == 0)
     {
-      const int     i = n % TX, j = (n / TX) % TY, k = n / (TX * TY);
-      const int64_t cell = (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)by * (z0 + k));
-      for (int v = 0; v < 5; ++v)
-        a.U2[((int64_t)blk * 5 + v) * a.ncell + cell] = a.U[((int64_t)blk * 5 + v) * a.ncell + cell];
+      for (int n = tid; n < C::NCELL; n += NT)
+      {
+        const int     i = n % TX, j = (n / TX) % TY, k = n / (TX * TY);
+        const int64_t cell = (x0 + i) + (int64_t)bx * ((y0 + j) + (int64_t)by * (z0 + k));
+        for (int v = 0; v < 5; ++v)
+          a.U2[((int64_t)blk * 5 + v) * a.ncell + cell] = a.U[((int64_t)blk * 5 + v) * a.ncell + cell];
+      }
+      // faces: the tile's tiles_per_block share of the block's face array
+      for (int64_t f = (int64_t)(tile - blk * tiles_per_block) * NT + tid; f < a.nface;
+           f += (int64_t)tiles_per_block * NT)
+        a.B2[(int64_t)blk * a.nface + f] = a.B[(int64_t)blk * a.nface + f];
     }
-    // faces: the tile's tiles_per_block share of the block's face array
-    for (int64_t f = (int64_t)(tile - blk * tiles_per_block) * NT + tid; f < a.nface;
-         f += (int64_t)tiles_per_block * NT)
-      a.B2[(int64_t)blk * a.nface + f] = a.B[(int64_t)blk * a.nface + f];
     if constexpr (C::PIPE)
     {
       // staged data of this tile unused; the area takes the next tile's gather

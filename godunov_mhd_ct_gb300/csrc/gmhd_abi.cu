@@ -517,7 +517,7 @@ fill_outside_faces_kernel(FillArgs a)
 // ---- device-side time control of gmhd_advance -----------------------------------------------
 __global__ void
 advance_time_kernel(const unsigned long long * invdt, double cfl, double * t, const double * t_end, double * dt_cur,
-                    double * dt_log, int32_t * counter, int np, int64_t log_cap)
+                    double * dt_log, int32_t * counter, int np, int64_t log_cap, int skip_ok)
 {
   const int n = *counter;
   for (int p = threadIdx.x; p < np; p += blockDim.x)
@@ -531,10 +531,16 @@ advance_time_kernel(const unsigned long long * invdt, double cfl, double * t, co
       if (!(rem > 0.0))
         dt = 0.0;
     }
-    dt_cur[p] = dt;
-    t[p] += dt;
     if ((int64_t)(n + 1) * np <= log_cap)
       dt_log[(int64_t)n * np + p] = dt;
+    // A problem past its end time is copied through by the step (dt = +0). After one such step both
+    // state buffers of the ping-pong hold its final state, so the next steps leave it alone: dt = -0
+    // tells the step to skip its tiles (Hancock loop only; gmhd_advance resets dt_cur to NaN when it
+    // starts, so the first step of a call always copies through).
+    if (skip_ok && dt == 0.0 && dt_cur[p] == 0.0)
+      dt = -0.0;
+    dt_cur[p] = dt;
+    t[p] += dt;
   }
   __syncthreads();
   if (threadIdx.x == 0)
@@ -620,7 +626,7 @@ enqueue_iteration_rk2(gmhd_ctx * ctx, const double * Uc, double * Un, const doub
   const int np = ctx->n_problems;
   advance_time_kernel<<<1, 256, 0, s>>>(ctx->d_invdt + (size_t)slot_in * np, ctx->p.cfl, ctx->d_t,
                                         has_tend ? ctx->d_tend : nullptr, ctx->d_dt, ctx->d_dtlog, ctx->d_counter,
-                                        np, ctx->dtlog_cap);
+                                        np, ctx->dtlog_cap, 0);
   GMHD_CUDA(cudaGetLastError());
   int rc = enqueue_fill(ctx, const_cast<double *>(Uc), const_cast<double *>(Bc), s);
   if (rc)
@@ -652,7 +658,7 @@ enqueue_iteration(gmhd_ctx * ctx, const double * Uc, double * Un, const double *
   const int np = ctx->n_problems;
   advance_time_kernel<<<1, 256, 0, s>>>(ctx->d_invdt + (size_t)slot_in * np, ctx->p.cfl, ctx->d_t,
                                         has_tend ? ctx->d_tend : nullptr, ctx->d_dt, ctx->d_dtlog, ctx->d_counter,
-                                        np, ctx->dtlog_cap);
+                                        np, ctx->dtlog_cap, 1);
   GMHD_CUDA(cudaGetLastError());
   unsigned long long * out = ctx->d_invdt + (size_t)(1 - slot_in) * np;
   GMHD_CUDA(cudaMemsetAsync(out, 0, sizeof(unsigned long long) * np, s));
@@ -1289,6 +1295,8 @@ gmhd_advance(gmhd_ctx * ctx, double * U, double * U2, double * B, double * B2, i
   if (t_end)
     GMHD_CUDA(cudaMemcpyAsync(ctx->d_tend, t_end, sizeof(double) * np, cudaMemcpyHostToDevice, s));
   GMHD_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(int32_t), s));
+  // no step of this call has copied a finished problem through yet (NaN: not a dt of 0)
+  GMHD_CUDA(cudaMemsetAsync(ctx->d_dt, 0xff, sizeof(double) * np, s));
   // CFL of the initial state into slot 0 (SolverGodunovMHD ctor: compute_dt, .cpp:180)
   if ((rc = enqueue_inv_dt(ctx, U, B, ctx->d_invdt, s, false)))
     return rc;

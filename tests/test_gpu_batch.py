@@ -94,3 +94,40 @@ def test_3d_batch_with_staggered_end_times(oracle_lib, precision):
             l1 = float(np.abs(Ug[sl, 0] - Uo[:, 0]).sum() / np.abs(Uo[:, 0]).sum())
             assert l1 <= 1e-6
             assert np.count_nonzero(dtlog[:, p]) == n_active
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_finished_problems_skipped_across_calls(dim):
+    """A finished problem is copied through by one step and then skipped; the state stays exact when the
+    run is split into calls of odd and even lengths whose scratch buffers start as NaN (each call's first
+    step copies a finished problem through again)."""
+    st = settings(gamma0=5.0 / 3.0, cfl=0.4, slope_type=2.0)
+    if dim == 2:
+        meshes, states, mesh, problem, U, B = _batch(5, seed=8, sizes=(32, 64))
+        t_end = np.array([4e-3, 1e-2, 6e-3, 2e-2, 8e-3])
+    else:
+        meshes = [BlockMesh.uniform(3, level=1, block=(16, 16, 16)) for _ in range(3)]
+        states = [wl.random_smooth(m, seed=60 + p) for p, m in enumerate(meshes)]
+        mesh, problem = BlockMesh.batch(meshes)
+        U = np.concatenate([s[0] for s in states])
+        B = np.concatenate([s[1] for s in states])
+        t_end = np.array([5e-3, 1.5e-2, 1e-2])
+    n = len(meshes)
+    ref = GodunovImplemGB300(st, mesh, precision="fp64", problem=problem, n_problems=n)
+    rU, rB = torch.from_numpy(U).cuda(), torch.from_numpy(B).cuda()
+    ref.advance(rU, torch.empty_like(rU), rB, torch.empty_like(rB), 30, t=0.0, t_end=t_end, use_graph=False)
+    impl = GodunovImplemGB300(st, mesh, precision="fp64", problem=problem, n_problems=n)
+    dU, dB = torch.from_numpy(U).cuda(), torch.from_numpy(B).cuda()
+    t = np.zeros(n)
+    logs = []
+    for k in (3, 4, 5, 2, 7, 9):
+        U2 = torch.full_like(dU, float("nan"))
+        B2 = torch.full_like(dB, float("nan"))
+        dtlog, t = impl.advance(dU, U2, dB, B2, k, t=t, t_end=t_end)
+        logs.append(dtlog)
+    dtlog = np.concatenate(logs)
+    assert np.allclose(t, t_end, rtol=0, atol=1e-15)
+    assert not np.signbit(dtlog).any()  # the log holds +0 for finished problems
+    assert (dtlog[-1] == 0.0).all()
+    assert np.array_equal(dU.cpu().numpy(), rU.cpu().numpy())
+    assert np.array_equal(dB.cpu().numpy(), rB.cpu().numpy())
