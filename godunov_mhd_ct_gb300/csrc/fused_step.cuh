@@ -1364,13 +1364,20 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
 
   // SIMPLE_COPY ghosts of a coarser neighbour take the coarse cell's own cell-centred B
   // (ConvertToPrimitivesVariablesFunctor.cpp:439-446), kept by the ghost prepass in Bccv
-  const bool coarse_copy = C::AMR && a.prolongation == 0;
+  // (one bit per neighbour slot holding such a coarser region; most tiles have none)
+  unsigned coarse_mask = 0u;
+  if (C::AMR && a.prolongation == 0)
+  {
+    const int lane = tid & 31;
+    coarse_mask = __ballot_sync(0xffffffffu, lane < 27 && s_kind[lane] == RK_COARSER && s_nbr[lane] >= a.n_blocks);
+  }
+  const bool coarse_copy = coarse_mask != 0u;
   auto       coarse_bcc = [&](int ci, int cj, int ck, double * bc) -> bool {
     const int ox = cell_off(ci, bx), oy = cell_off(cj, by), oz = D3 ? cell_off(ck, bz) : 0;
     if ((ox | oy | oz) == 0)
       return false;
     const int sl = nb_slot(ox, oy, oz);
-    if (s_kind[sl] != RK_COARSER || s_nbr[sl] < a.n_blocks)
+    if (!((coarse_mask >> sl) & 1u))
       return false;
     const int64_t  loc = (ci - ox * bx) + (int64_t)bx * ((cj - oy * by) + (int64_t)by * (ck - oz * bz));
     const double * Bc = a.Bccv + (int64_t)(s_nbr[sl] - a.n_blocks) * 3 * a.ncell + loc;
@@ -1383,14 +1390,23 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
   // A ghost cell inside an outside block takes its cell-centred B from that block's own faces
   // (get_conservative_vars of the outside cell, ConvertToPrimitivesVariablesFunctor.cpp:175-221), whose
   // copy of the shared border face is FillOutside's (a WALL copies the same face index)
-  const bool has_outside = a.n_blocks > a.n_owned;
+  // (the slots of this tile's block whose neighbour is an outside block, one bit each; most tiles have none)
+  unsigned out_mask = 0u;
+  if (a.n_blocks > a.n_owned)
+  {
+    const int lane = tid & 31;
+    const int nbl = lane < 27 ? s_nbr[lane] : -1;
+    out_mask = __ballot_sync(0xffffffffu, nbl >= a.n_owned && nbl < a.n_blocks);
+  }
+  const bool has_outside = out_mask != 0u;
   auto       outside_bcc = [&](int ci, int cj, int ck, double * bc) -> bool {
     const int ox = cell_off(ci, bx), oy = cell_off(cj, by), oz = D3 ? cell_off(ck, bz) : 0;
     if ((ox | oy | oz) == 0)
       return false;
-    const int nb = s_nbr[nb_slot(ox, oy, oz)];
-    if (nb < a.n_owned || nb >= a.n_blocks)
+    const int sl = nb_slot(ox, oy, oz);
+    if (!((out_mask >> sl) & 1u))
       return false;
+    const int nb = s_nbr[sl];
     const int      li = ci - ox * bx, lj = cj - oy * by, lk = ck - oz * bz;
     const double * Bn = a.B + (int64_t)nb * a.nface;
     const int64_t  xr = li + (int64_t)(bx + 1) * (lj + (int64_t)by * lk);
