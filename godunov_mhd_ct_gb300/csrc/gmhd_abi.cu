@@ -57,6 +57,13 @@ struct gmhd_ctx
   cudaStream_t a_in = nullptr, a_run = nullptr, a_out = nullptr;
   cudaEvent_t  a_in_done[2] = {nullptr, nullptr}, a_run_done[2] = {nullptr, nullptr}, a_out_done[2] = {nullptr, nullptr};
   int          a_next = 0;
+  // chunked gmhd_step_host on conforming meshes without outside blocks: the owned blocks in hp_k
+  // contiguous chunks (hp_begin[k] .. hp_begin[k+1]); chunk k steps once chunks 0 .. hp_dep[k] are in
+  // (its blocks' neighbours lie there), in the order hp_order; its copy-out follows its step
+  static constexpr int HP_MAX = 8;
+  int                  hp_k = 0;
+  std::vector<int>     hp_begin, hp_dep, hp_order;
+  cudaEvent_t          hp_in[HP_MAX] = {}, hp_run[HP_MAX] = {}, hp_start = nullptr, hp_end = nullptr;
   // own stream for graph capture when the caller passes the legacy stream
   cudaStream_t own_stream = nullptr;
   // cached graph of two steps
@@ -945,7 +952,56 @@ gmhd_destroy(gmhd_ctx * ctx)
     for (cudaEvent_t ev : {ctx->a_in_done[k], ctx->a_run_done[k], ctx->a_out_done[k]})
       if (ev)
         cudaEventDestroy(ev);
+  for (int k = 0; k < gmhd_ctx::HP_MAX; ++k)
+    for (cudaEvent_t ev : {ctx->hp_in[k], ctx->hp_run[k]})
+      if (ev)
+        cudaEventDestroy(ev);
+  for (cudaEvent_t ev : {ctx->hp_start, ctx->hp_end})
+    if (ev)
+      cudaEventDestroy(ev);
   delete ctx;
+}
+
+// The chunk plan of gmhd_step_host (conforming meshes without outside blocks, at least 16 owned
+// blocks): up to 8 contiguous chunks of owned blocks; a chunk can step once every chunk that holds a
+// neighbour of its blocks has been copied in, and the copy-in runs in chunk order, so chunk k waits
+// for chunk hp_dep[k] (the highest such index); chunks step in the order of that readiness.
+static void
+plan_host_chunks(gmhd_ctx * ctx, const gmhd_mesh * m, bool amr)
+{
+  ctx->hp_k = 0;
+  ctx->hp_begin.clear();
+  ctx->hp_dep.clear();
+  ctx->hp_order.clear();
+  const int n = m->n_owned;
+  if (amr || m->n_blocks != n || n < 16)
+    return;
+  const int K = std::min(gmhd_ctx::HP_MAX, n / 8);
+  ctx->hp_begin.resize(K + 1);
+  for (int k = 0; k <= K; ++k)
+    ctx->hp_begin[k] = (int)((int64_t)k * n / K);
+  std::vector<int> chunk_of(n);
+  for (int k = 0; k < K; ++k)
+    for (int b = ctx->hp_begin[k]; b < ctx->hp_begin[k + 1]; ++b)
+      chunk_of[b] = k;
+  ctx->hp_dep.assign(K, 0);
+  for (int b = 0; b < n; ++b)
+  {
+    int & d = ctx->hp_dep[chunk_of[b]];
+    d = std::max(d, chunk_of[b]);
+    for (int sl = 0; sl < 27; ++sl)
+    {
+      const int nb = m->neighbor[(int64_t)b * 27 + sl];
+      if (nb >= 0 && nb < n)
+        d = std::max(d, chunk_of[nb]);
+    }
+  }
+  ctx->hp_order.resize(K);
+  for (int k = 0; k < K; ++k)
+    ctx->hp_order[k] = k;
+  std::stable_sort(ctx->hp_order.begin(), ctx->hp_order.end(),
+                   [&](int x, int y) { return ctx->hp_dep[x] < ctx->hp_dep[y]; });
+  ctx->hp_k = K;
 }
 
 int
@@ -1092,6 +1148,7 @@ gmhd_set_mesh(gmhd_ctx * ctx, const gmhd_mesh * m)
   // all tables in one staged batch on own_stream, complete before any step reads them
   if ((rc = up_flush(ctx)))
     return rc;
+  plan_host_chunks(ctx, m, amr);
   ctx->has_mesh = true;
   ctx->mesh_version++;
   return GMHD_OK;
@@ -1367,6 +1424,75 @@ gmhd_advance(gmhd_ctx * ctx, double * U, double * U2, double * B, double * B2, i
   return GMHD_OK;
 }
 
+// gmhd_step_host in chunks (plan_host_chunks): copy-in on a_in, chunk steps on the caller's stream as
+// their inputs land, each chunk's copy-out on a_out right after its step, so that the copies in both
+// directions overlap the steps
+static int
+step_host_chunked(gmhd_ctx * ctx, const double * U, double * U2, const double * B, double * B2, double dt,
+                  cudaStream_t s)
+{
+  const int K = ctx->hp_k;
+  if (!ctx->a_in)
+  {
+    GMHD_CUDA(cudaStreamCreateWithFlags(&ctx->a_in, cudaStreamNonBlocking));
+    GMHD_CUDA(cudaStreamCreateWithFlags(&ctx->a_run, cudaStreamNonBlocking));
+    GMHD_CUDA(cudaStreamCreateWithFlags(&ctx->a_out, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k)
+    {
+      GMHD_CUDA(cudaEventCreateWithFlags(&ctx->a_in_done[k], cudaEventDisableTiming));
+      GMHD_CUDA(cudaEventCreateWithFlags(&ctx->a_run_done[k], cudaEventDisableTiming));
+      GMHD_CUDA(cudaEventCreateWithFlags(&ctx->a_out_done[k], cudaEventDisableTiming));
+    }
+  }
+  if (!ctx->hp_start)
+  {
+    GMHD_CUDA(cudaEventCreateWithFlags(&ctx->hp_start, cudaEventDisableTiming));
+    GMHD_CUDA(cudaEventCreateWithFlags(&ctx->hp_end, cudaEventDisableTiming));
+    for (int k = 0; k < gmhd_ctx::HP_MAX; ++k)
+    {
+      GMHD_CUDA(cudaEventCreateWithFlags(&ctx->hp_in[k], cudaEventDisableTiming));
+      GMHD_CUDA(cudaEventCreateWithFlags(&ctx->hp_run[k], cudaEventDisableTiming));
+    }
+  }
+  const size_t cu = (size_t)5 * ctx->ncell, cb = (size_t)ctx->nface; // doubles per block
+  // the copies start after the work the caller queued before this call
+  GMHD_CUDA(cudaEventRecord(ctx->hp_start, s));
+  GMHD_CUDA(cudaStreamWaitEvent(ctx->a_in, ctx->hp_start, 0));
+  GMHD_CUDA(cudaStreamWaitEvent(ctx->a_out, ctx->hp_start, 0));
+  for (int k = 0; k < K; ++k)
+  {
+    const size_t b0 = (size_t)ctx->hp_begin[k], nblk = (size_t)(ctx->hp_begin[k + 1] - ctx->hp_begin[k]);
+    GMHD_CUDA(cudaMemcpyAsync(ctx->d_U + b0 * cu, U + b0 * cu, nblk * cu * sizeof(double), cudaMemcpyHostToDevice,
+                              ctx->a_in));
+    GMHD_CUDA(cudaMemcpyAsync(ctx->d_B + b0 * cb, B + b0 * cb, nblk * cb * sizeof(double), cudaMemcpyHostToDevice,
+                              ctx->a_in));
+    GMHD_CUDA(cudaEventRecord(ctx->hp_in[k], ctx->a_in));
+  }
+  for (int i = 0; i < K; ++i)
+  {
+    const int k = ctx->hp_order[i];
+    GMHD_CUDA(cudaStreamWaitEvent(s, ctx->hp_in[ctx->hp_dep[k]], 0));
+    gmhd::StepArgs a = make_args(ctx, ctx->d_U, ctx->d_U2, ctx->d_B, ctx->d_B2);
+    a.dt = dt;
+    a.blk_begin = ctx->hp_begin[k];
+    a.blk_count = ctx->hp_begin[k + 1] - ctx->hp_begin[k];
+    int rc;
+    if ((rc = launch_step(ctx, a, s)))
+      return rc;
+    GMHD_CUDA(cudaEventRecord(ctx->hp_run[k], s));
+    GMHD_CUDA(cudaStreamWaitEvent(ctx->a_out, ctx->hp_run[k], 0));
+    const size_t b0 = (size_t)a.blk_begin, nblk = (size_t)a.blk_count;
+    GMHD_CUDA(cudaMemcpyAsync(U2 + b0 * cu, ctx->d_U2 + b0 * cu, nblk * cu * sizeof(double), cudaMemcpyDeviceToHost,
+                              ctx->a_out));
+    GMHD_CUDA(cudaMemcpyAsync(B2 + b0 * cb, ctx->d_B2 + b0 * cb, nblk * cb * sizeof(double), cudaMemcpyDeviceToHost,
+                              ctx->a_out));
+  }
+  GMHD_CUDA(cudaEventRecord(ctx->hp_end, ctx->a_out));
+  GMHD_CUDA(cudaStreamWaitEvent(s, ctx->hp_end, 0));
+  GMHD_CUDA(cudaStreamSynchronize(s));
+  return GMHD_OK;
+}
+
 int
 gmhd_step_host(gmhd_ctx * ctx, const double * U, double * U2, const double * B, double * B2, double dt, void * stream)
 {
@@ -1385,6 +1511,12 @@ gmhd_step_host(gmhd_ctx * ctx, const double * U, double * U2, const double * B, 
       return rc;
   }
   cudaStream_t s = (cudaStream_t)stream;
+  if (ctx->hp_k > 1)
+  {
+    if (!(dt >= 0.0))
+      return GMHD_ERR_ARGUMENT;
+    return step_host_chunked(ctx, U, U2, B, B2, dt, s);
+  }
   GMHD_CUDA(cudaMemcpyAsync(ctx->d_U, U, nu * sizeof(double), cudaMemcpyHostToDevice, s));
   GMHD_CUDA(cudaMemcpyAsync(ctx->d_B, B, nb * sizeof(double), cudaMemcpyHostToDevice, s));
   if ((rc = gmhd_step(ctx, ctx->d_U, ctx->d_U2, ctx->d_B, ctx->d_B2, dt, stream)))
