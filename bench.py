@@ -325,6 +325,8 @@ def leg_config2(levels=(5, 10), steps=500, every=10):
                         f"{cycles * every} steps",
             "leaves_initial": mesh0.n_owned, "leaves_final": mm.n_owned, "value": rate_m,
             "ms_per_step": 1e3 * el_m / (cycles * every), "regrid_share": float(sum(rs) / el_m),
+            "regrid_ms_per_cycle": {k: 1e3 * v / max(1, cycles - 1) for k, v in
+                                    zip(("flags", "adapt_and_tables", "remap", "set_mesh"), rs)},
             "fp64_value": rate_f, "accuracy": dict(_accuracy(mesh0, U0, mm, Um, Bm, Uf, Bf),
                                                    against="FP64 GPU path, same mesh sequence")}
 
