@@ -448,22 +448,25 @@ amr_border_emf(const TileView<C> & t, const int * gi, int v0, int v1, typename C
     all_same = all_same && valid && kd[n] != RK_COARSER && kd[n] != RK_FINER;
   }
   double out = to_d<R>(val);
-  // The averages of copies of the same value are taken in FP64 (the FP64 path: as the reference, in
-  // its order). On the mixed path FP64 makes them exact for an FP32 value (k v / k == v), so a fine
-  // block's corrected edge equals the raw value its coarse neighbour reads back, and the coarse / fine
-  // face copies stay consistent; in FP32, (3 v) / 3 can differ from v by one ulp.
+  // The averages of copies of the same value: the FP64 path takes them as the reference does, in its
+  // order: ((0 + v) + v + v) / 3 can differ from v by one ulp). On the mixed path v is an FP32 value, so
+  // k v (k <= 4) is exact in FP64 and the FP64 average is v itself: the value is kept as it is, with no
+  // FP64 division, and a fine block's corrected edge equals the raw value its coarse neighbour reads back.
   if (coarser)
   {
-    double acc = to_d<R>(val);
-    int    count = 1;
+    if constexpr (C::EXACT)
+    {
+      double acc = to_d<R>(val);
+      int    count = 1;
 #pragma unroll
-    for (int n = 0; n < 3; ++n)
-      if (kd[n] == RK_SAME)
-      {
-        acc += to_d<R>(val);
-        ++count;
-      }
-    out = acc / (double)count;
+      for (int n = 0; n < 3; ++n)
+        if (kd[n] == RK_SAME)
+        {
+          acc += to_d<R>(val);
+          ++count;
+        }
+      out = acc / (double)count;
+    }
   }
   else if (finer)
   {
@@ -504,7 +507,7 @@ amr_border_emf(const TileView<C> & t, const int * gi, int v0, int v1, typename C
     }
     out = acc / (double)count / (double)(1 << (C::DIM - 1));
   }
-  if (all_same)
+  if (all_same && C::EXACT)
   {
     double acc = 0.0;
     int    count = 1;
