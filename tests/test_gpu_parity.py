@@ -94,7 +94,7 @@ def test_step_host_buffers(oracle_lib):
 
 
 @pytest.mark.parametrize("dim,level,block,precision,tile", [
-    (3, 2, (16, 16, 16), "mixed", 0), (3, 2, (16, 16, 16), "fp64", 0), (3, 1, (32, 32, 32), "mixed", 16),
+    (3, 2, (16, 16, 16), "mixed", 0), (3, 2, (16, 16, 16), "fp64", 0), (3, 2, (32, 32, 32), "mixed", 16),
     (2, 4, (16, 16, 1), "mixed", 0), (2, 4, (16, 16, 1), "fp64", 0)])
 def test_step_host_chunked_matches_step(dim, level, block, precision, tile):
     """gmhd_step_host copies in, steps and copies out in chunks of blocks that overlap one another:
