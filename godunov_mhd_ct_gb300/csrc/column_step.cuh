@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(K::NT, 2) column_step_kernel(const StepArgs a)
   const int tid = threadIdx.x;
   const int bx = a.bx, by = a.by, bz = a.bz;
   const int cols_x = bx / TX, cols_per_block = cols_x * (by / TY);
-  const int n_work = (a.blk_count ? a.blk_count : a.n_owned) * cols_per_block;
+  const int n_work = (a.blk_list ? a.blk_count : a.n_owned) * cols_per_block;
   auto      cell_off = [](int c, int n) { return c < 0 ? -1 : (c >= n ? 1 : 0); };
   auto      face_off = [](int f, int n) { return f < 0 ? -1 : (f > n ? 1 : 0); };
 
@@ -347,8 +347,8 @@ __global__ void __launch_bounds__(K::NT, 2) column_step_kernel(const StepArgs a)
 
   for (int work = blockIdx.x; work < n_work; work += gridDim.x)
   {
-    const int blk = a.blk_begin + work / cols_per_block;
-    const int cidx = work - (blk - a.blk_begin) * cols_per_block;
+    const int blk = a.blk_list ? a.blk_list[work / cols_per_block] : work / cols_per_block;
+    const int cidx = work % cols_per_block;
     const int x0 = (cidx % cols_x) * TX, y0 = (cidx / cols_x) * TY;
     if (tid < 32)
     {

@@ -48,8 +48,9 @@ struct StepArgs
   int                        n_blocks;          // ids >= n_blocks in `neighbor` are virtual blocks
   Sources                    src;               // gravity / viscosity (viscous fluxes need C::VISC)
   int                        tile;              // host dispatch: tile x extent asked for (0: largest that fits)
-  // owned blocks [blk_begin, blk_begin + blk_count) only (blk_count 0: all); conforming meshes (no tile list)
-  int                        blk_begin, blk_count;
+  // the owned blocks blk_list[0 .. blk_count) only (device array; null: all); conforming meshes (no tile list)
+  const int32_t *            blk_list;
+  int                        blk_count;
 
   // ---- coarse/fine meshes (all null / zero when no block has a neighbour at another level) ----
   // Neighbour regions at another level are presented to the gather as virtual same-level blocks
@@ -874,15 +875,16 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
   // ---- PIPE: staging of a tile's gather ----------------------------------------------------------
   double *  stage = reinterpret_cast<double *>(sm + C::OFF_SL);
   // tile lists exist on coarse/fine meshes only (the AMR instantiations)
-  const int tile0 = a.blk_begin * tiles_per_block; // first tile of a block-range launch
   const int n_work =
-    C::PIPE ? ((C::AMR && a.tile_list) ? a.n_list : (a.blk_count ? a.blk_count : a.n_owned) * tiles_per_block) : 0;
-  // tile of work item w (a pass's list entry: ~tile marks a side-data-only tile)
+    C::PIPE ? ((C::AMR && a.tile_list) ? a.n_list : (a.blk_list ? a.blk_count : a.n_owned) * tiles_per_block) : 0;
+  // tile of work item w: all tiles of the owned blocks, of the listed blocks, or (coarse/fine passes) a pass's
+  // list entry (~tile marks a side-data-only tile)
   auto tile_at = [&](int w) {
-    if constexpr (C::AMR)
-      return a.tile_list ? a.tile_list[w] : tile0 + w;
-    else
-      return tile0 + w;
+    if (C::AMR && a.tile_list)
+      return (int)a.tile_list[w];
+    if (a.blk_list)
+      return a.blk_list[w / tiles_per_block] * tiles_per_block + w % tiles_per_block;
+    return w;
   };
   // neighbour table (and region kinds) of work item w into buffer buf (warp 0), with the slots whose
   // block is at another level
@@ -1061,7 +1063,7 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
   const int buf = iter & 1;
   const bool has_next = C::PIPE && work + (int)gridDim.x < n_work;
   int *     s_nbr = s_nbr0 + (C::PIPE ? 32 * buf : 0);
-  int       tile = C::PIPE ? tile_at(work) : tile0 + (int)blockIdx.x;
+  int       tile = tile_at(C::PIPE ? work : (int)blockIdx.x);
   bool      side_only = false; // pass 1 of a tile that also runs in pass 2: side data only
   if (C::AMR && a.tile_list)
   {

@@ -57,13 +57,22 @@ struct gmhd_ctx
   cudaStream_t a_in = nullptr, a_run = nullptr, a_out = nullptr;
   cudaEvent_t  a_in_done[2] = {nullptr, nullptr}, a_run_done[2] = {nullptr, nullptr}, a_out_done[2] = {nullptr, nullptr};
   int          a_next = 0;
-  // chunked gmhd_step_host on conforming meshes without outside blocks: the owned blocks in hp_k
-  // contiguous chunks (hp_begin[k] .. hp_begin[k+1]); chunk k steps once chunks 0 .. hp_dep[k] are in
-  // (its blocks' neighbours lie there), in the order hp_order; its copy-out follows its step
-  static constexpr int HP_MAX = 8;
-  int                  hp_k = 0;
-  std::vector<int>     hp_begin, hp_dep, hp_order;
-  cudaEvent_t          hp_in[HP_MAX] = {}, hp_run[HP_MAX] = {}, hp_start = nullptr, hp_end = nullptr;
+  // chunked gmhd_step_host on conforming meshes without outside blocks (plan_host_chunks): hp_k chunks
+  // of owned blocks, hp_blocks[hp_off[k] .. hp_off[k+1]) (ascending ids; on the device in d_hp_blocks),
+  // copied as the strided runs hp_copy[hp_coff[k] .. hp_coff[k+1]); chunk k steps once chunks
+  // 0 .. hp_dep[k] are in (its blocks' neighbours lie there), in the order hp_order, and its copy-out
+  // follows its step
+  struct HostRuns
+  {
+    int start, len, stride, count; // blocks start + i * stride .. + len, i < count
+  };
+  static constexpr int  HP_MAX = 8;
+  int                   hp_k = 0;
+  std::vector<int>      hp_off, hp_coff, hp_dep, hp_order;
+  std::vector<int32_t>  hp_blocks;
+  std::vector<HostRuns> hp_copy;
+  int32_t *             d_hp_blocks = nullptr;
+  cudaEvent_t           hp_in[HP_MAX] = {}, hp_run[HP_MAX] = {}, hp_start = nullptr, hp_end = nullptr;
   // own stream for graph capture when the caller passes the legacy stream
   cudaStream_t own_stream = nullptr;
   // cached graph of two steps
@@ -268,7 +277,8 @@ void
 release_all(gmhd_ctx * c)
 {
   reset_mesh(c);
-  for (int32_t ** p : {&c->d_neighbor, &c->d_level, &c->d_problem, &c->d_out_src, &c->d_out_normal, &c->d_counter})
+  for (int32_t ** p : {&c->d_neighbor, &c->d_level, &c->d_problem, &c->d_out_src, &c->d_out_normal, &c->d_counter,
+                       &c->d_hp_blocks})
     drelease(c, p);
   drelease(c, &c->d_invdt);
   for (double ** p : {&c->d_dt, &c->d_t, &c->d_tend, &c->d_dtlog, &c->d_U, &c->d_U2, &c->d_B, &c->d_B2, &c->d_Urk,
@@ -963,27 +973,73 @@ gmhd_destroy(gmhd_ctx * ctx)
 }
 
 // The chunk plan of gmhd_step_host (conforming meshes without outside blocks, at least 16 owned
-// blocks): up to 8 contiguous chunks of owned blocks; a chunk can step once every chunk that holds a
-// neighbour of its blocks has been copied in, and the copy-in runs in chunk order, so chunk k waits
-// for chunk hp_dep[k] (the highest such index); chunks step in the order of that readiness.
-static void
+// blocks). With block coordinates the chunks are slabs along the last axis (z in 3D, y in 2D): bucket
+// k of 8 holds the blocks whose coordinate falls in the k-th eighth of their problem's extent, so that
+// a slab needs only its own and the two adjacent slabs and most slabs can step while later ones are
+// still being copied in; without coordinates, up to 8 contiguous ranges of block ids. The copy-in runs
+// in chunk order, so chunk k waits for chunk hp_dep[k] (the highest chunk holding a neighbour of one of
+// its blocks); chunks step in the order of that readiness. A chunk's blocks are copied as runs of
+// consecutive ids, runs of equal length at a constant stride merged into one strided copy.
+static int
 plan_host_chunks(gmhd_ctx * ctx, const gmhd_mesh * m, bool amr)
 {
   ctx->hp_k = 0;
-  ctx->hp_begin.clear();
+  ctx->hp_off.clear();
+  ctx->hp_coff.clear();
   ctx->hp_dep.clear();
   ctx->hp_order.clear();
+  ctx->hp_blocks.clear();
+  ctx->hp_copy.clear();
   const int n = m->n_owned;
   if (amr || m->n_blocks != n || n < 16)
-    return;
-  const int K = std::min(gmhd_ctx::HP_MAX, n / 8);
-  ctx->hp_begin.resize(K + 1);
-  for (int k = 0; k <= K; ++k)
-    ctx->hp_begin[k] = (int)((int64_t)k * n / K);
-  std::vector<int> chunk_of(n);
+    return GMHD_OK;
+  constexpr int        NB = gmhd_ctx::HP_MAX;
+  std::vector<int>     bucket(n);
+  if (m->coord)
+  {
+    const int             a = m->dim - 1;
+    const int             np = m->problem ? m->n_problems : 1;
+    std::vector<int32_t>  ext(np, 0);
+    for (int b = 0; b < n; ++b)
+    {
+      const int p = m->problem ? m->problem[b] : 0;
+      ext[p] = std::max(ext[p], m->coord[3 * b + a] + 1);
+    }
+    for (int b = 0; b < n; ++b)
+    {
+      const int p = m->problem ? m->problem[b] : 0;
+      const int c = std::max(0, m->coord[3 * b + a]);
+      bucket[b] = (int)std::min<int64_t>(NB - 1, (int64_t)c * NB / std::max(1, ext[p]));
+    }
+  }
+  else
+    for (int b = 0; b < n; ++b)
+      bucket[b] = (int)((int64_t)b * NB / n);
+  // chunks: the non-empty buckets, in bucket order
+  std::vector<int> chunk_of_bucket(NB, -1);
+  std::vector<int> count(NB, 0);
+  for (int b = 0; b < n; ++b)
+    ++count[bucket[b]];
+  int K = 0;
+  for (int q = 0; q < NB; ++q)
+    if (count[q])
+      chunk_of_bucket[q] = K++;
+  if (K < 2)
+    return GMHD_OK;
+  ctx->hp_off.assign(K + 1, 0);
+  for (int q = 0; q < NB; ++q)
+    if (count[q])
+      ctx->hp_off[chunk_of_bucket[q] + 1] = count[q];
   for (int k = 0; k < K; ++k)
-    for (int b = ctx->hp_begin[k]; b < ctx->hp_begin[k + 1]; ++b)
-      chunk_of[b] = k;
+    ctx->hp_off[k + 1] += ctx->hp_off[k];
+  ctx->hp_blocks.resize(n);
+  std::vector<int> fill(ctx->hp_off.begin(), ctx->hp_off.end() - 1);
+  std::vector<int> chunk_of(n);
+  for (int b = 0; b < n; ++b) // ascending ids within each chunk
+  {
+    chunk_of[b] = chunk_of_bucket[bucket[b]];
+    ctx->hp_blocks[fill[chunk_of[b]]++] = b;
+  }
   ctx->hp_dep.assign(K, 0);
   for (int b = 0; b < n; ++b)
   {
@@ -1001,7 +1057,41 @@ plan_host_chunks(gmhd_ctx * ctx, const gmhd_mesh * m, bool amr)
     ctx->hp_order[k] = k;
   std::stable_sort(ctx->hp_order.begin(), ctx->hp_order.end(),
                    [&](int x, int y) { return ctx->hp_dep[x] < ctx->hp_dep[y]; });
+  // runs of consecutive ids, then runs of one length at one stride merged
+  ctx->hp_coff.assign(1, 0);
+  for (int k = 0; k < K; ++k)
+  {
+    std::vector<std::pair<int, int>> runs;
+    for (int i = ctx->hp_off[k]; i < ctx->hp_off[k + 1]; ++i)
+    {
+      const int b = ctx->hp_blocks[i];
+      if (!runs.empty() && runs.back().first + runs.back().second == b)
+        ++runs.back().second;
+      else
+        runs.push_back({b, 1});
+    }
+    for (size_t r = 0; r < runs.size();)
+    {
+      gmhd_ctx::HostRuns h{runs[r].first, runs[r].second, 0, 1};
+      size_t e = r + 1;
+      if (e < runs.size() && runs[e].second == h.len)
+      {
+        h.stride = runs[e].first - h.start;
+        while (e < runs.size() && runs[e].second == h.len && runs[e].first - runs[e - 1].first == h.stride)
+          ++e;
+        h.count = (int)(e - r);
+      }
+      ctx->hp_copy.push_back(h);
+      r = e;
+    }
+    ctx->hp_coff.push_back((int)ctx->hp_copy.size());
+  }
+  int rc;
+  if ((rc = dalloc(ctx, &ctx->d_hp_blocks, (size_t)n)))
+    return rc;
+  up_copy(ctx, ctx->d_hp_blocks, ctx->hp_blocks.data(), sizeof(int32_t) * (size_t)n);
   ctx->hp_k = K;
+  return GMHD_OK;
 }
 
 int
@@ -1145,10 +1235,14 @@ gmhd_set_mesh(gmhd_ctx * ctx, const gmhd_mesh * m)
     ctx->uploads.clear();
     return rc;
   }
+  if ((rc = plan_host_chunks(ctx, m, amr)))
+  {
+    ctx->uploads.clear();
+    return rc;
+  }
   // all tables in one staged batch on own_stream, complete before any step reads them
   if ((rc = up_flush(ctx)))
     return rc;
-  plan_host_chunks(ctx, m, amr);
   ctx->has_mesh = true;
   ctx->mesh_version++;
   return GMHD_OK;
@@ -1424,12 +1518,33 @@ gmhd_advance(gmhd_ctx * ctx, double * U, double * U2, double * B, double * B2, i
   return GMHD_OK;
 }
 
-// gmhd_step_host in chunks (plan_host_chunks): copy-in on a_in, chunk steps on the caller's stream as
-// their inputs land, each chunk's copy-out on a_out right after its step, so that the copies in both
-// directions overlap the steps
+// gmhd_step_host in chunks (plan_host_chunks): copy-in on a_in, chunk steps on a compute stream as their
+// inputs land, each chunk's copy-out on a_out right after its step, so that the copies in both
+// directions overlap the steps. The compute stream is the caller's, or the context's own stream
+// ordered after and before the legacy stream when the caller passes none.
+static int
+copy_runs(gmhd_ctx * ctx, int k, double * dst, const double * src, size_t per_block, cudaMemcpyKind kind,
+          cudaStream_t st)
+{
+  const size_t bytes = per_block * sizeof(double);
+  for (int g = ctx->hp_coff[k]; g < ctx->hp_coff[k + 1]; ++g)
+  {
+    const gmhd_ctx::HostRuns & h = ctx->hp_copy[g];
+    const size_t               off = (size_t)h.start * per_block;
+    if (h.count == 1)
+      GMHD_CUDA(cudaMemcpyAsync(dst + off, src + off, (size_t)h.len * bytes, kind, st));
+    else
+    {
+      const size_t pitch = (size_t)h.stride * bytes;
+      GMHD_CUDA(cudaMemcpy2DAsync(dst + off, pitch, src + off, pitch, (size_t)h.len * bytes, (size_t)h.count, kind, st));
+    }
+  }
+  return GMHD_OK;
+}
+
 static int
 step_host_chunked(gmhd_ctx * ctx, const double * U, double * U2, const double * B, double * B2, double dt,
-                  cudaStream_t s)
+                  cudaStream_t caller)
 {
   const int K = ctx->hp_k;
   if (!ctx->a_in)
@@ -1454,18 +1569,20 @@ step_host_chunked(gmhd_ctx * ctx, const double * U, double * U2, const double * 
       GMHD_CUDA(cudaEventCreateWithFlags(&ctx->hp_run[k], cudaEventDisableTiming));
     }
   }
+  cudaStream_t s = caller ? caller : ctx->own_stream;
   const size_t cu = (size_t)5 * ctx->ncell, cb = (size_t)ctx->nface; // doubles per block
-  // the copies start after the work the caller queued before this call
-  GMHD_CUDA(cudaEventRecord(ctx->hp_start, s));
+  // the copies and steps start after the work queued before this call on the caller's stream
+  GMHD_CUDA(cudaEventRecord(ctx->hp_start, caller));
   GMHD_CUDA(cudaStreamWaitEvent(ctx->a_in, ctx->hp_start, 0));
   GMHD_CUDA(cudaStreamWaitEvent(ctx->a_out, ctx->hp_start, 0));
+  if (s != caller)
+    GMHD_CUDA(cudaStreamWaitEvent(s, ctx->hp_start, 0));
+  int rc;
   for (int k = 0; k < K; ++k)
   {
-    const size_t b0 = (size_t)ctx->hp_begin[k], nblk = (size_t)(ctx->hp_begin[k + 1] - ctx->hp_begin[k]);
-    GMHD_CUDA(cudaMemcpyAsync(ctx->d_U + b0 * cu, U + b0 * cu, nblk * cu * sizeof(double), cudaMemcpyHostToDevice,
-                              ctx->a_in));
-    GMHD_CUDA(cudaMemcpyAsync(ctx->d_B + b0 * cb, B + b0 * cb, nblk * cb * sizeof(double), cudaMemcpyHostToDevice,
-                              ctx->a_in));
+    if ((rc = copy_runs(ctx, k, ctx->d_U, U, cu, cudaMemcpyHostToDevice, ctx->a_in)) ||
+        (rc = copy_runs(ctx, k, ctx->d_B, B, cb, cudaMemcpyHostToDevice, ctx->a_in)))
+      return rc;
     GMHD_CUDA(cudaEventRecord(ctx->hp_in[k], ctx->a_in));
   }
   for (int i = 0; i < K; ++i)
@@ -1474,22 +1591,19 @@ step_host_chunked(gmhd_ctx * ctx, const double * U, double * U2, const double * 
     GMHD_CUDA(cudaStreamWaitEvent(s, ctx->hp_in[ctx->hp_dep[k]], 0));
     gmhd::StepArgs a = make_args(ctx, ctx->d_U, ctx->d_U2, ctx->d_B, ctx->d_B2);
     a.dt = dt;
-    a.blk_begin = ctx->hp_begin[k];
-    a.blk_count = ctx->hp_begin[k + 1] - ctx->hp_begin[k];
-    int rc;
+    a.blk_list = ctx->d_hp_blocks + ctx->hp_off[k];
+    a.blk_count = ctx->hp_off[k + 1] - ctx->hp_off[k];
     if ((rc = launch_step(ctx, a, s)))
       return rc;
     GMHD_CUDA(cudaEventRecord(ctx->hp_run[k], s));
     GMHD_CUDA(cudaStreamWaitEvent(ctx->a_out, ctx->hp_run[k], 0));
-    const size_t b0 = (size_t)a.blk_begin, nblk = (size_t)a.blk_count;
-    GMHD_CUDA(cudaMemcpyAsync(U2 + b0 * cu, ctx->d_U2 + b0 * cu, nblk * cu * sizeof(double), cudaMemcpyDeviceToHost,
-                              ctx->a_out));
-    GMHD_CUDA(cudaMemcpyAsync(B2 + b0 * cb, ctx->d_B2 + b0 * cb, nblk * cb * sizeof(double), cudaMemcpyDeviceToHost,
-                              ctx->a_out));
+    if ((rc = copy_runs(ctx, k, U2, ctx->d_U2, cu, cudaMemcpyDeviceToHost, ctx->a_out)) ||
+        (rc = copy_runs(ctx, k, B2, ctx->d_B2, cb, cudaMemcpyDeviceToHost, ctx->a_out)))
+      return rc;
   }
   GMHD_CUDA(cudaEventRecord(ctx->hp_end, ctx->a_out));
-  GMHD_CUDA(cudaStreamWaitEvent(s, ctx->hp_end, 0));
-  GMHD_CUDA(cudaStreamSynchronize(s));
+  GMHD_CUDA(cudaStreamWaitEvent(caller, ctx->hp_end, 0));
+  GMHD_CUDA(cudaStreamSynchronize(caller));
   return GMHD_OK;
 }
 

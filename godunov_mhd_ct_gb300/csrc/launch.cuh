@@ -29,7 +29,7 @@ launch_fused(StepArgs a, cudaStream_t stream)
   a.tiles_y = a.by / C::TY;
   a.tiles_z = C::DIM == 3 ? a.bz / C::TZ : 1;
   long long nblocks = a.tile_list ? (long long)a.n_list
-                                  : (long long)(a.blk_count ? a.blk_count : a.n_owned) * a.tiles_x * a.tiles_y * a.tiles_z;
+                                  : (long long)(a.blk_list ? a.blk_count : a.n_owned) * a.tiles_x * a.tiles_y * a.tiles_z;
   if (nblocks <= 0)
     return 0;
   if constexpr (C::PIPE)

@@ -19,7 +19,7 @@ launch_column(const StepArgs & a, cudaStream_t stream)
   using K = COL_16x8;
   if (a.bx % K::TX || a.by % K::TY || a.kind || a.tile_list)
     return -1;
-  const long long n_work = (long long)(a.blk_count ? a.blk_count : a.n_owned) * (a.bx / K::TX) * (a.by / K::TY);
+  const long long n_work = (long long)(a.blk_list ? a.blk_count : a.n_owned) * (a.bx / K::TX) * (a.by / K::TY);
   if (n_work <= 0)
     return 0;
   if (g_column_ctas <= 0)
