@@ -639,8 +639,9 @@ def main():
         e2e_ind_s = (time.perf_counter() - t0) / ne_async
         out["e2e"] = {"value": cells / e2e_dep_s, "unit": UNIT, "h2d_bytes_per_step": int(U.nbytes + B.nbytes),
                       "d2h_bytes_per_step": int(U[:n].nbytes + B[:n].nbytes),
-                      "path": "gmhd_step_host (C ABI, pinned host buffers): copy in, step, copy out, return; a "
-                              "dependent chain, each step's input the previous step's host output; mixed, dt fixed",
+                      "path": "gmhd_step_host (C ABI, pinned host buffers): copy in, step, copy out, return, the "
+                              "copies overlapped with the step slab by slab; a dependent chain, each step's input "
+                              "the previous step's host output; mixed, dt fixed",
                       "independent_value": cells / e2e_ind_s,
                       "independent_path": "gmhd_step_host_async: independent steps on the same host input, copy-in, "
                                           "step and copy-out of consecutive steps overlapped"}
