@@ -39,7 +39,8 @@ class GmhdMesh(ctypes.Structure):
     _fields_ = [("dim", ctypes.c_int32), ("bx", ctypes.c_int32), ("by", ctypes.c_int32), ("bz", ctypes.c_int32),
                 ("n_blocks", ctypes.c_int32), ("n_owned", ctypes.c_int32), ("level", _ip), ("neighbor", _ip),
                 ("problem", _ip), ("n_problems", ctypes.c_int32), ("outside_src", _ip), ("outside_normal", _ip),
-                ("bc", ctypes.c_int32 * 6), ("coord", _ip), ("fine_neighbor", _ip)]
+                ("bc", ctypes.c_int32 * 6), ("coord", _ip), ("fine_neighbor", _ip), ("n_fine", ctypes.c_int64),
+                ("fine_at", ctypes.POINTER(ctypes.c_int64)), ("fine_id", _ip)]
 
 
 class GmhdRefineParams(ctypes.Structure):
@@ -89,6 +90,7 @@ def lib():
     L.gmhd_forest_build.argtypes = [ctypes.c_int32, vp, vp] + [ctypes.c_int32] * 6 + [vp, vp]
     L.gmhd_forest_sizes.argtypes = [vp] + [ctypes.POINTER(ctypes.c_int32)] * 3
     L.gmhd_forest_tables.argtypes = [vp] * 8
+    L.gmhd_forest_fine.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), vp, vp]
     L.gmhd_forest_destroy.argtypes = [vp]
     L.gmhd_last_status.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32)]
     L.gmhd_last_cuda_error.argtypes = [vp]
@@ -114,7 +116,7 @@ def exported_symbols():
     return ["gmhd_create", "gmhd_destroy", "gmhd_set_mesh", "gmhd_mem_bytes", "gmhd_step", "gmhd_inv_dt",
             "gmhd_fill_outside", "gmhd_advance", "gmhd_step_host", "gmhd_last_status", "gmhd_last_cuda_error",
             "gmhd_error_string", "gmhd_layout_check", "gmhd_inv_dt_noalloc", "gmhd_step_host_async",
-            "gmhd_refine_flags", "gmhd_remap", "gmhd_forest_build", "gmhd_forest_sizes", "gmhd_forest_tables",
+            "gmhd_refine_flags", "gmhd_remap", "gmhd_forest_build", "gmhd_forest_sizes", "gmhd_forest_tables", "gmhd_forest_fine",
             "gmhd_forest_destroy", "gmhd_autotune", "gmhd_set_tile"]
 
 
@@ -145,16 +147,31 @@ class MeshTables:
         # coarse/fine meshes: block coordinates and the children of refined neighbour regions
         self.coord = np.ascontiguousarray(mesh.coords, dtype=np.int32).reshape(-1)
         c.coord = self.coord.ctypes.data_as(_ip)
-        fine = getattr(mesh, "fine_neighbor", None)
-        self.fine = None if fine is None else np.ascontiguousarray(fine, dtype=np.int32).reshape(-1)
-        c.fine_neighbor = self.fine.ctypes.data_as(_ip) if self.fine is not None else ctypes.cast(None, _ip)
+        # the children list when the mesh has one (no dense table built), else the dense table
+        fl = getattr(mesh, "fine_list", None)
+        self.fine = None
+        c.fine_neighbor = ctypes.cast(None, _ip)
+        c.n_fine = 0
+        c.fine_at = ctypes.cast(None, ctypes.POINTER(ctypes.c_int64))
+        c.fine_id = ctypes.cast(None, _ip)
+        if fl is not None and fl[0].size:
+            self.fine_at = np.ascontiguousarray(fl[0], dtype=np.int64)
+            self.fine_id = np.ascontiguousarray(fl[1], dtype=np.int32)
+            c.n_fine = int(self.fine_at.size)
+            c.fine_at = self.fine_at.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+            c.fine_id = self.fine_id.ctypes.data_as(_ip)
+        else:
+            fine = getattr(mesh, "fine_neighbor", None)
+            self.fine = None if fine is None else np.ascontiguousarray(fine, dtype=np.int32).reshape(-1)
+            if self.fine is not None:
+                c.fine_neighbor = self.fine.ctypes.data_as(_ip)
         self.c = c
 
 
 def forest_build(dim, bricks, periodic, block, level_min, level_max, keys, flags=None):
     """Native leaf forest (gmhd_forest_build): returns a dict of numpy tables (level, coord, neighbor,
-    fine_neighbor [n_blocks, 27, 8] or None on a single-level leaf set, outside_src, outside_normal,
-    remap [n_owned, 15], n_owned)."""
+    fine_list = (at, id), the entries of the [n_blocks, 27, 8] children table that are not -1, or None on a
+    single-level leaf set, outside_src, outside_normal, remap [n_owned, 15], n_owned)."""
     L = lib()
     keys = np.ascontiguousarray(np.asarray(keys, dtype=np.int32).reshape(-1, 4))
     br = np.ascontiguousarray(np.asarray(bricks, dtype=np.int32)[:3])
@@ -171,13 +188,19 @@ def forest_build(dim, bricks, periodic, block, level_min, level_max, keys, flags
         check(L.gmhd_forest_sizes(h, ctypes.byref(no), ctypes.byref(nb), ctypes.byref(fine)), "gmhd_forest_sizes")
         no, nb = no.value, nb.value
         t = {"level": np.empty(nb, np.int32), "coord": np.empty((nb, 3), np.int32),
-             "neighbor": np.empty((nb, 27), np.int32),
-             "fine_neighbor": np.empty((nb, 27, 8), np.int32) if fine.value else None,
+             "neighbor": np.empty((nb, 27), np.int32), "fine_neighbor": None,
              "outside_src": np.empty(nb - no, np.int32), "outside_normal": np.empty((nb - no, 3), np.int32),
              "remap": np.empty((no, 15), np.int32)}
         keys = ("level", "coord", "neighbor", "fine_neighbor", "outside_src", "outside_normal", "remap")
         check(L.gmhd_forest_tables(h, *(t[k].ctypes.data if t[k] is not None and t[k].size else None
                                         for k in keys)), "gmhd_forest_tables")
+        t["fine_list"] = None
+        if fine.value:
+            n = ctypes.c_int64()
+            check(L.gmhd_forest_fine(h, ctypes.byref(n), None, None), "gmhd_forest_fine")
+            at, ids = np.empty(n.value, np.int64), np.empty(n.value, np.int32)
+            check(L.gmhd_forest_fine(h, ctypes.byref(n), at.ctypes.data, ids.ctypes.data), "gmhd_forest_fine")
+            t["fine_list"] = (at, ids)
         t["n_owned"] = no
         return t
     finally:

@@ -691,6 +691,19 @@ gmhd_forest_tables(const gmhd_forest * f, int32_t * level, int32_t * coord, int3
   return GMHD_OK;
 }
 
+int
+gmhd_forest_fine(const gmhd_forest * f, int64_t * n_fine, int64_t * at, int32_t * id)
+{
+  if (!f || !n_fine)
+    return GMHD_ERR_ARGUMENT;
+  *n_fine = (int64_t)f->fine_at.size();
+  if (at && !f->fine_at.empty())
+    std::memcpy(at, f->fine_at.data(), f->fine_at.size() * sizeof(int64_t));
+  if (id && !f->fine_id.empty())
+    std::memcpy(id, f->fine_id.data(), f->fine_id.size() * sizeof(int32_t));
+  return GMHD_OK;
+}
+
 void
 gmhd_forest_destroy(gmhd_forest * f)
 {

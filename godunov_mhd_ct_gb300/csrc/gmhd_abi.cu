@@ -88,6 +88,10 @@ struct gmhd_ctx
   int       n_virtual = 0, n_list1 = 0, n_list2 = 0, flux_face_stride = 0;
   int8_t *  d_kind = nullptr;
   int32_t * d_fine = nullptr;
+  // the children list of gmhd_mesh (fine_at, fine_id), scattered into d_fine after the uploads
+  int64_t * d_fine_at = nullptr;
+  int32_t * d_fine_id = nullptr;
+  int64_t   fine_scatter = 0; // entries still to scatter at the next up_flush
   int32_t * d_coord = nullptr;
   int32_t * d_vmap = nullptr;
   int32_t * d_nbr_real = nullptr;
@@ -147,6 +151,14 @@ up_set(gmhd_ctx * c, void * dst, int fill, size_t bytes)
   if (bytes)
     c->uploads.push_back(gmhd_ctx::Upload{dst, nullptr, bytes, fill});
 }
+// children-list entries of a coarse/fine mesh into the dense table (indices checked on the host)
+__global__ void
+fine_scatter_kernel(const int64_t * __restrict__ at, const int32_t * __restrict__ id, int64_t n, int32_t * fine)
+{
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    fine[at[i]] = id[i];
+}
+
 // stage the recorded copies through the page-locked buffer, issue everything on own_stream and wait
 int
 up_flush(gmhd_ctx * c)
@@ -187,6 +199,14 @@ up_flush(gmhd_ctx * c)
       break;
   }
   c->uploads.clear();
+  if (e == cudaSuccess && c->fine_scatter > 0)
+  {
+    const int64_t n = c->fine_scatter;
+    const int     grid = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+    fine_scatter_kernel<<<grid, 256, 0, c->own_stream>>>(c->d_fine_at, c->d_fine_id, n, c->d_fine);
+    e = cudaGetLastError();
+  }
+  c->fine_scatter = 0;
   const cudaError_t e2 = cudaStreamSynchronize(c->own_stream);
   return cuda_fail(c, e != cudaSuccess ? e : e2);
 }
@@ -245,6 +265,8 @@ release_amr(gmhd_ctx * c)
 {
   drelease(c, &c->d_kind);
   drelease(c, &c->d_fine);
+  drelease(c, &c->d_fine_at);
+  drelease(c, &c->d_fine_id);
   drelease(c, &c->d_coord);
   drelease(c, &c->d_vmap);
   drelease(c, &c->d_nbr_real);
@@ -878,7 +900,17 @@ setup_amr(gmhd_ctx * ctx, const gmhd_mesh * m, const std::vector<int8_t> & kind)
   if (m->fine_neighbor)
     up_copy(ctx, ctx->d_fine, m->fine_neighbor, sizeof(int32_t) * m->n_blocks * 27 * 8);
   else
+  {
     up_set(ctx, ctx->d_fine, 0xff, sizeof(int32_t) * m->n_blocks * 27 * 8);
+    if (m->n_fine > 0)
+    {
+      if ((rc = dalloc(ctx, &ctx->d_fine_at, (size_t)m->n_fine)) || (rc = dalloc(ctx, &ctx->d_fine_id, (size_t)m->n_fine)))
+        return rc;
+      up_copy(ctx, ctx->d_fine_at, m->fine_at, sizeof(int64_t) * (size_t)m->n_fine);
+      up_copy(ctx, ctx->d_fine_id, m->fine_id, sizeof(int32_t) * (size_t)m->n_fine);
+      ctx->fine_scatter = m->n_fine;
+    }
+  }
   up_set(ctx, ctx->d_Uv, 0, sizeof(double) * (size_t)nv * 5 * ctx->ncell);
   up_set(ctx, ctx->d_Bv, 0, sizeof(double) * (size_t)nv * ctx->nface);
   up_set(ctx, ctx->d_Bccv, 0, sizeof(double) * (size_t)nv * 3 * ctx->ncell);
@@ -1121,10 +1153,34 @@ gmhd_set_mesh(gmhd_ctx * ctx, const gmhd_mesh * m)
     if (m->problem && (m->problem[b] < 0 || m->problem[b] >= np))
       return GMHD_ERR_MESH;
   }
+  // the children list (read when there is no dense table): every entry checked, and the slots that have
+  // children marked
+  const bool           fine_list = !m->fine_neighbor && m->n_fine > 0;
+  std::vector<uint8_t> has_child;
+  if (!m->fine_neighbor && m->n_fine < 0)
+    return GMHD_ERR_ARGUMENT;
+  if (fine_list)
+  {
+    if (!m->fine_at || !m->fine_id)
+      return GMHD_ERR_ARGUMENT;
+    has_child.assign((size_t)m->n_owned * 27, 0);
+    for (int64_t i = 0; i < m->n_fine; ++i)
+    {
+      const int64_t at = m->fine_at[i];
+      const int64_t bs = at / 8;
+      const int     b = (int)(bs / 27), c = (int)(at % 8), id = m->fine_id[i];
+      if (at < 0 || b >= m->n_owned || c >= (1 << m->dim) || id < 0 || id >= m->n_owned)
+        return GMHD_ERR_MESH;
+      if (m->level[id] != m->level[b] + 1 || (m->problem && m->problem[id] != m->problem[b]))
+        return GMHD_ERR_MESH;
+      has_child[(size_t)bs] = 1;
+    }
+  }
   // kind of every neighbour region of the owned blocks (same level, one coarser, one finer, outside);
   // the fine-neighbour entries are checked where they are read (regions without a same-level or
   // coarser neighbour)
   ctx->uploads.clear();
+  ctx->fine_scatter = 0;
   std::vector<int8_t> & kind = ctx->h_kind;
   kind.assign((size_t)m->n_owned * 27, (int8_t)gmhd::RK_MISSING);
   bool amr = false;
@@ -1159,6 +1215,15 @@ gmhd_set_mesh(gmhd_ctx * ctx, const gmhd_mesh * m)
         }
         else
           return GMHD_ERR_MESH; // not 2:1 balanced, or a coarser neighbour without coordinates
+        continue;
+      }
+      if (fine_list)
+      {
+        if (has_child[(size_t)b * 27 + s])
+        {
+          k = gmhd::RK_FINER;
+          amr = true;
+        }
         continue;
       }
       if (!m->fine_neighbor)

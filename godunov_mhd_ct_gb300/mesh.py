@@ -48,9 +48,24 @@ class BlockMesh:
     outside_src: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     outside_normal: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.int32))
     # [n_blocks, 27, 8] leaves covering a neighbour region one level finer (children x fastest,
-    # -1 where absent); None on meshes without level jumps
+    # -1 where absent); None on meshes without level jumps. Meshes from the native forest carry the
+    # table as a list instead (fine_list = (flat indices, ids) of its entries that are not -1) and
+    # build the dense array only when it is read.
     fine_neighbor: np.ndarray | None = None
     bricks: tuple = (1, 1, 1)  # root trees per direction
+    fine_list: tuple | None = None
+
+    def __getattribute__(self, name):
+        if name == "fine_neighbor":
+            dense = object.__getattribute__(self, "fine_neighbor")
+            fl = object.__getattribute__(self, "fine_list")
+            if dense is None and fl is not None:
+                dense = np.full(self.n_blocks * 27 * 8, -1, np.int32)
+                dense[fl[0]] = fl[1]
+                dense = dense.reshape(self.n_blocks, 27, 8)
+                object.__setattr__(self, "fine_neighbor", dense)
+            return dense
+        return object.__getattribute__(self, name)
 
     @property
     def n_blocks(self) -> int:
@@ -75,7 +90,7 @@ class BlockMesh:
 
     @property
     def is_amr(self) -> bool:
-        if self.fine_neighbor is not None:
+        if object.__getattribute__(self, "fine_neighbor") is not None or self.fine_list is not None:
             return True
         return self.n_owned > 0 and bool(np.any(self.level[: self.n_owned] != self.level[0]))
 
@@ -360,6 +375,6 @@ class _Forest:
         mesh = BlockMesh(dim=self.dim, block=self.block, level=lv, neighbor=t["neighbor"],
                          coords=t["coord"].astype(np.int64), n_owned=no, grid=self.ext(int(lv[:no].max())),
                          periodic=self.per, scaling_factor=scaling_factor, outside_src=t["outside_src"],
-                         outside_normal=t["outside_normal"], fine_neighbor=t["fine_neighbor"],
+                         outside_normal=t["outside_normal"], fine_list=t["fine_list"],
                          bricks=self.bricks)
         return mesh, t["remap"]

@@ -163,6 +163,12 @@ typedef struct gmhd_mesh
                                      (needed when a neighbour is coarser; orchard-key position) */
   const int32_t * fine_neighbor;  /* [27 * 8 * n_blocks] children of refined neighbour regions, or
                                      NULL on meshes without finer neighbours */
+  /* The same children as a list, read when fine_neighbor is NULL: entry i is
+   * fine_neighbor[fine_at[i]] = fine_id[i], every other entry -1 (gmhd_forest_fine gives this list;
+   * it avoids building and uploading the mostly empty table). n_fine = 0: no list. */
+  int64_t         n_fine;
+  const int64_t * fine_at;
+  const int32_t * fine_id;
 } gmhd_mesh;
 
 typedef struct gmhd_ctx gmhd_ctx;
@@ -302,6 +308,10 @@ int gmhd_forest_sizes(const gmhd_forest * forest, int32_t * n_owned, int32_t * n
  * outside_normal[3 (n_blocks - n_owned)], remap[15 n_owned] (the rows gmhd_remap takes). */
 int  gmhd_forest_tables(const gmhd_forest * forest, int32_t * level, int32_t * coord, int32_t * neighbor,
                         int32_t * fine_neighbor, int32_t * outside_src, int32_t * outside_normal, int32_t * remap);
+/* The children table of the leaf set as a list (the entries of fine_neighbor that are not -1):
+ * *n_fine receives their count; at[*n_fine] (int64 indices into the [27 * 8 n_blocks] table) and
+ * id[*n_fine] are filled when not NULL (sized by a first call with NULL). */
+int  gmhd_forest_fine(const gmhd_forest * forest, int64_t * n_fine, int64_t * at, int32_t * id);
 void gmhd_forest_destroy(gmhd_forest * forest);
 
 /* Stream-ordered gmhd_step_host (no counterpart in the reference; it exists for callers that keep the
