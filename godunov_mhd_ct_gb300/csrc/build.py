@@ -28,7 +28,7 @@ UNITS = {
     "gmhd_abi.cu": ["--fmad=false"],
     "noalloc.cu": ["--fmad=false"],
     "amr.cu": ["--fmad=false"],
-    "forest.cpp": [],
+    "forest.cpp": ["-Xcompiler", "-pthread"],
 }
 HEADERS = ["mhd_math.cuh", "fused_step.cuh", "column_step.cuh", "launch.cuh",
            os.path.join("..", "..", "include", "gmhd.h")]
@@ -68,7 +68,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
             raise RuntimeError(f"nvcc failed for {cmd[-3]}")
     objs = [os.path.join(OBJDIR, u.rsplit(".", 1)[0] + ".o") for u in UNITS]
     if force or jobs or _stale(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             print(r.stdout + r.stderr)

@@ -9,6 +9,7 @@
 #include <cstdint>
 #include <cstring>
 #include <new>
+#include <thread>
 #include <vector>
 
 #include "../../include/gmhd.h"
@@ -300,6 +301,29 @@ struct gmhd_forest
 
 namespace
 {
+// fn(t, lo, hi) over [0, n) in contiguous ranges, one per host thread (up to 16; serial below 4,096
+// items); range t precedes range t + 1, so results gathered per range keep the serial order
+template <class F>
+int
+for_ranges(int n, F fn)
+{
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const int      nt = n < 4096 ? 1 : (int)std::min<unsigned>(hw, (unsigned)(n / 1024));
+  if (nt <= 1)
+  {
+    fn(0, 0, n);
+    return 1;
+  }
+  std::vector<std::thread> th;
+  th.reserve(nt - 1);
+  for (int t = 1; t < nt; ++t)
+    th.emplace_back([&, t] { fn(t, (int)((int64_t)t * n / nt), (int)((int64_t)(t + 1) * n / nt)); });
+  fn(0, 0, (int)((int64_t)n / nt));
+  for (std::thread & x : th)
+    x.join();
+  return nt;
+}
+
 // mesh tables of a balanced leaf set
 // every third bit of v (v < 2^21): the usual "part 1 by 2" interleave by shifts and masks
 inline uint64_t
@@ -447,53 +471,69 @@ build(const Forest & f, const KeyTable & leaves, gmhd_forest & out)
     out.coord[3 * b + 1] = k.y;
     out.coord[3 * b + 2] = k.z;
   }
-  for (int b = 0; b < n_owned; ++b)
-  {
-    const Key k = out.owned[b];
-    out.neighbor[(size_t)b * 27 + 13] = b; // the block itself
-    for (int o = 0; o < f.noffs; ++o)
+  // neighbour tables, the owned blocks in ranges over host threads (lookups only; the children found
+  // are gathered per range, in block order)
+  constexpr int                     MAXT = 16;
+  std::vector<std::vector<int64_t>> fat(MAXT);
+  std::vector<std::vector<int32_t>> fid(MAXT);
+  std::vector<char>                 bad(MAXT, 0);
+  const int nt = for_ranges(n_owned, [&](int t, int lo, int hi) {
+    for (int b = lo; b < hi && !bad[t]; ++b)
     {
-      const int s = (f.offs[o][2] + 1) * 9 + (f.offs[o][1] + 1) * 3 + (f.offs[o][0] + 1);
-      int       r[3] = {k.x + f.offs[o][0], k.y + f.offs[o][1], k.z + f.offs[o][2]};
-      int       c[3] = {r[0], r[1], r[2]};
-      if (!f.wrap(k.L, r))
+      const Key k = out.owned[b];
+      out.neighbor[(size_t)b * 27 + 13] = b; // the block itself
+      for (int o = 0; o < f.noffs; ++o)
       {
-        int w[3];
-        for (int d = 0; d < 3; ++d)
+        const int s = (f.offs[o][2] + 1) * 9 + (f.offs[o][1] + 1) * 3 + (f.offs[o][0] + 1);
+        int       r[3] = {k.x + f.offs[o][0], k.y + f.offs[o][1], k.z + f.offs[o][2]};
+        int       c[3] = {r[0], r[1], r[2]};
+        if (!f.wrap(k.L, r))
         {
-          w[d] = f.per[d] ? Forest::periodic(c[d], f.ext(k.L, d)) : c[d];
+          int w[3];
+          for (int d = 0; d < 3; ++d)
+            w[d] = f.per[d] ? Forest::periodic(c[d], f.ext(k.L, d)) : c[d];
+          out.neighbor[(size_t)b * 27 + s] = *out_ids.find(pack(k.L, w[0] + 1, w[1] + 1, w[2] + 1));
+          continue;
         }
-        out.neighbor[(size_t)b * 27 + s] = *out_ids.find(pack(k.L, w[0] + 1, w[1] + 1, w[2] + 1));
-        continue;
-      }
-      const int32_t * it = ids.find(pack(k.L, r[0], r[1], r[2]));
-      if (it)
-      {
-        out.neighbor[(size_t)b * 27 + s] = *it;
-        continue;
-      }
-      if (k.L >= 1 && (it = ids.find(pack(k.L - 1, r[0] >> 1, r[1] >> 1, r[2] >> 1))))
-      {
-        out.neighbor[(size_t)b * 27 + s] = *it;
-        continue;
-      }
-      bool      found = false;
-      const Key rk{k.L, r[0], r[1], r[2]};
-      for (int ch = 0; ch < f.nkids(); ++ch)
-        if ((it = ids.find(f.kid(rk, ch))))
+        const int32_t * it = ids.find(pack(k.L, r[0], r[1], r[2]));
+        if (it)
         {
-          out.fine_at.push_back(((int64_t)b * 27 + s) * 8 + ch);
-          out.fine_id.push_back(*it);
-          found = true;
+          out.neighbor[(size_t)b * 27 + s] = *it;
+          continue;
         }
-      out.has_fine = out.has_fine || found;
-      if (!found)
-      {
-        out.n_owned = -2; // not 2:1 balanced
-        return;
+        if (k.L >= 1 && (it = ids.find(pack(k.L - 1, r[0] >> 1, r[1] >> 1, r[2] >> 1))))
+        {
+          out.neighbor[(size_t)b * 27 + s] = *it;
+          continue;
+        }
+        bool      found = false;
+        const Key rk{k.L, r[0], r[1], r[2]};
+        for (int ch = 0; ch < f.nkids(); ++ch)
+          if ((it = ids.find(f.kid(rk, ch))))
+          {
+            fat[t].push_back(((int64_t)b * 27 + s) * 8 + ch);
+            fid[t].push_back(*it);
+            found = true;
+          }
+        if (!found)
+        {
+          bad[t] = 1; // not 2:1 balanced
+          break;
+        }
       }
     }
+  });
+  for (int t = 0; t < nt; ++t)
+  {
+    if (bad[t])
+    {
+      out.n_owned = -2;
+      return;
+    }
+    out.fine_at.insert(out.fine_at.end(), fat[t].begin(), fat[t].end());
+    out.fine_id.insert(out.fine_id.end(), fid[t].begin(), fid[t].end());
   }
+  out.has_fine = !out.fine_at.empty();
 }
 
 } // namespace
