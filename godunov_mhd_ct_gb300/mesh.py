@@ -47,25 +47,21 @@ class BlockMesh:
     scaling_factor: float = 1.0
     outside_src: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     outside_normal: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.int32))
-    # [n_blocks, 27, 8] leaves covering a neighbour region one level finer (children x fastest,
-    # -1 where absent); None on meshes without level jumps. Meshes from the native forest carry the
-    # table as a list instead (fine_list = (flat indices, ids) of its entries that are not -1) and
-    # build the dense array only when it is read.
-    fine_neighbor: np.ndarray | None = None
     bricks: tuple = (1, 1, 1)  # root trees per direction
+    # children of neighbour regions one level finer, as a list: (flat indices into the [n_blocks, 27, 8]
+    # table, leaf ids) of its entries that are not -1; None on meshes without level jumps
     fine_list: tuple | None = None
+    _fine_dense: np.ndarray | None = field(default=None, repr=False)
 
-    def __getattribute__(self, name):
-        if name == "fine_neighbor":
-            dense = object.__getattribute__(self, "fine_neighbor")
-            fl = object.__getattribute__(self, "fine_list")
-            if dense is None and fl is not None:
-                dense = np.full(self.n_blocks * 27 * 8, -1, np.int32)
-                dense[fl[0]] = fl[1]
-                dense = dense.reshape(self.n_blocks, 27, 8)
-                object.__setattr__(self, "fine_neighbor", dense)
-            return dense
-        return object.__getattribute__(self, name)
+    @property
+    def fine_neighbor(self) -> np.ndarray | None:
+        """[n_blocks, 27, 8] leaves covering a neighbour region one level finer (children x fastest, -1
+        where absent), built from fine_list when first read; None on meshes without level jumps."""
+        if self._fine_dense is None and self.fine_list is not None:
+            dense = np.full(self.n_blocks * 27 * 8, -1, np.int32)
+            dense[self.fine_list[0]] = self.fine_list[1]
+            self._fine_dense = dense.reshape(self.n_blocks, 27, 8)
+        return self._fine_dense
 
     @property
     def n_blocks(self) -> int:
@@ -90,7 +86,7 @@ class BlockMesh:
 
     @property
     def is_amr(self) -> bool:
-        if object.__getattribute__(self, "fine_neighbor") is not None or self.fine_list is not None:
+        if self.fine_list is not None:
             return True
         return self.n_owned > 0 and bool(np.any(self.level[: self.n_owned] != self.level[0]))
 

@@ -156,3 +156,37 @@ def test_leaf_set_covers_the_domain_once():
         cover[z * s:(z + 1) * s, y * s:(y + 1) * s, x * s:(x + 1) * s] += 1
     assert (cover == 1).all()
     assert len({tuple(k) for k in m.leaf_keys().tolist()}) == m.n_owned
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_children_list_matches_dense_table(dim):
+    """gmhd_forest_fine gives exactly the entries of the dense children table that are not -1, in
+    ascending table order, and the mesh built from the list reads back the same dense table."""
+    import ctypes
+
+    from godunov_mhd_ct_gb300 import _native as nat
+    from godunov_mhd_ct_gb300 import workloads as wl
+
+    block = (8, 8, 8) if dim == 3 else (8, 8, 1)
+    mesh = BlockMesh.amr(dim, wl.refine_band((0.5, 0.5, 0.5), 0.0, 0.2, axes=dim), base_level=2, max_level=3,
+                         block=block)
+    assert mesh.fine_list is not None and mesh.fine_list[0].size > 0
+    at, ids = mesh.fine_list
+    assert np.all(np.diff(at) > 0)
+    L = nat.lib()
+    keys = np.ascontiguousarray(mesh.leaf_keys(), dtype=np.int32).reshape(-1, 4)
+    br = np.ones(3, np.int32)
+    pe = np.ones(3, np.int32)
+    h = L.gmhd_forest_build(dim, br.ctypes.data, pe.ctypes.data, *block, 2, 3, keys.shape[0], keys.ctypes.data, None)
+    assert h
+    try:
+        nb = mesh.n_blocks
+        dense = np.empty(nb * 27 * 8, np.int32)
+        assert L.gmhd_forest_tables(h, None, None, None, dense.ctypes.data, None, None, None) == 0
+        n = ctypes.c_int64()
+        assert L.gmhd_forest_fine(h, ctypes.byref(n), None, None) == 0
+        assert n.value == int(np.count_nonzero(dense >= 0)) == at.size
+    finally:
+        L.gmhd_forest_destroy(h)
+    assert np.array_equal(np.nonzero(dense >= 0)[0], at) and np.array_equal(dense[at], ids)
+    assert np.array_equal(mesh.fine_neighbor.reshape(-1), dense)
