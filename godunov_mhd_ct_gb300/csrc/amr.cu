@@ -275,13 +275,15 @@ near_range(int o, int n, bool normal, int & lo, int & len)
   }
 }
 
-// One CTA per virtual block (grid-stride), its threads over the cells and faces of the region's
-// near layer.
+// One warp per virtual block (grid-stride over the warps of all CTAs), its lanes over the cells and
+// faces of the region's near layer.
 __global__ void __launch_bounds__(256)
 ghost_prepass_kernel(const GhostArgs g)
 {
   const int b[3] = {g.bx, g.by, g.bz};
-  for (int v = blockIdx.x; v < g.n_virtual; v += gridDim.x)
+  // one warp per virtual block: a region's near layer is a few dozen to a few hundred cells and faces
+  const int wpb = blockDim.x >> 5, lane = threadIdx.x & 31;
+  for (int v = blockIdx.x * wpb + (threadIdx.x >> 5); v < g.n_virtual; v += gridDim.x * wpb)
   {
     const int     blk = g.vmap[2 * v], slot = g.vmap[2 * v + 1];
     const int     o[3] = {slot % 3 - 1, (slot / 3) % 3 - 1, slot / 9 - 1};
@@ -305,7 +307,7 @@ ghost_prepass_kernel(const GhostArgs g)
     }
     // cnt[3] (cells) first, then faces x, y, z
     const int total = cnt[3] + cnt[0] + cnt[1] + cnt[2];
-    for (int it = threadIdx.x; it < total; it += blockDim.x)
+    for (int it = lane; it < total; it += 32)
     {
       if (it < cnt[3])
       {
@@ -450,7 +452,8 @@ launch_ghost_prepass(const GhostArgs & g, cudaStream_t stream)
 {
   if (g.n_virtual <= 0)
     return 0;
-  const int grid = g.n_virtual < 152 * 32 ? g.n_virtual : 152 * 32;
+  const int want = (g.n_virtual + 7) / 8; // 8 warps (virtual blocks) per CTA
+  const int grid = want < 152 * 16 ? want : 152 * 16;
   ghost_prepass_kernel<<<grid, 256, 0, stream>>>(g);
   return (int)cudaGetLastError();
 }
