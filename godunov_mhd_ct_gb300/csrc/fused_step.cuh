@@ -102,10 +102,11 @@ struct Cfg
   using R = R_;
   static constexpr bool AMR = AMR_;   // coarse/fine mesh support compiled in
   static constexpr bool VISC = VISC_; // viscous fluxes compiled in
-  // CTAs per SM the register allocation must allow. 2D 16x16 tiles: four on the mixed path (32 warps
-  // per SM, 62-64 registers without spills; 20-25 % faster than the two CTAs of an unconstrained
-  // allocation), two on the FP64 path (128 registers, a few spilled bytes; 13 % faster than one CTA)
-  static constexpr int MINB = (DIM_ == 2 && TX_ == 16 && NT_ == 256) ? (EXACT_ ? 2 : 4) : 1;
+  // CTAs per SM the register allocation must allow. 2D 16x16 tiles: three on the mixed path (24 warps
+  // per SM, 74-76 registers without spills; 3 % faster than four CTAs at 64 registers on the 1024
+  // field loops, and four were 20-25 % faster than the two CTAs of an unconstrained allocation), two
+  // on the FP64 path (128 registers, a few spilled bytes; 13 % faster than one CTA)
+  static constexpr int MINB = (DIM_ == 2 && TX_ == 16 && NT_ == 256) ? (EXACT_ ? 2 : 3) : 1;
   static constexpr int  DIM = DIM_;
   static constexpr int  TX = TX_;
   static constexpr int  TY = TY_;
