@@ -86,11 +86,6 @@ struct gmhd_ctx
   // coarse/fine meshes: virtual neighbour blocks, two-pass tile lists, fine-side data
   bool      amr = false;
   int       n_virtual = 0, n_list1 = 0, n_list2 = 0, flux_face_stride = 0;
-  // the first n_list1a entries of pass 1 read no virtual block: they run beside the ghost prepass, which
-  // goes on amr_side between the events amr_fork and amr_join
-  int          n_list1a = 0;
-  cudaStream_t amr_side = nullptr;
-  cudaEvent_t  amr_fork = nullptr, amr_join = nullptr;
   int8_t *  d_kind = nullptr;
   int32_t * d_fine = nullptr;
   // the children list of gmhd_mesh (fine_at, fine_id), scattered into d_fine after the uploads
@@ -291,7 +286,7 @@ void
 reset_mesh(gmhd_ctx * c)
 {
   c->amr = false;
-  c->n_virtual = c->n_list1 = c->n_list2 = c->flux_face_stride = c->n_list1a = 0;
+  c->n_virtual = c->n_list1 = c->n_list2 = c->flux_face_stride = 0;
   if (c->graph_exec)
   {
     cudaGraphExecDestroy(c->graph_exec);
@@ -418,18 +413,9 @@ launch_step(gmhd_ctx * ctx, const gmhd::StepArgs & a0, cudaStream_t s)
   g.nfy = ctx->nfy;
   g.nface = ctx->nface;
   g.health = ctx->d_health;
-  // the prepass on the side stream, beside the pass-1 tiles that read no virtual block
-  const bool split = ctx->n_list1a > 0 && ctx->n_virtual > 0 && ctx->amr_side;
-  if (split)
-  {
-    GMHD_CUDA(cudaEventRecord(ctx->amr_fork, s));
-    GMHD_CUDA(cudaStreamWaitEvent(ctx->amr_side, ctx->amr_fork, 0));
-  }
-  int rc = gmhd::launch_ghost_prepass(g, split ? ctx->amr_side : s);
+  int rc = gmhd::launch_ghost_prepass(g, s);
   if (rc != 0)
     return cuda_fail(ctx, (cudaError_t)rc);
-  if (split)
-    GMHD_CUDA(cudaEventRecord(ctx->amr_join, ctx->amr_side));
   gmhd::StepArgs a = a0;
   a.kind = ctx->d_kind;
   a.fine = ctx->d_fine;
@@ -442,22 +428,11 @@ launch_step(gmhd_ctx * ctx, const gmhd::StepArgs & a0, cudaStream_t s)
   a.flux_face_stride = ctx->flux_face_stride;
   a.emf_side = ctx->d_emf_side;
   a.emf_slot = ctx->d_emf_slot;
-  const int n1a = split ? ctx->n_list1a : 0;
-  if (n1a > 0)
+  if (ctx->n_list1 > 0)
   {
     a.pass = 1;
     a.tile_list = ctx->d_list1;
-    a.n_list = n1a;
-    if ((rc = launch_one(ctx, a, s)))
-      return rc;
-  }
-  if (split)
-    GMHD_CUDA(cudaStreamWaitEvent(s, ctx->amr_join, 0));
-  if (ctx->n_list1 > n1a)
-  {
-    a.pass = 1;
-    a.tile_list = ctx->d_list1 + n1a;
-    a.n_list = ctx->n_list1 - n1a;
+    a.n_list = ctx->n_list1;
     if ((rc = launch_one(ctx, a, s)))
       return rc;
   }
@@ -788,18 +763,13 @@ build_tile_lists(gmhd_ctx * ctx, int dim, const std::vector<int8_t> & kind)
         }
         touch[cx + 4 * (cy + 4 * cz)] = m;
       }
-  // pass 1 in two parts: first the tiles that read no virtual block (they can run beside the ghost
-  // prepass), then the others
-  std::vector<int32_t> list1b;
-  const bool           have_knbr = ctx->h_knbr.size() >= (size_t)ctx->n_owned * 27;
   for (int b = 0; b < ctx->n_owned; ++b)
   {
-    uint32_t finer = 0, coarser = 0, virt = 0;
+    uint32_t finer = 0, coarser = 0;
     for (int s = 0; s < 27; ++s)
     {
       finer |= (kind[(size_t)b * 27 + s] == gmhd::RK_FINER ? 1u : 0u) << s;
       coarser |= (kind[(size_t)b * 27 + s] == gmhd::RK_COARSER ? 1u : 0u) << s;
-      virt |= (!have_knbr || ctx->h_knbr[(size_t)b * 27 + s] >= ctx->n_blocks ? 1u : 0u) << s;
     }
     for (int t = 0; t < tpb; ++t)
     {
@@ -808,17 +778,15 @@ build_tile_lists(gmhd_ctx * ctx, int dim, const std::vector<int8_t> & kind)
       const bool     fin = (finer & m) != 0, coa = (coarser & m) != 0;
       const int32_t  id = b * tpb + t;
       if (!fin)
-        ((virt & m) ? list1b : list1).push_back(id);
+        list1.push_back(id);
       else
       {
         if (coa)
-          list1b.push_back(~id);
+          list1.push_back(~id);
         list2.push_back(id);
       }
     }
   }
-  ctx->n_list1a = (int)list1.size();
-  list1.insert(list1.end(), list1b.begin(), list1b.end());
 }
 
 // Make `tile` the context's tile request; on a coarse/fine mesh rebuild and upload the tile lists for
@@ -946,12 +914,6 @@ setup_amr(gmhd_ctx * ctx, const gmhd_mesh * m, const std::vector<int8_t> & kind)
   up_set(ctx, ctx->d_Uv, 0, sizeof(double) * (size_t)nv * 5 * ctx->ncell);
   up_set(ctx, ctx->d_Bv, 0, sizeof(double) * (size_t)nv * ctx->nface);
   up_set(ctx, ctx->d_Bccv, 0, sizeof(double) * (size_t)nv * 3 * ctx->ncell);
-  if (!ctx->amr_side)
-  {
-    GMHD_CUDA(cudaStreamCreateWithFlags(&ctx->amr_side, cudaStreamNonBlocking));
-    GMHD_CUDA(cudaEventCreateWithFlags(&ctx->amr_fork, cudaEventDisableTiming));
-    GMHD_CUDA(cudaEventCreateWithFlags(&ctx->amr_join, cudaEventDisableTiming));
-  }
   ctx->amr = true;
   ctx->n_virtual = nv;
   ctx->n_list1 = (int)ctx->h_list1.size();
@@ -1036,14 +998,9 @@ gmhd_destroy(gmhd_ctx * ctx)
     for (cudaEvent_t ev : {ctx->hp_in[k], ctx->hp_run[k]})
       if (ev)
         cudaEventDestroy(ev);
-  for (cudaEvent_t ev : {ctx->hp_start, ctx->hp_end, ctx->amr_fork, ctx->amr_join})
+  for (cudaEvent_t ev : {ctx->hp_start, ctx->hp_end})
     if (ev)
       cudaEventDestroy(ev);
-  if (ctx->amr_side)
-  {
-    cudaStreamSynchronize(ctx->amr_side);
-    cudaStreamDestroy(ctx->amr_side);
-  }
   delete ctx;
 }
 
