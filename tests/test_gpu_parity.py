@@ -121,6 +121,36 @@ def test_step_host_chunked_matches_step(dim, level, block, precision, tile):
     assert np.array_equal(hU2.numpy()[:n], ref_U[:n]) and np.array_equal(hB2.numpy()[:n], ref_B[:n])
 
 
+@pytest.mark.parametrize("case", ["batch", "walls"])
+def test_step_host_batched_and_walled(case):
+    """gmhd_step_host on a batch of independent problems (chunks by each problem's extent) and on a mesh
+    with outside blocks (no chunking: the outside fill needs every block): equal to gmhd_step."""
+    st = settings()
+    if case == "batch":
+        meshes, states, _ = wl.field_loop_batch(6, seed=5, sizes=(32, 64))
+        mesh, problem = BlockMesh.batch(meshes)
+        U = np.concatenate([s_[0] for s_ in states])
+        B = np.concatenate([s_[1] for s_ in states])
+        impl = GodunovImplemGB300(st, mesh, problem=problem, n_problems=len(meshes))
+        dt = 1e-3
+    else:
+        mesh = BlockMesh.uniform(3, level=2, block=(8, 8, 8), periodic=(True, False, True))
+        U, B = wl.kelvin_helmholtz(mesh, seed=3)
+        impl = GodunovImplemGB300(settings(gamma0=1.4), mesh, bc=(1, 1, 3, 3, 1, 1))
+        dU0, dB0 = _dev(U), _dev(B)
+        impl.fill_outside(dU0, dB0)
+        U, B = dU0.cpu().numpy(), dB0.cpu().numpy()
+        dt = 0.2 / float(np.max(impl.compute_inv_dt(dU0, dB0)))
+    assert mesh.n_owned >= 16
+    dU, dB = _dev(U), _dev(B)
+    dU2, dB2 = torch.empty_like(dU), torch.empty_like(dB)
+    impl.do_time_step(dU, dU2, dB, dB2, dt)
+    torch.cuda.synchronize()
+    n = mesh.n_owned
+    U2, B2 = impl.step_host(U, B, dt)
+    assert np.array_equal(U2[:n], dU2.cpu().numpy()[:n]) and np.array_equal(B2[:n], dB2.cpu().numpy()[:n])
+
+
 @pytest.mark.parametrize("dim", [2, 3])
 def test_uniform_state_preserved(dim):
     mesh = BlockMesh.uniform(dim, level=1 if dim == 3 else 2, block=(16, 16, 16) if dim == 3 else (16, 16, 1))
