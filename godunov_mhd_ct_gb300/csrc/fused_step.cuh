@@ -66,7 +66,7 @@ struct StepArgs
   // tiles that have both) and stores the fine-side face fluxes and raw border EMFs that coarse
   // neighbours need; pass 2 runs the tiles next to finer blocks and reads them
   // (ReadFluxesAndConservativeUpdateFunctor.cpp:141-172, CorrectEmfAtBlockBorderFunctor.cpp:94-360).
-  const int32_t * tile_list;  // tiles of this launch, ~tile for side-data-only tiles; null: all tiles
+  const int32_t * tile_list;  // tiles of this launch (coarse/fine passes: ~tile for side-data-only tiles); null: all
   int             n_list;     // entries of tile_list
   int             pass;       // 0 (single pass), 1 or 2
   double *        flux_side;  // [slot][2*dim faces][NFV][flux_face_stride] fluxes * dt/dx
@@ -875,13 +875,13 @@ __global__ void __launch_bounds__(C::NT, C::MINB) fused_step_kernel(const StepAr
 
   // ---- PIPE: staging of a tile's gather ----------------------------------------------------------
   double *  stage = reinterpret_cast<double *>(sm + C::OFF_SL);
-  // tile lists exist on coarse/fine meshes only (the AMR instantiations)
+  // work items: a tile list (the coarse/fine passes, the chunks of the host-buffer step), the tiles of a
+  // block list, or all tiles of the owned blocks
   const int n_work =
-    C::PIPE ? ((C::AMR && a.tile_list) ? a.n_list : (a.blk_list ? a.blk_count : a.n_owned) * tiles_per_block) : 0;
-  // tile of work item w: all tiles of the owned blocks, of the listed blocks, or (coarse/fine passes) a pass's
-  // list entry (~tile marks a side-data-only tile)
+    C::PIPE ? (a.tile_list ? a.n_list : (a.blk_list ? a.blk_count : a.n_owned) * tiles_per_block) : 0;
+  // tile of work item w (a coarse/fine pass's list entry ~tile marks a side-data-only tile)
   auto tile_at = [&](int w) {
-    if (C::AMR && a.tile_list)
+    if (a.tile_list)
       return (int)a.tile_list[w];
     if (a.blk_list)
       return a.blk_list[w / tiles_per_block] * tiles_per_block + w % tiles_per_block;

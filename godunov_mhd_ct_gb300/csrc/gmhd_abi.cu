@@ -73,6 +73,13 @@ struct gmhd_ctx
   std::vector<HostRuns> hp_copy;
   int32_t *             d_hp_blocks = nullptr;
   cudaEvent_t           hp_in[HP_MAX] = {}, hp_run[HP_MAX] = {}, hp_start = nullptr, hp_end = nullptr;
+  // per owned block: its chunk, and the chunk of the block in each of its 27 neighbour slots (-1: none)
+  std::vector<int8_t>   hp_chunk, hp_nchunk;
+  // tile-level schedule for the current tile choice: group k (launched once chunks 0 .. k are in) is
+  // d_hp_tiles[hp_toff[k] .. hp_toff[k+1]); chunk c's results are complete after group hp_done[c]
+  int                   hp_tile_key = -1;
+  std::vector<int>      hp_toff, hp_done;
+  int32_t *             d_hp_tiles = nullptr;
   // own stream for graph capture when the caller passes the legacy stream
   cudaStream_t own_stream = nullptr;
   // cached graph of two steps
@@ -300,7 +307,7 @@ release_all(gmhd_ctx * c)
 {
   reset_mesh(c);
   for (int32_t ** p : {&c->d_neighbor, &c->d_level, &c->d_problem, &c->d_out_src, &c->d_out_normal, &c->d_counter,
-                       &c->d_hp_blocks})
+                       &c->d_hp_blocks, &c->d_hp_tiles})
     drelease(c, p);
   drelease(c, &c->d_invdt);
   for (double ** p : {&c->d_dt, &c->d_t, &c->d_tend, &c->d_dtlog, &c->d_U, &c->d_U2, &c->d_B, &c->d_B2, &c->d_Urk,
@@ -1016,6 +1023,7 @@ static int
 plan_host_chunks(gmhd_ctx * ctx, const gmhd_mesh * m, bool amr)
 {
   ctx->hp_k = 0;
+  ctx->hp_tile_key = -1;
   ctx->hp_off.clear();
   ctx->hp_coff.clear();
   ctx->hp_dep.clear();
@@ -1089,6 +1097,19 @@ plan_host_chunks(gmhd_ctx * ctx, const gmhd_mesh * m, bool amr)
     ctx->hp_order[k] = k;
   std::stable_sort(ctx->hp_order.begin(), ctx->hp_order.end(),
                    [&](int x, int y) { return ctx->hp_dep[x] < ctx->hp_dep[y]; });
+  ctx->hp_chunk.resize(n);
+  ctx->hp_nchunk.assign((size_t)n * 27, (int8_t)-1);
+  for (int b = 0; b < n; ++b)
+  {
+    ctx->hp_chunk[b] = (int8_t)chunk_of[b];
+    for (int sl = 0; sl < 27; ++sl)
+    {
+      const int nb = m->neighbor[(int64_t)b * 27 + sl];
+      if (nb >= 0 && nb < n)
+        ctx->hp_nchunk[(size_t)b * 27 + sl] = (int8_t)chunk_of[nb];
+    }
+  }
+  ctx->hp_tile_key = -1;
   // runs of consecutive ids, then runs of one length at one stride merged
   ctx->hp_coff.assign(1, 0);
   for (int k = 0; k < K; ++k)
@@ -1607,6 +1628,88 @@ copy_runs(gmhd_ctx * ctx, int k, double * dst, const double * src, size_t per_bl
   return GMHD_OK;
 }
 
+// The tile-level schedule of the chunked host step for the context's tile choice: a tile reads the
+// neighbour blocks in the slots its position in the block touches, so it can step once the highest chunk
+// among its own and those blocks' chunks is in; tiles are grouped by that chunk (a slab's tiles away from its
+// two neighbour slabs start as soon as the slab itself has arrived). Not used for the column step, whose
+// columns span the whole block (block lists then, as planned per chunk).
+static int
+plan_host_tiles(gmhd_ctx * ctx)
+{
+  int T[3];
+  const bool mixed = ctx->p.precision == GMHD_PRECISION_MIXED;
+  const bool visc = ctx->p.viscosity_enabled != 0;
+  if (mixed)
+    gmhd::tile_shape_mixed(ctx->dim, ctx->bx, ctx->by, ctx->bz, visc, false, ctx->tile, T);
+  else
+    gmhd::tile_shape_fp64(ctx->dim, ctx->bx, ctx->by, ctx->bz, visc, ctx->tile, T);
+  const int key = (T[0] << 16) | (T[1] << 8) | T[2];
+  if (key == ctx->hp_tile_key)
+    return GMHD_OK;
+  const int K = ctx->hp_k, n = ctx->n_owned;
+  ctx->hp_toff.assign(K + 1, 0);
+  ctx->hp_done.assign(K, 0);
+  const bool column = ctx->dim == 3 && T[2] == ctx->bz && T[0] == 16 && T[1] == 8 && mixed;
+  if (column || ctx->bx % T[0] || ctx->by % T[1] || ctx->bz % T[2])
+  {
+    ctx->hp_tile_key = key;
+    ctx->hp_toff.clear(); // block-level chunks
+    return GMHD_OK;
+  }
+  const int nt[3] = {ctx->bx / T[0], ctx->by / T[1], ctx->dim == 3 ? ctx->bz / T[2] : 1};
+  const int tpb = nt[0] * nt[1] * nt[2];
+  // neighbour slots touched by a tile at each position class (first / last / both / neither per axis)
+  auto     cls_of = [](int c, int nn) { return (c == 0 ? 1 : 0) | (c == nn - 1 ? 2 : 0); };
+  uint32_t touch[64];
+  for (int c = 0; c < 64; ++c)
+  {
+    const int cl[3] = {c & 3, (c >> 2) & 3, c >> 4};
+    uint32_t  msk = 0;
+    for (int sl = 0; sl < 27; ++sl)
+    {
+      const int o[3] = {sl % 3 - 1, (sl / 3) % 3 - 1, sl / 9 - 1};
+      bool      t = true;
+      for (int d = 0; d < 3; ++d)
+        if (o[d] != 0 && !(cl[d] & (o[d] < 0 ? 1 : 2)))
+          t = false;
+      if (t)
+        msk |= 1u << sl;
+    }
+    touch[c] = msk;
+  }
+  std::vector<std::vector<int32_t>> groups(K);
+  for (int k = 0; k < K; ++k)
+    for (int i = ctx->hp_off[k]; i < ctx->hp_off[k + 1]; ++i)
+    {
+      const int b = ctx->hp_blocks[i];
+      for (int t = 0; t < tpb; ++t)
+      {
+        const int      tc[3] = {t % nt[0], (t / nt[0]) % nt[1], t / (nt[0] * nt[1])};
+        const uint32_t msk = touch[cls_of(tc[0], nt[0]) + 4 * (cls_of(tc[1], nt[1]) + 4 * cls_of(tc[2], nt[2]))];
+        int            dep = k;
+        for (int sl = 0; sl < 27; ++sl)
+          if ((msk >> sl) & 1u)
+            dep = std::max(dep, (int)ctx->hp_nchunk[(size_t)b * 27 + sl]);
+        groups[dep].push_back(b * tpb + t);
+        ctx->hp_done[k] = std::max(ctx->hp_done[k], dep);
+      }
+    }
+  std::vector<int32_t> all;
+  all.reserve((size_t)n * tpb);
+  for (int k = 0; k < K; ++k)
+  {
+    ctx->hp_toff[k] = (int)all.size();
+    all.insert(all.end(), groups[k].begin(), groups[k].end());
+  }
+  ctx->hp_toff[K] = (int)all.size();
+  int rc;
+  if ((rc = dalloc(ctx, &ctx->d_hp_tiles, all.size())))
+    return rc;
+  GMHD_CUDA(cudaMemcpy(ctx->d_hp_tiles, all.data(), all.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  ctx->hp_tile_key = key;
+  return GMHD_OK;
+}
+
 static int
 step_host_chunked(gmhd_ctx * ctx, const double * U, double * U2, const double * B, double * B2, double dt,
                   cudaStream_t caller)
@@ -1634,6 +1737,9 @@ step_host_chunked(gmhd_ctx * ctx, const double * U, double * U2, const double * 
       GMHD_CUDA(cudaEventCreateWithFlags(&ctx->hp_run[k], cudaEventDisableTiming));
     }
   }
+  int rc;
+  if ((rc = plan_host_tiles(ctx)))
+    return rc;
   cudaStream_t s = caller ? caller : ctx->own_stream;
   const size_t cu = (size_t)5 * ctx->ncell, cb = (size_t)ctx->nface; // doubles per block
   // the copies and steps start after the work queued before this call on the caller's stream
@@ -1642,7 +1748,6 @@ step_host_chunked(gmhd_ctx * ctx, const double * U, double * U2, const double * 
   GMHD_CUDA(cudaStreamWaitEvent(ctx->a_out, ctx->hp_start, 0));
   if (s != caller)
     GMHD_CUDA(cudaStreamWaitEvent(s, ctx->hp_start, 0));
-  int rc;
   for (int k = 0; k < K; ++k)
   {
     if ((rc = copy_runs(ctx, k, ctx->d_U, U, cu, cudaMemcpyHostToDevice, ctx->a_in)) ||
@@ -1650,20 +1755,45 @@ step_host_chunked(gmhd_ctx * ctx, const double * U, double * U2, const double * 
       return rc;
     GMHD_CUDA(cudaEventRecord(ctx->hp_in[k], ctx->a_in));
   }
+  auto copy_out = [&](int c) -> int {
+    int r;
+    if ((r = copy_runs(ctx, c, U2, ctx->d_U2, cu, cudaMemcpyDeviceToHost, ctx->a_out)) ||
+        (r = copy_runs(ctx, c, B2, ctx->d_B2, cb, cudaMemcpyDeviceToHost, ctx->a_out)))
+      return r;
+    return GMHD_OK;
+  };
+  const bool by_tiles = !ctx->hp_toff.empty();
   for (int i = 0; i < K; ++i)
   {
-    const int k = ctx->hp_order[i];
-    GMHD_CUDA(cudaStreamWaitEvent(s, ctx->hp_in[ctx->hp_dep[k]], 0));
+    // tile groups in chunk order, or (column step) whole chunks in the order of their readiness
+    const int k = by_tiles ? i : ctx->hp_order[i];
     gmhd::StepArgs a = make_args(ctx, ctx->d_U, ctx->d_U2, ctx->d_B, ctx->d_B2);
     a.dt = dt;
-    a.blk_list = ctx->d_hp_blocks + ctx->hp_off[k];
-    a.blk_count = ctx->hp_off[k + 1] - ctx->hp_off[k];
+    if (by_tiles)
+    {
+      if (ctx->hp_toff[k + 1] == ctx->hp_toff[k])
+        continue;
+      GMHD_CUDA(cudaStreamWaitEvent(s, ctx->hp_in[k], 0));
+      a.tile_list = ctx->d_hp_tiles + ctx->hp_toff[k];
+      a.n_list = ctx->hp_toff[k + 1] - ctx->hp_toff[k];
+    }
+    else
+    {
+      GMHD_CUDA(cudaStreamWaitEvent(s, ctx->hp_in[ctx->hp_dep[k]], 0));
+      a.blk_list = ctx->d_hp_blocks + ctx->hp_off[k];
+      a.blk_count = ctx->hp_off[k + 1] - ctx->hp_off[k];
+    }
     if ((rc = launch_step(ctx, a, s)))
       return rc;
     GMHD_CUDA(cudaEventRecord(ctx->hp_run[k], s));
     GMHD_CUDA(cudaStreamWaitEvent(ctx->a_out, ctx->hp_run[k], 0));
-    if ((rc = copy_runs(ctx, k, U2, ctx->d_U2, cu, cudaMemcpyDeviceToHost, ctx->a_out)) ||
-        (rc = copy_runs(ctx, k, B2, ctx->d_B2, cb, cudaMemcpyDeviceToHost, ctx->a_out)))
+    if (by_tiles)
+    {
+      for (int c = 0; c < K; ++c)
+        if (ctx->hp_done[c] == k && (rc = copy_out(c)))
+          return rc;
+    }
+    else if ((rc = copy_out(k)))
       return rc;
   }
   GMHD_CUDA(cudaEventRecord(ctx->hp_end, ctx->a_out));
