@@ -80,6 +80,13 @@ struct gmhd_ctx
   int                   hp_tile_key = -1;
   std::vector<int>      hp_toff, hp_done;
   int32_t *             d_hp_tiles = nullptr;
+  // the launches of the tile-level schedule: group k's tiles of chunk c's blocks, d_hp_tiles[off .. off + n);
+  // the launch that completes a chunk comes first within its group
+  struct HostLaunch
+  {
+    int k, c, off, n;
+  };
+  std::vector<HostLaunch> hp_launch;
   // own stream for graph capture when the caller passes the legacy stream
   cudaStream_t own_stream = nullptr;
   // cached graph of two steps
@@ -1677,7 +1684,8 @@ plan_host_tiles(gmhd_ctx * ctx)
     }
     touch[c] = msk;
   }
-  std::vector<std::vector<int32_t>> groups(K);
+  // tiles by (group, chunk of their block)
+  std::vector<std::vector<int32_t>> groups((size_t)K * K);
   for (int k = 0; k < K; ++k)
     for (int i = ctx->hp_off[k]; i < ctx->hp_off[k + 1]; ++i)
     {
@@ -1690,16 +1698,27 @@ plan_host_tiles(gmhd_ctx * ctx)
         for (int sl = 0; sl < 27; ++sl)
           if ((msk >> sl) & 1u)
             dep = std::max(dep, (int)ctx->hp_nchunk[(size_t)b * 27 + sl]);
-        groups[dep].push_back(b * tpb + t);
+        groups[(size_t)dep * K + k].push_back(b * tpb + t);
         ctx->hp_done[k] = std::max(ctx->hp_done[k], dep);
       }
     }
+  // launches: per group, first the chunks this group completes (so that their copy-out starts early),
+  // then the rest of the group's tiles
   std::vector<int32_t> all;
   all.reserve((size_t)n * tpb);
+  ctx->hp_launch.clear();
   for (int k = 0; k < K; ++k)
   {
     ctx->hp_toff[k] = (int)all.size();
-    all.insert(all.end(), groups[k].begin(), groups[k].end());
+    for (int pass = 0; pass < 2; ++pass)
+      for (int c = 0; c < K; ++c)
+      {
+        const std::vector<int32_t> & g = groups[(size_t)k * K + c];
+        if (g.empty() || (ctx->hp_done[c] == k) != (pass == 0))
+          continue;
+        ctx->hp_launch.push_back(gmhd_ctx::HostLaunch{k, c, (int)all.size(), (int)g.size()});
+        all.insert(all.end(), g.begin(), g.end());
+      }
   }
   ctx->hp_toff[K] = (int)all.size();
   int rc;
@@ -1762,40 +1781,49 @@ step_host_chunked(gmhd_ctx * ctx, const double * U, double * U2, const double * 
       return r;
     return GMHD_OK;
   };
-  const bool by_tiles = !ctx->hp_toff.empty();
-  for (int i = 0; i < K; ++i)
+  if (!ctx->hp_toff.empty())
   {
-    // tile groups in chunk order, or (column step) whole chunks in the order of their readiness
-    const int k = by_tiles ? i : ctx->hp_order[i];
-    gmhd::StepArgs a = make_args(ctx, ctx->d_U, ctx->d_U2, ctx->d_B, ctx->d_B2);
-    a.dt = dt;
-    if (by_tiles)
+    // tile groups in chunk order; each chunk's copy-out right after the launch that completes it
+    int waited = -1;
+    for (const gmhd_ctx::HostLaunch & L : ctx->hp_launch)
     {
-      if (ctx->hp_toff[k + 1] == ctx->hp_toff[k])
-        continue;
-      GMHD_CUDA(cudaStreamWaitEvent(s, ctx->hp_in[k], 0));
-      a.tile_list = ctx->d_hp_tiles + ctx->hp_toff[k];
-      a.n_list = ctx->hp_toff[k + 1] - ctx->hp_toff[k];
+      if (L.k != waited)
+      {
+        GMHD_CUDA(cudaStreamWaitEvent(s, ctx->hp_in[L.k], 0));
+        waited = L.k;
+      }
+      gmhd::StepArgs a = make_args(ctx, ctx->d_U, ctx->d_U2, ctx->d_B, ctx->d_B2);
+      a.dt = dt;
+      a.tile_list = ctx->d_hp_tiles + L.off;
+      a.n_list = L.n;
+      if ((rc = launch_step(ctx, a, s)))
+        return rc;
+      if (ctx->hp_done[L.c] == L.k)
+      {
+        GMHD_CUDA(cudaEventRecord(ctx->hp_run[L.c], s));
+        GMHD_CUDA(cudaStreamWaitEvent(ctx->a_out, ctx->hp_run[L.c], 0));
+        if ((rc = copy_out(L.c)))
+          return rc;
+      }
     }
-    else
+  }
+  else
+    for (int i = 0; i < K; ++i)
     {
+      // (column step) whole chunks in the order of their readiness
+      const int      k = ctx->hp_order[i];
+      gmhd::StepArgs a = make_args(ctx, ctx->d_U, ctx->d_U2, ctx->d_B, ctx->d_B2);
+      a.dt = dt;
       GMHD_CUDA(cudaStreamWaitEvent(s, ctx->hp_in[ctx->hp_dep[k]], 0));
       a.blk_list = ctx->d_hp_blocks + ctx->hp_off[k];
       a.blk_count = ctx->hp_off[k + 1] - ctx->hp_off[k];
+      if ((rc = launch_step(ctx, a, s)))
+        return rc;
+      GMHD_CUDA(cudaEventRecord(ctx->hp_run[k], s));
+      GMHD_CUDA(cudaStreamWaitEvent(ctx->a_out, ctx->hp_run[k], 0));
+      if ((rc = copy_out(k)))
+        return rc;
     }
-    if ((rc = launch_step(ctx, a, s)))
-      return rc;
-    GMHD_CUDA(cudaEventRecord(ctx->hp_run[k], s));
-    GMHD_CUDA(cudaStreamWaitEvent(ctx->a_out, ctx->hp_run[k], 0));
-    if (by_tiles)
-    {
-      for (int c = 0; c < K; ++c)
-        if (ctx->hp_done[c] == k && (rc = copy_out(c)))
-          return rc;
-    }
-    else if ((rc = copy_out(k)))
-      return rc;
-  }
   GMHD_CUDA(cudaEventRecord(ctx->hp_end, ctx->a_out));
   GMHD_CUDA(cudaStreamWaitEvent(caller, ctx->hp_end, 0));
   GMHD_CUDA(cudaStreamSynchronize(caller));
