@@ -257,8 +257,8 @@ int gmhd_set_tile(gmhd_ctx * ctx, int32_t tile);
 /* gmhd_step on HOST arrays: copies U, B to the device, runs the step, copies U2, B2 back, and returns
  * when U2, B2 hold the result. On conforming meshes without outside blocks (16 or more blocks) the work
  * is split into up to 8 chunks of blocks (slabs along the last axis when the mesh carries block
- * coordinates): a chunk steps as soon as the blocks it reads have been copied in and its results are
- * copied out while the next chunks step, so the copies in both directions overlap the step. The
+ * coordinates): a tile steps as soon as the blocks it reads have been copied in, and a chunk's results are
+ * copied out while the next tiles step, so the copies in both directions overlap the step. The
  * results equal gmhd_step's bit for bit. Host buffers should be page-locked for the copies to run at
  * full speed and overlap. */
 int gmhd_step_host(gmhd_ctx * ctx, const double * U, double * U2, const double * B, double * B2, double dt,
